@@ -1,0 +1,303 @@
+"""Benchmark: plain `path` tracer on the many-spheres stress scene.
+
+Workload: 10,000 icospheres (subdivision 2, 3.2 M triangles) with lognormal
+radii, 40/30/20/10 diffuse / rough_metal / rough_glass / disney, constant sky
+plus 20 sphere emitters; 1920x1080, max depth 16, Russian roulette from 3.
+One step = one sample per pixel over the whole frame (2,073,600 samples).
+
+Reported:
+* value  -- samples/s with the scene resident in HBM, device-timed with CUDA
+  events on the library's stream over K steps (one job of K samples/pixel);
+* e2e    -- the same metric through the public C ABI with host buffers: each
+  step submits a 1-spp job, waits, and copies the film to pinned host memory;
+* roofline -- the dominant kernel (BVH8 closest-hit traversal, `extend`):
+  algorithmic bytes per launch (queue entry + ray + hit record + 80 B per node
+  visited + 48 B per primitive tested) / its average launch time, against the
+  measured HBM copy bandwidth;
+* cpu_baseline -- the CPU oracle (C++ restatement of the reference's path
+  loop with a SAH BVH) on this host's cores, on a bounded row sample.
+
+`--impl reference` times that CPU implementation alone on the same workload
+(the reference itself needs Embree/oneTBB/Eigen, which are not available).
+"""
+
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import tempfile
+import threading
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+W, H = 1920, 1080
+MAX_DEPTH = 16
+BYTES_QUEUE, BYTES_RAY, BYTES_HIT, BYTES_NODE, BYTES_PRIM = 4, 32, 32, 80, 48
+
+
+def _peaks():
+    path = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(path):
+        with open(path) as fh:
+            d = json.load(fh)
+        return float(d.get("hbm_gbs", 6800.0)), "measured"
+    return 6800.0, "fallback"
+
+
+class ClockSampler:
+    """Samples SM clocks and throttle reasons with nvidia-smi during the timed region."""
+
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu):
+        self.gpu = gpu
+        self.rows = []
+        self.proc = None
+        self.thread = None
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.gpu), "--query-gpu=" + self.FIELDS,
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+        except OSError:
+            self.proc = None
+            return
+        self.thread = threading.Thread(target=self._read, daemon=True)
+        self.thread.start()
+
+    def _read(self):
+        for line in self.proc.stdout:
+            parts = [p.strip() for p in line.split(",")]
+            if len(parts) >= 9:
+                self.rows.append(parts)
+
+    def stop(self):
+        if self.proc is not None:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=2)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+        if self.thread is not None:
+            self.thread.join(timeout=2)
+        sm = [float(r[1]) for r in self.rows if r[1].replace(".", "").isdigit()]
+        mx = [float(r[2]) for r in self.rows if r[2].replace(".", "").isdigit()]
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = sorted({names[k] for r in self.rows for k in range(4) if r[5 + k].lower() == "active"})
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(mx) if mx else None,
+                "reasons": reasons, "samples": len(self.rows)}
+
+
+def make_scene(tmp, n_spheres=10000, width=W, height=H, seed=2):
+    from radiantiumplusplus_gb300 import scenes
+    sc, assets = scenes.many_spheres(n_spheres=n_spheres, width=width, height=height, spp=1, max_depth=MAX_DEPTH,
+                                     seed=seed)
+    return scenes.write_scene(tmp, sc, assets)
+
+
+def cpu_baseline(scene_path, row_step=8, spp=1):
+    """Times the CPU oracle on rows [0, H) step `row_step`, `spp` samples per pixel."""
+    sys.path.insert(0, os.path.join(ROOT, "tests"))
+    import oracle_lib
+    o = oracle_lib.OracleScene.from_file(scene_path)
+    threads = os.cpu_count() or 1
+    t0 = time.perf_counter()
+    _, stats = o.render(rows=(0, o.height, row_step), samples=(0, spp), threads=threads)
+    dt = time.perf_counter() - t0
+    n = int(stats[2])
+    rays = int(stats[0] + stats[1])
+    o.close()
+    return {"value": n / dt, "unit": "samples/s", "cores": threads, "kind": "port",
+            "sample": "rows 0..%d step %d of the %dx%d many-spheres frame at %d spp (%d samples, %.1f s)"
+                      % (o.height, row_step, o.width, o.height, spp, n, dt),
+            "mrays_per_s": rays / dt / 1e6}
+
+
+def dist_setup():
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    if world > 1:
+        import torch.distributed as dist
+        import torch
+        backend = "nccl" if torch.cuda.is_available() else "gloo"
+        dist.init_process_group(backend=backend)
+    return world, rank, local
+
+
+def barrier(world):
+    if world > 1:
+        import torch.distributed as dist
+        dist.barrier()
+
+
+def allreduce_max(world, v):
+    if world <= 1:
+        return v
+    import torch
+    import torch.distributed as dist
+    t = torch.tensor([v], dtype=torch.float64, device="cuda" if torch.cuda.is_available() else "cpu")
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def run_reference(args, world, rank):
+    if rank != 0:
+        return
+    with tempfile.TemporaryDirectory(prefix="rad_bench_") as tmp:
+        path = make_scene(tmp)
+        sys.path.insert(0, os.path.join(ROOT, "tests"))
+        import oracle_lib
+        o = oracle_lib.OracleScene.from_file(path)
+        threads = os.cpu_count() or 1
+        row_step = 16
+        for _ in range(args.warmup):
+            o.render(rows=(0, H, row_step * 4), samples=(0, 1), threads=threads)
+        n_tot, t_tot = 0, 0.0
+        for k in range(args.steps):
+            t0 = time.perf_counter()
+            _, st = o.render(rows=(k % row_step, H, row_step), samples=(0, 1), threads=threads)
+            t_tot += time.perf_counter() - t0
+            n_tot += int(st[2])
+        value = n_tot / t_tot
+        line = {"impl": "reference", "metric": "samples/s (path, many-spheres 1920x1080, depth 16)", "value": value,
+                "unit": "samples/s", "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
+                "ms_per_step": 1000 * t_tot / args.steps, "higher_is_better": True, "scaling": "weak",
+                "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded generator)",
+                "config": {"workload": "many_spheres_1080p", "spheres": 10000, "triangles": 3200000,
+                           "width": W, "height": H, "max_depth": MAX_DEPTH, "sample_per_step": "1/%d of rows, 1 spp" % row_step},
+                "cpu_baseline": {"value": value, "unit": "samples/s", "cores": threads, "kind": "port",
+                                 "sample": "every %d-th row of the frame at 1 spp per step" % row_step},
+                "e2e": {"value": value, "unit": "samples/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+        print(json.dumps(line), flush=True)
+
+
+def run_ours(args, world, rank, local):
+    import numpy as np
+    import torch
+    import radiantiumplusplus_gb300 as rad
+
+    torch.cuda.set_device(local)
+    rad.init({"device": local})
+    hbm_peak, peak_src = _peaks()
+    with tempfile.TemporaryDirectory(prefix="rad_bench_") as tmp:
+        path = make_scene(tmp, seed=2)
+        t0 = time.perf_counter()
+        scene = rad.Scene.from_file(path)
+        load_s = time.perf_counter() - t0
+        spp_step = 1
+        # traversal statistics for the roofline's algorithmic bytes (not timed)
+        j = scene.submit(spp=1, first_sample=10_000, count_traversal=True)
+        j.wait()
+        cs = j.stats()
+        j.close()
+        nodes_per_ray = cs["trav_nodes_closest"] / max(1, cs["rays_closest"])
+        prims_per_ray = cs["trav_prims_closest"] / max(1, cs["rays_closest"])
+        # warm-up
+        j = scene.submit(spp=max(1, args.warmup) * spp_step, first_sample=20_000)
+        j.wait()
+        j.close()
+        # ---- device-timed value: one job of K samples per pixel, events on the library stream
+        clocks = ClockSampler(local)
+        barrier(world)
+        torch.cuda.synchronize()
+        clocks.start()
+        job = scene.submit(spp=args.steps * spp_step, first_sample=0, profile=True)
+        job.wait()
+        torch.cuda.synchronize()
+        barrier(world)
+        clk = clocks.stop()
+        st = job.stats()
+        job.close()
+        gpu_s = allreduce_max(world, st["gpu_ms"] / 1000.0)
+        samples = st["samples"] * world
+        value = samples / gpu_s
+        mrays = (st["rays_closest"] + st["rays_shadow"]) * world / gpu_s / 1e6
+        # ---- e2e through the C ABI with host buffers: submit 1 spp, wait, film -> pinned host
+        pinned = torch.empty((H, W, 3), dtype=torch.float32, pin_memory=True)
+        host_film = pinned.numpy()
+        barrier(world)
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        for k in range(args.steps):
+            jj = scene.submit(spp=spp_step, first_sample=30_000 + k)
+            jj.wait()
+            jj.film(out=host_film)
+            jj.close()
+        torch.cuda.synchronize()
+        e2e_s = allreduce_max(world, time.perf_counter() - t0)
+        barrier(world)
+        e2e_value = args.steps * W * H * spp_step * world / e2e_s
+        # ---- roofline for the dominant kernel
+        kern = {"extend": st["ms_extend"], "shade": st["ms_shade"], "shadow": st["ms_shadow"],
+                "generate": st["ms_generate"], "accumulate": st["ms_accumulate"]}
+        dominant = max(kern, key=kern.get)
+        n_ext = max(1, st["n_extend"])
+        ext_bytes = st["rays_closest"] * (BYTES_QUEUE + BYTES_RAY + BYTES_HIT + nodes_per_ray * BYTES_NODE
+                                          + prims_per_ray * BYTES_PRIM)
+        ext_launch_ms = st["ms_extend"] / n_ext
+        achieved = (ext_bytes / n_ext) / (ext_launch_ms / 1000.0) / 1e9 if ext_launch_ms > 0 else 0.0
+        cpu = None
+        if rank == 0 and world == 1 and not args.no_cpu:
+            cpu = cpu_baseline(path, row_step=args.cpu_row_step)
+        scene.close()
+    line = {
+        "metric": "samples/s (path, many-spheres 1920x1080, depth 16)",
+        "value": value, "unit": "samples/s", "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
+        "ms_per_step": 1000.0 * gpu_s / args.steps, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded generator, no dataset)",
+        "config": {"workload": "many_spheres_1080p", "spheres": 10000, "triangles": 3200000, "emitters": 20,
+                   "width": W, "height": H, "spp_per_step": spp_step, "max_depth": MAX_DEPTH, "rr_depth": 3,
+                   "parallelism": "replicas" if world > 1 else "single_gpu",
+                   "l2": "inputs larger than L2: resident scene + path state > 129 MB",
+                   "scene_load_s": round(load_s, 3)},
+        "mrays_per_s": mrays,
+        "rays_per_sample": (st["rays_closest"] + st["rays_shadow"]) / max(1, st["samples"]),
+        "gpu_launches": st["kernel_launches"],
+        "kernel_ms": {k: round(v, 3) for k, v in kern.items()},
+        "roofline": {"bound": "hbm", "kernel": "extend (BVH8 closest hit)", "achieved": achieved, "peak": hbm_peak,
+                     "unit": "GB/s", "frac": achieved / hbm_peak, "traffic": None,
+                     "peak_source": peak_src, "dominant_kernel_by_time": dominant,
+                     "nodes_per_ray": nodes_per_ray, "prims_per_ray": prims_per_ray,
+                     "bytes_per_ray": BYTES_QUEUE + BYTES_RAY + BYTES_HIT + nodes_per_ray * BYTES_NODE
+                     + prims_per_ray * BYTES_PRIM},
+        "e2e": {"value": e2e_value, "unit": "samples/s", "h2d_bytes_per_step": 16,
+                "d2h_bytes_per_step": W * H * 3 * 4},
+        "clocks": clk,
+    }
+    if cpu is not None:
+        line["cpu_baseline"] = cpu
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline leg")
+    ap.add_argument("--cpu-row-step", type=int, default=4)
+    args = ap.parse_args()
+    world, rank, local = dist_setup()
+    if args.impl == "reference":
+        run_reference(args, world, rank)
+    else:
+        run_ours(args, world, rank, local)
+    if world > 1:
+        import torch.distributed as dist
+        dist.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,159 @@
+/*
+ * radgpu -- GB300 (sm_103a) wavefront path tracer behind a C ABI.
+ *
+ * Drop-in replacement for the RadiantiumPlusPlus offline hot path: the
+ * `path` and `vol_path` renderers (module/rad.offline/src/renderer/path.cpp,
+ * vol_path.cpp), their sample-renderer driver (sample_renderer.cpp) and the
+ * Embree accelerator (src/accel/embree.cpp). Scenes are the reference's JSON
+ * format with the same factory names. Plain pointers and sizes only: no C++
+ * or torch types cross this boundary, and no exception escapes it.
+ *
+ * Every function returns an int status: RAD_OK (0) or one of RAD_ERR_*; the
+ * message of the last failure on the calling thread is available from
+ * rad_last_error(). Device faults are reported as status words, never traps.
+ */
+#ifndef RADGPU_H_
+#define RADGPU_H_
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#if defined(__GNUC__)
+#define RAD_API __attribute__((visibility("default")))
+#else
+#define RAD_API
+#endif
+
+/* Status codes. RAD_ERR_UNKNOWN_FACTORY mirrors the reference's
+ * RadArgumentException("cannot find factory") (rad.core/src/factory.cpp:13-19). */
+#define RAD_OK 0
+#define RAD_ERR_INVALID_ARG 1
+#define RAD_ERR_JSON 2
+#define RAD_ERR_UNKNOWN_FACTORY 3
+#define RAD_ERR_IO 4
+#define RAD_ERR_CUDA 5
+#define RAD_ERR_OUT_OF_MEMORY 6
+#define RAD_ERR_ADMISSION 7 /* job footprint exceeds the device budget */
+#define RAD_ERR_TIMEOUT 8
+#define RAD_ERR_CANCELLED 9
+#define RAD_ERR_NOT_READY 10
+#define RAD_ERR_NO_DEVICE 11
+#define RAD_ERR_DEVICE_CHECK 12 /* a device-side bounds/iteration check fired */
+#define RAD_ERR_UNSUPPORTED 13
+
+typedef struct rad_scene rad_scene; /* resident scene: BVH8 + materials + lights + media */
+typedef struct rad_job rad_job;     /* one render: film, sample counters, queues */
+
+/* Scene summary (camera, sampler and renderer settings from the JSON). */
+typedef struct rad_scene_info {
+  int32_t width, height;
+  int32_t spp;          /* sampler.sample_count (sampler.cpp:6) */
+  uint32_t seed;        /* sampler.seed */
+  int32_t max_depth;    /* renderer.max_depth, -1 = unbounded */
+  int32_t rr_depth;     /* renderer.rr_depth */
+  int32_t is_vol_path;  /* 1 for "vol_path", 0 for "path" */
+  int32_t n_shapes, n_lights, n_media, n_materials;
+  uint64_t n_prims;     /* triangles + analytic primitives */
+  uint64_t n_bvh_nodes; /* 8-wide nodes */
+  uint64_t device_bytes;
+} rad_scene_info;
+
+/* One render request. spp = 0 takes the scene's sample_count; seed = UINT32_MAX
+ * takes the scene's sampler seed. first_sample lets a job continue an earlier
+ * one with disjoint sample indices (resumable accumulation). */
+typedef struct rad_job_desc {
+  uint32_t spp;
+  uint32_t seed;
+  uint32_t first_sample;
+  uint32_t flags; /* RAD_JOB_* */
+} rad_job_desc;
+
+#define RAD_JOB_PROFILE_KERNELS 1u /* time every kernel launch with CUDA events */
+#define RAD_JOB_SYNC 2u            /* render on the calling thread, return when done */
+#define RAD_JOB_COUNT_TRAVERSAL 4u /* count BVH8 node visits / primitive tests (slower) */
+
+/* Counters of one job. Rays = primary + extension + shadow rays traced. */
+typedef struct rad_stats {
+  uint64_t samples;          /* pixel samples finished */
+  uint64_t invalid_samples;  /* NaN/Inf/negative samples dropped (sample_renderer.cpp:101-105) */
+  uint64_t rays_closest;     /* primary + extension rays */
+  uint64_t rays_shadow;
+  uint64_t kernel_launches;  /* kernels this library launched for the job */
+  double gpu_ms;             /* device time of the job's waves (CUDA events) */
+  double wall_ms;            /* host time from start of execution to completion */
+  double queue_ms;           /* host time from submit to start of execution */
+  /* per-kernel device time when RAD_JOB_PROFILE_KERNELS is set */
+  double ms_generate, ms_extend, ms_shade, ms_shadow, ms_accumulate, ms_volpath;
+  uint64_t n_extend, n_shade, n_shadow;
+  /* with RAD_JOB_COUNT_TRAVERSAL: node visits and primitive tests */
+  uint64_t trav_nodes_closest, trav_prims_closest, trav_nodes_shadow, trav_prims_shadow;
+} rad_stats;
+
+/* ---- library ------------------------------------------------------------ */
+/* config_json may be NULL. Keys: "device" (int), "budget_bytes" (admission
+ * budget for resident scenes + films, default 150e9), "max_paths" (paths in
+ * flight per wave), "block_size". Idempotent. */
+RAD_API int rad_init(const char* config_json);
+RAD_API int rad_shutdown(void);
+/* Copies the calling thread's last error message (NUL-terminated). */
+RAD_API int rad_last_error(char* buf, size_t size);
+RAD_API int rad_version(int32_t* major, int32_t* minor);
+
+/* ---- scenes (BuildContext::SetFromJson + Build, build_context.cpp:47-321) -- */
+RAD_API int rad_scene_load_json(const char* json_text, const char* base_dir, rad_scene** out);
+RAD_API int rad_scene_load_file(const char* path, rad_scene** out);
+RAD_API int rad_scene_destroy(rad_scene* scene);
+RAD_API int rad_scene_info_get(const rad_scene* scene, rad_scene_info* info);
+/* Device bytes the scene holds (BVH + primitives + materials + media). */
+RAD_API int rad_scene_footprint(const rad_scene* scene, uint64_t* bytes);
+
+/* ---- jobs (Renderer::Start/Wait/Stop/..., renderer.h:19-48) --------------- */
+/* Non-blocking unless RAD_JOB_SYNC: the job joins the serving loop, which
+ * admits it once its film fits the device budget and interleaves its waves
+ * with the other running jobs. */
+RAD_API int rad_job_submit(rad_scene* scene, const rad_job_desc* desc, rad_job** out);
+/* timeout_ms < 0 waits forever; returns RAD_ERR_TIMEOUT if not done in time. */
+RAD_API int rad_job_wait(rad_job* job, int64_t timeout_ms);
+RAD_API int rad_job_cancel(rad_job* job);
+/* Thread-safe progress in pixel samples: done, total. */
+RAD_API int rad_job_progress(rad_job* job, uint64_t* done, uint64_t* total);
+/* Film (sum / spp, sample_renderer.cpp:109-114), row-major RGB fp32, width x height. */
+RAD_API int rad_job_film(rad_job* job, float* rgb, int32_t width, int32_t height);
+RAD_API int rad_job_stats(rad_job* job, rad_stats* stats);
+RAD_API int rad_job_destroy(rad_job* job);
+
+/* ---- parity entry points ------------------------------------------------- */
+/* Accel::RayIntersectPreliminary / RayIntersect (accel.h:10-30).
+ * rays: n x 8 floats (ox, oy, oz, tmin, dx, dy, dz, tmax), host memory.
+ * hits: n x 5 words: closest -> (t, u, v, prim id, front) with prim id =
+ * 0xffffffff on a miss (t, u, v floats; prim, front uint32); any -> word 3 is
+ * 1 when occluded. Prim id = shape prefix offset + primitive index in shape. */
+RAD_API int rad_trace_batch(rad_scene* scene, const float* rays, int64_t n, float* hits, int32_t any_hit);
+/* Same on device pointers, on the library's stream, asynchronous. */
+RAD_API int rad_trace_batch_device(rad_scene* scene, const float* d_rays, int64_t n, float* d_hits, int32_t any_hit);
+/* Bsdf::Eval + Bsdf::Pdf (bsdf.h:103-142) for one BSDF given as reference JSON,
+ * e.g. {"type":"rough_metal","alpha":0.2}. wi, wo: n x 3 local directions;
+ * f: n x 3 (cosine-weighted); pdf: n. Host memory. */
+RAD_API int rad_bsdf_eval_batch(const char* bsdf_json, const float* wi, const float* wo, int64_t n, float* f,
+                                float* pdf);
+/* Bsdf::Sample. u: n x 3 (lobe, dir.x, dir.y). Outputs as the reference's
+ * BsdfSampleResult: wo n x 3, pdf n, f n x 3, eta n, type n (BsdfType bits). */
+RAD_API int rad_bsdf_sample_batch(const char* bsdf_json, const float* wi, const float* u, int64_t n, float* wo,
+                                  float* pdf, float* f, float* eta, uint32_t* type);
+/* Perspective::SampleRay (perspective.cpp:73-82) for pixel samples, jitter from
+ * each sample's own stream. pixels: n (x + y * width); out: n x 8 rays. */
+RAD_API int rad_camera_rays(rad_scene* scene, const uint32_t* pixels, int64_t n, uint32_t sample, uint32_t seed,
+                            float* rays);
+/* Radiance of individual pixel samples (Li), n x 3, through the same kernels
+ * as a job. */
+RAD_API int rad_render_samples(rad_scene* scene, const uint32_t* pixels, const uint32_t* samples, int64_t n,
+                               uint32_t seed, float* radiance);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* RADGPU_H_ */

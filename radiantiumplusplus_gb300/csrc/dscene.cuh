@@ -1,0 +1,311 @@
+// Device scene functions: hit -> SurfaceInteraction (mesh_base.cpp:38-82,
+// rectangle.cpp:186-199, sphere.cpp:215-249, interaction.cpp:45-53), light
+// sampling and densities (scene.cpp:65-113, area.cpp, skybox.cpp, shape.cpp,
+// sphere.cpp:265-328), spawn offsets (interaction.cpp:10-26) and the
+// perspective camera (perspective.cpp:73-82).
+#pragma once
+#include "dtrace.cuh"
+
+namespace rad {
+
+struct SurfInt {
+  float T;
+  V3 P, N;  // geometric normal
+  int shape;
+  Frame sh;
+  V3 Wi;
+};
+
+// interaction.cpp:10-16
+RD V3 OffsetP(V3 P, V3 N, V3 d) {
+  float m = fmaxr(fmaxr(fabsf(P.x), fabsf(P.y)), fabsf(P.z));
+  float mag = (1.f + m) * kRayEps;
+  mag = MulSign(mag, dot(N, d));
+  return Fmadd(v3s(mag), N, P);
+}
+
+RD V3 ShapeM3(const ShapeRec& s, int i) { return V3{s.m[i], s.m[i + 1], s.m[i + 2]}; }
+
+// HitShapeRecord::ComputeSurfaceInteraction for a hit of ray (O, D).
+RD SurfInt ComputeSI(const DevScene& S, V3 O, V3 D, const TraceHit& h) {
+  SurfInt si;
+  const ShapeRec& sh = S.shapes[h.shape];
+  si.T = h.t;
+  si.shape = (int)h.shape;
+  V3 dPdU;
+  V3 shN;
+  if (sh.kind == SHAPE_MESH) {
+    uint32_t tri = (h.prim - sh.primOffset) + sh.triOffset;
+    uint32_t f0 = __ldg(S.idx + 3 * (size_t)tri), f1 = __ldg(S.idx + 3 * (size_t)tri + 1),
+             f2 = __ldg(S.idx + 3 * (size_t)tri + 2);
+    V3 p0 = ld3(S.pos + 3 * (size_t)f0), p1 = ld3(S.pos + 3 * (size_t)f1), p2 = ld3(S.pos + 3 * (size_t)f2);
+    float b0 = 1.f - h.u - h.v, b1 = h.u, b2 = h.v;
+    V3 dp0 = p1 - p0, dp1 = p2 - p0;
+    si.P = p0 * b0 + (p1 * b1 + (p2 * b2));
+    si.N = normalized(cross(dp0, dp1));
+    if (!sh.hasUV) {
+      V3 X, Y;
+      CoordinateSystem(si.N, X, Y);
+      dPdU = X;
+    } else {
+      const float* uvp = S.uv;
+      float u0x = uvp[2 * f0], u0y = uvp[2 * f0 + 1], u1x = uvp[2 * f1], u1y = uvp[2 * f1 + 1];
+      float u2x = uvp[2 * f2], u2y = uvp[2 * f2 + 1];
+      float d0x = u1x - u0x, d0y = u1y - u0y, d1x = u2x - u0x, d1y = u2y - u0y;
+      float det = d0x * d1y - (d0y * d1x);
+      float invDet = det == 0.f ? 0.f : Rcp(det);
+      dPdU = invDet == 0.f ? v3s(0.f) : (d1y * dp0 - (d0y * dp1)) * invDet;
+    }
+    if (!sh.hasNormals) {
+      shN = si.N;
+    } else {
+      V3 n0 = ld3(S.nrm + 3 * (size_t)f0), n1 = ld3(S.nrm + 3 * (size_t)f1), n2 = ld3(S.nrm + 3 * (size_t)f2);
+      V3 n = n0 * b0 + (n1 * b1 + (n2 * b2));
+      float il = Rsqrt(sqnorm(n));
+      shN = n * il;
+    }
+  } else if (sh.kind == SHAPE_RECT) {
+    V3 N = ShapeM3(sh, 18), Tr = ShapeM3(sh, 21);
+    V3 p = D * h.t + O;
+    si.P = N * dot(Tr - p, N) + p;
+    si.N = N;
+    shN = N;
+    dPdU = ShapeM3(sh, 12);
+  } else {
+    V3 c{sh.m[0], sh.m[1], sh.m[2]};
+    float rad = sh.m[3];
+    V3 gn = normalized((D * h.t + O) - c);
+    shN = gn;
+    si.P = Fmadd(gn, v3s(rad), c);
+    V3 local = AffineRows(sh.m + 4, si.P);
+    V3 du{-local.y, local.x, 0.f};
+    dPdU = LinearRows(sh.m + 16, du * (2.f * kPi));
+    si.N = gn;
+  }
+  // interaction.cpp:45-53
+  si.sh.N = shN;
+  if (is_zero(dPdU)) {
+    V3 X, Y;
+    CoordinateSystem(shN, X, Y);
+    si.sh.S = X;
+  } else {
+    si.sh.S = normalized(shN * (-dot(shN, dPdU)) + dPdU);
+  }
+  si.sh.T = cross(shN, si.sh.S);
+  si.Wi = ToLocal(si.sh, -D);
+  return si;
+}
+
+// ---------------------------------------------------------------- lights
+struct DirSample {
+  V3 P, N, Dir;
+  float Pdf, Dist;
+  bool IsDelta;
+};
+
+// Mesh area CDF: DiscreteDistribution1D::SampleReuse (distribution.cpp:36-53).
+RD uint32_t CdfLowerBound(const float* cdf, uint32_t n, float value) {
+  uint32_t lo = 0, len = n;
+  while (len > 0) {
+    uint32_t half = len >> 1;
+    uint32_t mid = lo + half;
+    if (cdf[2 * (size_t)mid] < value) {
+      lo = mid + 1;
+      len = len - half - 1;
+    } else {
+      len = half;
+    }
+  }
+  return lo;
+}
+
+// Shape::SamplePosition + SampleDirection (shape.cpp:7-19, mesh_base.cpp:84-110,
+// rectangle.cpp:204-214, sphere.cpp:251-320).
+RD DirSample ShapeSampleDirection(const DevScene& S, const ShapeRec& sh, V3 refP, V2 xi) {
+  DirSample d;
+  if (sh.kind != SHAPE_SPHERE) {
+    V3 P, N;
+    float pdf;
+    if (sh.kind == SHAPE_MESH) {
+      const float* cdf = S.cdf + 2 * (size_t)sh.cdfOffset;
+      float value = xi.y * sh.cdfSum;
+      uint32_t idx = CdfLowerBound(cdf, sh.primCount, value);
+      float pm = cdf[2 * (size_t)idx + 1] * sh.cdfNorm;
+      float cd = idx == 0 ? 0.f : cdf[2 * (size_t)(idx - 1)] * sh.cdfNorm;
+      V2 txi{xi.x, (xi.y - cd) / pm};
+      uint32_t tri = idx + sh.triOffset;
+      uint32_t f0 = S.idx[3 * (size_t)tri], f1 = S.idx[3 * (size_t)tri + 1], f2 = S.idx[3 * (size_t)tri + 2];
+      V3 p0 = ld3(S.pos + 3 * (size_t)f0), p1 = ld3(S.pos + 3 * (size_t)f1), p2 = ld3(S.pos + 3 * (size_t)f2);
+      V3 e0 = p1 - p0, e1 = p2 - p0;
+      V2 b = SquareToUniformTriangle(txi);
+      P = e0 * b.x + (e1 * b.y + p0);
+      pdf = sh.cdfNorm;
+      if (!sh.hasNormals) {
+        N = normalized(cross(e0, e1));
+      } else {
+        V3 n0 = ld3(S.nrm + 3 * (size_t)f0), n1 = ld3(S.nrm + 3 * (size_t)f1), n2 = ld3(S.nrm + 3 * (size_t)f2);
+        N = normalized(n0 * (1.f - b.x - b.y) + (n1 * b.x + (n2 * b.y)));
+      }
+    } else {
+      float sx = xi.x * 2.f - 1.f, sy = xi.y * 2.f - 1.f;
+      P = AffineRows(sh.m, V3{sx, sy, 0.f});
+      N = ShapeM3(sh, 18);
+      pdf = 1.f / sh.surfaceArea;
+    }
+    d.P = P;
+    d.N = N;
+    d.IsDelta = false;
+    V3 dir = P - refP;
+    float distanceSquared = sqnorm(dir);
+    d.Dist = sqrtf(distanceSquared);
+    d.Dir = dir / d.Dist;
+    float dp = fabsf(dot(d.Dir, N));
+    float x = distanceSquared / dp;
+    d.Pdf = pdf * (isfinite(x) ? x : 0.f);
+    return d;
+  }
+  V3 c{sh.m[0], sh.m[1], sh.m[2]};
+  float radius = sh.m[3];
+  V3 dcv = c - refP;
+  float dc2 = sqnorm(dcv);
+  float radiusAdj = radius * (1.f - kRayEps);
+  if (dc2 > Sqr(radiusAdj)) {
+    float invDc = Rsqrt(dc2);
+    float sinThetaMax = radius * invDc;
+    float sinThetaMax2 = Sqr(sinThetaMax);
+    float invSinThetaMax = Rcp(sinThetaMax);
+    float cosThetaMax = SafeSqrt(1.f - sinThetaMax2);
+    float sinTheta2 = sinThetaMax2 > 0.00068523262f ? 1.f - Sqr(fmaf(cosThetaMax - 1.f, xi.x, 1.f))
+                                                   : sinThetaMax2 * xi.x;
+    float cosTheta = SafeSqrt(1.f - sinTheta2);
+    float cosAlpha = sinTheta2 * invSinThetaMax + cosTheta * SafeSqrt(fmaf(-sinTheta2, Sqr(invSinThetaMax), 1.f));
+    float sinAlpha = SafeSqrt(fmaf(-cosAlpha, cosAlpha, 1.f));
+    float ph = xi.y * (2.f * kPi);
+    float sinPhi = sinf(ph), cosPhi = cosf(ph);
+    Frame fr = FrameFromN(dcv * -invDc);
+    V3 dd = ToWorld(fr, V3{cosPhi * sinAlpha, sinPhi * sinAlpha, cosAlpha});
+    d.P = Fmadd(dd, v3s(radius), c);
+    d.N = dd;
+    V3 dir = d.P - refP;
+    float dist2 = sqnorm(dir);
+    d.Dist = sqrtf(dist2);
+    d.Dir = dir / d.Dist;
+    d.Pdf = SquareToUniformConePdf(cosThetaMax);
+  } else {
+    V3 dd = SquareToUniformSphere(xi);
+    d.P = Fmadd(dd, v3s(radius), c);
+    d.N = dd;
+    V3 dir = d.P - refP;
+    float dist2 = sqnorm(dir);
+    d.Dist = sqrtf(dist2);
+    d.Dir = dir / d.Dist;
+    d.Pdf = (1.f / sh.surfaceArea) * dist2 / AbsDot(d.Dir, d.N);
+  }
+  d.IsDelta = radius == 0.f;
+  return d;
+}
+
+// shape.cpp:21-25 / sphere.cpp:322-328
+RD float ShapePdfDirection(const ShapeRec& sh, V3 refP, V3 dir, V3 n, float dist) {
+  if (sh.kind == SHAPE_SPHERE) {
+    V3 c{sh.m[0], sh.m[1], sh.m[2]};
+    float sinAlpha = sh.m[3] * Rcp(norm(c - refP));
+    float cosAlpha = SafeSqrt(1.f - sinAlpha * sinAlpha);
+    return sinAlpha < kOneMinusEps ? SquareToUniformConePdf(cosAlpha)
+                                   : (1.f / sh.surfaceArea) * Sqr(dist) / AbsDot(dir, n);
+  }
+  float pdf = sh.kind == SHAPE_MESH ? sh.cdfNorm : 1.f / sh.surfaceArea;
+  float dp = fabsf(dot(dir, n));
+  pdf *= dp == 0.f ? 0.f : Sqr(dist) / dp;
+  return pdf;
+}
+
+// scene.cpp:65-96: uniform light pick, then the light's direction sample.
+RD DirSample SampleLightDirection(const DevScene& S, V3 refP, float xiL, V2 xi, V3& li) {
+  DirSample d{};
+  li = v3s(0.f);
+  int index;
+  float pick;
+  if (S.nLights < 2) {
+    if (S.nLights == 1) {
+      index = 0;
+      pick = 1.f;
+    } else {
+      d.Pdf = 0.f;
+      return d;
+    }
+  } else {
+    float lf = xiL * (float)S.nLights;
+    uint32_t iu = (uint32_t)lf;
+    index = (int)(iu < S.nLights - 1 ? iu : S.nLights - 1);
+    pick = S.lightPdf;
+  }
+  const LightRec& L = S.lights[index];
+  V3 rad{L.radiance[0], L.radiance[1], L.radiance[2]};
+  if (L.kind == LIGHT_AREA) {
+    d = ShapeSampleDirection(S, S.shapes[L.shape], refP, xi);
+    li = dot(-d.Dir, d.N) >= 0.f ? rad : v3s(0.f);
+  } else {
+    V3 wc{L.world[0], L.world[1], L.world[2]};
+    float radius = fmaxr(L.world[3], norm(refP - wc));
+    float dist = 2.f * radius;
+    V3 worldDir;
+    if (L.kind == LIGHT_SKYBOX) {
+      V3 dir = normalized(SquareToUniformSphere(xi));
+      worldDir = LinearRows(L.lin, dir);
+      d.N = -worldDir;
+      d.Pdf = SquareToUniformSpherePdf();
+      d.IsDelta = false;
+    } else {
+      V3 ld{L.dir[0], L.dir[1], L.dir[2]};
+      worldDir = -ld;
+      d.N = ld;
+      d.Pdf = 1.f;
+      d.IsDelta = true;
+    }
+    d.P = worldDir * dist + refP;
+    d.Dir = worldDir;
+    d.Dist = dist;
+    li = rad;
+  }
+  d.Pdf *= pick;
+  return d;
+}
+
+// scene.cpp:98-103
+RD float PdfLightDirection(const DevScene& S, int light, V3 refP, V3 dir, V3 n, float dist) {
+  const LightRec& L = S.lights[light];
+  float p = 0.f;
+  if (L.kind == LIGHT_AREA) {
+    p = dot(-dir, n) >= 0.f ? ShapePdfDirection(S.shapes[L.shape], refP, dir, n, dist) : 0.f;
+  } else if (L.kind == LIGHT_SKYBOX) {
+    p = SquareToUniformSpherePdf();
+  }
+  return p * S.lightPdf;
+}
+
+// area.cpp:42-45 / skybox.cpp:53-63 (constant radiance)
+RD V3 EvalLightAt(const DevScene& S, int light, const SurfInt* si) {
+  const LightRec& L = S.lights[light];
+  V3 rad{L.radiance[0], L.radiance[1], L.radiance[2]};
+  if (L.kind == LIGHT_AREA) return dot(ToWorld(si->sh, si->Wi), si->N) >= 0.f ? rad : v3s(0.f);
+  if (L.kind == LIGHT_SKYBOX) return rad;
+  return v3s(0.f);
+}
+
+// ---------------------------------------------------------------- camera
+RD void CameraRay(const CameraRec& c, float sx, float sy, V3& O, V3& D, float& tmin, float& tmax) {
+  float tx = sx * (1.f / (float)c.width), ty = sy * (1.f / (float)c.height);
+  V3 nearP = Affine4(c.clipToCamera, V3{tx, ty, 0.f});
+  V3 dir = normalized(nearP);
+  float invZ = Rcp(dir.z);
+  O = Affine4(c.camToWorld, V3{0.f, 0.f, 0.f});
+  V3 lw{(c.camToWorld[0] * dir.x + c.camToWorld[1] * dir.y) + c.camToWorld[2] * dir.z,
+        (c.camToWorld[4] * dir.x + c.camToWorld[5] * dir.y) + c.camToWorld[6] * dir.z,
+        (c.camToWorld[8] * dir.x + c.camToWorld[9] * dir.y) + c.camToWorld[10] * dir.z};
+  D = normalized(lw);
+  tmin = c.nearZ * invZ;
+  tmax = c.farZ * invZ;
+}
+
+}  // namespace rad

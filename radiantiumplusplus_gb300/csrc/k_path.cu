@@ -1,0 +1,370 @@
+// Wavefront `path` integrator (Path::Li, rad.offline/src/renderer/path.cpp:131-236)
+// split into stages over per-bounce path queues:
+//   generate   -- camera ray per pixel sample (perspective.cpp:73-82), PCG stream
+//   extend     -- closest hit for every queued path (BVH8, embree.cpp:87-111)
+//   shade      -- emitter MIS, NEE light sample + BSDF eval/pdf (emits a shadow
+//                 record), BSDF sample, Russian roulette, next ray; survivors are
+//                 appended to the next queue with warp-aggregated atomics
+//   shadow     -- occlusion of the NEE rays (scene.cpp:53-63); unoccluded
+//                 contributions are added to the path's radiance
+//   accumulate -- film += radiance with the reference's invalid-sample drop
+//                 (sample_renderer.cpp:93-114)
+// Every stage is a grid-stride kernel over a device-side count, so a whole wave
+// is a fixed launch sequence that a CUDA graph can capture.
+#include "dbsdf.cuh"
+#include "dscene.cuh"
+#include "kernels.h"
+
+namespace rad {
+
+constexpr int kBlock = 128;
+
+static int g_gridBlocks = 0;
+int PathGridBlocks() {
+  if (g_gridBlocks == 0) {
+    int dev = 0, sms = 148;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    g_gridBlocks = sms * 8;
+  }
+  return g_gridBlocks;
+}
+
+RD float MisWeight(float a, float b) {  // path.cpp:231-236
+  a *= a;
+  b *= b;
+  float w = a / (a + b);
+  return isfinite(w) ? w : 0.f;
+}
+
+// Warp-aggregated append: one atomic per warp; returns the slot for this lane.
+__device__ __forceinline__ uint32_t WarpAppend(uint32_t* counter, bool pred) {
+  uint32_t mask = __ballot_sync(0xffffffffu, pred);
+  uint32_t lane = threadIdx.x & 31u;
+  uint32_t base = 0;
+  if (mask) {
+    int leader = __ffs(mask) - 1;
+    if ((int)lane == leader) base = atomicAdd(counter, (uint32_t)__popc(mask));
+    base = __shfl_sync(0xffffffffu, base, leader);
+  }
+  return base + __popc(mask & ((1u << lane) - 1u));
+}
+
+__global__ void __launch_bounds__(kBlock) KGenerate(DevScene S, PathBuffers B, WaveParams w) {
+  uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i == 0) {
+    for (int k = 0; k < kMiscBase; k++) B.counters[k] = 0u;
+    B.counters[kMiscBase] = 0u;
+    B.counters[kMiscBase + 2] = 0u;
+    B.counters[kMiscBase + 3] = 0u;
+    B.counters[0] = w.count;
+  }
+  if (i >= w.count) return;
+  uint32_t pix = w.pixelList ? w.pixelList[i] : w.pixelBegin + i;
+  uint32_t smp = w.sampleList ? w.sampleList[i] : w.sample;
+  uint32_t x = pix % (uint32_t)S.cam.width, y = pix / (uint32_t)S.cam.width;
+  Pcg32 rng = PcgForSample(pix, smp, w.seed);
+  float jx = Next1D(rng);
+  float jy = Next1D(rng);
+  V3 O, D;
+  float tmin, tmax;
+  CameraRay(S.cam, (float)x + jx, (float)y + jy, O, D, tmin, tmax);
+  B.rayO[i] = make_float4(O.x, O.y, O.z, tmin);
+  B.rayD[i] = make_float4(D.x, D.y, D.z, tmax);
+  B.thr[i] = make_float4(1.f, 1.f, 1.f, 1.f);
+  B.L[i] = make_float4(0.f, 0.f, 0.f, 1.f);
+  B.prev[i] = make_float4(0.f, 0.f, 0.f, __uint_as_float(1u));
+  B.rng[i] = make_uint2((uint32_t)rng.state, (uint32_t)(rng.state >> 32));
+  B.pixel[i] = pix;
+  B.q[0][i] = i;
+}
+
+// Adds per-warp sums of traversal counters into 64-bit totals (counting variants only).
+__device__ __forceinline__ void FlushTravCounts(unsigned long long* out, uint32_t nodes, uint32_t prims) {
+  for (int o = 16; o > 0; o >>= 1) {
+    nodes += __shfl_down_sync(0xffffffffu, nodes, o);
+    prims += __shfl_down_sync(0xffffffffu, prims, o);
+  }
+  if ((threadIdx.x & 31u) == 0) {
+    atomicAdd(out, (unsigned long long)nodes);
+    atomicAdd(out + 1, (unsigned long long)prims);
+  }
+}
+
+template <bool COUNT>
+__global__ void __launch_bounds__(kBlock) KExtend(DevScene S, PathBuffers B, int depth, unsigned long long* trav) {
+  uint32_t count = B.counters[depth];
+  const uint32_t* qin = B.q[depth & 1];
+  uint32_t* err = B.counters + kMiscBase + 1;
+  uint32_t nN = 0, nP = 0;
+  for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < count; i += gridDim.x * blockDim.x) {
+    uint32_t p = qin[i];
+    float4 o = B.rayO[p], d = B.rayD[p];
+    RayPre r = MakeRayPre(V3{o.x, o.y, o.z}, V3{d.x, d.y, d.z}, o.w);
+    TraceHit h;
+    TraceBvh8<false, COUNT>(S, r, d.w, h, err, &nN, &nP);
+    HitRec hr;
+    hr.t = h.t;
+    hr.u = h.u;
+    hr.v = h.v;
+    hr.prim = h.prim;
+    hr.shape = h.shape;
+    hr.front = h.front;
+    hr.pad[0] = hr.pad[1] = 0;
+    B.hit[p] = hr;
+  }
+  if (COUNT) FlushTravCounts(trav, nN, nP);
+}
+
+__global__ void __launch_bounds__(kBlock) KShade(DevScene S, PathBuffers B, int depth) {
+  uint32_t count = B.counters[depth];
+  const uint32_t* qin = B.q[depth & 1];
+  uint32_t* qout = B.q[(depth + 1) & 1];
+  uint32_t* cntOut = B.counters + depth + 1;
+  uint32_t* cntSh = B.counters + kShadowBase + depth;
+  uint32_t stride = gridDim.x * blockDim.x;
+  // warp-uniform loop so every lane takes part in the appends
+  for (uint32_t base = blockIdx.x * blockDim.x; base < count; base += stride) {
+    uint32_t i = base + threadIdx.x;
+    bool active = i < count;
+    bool keep = false, shadow = false;
+    uint32_t p = 0;
+    float4 shO = make_float4(0, 0, 0, 0), shD = shO, shC = shO;
+    if (active) {
+      p = qin[i];
+      HitRec h = B.hit[p];
+      float4 ro = B.rayO[p], rd = B.rayD[p];
+      float4 thr4 = B.thr[p], L4 = B.L[p], pv = B.prev[p];
+      uint2 rs = B.rng[p];
+      Pcg32 rng;
+      rng.state = ((uint64_t)rs.y << 32) | rs.x;
+      V3 O{ro.x, ro.y, ro.z}, D{rd.x, rd.y, rd.z};
+      V3 thr{thr4.x, thr4.y, thr4.z};
+      float eta = thr4.w;
+      V3 L{L4.x, L4.y, L4.z};
+      float prevPdf = L4.w;
+      uint32_t pflags = __float_as_uint(pv.w);
+      bool specular = pflags & 1u;
+      V3 prevP{pv.x, pv.y, pv.z};
+      bool anyHit = h.prim != kNoPrim;
+      SurfInt si;
+      if (anyHit) {
+        TraceHit th{h.t, h.u, h.v, h.prim, h.shape, h.front};
+        si = ComputeSI(S, O, D, th);
+      } else {
+        si.T = kInf;
+        si.P = v3s(0.f);
+        si.N = v3s(0.f);
+        si.shape = -1;
+        si.sh.S = si.sh.T = si.sh.N = v3s(0.f);
+        si.Wi = -D;  // scene.cpp:45-47: world-space -D on a miss
+      }
+      int hitLight = anyHit ? S.shapes[h.shape].light : S.envLight;
+      if (hitLight >= 0) {
+        float weight;
+        if (specular) {
+          weight = 1.f;
+        } else {
+          // SurfaceInteraction::ToDsr (interaction.cpp:68-74)
+          V3 rel = si.P - prevP;
+          float dist = norm(rel);
+          V3 dir = anyHit ? rel / dist : -si.Wi;
+          float lightPdf = PdfLightDirection(S, hitLight, prevP, dir, si.sh.N, dist);
+          weight = MisWeight(prevPdf, lightPdf);
+        }
+        V3 li = EvalLightAt(S, hitLight, &si);
+        L = L + cmul(thr, li) * weight;
+      }
+      bool stop = !anyHit || (S.maxDepth >= 0 && depth + 1 >= S.maxDepth);
+      int bsdf = -1;
+      if (!stop) {
+        const ShapeRec& shp = S.shapes[h.shape];
+        if (shp.light >= 0 || shp.bsdf < 0) stop = true;
+        bsdf = shp.bsdf;
+      }
+      if (!stop) {
+        const MatRec* mats = S.mats;
+        if (mats[bsdf].flags & BT_NODELTA) {
+          float xl = Next1D(rng);
+          V2 xd = Next2D(rng);
+          V3 li;
+          DirSample dsr = SampleLightDirection(S, si.P, xl, xd, li);
+          if (dsr.Pdf > 0.f) {
+            V3 wo = ToLocal(si.sh, dsr.Dir);
+            V3 f;
+            float bsdfPdf;
+            BsdfEvalPdf(mats, (uint32_t)bsdf, si.Wi, wo, f, bsdfPdf);
+            // Scene::IsOcclude (scene.cpp:53-63)
+            V3 so = OffsetP(si.P, si.N, dsr.P - si.P);
+            V3 sd = dsr.P - so;
+            float sdist = norm(sd);
+            if (!(sdist < kShadowEps)) {
+              sd = sd / sdist;
+              float weight = dsr.IsDelta ? 1.f : MisWeight(dsr.Pdf, bsdfPdf);
+              V3 c = cmul(cmul(thr, f), li) * weight / dsr.Pdf;
+              shadow = true;
+              shO = make_float4(so.x, so.y, so.z, sdist * (1.f - kShadowEps));
+              shD = make_float4(sd.x, sd.y, sd.z, __uint_as_float(p));
+              shC = make_float4(c.x, c.y, c.z, 0.f);
+            }
+          }
+        }
+        float xl = Next1D(rng);
+        V2 xd = Next2D(rng);
+        BsdfSampleRes bs = BsdfSample(mats, (uint32_t)bsdf, si.Wi, xl, xd);
+        if (bs.pdf <= 0.f) {
+          stop = true;
+        } else {
+          thr = cmul(thr, bs.f) / bs.pdf;
+          eta *= bs.eta;
+          V3 nd = ToWorld(si.sh, bs.wo);
+          V3 no = OffsetP(si.P, si.N, nd);
+          prevPdf = bs.pdf;
+          prevP = si.P;
+          specular = (bs.type & BT_DELTA) != 0u;
+          if (depth >= S.rrDepth) {
+            float rr = fminr(max_comp(thr) * Sqr(eta), 0.95f);
+            if (Next1D(rng) > rr) {
+              stop = true;
+            } else {
+              thr = thr * Rcp(rr);
+            }
+          }
+          if (!stop) {
+            keep = true;
+            B.rayO[p] = make_float4(no.x, no.y, no.z, 0.f);
+            B.rayD[p] = make_float4(nd.x, nd.y, nd.z, kFloatMax);
+            B.thr[p] = make_float4(thr.x, thr.y, thr.z, eta);
+            B.prev[p] = make_float4(prevP.x, prevP.y, prevP.z, __uint_as_float(specular ? 1u : 0u));
+            B.rng[p] = make_uint2((uint32_t)rng.state, (uint32_t)(rng.state >> 32));
+          }
+        }
+      }
+      B.L[p] = make_float4(L.x, L.y, L.z, prevPdf);
+    }
+    uint32_t slot = WarpAppend(cntOut, keep);
+    if (keep) qout[slot] = p;
+    uint32_t sslot = WarpAppend(cntSh, shadow);
+    if (shadow) {
+      B.shO[sslot] = shO;
+      B.shD[sslot] = shD;
+      B.shC[sslot] = shC;
+    }
+  }
+}
+
+template <bool COUNT>
+__global__ void __launch_bounds__(kBlock) KShadow(DevScene S, PathBuffers B, int depth, unsigned long long* trav) {
+  uint32_t count = B.counters[kShadowBase + depth];
+  uint32_t* err = B.counters + kMiscBase + 1;
+  uint32_t nN = 0, nP = 0;
+  for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < count; i += gridDim.x * blockDim.x) {
+    float4 o = B.shO[i], d = B.shD[i];
+    RayPre r = MakeRayPre(V3{o.x, o.y, o.z}, V3{d.x, d.y, d.z}, 0.f);
+    TraceHit h;
+    bool occ = TraceBvh8<true, COUNT>(S, r, o.w, h, err, &nN, &nP);
+    if (!occ) {
+      uint32_t p = __float_as_uint(d.w);
+      float4 c = B.shC[i];
+      float4 l = B.L[p];
+      B.L[p] = make_float4(l.x + c.x, l.y + c.y, l.z + c.z, l.w);
+    }
+  }
+  if (COUNT) FlushTravCounts(trav + 2, nN, nP);
+}
+
+// sample_renderer.cpp:101-105: drop NaN in any channel, Inf / negative in the
+// first channel only (spectrum.h:28-29), the sample still counts in 1/spp.
+__global__ void __launch_bounds__(256) KAccumulate(PathBuffers B, FilmView film, uint32_t count) {
+  uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i == 0 && film.stats) {
+    unsigned long long cl = 0, sh = 0;
+    for (int k = 0; k <= kMaxBounce; k++) {
+      cl += B.counters[k];
+      sh += B.counters[kShadowBase + k];
+    }
+    cl += B.counters[kMiscBase + 2];
+    sh += B.counters[kMiscBase + 3];
+    film.stats[0] += cl;
+    film.stats[1] += sh;
+    film.stats[3] += count;
+  }
+  bool bad = false;
+  if (i < count) {
+    float4 l = B.L[i];
+    uint32_t pix = B.pixel[i];
+    bad = isnan(l.x) || isnan(l.y) || isnan(l.z) || isinf(l.x) || l.x < 0.f;
+    float4 a = film.accum[pix];
+    if (!bad) {
+      a.x += l.x;
+      a.y += l.y;
+      a.z += l.z;
+    }
+    a.w += 1.f;
+    film.accum[pix] = a;
+  }
+  uint32_t m = __ballot_sync(0xffffffffu, bad);
+  if (m && (threadIdx.x & 31u) == 0 && film.stats) atomicAdd(film.stats + 2, (unsigned long long)__popc(m));
+}
+
+__global__ void KGatherRadiance(PathBuffers B, uint32_t count, float* out) {
+  uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= count) return;
+  float4 l = B.L[i];
+  out[3 * i] = l.x;
+  out[3 * i + 1] = l.y;
+  out[3 * i + 2] = l.z;
+}
+
+__global__ void KResolveFilm(FilmView film, float scale, float* out) {
+  uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= (uint32_t)(film.width * film.height)) return;
+  float4 a = film.accum[i];
+  out[3 * i] = a.x * scale;
+  out[3 * i + 1] = a.y * scale;
+  out[3 * i + 2] = a.z * scale;
+}
+
+cudaError_t LaunchGenerate(const DevScene& S, const PathBuffers& B, const WaveParams& w, cudaStream_t st) {
+  uint32_t n = w.count > 0 ? w.count : 1;
+  KGenerate<<<(n + kBlock - 1) / kBlock, kBlock, 0, st>>>(S, B, w);
+  return cudaGetLastError();
+}
+cudaError_t LaunchExtend(const DevScene& S, const PathBuffers& B, int depth, int grid, cudaStream_t st,
+                         unsigned long long* trav) {
+  if (trav)
+    KExtend<true><<<grid, kBlock, 0, st>>>(S, B, depth, trav);
+  else
+    KExtend<false><<<grid, kBlock, 0, st>>>(S, B, depth, nullptr);
+  return cudaGetLastError();
+}
+cudaError_t LaunchShade(const DevScene& S, const PathBuffers& B, int depth, int grid, cudaStream_t st) {
+  KShade<<<grid, kBlock, 0, st>>>(S, B, depth);
+  return cudaGetLastError();
+}
+cudaError_t LaunchShadow(const DevScene& S, const PathBuffers& B, int depth, int grid, cudaStream_t st,
+                         unsigned long long* trav) {
+  if (trav)
+    KShadow<true><<<grid, kBlock, 0, st>>>(S, B, depth, trav);
+  else
+    KShadow<false><<<grid, kBlock, 0, st>>>(S, B, depth, nullptr);
+  return cudaGetLastError();
+}
+cudaError_t LaunchAccumulate(const PathBuffers& B, const FilmView& film, uint32_t count, cudaStream_t st) {
+  if (count == 0) return cudaSuccess;
+  KAccumulate<<<(count + 255) / 256, 256, 0, st>>>(B, film, count);
+  return cudaGetLastError();
+}
+cudaError_t LaunchGatherRadiance(const PathBuffers& B, uint32_t count, float* out, cudaStream_t st) {
+  if (count == 0) return cudaSuccess;
+  KGatherRadiance<<<(count + 255) / 256, 256, 0, st>>>(B, count, out);
+  return cudaGetLastError();
+}
+cudaError_t LaunchResolveFilm(const FilmView& film, float scale, float* out, cudaStream_t st) {
+  uint32_t n = (uint32_t)(film.width * film.height);
+  if (n == 0) return cudaSuccess;
+  KResolveFilm<<<(n + 255) / 256, 256, 0, st>>>(film, scale, out);
+  return cudaGetLastError();
+}
+
+}  // namespace rad

@@ -1,0 +1,75 @@
+// Host-side launchers of the sm_103a kernels (implemented in k_*.cu).
+#pragma once
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include "records.h"
+
+namespace rad {
+
+// Wavefront path state, structure of arrays, one slot per path in flight.
+struct PathBuffers {
+  float4* rayO;    // origin xyz, tmin
+  float4* rayD;    // direction xyz, tmax
+  float4* thr;     // throughput rgb, eta
+  float4* L;       // radiance rgb, previous BSDF pdf
+  float4* prev;    // previous shading point xyz, flags (bit 0 specular path) | depth << 8
+  uint2* rng;      // PCG32 state
+  uint32_t* pixel; // film pixel index
+  HitRec* hit;
+  uint32_t* q[2];  // active path queues (ping-pong)
+  float4* shO;     // shadow ray origin xyz, tmax
+  float4* shD;     // shadow ray direction xyz, path slot bits
+  float4* shC;     // shadow contribution rgb
+  uint32_t* counters;  // [0, kMaxBounce]: active counts; [kShadowBase, +kMaxBounce]: shadow counts; kMisc..
+  uint32_t capacity;
+};
+
+constexpr int kMaxBounce = 256;
+constexpr int kShadowBase = kMaxBounce + 1;
+constexpr int kMiscBase = 2 * kMaxBounce + 2;  // [0] spare, [1] device error word (sticky),
+                                               // [2] vol closest rays, [3] vol shadow-side rays
+constexpr int kCounterWords = kMiscBase + 8;
+
+struct FilmView {
+  float4* accum;  // rgb sum, sample count in w
+  int32_t width, height;
+  // job counters (64-bit, device): [0] closest rays, [1] shadow rays,
+  // [2] invalid samples, [3] samples, [4..7] traversal counts (see LaunchExtend)
+  unsigned long long* stats;
+};
+
+// ---- parity kernels (k_parity.cu)
+cudaError_t LaunchBsdfEval(const MatRec* mats, const float* wi, const float* wo, int64_t n, float* f, float* pdf,
+                           cudaStream_t st);
+cudaError_t LaunchBsdfSample(const MatRec* mats, const float* wi, const float* u, int64_t n, float* wo, float* pdf,
+                             float* f, float* eta, uint32_t* type, cudaStream_t st);
+cudaError_t LaunchTrace(const DevScene& S, const float* rays, int64_t n, float* hits, int anyHit, uint32_t* err,
+                        cudaStream_t st);
+cudaError_t LaunchCameraRays(const DevScene& S, const uint32_t* pix, int64_t n, uint32_t sample, uint32_t seed,
+                             float* out, cudaStream_t st);
+
+// ---- wavefront path tracer (k_path.cu)
+struct WaveParams {
+  uint32_t pixelBegin, count;  // pixels [pixelBegin, pixelBegin + count) of the film
+  uint32_t sample, seed;
+  const uint32_t* pixelList;   // optional explicit pixel list (parity hook)
+  const uint32_t* sampleList;  // optional explicit per-path sample indices
+};
+int PathGridBlocks();
+cudaError_t LaunchGenerate(const DevScene& S, const PathBuffers& B, const WaveParams& w, cudaStream_t st);
+// trav (optional, 4 x u64): extend node visits, extend prim tests, shadow node visits, shadow prim tests
+cudaError_t LaunchExtend(const DevScene& S, const PathBuffers& B, int depth, int grid, cudaStream_t st,
+                         unsigned long long* trav = nullptr);
+cudaError_t LaunchShade(const DevScene& S, const PathBuffers& B, int depth, int grid, cudaStream_t st);
+cudaError_t LaunchShadow(const DevScene& S, const PathBuffers& B, int depth, int grid, cudaStream_t st,
+                         unsigned long long* trav = nullptr);
+cudaError_t LaunchAccumulate(const PathBuffers& B, const FilmView& film, uint32_t count, cudaStream_t st);
+cudaError_t LaunchGatherRadiance(const PathBuffers& B, uint32_t count, float* out, cudaStream_t st);
+cudaError_t LaunchResolveFilm(const FilmView& film, float scale, float* out, cudaStream_t st);
+
+// ---- volumetric path tracer (k_vol.cu): one thread per path, full Li loop
+cudaError_t LaunchVolPath(const DevScene& S, const PathBuffers& B, const WaveParams& w, uint32_t* err,
+                          cudaStream_t st);
+
+}  // namespace rad

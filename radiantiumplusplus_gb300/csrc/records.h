@@ -1,0 +1,161 @@
+// Device-resident scene and path-state layouts shared by the host builder and
+// the sm_103a kernels. Plain PODs, fixed sizes (static_assert'ed), all float
+// data in FP32 as the reference computes (RAD_FLOAT_32_WEIGHT,
+// rad.offline/CMakeLists.txt:4,76-82).
+#pragma once
+#include <stdint.h>
+
+#if defined(__CUDACC__)
+#define RAD_HD __host__ __device__
+#else
+#define RAD_HD
+#endif
+
+namespace rad {
+
+// ---------------------------------------------------------------- BSDFs
+enum MatKind : uint32_t { MAT_NONE = 0, MAT_DIFFUSE = 1, MAT_ROUGH_METAL = 2, MAT_ROUGH_GLASS = 3, MAT_DISNEY = 4,
+                          MAT_TWO_SIDE = 5 };
+
+// BsdfType bits (rad.offline/include/rad/offline/render/bsdf.h:32-50)
+enum : uint32_t { BT_DIFFUSE = 1, BT_GLOSSY = 2, BT_DELTA = 4, BT_REFLECTION = 8, BT_TRANSMISSION = 16,
+                  BT_NODELTA = 3 };
+
+// Disney "present" flags (disney.cpp:459-471)
+enum : uint32_t { DF_ANISO = 1, DF_SPECTRANS = 2, DF_SHEEN = 4, DF_SHEENTINT = 8, DF_FLATNESS = 16,
+                  DF_SPECTINT = 32, DF_METALLIC = 64, DF_CLEARCOAT = 128 };
+
+// One BSDF instance: 96 bytes. p[] layout per kind:
+//  diffuse:     p0..2 reflectance
+//  rough_metal: p0..2 R, p3..5 eta, p6..8 k, p9 alphaX, p10 alphaY, p11 ggx(1)/beckmann(0), p12 sampleVisible
+//  rough_glass: p0..2 R, p3..5 T, p6 eta, p7 invEta, p9 alphaX, p10 alphaY, p11 ggx, p12 sampleVisible
+//  disney:      p0..2 baseColor, p3 roughness, p4 anisotropic, p5 specTrans, p6 sheen, p7 sheenTint,
+//               p8 flatness, p9 specTint, p10 metallic, p11 clearcoat, p12 clearcoatGloss, p13 eta,
+//               p14 specularSample, p15 clearcoatSample; aux = diffuseReflectSample
+//  two_side:    ref0 outside material index, ref1 inside material index
+struct alignas(16) MatRec {
+  uint32_t kind;
+  uint32_t flags;      // BsdfType bits of the instance
+  uint32_t dflags;     // Disney present flags
+  uint32_t ref0, ref1; // two_side children
+  float aux;           // disney: diffuse_reflectance_sampling_rate
+  uint32_t pad[2];
+  float p[16];
+};
+static_assert(sizeof(MatRec) == 96, "MatRec must stay 96 bytes");
+
+// ---------------------------------------------------------------- shapes
+enum ShapeKind : uint32_t { SHAPE_MESH = 0, SHAPE_RECT = 1, SHAPE_SPHERE = 2 };
+
+// One shape: 208 bytes.
+struct alignas(16) ShapeRec {
+  uint32_t kind;
+  int32_t bsdf, light, inMedium, outMedium;
+  uint32_t primOffset, primCount;  // global primitive id range
+  uint32_t triOffset;              // mesh: first triangle in the global index array
+  uint32_t hasNormals, hasUV;
+  uint32_t cdfOffset;              // mesh: area CDF offset (emitters)
+  float surfaceArea;
+  float cdfSum, cdfNorm;           // DiscreteDistribution1D sum / normalization
+  uint32_t pad0[2];
+  // rect: toWorld rows (3x4), frame S/T/N; sphere: center, radius, toLocal rows (3x4), toWorld linear (3x3)
+  float m[36];
+};
+static_assert(sizeof(ShapeRec) == 208, "ShapeRec size");
+
+// ---------------------------------------------------------------- lights
+enum LightKind : uint32_t { LIGHT_AREA = 0, LIGHT_SKYBOX = 1, LIGHT_DIRECTIONAL = 2 };
+struct alignas(16) LightRec {
+  uint32_t kind;
+  int32_t shape;
+  uint32_t pad[2];
+  float radiance[4];   // rgb (area radiance, sky radiance, directional irradiance)
+  float dir[4];        // directional: world direction the light travels
+  float world[4];      // world bounding sphere center xyz, radius w (skybox.cpp:139-144)
+  float lin[12];       // skybox toWorld linear part, rows of 4
+};
+static_assert(sizeof(LightRec) == 112, "LightRec size");
+
+// ---------------------------------------------------------------- media
+enum MediumKind : uint32_t { MED_HOMOGENEOUS = 0, MED_HETEROGENEOUS = 1 };
+struct alignas(16) MediumRec {
+  uint32_t kind;
+  uint32_t hg;            // 1 = henyey-greenstein, 0 = isotropic
+  uint32_t gridSigma;     // sigma_t from a grid
+  uint32_t repeatWrap;
+  float g, scale, maxDensity, pad0;
+  float sigmaT[4], albedo[4];
+  float bbMin[4], bbMax[4];
+  float toLocal[12];      // heterogeneous: world -> [0,1]^3 grid space, rows of 4
+  int32_t nx, ny, nz, channels;
+  uint64_t gridOffset;    // float offset of the grid in the volume pool
+  uint64_t pad1;
+};
+static_assert(sizeof(MediumRec) == 176, "MediumRec size");
+
+// ---------------------------------------------------------------- camera
+struct alignas(16) CameraRec {
+  float clipToCamera[16];  // cameraToClip.ToLocal (perspective.cpp:79)
+  float camToWorld[16];    // cameraToWorld.ToWorld
+  float nearZ, farZ;
+  int32_t width, height;
+};
+
+// ---------------------------------------------------------------- BVH8
+// 80-byte 8-wide node with 8-bit quantised child boxes (5 x uint4):
+//  q0 = (px, py, pz, ex | ey<<8 | ez<<16 | imask<<24)
+//  q1 = (childBase, primBase, meta[0..3], meta[4..7])
+//  q2 = (qlo.x[0..7], qlo.y[0..7]); q3 = (qlo.z[0..7], qhi.x[0..7]); q4 = (qhi.y[0..7], qhi.z[0..7])
+// Child slot s is internal when imask bit s is set (node = childBase + number
+// of internal slots below s). Otherwise meta[s] = 0 marks an empty slot, else
+// bit 7 = analytic primitives, bits 6..5 = primitive count (1..3), bits 4..0 =
+// offset from primBase. Slots are assigned by ray octant at build time so that
+// visiting slot (b ^ octant) for b = 0..7 is close to front-to-back.
+struct alignas(16) Bvh8Node {
+  uint32_t w[20];
+};
+static_assert(sizeof(Bvh8Node) == 80, "Bvh8Node must be 80 bytes");
+
+// Leaf-order primitive record, 48 bytes (3 x float4):
+//  triangle: (v0, prim id bits) (v1, shape id bits) (v2, 0)
+//  rectangle: rows of the float32 world->object matrix (rectangle.cpp:34-46)
+//  sphere:   (center, radius) (-, -, -, -) (-, -, -, -)
+// primInfo (uint2, leaf order): (global prim id, shape id | kind << 28).
+struct alignas(16) PrimRec {
+  float v[12];
+};
+static_assert(sizeof(PrimRec) == 48, "PrimRec must be 48 bytes");
+
+// ---------------------------------------------------------------- scene
+struct DevScene {
+  const Bvh8Node* nodes;
+  const PrimRec* prims;
+  const uint32_t* primInfo;   // 2 words per leaf-order primitive
+  const ShapeRec* shapes;
+  const MatRec* mats;
+  const LightRec* lights;
+  const MediumRec* media;
+  const float* pos;            // global vertex positions, 3 floats each
+  const float* nrm;            // global vertex normals (or null)
+  const float* uv;             // global vertex uvs (or null)
+  const uint32_t* idx;         // global triangle indices, 3 per triangle
+  const float* cdf;            // emitter-mesh area CDF / PMF (2 floats per triangle)
+  const float* volume;         // density grids
+  uint32_t nNodes, nPrims, nShapes, nLights;
+  uint32_t nMedia, nMats;
+  int32_t envLight, globalMedium;
+  float lightPdf;
+  int32_t maxDepth, rrDepth, isVol;
+  CameraRec cam;
+};
+
+// Hit record written by the extend kernel, 32 bytes.
+struct alignas(16) HitRec {
+  float t, u, v;
+  uint32_t prim;   // global prim id, 0xffffffff = miss
+  uint32_t shape;
+  uint32_t front;
+  uint32_t pad[2];
+};
+
+}  // namespace rad

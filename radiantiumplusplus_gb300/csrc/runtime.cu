@@ -1,0 +1,963 @@
+// C ABI of include/radgpu.h: library state, resident scenes, render jobs and
+// the serving loop. The reference's Renderer::Start spawns one render thread
+// that walks TBB tiles (sample_renderer.cpp:60-122); here one worker thread
+// owns the CUDA stream, admits submitted jobs against a device-memory budget,
+// and interleaves their waves (one wave = one sample index over a job's
+// pixels) round-robin, so jobs that arrive while others run are admitted as
+// soon as memory allows and share the device at wave granularity.
+#include <algorithm>
+#include <atomic>
+#include <chrono>
+#include <condition_variable>
+#include <cstdio>
+#include <cstring>
+#include <deque>
+#include <fstream>
+#include <mutex>
+#include <sstream>
+#include <string>
+#include <thread>
+#include <vector>
+
+#include "../../include/radgpu.h"
+#include "host_scene.h"
+#include "kernels.h"
+
+using namespace rad;
+
+namespace {
+
+thread_local std::string t_err;
+
+struct Error {
+  int code;
+  std::string msg;
+};
+
+void Check(cudaError_t e, const char* what) {
+  if (e != cudaSuccess) {
+    if (e == cudaErrorMemoryAllocation) {
+      cudaGetLastError();
+      throw Error{RAD_ERR_OUT_OF_MEMORY, std::string(what) + ": " + cudaGetErrorString(e)};
+    }
+    throw Error{RAD_ERR_CUDA, std::string(what) + ": " + cudaGetErrorString(e)};
+  }
+}
+
+int Fail(int code, const std::string& msg) {
+  t_err = msg;
+  return code;
+}
+
+template <typename F>
+int Guard(F&& f) {
+  try {
+    f();
+    return RAD_OK;
+  } catch (const Error& e) {
+    return Fail(e.code, e.msg);
+  } catch (const JsonError& e) {
+    return Fail(RAD_ERR_JSON, e.what());
+  } catch (const FactoryError& e) {
+    return Fail(RAD_ERR_UNKNOWN_FACTORY, e.what());
+  } catch (const IoError& e) {
+    return Fail(RAD_ERR_IO, e.what());
+  } catch (const ConfigError& e) {
+    return Fail(RAD_ERR_INVALID_ARG, e.what());
+  } catch (const std::bad_alloc&) {
+    return Fail(RAD_ERR_OUT_OF_MEMORY, "host allocation failed");
+  } catch (const std::exception& e) {
+    return Fail(RAD_ERR_INVALID_ARG, e.what());
+  }
+}
+
+double NowMs() {
+  using namespace std::chrono;
+  return duration<double, std::milli>(steady_clock::now().time_since_epoch()).count();
+}
+
+template <typename T>
+T* DevAlloc(size_t count, std::vector<void*>& owner, uint64_t& bytes) {
+  if (count == 0) return nullptr;
+  void* p = nullptr;
+  Check(cudaMalloc(&p, count * sizeof(T)), "cudaMalloc");
+  owner.push_back(p);
+  bytes += count * sizeof(T);
+  return static_cast<T*>(p);
+}
+
+enum JobState { kQueued, kRunning, kCompleting, kDone };
+
+}  // namespace
+
+struct rad_scene {
+  DevScene dev{};
+  std::vector<void*> allocs;
+  uint64_t bytes = 0;
+  rad_scene_info info{};
+  std::atomic<int> jobs{0};
+};
+
+struct rad_job {
+  rad_scene* scene = nullptr;
+  uint32_t spp = 0, seed = 0, first = 0, flags = 0;
+  uint64_t total = 0;
+  uint32_t nextSample = 0;
+  uint32_t chunkCursor = 0;
+  float4* accum = nullptr;
+  unsigned long long* dStats = nullptr;
+  unsigned long long* hStats = nullptr;  // pinned
+  float* resolve = nullptr;
+  uint64_t filmBytes = 0;
+  JobState state = kQueued;
+  int status = RAD_OK;
+  std::string err;
+  bool cancel = false;
+  std::atomic<uint64_t> launched{0};
+  cudaEvent_t evStart = nullptr, evEnd = nullptr;
+  double tSubmit = 0, tStart = 0, tEnd = 0;
+  rad_stats stats{};
+  std::vector<std::pair<cudaEvent_t, cudaEvent_t>> profEv;
+  std::vector<int> profKind;
+  std::mutex m;
+  std::condition_variable cv;
+};
+
+namespace {
+
+struct Lib {
+  bool inited = false;
+  int device = 0;
+  int sms = 0;
+  cudaStream_t stream = nullptr;
+  uint64_t budget = 150ull * 1000 * 1000 * 1000;
+  std::atomic<uint64_t> used{0};
+  uint32_t maxPaths = 1u << 21;
+  PathBuffers paths{};
+  std::vector<void*> pathAllocs;
+  uint64_t pathBytes = 0;
+  uint32_t* hCounters = nullptr;  // pinned
+  std::mutex gpuMu;
+  // serving loop
+  std::thread worker;
+  std::mutex qmu;
+  std::condition_variable qcv;
+  std::deque<rad_job*> pending;
+  std::vector<rad_job*> running;
+  size_t rr = 0;
+  bool stop = false;
+  std::vector<cudaEvent_t> evPool;
+};
+
+Lib& L() {
+  static Lib lib;
+  return lib;
+}
+std::mutex g_initMu;
+
+cudaEvent_t GetEvent() {
+  Lib& lib = L();
+  if (!lib.evPool.empty()) {
+    cudaEvent_t e = lib.evPool.back();
+    lib.evPool.pop_back();
+    return e;
+  }
+  cudaEvent_t e;
+  Check(cudaEventCreate(&e), "cudaEventCreate");
+  return e;
+}
+
+void AllocPaths(Lib& lib) {
+  uint32_t P = lib.maxPaths;
+  PathBuffers& B = lib.paths;
+  auto& o = lib.pathAllocs;
+  uint64_t& b = lib.pathBytes;
+  B.rayO = DevAlloc<float4>(P, o, b);
+  B.rayD = DevAlloc<float4>(P, o, b);
+  B.thr = DevAlloc<float4>(P, o, b);
+  B.L = DevAlloc<float4>(P, o, b);
+  B.prev = DevAlloc<float4>(P, o, b);
+  B.rng = DevAlloc<uint2>(P, o, b);
+  B.pixel = DevAlloc<uint32_t>(P, o, b);
+  B.hit = DevAlloc<HitRec>(P, o, b);
+  B.q[0] = DevAlloc<uint32_t>(P, o, b);
+  B.q[1] = DevAlloc<uint32_t>(P, o, b);
+  B.shO = DevAlloc<float4>(P, o, b);
+  B.shD = DevAlloc<float4>(P, o, b);
+  B.shC = DevAlloc<float4>(P, o, b);
+  B.counters = DevAlloc<uint32_t>(kCounterWords, o, b);
+  Check(cudaMemset(B.counters, 0, kCounterWords * sizeof(uint32_t)), "cudaMemset");
+  B.capacity = P;
+  Check(cudaMallocHost(&lib.hCounters, kCounterWords * sizeof(uint32_t)), "cudaMallocHost");
+  lib.used += b;
+}
+
+void WorkerMain();
+
+void InitLocked(const char* cfg) {
+  Lib& lib = L();
+  if (lib.inited) return;
+  if (cfg && *cfg) {
+    JValue c = JsonReader::Parse(cfg);
+    if (const JValue* v = c.get("device")) lib.device = (int)v->n;
+    if (const JValue* v = c.get("budget_bytes")) lib.budget = (uint64_t)v->n;
+    if (const JValue* v = c.get("max_paths")) lib.maxPaths = (uint32_t)v->n;
+  }
+  if (lib.maxPaths < 1024) lib.maxPaths = 1024;
+  int n = 0;
+  cudaError_t e = cudaGetDeviceCount(&n);
+  if (e != cudaSuccess || n == 0) {
+    cudaGetLastError();
+    throw Error{RAD_ERR_NO_DEVICE, "no CUDA device available"};
+  }
+  if (lib.device < 0 || lib.device >= n) throw Error{RAD_ERR_INVALID_ARG, "device index out of range"};
+  Check(cudaSetDevice(lib.device), "cudaSetDevice");
+  Check(cudaDeviceGetAttribute(&lib.sms, cudaDevAttrMultiProcessorCount, lib.device), "attribute");
+  Check(cudaStreamCreateWithFlags(&lib.stream, cudaStreamNonBlocking), "cudaStreamCreate");
+  AllocPaths(lib);
+  lib.stop = false;
+  lib.worker = std::thread(WorkerMain);
+  lib.inited = true;
+}
+
+void EnsureInit() {
+  std::lock_guard<std::mutex> g(g_initMu);
+  InitLocked(nullptr);
+}
+
+// ---- one wave of a job (caller holds gpuMu) --------------------------------
+struct ProfSink {
+  rad_job* job;
+  void Begin(int kind, cudaEvent_t& a) {
+    if (!job || !(job->flags & RAD_JOB_PROFILE_KERNELS)) return;
+    a = GetEvent();
+    cudaEventRecord(a, L().stream);
+    (void)kind;
+  }
+  void End(int kind, cudaEvent_t a) {
+    if (!job || !(job->flags & RAD_JOB_PROFILE_KERNELS)) return;
+    cudaEvent_t b = GetEvent();
+    cudaEventRecord(b, L().stream);
+    job->profEv.push_back({a, b});
+    job->profKind.push_back(kind);
+  }
+};
+
+// Launches the bounce loop for `count` generated paths. Returns kernels launched.
+uint64_t LaunchBounces(const DevScene& S, uint32_t count, ProfSink& ps, unsigned long long* trav = nullptr) {
+  Lib& lib = L();
+  uint64_t launches = 0;
+  int grid = std::max(1, std::min(lib.sms * 8, (int)((count + 127) / 128)));
+  int iters = S.maxDepth >= 0 ? std::max(1, S.maxDepth) : kMaxBounce;
+  if (iters > kMaxBounce) iters = kMaxBounce;
+  for (int d = 0; d < iters; d++) {
+    cudaEvent_t a = nullptr;
+    ps.Begin(1, a);
+    Check(LaunchExtend(S, lib.paths, d, grid, lib.stream, trav), "extend");
+    ps.End(1, a);
+    ps.Begin(2, a);
+    Check(LaunchShade(S, lib.paths, d, grid, lib.stream), "shade");
+    ps.End(2, a);
+    ps.Begin(3, a);
+    Check(LaunchShadow(S, lib.paths, d, grid, lib.stream, trav), "shadow");
+    ps.End(3, a);
+    launches += 3;
+    if (S.maxDepth < 0 && (d % 8) == 7) {
+      // unbounded depth: stop once the next queue is empty
+      Check(cudaMemcpyAsync(lib.hCounters, lib.paths.counters, (d + 2) * sizeof(uint32_t), cudaMemcpyDeviceToHost,
+                            lib.stream),
+            "counter readback");
+      Check(cudaStreamSynchronize(lib.stream), "sync");
+      if (lib.hCounters[d + 1] == 0) break;
+    }
+  }
+  return launches;
+}
+
+// Runs wave(s) for the job's next sample index over all its pixels.
+void RunWave(rad_job* j) {
+  Lib& lib = L();
+  const DevScene& S = j->scene->dev;
+  uint32_t W = (uint32_t)S.cam.width, H = (uint32_t)S.cam.height;
+  uint64_t npix = (uint64_t)W * H;
+  ProfSink ps{j};
+  FilmView film{j->accum, (int32_t)W, (int32_t)H, j->dStats};
+  for (uint64_t p0 = 0; p0 < npix; p0 += lib.maxPaths) {
+    uint32_t count = (uint32_t)std::min<uint64_t>(lib.maxPaths, npix - p0);
+    WaveParams w{(uint32_t)p0, count, j->first + j->nextSample, j->seed, nullptr, nullptr};
+    cudaEvent_t a = nullptr;
+    ps.Begin(0, a);
+    Check(LaunchGenerate(S, lib.paths, w, lib.stream), "generate");
+    ps.End(0, a);
+    uint64_t launches = 1;
+    if (S.isVol) {
+      ps.Begin(5, a);
+      Check(LaunchVolPath(S, lib.paths, w, lib.paths.counters + kMiscBase + 1, lib.stream), "vol_path");
+      ps.End(5, a);
+      launches++;
+    } else {
+      launches += LaunchBounces(S, count, ps, (j->flags & RAD_JOB_COUNT_TRAVERSAL) ? j->dStats + 4 : nullptr);
+    }
+    ps.Begin(4, a);
+    Check(LaunchAccumulate(lib.paths, film, count, lib.stream), "accumulate");
+    ps.End(4, a);
+    launches++;
+    j->stats.kernel_launches += launches;
+  }
+  j->nextSample++;
+  j->launched += npix;
+}
+
+void FinishJob(rad_job* j, int status, const std::string& err) {
+  Lib& lib = L();
+  if (j->accum) {
+    // film memory stays until rad_job_destroy (the user reads it after wait)
+  }
+  {
+    std::lock_guard<std::mutex> g(j->m);
+    j->status = status;
+    j->err = err;
+    j->state = kDone;
+    j->tEnd = NowMs();
+  }
+  j->cv.notify_all();
+  (void)lib;
+}
+
+void CompleteJob(rad_job* j) {
+  // called after evEnd completed
+  float ms = 0;
+  if (j->evStart && j->evEnd) cudaEventElapsedTime(&ms, j->evStart, j->evEnd);
+  j->stats.gpu_ms = ms;
+  j->stats.rays_closest = j->hStats[0];
+  j->stats.rays_shadow = j->hStats[1];
+  j->stats.invalid_samples = j->hStats[2];
+  j->stats.samples = j->hStats[3];
+  j->stats.trav_nodes_closest = j->hStats[4];
+  j->stats.trav_prims_closest = j->hStats[5];
+  j->stats.trav_nodes_shadow = j->hStats[6];
+  j->stats.trav_prims_shadow = j->hStats[7];
+  double acc[6] = {0, 0, 0, 0, 0, 0};
+  uint64_t cnt[6] = {0, 0, 0, 0, 0, 0};
+  for (size_t k = 0; k < j->profEv.size(); k++) {
+    float e = 0;
+    cudaEventElapsedTime(&e, j->profEv[k].first, j->profEv[k].second);
+    acc[j->profKind[k]] += e;
+    cnt[j->profKind[k]]++;
+    L().evPool.push_back(j->profEv[k].first);
+    L().evPool.push_back(j->profEv[k].second);
+  }
+  j->profEv.clear();
+  j->profKind.clear();
+  j->stats.ms_generate = acc[0];
+  j->stats.ms_extend = acc[1];
+  j->stats.ms_shade = acc[2];
+  j->stats.ms_shadow = acc[3];
+  j->stats.ms_accumulate = acc[4];
+  j->stats.ms_volpath = acc[5];
+  j->stats.n_extend = cnt[1];
+  j->stats.n_shade = cnt[2];
+  j->stats.n_shadow = cnt[3];
+  uint32_t errWord = 0;
+  cudaMemcpy(&errWord, L().paths.counters + kMiscBase + 1, 4, cudaMemcpyDeviceToHost);
+  if (errWord) cudaMemset(L().paths.counters + kMiscBase + 1, 0, 4);
+  j->stats.wall_ms = NowMs() - j->tStart;
+  j->stats.queue_ms = j->tStart - j->tSubmit;
+  if (errWord) {
+    FinishJob(j, RAD_ERR_DEVICE_CHECK, "device-side check fired (traversal stack or iteration bound), code " +
+                                           std::to_string(errWord));
+    return;
+  }
+  FinishJob(j, j->cancel ? RAD_ERR_CANCELLED : RAD_OK, j->cancel ? "job cancelled" : "");
+}
+
+bool AdmitFilm(rad_job* j) {
+  Lib& lib = L();
+  uint64_t need = j->filmBytes;
+  uint64_t cur = lib.used.load();
+  if (cur + need > lib.budget) return false;
+  lib.used += need;
+  return true;
+}
+
+void AllocJobFilm(rad_job* j) {
+  const DevScene& S = j->scene->dev;
+  size_t npix = (size_t)S.cam.width * S.cam.height;
+  Check(cudaMalloc(&j->accum, npix * sizeof(float4)), "film");
+  Check(cudaMalloc(&j->dStats, 8 * sizeof(unsigned long long)), "stats");
+  Check(cudaMallocHost(&j->hStats, 8 * sizeof(unsigned long long)), "stats host");
+  std::memset(j->hStats, 0, 8 * sizeof(unsigned long long));
+  Check(cudaMemsetAsync(j->accum, 0, npix * sizeof(float4), L().stream), "memset film");
+  Check(cudaMemsetAsync(j->dStats, 0, 8 * sizeof(unsigned long long), L().stream), "memset stats");
+  Check(cudaEventCreate(&j->evStart), "event");
+  Check(cudaEventCreate(&j->evEnd), "event");
+}
+
+// Runs a job to completion on the calling thread (RAD_JOB_SYNC or worker).
+void StartJob(rad_job* j) {
+  AllocJobFilm(j);
+  j->tStart = NowMs();
+  Check(cudaEventRecord(j->evStart, L().stream), "event record");
+  j->state = kRunning;
+}
+
+void EndJobLaunch(rad_job* j) {
+  Check(cudaMemcpyAsync(j->hStats, j->dStats, 8 * sizeof(unsigned long long), cudaMemcpyDeviceToHost, L().stream),
+        "stats readback");
+  Check(cudaEventRecord(j->evEnd, L().stream), "event record");
+  j->state = kCompleting;
+}
+
+void WorkerMain() {
+  Lib& lib = L();
+  cudaSetDevice(lib.device);
+  std::vector<rad_job*> completing;
+  for (;;) {
+    rad_job* j = nullptr;
+    {
+      std::unique_lock<std::mutex> lk(lib.qmu);
+      // admission: films that fit the budget join the running set
+      for (auto it = lib.pending.begin(); it != lib.pending.end();) {
+        rad_job* p = *it;
+        if (p->cancel) {
+          it = lib.pending.erase(it);
+          FinishJob(p, RAD_ERR_CANCELLED, "job cancelled before admission");
+          continue;
+        }
+        if (AdmitFilm(p)) {
+          lib.running.push_back(p);
+          p->state = kRunning;
+          it = lib.pending.erase(it);
+          continue;
+        }
+        if (lib.running.empty() && completing.empty()) {
+          // nothing running can free memory: this job can never be admitted
+          it = lib.pending.erase(it);
+          FinishJob(p, RAD_ERR_ADMISSION, "job film exceeds the device budget");
+          continue;
+        }
+        ++it;
+      }
+      if (lib.running.empty() && completing.empty()) {
+        if (lib.stop) break;
+        lib.qcv.wait(lk);
+        continue;
+      }
+      if (!lib.running.empty()) {
+        lib.rr = lib.rr % lib.running.size();
+        j = lib.running[lib.rr];
+        lib.rr++;
+      }
+    }
+    if (j) {
+      std::lock_guard<std::mutex> g(lib.gpuMu);
+      try {
+        if (!j->accum) StartJob(j);
+        if (!j->cancel && j->nextSample < j->spp) RunWave(j);
+        if (j->cancel || j->nextSample >= j->spp) {
+          EndJobLaunch(j);
+          std::lock_guard<std::mutex> lk(lib.qmu);
+          lib.running.erase(std::find(lib.running.begin(), lib.running.end(), j));
+          completing.push_back(j);
+        }
+      } catch (const Error& e) {
+        std::lock_guard<std::mutex> lk(lib.qmu);
+        auto it = std::find(lib.running.begin(), lib.running.end(), j);
+        if (it != lib.running.end()) lib.running.erase(it);
+        FinishJob(j, e.code, e.msg);
+      }
+    }
+    // retire finished jobs
+    for (auto it = completing.begin(); it != completing.end();) {
+      rad_job* c = *it;
+      cudaError_t q = cudaEventQuery(c->evEnd);
+      if (q == cudaSuccess) {
+        std::lock_guard<std::mutex> g(lib.gpuMu);
+        CompleteJob(c);
+        it = completing.erase(it);
+      } else if (q == cudaErrorNotReady) {
+        ++it;
+      } else {
+        FinishJob(c, RAD_ERR_CUDA, cudaGetErrorString(q));
+        it = completing.erase(it);
+      }
+    }
+    if (!j && !completing.empty()) std::this_thread::sleep_for(std::chrono::microseconds(50));
+  }
+}
+
+uint64_t SceneUpload(const HostScene& hs, rad_scene* sc) {
+  DevScene& D = sc->dev;
+  auto& o = sc->allocs;
+  uint64_t b = 0;
+  auto up = [&](auto* dst, const auto& v) {
+    if (!v.empty()) Check(cudaMemcpy(dst, v.data(), v.size() * sizeof(v[0]), cudaMemcpyHostToDevice), "upload");
+  };
+  Bvh8Node* nodes = DevAlloc<Bvh8Node>(hs.nodes.size(), o, b);
+  PrimRec* prims = DevAlloc<PrimRec>(hs.prims.size(), o, b);
+  uint32_t* pinfo = DevAlloc<uint32_t>(hs.primInfo.size(), o, b);
+  ShapeRec* shapes = DevAlloc<ShapeRec>(hs.shapes.size(), o, b);
+  MatRec* mats = DevAlloc<MatRec>(hs.mats.size(), o, b);
+  LightRec* lights = DevAlloc<LightRec>(hs.lights.size(), o, b);
+  MediumRec* media = DevAlloc<MediumRec>(hs.media.size(), o, b);
+  float* pos = DevAlloc<float>(hs.pos.size(), o, b);
+  float* nrm = DevAlloc<float>(hs.nrm.size(), o, b);
+  float* uv = DevAlloc<float>(hs.uv.size(), o, b);
+  uint32_t* idx = DevAlloc<uint32_t>(hs.idx.size(), o, b);
+  float* cdf = DevAlloc<float>(hs.cdf.size(), o, b);
+  float* vol = DevAlloc<float>(hs.volume.size(), o, b);
+  up(nodes, hs.nodes);
+  up(prims, hs.prims);
+  up(pinfo, hs.primInfo);
+  up(shapes, hs.shapes);
+  up(mats, hs.mats);
+  up(lights, hs.lights);
+  up(media, hs.media);
+  up(pos, hs.pos);
+  up(nrm, hs.nrm);
+  up(uv, hs.uv);
+  up(idx, hs.idx);
+  up(cdf, hs.cdf);
+  up(vol, hs.volume);
+  D.nodes = nodes;
+  D.prims = prims;
+  D.primInfo = pinfo;
+  D.shapes = shapes;
+  D.mats = mats;
+  D.lights = lights;
+  D.media = media;
+  D.pos = pos;
+  D.nrm = nrm;
+  D.uv = uv;
+  D.idx = idx;
+  D.cdf = cdf;
+  D.volume = vol;
+  D.nNodes = (uint32_t)hs.nodes.size();
+  D.nPrims = (uint32_t)hs.prims.size();
+  D.nShapes = (uint32_t)hs.shapes.size();
+  D.nLights = (uint32_t)hs.lights.size();
+  D.nMedia = (uint32_t)hs.media.size();
+  D.nMats = (uint32_t)hs.mats.size();
+  D.envLight = hs.envLight;
+  D.globalMedium = hs.globalMedium;
+  D.lightPdf = hs.lightPdf;
+  D.maxDepth = hs.maxDepth;
+  D.rrDepth = hs.rrDepth;
+  D.isVol = hs.isVol ? 1 : 0;
+  D.cam = hs.cam;
+  return b;
+}
+
+void FreeAll(std::vector<void*>& v) {
+  for (void* p : v) cudaFree(p);
+  v.clear();
+}
+
+std::string ReadFile(const std::string& path) {
+  std::ifstream in(path, std::ios::binary);
+  if (!in) throw IoError("cannot open " + path);
+  std::stringstream ss;
+  ss << in.rdbuf();
+  return ss.str();
+}
+
+template <typename T>
+struct DevBuf {
+  T* p = nullptr;
+  explicit DevBuf(size_t n) {
+    if (n) Check(cudaMalloc(&p, n * sizeof(T)), "cudaMalloc");
+  }
+  ~DevBuf() {
+    if (p) cudaFree(p);
+  }
+};
+
+}  // namespace
+
+// ============================================================================
+extern "C" {
+
+int rad_init(const char* config_json) {
+  return Guard([&] {
+    std::lock_guard<std::mutex> g(g_initMu);
+    InitLocked(config_json);
+  });
+}
+
+int rad_shutdown(void) {
+  return Guard([&] {
+    std::lock_guard<std::mutex> g(g_initMu);
+    Lib& lib = L();
+    if (!lib.inited) return;
+    {
+      std::lock_guard<std::mutex> lk(lib.qmu);
+      lib.stop = true;
+    }
+    lib.qcv.notify_all();
+    if (lib.worker.joinable()) lib.worker.join();
+    cudaStreamSynchronize(lib.stream);
+    FreeAll(lib.pathAllocs);
+    lib.used -= lib.pathBytes;
+    lib.pathBytes = 0;
+    if (lib.hCounters) cudaFreeHost(lib.hCounters);
+    lib.hCounters = nullptr;
+    for (cudaEvent_t e : lib.evPool) cudaEventDestroy(e);
+    lib.evPool.clear();
+    cudaStreamDestroy(lib.stream);
+    lib.stream = nullptr;
+    lib.inited = false;
+  });
+}
+
+int rad_last_error(char* buf, size_t size) {
+  if (!buf || size == 0) return RAD_ERR_INVALID_ARG;
+  std::snprintf(buf, size, "%s", t_err.c_str());
+  return RAD_OK;
+}
+
+int rad_version(int32_t* major, int32_t* minor) {
+  if (major) *major = 0;
+  if (minor) *minor = 1;
+  return RAD_OK;
+}
+
+int rad_scene_load_json(const char* json_text, const char* base_dir, rad_scene** out) {
+  if (!json_text || !out) return Fail(RAD_ERR_INVALID_ARG, "null argument");
+  *out = nullptr;
+  return Guard([&] {
+    EnsureInit();
+    HostScene hs;
+    BuildHostScene(json_text, base_dir ? base_dir : "", hs);
+    Lib& lib = L();
+    rad_scene* sc = new rad_scene();
+    try {
+      std::lock_guard<std::mutex> g(lib.gpuMu);
+      sc->bytes = SceneUpload(hs, sc);
+    } catch (...) {
+      FreeAll(sc->allocs);
+      delete sc;
+      throw;
+    }
+    if (lib.used.load() + sc->bytes > lib.budget) {
+      FreeAll(sc->allocs);
+      delete sc;
+      throw Error{RAD_ERR_ADMISSION, "scene does not fit the device budget"};
+    }
+    lib.used += sc->bytes;
+    rad_scene_info& in = sc->info;
+    in.width = hs.cam.width;
+    in.height = hs.cam.height;
+    in.spp = hs.spp;
+    in.seed = hs.seed;
+    in.max_depth = hs.maxDepth;
+    in.rr_depth = hs.rrDepth;
+    in.is_vol_path = hs.isVol ? 1 : 0;
+    in.n_shapes = (int32_t)hs.shapes.size();
+    in.n_lights = (int32_t)hs.lights.size();
+    in.n_media = (int32_t)hs.media.size();
+    in.n_materials = (int32_t)hs.mats.size();
+    in.n_prims = hs.nPrims;
+    in.n_bvh_nodes = hs.nodes.size();
+    in.device_bytes = sc->bytes;
+    *out = sc;
+  });
+}
+
+int rad_scene_load_file(const char* path, rad_scene** out) {
+  if (!path || !out) return Fail(RAD_ERR_INVALID_ARG, "null argument");
+  std::string text;
+  int st = Guard([&] { text = ReadFile(path); });
+  if (st != RAD_OK) return st;
+  std::string p(path);
+  size_t slash = p.find_last_of('/');
+  std::string dir = slash == std::string::npos ? std::string(".") : p.substr(0, slash);
+  return rad_scene_load_json(text.c_str(), dir.c_str(), out);
+}
+
+int rad_scene_destroy(rad_scene* scene) {
+  if (!scene) return RAD_OK;
+  if (scene->jobs.load() > 0) return Fail(RAD_ERR_INVALID_ARG, "scene still has live jobs");
+  return Guard([&] {
+    Lib& lib = L();
+    std::lock_guard<std::mutex> g(lib.gpuMu);
+    cudaStreamSynchronize(lib.stream);
+    FreeAll(scene->allocs);
+    lib.used -= scene->bytes;
+    delete scene;
+  });
+}
+
+int rad_scene_info_get(const rad_scene* scene, rad_scene_info* info) {
+  if (!scene || !info) return Fail(RAD_ERR_INVALID_ARG, "null argument");
+  *info = scene->info;
+  return RAD_OK;
+}
+
+int rad_scene_footprint(const rad_scene* scene, uint64_t* bytes) {
+  if (!scene || !bytes) return Fail(RAD_ERR_INVALID_ARG, "null argument");
+  *bytes = scene->bytes;
+  return RAD_OK;
+}
+
+int rad_job_submit(rad_scene* scene, const rad_job_desc* desc, rad_job** out) {
+  if (!scene || !out) return Fail(RAD_ERR_INVALID_ARG, "null argument");
+  *out = nullptr;
+  return Guard([&] {
+    EnsureInit();
+    Lib& lib = L();
+    rad_job* j = new rad_job();
+    j->scene = scene;
+    j->spp = desc && desc->spp ? desc->spp : (uint32_t)scene->info.spp;
+    j->seed = desc && desc->seed != UINT32_MAX ? desc->seed : scene->info.seed;
+    j->first = desc ? desc->first_sample : 0;
+    j->flags = desc ? desc->flags : 0;
+    uint64_t npix = (uint64_t)scene->info.width * scene->info.height;
+    j->total = npix * j->spp;
+    j->filmBytes = npix * sizeof(float4) + 64;
+    j->tSubmit = NowMs();
+    scene->jobs++;
+    *out = j;
+    if (j->flags & RAD_JOB_SYNC) {
+      if (j->filmBytes + lib.used.load() > lib.budget) {
+        FinishJob(j, RAD_ERR_ADMISSION, "job film exceeds the device budget");
+        return;
+      }
+      lib.used += j->filmBytes;
+      std::lock_guard<std::mutex> g(lib.gpuMu);
+      try {
+        StartJob(j);
+        while (j->nextSample < j->spp && !j->cancel) RunWave(j);
+        EndJobLaunch(j);
+        Check(cudaEventSynchronize(j->evEnd), "sync");
+        CompleteJob(j);
+      } catch (const Error& e) {
+        FinishJob(j, e.code, e.msg);
+      }
+      return;
+    }
+    {
+      std::lock_guard<std::mutex> lk(lib.qmu);
+      lib.pending.push_back(j);
+    }
+    lib.qcv.notify_all();
+  });
+}
+
+int rad_job_wait(rad_job* job, int64_t timeout_ms) {
+  if (!job) return Fail(RAD_ERR_INVALID_ARG, "null job");
+  std::unique_lock<std::mutex> lk(job->m);
+  auto done = [&] { return job->state == kDone; };
+  if (timeout_ms < 0) {
+    job->cv.wait(lk, done);
+  } else if (!job->cv.wait_for(lk, std::chrono::milliseconds(timeout_ms), done)) {
+    return Fail(RAD_ERR_TIMEOUT, "job not finished within the timeout");
+  }
+  if (job->status != RAD_OK) return Fail(job->status, job->err);
+  return RAD_OK;
+}
+
+int rad_job_cancel(rad_job* job) {
+  if (!job) return Fail(RAD_ERR_INVALID_ARG, "null job");
+  {
+    std::lock_guard<std::mutex> lk(L().qmu);
+    job->cancel = true;
+  }
+  L().qcv.notify_all();
+  return RAD_OK;
+}
+
+int rad_job_progress(rad_job* job, uint64_t* done, uint64_t* total) {
+  if (!job) return Fail(RAD_ERR_INVALID_ARG, "null job");
+  bool finished;
+  {
+    std::lock_guard<std::mutex> lk(job->m);
+    finished = job->state == kDone;
+  }
+  if (done) *done = finished && job->status == RAD_OK ? job->total : job->launched.load();
+  if (total) *total = job->total;
+  return RAD_OK;
+}
+
+int rad_job_film(rad_job* job, float* rgb, int32_t width, int32_t height) {
+  if (!job || !rgb) return Fail(RAD_ERR_INVALID_ARG, "null argument");
+  {
+    std::lock_guard<std::mutex> lk(job->m);
+    if (job->state != kDone) return Fail(RAD_ERR_NOT_READY, "job is still running");
+    if (job->status != RAD_OK && job->status != RAD_ERR_CANCELLED) return Fail(job->status, job->err);
+  }
+  const DevScene& S = job->scene->dev;
+  if (width != S.cam.width || height != S.cam.height) return Fail(RAD_ERR_INVALID_ARG, "film size mismatch");
+  if (!job->accum) return Fail(RAD_ERR_NOT_READY, "job has no film");
+  return Guard([&] {
+    Lib& lib = L();
+    std::lock_guard<std::mutex> g(lib.gpuMu);
+    size_t n = (size_t)width * height * 3;
+    if (!job->resolve) Check(cudaMalloc(&job->resolve, n * sizeof(float)), "cudaMalloc");
+    float scale = 1.0f / (float)job->spp;  // sample_renderer.cpp:109-114
+    Check(LaunchResolveFilm(FilmView{job->accum, width, height, nullptr}, scale, job->resolve, lib.stream), "resolve");
+    Check(cudaMemcpyAsync(rgb, job->resolve, n * sizeof(float), cudaMemcpyDeviceToHost, lib.stream), "film copy");
+    Check(cudaStreamSynchronize(lib.stream), "sync");
+  });
+}
+
+int rad_job_stats(rad_job* job, rad_stats* stats) {
+  if (!job || !stats) return Fail(RAD_ERR_INVALID_ARG, "null argument");
+  std::lock_guard<std::mutex> lk(job->m);
+  *stats = job->stats;
+  return RAD_OK;
+}
+
+int rad_job_destroy(rad_job* job) {
+  if (!job) return RAD_OK;
+  rad_job_cancel(job);
+  rad_job_wait(job, -1);
+  return Guard([&] {
+    Lib& lib = L();
+    std::lock_guard<std::mutex> g(lib.gpuMu);
+    cudaStreamSynchronize(lib.stream);
+    if (job->accum) {
+      cudaFree(job->accum);
+      lib.used -= job->filmBytes;
+    }
+    if (job->dStats) cudaFree(job->dStats);
+    if (job->hStats) cudaFreeHost(job->hStats);
+    if (job->resolve) cudaFree(job->resolve);
+    if (job->evStart) cudaEventDestroy(job->evStart);
+    if (job->evEnd) cudaEventDestroy(job->evEnd);
+    job->scene->jobs--;
+    delete job;
+  });
+}
+
+int rad_trace_batch_device(rad_scene* scene, const float* d_rays, int64_t n, float* d_hits, int32_t any_hit) {
+  if (!scene || (n > 0 && (!d_rays || !d_hits)) || n < 0) return Fail(RAD_ERR_INVALID_ARG, "bad argument");
+  return Guard([&] {
+    Lib& lib = L();
+    Check(LaunchTrace(scene->dev, d_rays, n, d_hits, any_hit, lib.paths.counters + kMiscBase + 1, lib.stream),
+          "trace");
+  });
+}
+
+int rad_trace_batch(rad_scene* scene, const float* rays, int64_t n, float* hits, int32_t any_hit) {
+  if (!scene || (n > 0 && (!rays || !hits)) || n < 0) return Fail(RAD_ERR_INVALID_ARG, "bad argument");
+  if (n == 0) return RAD_OK;
+  return Guard([&] {
+    Lib& lib = L();
+    std::lock_guard<std::mutex> g(lib.gpuMu);
+    DevBuf<float> dr(8 * n), dh(5 * n);
+    Check(cudaMemcpyAsync(dr.p, rays, 8 * n * sizeof(float), cudaMemcpyHostToDevice, lib.stream), "copy");
+    uint32_t zero = 0;
+    Check(cudaMemcpyAsync(lib.paths.counters + kMiscBase + 1, &zero, 4, cudaMemcpyHostToDevice, lib.stream), "copy");
+    Check(LaunchTrace(scene->dev, dr.p, n, dh.p, any_hit, lib.paths.counters + kMiscBase + 1, lib.stream), "trace");
+    Check(cudaMemcpyAsync(hits, dh.p, 5 * n * sizeof(float), cudaMemcpyDeviceToHost, lib.stream), "copy");
+    uint32_t err = 0;
+    Check(cudaMemcpyAsync(&err, lib.paths.counters + kMiscBase + 1, 4, cudaMemcpyDeviceToHost, lib.stream), "copy");
+    Check(cudaStreamSynchronize(lib.stream), "sync");
+    if (err) throw Error{RAD_ERR_DEVICE_CHECK, "traversal stack bound exceeded"};
+  });
+}
+
+int rad_bsdf_eval_batch(const char* bsdf_json, const float* wi, const float* wo, int64_t n, float* f, float* pdf) {
+  if (!bsdf_json || n < 0 || (n > 0 && (!wi || !wo || !f || !pdf))) return Fail(RAD_ERR_INVALID_ARG, "bad argument");
+  return Guard([&] {
+    EnsureInit();
+    std::vector<MatRec> mats;
+    BuildMaterialRecords(JsonReader::Parse(bsdf_json), mats);
+    if (n == 0) return;
+    Lib& lib = L();
+    std::lock_guard<std::mutex> g(lib.gpuMu);
+    DevBuf<MatRec> dm(mats.size());
+    DevBuf<float> dwi(3 * n), dwo(3 * n), df(3 * n), dp(n);
+    Check(cudaMemcpyAsync(dm.p, mats.data(), mats.size() * sizeof(MatRec), cudaMemcpyHostToDevice, lib.stream), "copy");
+    Check(cudaMemcpyAsync(dwi.p, wi, 12 * n, cudaMemcpyHostToDevice, lib.stream), "copy");
+    Check(cudaMemcpyAsync(dwo.p, wo, 12 * n, cudaMemcpyHostToDevice, lib.stream), "copy");
+    Check(LaunchBsdfEval(dm.p, dwi.p, dwo.p, n, df.p, dp.p, lib.stream), "bsdf eval");
+    Check(cudaMemcpyAsync(f, df.p, 12 * n, cudaMemcpyDeviceToHost, lib.stream), "copy");
+    Check(cudaMemcpyAsync(pdf, dp.p, 4 * n, cudaMemcpyDeviceToHost, lib.stream), "copy");
+    Check(cudaStreamSynchronize(lib.stream), "sync");
+  });
+}
+
+int rad_bsdf_sample_batch(const char* bsdf_json, const float* wi, const float* u, int64_t n, float* wo, float* pdf,
+                          float* f, float* eta, uint32_t* type) {
+  if (!bsdf_json || n < 0 || (n > 0 && (!wi || !u || !wo || !pdf || !f || !eta || !type)))
+    return Fail(RAD_ERR_INVALID_ARG, "bad argument");
+  return Guard([&] {
+    EnsureInit();
+    std::vector<MatRec> mats;
+    BuildMaterialRecords(JsonReader::Parse(bsdf_json), mats);
+    if (n == 0) return;
+    Lib& lib = L();
+    std::lock_guard<std::mutex> g(lib.gpuMu);
+    DevBuf<MatRec> dm(mats.size());
+    DevBuf<float> dwi(3 * n), du(3 * n), dwo(3 * n), dp(n), df(3 * n), de(n);
+    DevBuf<uint32_t> dt(n);
+    Check(cudaMemcpyAsync(dm.p, mats.data(), mats.size() * sizeof(MatRec), cudaMemcpyHostToDevice, lib.stream), "copy");
+    Check(cudaMemcpyAsync(dwi.p, wi, 12 * n, cudaMemcpyHostToDevice, lib.stream), "copy");
+    Check(cudaMemcpyAsync(du.p, u, 12 * n, cudaMemcpyHostToDevice, lib.stream), "copy");
+    Check(LaunchBsdfSample(dm.p, dwi.p, du.p, n, dwo.p, dp.p, df.p, de.p, dt.p, lib.stream), "bsdf sample");
+    Check(cudaMemcpyAsync(wo, dwo.p, 12 * n, cudaMemcpyDeviceToHost, lib.stream), "copy");
+    Check(cudaMemcpyAsync(pdf, dp.p, 4 * n, cudaMemcpyDeviceToHost, lib.stream), "copy");
+    Check(cudaMemcpyAsync(f, df.p, 12 * n, cudaMemcpyDeviceToHost, lib.stream), "copy");
+    Check(cudaMemcpyAsync(eta, de.p, 4 * n, cudaMemcpyDeviceToHost, lib.stream), "copy");
+    Check(cudaMemcpyAsync(type, dt.p, 4 * n, cudaMemcpyDeviceToHost, lib.stream), "copy");
+    Check(cudaStreamSynchronize(lib.stream), "sync");
+  });
+}
+
+int rad_camera_rays(rad_scene* scene, const uint32_t* pixels, int64_t n, uint32_t sample, uint32_t seed,
+                    float* rays) {
+  if (!scene || n < 0 || (n > 0 && (!pixels || !rays))) return Fail(RAD_ERR_INVALID_ARG, "bad argument");
+  if (n == 0) return RAD_OK;
+  uint64_t npix = (uint64_t)scene->info.width * scene->info.height;
+  for (int64_t i = 0; i < n; i++)
+    if (pixels[i] >= npix) return Fail(RAD_ERR_INVALID_ARG, "pixel index out of range");
+  return Guard([&] {
+    Lib& lib = L();
+    std::lock_guard<std::mutex> g(lib.gpuMu);
+    DevBuf<uint32_t> dp(n);
+    DevBuf<float> dr(8 * n);
+    Check(cudaMemcpyAsync(dp.p, pixels, 4 * n, cudaMemcpyHostToDevice, lib.stream), "copy");
+    Check(LaunchCameraRays(scene->dev, dp.p, n, sample, seed, dr.p, lib.stream), "camera");
+    Check(cudaMemcpyAsync(rays, dr.p, 32 * n, cudaMemcpyDeviceToHost, lib.stream), "copy");
+    Check(cudaStreamSynchronize(lib.stream), "sync");
+  });
+}
+
+int rad_render_samples(rad_scene* scene, const uint32_t* pixels, const uint32_t* samples, int64_t n, uint32_t seed,
+                       float* radiance) {
+  if (!scene || n < 0 || (n > 0 && (!pixels || !samples || !radiance))) return Fail(RAD_ERR_INVALID_ARG, "bad argument");
+  if (n == 0) return RAD_OK;
+  uint64_t npix = (uint64_t)scene->info.width * scene->info.height;
+  for (int64_t i = 0; i < n; i++)
+    if (pixels[i] >= npix) return Fail(RAD_ERR_INVALID_ARG, "pixel index out of range");
+  return Guard([&] {
+    Lib& lib = L();
+    std::lock_guard<std::mutex> g(lib.gpuMu);
+    DevBuf<uint32_t> dp(n), ds(n);
+    DevBuf<float> dout(3 * n);
+    Check(cudaMemcpyAsync(dp.p, pixels, 4 * n, cudaMemcpyHostToDevice, lib.stream), "copy");
+    Check(cudaMemcpyAsync(ds.p, samples, 4 * n, cudaMemcpyHostToDevice, lib.stream), "copy");
+    uint32_t zero = 0;
+    Check(cudaMemcpyAsync(lib.paths.counters + kMiscBase + 1, &zero, 4, cudaMemcpyHostToDevice, lib.stream), "copy");
+    for (int64_t b = 0; b < n; b += lib.maxPaths) {
+      uint32_t count = (uint32_t)std::min<int64_t>(lib.maxPaths, n - b);
+      WaveParams w{0, count, 0, seed, dp.p + b, ds.p + b};
+      ProfSink ps{nullptr};
+      Check(LaunchGenerate(scene->dev, lib.paths, w, lib.stream), "generate");
+      if (scene->dev.isVol) {
+        Check(LaunchVolPath(scene->dev, lib.paths, w, lib.paths.counters + kMiscBase + 1, lib.stream), "vol_path");
+      } else {
+        LaunchBounces(scene->dev, count, ps);
+      }
+      Check(LaunchGatherRadiance(lib.paths, count, dout.p + 3 * b, lib.stream), "gather");
+    }
+    Check(cudaMemcpyAsync(radiance, dout.p, 12 * n, cudaMemcpyDeviceToHost, lib.stream), "copy");
+    uint32_t err = 0;
+    Check(cudaMemcpyAsync(&err, lib.paths.counters + kMiscBase + 1, 4, cudaMemcpyDeviceToHost, lib.stream), "copy");
+    Check(cudaStreamSynchronize(lib.stream), "sync");
+    if (err) throw Error{RAD_ERR_DEVICE_CHECK, "device-side bound exceeded, code " + std::to_string(err)};
+  });
+}
+
+}  // extern "C"

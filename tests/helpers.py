@@ -1,0 +1,55 @@
+"""Shared test helpers: seeded scenes written to disk, direction batches."""
+import json
+import os
+
+import numpy as np
+
+from radiantiumplusplus_gb300 import scenes
+
+
+def write(dirpath, name, scene, assets=None):
+    d = os.path.join(str(dirpath), name)
+    path = scenes.write_scene(d, scene, assets)
+    with open(path) as fh:
+        return path, fh.read(), d
+
+
+def box(dirpath, w=64, h=64, spp=4, seed=1):
+    return write(dirpath, "box_%dx%d_%d_%d" % (w, h, spp, seed), scenes.box_room(w, h, spp, seed))
+
+
+def spheres(dirpath, n=300, emitters=5, w=96, h=64, spp=4):
+    sc, assets = scenes.many_spheres(n_spheres=n, n_emitters=emitters, width=w, height=h, spp=spp)
+    return write(dirpath, "spheres_%d_%dx%d" % (n, w, h), sc, assets)
+
+
+def volume(dirpath, w=48, h=48, spp=4, grid=32, max_depth=32):
+    sc, assets = scenes.volume_box(width=w, height=h, spp=spp, grid=grid, max_depth=max_depth)
+    return write(dirpath, "vol_%dx%d_%d" % (w, h, grid), sc, assets)
+
+
+def directions(rng, n):
+    d = rng.normal(size=(n, 3))
+    d /= np.linalg.norm(d, axis=1, keepdims=True)
+    return d.astype(np.float32)
+
+
+BSDFS = [
+    {"type": "diffuse", "reflectance": [0.3, 0.6, 0.9]},
+    {"type": "rough_metal", "alpha": 0.2},
+    {"type": "rough_metal", "alpha_u": 0.08, "alpha_v": 0.4},
+    {"type": "rough_metal", "alpha": 0.3, "distribution": "beckmann"},
+    {"type": "rough_metal", "alpha": 0.25, "sample_visible": False},
+    {"type": "rough_glass", "int_ior": 1.5, "ext_ior": 1.0, "alpha": 0.15},
+    {"type": "rough_glass", "int_ior": 1.33, "ext_ior": 1.0, "alpha": 0.05},
+    {"type": "disney", "base_color": [0.8, 0.3, 0.2], "roughness": 0.4, "metallic": 0.3, "spec_trans": 0.4,
+     "clearcoat": 0.7, "clearcoat_gloss": 0.5, "sheen": 0.6, "sheen_tint": 0.3, "spec_tint": 0.5,
+     "flatness": 0.3, "anisotropic": 0.4},
+    {"type": "disney", "base_color": [0.5, 0.5, 0.5], "roughness": 0.7},
+    {"type": "disney", "base_color": [0.9, 0.8, 0.1], "roughness": 0.2, "metallic": 1.0, "specular": 0.8},
+    {"type": "two_side", "two_side": {"type": "rough_metal", "alpha": 0.3}},
+]
+
+
+def bsdf_json(b):
+    return json.dumps(b)

@@ -1,0 +1,70 @@
+"""Serving loop: jobs of different scenes submitted together are admitted,
+interleaved on the device, and each result is identical to rendering it alone."""
+import time
+
+import numpy as np
+import pytest
+
+from helpers import box, spheres
+
+pytestmark = pytest.mark.gpu
+
+
+def test_mix_equals_alone(rad, scene_dir):
+    a = rad.Scene.from_file(box(scene_dir, 40, 40, 6)[0])
+    b = rad.Scene.from_file(spheres(scene_dir, 300, 4, 48, 32, 5)[0])
+    c = rad.Scene.from_file(box(scene_dir, 24, 56, 3, seed=9)[0])
+    alone = [s.render() for s in (a, b, c)]
+    jobs = [s.submit() for s in (a, b, c, a)]
+    for j in jobs:
+        j.wait()
+    mixed = [j.film() for j in jobs]
+    for k, ref in enumerate(alone + [alone[0]]):
+        assert np.array_equal(mixed[k], ref)
+    st = jobs[0].stats()
+    assert st["samples"] == 40 * 40 * 6
+    assert st["rays_closest"] >= st["samples"]
+    for j in jobs:
+        j.close()
+    for s in (a, b, c):
+        s.close()
+
+
+def test_progress_and_cancel(rad, scene_dir):
+    s = rad.Scene.from_file(box(scene_dir, 64, 64, 4)[0])
+    j = s.submit(spp=4000)
+    time.sleep(0.05)
+    j.cancel()
+    with pytest.raises(rad.RadError) as e:
+        j.wait()
+    assert e.value.code == 9  # RAD_ERR_CANCELLED
+    done, total = j.progress()
+    assert total == 64 * 64 * 4000 and done <= total
+    j.close()
+    j2 = s.submit(spp=2)
+    j2.wait()
+    assert j2.progress() == (64 * 64 * 2, 64 * 64 * 2)
+    j2.close()
+    s.close()
+
+
+def test_resume_disjoint_samples(rad, scene_dir):
+    """Two halves with disjoint sample indices sum to the full render (resumable accumulation)."""
+    s = rad.Scene.from_file(box(scene_dir, 32, 32, 8)[0])
+    full = s.render(spp=8)
+    h1 = s.render(spp=4, first_sample=0)
+    h2 = s.render(spp=4, first_sample=4)
+    assert np.allclose((h1 + h2) * 0.5, full, rtol=1e-5, atol=1e-6)
+    s.close()
+
+
+def test_errors_are_status_codes(rad, scene_dir):
+    with pytest.raises(rad.RadError) as e:
+        rad.Scene.from_json('{"camera": ')
+    assert e.value.code == 2  # RAD_ERR_JSON
+    with pytest.raises(rad.RadError) as e:
+        rad.Scene.from_json({"camera": {"type": "orthographic"}, "scene": [], "renderer": {"type": "path"}})
+    assert e.value.code == 3  # RAD_ERR_UNKNOWN_FACTORY
+    with pytest.raises(rad.RadError) as e:
+        rad.bsdf_eval({"type": "plastic_x"}, np.zeros((1, 3)), np.zeros((1, 3)))
+    assert e.value.code == 3

@@ -1,0 +1,103 @@
+"""Integrator parity: the wavefront `path` kernels and the `vol_path` kernel vs
+the CPU oracle, sample by sample on identical PCG streams, plus film-level
+checks (job film, z-test of the mean against a high-spp oracle reference).
+
+Per-sample tolerance: the GPU uses CUDA's sinf/cosf/logf/expf/powf while the
+oracle uses glibc's, so a path can diverge when a Russian-roulette or lobe
+decision sits on a 1-ulp boundary. Required: >= 97% of samples within 1e-3
+relative (absolute floor 1e-4), and the mean over all samples within 2%.
+"""
+import numpy as np
+import pytest
+
+from helpers import box, spheres, volume
+
+pytestmark = pytest.mark.gpu
+
+
+def _sample_parity(g, o, spp, min_frac=0.97):
+    W, H = g.width, g.height
+    pix = np.repeat(np.arange(W * H, dtype=np.uint32), spp)
+    smp = np.tile(np.arange(spp, dtype=np.uint32), W * H)
+    lg = g.render_samples(pix, smp)
+    lo = o.render_samples(pix, smp)
+    tol = 1e-3 * np.maximum(np.abs(lo), 1e-1)
+    close = (np.abs(lg - lo) <= tol).all(axis=1)
+    frac = close.mean()
+    mg, mo = lg.mean(0), lo.mean(0)
+    assert frac >= min_frac, "only %.4f of samples agree" % frac
+    assert np.all(np.abs(mg - mo) <= 0.02 * np.abs(mo) + 1e-6), (mg, mo)
+    return frac, lg, lo
+
+
+def test_path_samples_box(rad, oracle, scene_dir):
+    path, text, d = box(scene_dir, 48, 48, 4)
+    g, o = rad.Scene.from_file(path), oracle.OracleScene(text, d)
+    frac, _, _ = _sample_parity(g, o, 4, 0.98)
+    g.close()
+
+
+def test_path_samples_spheres(rad, oracle, scene_dir):
+    path, text, d = spheres(scene_dir, 400, 6, 64, 48)
+    g, o = rad.Scene.from_file(path), oracle.OracleScene(text, d)
+    _sample_parity(g, o, 2, 0.95)
+    g.close()
+
+
+def test_volpath_samples(rad, oracle, scene_dir):
+    path, text, d = volume(scene_dir, 32, 32, 2, grid=24)
+    g, o = rad.Scene.from_file(path), oracle.OracleScene(text, d)
+    _sample_parity(g, o, 2, 0.93)
+    g.close()
+
+
+def test_job_film_matches_samples(rad, scene_dir):
+    """The job film is the per-pixel mean of the same samples (sum in sample order, x 1/spp)."""
+    path, text, d = box(scene_dir, 32, 32, 4)
+    g = rad.Scene.from_file(path)
+    film = g.render()
+    W, H = 32, 32
+    pix = np.repeat(np.arange(W * H, dtype=np.uint32), 4)
+    smp = np.tile(np.arange(4, dtype=np.uint32), W * H)
+    L = g.render_samples(pix, smp).reshape(H * W, 4, 3)
+    acc = np.zeros((H * W, 3), np.float32)
+    for s in range(4):
+        li = L[:, s]
+        bad = np.isnan(li).any(1) | np.isinf(li[:, 0]) | (li[:, 0] < 0)
+        acc = acc + np.where(bad[:, None], 0, li).astype(np.float32)
+    ref = (acc * np.float32(1.0 / 4)).reshape(H, W, 3)
+    assert np.array_equal(film, ref)
+    g.close()
+
+
+def test_job_film_vs_oracle(rad, oracle, scene_dir):
+    path, text, d = box(scene_dir, 48, 48, 8)
+    g, o = rad.Scene.from_file(path), oracle.OracleScene(text, d)
+    fg = g.render()
+    fo, _ = o.render()
+    rel = np.abs(fg - fo) / np.maximum(np.abs(fo), 1e-2)
+    assert (rel.max(axis=2) < 1e-3).mean() > 0.95
+    assert abs(fg.mean() - fo.mean()) < 1e-3 * fo.mean()
+    g.close()
+
+
+def test_ztest_against_oracle_reference(rad, oracle, scene_dir):
+    """Per-pixel z-test of the 64-spp GPU mean against a high-spp oracle mean."""
+    W = H = 24
+    path, text, d = box(scene_dir, W, H, 64, seed=5)
+    g = rad.Scene.from_file(path)
+    ref_path, ref_text, ref_d = box(scene_dir, W, H, 2048, seed=99)
+    o = oracle.OracleScene(ref_text, ref_d)
+    ref, _ = o.render()
+    pix = np.repeat(np.arange(W * H, dtype=np.uint32), 64)
+    smp = np.tile(np.arange(64, dtype=np.uint32), W * H)
+    L = g.render_samples(pix, smp).reshape(H, W, 64, 3).astype(np.float64)
+    mean = L.mean(2)
+    var = L.var(2, ddof=1)
+    se = np.sqrt(var / 64 + var / 2048) + 1e-6
+    z = np.abs(mean - ref) / se
+    frac = (z > 4).mean()
+    assert frac < 0.02, "z-test failed on %.3f of pixel channels" % frac
+    rel_mse = np.mean((mean - ref) ** 2 / (ref ** 2 + 1e-2))
+    assert rel_mse < 0.05
+    g.close()
