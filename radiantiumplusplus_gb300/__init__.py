@@ -38,10 +38,18 @@ def lib():
     return _capi.load()
 
 
+_atexit_registered = False
+
+
 def init(config=None):
     """rad_init: select the device and set the admission budget (bytes)."""
+    global _atexit_registered
     cfg = json.dumps(config) if isinstance(config, dict) else config
     check(lib().rad_init(cfg.encode() if cfg else None))
+    if not _atexit_registered:
+        import atexit
+        atexit.register(lambda: lib().rad_shutdown())
+        _atexit_registered = True
 
 
 def shutdown():

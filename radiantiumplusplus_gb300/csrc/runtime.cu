@@ -149,9 +149,12 @@ struct Lib {
   std::vector<cudaEvent_t> evPool;
 };
 
+// Never destroyed: at process exit the worker thread may still be parked on
+// `qcv`, and destroying a condition variable with a waiter blocks forever.
+// rad_shutdown() is the orderly teardown (the Python package calls it atexit).
 Lib& L() {
-  static Lib lib;
-  return lib;
+  static Lib* lib = new Lib();
+  return *lib;
 }
 std::mutex g_initMu;
 
