@@ -153,6 +153,20 @@ RAD_API int rad_camera_rays(rad_scene* scene, const uint32_t* pixels, int64_t n,
 RAD_API int rad_render_samples(rad_scene* scene, const uint32_t* pixels, const uint32_t* samples, int64_t n,
                                uint32_t seed, float* radiance);
 
+/* ---- allocation-free variant --------------------------------------------- */
+/* No counterpart in the reference. Same result as rad_render_samples, for
+ * callers that cannot call cudaMalloc (a host whose device memory is all
+ * handed to its own pool, or a frame loop that must not let allocations
+ * synchronise the device): d_pixels, d_samples (n each) and d_radiance (n x 3)
+ * are device pointers the caller owns, and the path state lives in a fixed
+ * file-scope device array, so this call allocates nothing. n may be at most
+ * 16384 (RAD_ERR_INVALID_ARG beyond). Work runs on `stream` (a cudaStream_t,
+ * NULL = default stream) and the call returns when it has finished. The first
+ * call on a device looks up the array's address; make it before any stream
+ * capture. Every call shares the one array: calls that overlap on the GPU race. */
+RAD_API int rad_render_samples_noalloc(rad_scene* scene, const uint32_t* d_pixels, const uint32_t* d_samples,
+                                       int64_t n, uint32_t seed, float* d_radiance, void* stream);
+
 #ifdef __cplusplus
 }
 #endif

@@ -38,6 +38,7 @@ EXPORTS = [
     "rad_scene_footprint", "rad_job_submit", "rad_job_wait", "rad_job_cancel", "rad_job_progress",
     "rad_job_film", "rad_job_stats", "rad_job_destroy", "rad_trace_batch", "rad_trace_batch_device",
     "rad_bsdf_eval_batch", "rad_bsdf_sample_batch", "rad_camera_rays", "rad_render_samples",
+    "rad_render_samples_noalloc",
 ]
 
 
@@ -110,6 +111,7 @@ def load(path=LIB_PATH):
         "rad_bsdf_sample_batch": [ctypes.c_char_p, P, P, I64, P, P, P, P, P],
         "rad_camera_rays": [P, P, I64, ctypes.c_uint32, ctypes.c_uint32, P],
         "rad_render_samples": [P, P, P, I64, ctypes.c_uint32, P],
+        "rad_render_samples_noalloc": [P, P, P, I64, ctypes.c_uint32, P, P],
     }
     for name, args in sig.items():
         fn = getattr(L, name)

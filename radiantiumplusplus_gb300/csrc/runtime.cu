@@ -577,6 +577,13 @@ struct DevBuf {
 
 }  // namespace
 
+namespace rad {
+// Accessors for other translation units of the C ABI.
+const DevScene* SceneDevice(const rad_scene* scene) { return &scene->dev; }
+int SceneDeviceIndex() { return L().device; }
+int ReportError(int code, const char* msg) { return Fail(code, msg); }
+}  // namespace rad
+
 // ============================================================================
 extern "C" {
 
