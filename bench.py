@@ -211,13 +211,18 @@ def run_ours(args, world, rank, local):
         barrier(world)
         torch.cuda.synchronize()
         clocks.start()
-        job = scene.submit(spp=args.steps * spp_step, first_sample=0, profile=True)
+        job = scene.submit(spp=args.steps * spp_step, first_sample=0)
         job.wait()
         torch.cuda.synchronize()
         barrier(world)
         clk = clocks.stop()
         st = job.stats()
         job.close()
+        # per-kernel breakdown (events around every launch, so no graph replay): 2 extra samples, not timed
+        pj = scene.submit(spp=2, first_sample=40_000, profile=True)
+        pj.wait()
+        pst = pj.stats()
+        pj.close()
         gpu_s = allreduce_max(world, st["gpu_ms"] / 1000.0)
         samples = st["samples"] * world
         value = samples / gpu_s
@@ -238,13 +243,13 @@ def run_ours(args, world, rank, local):
         barrier(world)
         e2e_value = args.steps * W * H * spp_step * world / e2e_s
         # ---- roofline for the dominant kernel
-        kern = {"extend": st["ms_extend"], "shade": st["ms_shade"], "shadow": st["ms_shadow"],
-                "generate": st["ms_generate"], "accumulate": st["ms_accumulate"]}
+        kern = {"extend": pst["ms_extend"], "shade": pst["ms_shade"], "shadow": pst["ms_shadow"],
+                "generate": pst["ms_generate"], "accumulate": pst["ms_accumulate"]}
         dominant = max(kern, key=kern.get)
-        n_ext = max(1, st["n_extend"])
-        ext_bytes = st["rays_closest"] * (BYTES_QUEUE + BYTES_RAY + BYTES_HIT + nodes_per_ray * BYTES_NODE
-                                          + prims_per_ray * BYTES_PRIM)
-        ext_launch_ms = st["ms_extend"] / n_ext
+        n_ext = max(1, pst["n_extend"])
+        ext_bytes = pst["rays_closest"] * (BYTES_QUEUE + BYTES_RAY + BYTES_HIT + nodes_per_ray * BYTES_NODE
+                                           + prims_per_ray * BYTES_PRIM)
+        ext_launch_ms = pst["ms_extend"] / n_ext
         achieved = (ext_bytes / n_ext) / (ext_launch_ms / 1000.0) / 1e9 if ext_launch_ms > 0 else 0.0
         cpu = None
         if rank == 0 and world == 1 and not args.no_cpu:
@@ -263,7 +268,7 @@ def run_ours(args, world, rank, local):
         "mrays_per_s": mrays,
         "rays_per_sample": (st["rays_closest"] + st["rays_shadow"]) / max(1, st["samples"]),
         "gpu_launches": st["kernel_launches"],
-        "kernel_ms": {k: round(v, 3) for k, v in kern.items()},
+        "kernel_ms_profiled_2spp": {k: round(v, 3) for k, v in kern.items()},
         "roofline": {"bound": "hbm", "kernel": "extend (BVH8 closest hit)", "achieved": achieved, "peak": hbm_peak,
                      "unit": "GB/s", "frac": achieved / hbm_peak, "traffic": None,
                      "peak_source": peak_src, "dominant_kernel_by_time": dominant,
@@ -280,6 +285,125 @@ def run_ours(args, world, rank, local):
         print(json.dumps(line), flush=True)
 
 
+def run_volume(args, world, rank, local):
+    """Volumetric scene (vol_path): fBm density grid in a rough-dielectric box, 1024x1024, depth 32."""
+    import torch
+    import radiantiumplusplus_gb300 as rad
+    from radiantiumplusplus_gb300 import scenes
+    torch.cuda.set_device(local)
+    rad.init({"device": local})
+    res = args.vol_res
+    with tempfile.TemporaryDirectory(prefix="rad_bench_vol_") as tmp:
+        sc, assets = scenes.volume_box(width=res, height=res, spp=1, max_depth=32, grid=args.vol_grid)
+        path = scenes.write_scene(tmp, sc, assets)
+        scene = rad.Scene.from_file(path)
+        j = scene.submit(spp=args.warmup, first_sample=20_000)
+        j.wait()
+        j.close()
+        clocks = ClockSampler(local)
+        torch.cuda.synchronize()
+        clocks.start()
+        job = scene.submit(spp=args.steps, profile=True)
+        job.wait()
+        torch.cuda.synchronize()
+        clk = clocks.stop()
+        st = job.stats()
+        job.close()
+        value = st["samples"] / (st["gpu_ms"] / 1000.0)
+        cpu = None
+        if rank == 0 and not args.no_cpu:
+            sys.path.insert(0, os.path.join(ROOT, "tests"))
+            import oracle_lib
+            o = oracle_lib.OracleScene.from_file(path)
+            t0 = time.perf_counter()
+            _, cs = o.render(rows=(0, res, 16), samples=(0, 1), threads=os.cpu_count() or 1)
+            dt = time.perf_counter() - t0
+            cpu = {"value": int(cs[2]) / dt, "unit": "samples/s", "cores": os.cpu_count(), "kind": "port",
+                   "sample": "every 16th row of the %dx%d volume frame at 1 spp (%d samples, %.1f s)"
+                             % (res, res, int(cs[2]), dt)}
+        scene.close()
+    line = {"metric": "samples/s (vol_path, fBm volume %dx%d, depth 32)" % (res, res), "value": value,
+            "unit": "samples/s", "n_gpus": 1, "steps": args.steps, "warmup": args.warmup,
+            "ms_per_step": st["gpu_ms"] / args.steps, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded fBm grid)",
+            "config": {"workload": "volume_box", "width": res, "height": res, "grid": args.vol_grid,
+                       "max_depth": 32, "rr_depth": 5, "sigma_t_scale": 20, "albedo": 0.9, "hg_g": 0.6},
+            "mrays_per_s": (st["rays_closest"] + st["rays_shadow"]) / (st["gpu_ms"] / 1000.0) / 1e6,
+            "gpu_launches": st["kernel_launches"], "kernel_ms": {"vol_path": st["ms_volpath"]}, "clocks": clk}
+    if cpu:
+        line["cpu_baseline"] = cpu
+    print(json.dumps(line), flush=True)
+
+
+def run_serving(args, world, rank, local):
+    """Serving loop: Poisson arrivals of jobs over a pool of resident scenes; throughput and p50/p99 latency."""
+    import numpy as np
+    import torch
+    import radiantiumplusplus_gb300 as rad
+    from radiantiumplusplus_gb300 import scenes
+    torch.cuda.set_device(local)
+    rad.init({"device": local})
+    rng = np.random.default_rng(4)
+    pool = [(30, 256, 256, 8), (100, 512, 512, 10), (300, 1280, 720, 12), (1000, 256, 256, 14),
+            (3000, 512, 512, 16), (10000, 1920, 1080, 16)]
+    with tempfile.TemporaryDirectory(prefix="rad_bench_srv_") as tmp:
+        loaded = []
+        for k, (n, w, h, depth) in enumerate(pool):
+            sc, assets = scenes.many_spheres(n_spheres=n, n_emitters=8, width=w, height=h, spp=1, max_depth=depth,
+                                             seed=40 + k, extent=100.0 * (n / 10000.0) ** (1 / 3))
+            path = scenes.write_scene(os.path.join(tmp, "s%d" % k), sc, assets)
+            loaded.append(rad.Scene.from_file(path))
+        # service rate of each scene alone (samples/s) from one 2-spp job
+        alone = []
+        for sc in loaded:
+            j = sc.submit(spp=2)
+            j.wait()
+            st = j.stats()
+            j.close()
+            alone.append(st["samples"] / max(1e-6, st["gpu_ms"] / 1000.0))
+        results = []
+        for lam in args.rates:
+            n_jobs = max(4, int(lam * args.duration))
+            arrivals = np.cumsum(rng.exponential(1.0 / lam, n_jobs))
+            picks = rng.integers(0, len(loaded), n_jobs)
+            spps = np.exp(rng.uniform(np.log(args.spp_min), np.log(args.spp_max), n_jobs)).astype(int)
+            jobs = []
+            t0 = time.perf_counter()
+            for a, k, spp in zip(arrivals, picks, spps):
+                delay = t0 + a - time.perf_counter()
+                if delay > 0:
+                    time.sleep(delay)
+                jobs.append((loaded[k].submit(spp=int(spp)), k, int(spp)))
+            lat, stretch, samples = [], [], 0
+            for j, k, spp in jobs:
+                j.wait()
+                st = j.stats()
+                l_ms = st["queue_ms"] + st["wall_ms"]
+                lat.append(l_ms)
+                samples += st["samples"]
+                stretch.append(l_ms / (1000.0 * st["samples"] / alone[k]))
+                j.close()
+            makespan = time.perf_counter() - t0
+            lat = np.array(lat)
+            results.append({"rate_jobs_per_s": lam, "jobs": n_jobs, "throughput_samples_per_s": samples / makespan,
+                            "p50_ms": float(np.percentile(lat, 50)), "p99_ms": float(np.percentile(lat, 99)),
+                            "p99_over_p50": float(np.percentile(lat, 99) / np.percentile(lat, 50)),
+                            "stretch_p50": float(np.percentile(stretch, 50)),
+                            "stretch_p99": float(np.percentile(stretch, 99))})
+        for sc in loaded:
+            sc.close()
+    peak = max(r["throughput_samples_per_s"] for r in results)
+    line = {"metric": "serving: throughput and p50/p99 job latency (Poisson arrivals)", "value": peak,
+            "unit": "samples/s", "n_gpus": 1, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+            "dtype": "f32", "data": "synthetic (seeded many-spheres generator)",
+            "config": {"workload": "serving_mix", "scenes": [{"spheres": n, "triangles": 320 * n, "width": w,
+                                                              "height": h, "max_depth": d} for n, w, h, d in pool],
+                       "spp": "log-uniform [%d, %d]" % (args.spp_min, args.spp_max),
+                       "arrival_window_s": args.duration},
+            "alone_samples_per_s": alone, "sweep": results}
+    print(json.dumps(line), flush=True)
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -288,10 +412,21 @@ def main():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline leg")
     ap.add_argument("--cpu-row-step", type=int, default=4)
+    ap.add_argument("--workload", default="many_spheres", choices=["many_spheres", "volume", "serving"])
+    ap.add_argument("--vol-res", type=int, default=1024)
+    ap.add_argument("--vol-grid", type=int, default=256)
+    ap.add_argument("--rates", type=float, nargs="+", default=[1, 2, 5, 10, 20])
+    ap.add_argument("--duration", type=float, default=10.0, help="serving: arrival window per rate (s)")
+    ap.add_argument("--spp-min", type=int, default=4)
+    ap.add_argument("--spp-max", type=int, default=64)
     args = ap.parse_args()
     world, rank, local = dist_setup()
     if args.impl == "reference":
         run_reference(args, world, rank)
+    elif args.workload == "volume":
+        run_volume(args, world, rank, local)
+    elif args.workload == "serving":
+        run_serving(args, world, rank, local)
     else:
         run_ours(args, world, rank, local)
     if world > 1:

@@ -500,3 +500,53 @@ RD BsdfSampleRes BsdfSample(const MatRec* mats, uint32_t mi, V3 wi, float lobeXi
 }
 
 }  // namespace rad
+
+namespace rad {
+
+// Class-specialised dispatch for the material-sorted shade kernels: the leaf
+// kind K is known at compile time, so each kernel carries one BSDF's code.
+// A two-sided wrapper resolves to its outside / inside leaf as two_side.cpp does.
+template <int K>
+RD void LeafEvalPdfK(const MatRec& m, V3 wi, V3 wo, V3& f, float& pdf) {
+  if constexpr (K == MAT_DIFFUSE) DiffuseEvalPdf(m, wi, wo, f, pdf);
+  else if constexpr (K == MAT_ROUGH_METAL) MetalEvalPdf(m, wi, wo, f, pdf);
+  else if constexpr (K == MAT_ROUGH_GLASS) GlassEvalPdf(m, wi, wo, f, pdf);
+  else if constexpr (K == MAT_DISNEY) DisneyEvalPdf(m, wi, wo, f, pdf);
+  else LeafEvalPdf(m, wi, wo, f, pdf);
+}
+template <int K>
+RD BsdfSampleRes LeafSampleK(const MatRec& m, V3 wi, float lobeXi, V2 dirXi) {
+  if constexpr (K == MAT_DIFFUSE) return DiffuseSample(m, wi, dirXi);
+  else if constexpr (K == MAT_ROUGH_METAL) return MetalSample(m, wi, dirXi);
+  else if constexpr (K == MAT_ROUGH_GLASS) return GlassSample(m, wi, lobeXi, dirXi);
+  else if constexpr (K == MAT_DISNEY) return DisneySample(m, wi, lobeXi, dirXi);
+  else return LeafSample(m, wi, lobeXi, dirXi);
+}
+template <int K>
+RD void ClassEvalPdf(const MatRec* mats, uint32_t mi, V3 wi, V3 wo, V3& f, float& pdf) {
+  const MatRec& m = mats[mi];
+  if (m.kind != MAT_TWO_SIDE) {
+    LeafEvalPdfK<K>(m, wi, wo, f, pdf);
+  } else if (wi.z > 0.f) {
+    LeafEvalPdfK<K>(mats[m.ref0], wi, wo, f, pdf);
+  } else if (wi.z < 0.f) {
+    LeafEvalPdfK<K>(mats[m.ref1], V3{wi.x, wi.y, -wi.z}, V3{wo.x, wo.y, -wo.z}, f, pdf);
+  } else {
+    f = v3s(0.f);
+    pdf = 0.f;
+  }
+}
+template <int K>
+RD BsdfSampleRes ClassSample(const MatRec* mats, uint32_t mi, V3 wi, float lobeXi, V2 dirXi) {
+  const MatRec& m = mats[mi];
+  if (m.kind != MAT_TWO_SIDE) return LeafSampleK<K>(m, wi, lobeXi, dirXi);
+  if (wi.z > 0.f) return LeafSampleK<K>(mats[m.ref0], wi, lobeXi, dirXi);
+  if (wi.z < 0.f) {
+    BsdfSampleRes r = LeafSampleK<K>(mats[m.ref1], V3{wi.x, wi.y, -wi.z}, lobeXi, dirXi);
+    r.wo.z *= -1.f;
+    return r;
+  }
+  return BsdfSampleRes{};
+}
+
+}  // namespace rad

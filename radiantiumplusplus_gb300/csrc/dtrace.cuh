@@ -177,6 +177,15 @@ RD bool TestPrim(const DevScene& S, const RayPre& r, uint32_t lp, bool analytic,
 }
 
 RD uint32_t ByteOf(uint32_t w, uint32_t i) { return (w >> (8u * i)) & 0xffu; }
+// Byte i of w as a float, exactly: the byte becomes the low mantissa bits of
+// 2^23 (one byte permute), and 2^23 is subtracted (one add) -- no conversion unit.
+#if defined(RAD_HOST_EMULATION)
+RD float ByteAsFloat(uint32_t w, uint32_t i) { return (float)ByteOf(w, i); }
+#else
+RD float ByteAsFloat(uint32_t w, uint32_t i) {
+  return __uint_as_float(__byte_perm(w, 0x4B000000u, 0x7440u | i)) - 8388608.0f;
+}
+#endif
 
 // Closest hit (ANY = false) or occlusion (ANY = true). Returns false and sets
 // *err if the traversal stack would overflow (never silently truncates).
@@ -223,12 +232,12 @@ RD bool TraceBvh8(const DevScene& S, const RayPre& r, float tmax, TraceHit& h, u
       uint32_t meta = ByteOf(s < 4 ? q1.z : q1.w, i);
       bool internal = (imask >> s) & 1u;
       if (!internal && meta == 0u) continue;
-      float tnx = fmaf((float)ByteOf(w ? nx1 : nx0, i), ax, bx);
-      float tfx = fmaf((float)ByteOf(w ? fx1 : fx0, i), ax, bx);
-      float tny = fmaf((float)ByteOf(w ? ny1 : ny0, i), ay, by);
-      float tfy = fmaf((float)ByteOf(w ? fy1 : fy0, i), ay, by);
-      float tnz = fmaf((float)ByteOf(w ? nz1 : nz0, i), az, bz);
-      float tfz = fmaf((float)ByteOf(w ? fz1 : fz0, i), az, bz);
+      float tnx = fmaf(ByteAsFloat(w ? nx1 : nx0, i), ax, bx);
+      float tfx = fmaf(ByteAsFloat(w ? fx1 : fx0, i), ax, bx);
+      float tny = fmaf(ByteAsFloat(w ? ny1 : ny0, i), ay, by);
+      float tfy = fmaf(ByteAsFloat(w ? fy1 : fy0, i), ay, by);
+      float tnz = fmaf(ByteAsFloat(w ? nz1 : nz0, i), az, bz);
+      float tfz = fmaf(ByteAsFloat(w ? fz1 : fz0, i), az, bz);
       float tn = fmaxf(fmaxf(tnx, tny), fmaxf(tnz, r.tmin));
       float tf = fminf(fminf(tfx, tfy), fminf(tfz, tcur)) * 1.00000024f;
       if (tn <= tf) {

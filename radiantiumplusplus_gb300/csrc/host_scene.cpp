@@ -936,6 +936,19 @@ void BuildHostScene(const std::string& json, const std::string& baseDir, HostSce
     off += sh.primCount;
   }
   hs.nPrims = off;
+  for (const auto& sh : hs.shapes) {
+    uint8_t cls = SC_EMIT;
+    if (sh.light < 0 && sh.bsdf >= 0) {
+      const MatRec& m = hs.mats[sh.bsdf];
+      uint32_t kind = m.kind;
+      if (kind == MAT_TWO_SIDE) {
+        uint32_t a = hs.mats[m.ref0].kind, b = hs.mats[m.ref1].kind;
+        kind = (a == b && a != MAT_TWO_SIDE) ? a : MAT_NONE;
+      }
+      cls = (kind >= MAT_DIFFUSE && kind <= MAT_DISNEY) ? (uint8_t)kind : (uint8_t)SC_GENERIC;
+    }
+    hs.shapeClass.push_back(cls);
+  }
   BuildBvh8(hs);
   // scene.cpp:11-36 and skybox.cpp:139-144
   hs.lightPdf = 1.f / float(hs.lights.size());

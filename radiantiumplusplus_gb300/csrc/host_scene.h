@@ -43,6 +43,7 @@ struct HostScene {
   std::vector<float> cdf;
   std::vector<float> rectToObject;  // per rect shape: 12 floats (world -> object rows)
   std::vector<uint32_t> rectIndexOfShape;
+  std::vector<uint8_t> shapeClass;  // see records.h SC_*
   int envLight = -1, globalMedium = -1;
   float lightPdf = 0.f;
   uint64_t nPrims = 0;

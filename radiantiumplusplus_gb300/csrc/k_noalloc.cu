@@ -36,10 +36,11 @@ struct NoAllocScratch {
   uint32_t pixel[kNoAllocMaxSamples];
   uint32_t q0[kNoAllocMaxSamples];
   uint32_t q1[kNoAllocMaxSamples];
+  uint32_t classQ[kShadeClasses * kNoAllocMaxSamples];
   uint32_t counters[kCounterWords];
 };
 
-// About 3 MB per device (180 bytes of path state per sample).
+// About 3.4 MB per device (204 bytes of path state per sample).
 static __device__ __align__(256) NoAllocScratch g_noallocScratch;
 
 namespace {
@@ -63,6 +64,7 @@ PathBuffers ScratchBuffers(NoAllocScratch* s) {
   B.shO = s->shO;
   B.shD = s->shD;
   B.shC = s->shC;
+  B.classQ = s->classQ;
   B.counters = s->counters;
   B.capacity = kNoAllocMaxSamples;
   return B;

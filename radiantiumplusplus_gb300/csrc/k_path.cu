@@ -2,9 +2,11 @@
 // split into stages over per-bounce path queues:
 //   generate   -- camera ray per pixel sample (perspective.cpp:73-82), PCG stream
 //   extend     -- closest hit for every queued path (BVH8, embree.cpp:87-111)
-//   shade      -- emitter MIS, NEE light sample + BSDF eval/pdf (emits a shadow
-//                 record), BSDF sample, Russian roulette, next ray; survivors are
-//                 appended to the next queue with warp-aggregated atomics
+//   shade      -- one kernel per shade class (the extend stage sorts hits into
+//                 per-class queues): emitter MIS, NEE light sample + BSDF
+//                 eval/pdf (emits a shadow record), BSDF sample, Russian
+//                 roulette, next ray; survivors are appended to the next queue
+//                 with warp-aggregated atomics
 //   shadow     -- occlusion of the NEE rays (scene.cpp:53-63); unoccluded
 //                 contributions are added to the path's radiance
 //   accumulate -- film += radiance with the reference's invalid-sample drop
@@ -52,18 +54,16 @@ __device__ __forceinline__ uint32_t WarpAppend(uint32_t* counter, bool pred) {
 
 __global__ void __launch_bounds__(kBlock) KGenerate(DevScene S, PathBuffers B, WaveParams w) {
   uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
-  if (i == 0) {
-    for (int k = 0; k < kMiscBase; k++) B.counters[k] = 0u;
-    B.counters[kMiscBase] = 0u;
-    B.counters[kMiscBase + 2] = 0u;
-    B.counters[kMiscBase + 3] = 0u;
-    B.counters[0] = w.count;
+  // reset this wave's counters (all but the sticky device-error word)
+  for (uint32_t k = i; k < (uint32_t)kCounterWords; k += gridDim.x * blockDim.x) {
+    if (k != (uint32_t)(kMiscBase + 1)) B.counters[k] = k == 0 ? w.count : 0u;
   }
   if (i >= w.count) return;
   uint32_t pix = w.pixelList ? w.pixelList[i] : w.pixelBegin + i;
-  uint32_t smp = w.sampleList ? w.sampleList[i] : w.sample;
+  uint32_t smp = w.sampleList ? w.sampleList[i] : (w.ctx ? w.ctx->sample : w.sample);
+  uint32_t seed = w.ctx ? w.ctx->seed : w.seed;
   uint32_t x = pix % (uint32_t)S.cam.width, y = pix / (uint32_t)S.cam.width;
-  Pcg32 rng = PcgForSample(pix, smp, w.seed);
+  Pcg32 rng = PcgForSample(pix, smp, seed);
   float jx = Next1D(rng);
   float jy = Next1D(rng);
   V3 O, D;
@@ -92,38 +92,61 @@ __device__ __forceinline__ void FlushTravCounts(unsigned long long* out, uint32_
 }
 
 template <bool COUNT>
-__global__ void __launch_bounds__(kBlock) KExtend(DevScene S, PathBuffers B, int depth, unsigned long long* trav) {
+__global__ void __launch_bounds__(kBlock, 8) KExtend(DevScene S, PathBuffers B, int depth, unsigned long long* trav) {
   uint32_t count = B.counters[depth];
   const uint32_t* qin = B.q[depth & 1];
   uint32_t* err = B.counters + kMiscBase + 1;
+  uint32_t* classCnt = B.counters + kClassBase + depth * kShadeClasses;
+  bool lastDepth = S.maxDepth >= 0 && depth + 1 >= S.maxDepth;
   uint32_t nN = 0, nP = 0;
-  for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < count; i += gridDim.x * blockDim.x) {
-    uint32_t p = qin[i];
-    float4 o = B.rayO[p], d = B.rayD[p];
-    RayPre r = MakeRayPre(V3{o.x, o.y, o.z}, V3{d.x, d.y, d.z}, o.w);
-    TraceHit h;
-    TraceBvh8<false, COUNT>(S, r, d.w, h, err, &nN, &nP);
-    HitRec hr;
-    hr.t = h.t;
-    hr.u = h.u;
-    hr.v = h.v;
-    hr.prim = h.prim;
-    hr.shape = h.shape;
-    hr.front = h.front;
-    hr.pad[0] = hr.pad[1] = 0;
-    B.hit[p] = hr;
+  uint32_t lane = threadIdx.x & 31u;
+  // warp-uniform loop: every lane takes part in the class appends
+  for (uint32_t base = blockIdx.x * blockDim.x; base < count; base += gridDim.x * blockDim.x) {
+    uint32_t i = base + threadIdx.x;
+    uint32_t cls = 0xffu, p = 0;
+    if (i < count) {
+      p = qin[i];
+      float4 o = B.rayO[p], d = B.rayD[p];
+      RayPre r = MakeRayPre(V3{o.x, o.y, o.z}, V3{d.x, d.y, d.z}, o.w);
+      TraceHit h;
+      TraceBvh8<false, COUNT>(S, r, d.w, h, err, &nN, &nP);
+      HitRec hr;
+      hr.t = h.t;
+      hr.u = h.u;
+      hr.v = h.v;
+      hr.prim = h.prim;
+      hr.shape = h.shape;
+      hr.front = h.front;
+      hr.pad[0] = hr.pad[1] = 0;
+      B.hit[p] = hr;
+      cls = (h.prim == kNoPrim || lastDepth) ? SC_EMIT : (uint32_t)S.shapeClass[h.shape];
+    }
+    // group lanes by shade class; one atomic per class present in the warp
+    uint32_t grp = __match_any_sync(0xffffffffu, cls);
+    int leader = __ffs(grp) - 1;
+    uint32_t slot = 0;
+    if (cls != 0xffu && (int)lane == leader) slot = atomicAdd(classCnt + cls, (uint32_t)__popc(grp));
+    slot = __shfl_sync(0xffffffffu, slot, leader);
+    if (cls != 0xffu) {
+      slot += __popc(grp & ((1u << lane) - 1u));
+      B.classQ[(size_t)cls * B.capacity + slot] = p;
+    }
   }
   if (COUNT) FlushTravCounts(trav, nN, nP);
 }
 
-__global__ void __launch_bounds__(kBlock) KShade(DevScene S, PathBuffers B, int depth) {
-  uint32_t count = B.counters[depth];
-  const uint32_t* qin = B.q[depth & 1];
+// Path::Li for one bounce, for the paths of shade class K (path.cpp:141-225).
+// SC_EMIT: misses, emitter hits, shapes without a BSDF and the last bounce --
+// emitter MIS only, then the path ends. Other classes: hits on a non-emitter
+// shape with a BSDF of that class -- NEE, BSDF sample, Russian roulette.
+template <int K>
+__global__ void __launch_bounds__(kBlock) KShadeClass(DevScene S, PathBuffers B, int depth) {
+  uint32_t count = B.counters[kClassBase + depth * kShadeClasses + K];
+  const uint32_t* qin = B.classQ + (size_t)K * B.capacity;
   uint32_t* qout = B.q[(depth + 1) & 1];
   uint32_t* cntOut = B.counters + depth + 1;
   uint32_t* cntSh = B.counters + kShadowBase + depth;
   uint32_t stride = gridDim.x * blockDim.x;
-  // warp-uniform loop so every lane takes part in the appends
   for (uint32_t base = blockIdx.x * blockDim.x; base < count; base += stride) {
     uint32_t i = base + threadIdx.x;
     bool active = i < count;
@@ -134,55 +157,51 @@ __global__ void __launch_bounds__(kBlock) KShade(DevScene S, PathBuffers B, int 
       p = qin[i];
       HitRec h = B.hit[p];
       float4 ro = B.rayO[p], rd = B.rayD[p];
-      float4 thr4 = B.thr[p], L4 = B.L[p], pv = B.prev[p];
-      uint2 rs = B.rng[p];
-      Pcg32 rng;
-      rng.state = ((uint64_t)rs.y << 32) | rs.x;
       V3 O{ro.x, ro.y, ro.z}, D{rd.x, rd.y, rd.z};
+      float4 thr4 = B.thr[p];
       V3 thr{thr4.x, thr4.y, thr4.z};
-      float eta = thr4.w;
-      V3 L{L4.x, L4.y, L4.z};
-      float prevPdf = L4.w;
-      uint32_t pflags = __float_as_uint(pv.w);
-      bool specular = pflags & 1u;
-      V3 prevP{pv.x, pv.y, pv.z};
-      bool anyHit = h.prim != kNoPrim;
-      SurfInt si;
-      if (anyHit) {
-        TraceHit th{h.t, h.u, h.v, h.prim, h.shape, h.front};
-        si = ComputeSI(S, O, D, th);
-      } else {
-        si.T = kInf;
-        si.P = v3s(0.f);
-        si.N = v3s(0.f);
-        si.shape = -1;
-        si.sh.S = si.sh.T = si.sh.N = v3s(0.f);
-        si.Wi = -D;  // scene.cpp:45-47: world-space -D on a miss
-      }
-      int hitLight = anyHit ? S.shapes[h.shape].light : S.envLight;
-      if (hitLight >= 0) {
-        float weight;
-        if (specular) {
-          weight = 1.f;
-        } else {
-          // SurfaceInteraction::ToDsr (interaction.cpp:68-74)
-          V3 rel = si.P - prevP;
-          float dist = norm(rel);
-          V3 dir = anyHit ? rel / dist : -si.Wi;
-          float lightPdf = PdfLightDirection(S, hitLight, prevP, dir, si.sh.N, dist);
-          weight = MisWeight(prevPdf, lightPdf);
+      if constexpr (K == SC_EMIT) {
+        float4 L4 = B.L[p];
+        int hitLight = h.prim != kNoPrim ? S.shapes[h.shape].light : S.envLight;
+        if (hitLight >= 0) {
+          bool anyHit = h.prim != kNoPrim;
+          SurfInt si;
+          if (anyHit) {
+            TraceHit th{h.t, h.u, h.v, h.prim, h.shape, h.front};
+            si = ComputeSI(S, O, D, th);
+          } else {
+            si.T = kInf;
+            si.P = v3s(0.f);
+            si.N = v3s(0.f);
+            si.shape = -1;
+            si.sh.S = si.sh.T = si.sh.N = v3s(0.f);
+            si.Wi = -D;  // scene.cpp:45-47: world-space -D on a miss
+          }
+          float4 pv = B.prev[p];
+          bool specular = __float_as_uint(pv.w) & 1u;
+          float weight;
+          if (specular) {
+            weight = 1.f;
+          } else {
+            // SurfaceInteraction::ToDsr (interaction.cpp:68-74)
+            V3 prevP{pv.x, pv.y, pv.z};
+            V3 rel = si.P - prevP;
+            float dist = norm(rel);
+            V3 dir = anyHit ? rel / dist : -si.Wi;
+            weight = MisWeight(L4.w, PdfLightDirection(S, hitLight, prevP, dir, si.sh.N, dist));
+          }
+          V3 li = EvalLightAt(S, hitLight, &si);
+          V3 L = V3{L4.x, L4.y, L4.z} + cmul(thr, li) * weight;
+          B.L[p] = make_float4(L.x, L.y, L.z, L4.w);
         }
-        V3 li = EvalLightAt(S, hitLight, &si);
-        L = L + cmul(thr, li) * weight;
-      }
-      bool stop = !anyHit || (S.maxDepth >= 0 && depth + 1 >= S.maxDepth);
-      int bsdf = -1;
-      if (!stop) {
-        const ShapeRec& shp = S.shapes[h.shape];
-        if (shp.light >= 0 || shp.bsdf < 0) stop = true;
-        bsdf = shp.bsdf;
-      }
-      if (!stop) {
+      } else {
+        float eta = thr4.w;
+        uint2 rs = B.rng[p];
+        Pcg32 rng;
+        rng.state = ((uint64_t)rs.y << 32) | rs.x;
+        TraceHit th{h.t, h.u, h.v, h.prim, h.shape, h.front};
+        SurfInt si = ComputeSI(S, O, D, th);
+        uint32_t bsdf = (uint32_t)S.shapes[h.shape].bsdf;
         const MatRec* mats = S.mats;
         if (mats[bsdf].flags & BT_NODELTA) {
           float xl = Next1D(rng);
@@ -193,7 +212,7 @@ __global__ void __launch_bounds__(kBlock) KShade(DevScene S, PathBuffers B, int 
             V3 wo = ToLocal(si.sh, dsr.Dir);
             V3 f;
             float bsdfPdf;
-            BsdfEvalPdf(mats, (uint32_t)bsdf, si.Wi, wo, f, bsdfPdf);
+            ClassEvalPdf<K>(mats, bsdf, si.Wi, wo, f, bsdfPdf);
             // Scene::IsOcclude (scene.cpp:53-63)
             V3 so = OffsetP(si.P, si.N, dsr.P - si.P);
             V3 sd = dsr.P - so;
@@ -211,50 +230,50 @@ __global__ void __launch_bounds__(kBlock) KShade(DevScene S, PathBuffers B, int 
         }
         float xl = Next1D(rng);
         V2 xd = Next2D(rng);
-        BsdfSampleRes bs = BsdfSample(mats, (uint32_t)bsdf, si.Wi, xl, xd);
-        if (bs.pdf <= 0.f) {
-          stop = true;
-        } else {
+        BsdfSampleRes bs = ClassSample<K>(mats, bsdf, si.Wi, xl, xd);
+        if (bs.pdf > 0.f) {
           thr = cmul(thr, bs.f) / bs.pdf;
           eta *= bs.eta;
-          V3 nd = ToWorld(si.sh, bs.wo);
-          V3 no = OffsetP(si.P, si.N, nd);
-          prevPdf = bs.pdf;
-          prevP = si.P;
-          specular = (bs.type & BT_DELTA) != 0u;
+          bool survive = true;
           if (depth >= S.rrDepth) {
             float rr = fminr(max_comp(thr) * Sqr(eta), 0.95f);
             if (Next1D(rng) > rr) {
-              stop = true;
+              survive = false;
             } else {
               thr = thr * Rcp(rr);
             }
           }
-          if (!stop) {
+          if (survive) {
             keep = true;
+            V3 nd = ToWorld(si.sh, bs.wo);
+            V3 no = OffsetP(si.P, si.N, nd);
+            bool specular = (bs.type & BT_DELTA) != 0u;
             B.rayO[p] = make_float4(no.x, no.y, no.z, 0.f);
             B.rayD[p] = make_float4(nd.x, nd.y, nd.z, kFloatMax);
             B.thr[p] = make_float4(thr.x, thr.y, thr.z, eta);
-            B.prev[p] = make_float4(prevP.x, prevP.y, prevP.z, __uint_as_float(specular ? 1u : 0u));
+            B.prev[p] = make_float4(si.P.x, si.P.y, si.P.z, __uint_as_float(specular ? 1u : 0u));
             B.rng[p] = make_uint2((uint32_t)rng.state, (uint32_t)(rng.state >> 32));
+            float4 L4 = B.L[p];
+            B.L[p] = make_float4(L4.x, L4.y, L4.z, bs.pdf);
           }
         }
       }
-      B.L[p] = make_float4(L.x, L.y, L.z, prevPdf);
     }
-    uint32_t slot = WarpAppend(cntOut, keep);
-    if (keep) qout[slot] = p;
-    uint32_t sslot = WarpAppend(cntSh, shadow);
-    if (shadow) {
-      B.shO[sslot] = shO;
-      B.shD[sslot] = shD;
-      B.shC[sslot] = shC;
+    if constexpr (K != SC_EMIT) {
+      uint32_t slot = WarpAppend(cntOut, keep);
+      if (keep) qout[slot] = p;
+      uint32_t sslot = WarpAppend(cntSh, shadow);
+      if (shadow) {
+        B.shO[sslot] = shO;
+        B.shD[sslot] = shD;
+        B.shC[sslot] = shC;
+      }
     }
   }
 }
 
 template <bool COUNT>
-__global__ void __launch_bounds__(kBlock) KShadow(DevScene S, PathBuffers B, int depth, unsigned long long* trav) {
+__global__ void __launch_bounds__(kBlock, 8) KShadow(DevScene S, PathBuffers B, int depth, unsigned long long* trav) {
   uint32_t count = B.counters[kShadowBase + depth];
   uint32_t* err = B.counters + kMiscBase + 1;
   uint32_t nN = 0, nP = 0;
@@ -275,8 +294,13 @@ __global__ void __launch_bounds__(kBlock) KShadow(DevScene S, PathBuffers B, int
 
 // sample_renderer.cpp:101-105: drop NaN in any channel, Inf / negative in the
 // first channel only (spectrum.h:28-29), the sample still counts in 1/spp.
-__global__ void __launch_bounds__(256) KAccumulate(PathBuffers B, FilmView film, uint32_t count) {
+__global__ void __launch_bounds__(256) KAccumulate(PathBuffers B, FilmView film, uint32_t count, WaveCtx* ctx) {
   uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (ctx) {
+    film.accum = ctx->film;
+    film.stats = ctx->stats;
+    if (i == 0) ctx->sample += 1;  // generate of this wave has completed: advance for the next replay
+  }
   if (i == 0 && film.stats) {
     unsigned long long cl = 0, sh = 0;
     for (int k = 0; k <= kMaxBounce; k++) {
@@ -326,7 +350,7 @@ __global__ void KResolveFilm(FilmView film, float scale, float* out) {
 }
 
 cudaError_t LaunchGenerate(const DevScene& S, const PathBuffers& B, const WaveParams& w, cudaStream_t st) {
-  uint32_t n = w.count > 0 ? w.count : 1;
+  uint32_t n = w.count > (uint32_t)kCounterWords ? w.count : (uint32_t)kCounterWords;
   KGenerate<<<(n + kBlock - 1) / kBlock, kBlock, 0, st>>>(S, B, w);
   return cudaGetLastError();
 }
@@ -339,7 +363,12 @@ cudaError_t LaunchExtend(const DevScene& S, const PathBuffers& B, int depth, int
   return cudaGetLastError();
 }
 cudaError_t LaunchShade(const DevScene& S, const PathBuffers& B, int depth, int grid, cudaStream_t st) {
-  KShade<<<grid, kBlock, 0, st>>>(S, B, depth);
+  KShadeClass<SC_EMIT><<<grid, kBlock, 0, st>>>(S, B, depth);
+  KShadeClass<SC_DIFFUSE><<<grid, kBlock, 0, st>>>(S, B, depth);
+  KShadeClass<SC_METAL><<<grid, kBlock, 0, st>>>(S, B, depth);
+  KShadeClass<SC_GLASS><<<grid, kBlock, 0, st>>>(S, B, depth);
+  KShadeClass<SC_DISNEY><<<grid, kBlock, 0, st>>>(S, B, depth);
+  KShadeClass<SC_GENERIC><<<grid, kBlock, 0, st>>>(S, B, depth);
   return cudaGetLastError();
 }
 cudaError_t LaunchShadow(const DevScene& S, const PathBuffers& B, int depth, int grid, cudaStream_t st,
@@ -350,9 +379,10 @@ cudaError_t LaunchShadow(const DevScene& S, const PathBuffers& B, int depth, int
     KShadow<false><<<grid, kBlock, 0, st>>>(S, B, depth, nullptr);
   return cudaGetLastError();
 }
-cudaError_t LaunchAccumulate(const PathBuffers& B, const FilmView& film, uint32_t count, cudaStream_t st) {
+cudaError_t LaunchAccumulate(const PathBuffers& B, const FilmView& film, uint32_t count, cudaStream_t st,
+                             WaveCtx* ctx) {
   if (count == 0) return cudaSuccess;
-  KAccumulate<<<(count + 255) / 256, 256, 0, st>>>(B, film, count);
+  KAccumulate<<<(count + 255) / 256, 256, 0, st>>>(B, film, count, ctx);
   return cudaGetLastError();
 }
 cudaError_t LaunchGatherRadiance(const PathBuffers& B, uint32_t count, float* out, cudaStream_t st) {

@@ -21,7 +21,9 @@ struct PathBuffers {
   float4* shO;     // shadow ray origin xyz, tmax
   float4* shD;     // shadow ray direction xyz, path slot bits
   float4* shC;     // shadow contribution rgb
-  uint32_t* counters;  // [0, kMaxBounce]: active counts; [kShadowBase, +kMaxBounce]: shadow counts; kMisc..
+  uint32_t* classQ;    // kShadeClasses queues of `capacity` slots, filled by extend, read by shade
+  uint32_t* counters;  // [0, kMaxBounce]: active counts; [kShadowBase, +kMaxBounce]: shadow counts; kMisc..;
+                       // [kClassBase + depth * kShadeClasses + class]: shade-class counts
   uint32_t capacity;
 };
 
@@ -29,7 +31,8 @@ constexpr int kMaxBounce = 256;
 constexpr int kShadowBase = kMaxBounce + 1;
 constexpr int kMiscBase = 2 * kMaxBounce + 2;  // [0] spare, [1] device error word (sticky),
                                                // [2] vol closest rays, [3] vol shadow-side rays
-constexpr int kCounterWords = kMiscBase + 8;
+constexpr int kClassBase = kMiscBase + 8;
+constexpr int kCounterWords = kClassBase + (kMaxBounce + 1) * kShadeClasses;
 
 struct FilmView {
   float4* accum;  // rgb sum, sample count in w
@@ -55,6 +58,19 @@ struct WaveParams {
   uint32_t sample, seed;
   const uint32_t* pixelList;   // optional explicit pixel list (parity hook)
   const uint32_t* sampleList;  // optional explicit per-path sample indices
+  // Optional device-side wave context (graph replay): when set, the sample index,
+  // seed, film and stats come from here, and the accumulate stage advances the
+  // sample index, so one captured graph renders consecutive samples.
+  const struct WaveCtx* ctx;
+};
+
+// Per-job wave context in device memory, read by generate and accumulate.
+struct WaveCtx {
+  float4* film;
+  unsigned long long* stats;
+  uint32_t sample;  // next sample index; advanced by accumulate
+  uint32_t seed;
+  uint32_t pad[2];
 };
 int PathGridBlocks();
 cudaError_t LaunchGenerate(const DevScene& S, const PathBuffers& B, const WaveParams& w, cudaStream_t st);
@@ -64,7 +80,8 @@ cudaError_t LaunchExtend(const DevScene& S, const PathBuffers& B, int depth, int
 cudaError_t LaunchShade(const DevScene& S, const PathBuffers& B, int depth, int grid, cudaStream_t st);
 cudaError_t LaunchShadow(const DevScene& S, const PathBuffers& B, int depth, int grid, cudaStream_t st,
                          unsigned long long* trav = nullptr);
-cudaError_t LaunchAccumulate(const PathBuffers& B, const FilmView& film, uint32_t count, cudaStream_t st);
+cudaError_t LaunchAccumulate(const PathBuffers& B, const FilmView& film, uint32_t count, cudaStream_t st,
+                             struct WaveCtx* ctx = nullptr);
 cudaError_t LaunchGatherRadiance(const PathBuffers& B, uint32_t count, float* out, cudaStream_t st);
 cudaError_t LaunchResolveFilm(const FilmView& film, float scale, float* out, cudaStream_t st);
 

@@ -127,6 +127,12 @@ struct alignas(16) PrimRec {
 static_assert(sizeof(PrimRec) == 48, "PrimRec must be 48 bytes");
 
 // ---------------------------------------------------------------- scene
+// Shade classes: the extend stage sorts hits into one queue per class so that
+// each shade kernel runs one BSDF's code. 0 = miss / emitter / no BSDF (emission
+// only), 1..4 = MatKind of the (possibly two-sided) leaf BSDF, 5 = anything else.
+enum : uint32_t { SC_EMIT = 0, SC_DIFFUSE = 1, SC_METAL = 2, SC_GLASS = 3, SC_DISNEY = 4, SC_GENERIC = 5 };
+constexpr int kShadeClasses = 6;
+
 struct DevScene {
   const Bvh8Node* nodes;
   const PrimRec* prims;
@@ -141,6 +147,7 @@ struct DevScene {
   const uint32_t* idx;         // global triangle indices, 3 per triangle
   const float* cdf;            // emitter-mesh area CDF / PMF (2 floats per triangle)
   const float* volume;         // density grids
+  const uint8_t* shapeClass;   // shade class per shape
   uint32_t nNodes, nPrims, nShapes, nLights;
   uint32_t nMedia, nMats;
   int32_t envLight, globalMedium;

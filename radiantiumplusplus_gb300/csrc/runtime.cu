@@ -119,6 +119,10 @@ struct rad_job {
   rad_stats stats{};
   std::vector<std::pair<cudaEvent_t, cudaEvent_t>> profEv;
   std::vector<int> profKind;
+  // CUDA graph per pixel chunk: one captured wave replayed once per sample
+  WaveCtx* ctx = nullptr;  // device, one per chunk
+  std::vector<cudaGraphExec_t> graphs;
+  std::vector<uint64_t> graphKernels;
   std::mutex m;
   std::condition_variable cv;
 };
@@ -188,6 +192,7 @@ void AllocPaths(Lib& lib) {
   B.shO = DevAlloc<float4>(P, o, b);
   B.shD = DevAlloc<float4>(P, o, b);
   B.shC = DevAlloc<float4>(P, o, b);
+  B.classQ = DevAlloc<uint32_t>((size_t)P * kShadeClasses, o, b);
   B.counters = DevAlloc<uint32_t>(kCounterWords, o, b);
   Check(cudaMemset(B.counters, 0, kCounterWords * sizeof(uint32_t)), "cudaMemset");
   B.capacity = P;
@@ -264,7 +269,7 @@ uint64_t LaunchBounces(const DevScene& S, uint32_t count, ProfSink& ps, unsigned
     ps.Begin(3, a);
     Check(LaunchShadow(S, lib.paths, d, grid, lib.stream, trav), "shadow");
     ps.End(3, a);
-    launches += 3;
+    launches += 2 + kShadeClasses;
     if (S.maxDepth < 0 && (d % 8) == 7) {
       // unbounded depth: stop once the next queue is empty
       Check(cudaMemcpyAsync(lib.hCounters, lib.paths.counters, (d + 2) * sizeof(uint32_t), cudaMemcpyDeviceToHost,
@@ -277,8 +282,70 @@ uint64_t LaunchBounces(const DevScene& S, uint32_t count, ProfSink& ps, unsigned
   return launches;
 }
 
+// Graph replay applies to fixed-depth `path` jobs without per-kernel profiling
+// or traversal counting (those record events / host readbacks per launch).
+bool GraphEligible(const rad_job* j) {
+  const DevScene& S = j->scene->dev;
+  return !S.isVol && S.maxDepth >= 0 && !(j->flags & (RAD_JOB_PROFILE_KERNELS | RAD_JOB_COUNT_TRAVERSAL));
+}
+
+// Runs the job's next sample over its pixels as replays of one captured graph
+// per chunk (generate, bounces, accumulate); the accumulate stage advances the
+// sample index held in the chunk's device WaveCtx.
+void RunWaveGraph(rad_job* j) {
+  Lib& lib = L();
+  const DevScene& S = j->scene->dev;
+  uint32_t W = (uint32_t)S.cam.width, H = (uint32_t)S.cam.height;
+  uint64_t npix = (uint64_t)W * H;
+  size_t nChunks = (size_t)((npix + lib.maxPaths - 1) / lib.maxPaths);
+  if (j->graphs.empty()) {
+    Check(cudaMalloc(&j->ctx, nChunks * sizeof(WaveCtx)), "cudaMalloc");
+    std::vector<WaveCtx> host(nChunks);
+    for (auto& c : host) {
+      c = WaveCtx{};
+      c.film = j->accum;
+      c.stats = j->dStats;
+      c.sample = j->first + j->nextSample;
+      c.seed = j->seed;
+    }
+    Check(cudaMemcpy(j->ctx, host.data(), nChunks * sizeof(WaveCtx), cudaMemcpyHostToDevice), "ctx upload");
+    ProfSink none{nullptr};
+    FilmView film{j->accum, (int32_t)W, (int32_t)H, j->dStats};
+    for (size_t c = 0; c < nChunks; c++) {
+      uint64_t p0 = (uint64_t)c * lib.maxPaths;
+      uint32_t count = (uint32_t)std::min<uint64_t>(lib.maxPaths, npix - p0);
+      WaveParams w{(uint32_t)p0, count, 0, 0, nullptr, nullptr, j->ctx + c};
+      cudaGraph_t g = nullptr;
+      Check(cudaStreamBeginCapture(lib.stream, cudaStreamCaptureModeThreadLocal), "begin capture");
+      cudaError_t e1 = LaunchGenerate(S, lib.paths, w, lib.stream);
+      uint64_t k = 1 + LaunchBounces(S, count, none);
+      cudaError_t e2 = LaunchAccumulate(lib.paths, film, count, lib.stream, j->ctx + c);
+      cudaError_t e3 = cudaStreamEndCapture(lib.stream, &g);
+      Check(e1, "generate capture");
+      Check(e2, "accumulate capture");
+      Check(e3, "end capture");
+      cudaGraphExec_t ex = nullptr;
+      cudaError_t e4 = cudaGraphInstantiate(&ex, g, 0);
+      cudaGraphDestroy(g);
+      Check(e4, "graph instantiate");
+      j->graphs.push_back(ex);
+      j->graphKernels.push_back(k + 1);
+    }
+  }
+  for (size_t c = 0; c < j->graphs.size(); c++) {
+    Check(cudaGraphLaunch(j->graphs[c], lib.stream), "graph launch");
+    j->stats.kernel_launches += j->graphKernels[c];
+  }
+  j->nextSample++;
+  j->launched += npix;
+}
+
 // Runs wave(s) for the job's next sample index over all its pixels.
 void RunWave(rad_job* j) {
+  if (GraphEligible(j)) {
+    RunWaveGraph(j);
+    return;
+  }
   Lib& lib = L();
   const DevScene& S = j->scene->dev;
   uint32_t W = (uint32_t)S.cam.width, H = (uint32_t)S.cam.height;
@@ -447,9 +514,12 @@ void WorkerMain() {
         continue;
       }
       if (!lib.running.empty()) {
-        lib.rr = lib.rr % lib.running.size();
-        j = lib.running[lib.rr];
-        lib.rr++;
+        // least attained service: the running job with the fewest samples
+        // launched goes next (processor sharing by samples, so a small job is
+        // not held behind the waves of a large one); ties go to the earlier job
+        j = lib.running[0];
+        for (rad_job* c : lib.running)
+          if (c->launched.load() < j->launched.load()) j = c;
       }
     }
     if (j) {
@@ -509,6 +579,7 @@ uint64_t SceneUpload(const HostScene& hs, rad_scene* sc) {
   uint32_t* idx = DevAlloc<uint32_t>(hs.idx.size(), o, b);
   float* cdf = DevAlloc<float>(hs.cdf.size(), o, b);
   float* vol = DevAlloc<float>(hs.volume.size(), o, b);
+  uint8_t* scls = DevAlloc<uint8_t>(hs.shapeClass.size(), o, b);
   up(nodes, hs.nodes);
   up(prims, hs.prims);
   up(pinfo, hs.primInfo);
@@ -522,6 +593,7 @@ uint64_t SceneUpload(const HostScene& hs, rad_scene* sc) {
   up(idx, hs.idx);
   up(cdf, hs.cdf);
   up(vol, hs.volume);
+  up(scls, hs.shapeClass);
   D.nodes = nodes;
   D.prims = prims;
   D.primInfo = pinfo;
@@ -535,6 +607,7 @@ uint64_t SceneUpload(const HostScene& hs, rad_scene* sc) {
   D.idx = idx;
   D.cdf = cdf;
   D.volume = vol;
+  D.shapeClass = scls;
   D.nNodes = (uint32_t)hs.nodes.size();
   D.nPrims = (uint32_t)hs.prims.size();
   D.nShapes = (uint32_t)hs.shapes.size();
@@ -832,6 +905,8 @@ int rad_job_destroy(rad_job* job) {
     if (job->dStats) cudaFree(job->dStats);
     if (job->hStats) cudaFreeHost(job->hStats);
     if (job->resolve) cudaFree(job->resolve);
+    for (cudaGraphExec_t g : job->graphs) cudaGraphExecDestroy(g);
+    if (job->ctx) cudaFree(job->ctx);
     if (job->evStart) cudaEventDestroy(job->evStart);
     if (job->evEnd) cudaEventDestroy(job->evEnd);
     job->scene->jobs--;

@@ -68,3 +68,17 @@ def test_errors_are_status_codes(rad, scene_dir):
     with pytest.raises(rad.RadError) as e:
         rad.bsdf_eval({"type": "plastic_x"}, np.zeros((1, 3)), np.zeros((1, 3)))
     assert e.value.code == 3
+
+
+def test_graph_replay_equals_direct_launches(rad, scene_dir):
+    """Jobs replay one captured CUDA graph per wave; a profiled job launches kernels directly. Same film."""
+    s = rad.Scene.from_file(spheres(scene_dir, 200, 3, 40, 24, 5)[0])
+    g = s.submit(spp=5)
+    g.wait()
+    d = s.submit(spp=5, profile=True)
+    d.wait()
+    assert np.array_equal(g.film(), d.film())
+    assert g.stats()["samples"] == d.stats()["samples"] == 40 * 24 * 5
+    g.close()
+    d.close()
+    s.close()
