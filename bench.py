@@ -335,6 +335,88 @@ def run_volume(args, world, rank, local):
     print(json.dumps(line), flush=True)
 
 
+def run_guided(args, world, rank, local):
+    """Learned proposal vs plain BSDF sampling on the guided room (the sphere field in
+    a closed room lit only through a ceiling opening), 1920x1080, depth 16. relMSE
+    is measured over the frame; the guided job (fresh network, training in its
+    first quarter of samples) is run at increasing spp until it reaches the
+    plain job's 64-spp relMSE, and the wall-time ratio is reported. The reference
+    is a long guided render of the full frame (unbiased: every network state is a
+    valid proposal); plain path tracing of this scene does not converge in minutes."""
+    import numpy as np
+    import torch
+    import radiantiumplusplus_gb300 as rad
+    from radiantiumplusplus_gb300 import scenes
+    torch.cuda.set_device(local)
+    rad.init({"device": local})
+    Wg, Hg = args.guided_res
+    with tempfile.TemporaryDirectory(prefix="rad_bench_guided_") as tmp:
+        sc, assets = scenes.guided_room(n_spheres=args.guided_spheres, width=Wg, height=Hg, spp=64, max_depth=16)
+        path = scenes.write_scene(tmp, sc, assets)
+        scene = rad.Scene.from_file(path)
+        # Reference: a long guided render (the guided estimator is unbiased for any
+        # network state; a plain render of this scene does not converge in minutes).
+        scene.guide_enable({"log2_table": 19})
+        j = scene.submit(spp=args.guided_ref_spp, seed=777, guide=True)
+        j.wait()
+        ref = j.film().astype(np.float64)
+        j.close()
+
+        def relmse(film):
+            e = ((film.astype(np.float64) - ref) ** 2 / (ref ** 2 + 1e-2)).mean(axis=2).ravel()
+            srt = np.sort(e)
+            return float(e.mean()), float(srt[:int(0.99 * srt.size)].mean()), float(np.median(e))
+
+        def timed(spp, guide):
+            torch.cuda.synchronize()
+            t0 = time.perf_counter()
+            j = scene.submit(spp=spp, seed=11, guide=guide)
+            j.wait()
+            dt = time.perf_counter() - t0
+            st = j.stats()
+            f = j.film()
+            j.close()
+            return dt, st, f
+
+        timed(4, False)  # warm-up (graph capture, allocations)
+        scene.guide_enable({"log2_table": 19})
+        timed(4, True)
+        clocks = ClockSampler(local)
+        clocks.start()
+        tp, stp, fp = timed(64, False)
+        ep = relmse(fp)
+        runs = []
+        reached = None
+        for spp in args.guided_spp:
+            scene.guide_enable({"log2_table": 19})  # fresh network: training is part of the time
+            tg, stg, fg = timed(spp, True)
+            eg = relmse(fg)
+            runs.append({"spp": spp, "wall_s": tg, "relmse": eg[0], "relmse_trim1": eg[1], "relmse_median": eg[2],
+                         "mean_over_ref": float(fg.mean() / ref.mean()),
+                         "train_steps": stg["guide_train_steps"], "records": stg["guide_records"],
+                         "samples_per_s": stg["samples"] / tg,
+                         "mrays_per_s": (stg["rays_closest"] + stg["rays_shadow"]) / tg / 1e6})
+            if reached is None and eg[0] <= ep[0]:
+                reached = runs[-1]
+        clk = clocks.stop()
+        scene.close()
+    line = {"metric": "wall-time ratio guided/plain at plain 64-spp relMSE (guided room %dx%d, depth 16)" % (Wg, Hg),
+            "value": (reached["wall_s"] / tp) if reached else None, "unit": "ratio", "n_gpus": 1,
+            "steps": 1, "warmup": 1, "higher_is_better": False, "scaling": "weak", "vs_baseline": None,
+            "dtype": "f32 (guide network fp16 weights, fp32 accumulation)", "data": "synthetic (seeded generator)",
+            "config": {"workload": "guided_room", "spheres": args.guided_spheres, "width": Wg, "height": Hg,
+                       "max_depth": 16, "room": 200, "opening": 5, "irradiance": 1000,
+                       "reference": "guided render, %d spp" % args.guided_ref_spp, "ref_mean": float(ref.mean()),
+                       "guide": {"log2_table": 19, "levels": 16, "mlp": "3x64", "lobes": 8, "lr": 0.01,
+                                 "lr_mlp": 0.001, "train_fraction": 0.25}},
+            "plain": {"spp": 64, "wall_s": tp, "relmse": ep[0], "relmse_trim1": ep[1], "relmse_median": ep[2],
+                      "mean_over_ref": float(fp.mean() / ref.mean()),
+                      "samples_per_s": stp["samples"] / tp,
+                      "mrays_per_s": (stp["rays_closest"] + stp["rays_shadow"]) / tp / 1e6},
+            "guided": runs, "clocks": clk}
+    print(json.dumps(line), flush=True)
+
+
 def run_serving(args, world, rank, local):
     """Serving loop: Poisson arrivals of jobs over a pool of resident scenes; throughput and p50/p99 latency."""
     import numpy as np
@@ -412,7 +494,11 @@ def main():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline leg")
     ap.add_argument("--cpu-row-step", type=int, default=4)
-    ap.add_argument("--workload", default="many_spheres", choices=["many_spheres", "volume", "serving"])
+    ap.add_argument("--workload", default="many_spheres", choices=["many_spheres", "volume", "serving", "guided"])
+    ap.add_argument("--guided-res", type=int, nargs=2, default=[1920, 1080])
+    ap.add_argument("--guided-spheres", type=int, default=10000)
+    ap.add_argument("--guided-ref-spp", type=int, default=1024)
+    ap.add_argument("--guided-spp", type=int, nargs="+", default=[8, 16, 24, 32, 48, 64])
     ap.add_argument("--vol-res", type=int, default=1024)
     ap.add_argument("--vol-grid", type=int, default=256)
     ap.add_argument("--rates", type=float, nargs="+", default=[1, 2, 5, 10, 20])
@@ -425,6 +511,8 @@ def main():
         run_reference(args, world, rank)
     elif args.workload == "volume":
         run_volume(args, world, rank, local)
+    elif args.workload == "guided":
+        run_guided(args, world, rank, local)
     elif args.workload == "serving":
         run_serving(args, world, rank, local)
     else:

@@ -75,6 +75,9 @@ typedef struct rad_job_desc {
 #define RAD_JOB_PROFILE_KERNELS 1u /* time every kernel launch with CUDA events */
 #define RAD_JOB_SYNC 2u            /* render on the calling thread, return when done */
 #define RAD_JOB_COUNT_TRAVERSAL 4u /* count BVH8 node visits / primitive tests (slower) */
+#define RAD_JOB_GUIDE 8u           /* `path` only: sample directions with the scene's learned guide
+                                      (one-sample MIS with the BSDF) and train it during the
+                                      job's first train_fraction of samples; no reference counterpart */
 
 /* Counters of one job. Rays = primary + extension + shadow rays traced. */
 typedef struct rad_stats {
@@ -91,6 +94,10 @@ typedef struct rad_stats {
   uint64_t n_extend, n_shade, n_shadow;
   /* with RAD_JOB_COUNT_TRAVERSAL: node visits and primitive tests */
   uint64_t trav_nodes_closest, trav_prims_closest, trav_nodes_shadow, trav_prims_shadow;
+  /* with RAD_JOB_GUIDE: training records, Adam steps, and (with RAD_JOB_PROFILE_KERNELS)
+   * device time of the guide inference and training stages */
+  uint64_t guide_records, guide_train_steps;
+  double ms_guide_infer, ms_guide_train;
 } rad_stats;
 
 /* ---- library ------------------------------------------------------------ */
@@ -166,6 +173,56 @@ RAD_API int rad_render_samples(rad_scene* scene, const uint32_t* pixels, const u
  * capture. Every call shares the one array: calls that overlap on the GPU race. */
 RAD_API int rad_render_samples_noalloc(rad_scene* scene, const uint32_t* d_pixels, const uint32_t* d_samples,
                                        int64_t n, uint32_t seed, float* d_radiance, void* stream);
+
+/* ---- learned path guiding ------------------------------------------------ */
+/* No counterpart in the reference (its integrators sample the BSDF only). A
+ * scene may own one guide network: a 16-level hash grid over the shading
+ * position (2 features per level, 2^log2_table entries each) plus the shading
+ * normal and outgoing direction, into a 3 x 64 ReLU MLP (fp16 weights, fp32
+ * accumulation) whose 41 outputs give an 8-lobe von Mises-Fisher mixture over
+ * world directions and the probability c <= c_max of sampling it instead of
+ * the BSDF. Jobs submitted with RAD_JOB_GUIDE sample p = c q + (1 - c) p_bsdf
+ * (unbiased for any network state) and train the network online with Adam on
+ * their own paths during their first train_fraction of samples. */
+typedef struct rad_guide_info_t {
+  uint64_t n_params;   /* table + MLP weights */
+  uint64_t n_table;    /* levels x 2^log2_table x 2 */
+  uint32_t log2_table, levels;
+  uint32_t level_res[16];
+  float lo[3], hi[3];  /* world box mapped to the unit cube */
+  uint64_t adam_steps;
+  uint64_t device_bytes;
+} rad_guide_info_t;
+
+/* Creates (or re-creates, seeded) the scene's guide. config_json may be NULL;
+ * keys: log2_table (19), min_res (16), max_res (512), lr (0.01, hash table),
+ * lr_mlp (0.001), train_fraction (0.25), train_path_shift (4: 1 in 16 paths
+ * records training vertices), train_depth (8), steps_per_wave (8),
+ * record_capacity (2^20), weight_clamp (32), log_kappa_max (5), c_max (0.6),
+ * seed (5). A checkpoint carries the network, not these settings. Fails while
+ * jobs of the scene are live. */
+RAD_API int rad_guide_enable(rad_scene* scene, const char* config_json);
+RAD_API int rad_guide_info(rad_scene* scene, rad_guide_info_t* info);
+/* Serialises parameters and Adam moments into buf (host); *needed gets the
+ * size. buf = NULL only queries the size. */
+RAD_API int rad_guide_checkpoint(rad_scene* scene, void* buf, size_t size, size_t* needed);
+/* Replaces the scene's guide with a checkpoint's (RAD_ERR_INVALID_ARG if malformed). */
+RAD_API int rad_guide_load(rad_scene* scene, const void* buf, size_t size);
+/* Network on queries (n x 9: position, shading normal, outgoing direction;
+ * world space). raw (n x 48, optional): outputs; mix (n x 44, optional):
+ * 8 x (mu xyz, kappa), 8 lobe weights, c, 3 zeros. Creates a default guide if
+ * the scene has none. Host memory. */
+RAD_API int rad_guide_forward(rad_scene* scene, const float* queries, int64_t n, float* raw, float* mix);
+/* Mixture pdf of packed mixtures (n x 44 as above): at dirs (n x 3) when dirs
+ * is given, else of directions sampled from u (n x 3: lobe, two direction
+ * numbers) returned in out_dirs. Exactly one of dirs / u. Host memory. */
+RAD_API int rad_guide_mix_eval(const float* mix, const float* dirs, const float* u, int64_t n, float* pdf,
+                               float* out_dirs);
+/* Gradient of sum_i -w_i log p_i(wi_i) over records (n x 16: position, p_bsdf |
+ * normal, - | wo, - | wi, w) with respect to every parameter (grad: n_params,
+ * table first, summed over records); loss gets the summed loss. The same
+ * kernels as training. Host memory. */
+RAD_API int rad_guide_grad(rad_scene* scene, const float* records, int64_t n, float* grad, float* loss);
 
 #ifdef __cplusplus
 }

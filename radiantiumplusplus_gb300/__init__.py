@@ -117,8 +117,51 @@ class Scene:
                                        self.seed if seed is None else seed, _p(out)))
         return out
 
-    def submit(self, spp=0, seed=None, first_sample=0, profile=False, sync=False, count_traversal=False):
-        return Job(self, spp, seed, first_sample, profile, sync, count_traversal)
+    def submit(self, spp=0, seed=None, first_sample=0, profile=False, sync=False, count_traversal=False,
+               guide=False):
+        return Job(self, spp, seed, first_sample, profile, sync, count_traversal, guide)
+
+    # ---- learned path guiding (no counterpart in the reference)
+    def guide_enable(self, config=None):
+        """Create (re-seed) the scene's guide network; config: dict of rad_guide_enable keys."""
+        text = None if config is None else json.dumps(config).encode()
+        check(lib().rad_guide_enable(self._h, text))
+
+    def guide_info(self):
+        gi = _capi.GuideInfo()
+        check(lib().rad_guide_info(self._h, ctypes.byref(gi)))
+        return {"n_params": gi.n_params, "n_table": gi.n_table, "log2_table": gi.log2_table,
+                "levels": gi.levels, "level_res": list(gi.level_res), "lo": list(gi.lo), "hi": list(gi.hi),
+                "adam_steps": gi.adam_steps, "device_bytes": gi.device_bytes}
+
+    def guide_checkpoint(self):
+        """Parameters and Adam moments as bytes (see rad_guide_checkpoint)."""
+        need = ctypes.c_size_t()
+        check(lib().rad_guide_checkpoint(self._h, None, 0, ctypes.byref(need)))
+        buf = np.empty(need.value, dtype=np.uint8)
+        check(lib().rad_guide_checkpoint(self._h, _p(buf), buf.size, ctypes.byref(need)))
+        return buf.tobytes()
+
+    def guide_load(self, blob):
+        buf = np.frombuffer(blob, dtype=np.uint8)
+        check(lib().rad_guide_load(self._h, _p(buf), buf.size))
+
+    def guide_forward(self, queries):
+        """queries (n, 9): position, shading normal, wo -> (raw (n, 48), mixture (n, 44))."""
+        q = np.ascontiguousarray(queries, dtype=np.float32)
+        raw = np.zeros((q.shape[0], 48), dtype=np.float32)
+        mix = np.zeros((q.shape[0], 44), dtype=np.float32)
+        check(lib().rad_guide_forward(self._h, _p(q), q.shape[0], _p(raw), _p(mix)))
+        return raw, mix
+
+    def guide_grad(self, records):
+        """records (n, 16) -> (gradient over all parameters, summed loss)."""
+        r = np.ascontiguousarray(records, dtype=np.float32)
+        n_params = self.guide_info()["n_params"]
+        g = np.zeros(n_params, dtype=np.float32)
+        loss = ctypes.c_float()
+        check(lib().rad_guide_grad(self._h, _p(r), r.shape[0], _p(g), ctypes.byref(loss)))
+        return g, loss.value
 
     def render(self, spp=0, seed=None, first_sample=0):
         """Submit, wait and return the film (H, W, 3) float32."""
@@ -133,10 +176,12 @@ class Scene:
 class Job:
     """One render job (rad_job_*)."""
 
-    def __init__(self, scene, spp=0, seed=None, first_sample=0, profile=False, sync=False, count_traversal=False):
+    def __init__(self, scene, spp=0, seed=None, first_sample=0, profile=False, sync=False, count_traversal=False,
+                 guide=False):
         self.scene = scene
         flags = (_capi.RAD_JOB_PROFILE_KERNELS if profile else 0) | (_capi.RAD_JOB_SYNC if sync else 0)
         flags |= _capi.RAD_JOB_COUNT_TRAVERSAL if count_traversal else 0
+        flags |= _capi.RAD_JOB_GUIDE if guide else 0
         d = _capi.JobDesc(spp, 0xFFFFFFFF if seed is None else seed, first_sample, flags)
         h = ctypes.c_void_p()
         check(lib().rad_job_submit(scene.handle, ctypes.byref(d), ctypes.byref(h)))
@@ -272,3 +317,18 @@ def bsdf_sample(bsdf, wi, u):
     typ = np.zeros(n, dtype=np.uint32)
     check(lib().rad_bsdf_sample_batch(_bsdf_json(bsdf), _p(wi), _p(u), n, _p(wo), _p(pdf), _p(f), _p(eta), _p(typ)))
     return wo, pdf, f, eta, typ
+
+
+def guide_mix_eval(mix, dirs=None, u=None):
+    """Packed guide mixtures (n, 44): pdf at dirs (n, 3), or (directions, pdf) sampled from u (n, 3)."""
+    mix = np.ascontiguousarray(mix, dtype=np.float32)
+    n = mix.shape[0]
+    pdf = np.zeros(n, dtype=np.float32)
+    if dirs is not None:
+        d = np.ascontiguousarray(dirs, dtype=np.float32)
+        check(lib().rad_guide_mix_eval(_p(mix), _p(d), None, n, _p(pdf), None))
+        return pdf
+    uu = np.ascontiguousarray(u, dtype=np.float32)
+    out = np.zeros((n, 3), dtype=np.float32)
+    check(lib().rad_guide_mix_eval(_p(mix), None, _p(uu), n, _p(pdf), _p(out)))
+    return out, pdf

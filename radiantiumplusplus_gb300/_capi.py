@@ -30,6 +30,7 @@ RAD_ERR_UNSUPPORTED = 13
 RAD_JOB_PROFILE_KERNELS = 1
 RAD_JOB_SYNC = 2
 RAD_JOB_COUNT_TRAVERSAL = 4
+RAD_JOB_GUIDE = 8
 
 # Every symbol the header declares (the export test checks this list).
 EXPORTS = [
@@ -38,7 +39,8 @@ EXPORTS = [
     "rad_scene_footprint", "rad_job_submit", "rad_job_wait", "rad_job_cancel", "rad_job_progress",
     "rad_job_film", "rad_job_stats", "rad_job_destroy", "rad_trace_batch", "rad_trace_batch_device",
     "rad_bsdf_eval_batch", "rad_bsdf_sample_batch", "rad_camera_rays", "rad_render_samples",
-    "rad_render_samples_noalloc",
+    "rad_render_samples_noalloc", "rad_guide_enable", "rad_guide_info", "rad_guide_checkpoint",
+    "rad_guide_load", "rad_guide_forward", "rad_guide_mix_eval", "rad_guide_grad",
 ]
 
 
@@ -72,7 +74,15 @@ class Stats(ctypes.Structure):
                 ("ms_volpath", ctypes.c_double), ("n_extend", ctypes.c_uint64), ("n_shade", ctypes.c_uint64),
                 ("n_shadow", ctypes.c_uint64), ("trav_nodes_closest", ctypes.c_uint64),
                 ("trav_prims_closest", ctypes.c_uint64), ("trav_nodes_shadow", ctypes.c_uint64),
-                ("trav_prims_shadow", ctypes.c_uint64)]
+                ("trav_prims_shadow", ctypes.c_uint64), ("guide_records", ctypes.c_uint64),
+                ("guide_train_steps", ctypes.c_uint64), ("ms_guide_infer", ctypes.c_double),
+                ("ms_guide_train", ctypes.c_double)]
+
+
+class GuideInfo(ctypes.Structure):
+    _fields_ = [("n_params", ctypes.c_uint64), ("n_table", ctypes.c_uint64), ("log2_table", ctypes.c_uint32),
+                ("levels", ctypes.c_uint32), ("level_res", ctypes.c_uint32 * 16), ("lo", ctypes.c_float * 3),
+                ("hi", ctypes.c_float * 3), ("adam_steps", ctypes.c_uint64), ("device_bytes", ctypes.c_uint64)]
 
 
 _lib = None
@@ -112,6 +122,13 @@ def load(path=LIB_PATH):
         "rad_camera_rays": [P, P, I64, ctypes.c_uint32, ctypes.c_uint32, P],
         "rad_render_samples": [P, P, P, I64, ctypes.c_uint32, P],
         "rad_render_samples_noalloc": [P, P, P, I64, ctypes.c_uint32, P, P],
+        "rad_guide_enable": [P, ctypes.c_char_p],
+        "rad_guide_info": [P, P],
+        "rad_guide_checkpoint": [P, P, ctypes.c_size_t, P],
+        "rad_guide_load": [P, P, ctypes.c_size_t],
+        "rad_guide_forward": [P, P, I64, P, P],
+        "rad_guide_mix_eval": [P, P, P, I64, P, P],
+        "rad_guide_grad": [P, P, I64, P, P],
     }
     for name, args in sig.items():
         fn = getattr(L, name)

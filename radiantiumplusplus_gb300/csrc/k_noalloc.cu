@@ -50,7 +50,7 @@ std::mutex g_mu;
 NoAllocScratch* g_addr[kMaxDevices] = {nullptr};
 
 PathBuffers ScratchBuffers(NoAllocScratch* s) {
-  PathBuffers B;
+  PathBuffers B{};
   B.rayO = s->rayO;
   B.rayD = s->rayD;
   B.thr = s->thr;

@@ -135,12 +135,79 @@ __global__ void __launch_bounds__(kBlock, 8) KExtend(DevScene S, PathBuffers B, 
   if (COUNT) FlushTravCounts(trav, nN, nP);
 }
 
+// Guided scattering at a non-emitter hit (one-sample MIS between the guide
+// mixture and the BSDF, dguide.cuh): draws the selection, samples the chosen
+// strategy, weights by f cos / p_mix, applies Russian roulette as Path::Li does
+// (path.cpp:213-219), writes the next ray and, on training paths, appends a
+// training record (linked to this vertex's shadow record so the shadow stage
+// can add the NEE radiance it owes the record). Returns whether the path continues.
+template <int K>
+__device__ __forceinline__ bool GuidedScatter(const DevScene& S, const PathBuffers& B, const GuideDev& G, int depth,
+                                              uint32_t p, const SurfInt& si, V3 D, const MatRec* mats, uint32_t bsdf,
+                                              const float4* gmix, float gc, V3 thr, float eta, Pcg32& rng,
+                                              bool shadow, float4& shC) {
+  float us = Next1D(rng);
+  float xl = Next1D(rng);
+  V2 xd = Next2D(rng);
+  V3 f, wiW;
+  float pm, bpdf, etaS = 1.f;
+  bool delta = false, ok;
+  if (us < gc) {
+    wiW = GuideMixSamplePacked(gmix, xl, xd);
+    V3 wl = ToLocal(si.sh, wiW);
+    ClassEvalPdf<K>(mats, bsdf, si.Wi, wl, f, bpdf);
+    pm = gc * GuideMixPdfPacked(gmix, wiW) + (1.f - gc) * bpdf;
+    ok = pm > 0.f && !is_zero(f);
+  } else {
+    BsdfSampleRes bs = ClassSample<K>(mats, bsdf, si.Wi, xl, xd);
+    f = bs.f;
+    bpdf = bs.pdf;
+    etaS = bs.eta;
+    delta = (bs.type & BT_DELTA) != 0u;
+    wiW = ToWorld(si.sh, bs.wo);
+    pm = delta ? (1.f - gc) * bs.pdf : gc * GuideMixPdfPacked(gmix, wiW) + (1.f - gc) * bs.pdf;
+    ok = bs.pdf > 0.f && pm > 0.f;
+  }
+  if (!ok) return false;
+  V3 thr0 = thr;
+  thr = cmul(thr, f) / pm;
+  eta *= etaS;
+  if (depth >= S.rrDepth) {
+    float rr = fminr(max_comp(thr) * Sqr(eta), 0.95f);
+    if (Next1D(rng) > rr) return false;
+    thr = thr * Rcp(rr);
+  }
+  V3 no = OffsetP(si.P, si.N, wiW);
+  B.rayO[p] = make_float4(no.x, no.y, no.z, 0.f);
+  B.rayD[p] = make_float4(wiW.x, wiW.y, wiW.z, kFloatMax);
+  B.thr[p] = make_float4(thr.x, thr.y, thr.z, eta);
+  B.prev[p] = make_float4(si.P.x, si.P.y, si.P.z, __uint_as_float(delta ? 1u : 0u));
+  B.rng[p] = make_uint2((uint32_t)rng.state, (uint32_t)(rng.state >> 32));
+  float4 L4 = B.L[p];
+  B.L[p] = make_float4(L4.x, L4.y, L4.z, pm);
+  if (G.train && !delta && (uint32_t)depth < G.trainDepth &&
+      (G.trainShift == 0u || (GuideHash32(B.pixel[p] ^ G.trainSalt) >> (32u - G.trainShift)) == 0u)) {
+    uint32_t slot = atomicAdd(G.ctl, 1u);
+    if (slot < G.recCap) {
+      float4* r = G.rec + (size_t)slot * kGRecF4;
+      r[0] = make_float4(si.P.x, si.P.y, si.P.z, bpdf);
+      r[1] = make_float4(si.sh.N.x, si.sh.N.y, si.sh.N.z, __uint_as_float(p));
+      r[2] = make_float4(-D.x, -D.y, -D.z, pm);
+      r[3] = make_float4(wiW.x, wiW.y, wiW.z, 0.f);
+      r[4] = make_float4(L4.x, L4.y, L4.z, 0.f);
+      r[5] = make_float4(thr0.x, thr0.y, thr0.z, 0.f);
+      if (shadow) shC.w = __uint_as_float(slot + 1u);
+    }
+  }
+  return true;
+}
+
 // Path::Li for one bounce, for the paths of shade class K (path.cpp:141-225).
 // SC_EMIT: misses, emitter hits, shapes without a BSDF and the last bounce --
 // emitter MIS only, then the path ends. Other classes: hits on a non-emitter
 // shape with a BSDF of that class -- NEE, BSDF sample, Russian roulette.
-template <int K>
-__global__ void __launch_bounds__(kBlock) KShadeClass(DevScene S, PathBuffers B, int depth) {
+template <int K, bool GUIDED>
+__global__ void __launch_bounds__(kBlock) KShadeClass(DevScene S, PathBuffers B, GuideDev G, int depth) {
   uint32_t count = B.counters[kClassBase + depth * kShadeClasses + K];
   const uint32_t* qin = B.classQ + (size_t)K * B.capacity;
   uint32_t* qout = B.q[(depth + 1) & 1];
@@ -203,6 +270,12 @@ __global__ void __launch_bounds__(kBlock) KShadeClass(DevScene S, PathBuffers B,
         SurfInt si = ComputeSI(S, O, D, th);
         uint32_t bsdf = (uint32_t)S.shapes[h.shape].bsdf;
         const MatRec* mats = S.mats;
+        const float4* gmix = nullptr;
+        float gc = 0.f;
+        if constexpr (GUIDED) {
+          gmix = G.mix + (size_t)p * kGMixF4;
+          gc = gmix[10].x;
+        }
         if (mats[bsdf].flags & BT_NODELTA) {
           float xl = Next1D(rng);
           V2 xd = Next2D(rng);
@@ -213,6 +286,7 @@ __global__ void __launch_bounds__(kBlock) KShadeClass(DevScene S, PathBuffers B,
             V3 f;
             float bsdfPdf;
             ClassEvalPdf<K>(mats, bsdf, si.Wi, wo, f, bsdfPdf);
+            if constexpr (GUIDED) bsdfPdf = gc * GuideMixPdfPacked(gmix, dsr.Dir) + (1.f - gc) * bsdfPdf;
             // Scene::IsOcclude (scene.cpp:53-63)
             V3 so = OffsetP(si.P, si.N, dsr.P - si.P);
             V3 sd = dsr.P - so;
@@ -228,6 +302,9 @@ __global__ void __launch_bounds__(kBlock) KShadeClass(DevScene S, PathBuffers B,
             }
           }
         }
+        if constexpr (GUIDED) {
+          keep = GuidedScatter<K>(S, B, G, depth, p, si, D, mats, bsdf, gmix, gc, thr, eta, rng, shadow, shC);
+        } else {
         float xl = Next1D(rng);
         V2 xd = Next2D(rng);
         BsdfSampleRes bs = ClassSample<K>(mats, bsdf, si.Wi, xl, xd);
@@ -256,6 +333,7 @@ __global__ void __launch_bounds__(kBlock) KShadeClass(DevScene S, PathBuffers B,
             float4 L4 = B.L[p];
             B.L[p] = make_float4(L4.x, L4.y, L4.z, bs.pdf);
           }
+        }
         }
       }
     }
@@ -287,6 +365,12 @@ __global__ void __launch_bounds__(kBlock, 8) KShadow(DevScene S, PathBuffers B, 
       float4 c = B.shC[i];
       float4 l = B.L[p];
       B.L[p] = make_float4(l.x + c.x, l.y + c.y, l.z + c.z, l.w);
+      uint32_t rec = __float_as_uint(c.w);  // guide training record + 1, or 0
+      if (rec) {
+        float4* r4 = B.guideRec + (size_t)(rec - 1u) * kGRecF4 + 4;
+        float4 lb = *r4;
+        *r4 = make_float4(lb.x + c.x, lb.y + c.y, lb.z + c.z, lb.w);
+      }
     }
   }
   if (COUNT) FlushTravCounts(trav + 2, nN, nP);
@@ -362,13 +446,22 @@ cudaError_t LaunchExtend(const DevScene& S, const PathBuffers& B, int depth, int
     KExtend<false><<<grid, kBlock, 0, st>>>(S, B, depth, nullptr);
   return cudaGetLastError();
 }
-cudaError_t LaunchShade(const DevScene& S, const PathBuffers& B, int depth, int grid, cudaStream_t st) {
-  KShadeClass<SC_EMIT><<<grid, kBlock, 0, st>>>(S, B, depth);
-  KShadeClass<SC_DIFFUSE><<<grid, kBlock, 0, st>>>(S, B, depth);
-  KShadeClass<SC_METAL><<<grid, kBlock, 0, st>>>(S, B, depth);
-  KShadeClass<SC_GLASS><<<grid, kBlock, 0, st>>>(S, B, depth);
-  KShadeClass<SC_DISNEY><<<grid, kBlock, 0, st>>>(S, B, depth);
-  KShadeClass<SC_GENERIC><<<grid, kBlock, 0, st>>>(S, B, depth);
+cudaError_t LaunchShade(const DevScene& S, const PathBuffers& B, int depth, int grid, cudaStream_t st,
+                        const GuideDev* G) {
+  GuideDev none{};
+  KShadeClass<SC_EMIT, false><<<grid, kBlock, 0, st>>>(S, B, none, depth);
+  KShadeClass<SC_GLASS, false><<<grid, kBlock, 0, st>>>(S, B, none, depth);
+  if (G) {
+    KShadeClass<SC_DIFFUSE, true><<<grid, kBlock, 0, st>>>(S, B, *G, depth);
+    KShadeClass<SC_METAL, true><<<grid, kBlock, 0, st>>>(S, B, *G, depth);
+    KShadeClass<SC_DISNEY, true><<<grid, kBlock, 0, st>>>(S, B, *G, depth);
+    KShadeClass<SC_GENERIC, true><<<grid, kBlock, 0, st>>>(S, B, *G, depth);
+  } else {
+    KShadeClass<SC_DIFFUSE, false><<<grid, kBlock, 0, st>>>(S, B, none, depth);
+    KShadeClass<SC_METAL, false><<<grid, kBlock, 0, st>>>(S, B, none, depth);
+    KShadeClass<SC_DISNEY, false><<<grid, kBlock, 0, st>>>(S, B, none, depth);
+    KShadeClass<SC_GENERIC, false><<<grid, kBlock, 0, st>>>(S, B, none, depth);
+  }
   return cudaGetLastError();
 }
 cudaError_t LaunchShadow(const DevScene& S, const PathBuffers& B, int depth, int grid, cudaStream_t st,

@@ -3,6 +3,7 @@
 #include <cuda_runtime.h>
 #include <stdint.h>
 
+#include "dguide.cuh"
 #include "records.h"
 
 namespace rad {
@@ -25,6 +26,7 @@ struct PathBuffers {
   uint32_t* counters;  // [0, kMaxBounce]: active counts; [kShadowBase, +kMaxBounce]: shadow counts; kMisc..;
                        // [kClassBase + depth * kShadeClasses + class]: shade-class counts
   uint32_t capacity;
+  float4* guideRec;    // guide training records (shadow stage adds NEE into them), or null
 };
 
 constexpr int kMaxBounce = 256;
@@ -77,7 +79,9 @@ cudaError_t LaunchGenerate(const DevScene& S, const PathBuffers& B, const WavePa
 // trav (optional, 4 x u64): extend node visits, extend prim tests, shadow node visits, shadow prim tests
 cudaError_t LaunchExtend(const DevScene& S, const PathBuffers& B, int depth, int grid, cudaStream_t st,
                          unsigned long long* trav = nullptr);
-cudaError_t LaunchShade(const DevScene& S, const PathBuffers& B, int depth, int grid, cudaStream_t st);
+// G (optional): guide network; its classes then sample the one-sample MIS mixture.
+cudaError_t LaunchShade(const DevScene& S, const PathBuffers& B, int depth, int grid, cudaStream_t st,
+                        const GuideDev* G = nullptr);
 cudaError_t LaunchShadow(const DevScene& S, const PathBuffers& B, int depth, int grid, cudaStream_t st,
                          unsigned long long* trav = nullptr);
 cudaError_t LaunchAccumulate(const PathBuffers& B, const FilmView& film, uint32_t count, cudaStream_t st,
@@ -88,5 +92,27 @@ cudaError_t LaunchResolveFilm(const FilmView& film, float scale, float* out, cud
 // ---- volumetric path tracer (k_vol.cu): one thread per path, full Li loop
 cudaError_t LaunchVolPath(const DevScene& S, const PathBuffers& B, const WaveParams& w, uint32_t* err,
                           cudaStream_t st);
+
+// ---- guide network (k_guide.cu)
+cudaError_t GuideKernelsInit();
+cudaError_t LaunchGuideInfer(const DevScene& S, const PathBuffers& B, const GuideDev& G, int depth, uint32_t maxCount,
+                             cudaStream_t st);
+cudaError_t LaunchGuideQuery(const GuideDev& G, const float* queries, uint32_t n, float* raw, float4* mix,
+                             cudaStream_t st);
+cudaError_t LaunchGuideMixEval(const float4* mix, const float* dirs, const float* u, uint32_t n, float* pdf,
+                               float* outDirs, cudaStream_t st);
+cudaError_t LaunchGuideFinalize(const PathBuffers& B, const GuideDev& G, cudaStream_t st);
+// One training batch: records j * steps + step. With ctl, the count and the
+// mean weight come from the device (ctl[0], ctl[1]); else `count`, weights as given.
+cudaError_t LaunchGuideTrain(const GuideDev& G, const float4* rec, const uint32_t* ctl, uint32_t count, uint32_t cap,
+                             uint32_t steps, uint32_t step, float wClamp, float* gradTable, float* gradW,
+                             float* lossOut, uint32_t maxBatch, cudaStream_t st);
+// Adam step t (1-based). With ctl, the gradient scale is 1 / (size of batch `step`
+// of `steps`) from the device record count, and an empty batch changes nothing.
+// Parameters [0, split) step with lr, [split, n) with lr2.
+cudaError_t LaunchGuideAdam(float* p, float* m, float* v, float* g, __half* ph, uint64_t n, float lr, uint64_t split,
+                            float lr2, float b1, float b2, float eps, float gscale, uint32_t t, const uint32_t* ctl,
+                            uint32_t cap, uint32_t steps, uint32_t step, cudaStream_t st);
+cudaError_t LaunchFloatToHalf(const float* src, __half* dst, uint64_t n, cudaStream_t st);
 
 }  // namespace rad

@@ -20,6 +20,7 @@
 #include <vector>
 
 #include "../../include/radgpu.h"
+#include "guide_net.h"
 #include "host_scene.h"
 #include "kernels.h"
 
@@ -87,6 +88,8 @@ T* DevAlloc(size_t count, std::vector<void*>& owner, uint64_t& bytes) {
 }
 
 enum JobState { kQueued, kRunning, kCompleting, kDone };
+// device job counters: [0..3] rays, invalid, samples; [4..7] traversal; [8] guide records
+constexpr int kJobStatWords = 10;
 
 }  // namespace
 
@@ -96,6 +99,9 @@ struct rad_scene {
   uint64_t bytes = 0;
   rad_scene_info info{};
   std::atomic<int> jobs{0};
+  float worldLo[3] = {0, 0, 0}, worldHi[3] = {1, 1, 1};
+  GuideNet* guide = nullptr;  // learned proposal, created by rad_guide_enable / _load or a guided job
+  GuideConfig guideCfg;
 };
 
 struct rad_job {
@@ -119,6 +125,7 @@ struct rad_job {
   rad_stats stats{};
   std::vector<std::pair<cudaEvent_t, cudaEvent_t>> profEv;
   std::vector<int> profKind;
+  uint32_t trainSamples = 0;  // guided jobs train during their first trainSamples samples
   // CUDA graph per pixel chunk: one captured wave replayed once per sample
   WaveCtx* ctx = nullptr;  // device, one per chunk
   std::vector<cudaGraphExec_t> graphs;
@@ -151,6 +158,11 @@ struct Lib {
   size_t rr = 0;
   bool stop = false;
   std::vector<cudaEvent_t> evPool;
+  // guide buffers, allocated with the first guided wave
+  float4* guideMix = nullptr;  // kGMixF4 per path slot
+  float4* guideRec = nullptr;
+  uint32_t guideRecCap = 0;
+  uint64_t guideBytes = 0;
 };
 
 // Never destroyed: at process exit the worker thread may still be parked on
@@ -222,6 +234,7 @@ void InitLocked(const char* cfg) {
   Check(cudaSetDevice(lib.device), "cudaSetDevice");
   Check(cudaDeviceGetAttribute(&lib.sms, cudaDevAttrMultiProcessorCount, lib.device), "attribute");
   Check(cudaStreamCreateWithFlags(&lib.stream, cudaStreamNonBlocking), "cudaStreamCreate");
+  Check(GuideKernelsInit(), "guide kernel attributes");
   AllocPaths(lib);
   lib.stop = false;
   lib.worker = std::thread(WorkerMain);
@@ -252,7 +265,8 @@ struct ProfSink {
 };
 
 // Launches the bounce loop for `count` generated paths. Returns kernels launched.
-uint64_t LaunchBounces(const DevScene& S, uint32_t count, ProfSink& ps, unsigned long long* trav = nullptr) {
+uint64_t LaunchBounces(const DevScene& S, uint32_t count, ProfSink& ps, unsigned long long* trav = nullptr,
+                       const GuideDev* G = nullptr) {
   Lib& lib = L();
   uint64_t launches = 0;
   int grid = std::max(1, std::min(lib.sms * 8, (int)((count + 127) / 128)));
@@ -263,8 +277,14 @@ uint64_t LaunchBounces(const DevScene& S, uint32_t count, ProfSink& ps, unsigned
     ps.Begin(1, a);
     Check(LaunchExtend(S, lib.paths, d, grid, lib.stream, trav), "extend");
     ps.End(1, a);
+    if (G) {
+      ps.Begin(6, a);
+      Check(LaunchGuideInfer(S, lib.paths, *G, d, count, lib.stream), "guide inference");
+      ps.End(6, a);
+      launches++;
+    }
     ps.Begin(2, a);
-    Check(LaunchShade(S, lib.paths, d, grid, lib.stream), "shade");
+    Check(LaunchShade(S, lib.paths, d, grid, lib.stream, G), "shade");
     ps.End(2, a);
     ps.Begin(3, a);
     Check(LaunchShadow(S, lib.paths, d, grid, lib.stream, trav), "shadow");
@@ -286,7 +306,102 @@ uint64_t LaunchBounces(const DevScene& S, uint32_t count, ProfSink& ps, unsigned
 // or traversal counting (those record events / host readbacks per launch).
 bool GraphEligible(const rad_job* j) {
   const DevScene& S = j->scene->dev;
-  return !S.isVol && S.maxDepth >= 0 && !(j->flags & (RAD_JOB_PROFILE_KERNELS | RAD_JOB_COUNT_TRAVERSAL));
+  return !S.isVol && S.maxDepth >= 0 &&
+         !(j->flags & (RAD_JOB_PROFILE_KERNELS | RAD_JOB_COUNT_TRAVERSAL | RAD_JOB_GUIDE));
+}
+
+GuideNet& EnsureGuide(rad_scene* sc) {
+  if (!sc->guide) {
+    try {
+      sc->guide = GuideCreate(sc->guideCfg, sc->worldLo, sc->worldHi);
+    } catch (const std::runtime_error& e) {
+      throw Error{RAD_ERR_CUDA, e.what()};
+    }
+    L().used += sc->guide->bytes;
+  }
+  return *sc->guide;
+}
+
+void EnsureGuideBuffers(Lib& lib, uint32_t recCap) {
+  if (!lib.guideMix) {
+    Check(cudaMalloc(&lib.guideMix, (size_t)lib.maxPaths * kGMixF4 * sizeof(float4)), "guide mixtures");
+    lib.guideBytes += (uint64_t)lib.maxPaths * kGMixF4 * sizeof(float4);
+  }
+  if (lib.guideRecCap < recCap) {
+    if (lib.guideRec) {
+      cudaFree(lib.guideRec);
+      lib.guideBytes -= (uint64_t)lib.guideRecCap * kGRecF4 * sizeof(float4);
+    }
+    lib.guideRec = nullptr;
+    lib.guideRecCap = 0;
+    Check(cudaMalloc(&lib.guideRec, (size_t)recCap * kGRecF4 * sizeof(float4)), "guide records");
+    lib.guideRecCap = recCap;
+    lib.guideBytes += (uint64_t)recCap * kGRecF4 * sizeof(float4);
+  }
+  lib.paths.guideRec = lib.guideRec;
+}
+
+// Training steps after a guided training wave: record weights, then
+// cfg.stepsPerWave Adam steps, each on every stepsPerWave-th record.
+void GuideTrainWave(GuideNet& net, const GuideDev& G, ProfSink& ps, rad_job* j) {
+  Lib& lib = L();
+  cudaEvent_t a = nullptr;
+  ps.Begin(7, a);
+  Check(LaunchGuideFinalize(lib.paths, G, lib.stream), "guide finalize");
+  uint32_t S = net.cfg.stepsPerWave;
+  uint32_t maxBatch = (G.recCap + S - 1) / S;
+  for (uint32_t s = 0; s < S; s++) {
+    Check(LaunchGuideTrain(G, G.rec, G.ctl, 0, G.recCap, S, s, net.cfg.weightClamp, net.g, net.g + net.nTable,
+                           reinterpret_cast<float*>(net.ctl + 2), maxBatch, lib.stream),
+          "guide train");
+    net.step++;
+    Check(LaunchGuideAdam(net.p, net.m, net.v, net.g, net.ph, net.nParams, net.cfg.lr, net.nTable, net.cfg.lrMlp,
+                          net.cfg.beta1, net.cfg.beta2, net.cfg.eps, 1.f, net.step, G.ctl, G.recCap, S, s, lib.stream),
+          "guide adam");
+  }
+  ps.End(7, a);
+  j->stats.kernel_launches += 1 + 2 * S;
+  j->stats.guide_train_steps += S;
+}
+
+// A guided wave: the bounce loop with the guide inference stage, then (while
+// the job is in its training fraction) the training steps on its records.
+void RunWaveGuided(rad_job* j) {
+  Lib& lib = L();
+  const DevScene& S = j->scene->dev;
+  GuideNet& net = EnsureGuide(j->scene);
+  EnsureGuideBuffers(lib, net.cfg.recCap);
+  uint32_t W = (uint32_t)S.cam.width, H = (uint32_t)S.cam.height;
+  uint64_t npix = (uint64_t)W * H;
+  ProfSink ps{j};
+  FilmView film{j->accum, (int32_t)W, (int32_t)H, j->dStats};
+  bool train = j->nextSample < j->trainSamples;
+  for (uint64_t p0 = 0; p0 < npix; p0 += lib.maxPaths) {
+    uint32_t count = (uint32_t)std::min<uint64_t>(lib.maxPaths, npix - p0);
+    uint32_t smp = j->first + j->nextSample;
+    WaveParams w{(uint32_t)p0, count, smp, j->seed, nullptr, nullptr};
+    GuideDev G = GuideView(net);
+    G.mix = lib.guideMix;
+    G.rec = lib.guideRec;
+    G.recCap = net.cfg.recCap;
+    G.train = train ? 1u : 0u;
+    G.trainSalt = GuideHash32(smp * 0x9e3779b9u + j->seed * 0x85ebca6bu + (uint32_t)p0);
+    G.recTotal = j->dStats + 8;
+    if (train) Check(cudaMemsetAsync(net.ctl, 0, 4 * sizeof(uint32_t), lib.stream), "guide control reset");
+    cudaEvent_t a = nullptr;
+    ps.Begin(0, a);
+    Check(LaunchGenerate(S, lib.paths, w, lib.stream), "generate");
+    ps.End(0, a);
+    uint64_t launches = 1 + LaunchBounces(S, count, ps, nullptr, &G);
+    ps.Begin(4, a);
+    Check(LaunchAccumulate(lib.paths, film, count, lib.stream), "accumulate");
+    ps.End(4, a);
+    launches++;
+    j->stats.kernel_launches += launches;
+    if (train) GuideTrainWave(net, G, ps, j);
+  }
+  j->nextSample++;
+  j->launched += npix;
 }
 
 // Runs the job's next sample over its pixels as replays of one captured graph
@@ -344,6 +459,10 @@ void RunWaveGraph(rad_job* j) {
 void RunWave(rad_job* j) {
   if (GraphEligible(j)) {
     RunWaveGraph(j);
+    return;
+  }
+  if ((j->flags & RAD_JOB_GUIDE) && !j->scene->dev.isVol) {
+    RunWaveGuided(j);
     return;
   }
   Lib& lib = L();
@@ -407,8 +526,9 @@ void CompleteJob(rad_job* j) {
   j->stats.trav_prims_closest = j->hStats[5];
   j->stats.trav_nodes_shadow = j->hStats[6];
   j->stats.trav_prims_shadow = j->hStats[7];
-  double acc[6] = {0, 0, 0, 0, 0, 0};
-  uint64_t cnt[6] = {0, 0, 0, 0, 0, 0};
+  j->stats.guide_records = j->hStats[8];
+  double acc[8] = {0, 0, 0, 0, 0, 0, 0, 0};
+  uint64_t cnt[8] = {0, 0, 0, 0, 0, 0, 0, 0};
   for (size_t k = 0; k < j->profEv.size(); k++) {
     float e = 0;
     cudaEventElapsedTime(&e, j->profEv[k].first, j->profEv[k].second);
@@ -425,6 +545,8 @@ void CompleteJob(rad_job* j) {
   j->stats.ms_shadow = acc[3];
   j->stats.ms_accumulate = acc[4];
   j->stats.ms_volpath = acc[5];
+  j->stats.ms_guide_infer = acc[6];
+  j->stats.ms_guide_train = acc[7];
   j->stats.n_extend = cnt[1];
   j->stats.n_shade = cnt[2];
   j->stats.n_shadow = cnt[3];
@@ -454,11 +576,11 @@ void AllocJobFilm(rad_job* j) {
   const DevScene& S = j->scene->dev;
   size_t npix = (size_t)S.cam.width * S.cam.height;
   Check(cudaMalloc(&j->accum, npix * sizeof(float4)), "film");
-  Check(cudaMalloc(&j->dStats, 8 * sizeof(unsigned long long)), "stats");
-  Check(cudaMallocHost(&j->hStats, 8 * sizeof(unsigned long long)), "stats host");
-  std::memset(j->hStats, 0, 8 * sizeof(unsigned long long));
+  Check(cudaMalloc(&j->dStats, kJobStatWords * sizeof(unsigned long long)), "stats");
+  Check(cudaMallocHost(&j->hStats, kJobStatWords * sizeof(unsigned long long)), "stats host");
+  std::memset(j->hStats, 0, kJobStatWords * sizeof(unsigned long long));
   Check(cudaMemsetAsync(j->accum, 0, npix * sizeof(float4), L().stream), "memset film");
-  Check(cudaMemsetAsync(j->dStats, 0, 8 * sizeof(unsigned long long), L().stream), "memset stats");
+  Check(cudaMemsetAsync(j->dStats, 0, kJobStatWords * sizeof(unsigned long long), L().stream), "memset stats");
   Check(cudaEventCreate(&j->evStart), "event");
   Check(cudaEventCreate(&j->evEnd), "event");
 }
@@ -472,7 +594,8 @@ void StartJob(rad_job* j) {
 }
 
 void EndJobLaunch(rad_job* j) {
-  Check(cudaMemcpyAsync(j->hStats, j->dStats, 8 * sizeof(unsigned long long), cudaMemcpyDeviceToHost, L().stream),
+  Check(cudaMemcpyAsync(j->hStats, j->dStats, kJobStatWords * sizeof(unsigned long long), cudaMemcpyDeviceToHost,
+                        L().stream),
         "stats readback");
   Check(cudaEventRecord(j->evEnd, L().stream), "event record");
   j->state = kCompleting;
@@ -682,6 +805,12 @@ int rad_shutdown(void) {
     FreeAll(lib.pathAllocs);
     lib.used -= lib.pathBytes;
     lib.pathBytes = 0;
+    if (lib.guideMix) cudaFree(lib.guideMix);
+    if (lib.guideRec) cudaFree(lib.guideRec);
+    lib.guideMix = nullptr;
+    lib.guideRec = nullptr;
+    lib.guideRecCap = 0;
+    lib.guideBytes = 0;
     if (lib.hCounters) cudaFreeHost(lib.hCounters);
     lib.hCounters = nullptr;
     for (cudaEvent_t e : lib.evPool) cudaEventDestroy(e);
@@ -742,6 +871,12 @@ int rad_scene_load_json(const char* json_text, const char* base_dir, rad_scene**
     in.n_prims = hs.nPrims;
     in.n_bvh_nodes = hs.nodes.size();
     in.device_bytes = sc->bytes;
+    for (int a = 0; a < 3; a++) {
+      // guide position normalisation box: world bounds, widened by 0.1 % per side
+      float e = std::max(hs.worldHi[a] - hs.worldLo[a], 1e-3f);
+      sc->worldLo[a] = hs.worldLo[a] - 1e-3f * e;
+      sc->worldHi[a] = hs.worldHi[a] + 1e-3f * e;
+    }
     *out = sc;
   });
 }
@@ -766,6 +901,10 @@ int rad_scene_destroy(rad_scene* scene) {
     cudaStreamSynchronize(lib.stream);
     FreeAll(scene->allocs);
     lib.used -= scene->bytes;
+    if (scene->guide) {
+      lib.used -= scene->guide->bytes;
+      GuideDestroy(scene->guide);
+    }
     delete scene;
   });
 }
@@ -794,6 +933,8 @@ int rad_job_submit(rad_scene* scene, const rad_job_desc* desc, rad_job** out) {
     j->seed = desc && desc->seed != UINT32_MAX ? desc->seed : scene->info.seed;
     j->first = desc ? desc->first_sample : 0;
     j->flags = desc ? desc->flags : 0;
+    if (j->flags & RAD_JOB_GUIDE)
+      j->trainSamples = (uint32_t)std::ceil((double)scene->guideCfg.trainFraction * (double)j->spp);
     uint64_t npix = (uint64_t)scene->info.width * scene->info.height;
     j->total = npix * j->spp;
     j->filmBytes = npix * sizeof(float4) + 64;
@@ -1042,6 +1183,173 @@ int rad_render_samples(rad_scene* scene, const uint32_t* pixels, const uint32_t*
     Check(cudaMemcpyAsync(&err, lib.paths.counters + kMiscBase + 1, 4, cudaMemcpyDeviceToHost, lib.stream), "copy");
     Check(cudaStreamSynchronize(lib.stream), "sync");
     if (err) throw Error{RAD_ERR_DEVICE_CHECK, "device-side bound exceeded, code " + std::to_string(err)};
+  });
+}
+
+// ---- learned path guiding ----------------------------------------------------
+int rad_guide_enable(rad_scene* scene, const char* config_json) {
+  if (!scene) return Fail(RAD_ERR_INVALID_ARG, "null scene");
+  return Guard([&] {
+    EnsureInit();
+    GuideConfig cfg;
+    try {
+      GuideParseConfig(config_json, cfg);
+    } catch (const std::runtime_error& e) {
+      throw Error{RAD_ERR_INVALID_ARG, e.what()};
+    }
+    Lib& lib = L();
+    std::lock_guard<std::mutex> g(lib.gpuMu);
+    if (scene->jobs.load() > 0) throw Error{RAD_ERR_INVALID_ARG, "scene has live jobs"};
+    cudaStreamSynchronize(lib.stream);
+    if (scene->guide) {
+      lib.used -= scene->guide->bytes;
+      GuideDestroy(scene->guide);
+      scene->guide = nullptr;
+    }
+    scene->guideCfg = cfg;
+    EnsureGuide(scene);
+  });
+}
+
+int rad_guide_checkpoint(rad_scene* scene, void* buf, size_t size, size_t* needed) {
+  if (!scene) return Fail(RAD_ERR_INVALID_ARG, "null scene");
+  return Guard([&] {
+    Lib& lib = L();
+    std::lock_guard<std::mutex> g(lib.gpuMu);
+    if (!scene->guide) throw Error{RAD_ERR_NOT_READY, "scene has no guide network"};
+    size_t n = GuideCheckpointBytes(*scene->guide);
+    if (needed) *needed = n;
+    if (!buf) return;
+    if (size < n) throw Error{RAD_ERR_INVALID_ARG, "checkpoint buffer too small"};
+    cudaStreamSynchronize(lib.stream);
+    try {
+      GuideCheckpoint(*scene->guide, buf, lib.stream);
+    } catch (const std::runtime_error& e) {
+      throw Error{RAD_ERR_CUDA, e.what()};
+    }
+  });
+}
+
+int rad_guide_load(rad_scene* scene, const void* buf, size_t size) {
+  if (!scene || !buf) return Fail(RAD_ERR_INVALID_ARG, "null argument");
+  return Guard([&] {
+    EnsureInit();
+    Lib& lib = L();
+    std::lock_guard<std::mutex> g(lib.gpuMu);
+    if (scene->jobs.load() > 0) throw Error{RAD_ERR_INVALID_ARG, "scene has live jobs"};
+    cudaStreamSynchronize(lib.stream);
+    GuideNet* n = nullptr;
+    try {
+      n = GuideFromCheckpoint(buf, size, scene->guideCfg, lib.stream);
+    } catch (const std::runtime_error& e) {
+      throw Error{RAD_ERR_INVALID_ARG, e.what()};
+    }
+    if (scene->guide) {
+      lib.used -= scene->guide->bytes;
+      GuideDestroy(scene->guide);
+    }
+    scene->guide = n;
+    scene->guideCfg = n->cfg;
+    lib.used += n->bytes;
+  });
+}
+
+int rad_guide_forward(rad_scene* scene, const float* queries, int64_t n, float* raw, float* mix) {
+  if (!scene || n < 0 || (n > 0 && !queries)) return Fail(RAD_ERR_INVALID_ARG, "bad argument");
+  if (n == 0) return RAD_OK;
+  if (n > (int64_t)UINT32_MAX) return Fail(RAD_ERR_INVALID_ARG, "too many queries");
+  return Guard([&] {
+    EnsureInit();
+    Lib& lib = L();
+    std::lock_guard<std::mutex> g(lib.gpuMu);
+    GuideNet& net = EnsureGuide(scene);
+    DevBuf<float> dq(9 * n), draw(raw ? (size_t)kGOut * n : 0);
+    DevBuf<float4> dmix(mix ? (size_t)kGMixF4 * n : 0);
+    Check(cudaMemcpyAsync(dq.p, queries, 36 * n, cudaMemcpyHostToDevice, lib.stream), "copy");
+    GuideDev G = GuideView(net);
+    Check(LaunchGuideQuery(G, dq.p, (uint32_t)n, draw.p, dmix.p, lib.stream), "guide query");
+    if (raw) Check(cudaMemcpyAsync(raw, draw.p, sizeof(float) * kGOut * n, cudaMemcpyDeviceToHost, lib.stream), "copy");
+    if (mix)
+      Check(cudaMemcpyAsync(mix, dmix.p, sizeof(float4) * kGMixF4 * n, cudaMemcpyDeviceToHost, lib.stream), "copy");
+    Check(cudaStreamSynchronize(lib.stream), "sync");
+  });
+}
+
+int rad_guide_mix_eval(const float* mix, const float* dirs, const float* u, int64_t n, float* pdf, float* out_dirs) {
+  if (!mix || !pdf || n < 0 || (!dirs && !u) || (dirs && u) || (u && !out_dirs))
+    return Fail(RAD_ERR_INVALID_ARG, "bad argument");
+  if (n == 0) return RAD_OK;
+  return Guard([&] {
+    EnsureInit();
+    Lib& lib = L();
+    std::lock_guard<std::mutex> g(lib.gpuMu);
+    DevBuf<float4> dm((size_t)kGMixF4 * n);
+    DevBuf<float> dd(dirs ? 3 * n : 0), du(u ? 3 * n : 0), dp(n), dout(u ? 3 * n : 0);
+    Check(cudaMemcpyAsync(dm.p, mix, sizeof(float4) * kGMixF4 * n, cudaMemcpyHostToDevice, lib.stream), "copy");
+    if (dirs) Check(cudaMemcpyAsync(dd.p, dirs, 12 * n, cudaMemcpyHostToDevice, lib.stream), "copy");
+    if (u) Check(cudaMemcpyAsync(du.p, u, 12 * n, cudaMemcpyHostToDevice, lib.stream), "copy");
+    Check(LaunchGuideMixEval(dm.p, dd.p, du.p, (uint32_t)n, dp.p, dout.p, lib.stream), "mixture eval");
+    Check(cudaMemcpyAsync(pdf, dp.p, 4 * n, cudaMemcpyDeviceToHost, lib.stream), "copy");
+    if (u) Check(cudaMemcpyAsync(out_dirs, dout.p, 12 * n, cudaMemcpyDeviceToHost, lib.stream), "copy");
+    Check(cudaStreamSynchronize(lib.stream), "sync");
+  });
+}
+
+int rad_guide_grad(rad_scene* scene, const float* records, int64_t n, float* grad, float* loss) {
+  if (!scene || n < 0 || (n > 0 && !records) || !grad) return Fail(RAD_ERR_INVALID_ARG, "bad argument");
+  if (n > (int64_t)(1u << 26)) return Fail(RAD_ERR_INVALID_ARG, "too many records");
+  return Guard([&] {
+    EnsureInit();
+    Lib& lib = L();
+    std::lock_guard<std::mutex> g(lib.gpuMu);
+    GuideNet& net = EnsureGuide(scene);
+    // repack (P, b | N, - | wo, - | wi, w) rows into the kGRecF4 record layout
+    std::vector<float4> host((size_t)std::max<int64_t>(n, 1) * kGRecF4);
+    for (int64_t i = 0; i < n; i++)
+      for (int k = 0; k < 4; k++) {
+        const float* s = records + 16 * i + 4 * k;
+        host[(size_t)i * kGRecF4 + k] = make_float4(s[0], s[1], s[2], s[3]);
+      }
+    DevBuf<float4> drec(host.size());
+    DevBuf<float> dloss(1);
+    Check(cudaMemcpyAsync(drec.p, host.data(), host.size() * sizeof(float4), cudaMemcpyHostToDevice, lib.stream),
+          "copy");
+    Check(cudaMemsetAsync(dloss.p, 0, 4, lib.stream), "memset");
+    cudaStreamSynchronize(lib.stream);
+    Check(cudaMemsetAsync(net.g, 0, net.nParams * sizeof(float), lib.stream), "memset");
+    GuideDev G = GuideView(net);
+    if (n > 0)
+      Check(LaunchGuideTrain(G, drec.p, nullptr, (uint32_t)n, (uint32_t)n, 1, 0, INFINITY, net.g, net.g + net.nTable,
+                             dloss.p, (uint32_t)n, lib.stream),
+            "guide gradient");
+    Check(cudaMemcpyAsync(grad, net.g, net.nParams * sizeof(float), cudaMemcpyDeviceToHost, lib.stream), "copy");
+    float l = 0.f;
+    Check(cudaMemcpyAsync(&l, dloss.p, 4, cudaMemcpyDeviceToHost, lib.stream), "copy");
+    Check(cudaMemsetAsync(net.g, 0, net.nParams * sizeof(float), lib.stream), "memset");
+    Check(cudaStreamSynchronize(lib.stream), "sync");
+    if (loss) *loss = l;
+  });
+}
+
+int rad_guide_info(rad_scene* scene, rad_guide_info_t* info) {
+  if (!scene || !info) return Fail(RAD_ERR_INVALID_ARG, "null argument");
+  return Guard([&] {
+    Lib& lib = L();
+    std::lock_guard<std::mutex> g(lib.gpuMu);
+    if (!scene->guide) throw Error{RAD_ERR_NOT_READY, "scene has no guide network"};
+    const GuideNet& n = *scene->guide;
+    *info = rad_guide_info_t{};
+    info->n_params = n.nParams;
+    info->n_table = n.nTable;
+    info->log2_table = n.cfg.log2T;
+    info->levels = kGLevels;
+    for (int l = 0; l < kGLevels; l++) info->level_res[l] = n.res[l];
+    for (int a = 0; a < 3; a++) {
+      info->lo[a] = n.lo[a];
+      info->hi[a] = n.hi[a];
+    }
+    info->adam_steps = n.step;
+    info->device_bytes = n.bytes;
   });
 }
 

@@ -14,6 +14,9 @@ renderer, in this library and in the CPU oracle.
 * :func:`volume_box` -- the volumetric scene: an fBm density grid in a
   rough-dielectric box on a diffuse ground, a directional light plus a constant
   sky, ``vol_path`` renderer.
+* :func:`guided_room` -- hard indirect transport for path guiding: the
+  many-spheres field inside a closed cubic room lit only by a directional light
+  through a small square opening in the ceiling.
 """
 
 from __future__ import annotations
@@ -25,7 +28,7 @@ import struct
 
 import numpy as np
 
-__all__ = ["box_room", "many_spheres", "volume_box", "icosphere_obj", "write_scene"]
+__all__ = ["box_room", "many_spheres", "volume_box", "guided_room", "icosphere_obj", "write_scene"]
 
 
 def _rect(translate, rotate=None, scale=(1.0, 1.0, 1.0), **extra):
@@ -143,6 +146,64 @@ def many_spheres(n_spheres=10000, n_emitters=20, width=1920, height=1080, spp=25
         "camera": {"type": "perspective", "fov": 55.0, "resolution": [width, height], "far": 10 * extent,
                    "origin": [mid, mid, -0.4 * extent], "target": [mid, mid, mid], "up": [0.0, 1.0, 0.0]},
         "sampler": {"type": "independent", "sample_count": spp, "seed": sampler_seed},
+        "assets": [{"name": "ico", "type": "model_obj", "location": "ico.obj"}],
+        "scene": ents,
+        "accel": {"type": "embree"},
+        "renderer": {"type": "path", "max_depth": max_depth, "rr_depth": 3},
+    }
+    return scene, {"ico.obj": icosphere_obj(2)}
+
+
+def _sphere_bsdf(rng):
+    k = rng.uniform()
+    if k < 0.4:
+        return {"type": "diffuse", "reflectance": rng.uniform(0.1, 0.9, 3).round(6).tolist()}
+    if k < 0.7:
+        return {"type": "rough_metal", "alpha": round(float(rng.uniform(0.05, 0.5)), 6)}
+    if k < 0.9:
+        return {"type": "rough_glass", "int_ior": 1.5, "ext_ior": 1.0, "alpha": round(float(rng.uniform(0.0, 0.3)), 6)}
+    p = rng.uniform(size=14).round(6)
+    return {"type": "disney", "base_color": p[:3].tolist(), "roughness": float(p[3]), "anisotropic": float(p[4]),
+            "spec_trans": float(p[5]), "sheen": float(p[6]), "sheen_tint": float(p[7]), "flatness": float(p[8]),
+            "spec_tint": float(p[9]), "metallic": float(p[10]), "clearcoat": float(p[11]),
+            "clearcoat_gloss": float(p[12]), "specular": float(p[13])}
+
+
+def guided_room(n_spheres=10000, width=1920, height=1080, spp=64, max_depth=16, room=200.0, opening=5.0,
+                irradiance=1000.0, field=100.0, radius_scale=1.0, seed=5, sampler_seed=5):
+    """Closed room [0, room]^3 of grey Lambertian walls with a square `opening` in
+    the ceiling centre, the many-spheres field (icospheres with centres uniform in
+    a `field`^3 cube at the room centre, lognormal(0, 0.5) radii x radius_scale,
+    materials as in many_spheres), lit only by a directional light of the given
+    irradiance shining down through the opening. Returns (scene dict, {asset: text})."""
+    rng = np.random.default_rng(seed)
+    R, c, h = float(room), float(room) / 2.0, float(opening) / 2.0
+    wall = {"type": "diffuse", "reflectance": [0.7, 0.7, 0.7]}
+    ents = [
+        _rect((c, 0, c), ((1, 0, 0), -90), (c, c, 1), bsdf={"ref": "wall"}),          # floor, +y
+        _rect((c, c, 0), None, (c, c, 1), bsdf={"ref": "wall"}),                      # z = 0, +z
+        _rect((c, c, R), ((0, 1, 0), 180), (c, c, 1), bsdf={"ref": "wall"}),         # z = R, -z
+        _rect((0, c, c), ((0, 1, 0), 90), (c, c, 1), bsdf={"ref": "wall"}),           # x = 0, +x
+        _rect((R, c, c), ((0, 1, 0), -90), (c, c, 1), bsdf={"ref": "wall"}),          # x = R, -x
+        # ceiling (-y) as four strips around the opening
+        _rect((c, R, (c - h) / 2), ((1, 0, 0), 90), (c, (c - h) / 2, 1), bsdf={"ref": "wall"}),
+        _rect((c, R, (c + h + R) / 2), ((1, 0, 0), 90), (c, (R - c - h) / 2, 1), bsdf={"ref": "wall"}),
+        _rect(((c - h) / 2, R, c), ((1, 0, 0), 90), ((c - h) / 2, h, 1), bsdf={"ref": "wall"}),
+        _rect(((c + h + R) / 2, R, c), ((1, 0, 0), 90), ((R - c - h) / 2, h, 1), bsdf={"ref": "wall"}),
+    ]
+    f0 = c - field / 2.0
+    centres = rng.uniform(f0, f0 + field, size=(n_spheres, 3))
+    radii = rng.lognormal(0.0, 0.5, size=n_spheres) * radius_scale
+    for i in range(n_spheres):
+        ents.append({"to_world": {"translate": centres[i].round(5).tolist(), "scale": round(float(radii[i]), 6)},
+                     "shape": {"type": "mesh", "asset_name": "ico"}, "bsdf": _sphere_bsdf(rng)})
+    ents.append({"light": {"type": "directional", "direction": [0.08, -1.0, 0.05],
+                           "irradiance": [irradiance, irradiance, irradiance]}})
+    scene = {
+        "camera": {"type": "perspective", "fov": 70.0, "resolution": [width, height], "far": 10 * R,
+                   "origin": [c, 0.35 * R, 0.99 * R], "target": [c, 0.4 * R, 0.0], "up": [0.0, 1.0, 0.0]},
+        "sampler": {"type": "independent", "sample_count": spp, "seed": sampler_seed},
+        "bsdf_vars": [{"name": "wall", "bsdf": wall}],
         "assets": [{"name": "ico", "type": "model_obj", "location": "ico.obj"}],
         "scene": ents,
         "accel": {"type": "embree"},

@@ -44,6 +44,15 @@ def lib():
         L.orc_microfacet_d.argtypes = [ctypes.c_int, ctypes.c_float, ctypes.c_float, P]
         L.orc_pcg_u32.restype = ctypes.c_uint32
         L.orc_pcg_u32.argtypes = [ctypes.c_uint32, ctypes.c_uint32, ctypes.c_uint32, ctypes.c_int]
+        L.orc_guide_level_res.argtypes = [ctypes.c_uint32, ctypes.c_uint32, P]
+        L.orc_guide_forward.argtypes = [ctypes.c_uint32, P, P, P, ctypes.c_float, ctypes.c_float, P, P,
+                                        ctypes.c_int64, P, P, ctypes.c_int]
+        L.orc_guide_grad.restype = ctypes.c_double
+        L.orc_guide_grad.argtypes = [ctypes.c_uint32, P, P, P, ctypes.c_float, ctypes.c_float, P, P,
+                                     ctypes.c_int64, P, ctypes.c_int]
+        L.orc_guide_mix_pdf.argtypes = [P, P, ctypes.c_int64, P]
+        L.orc_half_round.restype = ctypes.c_float
+        L.orc_half_round.argtypes = [ctypes.c_float]
         _lib = L
     return _lib
 
@@ -139,3 +148,105 @@ def bsdf_sample(bsdf_json, wi, u):
     if lib().orc_bsdf_sample(bsdf_json.encode(), _p(wi), _p(u), n, _p(wo), _p(pdf), _p(f), _p(eta), _p(typ)) != 0:
         raise RuntimeError(lib().orc_last_error().decode())
     return wo, pdf, f, eta, typ
+
+
+# ---------------------------------------------------------------- guide network
+GUIDE_LEVELS = 16
+GUIDE_NW = 64 * 48 + 64 * 64 * 2 + 48 * 64
+
+
+class OracleGuide:
+    """CPU guide network with the GPU library's layout (table then MLP weights)."""
+
+    def __init__(self, log2t, lo, hi, params, min_res=16, max_res=512, log_kappa_max=5.0, c_max=0.6):
+        self.log2t = int(log2t)
+        self.log_kappa_max = float(log_kappa_max)
+        self.c_max = float(c_max)
+        self.res = np.zeros(GUIDE_LEVELS, dtype=np.uint32)
+        lib().orc_guide_level_res(min_res, max_res, _p(self.res))
+        self.lo = np.asarray(lo, dtype=np.float32)
+        hi = np.asarray(hi, dtype=np.float32)
+        ext = hi - self.lo
+        self.inv = np.where(ext > 1e-6, np.float32(1.0) / np.maximum(ext, np.float32(1e-30)), 1.0).astype(np.float32)
+        self.params = np.ascontiguousarray(params, dtype=np.float32)
+        self.n_table = GUIDE_LEVELS * (1 << self.log2t) * 2
+        assert self.params.size == self.n_table + GUIDE_NW
+
+    def forward(self, queries, exact=False):
+        q = np.ascontiguousarray(queries, dtype=np.float32)
+        raw = np.zeros((q.shape[0], 48), dtype=np.float32)
+        mix = np.zeros((q.shape[0], 44), dtype=np.float32)
+        lib().orc_guide_forward(self.log2t, _p(self.res), _p(self.lo), _p(self.inv), self.log_kappa_max,
+                                self.c_max, _p(self.params), _p(q),
+                                q.shape[0], _p(raw), _p(mix), 1 if exact else 0)
+        return raw, mix
+
+    def grad(self, records, exact=False):
+        r = np.ascontiguousarray(records, dtype=np.float32)
+        g = np.zeros(self.params.size, dtype=np.float64)
+        loss = lib().orc_guide_grad(self.log2t, _p(self.res), _p(self.lo), _p(self.inv), self.log_kappa_max,
+                                    self.c_max, _p(self.params), _p(r),
+                                    r.shape[0], _p(g), 1 if exact else 0)
+        return g, loss
+
+
+def guide_mix_pdf(mix, dirs):
+    m = np.ascontiguousarray(mix, dtype=np.float32)
+    d = np.ascontiguousarray(dirs, dtype=np.float32)
+    out = np.zeros(m.shape[0], dtype=np.float64)
+    lib().orc_guide_mix_pdf(_p(m), _p(d), m.shape[0], _p(out))
+    return out
+
+
+def guide_checkpoint(log2t, lo, hi, params, min_res=16, max_res=512, step=0):
+    """Bytes of a version-1 guide checkpoint holding `params` and zero Adam moments."""
+    import struct
+    res = np.zeros(GUIDE_LEVELS, dtype=np.uint32)
+    lib().orc_guide_level_res(min_res, max_res, _p(res))
+    n = int(np.asarray(params).size)
+    hd = b"RADGUID1" + struct.pack("<6I", 1, log2t, GUIDE_LEVELS, min_res, max_res, step)
+    hd += struct.pack("<Q", n) + struct.pack("<3f", *lo) + struct.pack("<3f", *hi) + res.astype("<u4").tobytes()
+    assert len(hd) == 128
+    p = np.ascontiguousarray(params, dtype="<f4").tobytes()
+    return hd + p + bytes(2 * len(p))
+
+
+def guide_random_params(log2t, seed, table_scale=0.5, weight_scale=1.0):
+    """Seeded parameters with non-trivial hash-grid features (unlike the +-1e-4 initialisation)."""
+    rng = np.random.default_rng(seed)
+    n_table = GUIDE_LEVELS * (1 << log2t) * 2
+    table = rng.uniform(-table_scale, table_scale, n_table)
+    w = np.concatenate([
+        rng.uniform(-1, 1, 64 * 48) * np.sqrt(6 / 48),
+        rng.uniform(-1, 1, 64 * 64) * np.sqrt(6 / 64),
+        rng.uniform(-1, 1, 64 * 64) * np.sqrt(6 / 64),
+        rng.uniform(-1, 1, 48 * 64) * np.sqrt(6 / 64) * 0.5,
+    ]) * weight_scale
+    w[64 * 48 + 2 * 64 * 64 + 41 * 64:] = 0.0  # unused output rows
+    return np.concatenate([table, w]).astype(np.float32)
+
+
+def guide_random_queries(n, lo, hi, seed):
+    rng = np.random.default_rng(seed)
+    P = rng.uniform(lo, hi, size=(n, 3))
+    N = rng.normal(size=(n, 3))
+    N /= np.linalg.norm(N, axis=1, keepdims=True)
+    wo = rng.normal(size=(n, 3))
+    wo /= np.linalg.norm(wo, axis=1, keepdims=True)
+    return np.concatenate([P, N, wo], axis=1).astype(np.float32)
+
+
+def guide_random_records(n, lo, hi, seed, w_max=2.0):
+    """Records (n, 16): P, p_bsdf | N, 0 | wo, 0 | wi, weight."""
+    rng = np.random.default_rng(seed + 1)
+    q = guide_random_queries(n, lo, hi, seed)
+    wi = rng.normal(size=(n, 3))
+    wi /= np.linalg.norm(wi, axis=1, keepdims=True)
+    b = rng.uniform(0.01, 1.0, n)
+    w = rng.uniform(0.0, w_max, n)
+    rec = np.zeros((n, 16), dtype=np.float32)
+    rec[:, 0:3], rec[:, 3] = q[:, 0:3], b
+    rec[:, 4:7] = q[:, 3:6]
+    rec[:, 8:11] = q[:, 6:9]
+    rec[:, 12:15], rec[:, 15] = wi, w
+    return rec
