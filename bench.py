@@ -303,12 +303,30 @@ def run_volume(args, world, rank, local):
         clocks = ClockSampler(local)
         torch.cuda.synchronize()
         clocks.start()
-        job = scene.submit(spp=args.steps, profile=True)
+        fast = dict(vol_fp16=True)
+        j = scene.submit(spp=args.warmup, first_sample=30_000, **fast)
+        j.wait()
+        j.close()
+        job = scene.submit(spp=args.steps, profile=True, **fast)
         job.wait()
         torch.cuda.synchronize()
         clk = clocks.stop()
         st = job.stats()
         job.close()
+        # the unbiased-depth estimator with the global and with the 16^3-brick majorants,
+        # and the reference's algorithm with the fp32 grid, on the same frame
+        jg = scene.submit(spp=max(1, args.steps // 4), profile=True, vol_real_depth=True, vol_fp16=True)
+        jg.wait()
+        st_glob = jg.stats()
+        jg.close()
+        jb = scene.submit(spp=max(1, args.steps // 4), profile=True, vol_bricks=True, vol_fp16=True)
+        jb.wait()
+        st_brk = jb.stats()
+        jb.close()
+        jr = scene.submit(spp=max(1, args.steps // 4), profile=True)
+        jr.wait()
+        st_ref = jr.stats()
+        jr.close()
         value = st["samples"] / (st["gpu_ms"] / 1000.0)
         cpu = None
         if rank == 0 and not args.no_cpu:
@@ -329,7 +347,18 @@ def run_volume(args, world, rank, local):
             "config": {"workload": "volume_box", "width": res, "height": res, "grid": args.vol_grid,
                        "max_depth": 32, "rr_depth": 5, "sigma_t_scale": 20, "albedo": 0.9, "hg_g": 0.6},
             "mrays_per_s": (st["rays_closest"] + st["rays_shadow"]) / (st["gpu_ms"] / 1000.0) / 1e6,
-            "gpu_launches": st["kernel_launches"], "kernel_ms": {"vol_path": st["ms_volpath"]}, "clocks": clk}
+            "gpu_launches": st["kernel_launches"], "kernel_ms": {"vol_path": st["ms_volpath"]}, "clocks": clk,
+            "mode": "the reference's delta tracking (global majorant, null collisions counted as depth) on the "
+                    "fp16 grid (RAD_JOB_VOL_FP16)",
+            "unbiased_depth": {"global_majorant_samples_per_s": st_glob["samples"] / (st_glob["gpu_ms"] / 1000.0),
+                               "brick_majorants_samples_per_s": st_brk["samples"] / (st_brk["gpu_ms"] / 1000.0),
+                               "brick_mrays_per_s": (st_brk["rays_closest"] + st_brk["rays_shadow"])
+                               / (st_brk["gpu_ms"] / 1000.0) / 1e6},
+            "reference_algorithm_fp32": {"mode": "global majorant, fp32 grid, null collisions counted as depth",
+                                    "spp": st_ref["samples"] // (res * res),
+                                    "samples_per_s": st_ref["samples"] / (st_ref["gpu_ms"] / 1000.0),
+                                    "mrays_per_s": (st_ref["rays_closest"] + st_ref["rays_shadow"])
+                                    / (st_ref["gpu_ms"] / 1000.0) / 1e6}}
     if cpu:
         line["cpu_baseline"] = cpu
     print(json.dumps(line), flush=True)

@@ -75,6 +75,13 @@ typedef struct rad_job_desc {
 #define RAD_JOB_PROFILE_KERNELS 1u /* time every kernel launch with CUDA events */
 #define RAD_JOB_SYNC 2u            /* render on the calling thread, return when done */
 #define RAD_JOB_COUNT_TRAVERSAL 4u /* count BVH8 node visits / primitive tests (slower) */
+#define RAD_JOB_VOL_BRICKS 16u     /* `vol_path`: free flights against 16^3-brick majorants of grid media
+                                      instead of the global majorant (fewer null collisions); implies
+                                      RAD_JOB_VOL_REAL_DEPTH */
+#define RAD_JOB_VOL_FP16 32u       /* `vol_path`: read the density grid's fp16 copy */
+#define RAD_JOB_VOL_REAL_DEPTH 64u /* `vol_path`: null collisions count neither toward max_depth nor for
+                                      Russian roulette. The reference counts them (vol_path.cpp:40-52
+                                      run per loop iteration), so its truncation depends on the majorant */
 #define RAD_JOB_GUIDE 8u           /* `path` only: sample directions with the scene's learned guide
                                       (one-sample MIS with the BSDF) and train it during the
                                       job's first train_fraction of samples; no reference counterpart */

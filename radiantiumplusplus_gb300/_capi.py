@@ -31,6 +31,9 @@ RAD_JOB_PROFILE_KERNELS = 1
 RAD_JOB_SYNC = 2
 RAD_JOB_COUNT_TRAVERSAL = 4
 RAD_JOB_GUIDE = 8
+RAD_JOB_VOL_BRICKS = 16
+RAD_JOB_VOL_FP16 = 32
+RAD_JOB_VOL_REAL_DEPTH = 64
 
 # Every symbol the header declares (the export test checks this list).
 EXPORTS = [

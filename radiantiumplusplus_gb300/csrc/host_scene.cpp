@@ -637,6 +637,31 @@ static MediumRec MakeMedium(const JValue& c, const M4f& toWorld, const std::map<
     md.gridOffset = hs.volume.size();
     hs.volume.insert(hs.volume.end(), it->second.data.begin(), it->second.data.end());
     maxValue = it->second.max;
+    if (!md.repeatWrap) {
+      // 16^3-brick majorants over voxel coordinates f = local * (n - 1). A point in
+      // cell [i, i + 1) interpolates voxels i - 1 .. i + 1 (the neighbour rule of
+      // grid.cpp:41-75), so a brick's bound is the maximum over its voxels dilated by one.
+      const int n[3] = {md.nx, md.ny, md.nz}, ch = md.channels;
+      int nb[3];
+      for (int a = 0; a < 3; a++) nb[a] = std::max(1, (n[a] - 1 + 15) / 16);
+      md.brickOffset = (uint32_t)hs.brickMaj.size();
+      md.hasBricks = 1;
+      const std::vector<float>& g = it->second.data;
+      for (int bz = 0; bz < nb[2]; bz++)
+        for (int by = 0; by < nb[1]; by++)
+          for (int bx = 0; bx < nb[0]; bx++) {
+            float m = 0.f;
+            int z0 = std::max(0, 16 * bz - 1), z1 = std::min(n[2] - 1, 16 * bz + 16);
+            int y0 = std::max(0, 16 * by - 1), y1 = std::min(n[1] - 1, 16 * by + 16);
+            int x0 = std::max(0, 16 * bx - 1), x1 = std::min(n[0] - 1, 16 * bx + 16);
+            for (int z = z0; z <= z1; z++)
+              for (int y = y0; y <= y1; y++)
+                for (int x = x0; x <= x1; x++)
+                  for (int c = 0; c < ch; c++)
+                    m = std::max(m, g[(((size_t)z * n[1] + y) * n[0] + x) * ch + c]);
+            hs.brickMaj.push_back(m * md.scale);
+          }
+    }
   }
   M4f affine = M4f::Identity();
   for (int i = 0; i < 3; i++) {

@@ -38,6 +38,7 @@ struct HostScene {
   std::vector<LightRec> lights;
   std::vector<MediumRec> media;
   std::vector<float> volume;
+  std::vector<float> brickMaj;  // 16^3-brick majorants of the grid media
   std::vector<float> pos, nrm, uv;
   std::vector<uint32_t> idx;
   std::vector<float> cdf;

@@ -5,9 +5,14 @@
 // ratio-tracking transmittance loop (vol_path.cpp:224-342) and index-matched
 // boundaries. Camera rays and PCG streams come from the wavefront generate
 // stage; the radiance goes to the path's L slot for the accumulate stage.
+#include <algorithm>
+
 #include "dbsdf.cuh"
 #include "dscene.cuh"
+#include "dvol.cuh"
+#ifndef RAD_HOST_EMULATION
 #include "kernels.h"
+#endif
 
 namespace rad {
 
@@ -15,113 +20,21 @@ constexpr int kVolBlock = 128;
 constexpr int kMaxTrLoop = 1 << 20;  // bound on transmittance-loop iterations (device check)
 constexpr int kMaxVolIter = 1 << 22; // bound on free-flight iterations per path
 
-struct MedInt {
-  float T;
-  V3 P;
-  Frame sh;
-  V3 Wi;
-  float MinT;
-  V3 sS, sN, sT, cE;
-};
-
-struct VRay {
-  V3 O, D;
-  float MinT, MaxT;
-};
-
-// grid.cpp:41-75 (trilinear with the half-texel neighbour rule), :88-103
-RD V3 EvalGrid(const DevScene& S, const MediumRec& md, V3 p) {
-  auto wrap = [&](float v) {
-    if (md.repeatWrap) return clampr(v - floorf(v), 0.f, 1.f);
-    return clampr(v, 0.f, 1.f);
-  };
-  V3 wp{wrap(p.x), wrap(p.y), wrap(p.z)};
-  V3 fp{wp.x * ((float)md.nx - 1.f), wp.y * ((float)md.ny - 1.f), wp.z * ((float)md.nz - 1.f)};
-  int ix = (int)fp.x, iy = (int)fp.y, iz = (int)fp.z;
-  int dpu = (fp.x > ((float)ix + 0.5f)) ? 1 : -1;
-  int dpv = (fp.y > ((float)iy + 0.5f)) ? 1 : -1;
-  int dpw = (fp.z > ((float)iz + 0.5f)) ? 1 : -1;
-  int apu = min(max(ix + dpu, 0), md.nx - 1);
-  int apv = min(max(iy + dpv, 0), md.ny - 1);
-  int apw = min(max(iz + dpw, 0), md.nz - 1);
-  float du = fminr(fabsf(fp.x - (float)ix - 0.5f), 1.f);
-  float dv = fminr(fabsf(fp.y - (float)iy - 0.5f), 1.f);
-  float dw = fminr(fabsf(fp.z - (float)iz - 0.5f), 1.f);
-  const float* g = S.volume + md.gridOffset;
-  int ch = md.channels;
-  auto rd = [&](int u, int v, int w) -> V3 {
-    size_t st = (((size_t)w * (size_t)md.ny + (size_t)v) * (size_t)md.nx + (size_t)u) * (size_t)ch;
-    if (ch == 1) return v3s(__ldg(g + st));
-    return V3{__ldg(g + st), __ldg(g + st + 1), __ldg(g + st + 2)};
-  };
-  V3 c000 = rd(ix, iy, iz), c100 = rd(apu, iy, iz), c010 = rd(ix, apv, iz), c001 = rd(ix, iy, apw);
-  V3 c110 = rd(apu, apv, iz), c011 = rd(ix, apv, apw), c101 = rd(apu, iy, apw), c111 = rd(apu, apv, apw);
-  V3 a = Fmadd(c000, v3s(1.f - du), c100 * du);
-  V3 b = Fmadd(c010, v3s(1.f - du), c110 * du);
-  V3 e = Fmadd(a, v3s(1.f - dv), b * dv);
-  V3 f = Fmadd(c001, v3s(1.f - du), c101 * du);
-  V3 g2 = Fmadd(c011, v3s(1.f - du), c111 * du);
-  V3 h = Fmadd(f, v3s(1.f - dv), g2 * dv);
-  return Fmadd(e, v3s(1.f - dw), h * dw);
-}
-
-// medium.cpp:19-43 with heterogeneous.cpp / homogeneous.cpp
-RD MedInt SampleInteraction(const DevScene& S, const MediumRec& md, const VRay& ray, float sample, int channel) {
-  MedInt mei;
-  mei.Wi = -ray.D;
-  mei.sh = FrameFromN(mei.Wi);
-  bool aabbIts;
-  float mint, maxt;
-  if (md.kind == MED_HOMOGENEOUS) {
-    aabbIts = true;
-    mint = 0.f;
-    maxt = kInf;
-  } else {
-    V3 lo{md.bbMin[0], md.bbMin[1], md.bbMin[2]}, hi{md.bbMax[0], md.bbMax[1], md.bbMax[2]};
-    bool contains = ray.O.x >= lo.x && ray.O.y >= lo.y && ray.O.z >= lo.z && ray.O.x <= hi.x && ray.O.y <= hi.y &&
-                    ray.O.z <= hi.z;
-    aabbIts = !is_zero(ray.D) || contains;
-    V3 rcp{1.f / ray.D.x, 1.f / ray.D.y, 1.f / ray.D.z};
-    V3 t1 = cmul(lo - ray.O, rcp), t2 = cmul(hi - ray.O, rcp);
-    V3 t1p{fminr(t1.x, t2.x), fminr(t1.y, t2.y), fminr(t1.z, t2.z)};
-    V3 t2p{fmaxr(t1.x, t2.x), fmaxr(t1.y, t2.y), fmaxr(t1.z, t2.z)};
-    mint = max_comp(t1p);
-    maxt = min_comp(t2p);
-    aabbIts = aabbIts && maxt >= mint;
-  }
-  aabbIts = aabbIts && (isfinite(mint) || isfinite(maxt));
-  bool active = aabbIts;
-  if (!active) {
-    mint = 0.f;
-    maxt = kInf;
-  }
-  mint = fmaxr(0.f, mint);
-  maxt = fminr(ray.MaxT, maxt);
-  V3 combined = md.kind == MED_HOMOGENEOUS ? V3{md.sigmaT[0], md.sigmaT[1], md.sigmaT[2]} * md.scale
-                                           : v3s(md.maxDensity);
-  float m = comp(combined, channel);
-  float sampledT = mint + (-logf(1.f - sample) / m);
-  bool validMi = active && (sampledT <= maxt);
-  mei.T = validMi ? sampledT : kInf;
-  mei.P = ray.D * sampledT + ray.O;
-  mei.MinT = mint;
-  V3 alb{md.albedo[0], md.albedo[1], md.albedo[2]};
-  if (md.kind == MED_HOMOGENEOUS) {
-    mei.sT = V3{md.sigmaT[0], md.sigmaT[1], md.sigmaT[2]} * md.scale;
-    mei.sS = cmul(mei.sT, alb);
-    mei.sN = v3s(0.f);
-  } else {
-    V3 local = AffineRows(md.toLocal, mei.P);
-    V3 e = md.gridSigma ? EvalGrid(S, md, local) : V3{md.sigmaT[0], md.sigmaT[1], md.sigmaT[2]};
-    mei.sT = e * md.scale;
-    mei.sS = cmul(mei.sT, alb);
-    mei.sN = v3s(md.maxDensity) - mei.sT;
-  }
-  mei.cE = combined;
-  return mei;
-}
-
 RD V3 ExpV(V3 v) { return V3{expf(v.x), expf(v.y), expf(v.z)}; }
+
+// Majorant transmittance relative to the hero channel, exp(-(cE - cE[ch]) t),
+// without forming exp(-cE t) itself: the reference's tr / pdf ratios
+// (medium.cpp:45-59, vol_path.cpp:262-272) underflow to 0 / 0 once cE t passes
+// ~100 (a long shadow segment), which drops the contribution. Used by the
+// non-reference estimators (realDepth / BRICKS); 1 for a scalar majorant.
+RD V3 RelTr(V3 cE, int ch, float t) {
+  float c = comp(cE, ch);
+  auto f = [&](float v) {
+    float d = v - c;
+    return (d == 0.f || !isfinite(t)) ? 1.f : expf(-d * t);
+  };
+  return V3{f(cE.x), f(cE.y), f(cE.z)};
+}
 
 RD float PhaseEval(const MediumRec& md, const MedInt& mi, V3 wo) {
   if (!md.hg) return SquareToUniformSpherePdf();
@@ -174,14 +87,30 @@ RD bool VTrace(const DevScene& S, const VRay& ray, SurfInt& si, uint32_t* err) {
 
 RD VRay Spawn(V3 P, V3 N, V3 d) { return VRay{OffsetP(P, N, d), d, 0.f, kFloatMax}; }
 
+// Out-of-line copies of the large pieces: one body each in the kernel instead
+// of one per call site keeps the loop within the instruction cache.
+#ifdef RAD_HOST_EMULATION
+#define RDN inline
+#else
+#define RDN __device__ __noinline__
+#endif
+RDN bool VTraceCall(const DevScene& S, const VRay& ray, SurfInt& si, uint32_t* err) { return VTrace(S, ray, si, err); }
+RDN void VBsdfEvalPdf(const MatRec* mats, uint32_t b, V3 wi, V3 wo, V3& f, float& pdf) {
+  BsdfEvalPdf(mats, b, wi, wo, f, pdf);
+}
+RDN BsdfSampleRes VBsdfSample(const MatRec* mats, uint32_t b, V3 wi, float xl, V2 xd) {
+  return BsdfSample(mats, b, wi, xl, xd);
+}
+
 RD int MediumOfHit(const DevScene& S, const SurfInt& si, V3 D) {
   const ShapeRec& sh = S.shapes[si.shape];
   return dot(D, si.N) > 0.f ? sh.outMedium : sh.inMedium;
 }
 
-// vol_path.cpp:224-342
-RD V3 VolSampleLight(const DevScene& S, Pcg32& rng, int medium, int channel, V3 refP, V3 refN, DirSample& dsr,
-                     uint32_t* err, uint64_t& nRays) {
+// vol_path.cpp:224-342. stable: RelTr ratios instead of the reference's (see RelTr).
+template <bool BRICKS, bool HALF>
+RDN V3 VolSampleLight(const DevScene& S, Pcg32& rng, int medium, int channel, V3 refP, V3 refN, DirSample& dsr,
+                     uint32_t* err, uint64_t& nRays, bool stable) {
   float xl = Next1D(rng);
   V2 xd = Next2D(rng);
   V3 li;
@@ -208,10 +137,10 @@ RD V3 VolSampleLight(const DevScene& S, Pcg32& rng, int medium, int channel, V3 
     bool activeSurface = active && !activeMedium;
     if (activeMedium) {
       const MediumRec& md = S.media[medium];
-      MedInt mei = SampleInteraction(S, md, ray, Next1D(rng), channel);
+      MedInt mei = SampleInteraction<BRICKS, HALF>(S, md, ray, Next1D(rng), channel);
       if (md.kind == MED_HOMOGENEOUS && mei.T != kInf) ray.MaxT = fminr(mei.T, remainingDist);
       if (needsIntersection) {
-        VTrace(S, ray, si, err);
+        VTraceCall(S, ray, si, err);
         nRays++;
       }
       if (si.T < mei.T) mei.T = kInf;
@@ -219,10 +148,18 @@ RD V3 VolSampleLight(const DevScene& S, Pcg32& rng, int medium, int channel, V3 
       {
         float t = fminr(remainingDist, fminr(mei.T, si.T)) - mei.MinT;
         if (t >= 0.f) {
-          V3 tr = ExpV(mei.cE * -t);
-          V3 ffp = (si.T < mei.T || mei.T > remainingDist) ? tr : cmul(tr, mei.cE);
-          float trPdf = comp(ffp, channel);
-          V3 mTr = trPdf > 0.f ? tr / trPdf : v3s(0.f);
+          bool pass = si.T < mei.T || mei.T > remainingDist;
+          V3 mTr;
+          if (stable) {
+            float m = comp(mei.cE, channel);
+            V3 rel = RelTr(mei.cE, channel, t);
+            mTr = pass ? rel : (m > 0.f ? rel / m : v3s(0.f));
+          } else {
+            V3 tr = ExpV(mei.cE * -t);
+            V3 ffp = pass ? tr : cmul(tr, mei.cE);
+            float trPdf = comp(ffp, channel);
+            mTr = trPdf > 0.f ? tr / trPdf : v3s(0.f);
+          }
           resultTr = cmul(resultTr, mTr);
         }
       }
@@ -240,7 +177,7 @@ RD V3 VolSampleLight(const DevScene& S, Pcg32& rng, int medium, int channel, V3 
     }
     bool intersect = activeSurface && needsIntersection;
     if (intersect) {
-      VTrace(S, ray, si, err);
+      VTraceCall(S, ray, si, err);
       nRays++;
     }
     needsIntersection = needsIntersection && !intersect;
@@ -262,158 +199,268 @@ RD V3 VolSampleLight(const DevScene& S, Pcg32& rng, int medium, int channel, V3 
   return cmul(li, resultTr);
 }
 
-__global__ void __launch_bounds__(kVolBlock) KVolPath(DevScene S, PathBuffers B, uint32_t count, uint32_t* err) {
-  uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
-  if (i >= count) return;
-  float4 ro = B.rayO[i], rd = B.rayD[i];
-  uint2 rs = B.rng[i];
-  Pcg32 rng;
-  rng.state = ((uint64_t)rs.y << 32) | rs.x;
-  VRay ray{V3{ro.x, ro.y, ro.z}, V3{rd.x, rd.y, rd.z}, ro.w, rd.w};
-  int medium = S.globalMedium;
-  V3 thr = v3s(1.f), result = v3s(0.f);
-  float eta = 1.f;
-  bool isSpecular = true;
-  V3 prevP = v3s(0.f);
-  float prevPdf = 1.f;
-  uint64_t nRays = 0, nShadow = 0;
-  int channel = (int)min((uint32_t)(Next1D(rng) * 3.f), 2u);
+// Per-path state of the `vol_path` loop (VolPath::Li's locals), so that a lane
+// can run a path one loop iteration at a time and take a new path when its own
+// ends (KVolPath).
+struct VolPathState {
+  VRay ray;
+  V3 thr, result, prevP;
+  float eta, prevPdf;
+  int medium, channel, depth, guard;
+  bool isSpecular, siValid, afterNull;
   SurfInt si;
-  si.T = kInf;
-  si.shape = -1;
-  for (int depth = 0, guard = 0;; depth++, guard++) {
-    if (guard >= kMaxVolIter) {
-      atomicOr(err, 4u);
-      break;
+  Pcg32 rng;
+  uint32_t nRays, nShadow;
+};
+
+RD void VolInit(const DevScene& S, VolPathState& p, VRay ray, Pcg32 rng) {
+  p.ray = ray;
+  p.rng = rng;
+  p.medium = S.globalMedium;
+  p.thr = v3s(1.f);
+  p.result = v3s(0.f);
+  p.eta = 1.f;
+  p.isSpecular = true;
+  p.prevP = v3s(0.f);
+  p.prevPdf = 1.f;
+  uint32_t ch3 = (uint32_t)(Next1D(p.rng) * 3.f);
+  p.channel = (int)(ch3 < 2u ? ch3 : 2u);
+  p.si.T = kInf;
+  p.si.shape = -1;
+  p.siValid = false;
+  p.afterNull = false;
+  p.depth = 0;
+  p.guard = 0;
+  p.nRays = p.nShadow = 0;
+}
+
+// One iteration of the loop of VolPath::Li (vol_path.cpp:40-215); false when
+// the path has ended (its radiance is in p.result).
+// BRICKS: brick majorants, and no re-trace after a null collision (the surface
+// ahead along the same line is unchanged; its distance shrinks by the flight).
+// HALF: fp16 grid. realDepth (mode bit kVolRealDepth, implied by BRICKS): null
+// collisions count neither toward max_depth nor for Russian roulette; the
+// reference counts them (vol_path.cpp:40-52 run once per loop iteration), which
+// ties its truncation to the majorant. All off = the reference's algorithm.
+template <bool BRICKS, bool HALF>
+RD bool VolStep(const DevScene& S, VolPathState& p, uint32_t mode, uint32_t* err) {
+  const bool realDepth = BRICKS || (mode & kVolRealDepth);
+  Pcg32& rng = p.rng;
+  VRay& ray = p.ray;
+  SurfInt& si = p.si;
+  V3& thr = p.thr;
+  const int channel = p.channel;
+  if (p.guard >= kMaxVolIter) {
+    atomicOr(err, 4u);
+    return false;
+  }
+  if (p.afterNull) p.depth--;  // realDepth: the null collision was free
+  if (p.depth >= S.rrDepth && !p.afterNull) {
+    float rr = fminr(max_comp(thr) * Sqr(p.eta), 0.95f);
+    if (Next1D(rng) > rr) return false;
+    thr = thr * Rcp(rr);
+  }
+  if (S.maxDepth >= 0 && p.depth + 1 >= S.maxDepth) return false;
+  bool isSampleMedium = p.medium >= 0;
+  bool isSampleSurface = !isSampleMedium;
+  bool isNullScatter = false, isMediumScatter = false, isMediumEscaped = false;
+  bool isSpectral = isSampleMedium;
+  MedInt mei;
+  mei.T = kInf;
+  if (isSampleMedium) {
+    const MediumRec& md = S.media[p.medium];
+    mei = SampleInteraction<BRICKS, HALF>(S, md, ray, Next1D(rng), channel);
+    if (md.kind == MED_HOMOGENEOUS && mei.T != kInf) ray.MaxT = mei.T;
+    if (!(BRICKS && p.siValid)) {
+      VTraceCall(S, ray, si, err);
+      p.nRays++;
     }
-    if (depth >= S.rrDepth) {
-      float rr = fminr(max_comp(thr) * Sqr(eta), 0.95f);
-      if (Next1D(rng) > rr) break;
-      thr = thr * Rcp(rr);
-    }
-    if (S.maxDepth >= 0 && depth + 1 >= S.maxDepth) break;
-    bool isSampleMedium = medium >= 0;
-    bool isSampleSurface = !isSampleMedium;
-    bool isNullScatter = false, isMediumScatter = false, isMediumEscaped = false;
-    bool isSpectral = isSampleMedium;
-    MedInt mei;
-    mei.T = kInf;
-    if (isSampleMedium) {
-      const MediumRec& md = S.media[medium];
-      mei = SampleInteraction(S, md, ray, Next1D(rng), channel);
-      if (md.kind == MED_HOMOGENEOUS && mei.T != kInf) ray.MaxT = mei.T;
-      VTrace(S, ray, si, err);
-      nRays++;
-      if (si.T < mei.T) mei.T = kInf;
-      if (isSpectral) {
-        // medium.cpp:45-59
-        V3 tr, ffp;
-        float t = fminr(mei.T, si.T) - mei.MinT;
+    p.siValid = false;
+    if (si.T < mei.T) mei.T = kInf;
+    if (isSpectral) {
+      // medium.cpp:45-59
+      V3 tr, ffp;
+      float t = fminr(mei.T, si.T) - mei.MinT;
+      if (realDepth) {
+        // tr / pdf formed as RelTr ratios (no underflow)
         if (t <= 0.f) {
           tr = ffp = v3s(1.f);
         } else {
-          tr = ExpV(mei.cE * -t);
-          ffp = si.T < mei.T ? tr : cmul(tr, mei.cE);
-          if (tr.x == ffp.x && tr.y == ffp.y && tr.z == ffp.z) tr = ffp = v3s(1.f);
+          tr = RelTr(mei.cE, channel, t);
+          ffp = si.T < mei.T ? v3s(1.f) : v3s(comp(mei.cE, channel));
         }
-        float pdf = comp(ffp, channel);
-        V3 after = cmul(thr, tr) / pdf;
-        thr = pdf <= 0.f ? v3s(0.f) : after;
+      } else if (t <= 0.f) {
+        tr = ffp = v3s(1.f);
+      } else {
+        tr = ExpV(mei.cE * -t);
+        ffp = si.T < mei.T ? tr : cmul(tr, mei.cE);
+        if (tr.x == ffp.x && tr.y == ffp.y && tr.z == ffp.z) tr = ffp = v3s(1.f);
       }
-      isMediumEscaped = mei.T == kInf;
-      isSampleMedium = mei.T != kInf;
-      bool nullScatter = Next1D(rng) > comp(mei.sT, channel) / comp(mei.cE, channel);
-      isNullScatter = nullScatter && isSampleMedium;
-      isMediumScatter = !isNullScatter && isSampleMedium;
-      if (isSpectral && isNullScatter) thr = cmul(thr, mei.sN) * comp(mei.cE, channel) / comp(mei.sN, channel);
-      if (isMediumScatter) prevP = mei.P;
+      float pdf = comp(ffp, channel);
+      V3 after = cmul(thr, tr) / pdf;
+      thr = pdf <= 0.f ? v3s(0.f) : after;
     }
-    if (isNullScatter) {
-      ray.O = mei.P;
-      si.T = si.T - mei.T;
-    }
-    if (isMediumScatter) {
-      const MediumRec& md = S.media[medium];
-      if (isSpectral) thr = cmul(thr, mei.sS) * comp(mei.cE, channel) / comp(mei.sT, channel);
-      DirSample dsr;
-      V3 li = VolSampleLight(S, rng, medium, channel, mei.P, v3s(0.f), dsr, err, nShadow);
-      if (dsr.Pdf > 0.f) {
-        float phaseVal = PhaseEval(md, mei, dsr.Dir);
-        float weight = dsr.IsDelta ? 1.f : VMis(dsr.Pdf, phaseVal);
-        result = result + cmul(thr, li) * weight * phaseVal / dsr.Pdf;
-      }
-      float phasePdf;
-      V3 wo = PhaseSample(md, mei, Next2D(rng), phasePdf);
-      ray = Spawn(mei.P, v3s(0.f), wo);
-      isSpecular = false;
-      prevPdf = phasePdf;
-    }
-    isSampleSurface = isSampleSurface || isMediumEscaped;
-    if (isSampleSurface) {
-      bool hit = VTrace(S, ray, si, err);
-      nRays++;
-      int hitLight = hit ? S.shapes[si.shape].light : S.envLight;
-      if (hitLight >= 0) {
-        float weight;
-        if (isSpecular) {
-          weight = 1.f;
-        } else {
-          V3 rel = si.P - prevP;
-          float dist = norm(rel);
-          V3 dir = hit ? rel / dist : -si.Wi;
-          weight = VMis(prevPdf, PdfLightDirection(S, hitLight, prevP, dir, si.sh.N, dist));
-        }
-        V3 li = EvalLightAt(S, hitLight, &si);
-        result = result + cmul(thr, li) * weight;
-      }
-      if (!hit) break;
-      const ShapeRec& shp = S.shapes[si.shape];
-      if (shp.light >= 0) break;
-      if (shp.bsdf < 0) {
-        ray = Spawn(si.P, si.N, ray.D);
-        medium = MediumOfHit(S, si, ray.D);
-        depth--;
-        continue;
-      }
-      const MatRec* mats = S.mats;
-      if (mats[shp.bsdf].flags & BT_NODELTA) {
-        DirSample dsr;
-        V3 li = VolSampleLight(S, rng, medium, channel, si.P, si.N, dsr, err, nShadow);
-        if (dsr.Pdf > 0.f) {
-          V3 wo = ToLocal(si.sh, dsr.Dir);
-          V3 f;
-          float bsdfPdf;
-          BsdfEvalPdf(mats, (uint32_t)shp.bsdf, si.Wi, wo, f, bsdfPdf);
-          float weight = dsr.IsDelta ? 1.f : VMis(dsr.Pdf, bsdfPdf);
-          result = result + cmul(cmul(thr, f), li) * weight / dsr.Pdf;
-        }
-      }
-      float xl = Next1D(rng);
-      V2 xd = Next2D(rng);
-      BsdfSampleRes bs = BsdfSample(mats, (uint32_t)shp.bsdf, si.Wi, xl, xd);
-      if (bs.pdf <= 0.f) break;
-      thr = cmul(thr, bs.f) / bs.pdf;
-      eta *= bs.eta;
-      V3 nd = ToWorld(si.sh, bs.wo);
-      ray = Spawn(si.P, si.N, nd);
-      prevPdf = bs.pdf;
-      prevP = si.P;
-      isSpecular = (bs.type & BT_DELTA) != 0u;
-      medium = MediumOfHit(S, si, ray.D);
-    }
-    if (!(isSampleSurface || isSampleMedium)) break;
+    isMediumEscaped = mei.T == kInf;
+    isSampleMedium = mei.T != kInf;
+    bool nullScatter = Next1D(rng) > comp(mei.sT, channel) / comp(mei.cE, channel);
+    isNullScatter = nullScatter && isSampleMedium;
+    isMediumScatter = !isNullScatter && isSampleMedium;
+    if (isSpectral && isNullScatter) thr = cmul(thr, mei.sN) * comp(mei.cE, channel) / comp(mei.sN, channel);
+    if (isMediumScatter) p.prevP = mei.P;
   }
-  B.L[i] = make_float4(result.x, result.y, result.z, 0.f);
+  p.afterNull = false;
+  if (isNullScatter) {
+    ray.O = mei.P;
+    si.T = si.T - mei.T;
+    p.siValid = BRICKS;
+    p.afterNull = realDepth;
+  }
+  if (isMediumScatter) {
+    const MediumRec& md = S.media[p.medium];
+    if (isSpectral) thr = cmul(thr, mei.sS) * comp(mei.cE, channel) / comp(mei.sT, channel);
+    DirSample dsr;
+    uint64_t ns = 0;
+    V3 li = VolSampleLight<BRICKS, HALF>(S, rng, p.medium, channel, mei.P, v3s(0.f), dsr, err, ns, realDepth);
+    p.nShadow += (uint32_t)ns;
+    if (dsr.Pdf > 0.f) {
+      float phaseVal = PhaseEval(md, mei, dsr.Dir);
+      float weight = dsr.IsDelta ? 1.f : VMis(dsr.Pdf, phaseVal);
+      p.result = p.result + cmul(thr, li) * weight * phaseVal / dsr.Pdf;
+    }
+    float phasePdf;
+    V3 wo = PhaseSample(md, mei, Next2D(rng), phasePdf);
+    ray = Spawn(mei.P, v3s(0.f), wo);
+    p.isSpecular = false;
+    p.prevPdf = phasePdf;
+  }
+  isSampleSurface = isSampleSurface || isMediumEscaped;
+  if (isSampleSurface) {
+    bool hit = VTraceCall(S, ray, si, err);
+    p.nRays++;
+    int hitLight = hit ? S.shapes[si.shape].light : S.envLight;
+    if (hitLight >= 0) {
+      float weight;
+      if (p.isSpecular) {
+        weight = 1.f;
+      } else {
+        V3 rel = si.P - p.prevP;
+        float dist = norm(rel);
+        V3 dir = hit ? rel / dist : -si.Wi;
+        weight = VMis(p.prevPdf, PdfLightDirection(S, hitLight, p.prevP, dir, si.sh.N, dist));
+      }
+      V3 li = EvalLightAt(S, hitLight, &si);
+      p.result = p.result + cmul(thr, li) * weight;
+    }
+    if (!hit) return false;
+    const ShapeRec& shp = S.shapes[si.shape];
+    if (shp.light >= 0) return false;
+    if (shp.bsdf < 0) {
+      ray = Spawn(si.P, si.N, ray.D);
+      p.medium = MediumOfHit(S, si, ray.D);
+      // depth-- then the loop increment: the index-matched boundary is free
+      p.guard++;
+      return true;
+    }
+    const MatRec* mats = S.mats;
+    if (mats[shp.bsdf].flags & BT_NODELTA) {
+      DirSample dsr;
+      uint64_t ns = 0;
+      V3 li = VolSampleLight<BRICKS, HALF>(S, rng, p.medium, channel, si.P, si.N, dsr, err, ns, realDepth);
+      p.nShadow += (uint32_t)ns;
+      if (dsr.Pdf > 0.f) {
+        V3 wo = ToLocal(si.sh, dsr.Dir);
+        V3 f;
+        float bsdfPdf;
+        VBsdfEvalPdf(mats, (uint32_t)shp.bsdf, si.Wi, wo, f, bsdfPdf);
+        float weight = dsr.IsDelta ? 1.f : VMis(dsr.Pdf, bsdfPdf);
+        p.result = p.result + cmul(cmul(thr, f), li) * weight / dsr.Pdf;
+      }
+    }
+    float xl = Next1D(rng);
+    V2 xd = Next2D(rng);
+    BsdfSampleRes bs = VBsdfSample(mats, (uint32_t)shp.bsdf, si.Wi, xl, xd);
+    if (bs.pdf <= 0.f) return false;
+    thr = cmul(thr, bs.f) / bs.pdf;
+    p.eta *= bs.eta;
+    V3 nd = ToWorld(si.sh, bs.wo);
+    ray = Spawn(si.P, si.N, nd);
+    p.prevPdf = bs.pdf;
+    p.prevP = si.P;
+    p.isSpecular = (bs.type & BT_DELTA) != 0u;
+    p.medium = MediumOfHit(S, si, ray.D);
+  }
+  if (!(isSampleSurface || isSampleMedium)) return false;
+  p.depth++;
+  p.guard++;
+  return true;
+}
+
+// The whole loop for one path (host-side checks and equivalence tests).
+template <bool BRICKS, bool HALF>
+RD V3 VolLi(const DevScene& S, Pcg32& rng, VRay ray, uint32_t mode, uint32_t* err, uint64_t& nRays,
+            uint64_t& nShadow) {
+  VolPathState p;
+  VolInit(S, p, ray, rng);
+  while (VolStep<BRICKS, HALF>(S, p, mode, err)) {
+  }
+  rng = p.rng;
+  nRays += p.nRays;
+  nShadow += p.nShadow;
+  return p.result;
+}
+
+#ifndef RAD_HOST_EMULATION
+// Persistent lanes: each thread runs its path one loop iteration at a time and
+// takes the next unstarted path (counter B.counters[kMiscBase + 4], reset by
+// the generate stage) as soon as its own ends, so warps stay full while path
+// lengths vary by orders of magnitude.
+template <bool BRICKS, bool HALF>
+__global__ void __launch_bounds__(kVolBlock)
+    KVolPath(DevScene S, PathBuffers B, uint32_t count, uint32_t* err, uint32_t mode) {
+  uint32_t* next = B.counters + kMiscBase + 4;
+  VolPathState p;
+  uint32_t idx = 0;
+  bool live = false;
+  unsigned long long nRays = 0, nShadow = 0;
+  for (;;) {
+    if (!live) {
+      idx = atomicAdd(next, 1u);
+      if (idx >= count) break;
+      float4 ro = B.rayO[idx], rd = B.rayD[idx];
+      uint2 rs = B.rng[idx];
+      Pcg32 rng;
+      rng.state = ((uint64_t)rs.y << 32) | rs.x;
+      VolInit(S, p, VRay{V3{ro.x, ro.y, ro.z}, V3{rd.x, rd.y, rd.z}, ro.w, rd.w}, rng);
+      live = true;
+    }
+    if (!VolStep<BRICKS, HALF>(S, p, mode, err)) {
+      B.L[idx] = make_float4(p.result.x, p.result.y, p.result.z, 0.f);
+      nRays += p.nRays;
+      nShadow += p.nShadow;
+      live = false;
+    }
+  }
   // ray counters: closest in [kMiscBase + 2], shadow-side traces in [kMiscBase + 3]
-  atomicAdd(B.counters + kMiscBase + 2, (uint32_t)nRays);
-  atomicAdd(B.counters + kMiscBase + 3, (uint32_t)nShadow);
+  if (nRays) atomicAdd(B.counters + kMiscBase + 2, (uint32_t)nRays);
+  if (nShadow) atomicAdd(B.counters + kMiscBase + 3, (uint32_t)nShadow);
 }
 
 cudaError_t LaunchVolPath(const DevScene& S, const PathBuffers& B, const WaveParams& w, uint32_t* err,
-                          cudaStream_t st) {
+                          cudaStream_t st, uint32_t mode) {
   if (w.count == 0) return cudaSuccess;
-  KVolPath<<<(w.count + kVolBlock - 1) / kVolBlock, kVolBlock, 0, st>>>(S, B, w.count, err);
+  int perSm = 0;
+  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&perSm, KVolPath<true, true>, kVolBlock, 0);
+  int cap = PathGridBlocks() / 8 * (perSm > 0 ? perSm : 4);
+  int blocks = (int)std::min<uint32_t>((w.count + kVolBlock - 1) / kVolBlock, (uint32_t)cap);
+  switch (mode & (kVolBricks | kVolHalf)) {
+    case 0: KVolPath<false, false><<<blocks, kVolBlock, 0, st>>>(S, B, w.count, err, mode); break;
+    case kVolBricks: KVolPath<true, false><<<blocks, kVolBlock, 0, st>>>(S, B, w.count, err, mode); break;
+    case kVolHalf: KVolPath<false, true><<<blocks, kVolBlock, 0, st>>>(S, B, w.count, err, mode); break;
+    default: KVolPath<true, true><<<blocks, kVolBlock, 0, st>>>(S, B, w.count, err, mode); break;
+  }
   return cudaGetLastError();
 }
+
+#endif  // RAD_HOST_EMULATION
 
 }  // namespace rad

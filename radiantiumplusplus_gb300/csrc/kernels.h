@@ -4,6 +4,7 @@
 #include <stdint.h>
 
 #include "dguide.cuh"
+#include "dvol.cuh"
 #include "records.h"
 
 namespace rad {
@@ -32,7 +33,8 @@ struct PathBuffers {
 constexpr int kMaxBounce = 256;
 constexpr int kShadowBase = kMaxBounce + 1;
 constexpr int kMiscBase = 2 * kMaxBounce + 2;  // [0] spare, [1] device error word (sticky),
-                                               // [2] vol closest rays, [3] vol shadow-side rays
+                                               // [2] vol closest rays, [3] vol shadow-side rays,
+                                               // [4] vol paths taken (KVolPath's refill counter)
 constexpr int kClassBase = kMiscBase + 8;
 constexpr int kCounterWords = kClassBase + (kMaxBounce + 1) * kShadeClasses;
 
@@ -90,8 +92,9 @@ cudaError_t LaunchGatherRadiance(const PathBuffers& B, uint32_t count, float* ou
 cudaError_t LaunchResolveFilm(const FilmView& film, float scale, float* out, cudaStream_t st);
 
 // ---- volumetric path tracer (k_vol.cu): one thread per path, full Li loop
+// mode bits kVolBricks / kVolHalf / kVolRealDepth: see dvol.cuh
 cudaError_t LaunchVolPath(const DevScene& S, const PathBuffers& B, const WaveParams& w, uint32_t* err,
-                          cudaStream_t st);
+                          cudaStream_t st, uint32_t mode = 0);
 
 // ---- guide network (k_guide.cu)
 cudaError_t GuideKernelsInit();

@@ -88,8 +88,9 @@ struct alignas(16) MediumRec {
   float bbMin[4], bbMax[4];
   float toLocal[12];      // heterogeneous: world -> [0,1]^3 grid space, rows of 4
   int32_t nx, ny, nz, channels;
-  uint64_t gridOffset;    // float offset of the grid in the volume pool
-  uint64_t pad1;
+  uint64_t gridOffset;    // element offset of the grid in the volume pools (fp32 and fp16 copies)
+  uint32_t brickOffset;   // first 16^3-brick majorant in the brick pool
+  uint32_t hasBricks;     // 1: brick majorants exist (clamped grids)
 };
 static_assert(sizeof(MediumRec) == 176, "MediumRec size");
 
@@ -147,6 +148,8 @@ struct DevScene {
   const uint32_t* idx;         // global triangle indices, 3 per triangle
   const float* cdf;            // emitter-mesh area CDF / PMF (2 floats per triangle)
   const float* volume;         // density grids
+  const uint16_t* volumeHalf;  // fp16 copy of the density grids (bit patterns)
+  const float* brickMaj;       // per-medium 16^3-brick majorants (scale applied)
   const uint8_t* shapeClass;   // shade class per shape
   uint32_t nNodes, nPrims, nShapes, nLights;
   uint32_t nMedia, nMats;

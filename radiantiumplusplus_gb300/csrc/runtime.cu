@@ -481,7 +481,9 @@ void RunWave(rad_job* j) {
     uint64_t launches = 1;
     if (S.isVol) {
       ps.Begin(5, a);
-      Check(LaunchVolPath(S, lib.paths, w, lib.paths.counters + kMiscBase + 1, lib.stream), "vol_path");
+      uint32_t mode = ((j->flags & RAD_JOB_VOL_BRICKS) ? kVolBricks : 0u) | ((j->flags & RAD_JOB_VOL_FP16) ? kVolHalf : 0u) |
+                      ((j->flags & RAD_JOB_VOL_REAL_DEPTH) ? kVolRealDepth : 0u);
+      Check(LaunchVolPath(S, lib.paths, w, lib.paths.counters + kMiscBase + 1, lib.stream, mode), "vol_path");
       ps.End(5, a);
       launches++;
     } else {
@@ -702,6 +704,8 @@ uint64_t SceneUpload(const HostScene& hs, rad_scene* sc) {
   uint32_t* idx = DevAlloc<uint32_t>(hs.idx.size(), o, b);
   float* cdf = DevAlloc<float>(hs.cdf.size(), o, b);
   float* vol = DevAlloc<float>(hs.volume.size(), o, b);
+  uint16_t* volHalf = DevAlloc<uint16_t>(hs.volume.size(), o, b);
+  float* bricks = DevAlloc<float>(hs.brickMaj.size(), o, b);
   uint8_t* scls = DevAlloc<uint8_t>(hs.shapeClass.size(), o, b);
   up(nodes, hs.nodes);
   up(prims, hs.prims);
@@ -716,6 +720,11 @@ uint64_t SceneUpload(const HostScene& hs, rad_scene* sc) {
   up(idx, hs.idx);
   up(cdf, hs.cdf);
   up(vol, hs.volume);
+  up(bricks, hs.brickMaj);
+  if (!hs.volume.empty()) {
+    Check(LaunchFloatToHalf(vol, reinterpret_cast<__half*>(volHalf), hs.volume.size(), 0), "fp16 grid");
+    Check(cudaDeviceSynchronize(), "sync");
+  }
   up(scls, hs.shapeClass);
   D.nodes = nodes;
   D.prims = prims;
@@ -730,6 +739,8 @@ uint64_t SceneUpload(const HostScene& hs, rad_scene* sc) {
   D.idx = idx;
   D.cdf = cdf;
   D.volume = vol;
+  D.volumeHalf = volHalf;
+  D.brickMaj = bricks;
   D.shapeClass = scls;
   D.nNodes = (uint32_t)hs.nodes.size();
   D.nPrims = (uint32_t)hs.prims.size();

@@ -101,3 +101,35 @@ def test_ztest_against_oracle_reference(rad, oracle, scene_dir):
     rel_mse = np.mean((mean - ref) ** 2 / (ref ** 2 + 1e-2))
     assert rel_mse < 0.05
     g.close()
+
+
+def _vol_replicas(s, n, spp, seed0, **flags):
+    out = []
+    for k in range(n):
+        j = s.submit(spp=spp, seed=seed0 + k, **flags)
+        j.wait()
+        out.append(j.film())
+        j.close()
+    return np.stack(out)
+
+
+@pytest.mark.parametrize("base,flags", [({}, {"vol_fp16": True}),
+                                        ({"vol_real_depth": True}, {"vol_bricks": True}),
+                                        ({"vol_real_depth": True}, {"vol_bricks": True, "vol_fp16": True})])
+def test_volpath_modes_keep_the_expectation(rad, scene_dir, base, flags):
+    """The fp16 grid and the brick majorants change which samples are drawn, not
+    what they estimate: per-pixel Welch z-test of independent replicas. Bricks are
+    compared with the global majorant under the same estimator (null collisions
+    free, underflow-free transmittance ratios), since the reference's depth rule
+    ties truncation to the majorant."""
+    path, text, d = volume(scene_dir, 24, 24, 4, grid=32)
+    s = rad.Scene.from_file(path)
+    a = _vol_replicas(s, 8, 256, 1, **base)
+    b = _vol_replicas(s, 8, 256, 101, **flags)
+    se = np.sqrt(a.var(0, ddof=1) / a.shape[0] + b.var(0, ddof=1) / b.shape[0]) + 1e-7
+    z = (b.mean(0) - a.mean(0)) / se
+    assert np.mean(np.abs(z) < 3.5) >= 0.98, np.mean(np.abs(z) < 3.5)
+    am, bm = a.mean(axis=(1, 2, 3)), b.mean(axis=(1, 2, 3))
+    zt = (bm.mean() - am.mean()) / np.sqrt(am.var(ddof=1) / am.size + bm.var(ddof=1) / bm.size)
+    assert abs(zt) < 4.0, zt
+    s.close()
