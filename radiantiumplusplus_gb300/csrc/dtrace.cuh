@@ -187,6 +187,116 @@ RD float ByteAsFloat(uint32_t w, uint32_t i) {
 }
 #endif
 
+// Resumable traversal state: the node to visit next and the stack depth (the
+// stack itself lives with the caller).
+struct TravState {
+  uint32_t node;
+  int sp;
+};
+constexpr int kTravContinue = 0, kTravDone = 1, kTravOverflow = 2;
+
+// One node visit of the BVH8 traversal: tests the node's 8 child boxes, tests
+// the primitives of the leaf children it hits, then picks the next node (the
+// nearest internal child hit, else the stack top). Returns kTravDone when the
+// ray is finished (or, for ANY, occluded), kTravOverflow if the stack would
+// overflow (sets *err), else kTravContinue.
+template <bool ANY, bool COUNT>
+RD int TravStep(const DevScene& S, const RayPre& r, TraceHit& h, uint2* stack, TravState& st, uint32_t* err,
+                uint32_t* nNodes, uint32_t* nPrims) {
+  const uint32_t nodeIdx = st.node;
+  if (COUNT) (*nNodes)++;
+  const uint4* np = reinterpret_cast<const uint4*>(S.nodes) + 5 * (size_t)nodeIdx;
+  uint4 q0 = __ldg(np), q1 = __ldg(np + 1), q2 = __ldg(np + 2), q3 = __ldg(np + 3), q4 = __ldg(np + 4);
+  float px = __uint_as_float(q0.x), py = __uint_as_float(q0.y), pz = __uint_as_float(q0.z);
+  uint32_t ex = q0.w & 0xffu, ey = (q0.w >> 8) & 0xffu, ez = (q0.w >> 16) & 0xffu;
+  uint32_t imask = q0.w >> 24;
+  float ax = __uint_as_float(ex << 23) * r.inv.x, bx = (px - r.O.x) * r.inv.x;
+  float ay = __uint_as_float(ey << 23) * r.inv.y, by = (py - r.O.y) * r.inv.y;
+  float az = __uint_as_float(ez << 23) * r.inv.z, bz = (pz - r.O.z) * r.inv.z;
+  // near/far quantised planes per axis by ray direction
+  uint32_t nx0 = r.inv.x >= 0.f ? q2.x : q3.z, nx1 = r.inv.x >= 0.f ? q2.y : q3.w;
+  uint32_t fx0 = r.inv.x >= 0.f ? q3.z : q2.x, fx1 = r.inv.x >= 0.f ? q3.w : q2.y;
+  uint32_t ny0 = r.inv.y >= 0.f ? q2.z : q4.x, ny1 = r.inv.y >= 0.f ? q2.w : q4.y;
+  uint32_t fy0 = r.inv.y >= 0.f ? q4.x : q2.z, fy1 = r.inv.y >= 0.f ? q4.y : q2.w;
+  uint32_t nz0 = r.inv.z >= 0.f ? q3.x : q4.z, nz1 = r.inv.z >= 0.f ? q3.y : q4.w;
+  uint32_t fz0 = r.inv.z >= 0.f ? q4.z : q3.x, fz1 = r.inv.z >= 0.f ? q4.w : q3.y;
+  uint32_t childBase = q1.x, primBase = q1.y;
+  uint32_t hitInternal = 0;  // bit (slot ^ oct)
+  uint32_t leafHits = 0;     // bit slot
+  float tcur = h.t;
+#pragma unroll
+  for (uint32_t s = 0; s < 8; s++) {
+    uint32_t w = s < 4 ? 0u : 1u, i = s & 3u;
+    uint32_t meta = ByteOf(s < 4 ? q1.z : q1.w, i);
+    bool internal = (imask >> s) & 1u;
+    if (!internal && meta == 0u) continue;
+    float tnx = fmaf(ByteAsFloat(w ? nx1 : nx0, i), ax, bx);
+    float tfx = fmaf(ByteAsFloat(w ? fx1 : fx0, i), ax, bx);
+    float tny = fmaf(ByteAsFloat(w ? ny1 : ny0, i), ay, by);
+    float tfy = fmaf(ByteAsFloat(w ? fy1 : fy0, i), ay, by);
+    float tnz = fmaf(ByteAsFloat(w ? nz1 : nz0, i), az, bz);
+    float tfz = fmaf(ByteAsFloat(w ? fz1 : fz0, i), az, bz);
+    float tn = fmaxf(fmaxf(tnx, tny), fmaxf(tnz, r.tmin));
+    float tf = fminf(fminf(tfx, tfy), fminf(tfz, tcur)) * 1.00000024f;
+    if (tn <= tf) {
+      if (internal)
+        hitInternal |= 1u << (s ^ r.oct);
+      else
+        leafHits |= 1u << s;
+    }
+  }
+  // ---- leaves of this node
+  while (leafHits) {
+    uint32_t s = __ffs(leafHits) - 1;
+    leafHits &= leafHits - 1;
+    uint32_t meta = ByteOf(s < 4 ? q1.z : q1.w, s & 3u);
+    uint32_t cnt = (meta >> 5) & 3u, off = meta & 31u;
+    bool analytic = (meta >> 7) & 1u;
+    for (uint32_t k = 0; k < cnt; k++) {
+      if (COUNT) (*nPrims)++;
+      if (TestPrim(S, r, primBase + off + k, analytic, h, ANY) && ANY) return kTravDone;
+    }
+  }
+  // ---- next node
+  if (hitInternal) {
+    uint32_t b = __ffs(hitInternal) - 1;
+    hitInternal &= hitInternal - 1;
+    uint32_t s = b ^ r.oct;
+    uint32_t child = childBase + __popc(imask & ((1u << s) - 1u));
+    if (hitInternal) {
+      if (st.sp >= kTraceStack) {
+        if (err) atomicOr(err, 1u);
+        return kTravOverflow;
+      }
+      stack[st.sp++] = make_uint2(childBase, (imask << 8) | hitInternal);
+    }
+    st.node = child;
+    return kTravContinue;
+  }
+  if (st.sp == 0) return kTravDone;
+  uint2 g = stack[st.sp - 1];
+  uint32_t m = g.y & 0xffu, im = g.y >> 8;
+  uint32_t b = __ffs(m) - 1;
+  m &= m - 1;
+  uint32_t s = b ^ r.oct;
+  st.node = g.x + __popc(im & ((1u << s) - 1u));
+  if (m)
+    stack[st.sp - 1].y = (im << 8) | m;
+  else
+    st.sp--;
+  return kTravContinue;
+}
+
+RD void TraceInit(float tmax, TraceHit& h, TravState& st) {
+  h.t = tmax;
+  h.prim = kNoPrim;
+  h.u = h.v = 0.f;
+  h.shape = 0;
+  h.front = 0;
+  st.node = 0;
+  st.sp = 0;
+}
+
 // Closest hit (ANY = false) or occlusion (ANY = true). Returns false and sets
 // *err if the traversal stack would overflow (never silently truncates).
 // COUNT = true also returns the number of nodes visited and primitives tested
@@ -194,99 +304,14 @@ RD float ByteAsFloat(uint32_t w, uint32_t i) {
 template <bool ANY, bool COUNT = false>
 RD bool TraceBvh8(const DevScene& S, const RayPre& r, float tmax, TraceHit& h, uint32_t* err,
                   uint32_t* nNodes = nullptr, uint32_t* nPrims = nullptr) {
-  h.t = tmax;
-  h.prim = kNoPrim;
-  h.u = h.v = 0.f;
-  h.shape = 0;
-  h.front = 0;
+  TravState st;
+  TraceInit(tmax, h, st);
   if (S.nNodes == 0) return false;
   uint2 stack[kTraceStack];
-  int sp = 0;
-  uint32_t nodeIdx = 0;
-  const uint4* N4 = reinterpret_cast<const uint4*>(S.nodes);
-  for (;;) {
-    // ---- visit node
-    if (COUNT) (*nNodes)++;
-    const uint4* np = N4 + 5 * (size_t)nodeIdx;
-    uint4 q0 = __ldg(np), q1 = __ldg(np + 1), q2 = __ldg(np + 2), q3 = __ldg(np + 3), q4 = __ldg(np + 4);
-    float px = __uint_as_float(q0.x), py = __uint_as_float(q0.y), pz = __uint_as_float(q0.z);
-    uint32_t ex = q0.w & 0xffu, ey = (q0.w >> 8) & 0xffu, ez = (q0.w >> 16) & 0xffu;
-    uint32_t imask = q0.w >> 24;
-    float ax = __uint_as_float(ex << 23) * r.inv.x, bx = (px - r.O.x) * r.inv.x;
-    float ay = __uint_as_float(ey << 23) * r.inv.y, by = (py - r.O.y) * r.inv.y;
-    float az = __uint_as_float(ez << 23) * r.inv.z, bz = (pz - r.O.z) * r.inv.z;
-    // near/far quantised planes per axis by ray direction
-    uint32_t nx0 = r.inv.x >= 0.f ? q2.x : q3.z, nx1 = r.inv.x >= 0.f ? q2.y : q3.w;
-    uint32_t fx0 = r.inv.x >= 0.f ? q3.z : q2.x, fx1 = r.inv.x >= 0.f ? q3.w : q2.y;
-    uint32_t ny0 = r.inv.y >= 0.f ? q2.z : q4.x, ny1 = r.inv.y >= 0.f ? q2.w : q4.y;
-    uint32_t fy0 = r.inv.y >= 0.f ? q4.x : q2.z, fy1 = r.inv.y >= 0.f ? q4.y : q2.w;
-    uint32_t nz0 = r.inv.z >= 0.f ? q3.x : q4.z, nz1 = r.inv.z >= 0.f ? q3.y : q4.w;
-    uint32_t fz0 = r.inv.z >= 0.f ? q4.z : q3.x, fz1 = r.inv.z >= 0.f ? q4.w : q3.y;
-    uint32_t childBase = q1.x, primBase = q1.y;
-    uint32_t hitInternal = 0;  // bit (slot ^ oct)
-    uint32_t leafHits = 0;     // bit slot
-    float tcur = h.t;
-#pragma unroll
-    for (uint32_t s = 0; s < 8; s++) {
-      uint32_t w = s < 4 ? 0u : 1u, i = s & 3u;
-      uint32_t meta = ByteOf(s < 4 ? q1.z : q1.w, i);
-      bool internal = (imask >> s) & 1u;
-      if (!internal && meta == 0u) continue;
-      float tnx = fmaf(ByteAsFloat(w ? nx1 : nx0, i), ax, bx);
-      float tfx = fmaf(ByteAsFloat(w ? fx1 : fx0, i), ax, bx);
-      float tny = fmaf(ByteAsFloat(w ? ny1 : ny0, i), ay, by);
-      float tfy = fmaf(ByteAsFloat(w ? fy1 : fy0, i), ay, by);
-      float tnz = fmaf(ByteAsFloat(w ? nz1 : nz0, i), az, bz);
-      float tfz = fmaf(ByteAsFloat(w ? fz1 : fz0, i), az, bz);
-      float tn = fmaxf(fmaxf(tnx, tny), fmaxf(tnz, r.tmin));
-      float tf = fminf(fminf(tfx, tfy), fminf(tfz, tcur)) * 1.00000024f;
-      if (tn <= tf) {
-        if (internal)
-          hitInternal |= 1u << (s ^ r.oct);
-        else
-          leafHits |= 1u << s;
-      }
-    }
-    // ---- leaves of this node
-    while (leafHits) {
-      uint32_t s = __ffs(leafHits) - 1;
-      leafHits &= leafHits - 1;
-      uint32_t meta = ByteOf(s < 4 ? q1.z : q1.w, s & 3u);
-      uint32_t cnt = (meta >> 5) & 3u, off = meta & 31u;
-      bool analytic = (meta >> 7) & 1u;
-      for (uint32_t k = 0; k < cnt; k++) {
-        if (COUNT) (*nPrims)++;
-        if (TestPrim(S, r, primBase + off + k, analytic, h, ANY) && ANY) return true;
-      }
-    }
-    // ---- next node
-    if (hitInternal) {
-      uint32_t b = __ffs(hitInternal) - 1;
-      hitInternal &= hitInternal - 1;
-      uint32_t s = b ^ r.oct;
-      uint32_t child = childBase + __popc(imask & ((1u << s) - 1u));
-      if (hitInternal) {
-        if (sp >= kTraceStack) {
-          if (err) atomicOr(err, 1u);
-          return false;
-        }
-        stack[sp++] = make_uint2(childBase, (imask << 8) | hitInternal);
-      }
-      nodeIdx = child;
-      continue;
-    }
-    if (sp == 0) break;
-    uint2 g = stack[sp - 1];
-    uint32_t m = g.y & 0xffu, im = g.y >> 8;
-    uint32_t b = __ffs(m) - 1;
-    m &= m - 1;
-    uint32_t s = b ^ r.oct;
-    nodeIdx = g.x + __popc(im & ((1u << s) - 1u));
-    if (m)
-      stack[sp - 1].y = (im << 8) | m;
-    else
-      sp--;
+  int res;
+  while ((res = TravStep<ANY, COUNT>(S, r, h, stack, st, err, nNodes, nPrims)) == kTravContinue) {
   }
+  if (res == kTravOverflow) return false;
   return h.prim != kNoPrim;
 }
 

@@ -91,25 +91,62 @@ __device__ __forceinline__ void FlushTravCounts(unsigned long long* out, uint32_
   }
 }
 
+// Persistent ray fetch: a warp keeps tracing one BVH8 node per lane per step
+// while at least kRefillBusy of its lanes are still busy; then the lanes whose
+// rays finished write their results and every idle lane takes the next ray of
+// the queue from a per-bounce counter (one atomic per warp). Lanes of a warp thus
+// stay busy although ray traversal lengths vary widely (one ray per thread left
+// ~9 of 32 lanes active per instruction).
+constexpr int kRefillBusy = 20;
+
 template <bool COUNT>
 __global__ void __launch_bounds__(kBlock, 8) KExtend(DevScene S, PathBuffers B, int depth, unsigned long long* trav) {
-  uint32_t count = B.counters[depth];
+  const uint32_t count = B.counters[depth];
   const uint32_t* qin = B.q[depth & 1];
+  uint32_t* fetch = B.counters + kFetchBase + 2 * depth;
   uint32_t* err = B.counters + kMiscBase + 1;
   uint32_t* classCnt = B.counters + kClassBase + depth * kShadeClasses;
-  bool lastDepth = S.maxDepth >= 0 && depth + 1 >= S.maxDepth;
+  const bool lastDepth = S.maxDepth >= 0 && depth + 1 >= S.maxDepth;
+  const uint32_t lane = threadIdx.x & 31u;
   uint32_t nN = 0, nP = 0;
-  uint32_t lane = threadIdx.x & 31u;
-  // warp-uniform loop: every lane takes part in the class appends
-  for (uint32_t base = blockIdx.x * blockDim.x; base < count; base += gridDim.x * blockDim.x) {
-    uint32_t i = base + threadIdx.x;
-    uint32_t cls = 0xffu, p = 0;
-    if (i < count) {
-      p = qin[i];
-      float4 o = B.rayO[p], d = B.rayD[p];
-      RayPre r = MakeRayPre(V3{o.x, o.y, o.z}, V3{d.x, d.y, d.z}, o.w);
-      TraceHit h;
-      TraceBvh8<false, COUNT>(S, r, d.w, h, err, &nN, &nP);
+  bool live = false, done = false, drained = false;
+  uint32_t p = 0;
+  RayPre r;
+  TraceHit h;
+  TravState st;
+  uint2 stack[kTraceStack];
+  for (;;) {
+    // ---- idle lanes take the next rays of the queue
+    uint32_t need = __ballot_sync(0xffffffffu, !live);
+    if (need && !drained) {
+      int leader = __ffs(need) - 1;
+      uint32_t base = 0;
+      if ((int)lane == leader) base = atomicAdd(fetch, (uint32_t)__popc(need));
+      base = __shfl_sync(0xffffffffu, base, leader);
+      if (base + (uint32_t)__popc(need) >= count) drained = true;
+      if (!live) {
+        uint32_t i = base + __popc(need & ((1u << lane) - 1u));
+        if (i < count) {
+          p = qin[i];
+          float4 o = B.rayO[p], d = B.rayD[p];
+          r = MakeRayPre(V3{o.x, o.y, o.z}, V3{d.x, d.y, d.z}, o.w);
+          TraceInit(d.w, h, st);
+          live = true;
+          done = S.nNodes == 0;
+        }
+      }
+    }
+    if (__ballot_sync(0xffffffffu, live) == 0u) break;
+    // ---- trace until too few lanes are busy (all of them once the queue is drained)
+    const int minBusy = drained ? 1 : kRefillBusy;
+    for (;;) {
+      if (live && !done) done = TravStep<false, COUNT>(S, r, h, stack, st, err, &nN, &nP) != kTravContinue;
+      if (__popc(__ballot_sync(0xffffffffu, live && !done)) < minBusy) break;
+    }
+    // ---- finished lanes: hit record and shade-class append
+    const bool fin = live && done;
+    uint32_t cls = 0xffu;
+    if (fin) {
       HitRec hr;
       hr.t = h.t;
       hr.u = h.u;
@@ -120,6 +157,7 @@ __global__ void __launch_bounds__(kBlock, 8) KExtend(DevScene S, PathBuffers B, 
       hr.pad[0] = hr.pad[1] = 0;
       B.hit[p] = hr;
       cls = (h.prim == kNoPrim || lastDepth) ? SC_EMIT : (uint32_t)S.shapeClass[h.shape];
+      live = false;
     }
     // group lanes by shade class; one atomic per class present in the warp
     uint32_t grp = __match_any_sync(0xffffffffu, cls);
@@ -352,25 +390,64 @@ __global__ void __launch_bounds__(kBlock) KShadeClass(DevScene S, PathBuffers B,
 
 template <bool COUNT>
 __global__ void __launch_bounds__(kBlock, 8) KShadow(DevScene S, PathBuffers B, int depth, unsigned long long* trav) {
-  uint32_t count = B.counters[kShadowBase + depth];
+  const uint32_t count = B.counters[kShadowBase + depth];
+  uint32_t* fetch = B.counters + kFetchBase + 2 * depth + 1;
   uint32_t* err = B.counters + kMiscBase + 1;
+  const uint32_t lane = threadIdx.x & 31u;
   uint32_t nN = 0, nP = 0;
-  for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < count; i += gridDim.x * blockDim.x) {
-    float4 o = B.shO[i], d = B.shD[i];
-    RayPre r = MakeRayPre(V3{o.x, o.y, o.z}, V3{d.x, d.y, d.z}, 0.f);
-    TraceHit h;
-    bool occ = TraceBvh8<true, COUNT>(S, r, o.w, h, err, &nN, &nP);
-    if (!occ) {
-      uint32_t p = __float_as_uint(d.w);
-      float4 c = B.shC[i];
-      float4 l = B.L[p];
-      B.L[p] = make_float4(l.x + c.x, l.y + c.y, l.z + c.z, l.w);
-      uint32_t rec = __float_as_uint(c.w);  // guide training record + 1, or 0
-      if (rec) {
-        float4* r4 = B.guideRec + (size_t)(rec - 1u) * kGRecF4 + 4;
-        float4 lb = *r4;
-        *r4 = make_float4(lb.x + c.x, lb.y + c.y, lb.z + c.z, lb.w);
+  bool live = false, done = false, drained = false, occ = false;
+  uint32_t i = 0;
+  RayPre r;
+  TraceHit h;
+  TravState st;
+  uint2 stack[kTraceStack];
+  for (;;) {
+    uint32_t need = __ballot_sync(0xffffffffu, !live);
+    if (need && !drained) {
+      int leader = __ffs(need) - 1;
+      uint32_t base = 0;
+      if ((int)lane == leader) base = atomicAdd(fetch, (uint32_t)__popc(need));
+      base = __shfl_sync(0xffffffffu, base, leader);
+      if (base + (uint32_t)__popc(need) >= count) drained = true;
+      if (!live) {
+        uint32_t k = base + __popc(need & ((1u << lane) - 1u));
+        if (k < count) {
+          i = k;
+          float4 o = B.shO[i], d = B.shD[i];
+          r = MakeRayPre(V3{o.x, o.y, o.z}, V3{d.x, d.y, d.z}, 0.f);
+          TraceInit(o.w, h, st);
+          live = true;
+          done = S.nNodes == 0;
+          occ = false;
+        }
       }
+    }
+    if (__ballot_sync(0xffffffffu, live) == 0u) break;
+    const int minBusy = drained ? 1 : kRefillBusy;
+    for (;;) {
+      if (live && !done) {
+        int res = TravStep<true, COUNT>(S, r, h, stack, st, err, &nN, &nP);
+        if (res != kTravContinue) {
+          done = true;
+          occ = res == kTravDone && h.prim != kNoPrim;
+        }
+      }
+      if (__popc(__ballot_sync(0xffffffffu, live && !done)) < minBusy) break;
+    }
+    if (live && done) {
+      if (!occ) {
+        uint32_t p = __float_as_uint(B.shD[i].w);
+        float4 c = B.shC[i];
+        float4 l = B.L[p];
+        B.L[p] = make_float4(l.x + c.x, l.y + c.y, l.z + c.z, l.w);
+        uint32_t rec = __float_as_uint(c.w);  // guide training record + 1, or 0
+        if (rec) {
+          float4* r4 = B.guideRec + (size_t)(rec - 1u) * kGRecF4 + 4;
+          float4 lb = *r4;
+          *r4 = make_float4(lb.x + c.x, lb.y + c.y, lb.z + c.z, lb.w);
+        }
+      }
+      live = false;
     }
   }
   if (COUNT) FlushTravCounts(trav + 2, nN, nP);

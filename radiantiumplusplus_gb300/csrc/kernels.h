@@ -36,7 +36,9 @@ constexpr int kMiscBase = 2 * kMaxBounce + 2;  // [0] spare, [1] device error wo
                                                // [2] vol closest rays, [3] vol shadow-side rays,
                                                // [4] vol paths taken (KVolPath's refill counter)
 constexpr int kClassBase = kMiscBase + 8;
-constexpr int kCounterWords = kClassBase + (kMaxBounce + 1) * kShadeClasses;
+// per-bounce ray-fetch counters of the persistent extend / shadow kernels
+constexpr int kFetchBase = kClassBase + (kMaxBounce + 1) * kShadeClasses;
+constexpr int kCounterWords = kFetchBase + 2 * (kMaxBounce + 1);
 
 struct FilmView {
   float4* accum;  // rgb sum, sample count in w
