@@ -195,6 +195,8 @@ def run_ours(args, world, rank, local):
         scene = rad.Scene.from_file(path)
         load_s = time.perf_counter() - t0
         spp_step = 1
+        # launch parameters of the traversal kernels for this scene (rad_autotune, not timed)
+        tune = scene.autotune()
         # traversal statistics for the roofline's algorithmic bytes (not timed)
         j = scene.submit(spp=1, first_sample=10_000, count_traversal=True)
         j.wait()
@@ -264,7 +266,10 @@ def run_ours(args, world, rank, local):
                    "width": W, "height": H, "spp_per_step": spp_step, "max_depth": MAX_DEPTH, "rr_depth": 3,
                    "parallelism": "replicas" if world > 1 else "single_gpu",
                    "l2": "inputs larger than L2: resident scene + path state > 129 MB",
-                   "scene_load_s": round(load_s, 3)},
+                   "scene_load_s": round(load_s, 3),
+                   "autotune": {"refill_busy": tune["refill_busy"], "blocks_per_sm": tune["blocks_per_sm"],
+                                "wave_ms_tuned": round(tune["best_ms"], 3),
+                                "wave_ms_default": round(tune["default_ms"], 3)}},
         "mrays_per_s": mrays,
         "rays_per_sample": (st["rays_closest"] + st["rays_shadow"]) / max(1, st["samples"]),
         "gpu_launches": st["kernel_launches"],

@@ -122,6 +122,13 @@ class Scene:
         return Job(self, spp, seed, first_sample, profile, sync, count_traversal, guide, vol_bricks, vol_fp16,
                    vol_real_depth)
 
+    def autotune(self, config=None):
+        """Pick the traversal launch parameters for this scene by timing waves (rad_autotune)."""
+        r = _capi.TuneResult()
+        text = None if config is None else json.dumps(config).encode()
+        check(lib().rad_autotune(self._h, text, ctypes.byref(r)))
+        return {k: getattr(r, k) for k, _ in r._fields_}
+
     # ---- learned path guiding (no counterpart in the reference)
     def guide_enable(self, config=None):
         """Create (re-seed) the scene's guide network; config: dict of rad_guide_enable keys."""

@@ -43,7 +43,7 @@ EXPORTS = [
     "rad_job_film", "rad_job_stats", "rad_job_destroy", "rad_trace_batch", "rad_trace_batch_device",
     "rad_bsdf_eval_batch", "rad_bsdf_sample_batch", "rad_camera_rays", "rad_render_samples",
     "rad_render_samples_noalloc", "rad_guide_enable", "rad_guide_info", "rad_guide_checkpoint",
-    "rad_guide_load", "rad_guide_forward", "rad_guide_mix_eval", "rad_guide_grad",
+    "rad_guide_load", "rad_guide_forward", "rad_guide_mix_eval", "rad_guide_grad", "rad_autotune",
 ]
 
 
@@ -80,6 +80,11 @@ class Stats(ctypes.Structure):
                 ("trav_prims_shadow", ctypes.c_uint64), ("guide_records", ctypes.c_uint64),
                 ("guide_train_steps", ctypes.c_uint64), ("ms_guide_infer", ctypes.c_double),
                 ("ms_guide_train", ctypes.c_double)]
+
+
+class TuneResult(ctypes.Structure):
+    _fields_ = [("refill_busy", ctypes.c_int32), ("blocks_per_sm", ctypes.c_int32), ("candidates", ctypes.c_int32),
+                ("best_ms", ctypes.c_double), ("default_ms", ctypes.c_double)]
 
 
 class GuideInfo(ctypes.Structure):
@@ -132,6 +137,7 @@ def load(path=LIB_PATH):
         "rad_guide_forward": [P, P, I64, P, P],
         "rad_guide_mix_eval": [P, P, P, I64, P, P],
         "rad_guide_grad": [P, P, I64, P, P],
+        "rad_autotune": [P, ctypes.c_char_p, P],
     }
     for name, args in sig.items():
         fn = getattr(L, name)

@@ -92,15 +92,14 @@ __device__ __forceinline__ void FlushTravCounts(unsigned long long* out, uint32_
 }
 
 // Persistent ray fetch: a warp keeps tracing one BVH8 node per lane per step
-// while at least kRefillBusy of its lanes are still busy; then the lanes whose
+// while at least `refillBusy` of its lanes are still busy; then the lanes whose
 // rays finished write their results and every idle lane takes the next ray of
 // the queue from a per-bounce counter (one atomic per warp). Lanes of a warp thus
 // stay busy although ray traversal lengths vary widely (one ray per thread left
 // ~9 of 32 lanes active per instruction).
-constexpr int kRefillBusy = 20;
-
 template <bool COUNT>
-__global__ void __launch_bounds__(kBlock, 8) KExtend(DevScene S, PathBuffers B, int depth, unsigned long long* trav) {
+__global__ void __launch_bounds__(kBlock, 8)
+    KExtend(DevScene S, PathBuffers B, int depth, unsigned long long* trav, int refillBusy) {
   const uint32_t count = B.counters[depth];
   const uint32_t* qin = B.q[depth & 1];
   uint32_t* fetch = B.counters + kFetchBase + 2 * depth;
@@ -138,7 +137,7 @@ __global__ void __launch_bounds__(kBlock, 8) KExtend(DevScene S, PathBuffers B, 
     }
     if (__ballot_sync(0xffffffffu, live) == 0u) break;
     // ---- trace until too few lanes are busy (all of them once the queue is drained)
-    const int minBusy = drained ? 1 : kRefillBusy;
+    const int minBusy = drained ? 1 : refillBusy;
     for (;;) {
       if (live && !done) done = TravStep<false, COUNT>(S, r, h, stack, st, err, &nN, &nP) != kTravContinue;
       if (__popc(__ballot_sync(0xffffffffu, live && !done)) < minBusy) break;
@@ -389,7 +388,8 @@ __global__ void __launch_bounds__(kBlock) KShadeClass(DevScene S, PathBuffers B,
 }
 
 template <bool COUNT>
-__global__ void __launch_bounds__(kBlock, 8) KShadow(DevScene S, PathBuffers B, int depth, unsigned long long* trav) {
+__global__ void __launch_bounds__(kBlock, 8)
+    KShadow(DevScene S, PathBuffers B, int depth, unsigned long long* trav, int refillBusy) {
   const uint32_t count = B.counters[kShadowBase + depth];
   uint32_t* fetch = B.counters + kFetchBase + 2 * depth + 1;
   uint32_t* err = B.counters + kMiscBase + 1;
@@ -423,7 +423,7 @@ __global__ void __launch_bounds__(kBlock, 8) KShadow(DevScene S, PathBuffers B, 
       }
     }
     if (__ballot_sync(0xffffffffu, live) == 0u) break;
-    const int minBusy = drained ? 1 : kRefillBusy;
+    const int minBusy = drained ? 1 : refillBusy;
     for (;;) {
       if (live && !done) {
         int res = TravStep<true, COUNT>(S, r, h, stack, st, err, &nN, &nP);
@@ -516,11 +516,11 @@ cudaError_t LaunchGenerate(const DevScene& S, const PathBuffers& B, const WavePa
   return cudaGetLastError();
 }
 cudaError_t LaunchExtend(const DevScene& S, const PathBuffers& B, int depth, int grid, cudaStream_t st,
-                         unsigned long long* trav) {
+                         unsigned long long* trav, int refillBusy) {
   if (trav)
-    KExtend<true><<<grid, kBlock, 0, st>>>(S, B, depth, trav);
+    KExtend<true><<<grid, kBlock, 0, st>>>(S, B, depth, trav, refillBusy);
   else
-    KExtend<false><<<grid, kBlock, 0, st>>>(S, B, depth, nullptr);
+    KExtend<false><<<grid, kBlock, 0, st>>>(S, B, depth, nullptr, refillBusy);
   return cudaGetLastError();
 }
 cudaError_t LaunchShade(const DevScene& S, const PathBuffers& B, int depth, int grid, cudaStream_t st,
@@ -542,11 +542,11 @@ cudaError_t LaunchShade(const DevScene& S, const PathBuffers& B, int depth, int 
   return cudaGetLastError();
 }
 cudaError_t LaunchShadow(const DevScene& S, const PathBuffers& B, int depth, int grid, cudaStream_t st,
-                         unsigned long long* trav) {
+                         unsigned long long* trav, int refillBusy) {
   if (trav)
-    KShadow<true><<<grid, kBlock, 0, st>>>(S, B, depth, trav);
+    KShadow<true><<<grid, kBlock, 0, st>>>(S, B, depth, trav, refillBusy);
   else
-    KShadow<false><<<grid, kBlock, 0, st>>>(S, B, depth, nullptr);
+    KShadow<false><<<grid, kBlock, 0, st>>>(S, B, depth, nullptr, refillBusy);
   return cudaGetLastError();
 }
 cudaError_t LaunchAccumulate(const PathBuffers& B, const FilmView& film, uint32_t count, cudaStream_t st,

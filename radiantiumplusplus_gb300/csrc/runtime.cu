@@ -102,6 +102,7 @@ struct rad_scene {
   float worldLo[3] = {0, 0, 0}, worldHi[3] = {1, 1, 1};
   GuideNet* guide = nullptr;  // learned proposal, created by rad_guide_enable / _load or a guided job
   GuideConfig guideCfg;
+  TraceTune tune;  // traversal launch parameters (rad_autotune)
 };
 
 struct rad_job {
@@ -265,17 +266,18 @@ struct ProfSink {
 };
 
 // Launches the bounce loop for `count` generated paths. Returns kernels launched.
-uint64_t LaunchBounces(const DevScene& S, uint32_t count, ProfSink& ps, unsigned long long* trav = nullptr,
-                       const GuideDev* G = nullptr) {
+uint64_t LaunchBounces(const DevScene& S, const TraceTune& tu, uint32_t count, ProfSink& ps,
+                       unsigned long long* trav = nullptr, const GuideDev* G = nullptr) {
   Lib& lib = L();
   uint64_t launches = 0;
   int grid = std::max(1, std::min(lib.sms * 8, (int)((count + 127) / 128)));
+  int tgrid = std::max(1, std::min(lib.sms * tu.blocksPerSm, (int)((count + 127) / 128)));
   int iters = S.maxDepth >= 0 ? std::max(1, S.maxDepth) : kMaxBounce;
   if (iters > kMaxBounce) iters = kMaxBounce;
   for (int d = 0; d < iters; d++) {
     cudaEvent_t a = nullptr;
     ps.Begin(1, a);
-    Check(LaunchExtend(S, lib.paths, d, grid, lib.stream, trav), "extend");
+    Check(LaunchExtend(S, lib.paths, d, tgrid, lib.stream, trav, tu.refillBusy), "extend");
     ps.End(1, a);
     if (G) {
       ps.Begin(6, a);
@@ -287,7 +289,7 @@ uint64_t LaunchBounces(const DevScene& S, uint32_t count, ProfSink& ps, unsigned
     Check(LaunchShade(S, lib.paths, d, grid, lib.stream, G), "shade");
     ps.End(2, a);
     ps.Begin(3, a);
-    Check(LaunchShadow(S, lib.paths, d, grid, lib.stream, trav), "shadow");
+    Check(LaunchShadow(S, lib.paths, d, tgrid, lib.stream, trav, tu.refillBusy), "shadow");
     ps.End(3, a);
     launches += 2 + kShadeClasses;
     if (S.maxDepth < 0 && (d % 8) == 7) {
@@ -392,7 +394,7 @@ void RunWaveGuided(rad_job* j) {
     ps.Begin(0, a);
     Check(LaunchGenerate(S, lib.paths, w, lib.stream), "generate");
     ps.End(0, a);
-    uint64_t launches = 1 + LaunchBounces(S, count, ps, nullptr, &G);
+    uint64_t launches = 1 + LaunchBounces(S, j->scene->tune, count, ps, nullptr, &G);
     ps.Begin(4, a);
     Check(LaunchAccumulate(lib.paths, film, count, lib.stream), "accumulate");
     ps.End(4, a);
@@ -433,7 +435,7 @@ void RunWaveGraph(rad_job* j) {
       cudaGraph_t g = nullptr;
       Check(cudaStreamBeginCapture(lib.stream, cudaStreamCaptureModeThreadLocal), "begin capture");
       cudaError_t e1 = LaunchGenerate(S, lib.paths, w, lib.stream);
-      uint64_t k = 1 + LaunchBounces(S, count, none);
+      uint64_t k = 1 + LaunchBounces(S, j->scene->tune, count, none);
       cudaError_t e2 = LaunchAccumulate(lib.paths, film, count, lib.stream, j->ctx + c);
       cudaError_t e3 = cudaStreamEndCapture(lib.stream, &g);
       Check(e1, "generate capture");
@@ -487,7 +489,8 @@ void RunWave(rad_job* j) {
       ps.End(5, a);
       launches++;
     } else {
-      launches += LaunchBounces(S, count, ps, (j->flags & RAD_JOB_COUNT_TRAVERSAL) ? j->dStats + 4 : nullptr);
+      launches += LaunchBounces(S, j->scene->tune, count, ps,
+                                (j->flags & RAD_JOB_COUNT_TRAVERSAL) ? j->dStats + 4 : nullptr);
     }
     ps.Begin(4, a);
     Check(LaunchAccumulate(lib.paths, film, count, lib.stream), "accumulate");
@@ -1185,7 +1188,7 @@ int rad_render_samples(rad_scene* scene, const uint32_t* pixels, const uint32_t*
       if (scene->dev.isVol) {
         Check(LaunchVolPath(scene->dev, lib.paths, w, lib.paths.counters + kMiscBase + 1, lib.stream), "vol_path");
       } else {
-        LaunchBounces(scene->dev, count, ps);
+        LaunchBounces(scene->dev, scene->tune, count, ps);
       }
       Check(LaunchGatherRadiance(lib.paths, count, dout.p + 3 * b, lib.stream), "gather");
     }
@@ -1361,6 +1364,83 @@ int rad_guide_info(rad_scene* scene, rad_guide_info_t* info) {
     }
     info->adam_steps = n.step;
     info->device_bytes = n.bytes;
+  });
+}
+
+// ---- autotuner ----------------------------------------------------------------
+// Times full waves (generate + the bounce loop, sample 0 of the first pixel
+// chunk, so every candidate traces the same paths) for each candidate launch
+// configuration and keeps the fastest in the scene.
+int rad_autotune(rad_scene* scene, const char* config_json, rad_tune_result* out) {
+  if (!scene) return Fail(RAD_ERR_INVALID_ARG, "null scene");
+  if (scene->dev.isVol) return Fail(RAD_ERR_UNSUPPORTED, "the autotuner covers the `path` traversal kernels");
+  return Guard([&] {
+    EnsureInit();
+    int reps = 2;
+    std::vector<int> refill = {12, 16, 20, 24, 28}, perSm = {4, 6, 8};
+    if (config_json && *config_json) {
+      JValue c = JsonReader::Parse(config_json);
+      if (const JValue* v = c.get("reps")) reps = std::max(1, (int)v->n);
+      auto list = [&](const char* k, std::vector<int>& dst, int lo, int hi) {
+        if (const JValue* v = c.get(k)) {
+          if (!v->isArr() || v->a.empty()) throw Error{RAD_ERR_INVALID_ARG, std::string(k) + " must be a list"};
+          dst.clear();
+          for (const JValue& e : v->a) {
+            int x = (int)e.n;
+            if (x < lo || x > hi) throw Error{RAD_ERR_INVALID_ARG, std::string(k) + " value out of range"};
+            dst.push_back(x);
+          }
+        }
+      };
+      list("refill_busy", refill, 1, 32);
+      list("blocks_per_sm", perSm, 1, 8);
+    }
+    Lib& lib = L();
+    std::lock_guard<std::mutex> g(lib.gpuMu);
+    const DevScene& S = scene->dev;
+    uint64_t npix = (uint64_t)S.cam.width * S.cam.height;
+    uint32_t count = (uint32_t)std::min<uint64_t>(npix, lib.maxPaths);
+    cudaEvent_t a = GetEvent(), b = GetEvent();
+    ProfSink none{nullptr};
+    auto wave = [&](const TraceTune& tu) {
+      WaveParams w{0, count, 0, scene->info.seed, nullptr, nullptr};
+      Check(LaunchGenerate(S, lib.paths, w, lib.stream), "generate");
+      LaunchBounces(S, tu, count, none);
+    };
+    rad_tune_result res{};
+    res.best_ms = 1e30;
+    for (int pb : perSm)
+      for (int rb : refill) {
+        TraceTune tu;
+        tu.refillBusy = rb;
+        tu.blocksPerSm = pb;
+        wave(tu);  // warm-up
+        Check(cudaEventRecord(a, lib.stream), "event");
+        for (int k = 0; k < reps; k++) wave(tu);
+        Check(cudaEventRecord(b, lib.stream), "event");
+        Check(cudaEventSynchronize(b), "sync");
+        float ms = 0.f;
+        cudaEventElapsedTime(&ms, a, b);
+        ms /= (float)reps;
+        if (rb == TraceTune{}.refillBusy && pb == TraceTune{}.blocksPerSm) res.default_ms = ms;
+        if (ms < res.best_ms) {
+          res.best_ms = ms;
+          res.refill_busy = rb;
+          res.blocks_per_sm = pb;
+        }
+        res.candidates++;
+      }
+    lib.evPool.push_back(a);
+    lib.evPool.push_back(b);
+    uint32_t errWord = 0;
+    Check(cudaMemcpy(&errWord, lib.paths.counters + kMiscBase + 1, 4, cudaMemcpyDeviceToHost), "copy");
+    if (errWord) {
+      cudaMemset(lib.paths.counters + kMiscBase + 1, 0, 4);
+      throw Error{RAD_ERR_DEVICE_CHECK, "device-side check fired while tuning"};
+    }
+    scene->tune.refillBusy = res.refill_busy;
+    scene->tune.blocksPerSm = res.blocks_per_sm;
+    if (out) *out = res;
   });
 }
 

@@ -82,3 +82,19 @@ def test_graph_replay_equals_direct_launches(rad, scene_dir):
     g.close()
     d.close()
     s.close()
+
+
+def test_autotune_picks_parameters_and_keeps_results(rad, scene_dir):
+    """The tuner only changes launch shapes: the film is bit-identical before and after."""
+    s = rad.Scene.from_file(spheres(scene_dir, 200, 3, 40, 24, 5)[0])
+    before = s.render(spp=3, seed=7)
+    r = s.autotune({"reps": 1})
+    assert r["candidates"] == 15 and r["refill_busy"] in (12, 16, 20, 24, 28) and r["blocks_per_sm"] in (4, 6, 8)
+    assert r["best_ms"] > 0 and r["best_ms"] <= r["default_ms"]
+    assert np.array_equal(before, s.render(spp=3, seed=7))
+    r2 = s.autotune({"refill_busy": [1, 32], "blocks_per_sm": [2], "reps": 1})
+    assert r2["candidates"] == 2 and r2["blocks_per_sm"] == 2
+    assert np.array_equal(before, s.render(spp=3, seed=7))
+    with pytest.raises(rad.RadError):
+        s.autotune({"refill_busy": [40]})
+    s.close()
