@@ -59,8 +59,11 @@ __global__ void __launch_bounds__(kBlock) KGenerate(DevScene S, PathBuffers B, W
     if (k != (uint32_t)(kMiscBase + 1)) B.counters[k] = k == 0 ? w.count : 0u;
   }
   if (i >= w.count) return;
-  uint32_t pix = w.pixelList ? w.pixelList[i] : w.pixelBegin + i;
-  uint32_t smp = w.sampleList ? w.sampleList[i] : (w.ctx ? w.ctx->sample : w.sample);
+  const uint32_t spw = w.spw > 1u ? w.spw : 1u;
+  const uint32_t npc = w.count / spw;  // pixels per sample of this wave
+  const uint32_t j = spw > 1u ? i % npc : i, s = spw > 1u ? i / npc : 0u;
+  uint32_t pix = w.pixelList ? w.pixelList[i] : w.pixelBegin + j;
+  uint32_t smp = w.sampleList ? w.sampleList[i] : (w.ctx ? w.ctx->sample : w.sample) + s;
   uint32_t seed = w.ctx ? w.ctx->seed : w.seed;
   uint32_t x = pix % (uint32_t)S.cam.width, y = pix / (uint32_t)S.cam.width;
   Pcg32 rng = PcgForSample(pix, smp, seed);
@@ -455,12 +458,15 @@ __global__ void __launch_bounds__(kBlock, 8)
 
 // sample_renderer.cpp:101-105: drop NaN in any channel, Inf / negative in the
 // first channel only (spectrum.h:28-29), the sample still counts in 1/spp.
-__global__ void __launch_bounds__(256) KAccumulate(PathBuffers B, FilmView film, uint32_t count, WaveCtx* ctx) {
+// One thread per pixel of the wave; with spw samples per wave it adds them in
+// sample order, so the film is the same as after spw one-sample waves.
+__global__ void __launch_bounds__(256)
+    KAccumulate(PathBuffers B, FilmView film, uint32_t count, WaveCtx* ctx, uint32_t spw) {
   uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
   if (ctx) {
     film.accum = ctx->film;
     film.stats = ctx->stats;
-    if (i == 0) ctx->sample += 1;  // generate of this wave has completed: advance for the next replay
+    if (i == 0) ctx->sample += spw;  // generate of this wave has completed: advance for the next replay
   }
   if (i == 0 && film.stats) {
     unsigned long long cl = 0, sh = 0;
@@ -474,22 +480,27 @@ __global__ void __launch_bounds__(256) KAccumulate(PathBuffers B, FilmView film,
     film.stats[1] += sh;
     film.stats[3] += count;
   }
-  bool bad = false;
-  if (i < count) {
-    float4 l = B.L[i];
+  const uint32_t npc = count / spw;
+  uint32_t nbad = 0;
+  if (i < npc) {
     uint32_t pix = B.pixel[i];
-    bad = isnan(l.x) || isnan(l.y) || isnan(l.z) || isinf(l.x) || l.x < 0.f;
     float4 a = film.accum[pix];
-    if (!bad) {
-      a.x += l.x;
-      a.y += l.y;
-      a.z += l.z;
+    for (uint32_t s = 0; s < spw; s++) {
+      float4 l = B.L[(size_t)s * npc + i];
+      bool bad = isnan(l.x) || isnan(l.y) || isnan(l.z) || isinf(l.x) || l.x < 0.f;
+      if (!bad) {
+        a.x += l.x;
+        a.y += l.y;
+        a.z += l.z;
+      } else {
+        nbad++;
+      }
+      a.w += 1.f;
     }
-    a.w += 1.f;
     film.accum[pix] = a;
   }
-  uint32_t m = __ballot_sync(0xffffffffu, bad);
-  if (m && (threadIdx.x & 31u) == 0 && film.stats) atomicAdd(film.stats + 2, (unsigned long long)__popc(m));
+  for (int o = 16; o > 0; o >>= 1) nbad += __shfl_down_sync(0xffffffffu, nbad, o);
+  if (nbad && (threadIdx.x & 31u) == 0 && film.stats) atomicAdd(film.stats + 2, (unsigned long long)nbad);
 }
 
 __global__ void KGatherRadiance(PathBuffers B, uint32_t count, float* out) {
@@ -550,9 +561,11 @@ cudaError_t LaunchShadow(const DevScene& S, const PathBuffers& B, int depth, int
   return cudaGetLastError();
 }
 cudaError_t LaunchAccumulate(const PathBuffers& B, const FilmView& film, uint32_t count, cudaStream_t st,
-                             WaveCtx* ctx) {
+                             WaveCtx* ctx, uint32_t spw) {
   if (count == 0) return cudaSuccess;
-  KAccumulate<<<(count + 255) / 256, 256, 0, st>>>(B, film, count, ctx);
+  if (spw < 1u) spw = 1u;
+  uint32_t npc = count / spw;
+  KAccumulate<<<(npc + 255) / 256, 256, 0, st>>>(B, film, count, ctx, spw);
   return cudaGetLastError();
 }
 cudaError_t LaunchGatherRadiance(const PathBuffers& B, uint32_t count, float* out, cudaStream_t st) {

@@ -68,6 +68,10 @@ struct WaveParams {
   // seed, film and stats come from here, and the accumulate stage advances the
   // sample index, so one captured graph renders consecutive samples.
   const struct WaveCtx* ctx;
+  // Samples per wave (0 or 1: one). With spw > 1 the wave holds spw consecutive
+  // samples of the same count / spw pixels: path i is pixel pixelBegin + i % (count / spw),
+  // sample sample + i / (count / spw). Small frames thus fill the wave.
+  uint32_t spw;
 };
 
 // Per-job wave context in device memory, read by generate and accumulate.
@@ -95,8 +99,10 @@ cudaError_t LaunchShade(const DevScene& S, const PathBuffers& B, int depth, int 
                         const GuideDev* G = nullptr);
 cudaError_t LaunchShadow(const DevScene& S, const PathBuffers& B, int depth, int grid, cudaStream_t st,
                          unsigned long long* trav = nullptr, int refillBusy = 20);
+// spw: samples per wave of the generate stage (per pixel, in sample order, as
+// spw one-sample waves would add them).
 cudaError_t LaunchAccumulate(const PathBuffers& B, const FilmView& film, uint32_t count, cudaStream_t st,
-                             struct WaveCtx* ctx = nullptr);
+                             struct WaveCtx* ctx = nullptr, uint32_t spw = 1);
 cudaError_t LaunchGatherRadiance(const PathBuffers& B, uint32_t count, float* out, cudaStream_t st);
 cudaError_t LaunchResolveFilm(const FilmView& film, float scale, float* out, cudaStream_t st);
 

@@ -127,6 +127,7 @@ struct rad_job {
   std::vector<std::pair<cudaEvent_t, cudaEvent_t>> profEv;
   std::vector<int> profKind;
   uint32_t trainSamples = 0;  // guided jobs train during their first trainSamples samples
+  uint32_t spw = 0;           // samples per wave (0 = not chosen yet; see WaveSamples)
   // CUDA graph per pixel chunk: one captured wave replayed once per sample
   WaveCtx* ctx = nullptr;  // device, one per chunk
   std::vector<cudaGraphExec_t> graphs;
@@ -409,11 +410,25 @@ void RunWaveGuided(rad_job* j) {
 // Runs the job's next sample over its pixels as replays of one captured graph
 // per chunk (generate, bounces, accumulate); the accumulate stage advances the
 // sample index held in the chunk's device WaveCtx.
+// Samples per wave of a job: a frame that fills less than half of the path
+// slots gets several consecutive samples per wave (up to its spp), so small
+// jobs run in few full waves instead of many nearly empty ones.
+uint32_t WaveSamples(rad_job* j) {
+  if (j->spw == 0) {
+    const DevScene& S = j->scene->dev;
+    uint64_t npix = (uint64_t)S.cam.width * S.cam.height;
+    uint64_t cap = L().maxPaths;
+    j->spw = (npix == 0 || npix * 2 > cap) ? 1u : (uint32_t)std::max<uint64_t>(1, std::min<uint64_t>(j->spp, cap / npix));
+  }
+  return j->spw;
+}
+
 void RunWaveGraph(rad_job* j) {
   Lib& lib = L();
   const DevScene& S = j->scene->dev;
   uint32_t W = (uint32_t)S.cam.width, H = (uint32_t)S.cam.height;
   uint64_t npix = (uint64_t)W * H;
+  const uint32_t spw = WaveSamples(j);
   size_t nChunks = (size_t)((npix + lib.maxPaths - 1) / lib.maxPaths);
   if (j->graphs.empty()) {
     Check(cudaMalloc(&j->ctx, nChunks * sizeof(WaveCtx)), "cudaMalloc");
@@ -430,13 +445,13 @@ void RunWaveGraph(rad_job* j) {
     FilmView film{j->accum, (int32_t)W, (int32_t)H, j->dStats};
     for (size_t c = 0; c < nChunks; c++) {
       uint64_t p0 = (uint64_t)c * lib.maxPaths;
-      uint32_t count = (uint32_t)std::min<uint64_t>(lib.maxPaths, npix - p0);
-      WaveParams w{(uint32_t)p0, count, 0, 0, nullptr, nullptr, j->ctx + c};
+      uint32_t count = (uint32_t)std::min<uint64_t>(lib.maxPaths, npix - p0) * spw;
+      WaveParams w{(uint32_t)p0, count, 0, 0, nullptr, nullptr, j->ctx + c, spw};
       cudaGraph_t g = nullptr;
       Check(cudaStreamBeginCapture(lib.stream, cudaStreamCaptureModeThreadLocal), "begin capture");
       cudaError_t e1 = LaunchGenerate(S, lib.paths, w, lib.stream);
       uint64_t k = 1 + LaunchBounces(S, j->scene->tune, count, none);
-      cudaError_t e2 = LaunchAccumulate(lib.paths, film, count, lib.stream, j->ctx + c);
+      cudaError_t e2 = LaunchAccumulate(lib.paths, film, count, lib.stream, j->ctx + c, spw);
       cudaError_t e3 = cudaStreamEndCapture(lib.stream, &g);
       Check(e1, "generate capture");
       Check(e2, "accumulate capture");
@@ -453,13 +468,14 @@ void RunWaveGraph(rad_job* j) {
     Check(cudaGraphLaunch(j->graphs[c], lib.stream), "graph launch");
     j->stats.kernel_launches += j->graphKernels[c];
   }
-  j->nextSample++;
-  j->launched += npix;
+  j->nextSample += spw;
+  j->launched += npix * spw;
 }
 
 // Runs wave(s) for the job's next sample index over all its pixels.
 void RunWave(rad_job* j) {
-  if (GraphEligible(j)) {
+  const uint32_t spw = WaveSamples(j);
+  if (GraphEligible(j) && j->spp - j->nextSample >= spw) {
     RunWaveGraph(j);
     return;
   }
@@ -473,9 +489,10 @@ void RunWave(rad_job* j) {
   uint64_t npix = (uint64_t)W * H;
   ProfSink ps{j};
   FilmView film{j->accum, (int32_t)W, (int32_t)H, j->dStats};
+  const uint32_t k = std::min(spw, j->spp - j->nextSample);  // samples in this wave
   for (uint64_t p0 = 0; p0 < npix; p0 += lib.maxPaths) {
-    uint32_t count = (uint32_t)std::min<uint64_t>(lib.maxPaths, npix - p0);
-    WaveParams w{(uint32_t)p0, count, j->first + j->nextSample, j->seed, nullptr, nullptr};
+    uint32_t count = (uint32_t)std::min<uint64_t>(lib.maxPaths, npix - p0) * k;
+    WaveParams w{(uint32_t)p0, count, j->first + j->nextSample, j->seed, nullptr, nullptr, nullptr, k};
     cudaEvent_t a = nullptr;
     ps.Begin(0, a);
     Check(LaunchGenerate(S, lib.paths, w, lib.stream), "generate");
@@ -493,13 +510,13 @@ void RunWave(rad_job* j) {
                                 (j->flags & RAD_JOB_COUNT_TRAVERSAL) ? j->dStats + 4 : nullptr);
     }
     ps.Begin(4, a);
-    Check(LaunchAccumulate(lib.paths, film, count, lib.stream), "accumulate");
+    Check(LaunchAccumulate(lib.paths, film, count, lib.stream, nullptr, k), "accumulate");
     ps.End(4, a);
     launches++;
     j->stats.kernel_launches += launches;
   }
-  j->nextSample++;
-  j->launched += npix;
+  j->nextSample += k;
+  j->launched += npix * k;
 }
 
 void FinishJob(rad_job* j, int status, const std::string& err) {
@@ -606,11 +623,31 @@ void EndJobLaunch(rad_job* j) {
   j->state = kCompleting;
 }
 
+// Waves the worker may have queued on the stream ahead of the GPU. Bounding
+// the run-ahead keeps scheduling decisions late: a job that arrives (or is
+// cancelled) meanwhile waits at most this many waves, instead of behind every
+// wave already enqueued.
+constexpr size_t kMaxWavesInFlight = 3;
+
 void WorkerMain() {
   Lib& lib = L();
   cudaSetDevice(lib.device);
   std::vector<rad_job*> completing;
+  std::deque<cudaEvent_t> inflight;  // one event per queued wave
+  auto release = [&](cudaEvent_t e) {
+    std::lock_guard<std::mutex> g(lib.gpuMu);
+    lib.evPool.push_back(e);
+  };
   for (;;) {
+    while (!inflight.empty() && cudaEventQuery(inflight.front()) == cudaSuccess) {
+      release(inflight.front());
+      inflight.pop_front();
+    }
+    while (inflight.size() >= kMaxWavesInFlight) {
+      cudaEventSynchronize(inflight.front());
+      release(inflight.front());
+      inflight.pop_front();
+    }
     rad_job* j = nullptr;
     {
       std::unique_lock<std::mutex> lk(lib.qmu);
@@ -654,7 +691,12 @@ void WorkerMain() {
       std::lock_guard<std::mutex> g(lib.gpuMu);
       try {
         if (!j->accum) StartJob(j);
-        if (!j->cancel && j->nextSample < j->spp) RunWave(j);
+        if (!j->cancel && j->nextSample < j->spp) {
+          RunWave(j);
+          cudaEvent_t e = GetEvent();
+          Check(cudaEventRecord(e, lib.stream), "event record");
+          inflight.push_back(e);
+        }
         if (j->cancel || j->nextSample >= j->spp) {
           EndJobLaunch(j);
           std::lock_guard<std::mutex> lk(lib.qmu);
@@ -684,6 +726,10 @@ void WorkerMain() {
       }
     }
     if (!j && !completing.empty()) std::this_thread::sleep_for(std::chrono::microseconds(50));
+  }
+  for (cudaEvent_t e : inflight) {
+    cudaEventSynchronize(e);
+    release(e);
   }
 }
 

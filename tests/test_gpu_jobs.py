@@ -31,19 +31,20 @@ def test_mix_equals_alone(rad, scene_dir):
 
 
 def test_progress_and_cancel(rad, scene_dir):
-    s = rad.Scene.from_file(box(scene_dir, 64, 64, 4)[0])
-    j = s.submit(spp=4000)
+    # long enough (seconds, even with many samples per wave) to be cancelled while running
+    s = rad.Scene.from_file(box(scene_dir, 256, 256, 4)[0])
+    j = s.submit(spp=20000)
     time.sleep(0.05)
     j.cancel()
     with pytest.raises(rad.RadError) as e:
         j.wait()
     assert e.value.code == 9  # RAD_ERR_CANCELLED
     done, total = j.progress()
-    assert total == 64 * 64 * 4000 and done <= total
+    assert total == 256 * 256 * 20000 and done < total
     j.close()
     j2 = s.submit(spp=2)
     j2.wait()
-    assert j2.progress() == (64 * 64 * 2, 64 * 64 * 2)
+    assert j2.progress() == (256 * 256 * 2, 256 * 256 * 2)
     j2.close()
     s.close()
 
