@@ -38,6 +38,9 @@ sys.path.insert(0, ROOT)
 
 W, H = 1920, 1080
 MAX_DEPTH = 16
+# DRAM bytes per KExtend launch on this workload, measured by ncu (one wave, mean of 16 launches);
+# algorithmic bytes per launch are ~7x larger, the rest is served from L1/L2.
+EXTEND_DRAM_BYTES_PER_LAUNCH = 125.9e6
 BYTES_QUEUE, BYTES_RAY, BYTES_HIT, BYTES_NODE, BYTES_PRIM = 4, 32, 32, 80, 48
 
 
@@ -196,7 +199,8 @@ def run_ours(args, world, rank, local):
         load_s = time.perf_counter() - t0
         spp_step = 1
         # launch parameters of the traversal kernels for this scene (rad_autotune, not timed)
-        tune = scene.autotune()
+        tune = scene.autotune() if not args.no_tune else {"refill_busy": 20, "blocks_per_sm": 8, "best_ms": 0.0,
+                                                             "default_ms": 0.0}
         # traversal statistics for the roofline's algorithmic bytes (not timed)
         j = scene.submit(spp=1, first_sample=10_000, count_traversal=True)
         j.wait()
@@ -275,7 +279,9 @@ def run_ours(args, world, rank, local):
         "gpu_launches": st["kernel_launches"],
         "kernel_ms_profiled_2spp": {k: round(v, 3) for k, v in kern.items()},
         "roofline": {"bound": "hbm", "kernel": "extend (BVH8 closest hit)", "achieved": achieved, "peak": hbm_peak,
-                     "unit": "GB/s", "frac": achieved / hbm_peak, "traffic": None,
+                     "unit": "GB/s", "frac": achieved / hbm_peak, "traffic": EXTEND_DRAM_BYTES_PER_LAUNCH,
+                     "traffic_source": "ncu dram__bytes_read.sum + dram__bytes_write.sum, mean over the 16 extend "
+                                       "launches of one wave of this workload (profiles/extend_many_spheres_1080p.md)",
                      "peak_source": peak_src, "dominant_kernel_by_time": dominant,
                      "nodes_per_ray": nodes_per_ray, "prims_per_ray": prims_per_ray,
                      "bytes_per_ray": BYTES_QUEUE + BYTES_RAY + BYTES_HIT + nodes_per_ray * BYTES_NODE
@@ -388,9 +394,10 @@ def run_guided(args, world, rank, local):
         sc, assets = scenes.guided_room(n_spheres=args.guided_spheres, width=Wg, height=Hg, spp=64, max_depth=16)
         path = scenes.write_scene(tmp, sc, assets)
         scene = rad.Scene.from_file(path)
+        gcfg = dict({"log2_table": 19}, **json.loads(args.guided_config))
         # Reference: a long guided render (the guided estimator is unbiased for any
         # network state; a plain render of this scene does not converge in minutes).
-        scene.guide_enable({"log2_table": 19})
+        scene.guide_enable(gcfg)
         j = scene.submit(spp=args.guided_ref_spp, seed=777, guide=True)
         j.wait()
         ref = j.film().astype(np.float64)
@@ -413,7 +420,7 @@ def run_guided(args, world, rank, local):
             return dt, st, f
 
         timed(4, False)  # warm-up (graph capture, allocations)
-        scene.guide_enable({"log2_table": 19})
+        scene.guide_enable(gcfg)
         timed(4, True)
         clocks = ClockSampler(local)
         clocks.start()
@@ -422,7 +429,7 @@ def run_guided(args, world, rank, local):
         runs = []
         reached = None
         for spp in args.guided_spp:
-            scene.guide_enable({"log2_table": 19})  # fresh network: training is part of the time
+            scene.guide_enable(gcfg)  # fresh network: training is part of the time
             tg, stg, fg = timed(spp, True)
             eg = relmse(fg)
             runs.append({"spp": spp, "wall_s": tg, "relmse": eg[0], "relmse_trim1": eg[1], "relmse_median": eg[2],
@@ -441,8 +448,7 @@ def run_guided(args, world, rank, local):
             "config": {"workload": "guided_room", "spheres": args.guided_spheres, "width": Wg, "height": Hg,
                        "max_depth": 16, "room": 200, "opening": 5, "irradiance": 1000,
                        "reference": "guided render, %d spp" % args.guided_ref_spp, "ref_mean": float(ref.mean()),
-                       "guide": {"log2_table": 19, "levels": 16, "mlp": "3x64", "lobes": 8, "lr": 0.01,
-                                 "lr_mlp": 0.001, "train_fraction": 0.25}},
+                       "guide": dict({"levels": 16, "mlp": "3x64", "lobes": 8}, **gcfg)},
             "plain": {"spp": 64, "wall_s": tp, "relmse": ep[0], "relmse_trim1": ep[1], "relmse_median": ep[2],
                       "mean_over_ref": float(fp.mean() / ref.mean()),
                       "samples_per_s": stp["samples"] / tp,
@@ -533,6 +539,8 @@ def main():
     ap.add_argument("--guided-spheres", type=int, default=10000)
     ap.add_argument("--guided-ref-spp", type=int, default=1024)
     ap.add_argument("--guided-spp", type=int, nargs="+", default=[8, 16, 24, 32, 48, 64])
+    ap.add_argument("--guided-config", default="{}", help="JSON of rad_guide_enable settings for the guided jobs")
+    ap.add_argument("--no-tune", action="store_true", help="skip rad_autotune (keeps launch indices fixed for ncu)")
     ap.add_argument("--vol-res", type=int, default=1024)
     ap.add_argument("--vol-grid", type=int, default=256)
     ap.add_argument("--rates", type=float, nargs="+", default=[1, 2, 5, 10, 20])
