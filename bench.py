@@ -199,8 +199,8 @@ def run_ours(args, world, rank, local):
         load_s = time.perf_counter() - t0
         spp_step = 1
         # launch parameters of the traversal kernels for this scene (rad_autotune, not timed)
-        tune = scene.autotune() if not args.no_tune else {"refill_busy": 20, "blocks_per_sm": 8, "best_ms": 0.0,
-                                                             "default_ms": 0.0}
+        tune = scene.autotune() if not args.no_tune else {"refill_busy": 20, "blocks_per_sm": 8, "leaf_frac8": 4,
+                                                             "best_ms": 0.0, "default_ms": 0.0}
         # traversal statistics for the roofline's algorithmic bytes (not timed)
         j = scene.submit(spp=1, first_sample=10_000, count_traversal=True)
         j.wait()
@@ -272,6 +272,7 @@ def run_ours(args, world, rank, local):
                    "l2": "inputs larger than L2: resident scene + path state > 129 MB",
                    "scene_load_s": round(load_s, 3),
                    "autotune": {"refill_busy": tune["refill_busy"], "blocks_per_sm": tune["blocks_per_sm"],
+                                "leaf_frac8": tune["leaf_frac8"],
                                 "wave_ms_tuned": round(tune["best_ms"], 3),
                                 "wave_ms_default": round(tune["default_ms"], 3)}},
         "mrays_per_s": mrays,

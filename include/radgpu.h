@@ -234,18 +234,22 @@ RAD_API int rad_guide_grad(rad_scene* scene, const float* records, int64_t n, fl
 /* ---- autotuner ------------------------------------------------------------ */
 /* No counterpart in the reference (its TBB tiles need no tuning). Picks the
  * launch parameters of the `path` traversal kernels for a scene by timing full
- * 1-spp waves: the warp refill threshold of the persistent closest-hit and
- * shadow kernels (lanes still tracing before idle lanes take new rays) and the
- * number of blocks per SM of their grids. The winner is kept in the scene and
- * used by later jobs and rad_render_samples; results do not depend on it.
- * config_json may be NULL; keys: refill_busy (list, default [12,16,20,24,28]),
- * blocks_per_sm (list, default [4,6,8]), reps (timed waves per candidate, 2).
+ * 1-spp waves, one axis at a time from the defaults (coordinate descent): the
+ * fraction of a warp's busy lanes that must hold pending leaves before it tests
+ * leaves (leaf_frac8 / 8), the warp refill threshold of the persistent
+ * closest-hit and shadow kernels (lanes still tracing before idle lanes take new
+ * rays) and the number of blocks per SM of their grids. The winner is kept in
+ * the scene and used by later jobs and rad_render_samples; results do not
+ * depend on it. config_json may be NULL; keys: leaf_frac8 (list, default
+ * [2,3,4,5,6]), refill_busy (list, default [16,20,24,28,32]), blocks_per_sm
+ * (list, default [4,6,8]), reps (timed waves per candidate, 2).
  * RAD_ERR_UNSUPPORTED for `vol_path` scenes. */
 typedef struct rad_tune_result {
   int32_t refill_busy, blocks_per_sm; /* chosen */
-  int32_t candidates;
+  int32_t candidates;                 /* configurations timed */
   double best_ms;    /* time of one wave with the chosen parameters */
-  double default_ms; /* with the defaults (20, 8), when they were among the candidates */
+  double default_ms; /* with the defaults (20, 8, 4), when they were timed */
+  int32_t leaf_frac8; /* chosen */
 } rad_tune_result;
 RAD_API int rad_autotune(rad_scene* scene, const char* config_json, rad_tune_result* out);
 

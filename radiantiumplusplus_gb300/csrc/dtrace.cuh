@@ -192,6 +192,10 @@ RD float ByteAsFloat(uint32_t w, uint32_t i) {
 struct TravState {
   uint32_t node;
   int sp;
+  uint32_t leafMask;         // leaf slots of the last visited node still to test
+  uint32_t meta0, meta1;     // that node's meta bytes
+  uint32_t primBase;
+  bool last;                 // no node left after those leaves
 };
 constexpr int kTravContinue = 0, kTravDone = 1, kTravOverflow = 2;
 
@@ -203,6 +207,19 @@ constexpr int kTravContinue = 0, kTravDone = 1, kTravOverflow = 2;
 template <bool ANY, bool COUNT>
 RD int TravStep(const DevScene& S, const RayPre& r, TraceHit& h, uint2* stack, TravState& st, uint32_t* err,
                 uint32_t* nNodes, uint32_t* nPrims) {
+  if (st.leafMask) {
+    // one pending leaf of the last visited node (its primitives, 1..3)
+    uint32_t s = __ffs(st.leafMask) - 1;
+    st.leafMask &= st.leafMask - 1;
+    uint32_t meta = ByteOf(s < 4 ? st.meta0 : st.meta1, s & 3u);
+    uint32_t cnt = (meta >> 5) & 3u, off = meta & 31u;
+    bool analytic = (meta >> 7) & 1u;
+    for (uint32_t k = 0; k < cnt; k++) {
+      if (COUNT) (*nPrims)++;
+      if (TestPrim(S, r, st.primBase + off + k, analytic, h, ANY) && ANY) return kTravDone;
+    }
+    return (st.leafMask == 0u && st.last) ? kTravDone : kTravContinue;
+  }
   const uint32_t nodeIdx = st.node;
   if (COUNT) (*nNodes)++;
   const uint4* np = reinterpret_cast<const uint4*>(S.nodes) + 5 * (size_t)nodeIdx;
@@ -245,18 +262,13 @@ RD int TravStep(const DevScene& S, const RayPre& r, TraceHit& h, uint2* stack, T
         leafHits |= 1u << s;
     }
   }
-  // ---- leaves of this node
-  while (leafHits) {
-    uint32_t s = __ffs(leafHits) - 1;
-    leafHits &= leafHits - 1;
-    uint32_t meta = ByteOf(s < 4 ? q1.z : q1.w, s & 3u);
-    uint32_t cnt = (meta >> 5) & 3u, off = meta & 31u;
-    bool analytic = (meta >> 7) & 1u;
-    for (uint32_t k = 0; k < cnt; k++) {
-      if (COUNT) (*nPrims)++;
-      if (TestPrim(S, r, primBase + off + k, analytic, h, ANY) && ANY) return kTravDone;
-    }
-  }
+  // ---- leaves of this node: tested in the following steps, before the next
+  // node visit (so the order of node visits and primitive tests is unchanged;
+  // the next node below was chosen from the child boxes alone)
+  st.leafMask = leafHits;
+  st.meta0 = q1.z;
+  st.meta1 = q1.w;
+  st.primBase = primBase;
   // ---- next node
   if (hitInternal) {
     uint32_t b = __ffs(hitInternal) - 1;
@@ -273,7 +285,10 @@ RD int TravStep(const DevScene& S, const RayPre& r, TraceHit& h, uint2* stack, T
     st.node = child;
     return kTravContinue;
   }
-  if (st.sp == 0) return kTravDone;
+  if (st.sp == 0) {
+    st.last = true;
+    return st.leafMask ? kTravContinue : kTravDone;
+  }
   uint2 g = stack[st.sp - 1];
   uint32_t m = g.y & 0xffu, im = g.y >> 8;
   uint32_t b = __ffs(m) - 1;
@@ -295,6 +310,8 @@ RD void TraceInit(float tmax, TraceHit& h, TravState& st) {
   h.front = 0;
   st.node = 0;
   st.sp = 0;
+  st.leafMask = 0;
+  st.last = false;
 }
 
 // Closest hit (ANY = false) or occlusion (ANY = true). Returns false and sets

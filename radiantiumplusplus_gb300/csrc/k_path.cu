@@ -102,7 +102,7 @@ __device__ __forceinline__ void FlushTravCounts(unsigned long long* out, uint32_
 // ~9 of 32 lanes active per instruction).
 template <bool COUNT>
 __global__ void __launch_bounds__(kBlock, 8)
-    KExtend(DevScene S, PathBuffers B, int depth, unsigned long long* trav, int refillBusy) {
+    KExtend(DevScene S, PathBuffers B, int depth, unsigned long long* trav, int refillBusy, int leafFrac8) {
   const uint32_t count = B.counters[depth];
   const uint32_t* qin = B.q[depth & 1];
   uint32_t* fetch = B.counters + kFetchBase + 2 * depth;
@@ -142,8 +142,14 @@ __global__ void __launch_bounds__(kBlock, 8)
     // ---- trace until too few lanes are busy (all of them once the queue is drained)
     const int minBusy = drained ? 1 : refillBusy;
     for (;;) {
-      if (live && !done) done = TravStep<false, COUNT>(S, r, h, stack, st, err, &nN, &nP) != kTravContinue;
-      if (__popc(__ballot_sync(0xffffffffu, live && !done)) < minBusy) break;
+      // leaf phase once at least leafFrac8 / 8 of the busy lanes hold pending
+      // leaves (the others wait), else a node phase for the lanes without
+      const bool busy = live && !done, pend = busy && st.leafMask != 0u;
+      const int nb = __popc(__ballot_sync(0xffffffffu, busy));
+      if (nb < minBusy || nb == 0) break;
+      const bool leafPhase = 8 * __popc(__ballot_sync(0xffffffffu, pend)) >= leafFrac8 * nb;
+      if (busy && pend == leafPhase)
+        done = TravStep<false, COUNT>(S, r, h, stack, st, err, &nN, &nP) != kTravContinue;
     }
     // ---- finished lanes: hit record and shade-class append
     const bool fin = live && done;
@@ -392,7 +398,7 @@ __global__ void __launch_bounds__(kBlock) KShadeClass(DevScene S, PathBuffers B,
 
 template <bool COUNT>
 __global__ void __launch_bounds__(kBlock, 8)
-    KShadow(DevScene S, PathBuffers B, int depth, unsigned long long* trav, int refillBusy) {
+    KShadow(DevScene S, PathBuffers B, int depth, unsigned long long* trav, int refillBusy, int leafFrac8) {
   const uint32_t count = B.counters[kShadowBase + depth];
   uint32_t* fetch = B.counters + kFetchBase + 2 * depth + 1;
   uint32_t* err = B.counters + kMiscBase + 1;
@@ -428,14 +434,17 @@ __global__ void __launch_bounds__(kBlock, 8)
     if (__ballot_sync(0xffffffffu, live) == 0u) break;
     const int minBusy = drained ? 1 : refillBusy;
     for (;;) {
-      if (live && !done) {
+      const bool busy = live && !done, pend = busy && st.leafMask != 0u;
+      const int nb = __popc(__ballot_sync(0xffffffffu, busy));
+      if (nb < minBusy || nb == 0) break;
+      const bool leafPhase = 8 * __popc(__ballot_sync(0xffffffffu, pend)) >= leafFrac8 * nb;
+      if (busy && pend == leafPhase) {
         int res = TravStep<true, COUNT>(S, r, h, stack, st, err, &nN, &nP);
         if (res != kTravContinue) {
           done = true;
           occ = res == kTravDone && h.prim != kNoPrim;
         }
       }
-      if (__popc(__ballot_sync(0xffffffffu, live && !done)) < minBusy) break;
     }
     if (live && done) {
       if (!occ) {
@@ -527,11 +536,11 @@ cudaError_t LaunchGenerate(const DevScene& S, const PathBuffers& B, const WavePa
   return cudaGetLastError();
 }
 cudaError_t LaunchExtend(const DevScene& S, const PathBuffers& B, int depth, int grid, cudaStream_t st,
-                         unsigned long long* trav, int refillBusy) {
+                         unsigned long long* trav, int refillBusy, int leafFrac8) {
   if (trav)
-    KExtend<true><<<grid, kBlock, 0, st>>>(S, B, depth, trav, refillBusy);
+    KExtend<true><<<grid, kBlock, 0, st>>>(S, B, depth, trav, refillBusy, leafFrac8);
   else
-    KExtend<false><<<grid, kBlock, 0, st>>>(S, B, depth, nullptr, refillBusy);
+    KExtend<false><<<grid, kBlock, 0, st>>>(S, B, depth, nullptr, refillBusy, leafFrac8);
   return cudaGetLastError();
 }
 cudaError_t LaunchShade(const DevScene& S, const PathBuffers& B, int depth, int grid, cudaStream_t st,
@@ -553,11 +562,11 @@ cudaError_t LaunchShade(const DevScene& S, const PathBuffers& B, int depth, int 
   return cudaGetLastError();
 }
 cudaError_t LaunchShadow(const DevScene& S, const PathBuffers& B, int depth, int grid, cudaStream_t st,
-                         unsigned long long* trav, int refillBusy) {
+                         unsigned long long* trav, int refillBusy, int leafFrac8) {
   if (trav)
-    KShadow<true><<<grid, kBlock, 0, st>>>(S, B, depth, trav, refillBusy);
+    KShadow<true><<<grid, kBlock, 0, st>>>(S, B, depth, trav, refillBusy, leafFrac8);
   else
-    KShadow<false><<<grid, kBlock, 0, st>>>(S, B, depth, nullptr, refillBusy);
+    KShadow<false><<<grid, kBlock, 0, st>>>(S, B, depth, nullptr, refillBusy, leafFrac8);
   return cudaGetLastError();
 }
 cudaError_t LaunchAccumulate(const PathBuffers& B, const FilmView& film, uint32_t count, cudaStream_t st,

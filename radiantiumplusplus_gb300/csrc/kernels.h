@@ -86,19 +86,21 @@ int PathGridBlocks();
 cudaError_t LaunchGenerate(const DevScene& S, const PathBuffers& B, const WaveParams& w, cudaStream_t st);
 // Launch parameters of the persistent traversal kernels, chosen per scene by
 // the autotuner (rad_autotune): a warp refills its idle lanes once fewer than
-// refillBusy lanes are still tracing; grids hold blocksPerSm blocks per SM.
+// refillBusy lanes are still tracing; it tests pending leaves once at least
+// leafFrac8 / 8 of its busy lanes hold some; grids hold blocksPerSm blocks per SM.
 struct TraceTune {
   int32_t refillBusy = 20;
   int32_t blocksPerSm = 8;
+  int32_t leafFrac8 = 4;
 };
 // trav (optional, 4 x u64): extend node visits, extend prim tests, shadow node visits, shadow prim tests
 cudaError_t LaunchExtend(const DevScene& S, const PathBuffers& B, int depth, int grid, cudaStream_t st,
-                         unsigned long long* trav = nullptr, int refillBusy = 20);
+                         unsigned long long* trav = nullptr, int refillBusy = 20, int leafFrac8 = 4);
 // G (optional): guide network; its classes then sample the one-sample MIS mixture.
 cudaError_t LaunchShade(const DevScene& S, const PathBuffers& B, int depth, int grid, cudaStream_t st,
                         const GuideDev* G = nullptr);
 cudaError_t LaunchShadow(const DevScene& S, const PathBuffers& B, int depth, int grid, cudaStream_t st,
-                         unsigned long long* trav = nullptr, int refillBusy = 20);
+                         unsigned long long* trav = nullptr, int refillBusy = 20, int leafFrac8 = 4);
 // spw: samples per wave of the generate stage (per pixel, in sample order, as
 // spw one-sample waves would add them).
 cudaError_t LaunchAccumulate(const PathBuffers& B, const FilmView& film, uint32_t count, cudaStream_t st,

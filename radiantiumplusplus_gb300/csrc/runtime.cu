@@ -278,7 +278,7 @@ uint64_t LaunchBounces(const DevScene& S, const TraceTune& tu, uint32_t count, P
   for (int d = 0; d < iters; d++) {
     cudaEvent_t a = nullptr;
     ps.Begin(1, a);
-    Check(LaunchExtend(S, lib.paths, d, tgrid, lib.stream, trav, tu.refillBusy), "extend");
+    Check(LaunchExtend(S, lib.paths, d, tgrid, lib.stream, trav, tu.refillBusy, tu.leafFrac8), "extend");
     ps.End(1, a);
     if (G) {
       ps.Begin(6, a);
@@ -290,7 +290,7 @@ uint64_t LaunchBounces(const DevScene& S, const TraceTune& tu, uint32_t count, P
     Check(LaunchShade(S, lib.paths, d, grid, lib.stream, G), "shade");
     ps.End(2, a);
     ps.Begin(3, a);
-    Check(LaunchShadow(S, lib.paths, d, tgrid, lib.stream, trav, tu.refillBusy), "shadow");
+    Check(LaunchShadow(S, lib.paths, d, tgrid, lib.stream, trav, tu.refillBusy, tu.leafFrac8), "shadow");
     ps.End(3, a);
     launches += 2 + kShadeClasses;
     if (S.maxDepth < 0 && (d % 8) == 7) {
@@ -1423,7 +1423,7 @@ int rad_autotune(rad_scene* scene, const char* config_json, rad_tune_result* out
   return Guard([&] {
     EnsureInit();
     int reps = 2;
-    std::vector<int> refill = {12, 16, 20, 24, 28}, perSm = {4, 6, 8};
+    std::vector<int> leaf = {2, 3, 4, 5, 6}, refill = {16, 20, 24, 28, 32}, perSm = {4, 6, 8};
     if (config_json && *config_json) {
       JValue c = JsonReader::Parse(config_json);
       if (const JValue* v = c.get("reps")) reps = std::max(1, (int)v->n);
@@ -1438,6 +1438,7 @@ int rad_autotune(rad_scene* scene, const char* config_json, rad_tune_result* out
           }
         }
       };
+      list("leaf_frac8", leaf, 1, 8);
       list("refill_busy", refill, 1, 32);
       list("blocks_per_sm", perSm, 1, 8);
     }
@@ -1453,29 +1454,55 @@ int rad_autotune(rad_scene* scene, const char* config_json, rad_tune_result* out
       Check(LaunchGenerate(S, lib.paths, w, lib.stream), "generate");
       LaunchBounces(S, tu, count, none);
     };
-    rad_tune_result res{};
-    res.best_ms = 1e30;
-    for (int pb : perSm)
-      for (int rb : refill) {
-        TraceTune tu;
-        tu.refillBusy = rb;
-        tu.blocksPerSm = pb;
-        wave(tu);  // warm-up
-        Check(cudaEventRecord(a, lib.stream), "event");
-        for (int k = 0; k < reps; k++) wave(tu);
-        Check(cudaEventRecord(b, lib.stream), "event");
-        Check(cudaEventSynchronize(b), "sync");
-        float ms = 0.f;
-        cudaEventElapsedTime(&ms, a, b);
-        ms /= (float)reps;
-        if (rb == TraceTune{}.refillBusy && pb == TraceTune{}.blocksPerSm) res.default_ms = ms;
-        if (ms < res.best_ms) {
-          res.best_ms = ms;
-          res.refill_busy = rb;
-          res.blocks_per_sm = pb;
+    std::vector<std::pair<TraceTune, float>> timed;
+    auto time = [&](const TraceTune& tu) -> float {
+      for (const auto& t : timed)
+        if (t.first.refillBusy == tu.refillBusy && t.first.blocksPerSm == tu.blocksPerSm &&
+            t.first.leafFrac8 == tu.leafFrac8)
+          return t.second;
+      wave(tu);  // warm-up
+      Check(cudaEventRecord(a, lib.stream), "event");
+      for (int k = 0; k < reps; k++) wave(tu);
+      Check(cudaEventRecord(b, lib.stream), "event");
+      Check(cudaEventSynchronize(b), "sync");
+      float ms = 0.f;
+      cudaEventElapsedTime(&ms, a, b);
+      ms /= (float)reps;
+      timed.push_back({tu, ms});
+      return ms;
+    };
+    // coordinate descent from the defaults: each axis in turn, the others held at
+    // the best values found so far
+    TraceTune best;
+    if (std::find(leaf.begin(), leaf.end(), best.leafFrac8) == leaf.end()) best.leafFrac8 = leaf[0];
+    if (std::find(refill.begin(), refill.end(), best.refillBusy) == refill.end()) best.refillBusy = refill[0];
+    if (std::find(perSm.begin(), perSm.end(), best.blocksPerSm) == perSm.end()) best.blocksPerSm = perSm[0];
+    float bestMs = time(best);
+    auto axis = [&](const std::vector<int>& vals, int32_t TraceTune::*field) {
+      for (int v : vals) {
+        TraceTune tu = best;
+        tu.*field = v;
+        float ms = time(tu);
+        if (ms < bestMs) {
+          bestMs = ms;
+          best = tu;
         }
-        res.candidates++;
       }
+    };
+    axis(leaf, &TraceTune::leafFrac8);
+    axis(refill, &TraceTune::refillBusy);
+    axis(perSm, &TraceTune::blocksPerSm);
+    rad_tune_result res{};
+    res.refill_busy = best.refillBusy;
+    res.blocks_per_sm = best.blocksPerSm;
+    res.leaf_frac8 = best.leafFrac8;
+    res.best_ms = bestMs;
+    res.candidates = (int32_t)timed.size();
+    const TraceTune def;
+    for (const auto& t : timed)
+      if (t.first.refillBusy == def.refillBusy && t.first.blocksPerSm == def.blocksPerSm &&
+          t.first.leafFrac8 == def.leafFrac8)
+        res.default_ms = t.second;
     lib.evPool.push_back(a);
     lib.evPool.push_back(b);
     uint32_t errWord = 0;
@@ -1484,8 +1511,7 @@ int rad_autotune(rad_scene* scene, const char* config_json, rad_tune_result* out
       cudaMemset(lib.paths.counters + kMiscBase + 1, 0, 4);
       throw Error{RAD_ERR_DEVICE_CHECK, "device-side check fired while tuning"};
     }
-    scene->tune.refillBusy = res.refill_busy;
-    scene->tune.blocksPerSm = res.blocks_per_sm;
+    scene->tune = best;
     if (out) *out = res;
   });
 }

@@ -90,11 +90,12 @@ def test_autotune_picks_parameters_and_keeps_results(rad, scene_dir):
     s = rad.Scene.from_file(spheres(scene_dir, 200, 3, 40, 24, 5)[0])
     before = s.render(spp=3, seed=7)
     r = s.autotune({"reps": 1})
-    assert r["candidates"] == 15 and r["refill_busy"] in (12, 16, 20, 24, 28) and r["blocks_per_sm"] in (4, 6, 8)
+    assert r["candidates"] == 11 and r["refill_busy"] in (16, 20, 24, 28, 32) and r["blocks_per_sm"] in (4, 6, 8)
+    assert r["leaf_frac8"] in (2, 3, 4, 5, 6)
     assert r["best_ms"] > 0 and r["best_ms"] <= r["default_ms"]
     assert np.array_equal(before, s.render(spp=3, seed=7))
-    r2 = s.autotune({"refill_busy": [1, 32], "blocks_per_sm": [2], "reps": 1})
-    assert r2["candidates"] == 2 and r2["blocks_per_sm"] == 2
+    r2 = s.autotune({"refill_busy": [1, 32], "blocks_per_sm": [2], "leaf_frac8": [8], "reps": 1})
+    assert r2["candidates"] == 2 and r2["blocks_per_sm"] == 2 and r2["leaf_frac8"] == 8
     assert np.array_equal(before, s.render(spp=3, seed=7))
     with pytest.raises(rad.RadError):
         s.autotune({"refill_busy": [40]})
