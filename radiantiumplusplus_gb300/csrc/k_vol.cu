@@ -208,10 +208,18 @@ struct VolPathState {
   float eta, prevPdf;
   int medium, channel, depth, guard;
   bool isSpecular, siValid, afterNull;
+  int act;      // next part of the loop iteration: kActTop, kActScatter or kActSurface
+  V3 scatterP;  // kActScatter: the real collision
   SurfInt si;
   Pcg32 rng;
   uint32_t nRays, nShadow;
 };
+// Parts of one iteration of the VolPath::Li loop (vol_path.cpp:40-215): the top
+// (Russian roulette, depth test, free flight, null / real decision), the medium
+// scatter (phase NEE + phase sampling) and the surface part (trace, emission,
+// BSDF NEE and sampling). A path runs them in this order, so its arithmetic and
+// random numbers are those of the loop; KVolPath runs one kind per warp step.
+constexpr int kActTop = 0, kActScatter = 1, kActSurface = 2;
 
 RD void VolInit(const DevScene& S, VolPathState& p, VRay ray, Pcg32 rng) {
   p.ray = ray;
@@ -231,19 +239,27 @@ RD void VolInit(const DevScene& S, VolPathState& p, VRay ray, Pcg32 rng) {
   p.afterNull = false;
   p.depth = 0;
   p.guard = 0;
+  p.act = kActTop;
   p.nRays = p.nShadow = 0;
 }
 
-// One iteration of the loop of VolPath::Li (vol_path.cpp:40-215); false when
-// the path has ended (its radiance is in p.result).
-// BRICKS: brick majorants, and no re-trace after a null collision (the surface
-// ahead along the same line is unchanged; its distance shrinks by the flight).
-// HALF: fp16 grid. realDepth (mode bit kVolRealDepth, implied by BRICKS): null
-// collisions count neither toward max_depth nor for Russian roulette; the
-// reference counts them (vol_path.cpp:40-52 run once per loop iteration), which
-// ties its truncation to the majorant. All off = the reference's algorithm.
+// End of a loop iteration (the loop's increment).
+RD bool VolNextIteration(VolPathState& p) {
+  p.depth++;
+  p.guard++;
+  p.act = kActTop;
+  return true;
+}
+
+// Top of an iteration. BRICKS: brick majorants, and no re-trace after a null
+// collision (the surface ahead along the same line is unchanged; its distance
+// shrinks by the flight). HALF: fp16 grid. realDepth (mode bit kVolRealDepth,
+// implied by BRICKS): null collisions count neither toward max_depth nor for
+// Russian roulette; the reference counts them (vol_path.cpp:40-52 run once per
+// loop iteration), which ties its truncation to the majorant. All off = the
+// reference's algorithm. Returns false when the path has ended.
 template <bool BRICKS, bool HALF>
-RD bool VolStep(const DevScene& S, VolPathState& p, uint32_t mode, uint32_t* err) {
+RD bool VolTop(const DevScene& S, VolPathState& p, uint32_t mode, uint32_t* err) {
   const bool realDepth = BRICKS || (mode & kVolRealDepth);
   Pcg32& rng = p.rng;
   VRay& ray = p.ray;
@@ -261,138 +277,162 @@ RD bool VolStep(const DevScene& S, VolPathState& p, uint32_t mode, uint32_t* err
     thr = thr * Rcp(rr);
   }
   if (S.maxDepth >= 0 && p.depth + 1 >= S.maxDepth) return false;
-  bool isSampleMedium = p.medium >= 0;
-  bool isSampleSurface = !isSampleMedium;
-  bool isNullScatter = false, isMediumScatter = false, isMediumEscaped = false;
-  bool isSpectral = isSampleMedium;
-  MedInt mei;
-  mei.T = kInf;
-  if (isSampleMedium) {
-    const MediumRec& md = S.media[p.medium];
-    mei = SampleInteraction<BRICKS, HALF>(S, md, ray, Next1D(rng), channel);
-    if (md.kind == MED_HOMOGENEOUS && mei.T != kInf) ray.MaxT = mei.T;
-    if (!(BRICKS && p.siValid)) {
-      VTraceCall(S, ray, si, err);
-      p.nRays++;
-    }
-    p.siValid = false;
-    if (si.T < mei.T) mei.T = kInf;
-    if (isSpectral) {
-      // medium.cpp:45-59
-      V3 tr, ffp;
-      float t = fminr(mei.T, si.T) - mei.MinT;
-      if (realDepth) {
-        // tr / pdf formed as RelTr ratios (no underflow)
-        if (t <= 0.f) {
-          tr = ffp = v3s(1.f);
-        } else {
-          tr = RelTr(mei.cE, channel, t);
-          ffp = si.T < mei.T ? v3s(1.f) : v3s(comp(mei.cE, channel));
-        }
-      } else if (t <= 0.f) {
+  p.afterNull = false;
+  if (p.medium < 0) {
+    p.act = kActSurface;
+    return true;
+  }
+  const MediumRec& md = S.media[p.medium];
+  MedInt mei = SampleInteraction<BRICKS, HALF>(S, md, ray, Next1D(rng), channel);
+  if (md.kind == MED_HOMOGENEOUS && mei.T != kInf) ray.MaxT = mei.T;
+  if (!(BRICKS && p.siValid)) {
+    VTraceCall(S, ray, si, err);
+    p.nRays++;
+  }
+  p.siValid = false;
+  if (si.T < mei.T) mei.T = kInf;
+  {
+    // medium.cpp:45-59
+    V3 tr, ffp;
+    float t = fminr(mei.T, si.T) - mei.MinT;
+    if (realDepth) {
+      // tr / pdf formed as RelTr ratios (no underflow)
+      if (t <= 0.f) {
         tr = ffp = v3s(1.f);
       } else {
-        tr = ExpV(mei.cE * -t);
-        ffp = si.T < mei.T ? tr : cmul(tr, mei.cE);
-        if (tr.x == ffp.x && tr.y == ffp.y && tr.z == ffp.z) tr = ffp = v3s(1.f);
+        tr = RelTr(mei.cE, channel, t);
+        ffp = si.T < mei.T ? v3s(1.f) : v3s(comp(mei.cE, channel));
       }
-      float pdf = comp(ffp, channel);
-      V3 after = cmul(thr, tr) / pdf;
-      thr = pdf <= 0.f ? v3s(0.f) : after;
+    } else if (t <= 0.f) {
+      tr = ffp = v3s(1.f);
+    } else {
+      tr = ExpV(mei.cE * -t);
+      ffp = si.T < mei.T ? tr : cmul(tr, mei.cE);
+      if (tr.x == ffp.x && tr.y == ffp.y && tr.z == ffp.z) tr = ffp = v3s(1.f);
     }
-    isMediumEscaped = mei.T == kInf;
-    isSampleMedium = mei.T != kInf;
-    bool nullScatter = Next1D(rng) > comp(mei.sT, channel) / comp(mei.cE, channel);
-    isNullScatter = nullScatter && isSampleMedium;
-    isMediumScatter = !isNullScatter && isSampleMedium;
-    if (isSpectral && isNullScatter) thr = cmul(thr, mei.sN) * comp(mei.cE, channel) / comp(mei.sN, channel);
-    if (isMediumScatter) p.prevP = mei.P;
+    float pdf = comp(ffp, channel);
+    V3 after = cmul(thr, tr) / pdf;
+    thr = pdf <= 0.f ? v3s(0.f) : after;
   }
-  p.afterNull = false;
-  if (isNullScatter) {
+  const bool escaped = mei.T == kInf;
+  bool nullScatter = Next1D(rng) > comp(mei.sT, channel) / comp(mei.cE, channel);
+  if (escaped) {
+    p.act = kActSurface;
+    return true;
+  }
+  if (nullScatter) {
+    thr = cmul(thr, mei.sN) * comp(mei.cE, channel) / comp(mei.sN, channel);
     ray.O = mei.P;
     si.T = si.T - mei.T;
     p.siValid = BRICKS;
     p.afterNull = realDepth;
+    return VolNextIteration(p);
   }
-  if (isMediumScatter) {
-    const MediumRec& md = S.media[p.medium];
-    if (isSpectral) thr = cmul(thr, mei.sS) * comp(mei.cE, channel) / comp(mei.sT, channel);
+  // real collision: the scatter part follows
+  p.prevP = mei.P;
+  thr = cmul(thr, mei.sS) * comp(mei.cE, channel) / comp(mei.sT, channel);
+  p.scatterP = mei.P;
+  p.act = kActScatter;
+  return true;
+}
+
+// Medium scatter: phase-function NEE and the next direction.
+template <bool BRICKS, bool HALF>
+RD bool VolScatter(const DevScene& S, VolPathState& p, uint32_t mode, uint32_t* err) {
+  const bool realDepth = BRICKS || (mode & kVolRealDepth);
+  const MediumRec& md = S.media[p.medium];
+  MedInt mei;  // the phase functions read the incident direction and its frame
+  mei.Wi = -p.ray.D;
+  mei.sh = FrameFromN(mei.Wi);
+  mei.P = p.scatterP;
+  DirSample dsr;
+  uint64_t ns = 0;
+  V3 li = VolSampleLight<BRICKS, HALF>(S, p.rng, p.medium, p.channel, mei.P, v3s(0.f), dsr, err, ns, realDepth);
+  p.nShadow += (uint32_t)ns;
+  if (dsr.Pdf > 0.f) {
+    float phaseVal = PhaseEval(md, mei, dsr.Dir);
+    float weight = dsr.IsDelta ? 1.f : VMis(dsr.Pdf, phaseVal);
+    p.result = p.result + cmul(p.thr, li) * weight * phaseVal / dsr.Pdf;
+  }
+  float phasePdf;
+  V3 wo = PhaseSample(md, mei, Next2D(p.rng), phasePdf);
+  p.ray = Spawn(mei.P, v3s(0.f), wo);
+  p.isSpecular = false;
+  p.prevPdf = phasePdf;
+  return VolNextIteration(p);
+}
+
+// Surface part: trace, emission with MIS, BSDF NEE, BSDF sampling.
+template <bool BRICKS, bool HALF>
+RD bool VolSurface(const DevScene& S, VolPathState& p, uint32_t mode, uint32_t* err) {
+  const bool realDepth = BRICKS || (mode & kVolRealDepth);
+  VRay& ray = p.ray;
+  SurfInt& si = p.si;
+  V3& thr = p.thr;
+  bool hit = VTraceCall(S, ray, si, err);
+  p.nRays++;
+  int hitLight = hit ? S.shapes[si.shape].light : S.envLight;
+  if (hitLight >= 0) {
+    float weight;
+    if (p.isSpecular) {
+      weight = 1.f;
+    } else {
+      V3 rel = si.P - p.prevP;
+      float dist = norm(rel);
+      V3 dir = hit ? rel / dist : -si.Wi;
+      weight = VMis(p.prevPdf, PdfLightDirection(S, hitLight, p.prevP, dir, si.sh.N, dist));
+    }
+    V3 li = EvalLightAt(S, hitLight, &si);
+    p.result = p.result + cmul(thr, li) * weight;
+  }
+  if (!hit) return false;
+  const ShapeRec& shp = S.shapes[si.shape];
+  if (shp.light >= 0) return false;
+  if (shp.bsdf < 0) {
+    ray = Spawn(si.P, si.N, ray.D);
+    p.medium = MediumOfHit(S, si, ray.D);
+    // depth-- then the loop increment: the index-matched boundary is free
+    p.guard++;
+    p.act = kActTop;
+    return true;
+  }
+  const MatRec* mats = S.mats;
+  if (mats[shp.bsdf].flags & BT_NODELTA) {
     DirSample dsr;
     uint64_t ns = 0;
-    V3 li = VolSampleLight<BRICKS, HALF>(S, rng, p.medium, channel, mei.P, v3s(0.f), dsr, err, ns, realDepth);
+    V3 li = VolSampleLight<BRICKS, HALF>(S, p.rng, p.medium, p.channel, si.P, si.N, dsr, err, ns, realDepth);
     p.nShadow += (uint32_t)ns;
     if (dsr.Pdf > 0.f) {
-      float phaseVal = PhaseEval(md, mei, dsr.Dir);
-      float weight = dsr.IsDelta ? 1.f : VMis(dsr.Pdf, phaseVal);
-      p.result = p.result + cmul(thr, li) * weight * phaseVal / dsr.Pdf;
+      V3 wo = ToLocal(si.sh, dsr.Dir);
+      V3 f;
+      float bsdfPdf;
+      VBsdfEvalPdf(mats, (uint32_t)shp.bsdf, si.Wi, wo, f, bsdfPdf);
+      float weight = dsr.IsDelta ? 1.f : VMis(dsr.Pdf, bsdfPdf);
+      p.result = p.result + cmul(cmul(thr, f), li) * weight / dsr.Pdf;
     }
-    float phasePdf;
-    V3 wo = PhaseSample(md, mei, Next2D(rng), phasePdf);
-    ray = Spawn(mei.P, v3s(0.f), wo);
-    p.isSpecular = false;
-    p.prevPdf = phasePdf;
   }
-  isSampleSurface = isSampleSurface || isMediumEscaped;
-  if (isSampleSurface) {
-    bool hit = VTraceCall(S, ray, si, err);
-    p.nRays++;
-    int hitLight = hit ? S.shapes[si.shape].light : S.envLight;
-    if (hitLight >= 0) {
-      float weight;
-      if (p.isSpecular) {
-        weight = 1.f;
-      } else {
-        V3 rel = si.P - p.prevP;
-        float dist = norm(rel);
-        V3 dir = hit ? rel / dist : -si.Wi;
-        weight = VMis(p.prevPdf, PdfLightDirection(S, hitLight, p.prevP, dir, si.sh.N, dist));
-      }
-      V3 li = EvalLightAt(S, hitLight, &si);
-      p.result = p.result + cmul(thr, li) * weight;
-    }
-    if (!hit) return false;
-    const ShapeRec& shp = S.shapes[si.shape];
-    if (shp.light >= 0) return false;
-    if (shp.bsdf < 0) {
-      ray = Spawn(si.P, si.N, ray.D);
-      p.medium = MediumOfHit(S, si, ray.D);
-      // depth-- then the loop increment: the index-matched boundary is free
-      p.guard++;
-      return true;
-    }
-    const MatRec* mats = S.mats;
-    if (mats[shp.bsdf].flags & BT_NODELTA) {
-      DirSample dsr;
-      uint64_t ns = 0;
-      V3 li = VolSampleLight<BRICKS, HALF>(S, rng, p.medium, channel, si.P, si.N, dsr, err, ns, realDepth);
-      p.nShadow += (uint32_t)ns;
-      if (dsr.Pdf > 0.f) {
-        V3 wo = ToLocal(si.sh, dsr.Dir);
-        V3 f;
-        float bsdfPdf;
-        VBsdfEvalPdf(mats, (uint32_t)shp.bsdf, si.Wi, wo, f, bsdfPdf);
-        float weight = dsr.IsDelta ? 1.f : VMis(dsr.Pdf, bsdfPdf);
-        p.result = p.result + cmul(cmul(thr, f), li) * weight / dsr.Pdf;
-      }
-    }
-    float xl = Next1D(rng);
-    V2 xd = Next2D(rng);
-    BsdfSampleRes bs = VBsdfSample(mats, (uint32_t)shp.bsdf, si.Wi, xl, xd);
-    if (bs.pdf <= 0.f) return false;
-    thr = cmul(thr, bs.f) / bs.pdf;
-    p.eta *= bs.eta;
-    V3 nd = ToWorld(si.sh, bs.wo);
-    ray = Spawn(si.P, si.N, nd);
-    p.prevPdf = bs.pdf;
-    p.prevP = si.P;
-    p.isSpecular = (bs.type & BT_DELTA) != 0u;
-    p.medium = MediumOfHit(S, si, ray.D);
-  }
-  if (!(isSampleSurface || isSampleMedium)) return false;
-  p.depth++;
-  p.guard++;
-  return true;
+  float xl = Next1D(p.rng);
+  V2 xd = Next2D(p.rng);
+  BsdfSampleRes bs = VBsdfSample(mats, (uint32_t)shp.bsdf, si.Wi, xl, xd);
+  if (bs.pdf <= 0.f) return false;
+  thr = cmul(thr, bs.f) / bs.pdf;
+  p.eta *= bs.eta;
+  V3 nd = ToWorld(si.sh, bs.wo);
+  ray = Spawn(si.P, si.N, nd);
+  p.prevPdf = bs.pdf;
+  p.prevP = si.P;
+  p.isSpecular = (bs.type & BT_DELTA) != 0u;
+  p.medium = MediumOfHit(S, si, ray.D);
+  return VolNextIteration(p);
+}
+
+// The next part of the path's current iteration; false when the path has ended
+// (its radiance is in p.result).
+template <bool BRICKS, bool HALF>
+RD bool VolStep(const DevScene& S, VolPathState& p, uint32_t mode, uint32_t* err) {
+  if (p.act == kActScatter) return VolScatter<BRICKS, HALF>(S, p, mode, err);
+  if (p.act == kActSurface) return VolSurface<BRICKS, HALF>(S, p, mode, err);
+  return VolTop<BRICKS, HALF>(S, p, mode, err);
 }
 
 // The whole loop for one path (host-side checks and equivalence tests).
@@ -410,34 +450,61 @@ RD V3 VolLi(const DevScene& S, Pcg32& rng, VRay ray, uint32_t mode, uint32_t* er
 }
 
 #ifndef RAD_HOST_EMULATION
-// Persistent lanes: each thread runs its path one loop iteration at a time and
-// takes the next unstarted path (counter B.counters[kMiscBase + 4], reset by
-// the generate stage) as soon as its own ends, so warps stay full while path
-// lengths vary by orders of magnitude.
+// Persistent lanes: each thread runs its path one part of a loop iteration at a
+// time and takes the next unstarted path (counter B.counters[kMiscBase + 4],
+// reset by the generate stage) when its own ends. Each warp step runs the part
+// (top / medium scatter / surface) that most of the warp's live lanes are at, so
+// a warp executes one code path at a time while paths stay in different phases.
 template <bool BRICKS, bool HALF>
 __global__ void __launch_bounds__(kVolBlock)
     KVolPath(DevScene S, PathBuffers B, uint32_t count, uint32_t* err, uint32_t mode) {
   uint32_t* next = B.counters + kMiscBase + 4;
+  const uint32_t lane = threadIdx.x & 31u;
   VolPathState p;
   uint32_t idx = 0;
-  bool live = false;
+  bool live = false, drained = false;
   unsigned long long nRays = 0, nShadow = 0;
   for (;;) {
-    if (!live) {
-      idx = atomicAdd(next, 1u);
-      if (idx >= count) break;
-      float4 ro = B.rayO[idx], rd = B.rayD[idx];
-      uint2 rs = B.rng[idx];
-      Pcg32 rng;
-      rng.state = ((uint64_t)rs.y << 32) | rs.x;
-      VolInit(S, p, VRay{V3{ro.x, ro.y, ro.z}, V3{rd.x, rd.y, rd.z}, ro.w, rd.w}, rng);
-      live = true;
+    uint32_t need = __ballot_sync(0xffffffffu, !live);
+    if (need && !drained) {
+      int leader = __ffs(need) - 1;
+      uint32_t base = 0;
+      if ((int)lane == leader) base = atomicAdd(next, (uint32_t)__popc(need));
+      base = __shfl_sync(0xffffffffu, base, leader);
+      if (base + (uint32_t)__popc(need) >= count) drained = true;
+      if (!live) {
+        uint32_t i = base + __popc(need & ((1u << lane) - 1u));
+        if (i < count) {
+          idx = i;
+          float4 ro = B.rayO[idx], rd = B.rayD[idx];
+          uint2 rs = B.rng[idx];
+          Pcg32 rng;
+          rng.state = ((uint64_t)rs.y << 32) | rs.x;
+          VolInit(S, p, VRay{V3{ro.x, ro.y, ro.z}, V3{rd.x, rd.y, rd.z}, ro.w, rd.w}, rng);
+          live = true;
+        }
+      }
     }
-    if (!VolStep<BRICKS, HALF>(S, p, mode, err)) {
-      B.L[idx] = make_float4(p.result.x, p.result.y, p.result.z, 0.f);
-      nRays += p.nRays;
-      nShadow += p.nShadow;
-      live = false;
+    const uint32_t m0 = __ballot_sync(0xffffffffu, live && p.act == kActTop);
+    const uint32_t m1 = __ballot_sync(0xffffffffu, live && p.act == kActScatter);
+    const uint32_t m2 = __ballot_sync(0xffffffffu, live && p.act == kActSurface);
+    if ((m0 | m1 | m2) == 0u) break;
+    const int c0 = __popc(m0), c1 = __popc(m1), c2 = __popc(m2);
+    const int act = (c0 >= c1 && c0 >= c2) ? kActTop : (c1 >= c2 ? kActScatter : kActSurface);
+    if (live && p.act == act) {
+      bool alive;
+      if (act == kActTop)
+        alive = VolTop<BRICKS, HALF>(S, p, mode, err);
+      else if (act == kActScatter)
+        alive = VolScatter<BRICKS, HALF>(S, p, mode, err);
+      else
+        alive = VolSurface<BRICKS, HALF>(S, p, mode, err);
+      if (!alive) {
+        B.L[idx] = make_float4(p.result.x, p.result.y, p.result.z, 0.f);
+        nRays += p.nRays;
+        nShadow += p.nShadow;
+        live = false;
+      }
     }
   }
   // ray counters: closest in [kMiscBase + 2], shadow-side traces in [kMiscBase + 3]
