@@ -100,3 +100,20 @@ def test_autotune_picks_parameters_and_keeps_results(rad, scene_dir):
     with pytest.raises(rad.RadError):
         s.autotune({"refill_busy": [40]})
     s.close()
+
+
+def test_cli_renders_and_saves(rad, scene_dir):
+    """python -m radiantiumplusplus_gb300 --scene x.json writes <dir>/<stem>.exr equal to the job film."""
+    import os
+    import subprocess
+    import sys
+    from radiantiumplusplus_gb300.exr import read_exr
+    path = box(scene_dir, 32, 24, 4)[0]
+    r = subprocess.run([sys.executable, "-m", "radiantiumplusplus_gb300", "--scene", path], capture_output=True,
+                       text=True, timeout=300)
+    assert r.returncode == 0, r.stderr
+    out = os.path.join(os.path.dirname(path), "scene.exr")
+    assert os.path.exists(out) and "save result to" in r.stdout
+    s = rad.Scene.from_file(path)
+    assert np.allclose(read_exr(out), s.render(), rtol=0, atol=0)
+    s.close()

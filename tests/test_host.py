@@ -40,3 +40,14 @@ def test_unknown_factory_is_reported(oracle):
     sc["renderer"]["type"] = "bdpt_x"
     with pytest.raises(RuntimeError, match="cannot find factory"):
         oracle.OracleScene(json.dumps(sc), "")
+
+
+def test_cli_argument_errors():
+    """The CLI's argument errors (rad.offline.cli/main.cpp:14-33) need no GPU."""
+    import subprocess
+    import sys
+    r = subprocess.run([sys.executable, "-m", "radiantiumplusplus_gb300"], capture_output=True, text=True)
+    assert r.returncode == 2 and "--scene <scene.json>" in r.stderr
+    r = subprocess.run([sys.executable, "-m", "radiantiumplusplus_gb300", "--scene", "no_such_scene.json"],
+                       capture_output=True, text=True)
+    assert r.returncode == 2 and "cannot open file" in r.stderr
