@@ -829,6 +829,262 @@ struct DisneyBsdf final : Bsdf {
   }
 };
 
+// --------------------------------------------------------- perfect_mirror
+// perfect_mirror.cpp:17-62
+struct PerfectMirrorBsdf final : Bsdf {
+  Spectrum R, eta, k;
+  explicit PerfectMirrorBsdf(const Json* cfg) {
+    flags = BT_Delta | BT_Reflection;
+    R = ReadColor(cfg, "reflectance", V3(1));
+    eta = ReadColor(cfg, "eta", V3(0));
+    k = ReadColor(cfg, "k", V3(1));
+  }
+  std::pair<BsdfSample, Spectrum> Sample(const V3& wi, Float, const V2&) const override {
+    Float cosThetaI = wi.z;
+    if (cosThetaI <= 0) return {{}, Spectrum(0)};
+    BsdfSample bsr;
+    bsr.Wo = V3(-wi.x, -wi.y, wi.z);  // fresnel.cpp:10-12
+    bsr.Eta = 1;
+    bsr.Type = flags;
+    bsr.Pdf = 1;
+    Spectrum F = FresnelConductor(wi.z, eta, k);
+    return {bsr, cmul(R, F)};
+  }
+  Spectrum Eval(const V3&, const V3&) const override { return Spectrum(0); }
+  Float Pdf(const V3&, const V3&) const override { return 0; }
+};
+
+// ---------------------------------------------------------- perfect_glass
+// perfect_glass.cpp:17-87 (radiance transport)
+struct PerfectGlassBsdf final : Bsdf {
+  Spectrum R, T;
+  Float eta;
+  explicit PerfectGlassBsdf(const Json* cfg) {
+    flags = BT_Delta | BT_Reflection | BT_Transmission;
+    R = ReadColor(cfg, "reflectance", V3(1));
+    T = ReadColor(cfg, "transmittance", V3(1));
+    Float intIor = ReadF(cfg, "int_ior", Float(1.5046));
+    Float extIor = ReadF(cfg, "ext_ior", Float(1.000277));
+    eta = intIor / extIor;
+  }
+  std::pair<BsdfSample, Spectrum> Sample(const V3& wi, Float lobeXi, const V2&) const override {
+    Float ri, cosThetaT, etaIT, etaTI;
+    FresnelDielectric(wi.z, eta, ri, cosThetaT, etaIT, etaTI);
+    Float ti = 1 - ri;
+    BsdfSample bsr;
+    Spectrum f;
+    if (lobeXi <= ri) {
+      bsr.Wo = V3(-wi.x, -wi.y, wi.z);
+      bsr.Eta = 1;
+      bsr.Pdf = ri;
+      bsr.Type = BT_Delta | BT_Reflection;
+      f = R * ri;
+    } else {
+      bsr.Wo = V3(-etaTI * wi.x, -etaTI * wi.y, cosThetaT);  // fresnel.cpp:18-20
+      bsr.Eta = etaIT;
+      bsr.Pdf = ti;
+      bsr.Type = BT_Delta | BT_Transmission;
+      f = T * ti;
+      f = f * Sqr(etaTI);
+    }
+    return {bsr, f};
+  }
+  Spectrum Eval(const V3&, const V3&) const override { return Spectrum(0); }
+  Float Pdf(const V3&, const V3&) const override { return 0; }
+};
+
+// ------------------------------------------------- plastic / rough_plastic
+// fresnel.cpp:79-84
+static Float DiffuseReflectance(Float eta) {
+  Float invEta = Rcp(eta);
+  if (eta < 1) return Fmadd(Float(0.0636f), invEta, Fmadd(eta, Fmadd(eta, Float(-1.4399f), Float(0.7099f)), Float(0.6681f)));
+  // Horner(invEta, 0.919317, -3.4793, 6.75335, -7.80989, 4.98554, -1.36881) (math_base.h:90-105)
+  Float acc = Float(-1.36881f);
+  acc = Fmadd(invEta, acc, Float(4.98554f));
+  acc = Fmadd(invEta, acc, Float(-7.80989f));
+  acc = Fmadd(invEta, acc, Float(6.75335f));
+  acc = Fmadd(invEta, acc, Float(-3.4793f));
+  acc = Fmadd(invEta, acc, Float(0.919317f));
+  return acc;
+}
+static Float DielectricR(Float cosThetaI, Float eta) {
+  Float r, ct, eit, eti;
+  FresnelDielectric(cosThetaI, eta, r, ct, eit, eti);
+  return r;
+}
+// Constructor state shared by plastic.cpp:18-44 and rough_plastic.cpp:20-56.
+struct PlasticBase : Bsdf {
+  Float eta, fdrInt, invEta2, specularSampleWeight;
+  Spectrum diffuse, specular;
+  bool noLinear;
+  explicit PlasticBase(const Json* cfg) {
+    flags = BT_Diffuse | BT_Reflection | BT_Delta;
+    Float intIor = ReadF(cfg, "int_ior", Float(1.49f));
+    Float extIor = ReadF(cfg, "ext_ior", Float(1.000277f));
+    eta = intIor / extIor;
+    diffuse = ReadColor(cfg, "diffuse", V3(0.5f));
+    specular = ReadColor(cfg, "specular", V3(1));
+    noLinear = ReadB(cfg, "no_linear", false);
+    fdrInt = DiffuseReflectance(Float(1) / eta);
+    invEta2 = Float(1) / (eta * eta);
+    // the mean luminance over each texture's texels; constant textures are 1x1
+    double diffMean = 0, specMean = 0;
+    diffMean += Luminance(diffuse);
+    diffMean /= (1 * 1);
+    specMean += Luminance(specular);
+    specMean /= (1 * 1);
+    specularSampleWeight = (Float)(specMean / (diffMean + specMean));
+  }
+  Spectrum DiffuseTerm(Float fi, Float fo, Float cosThetaO) const {  // plastic.cpp:83-88
+    V3 num = diffuse * (1 / PI) * invEta2 * (1 - fi) * (1 - fo) * cosThetaO;
+    if (noLinear) {
+      V3 inv(Rcp(1 - diffuse.x * fdrInt), Rcp(1 - diffuse.y * fdrInt), Rcp(1 - diffuse.z * fdrInt));
+      return cmul(num, inv);
+    }
+    return num / (1 - fdrInt);
+  }
+};
+
+// plastic.cpp:16-139
+struct PlasticBsdf final : PlasticBase {
+  explicit PlasticBsdf(const Json* cfg) : PlasticBase(cfg) {}
+  std::pair<BsdfSample, Spectrum> Sample(const V3& wi, Float lobeXi, const V2& dirXi) const override {
+    Float cosThetaI = wi.z;
+    if (cosThetaI <= 0) return {{}, Spectrum(0)};
+    Float fi = DielectricR(cosThetaI, eta);
+    Float probSpec = fi * specularSampleWeight;
+    Float probDiff = (1 - fi) * (1 - specularSampleWeight);
+    probSpec = probSpec / (probSpec + probDiff);  // Delta and Diffuse both enabled
+    probDiff = 1 - probSpec;
+    BsdfSample bsr;
+    bsr.Eta = 1;
+    Spectrum f;
+    if (lobeXi < probSpec) {
+      bsr.Wo = V3(-wi.x, -wi.y, wi.z);
+      bsr.Pdf = probSpec;
+      bsr.Type = BT_Reflection | BT_Delta;
+      f = specular * fi;
+    } else {
+      bsr.Wo = SquareToCosineHemisphere(dirXi);
+      bsr.Pdf = SquareToCosineHemispherePdf(bsr.Wo) * probDiff;
+      bsr.Type = BT_Reflection | BT_Diffuse;
+      Float cosThetaO = bsr.Wo.z;
+      Float fo = DielectricR(cosThetaO, eta);
+      f = DiffuseTerm(fi, fo, cosThetaO);
+    }
+    return {bsr, f};
+  }
+  Spectrum Eval(const V3& wi, const V3& wo) const override {
+    Float cosThetaI = wi.z, cosThetaO = wo.z;
+    if (cosThetaI <= 0 || cosThetaO <= 0) return Spectrum(0);
+    Float fi = DielectricR(cosThetaI, eta);
+    Float fo = DielectricR(cosThetaO, eta);
+    return DiffuseTerm(fi, fo, cosThetaO);
+  }
+  Float Pdf(const V3& wi, const V3& wo) const override {
+    Float cosThetaI = wi.z, cosThetaO = wo.z;
+    if (cosThetaI <= 0 || cosThetaO <= 0) return 0;
+    Float fi = DielectricR(cosThetaI, eta);
+    Float probSpec = fi * specularSampleWeight;
+    Float probDiff = (1 - fi) * (1 - specularSampleWeight);
+    probDiff = probDiff / (probDiff + probSpec);
+    return SquareToCosineHemispherePdf(wo) * probDiff;
+  }
+};
+
+// rough_plastic.cpp:17-241 (default context: Glossy and Diffuse both enabled)
+struct RoughPlasticBsdf final : PlasticBase {
+  Microfacet dist;
+  explicit RoughPlasticBsdf(const Json* cfg) : PlasticBase(cfg) {
+    std::string d = ReadS(cfg, "distribution", "ggx");
+    dist.ggx = d != "beckmann";
+    dist.alphaX = dist.alphaY = ReadMono(cfg, "alpha", 0.1f);
+    dist.sampleVisible = ReadB(cfg, "sample_visible", true);
+  }
+  std::pair<BsdfSample, Spectrum> Sample(const V3& wi, Float lobeXi, const V2& dirXi) const override {
+    Float cosThetaI = wi.z;
+    if (cosThetaI <= 0) return {{}, Spectrum(0)};
+    Float fi = DielectricR(cosThetaI, eta);
+    Float probSpec = fi * specularSampleWeight;
+    Float probDiff = (1 - fi) * (1 - specularSampleWeight);
+    probSpec = probSpec / (probSpec + probDiff);
+    BsdfSample bsr;
+    bsr.Eta = 1;
+    if (lobeXi < probSpec) {
+      auto whp = dist.Sample(wi, dirXi);
+      if (whp.second <= 0) return {bsr, Spectrum(0)};
+      bsr.Wo = FresnelReflect(wi, whp.first);
+      bsr.Type = BT_Glossy | BT_Reflection;
+    } else {
+      bsr.Wo = SquareToCosineHemisphere(dirXi);
+      bsr.Type = BT_Diffuse | BT_Reflection;
+    }
+    bsr.Pdf = Pdf(wi, bsr.Wo);
+    if (bsr.Pdf <= 0) return {bsr, Spectrum(0)};
+    return {bsr, Eval(wi, bsr.Wo)};
+  }
+  Spectrum Eval(const V3& wi, const V3& wo) const override {
+    Float cosThetaI = wi.z, cosThetaO = wo.z;
+    if (cosThetaI <= 0 || cosThetaO <= 0) return Spectrum(0);
+    V3 wh = normalized(wo + wi);
+    Float F = DielectricR(dot(wi, wh), eta);
+    Float Dv = dist.D(wh);
+    Float Gv = dist.G(wi, wo, wh);
+    Spectrum spec = specular * Dv * Gv * F / (4 * cosThetaI);
+    Float fo = DielectricR(dot(wo, wh), eta);
+    Spectrum diff = DiffuseTerm(F, fo, cosThetaO);
+    return spec + diff;
+  }
+  Float Pdf(const V3& wi, const V3& wo) const override {
+    Float cosThetaI = wi.z, cosThetaO = wo.z;
+    if (cosThetaI <= 0 || cosThetaO <= 0) return 0;
+    Float fi = DielectricR(cosThetaI, eta);
+    Float probSpec = fi * specularSampleWeight;
+    Float probDiff = (1 - fi) * (1 - specularSampleWeight);
+    probSpec = probSpec / (probSpec + probDiff);
+    probDiff = 1 - probSpec;
+    V3 wh = normalized(wo + wi);
+    Float specPdf = dist.Pdf(wi, wh) / (4 * dot(wo, wh)) * probSpec;
+    Float diffPdf = SquareToCosineHemispherePdf(wo) * probDiff;
+    return specPdf + diffPdf;
+  }
+};
+
+// ------------------------------------------------------------------- mask
+// mask.cpp:10-69
+struct MaskBsdf final : Bsdf {
+  Float opacity;
+  std::unique_ptr<Bsdf> nested;
+  explicit MaskBsdf(const Json* cfg) {
+    opacity = ReadMono(cfg, "opacity", 0.5f);
+    if (!cfg || !cfg->has("nested")) throw std::runtime_error("mask needs a nested bsdf");
+    nested = MakeBsdf(cfg->find("nested"));
+    flags = nested->flags;
+  }
+  Float EvalOpacity() const { return std::clamp(opacity, Float(0), Float(1)); }
+  std::pair<BsdfSample, Spectrum> Sample(const V3& wi, Float lobeXi, const V2& dirXi) const override {
+    Float op = EvalOpacity();
+    BsdfSample bsr;
+    Spectrum result;
+    if (lobeXi < op) {
+      lobeXi /= op;
+      auto r = nested->Sample(wi, lobeXi, dirXi);
+      bsr = r.first;
+      bsr.Pdf *= op;
+      result = r.second * op;
+    } else {
+      result = Spectrum(1);
+      bsr.Pdf = 1 - op;
+      bsr.Eta = 1;
+      bsr.Wo = -wi;
+      bsr.Type = BT_Null;
+    }
+    return {bsr, result};
+  }
+  Spectrum Eval(const V3& wi, const V3& wo) const override { return nested->Eval(wi, wo) * EvalOpacity(); }
+  Float Pdf(const V3& wi, const V3& wo) const override { return nested->Pdf(wi, wo) * EvalOpacity(); }
+};
+
 // --------------------------------------------------------------- two_side
 // two_side.cpp:64-129
 struct TwoSideBsdf final : Bsdf {
@@ -880,6 +1136,11 @@ std::unique_ptr<Bsdf> MakeBsdf(const Json* cfg) {
   if (type == "rough_glass") return std::make_unique<RoughGlassBsdf>(cfg);
   if (type == "disney") return std::make_unique<DisneyBsdf>(cfg);
   if (type == "two_side") return std::make_unique<TwoSideBsdf>(cfg);
+  if (type == "perfect_mirror") return std::make_unique<PerfectMirrorBsdf>(cfg);
+  if (type == "perfect_glass") return std::make_unique<PerfectGlassBsdf>(cfg);
+  if (type == "plastic") return std::make_unique<PlasticBsdf>(cfg);
+  if (type == "rough_plastic") return std::make_unique<RoughPlasticBsdf>(cfg);
+  if (type == "mask") return std::make_unique<MaskBsdf>(cfg);
   throw std::runtime_error("cannot find factory: " + type);
 }
 

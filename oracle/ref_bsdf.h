@@ -1,6 +1,7 @@
 // ORACLE — TEST INFRASTRUCTURE ONLY (see ref_core.h).
 // BSDF restatement: rad.offline/include/rad/offline/render/bsdf.h:10-142 and
-// src/bsdf/{diffuse,rough_metal,rough_glass,disney,two_side}.cpp.
+// src/bsdf/{diffuse,rough_metal,rough_glass,disney,two_side,perfect_mirror,perfect_glass,
+// plastic,rough_plastic,mask}.cpp.
 #pragma once
 #include "ref_core.h"
 
@@ -37,7 +38,8 @@ struct Bsdf {
   virtual Float Pdf(const V3& wi, const V3& wo) const = 0;
 };
 
-// Factory by the reference's names: diffuse, rough_metal, rough_glass, disney, two_side.
+// Factory by the reference's names: diffuse, rough_metal, rough_glass, disney, two_side,
+// perfect_mirror, perfect_glass, plastic, rough_plastic, mask.
 std::unique_ptr<Bsdf> MakeBsdf(const Json* cfg);
 
 // Warps: rad.offline/src/warp.cpp:10-99

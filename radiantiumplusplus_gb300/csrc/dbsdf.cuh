@@ -1,8 +1,11 @@
 // Device BSDFs: diffuse (diffuse.cpp:46-99), rough_metal (rough_metal.cpp:22-176),
-// rough_glass (rough_glass.cpp:22-221), disney (disney.cpp:28-613) and
-// two_side (two_side.cpp:64-129). Eval and Pdf are fused into one call that
-// shares the half vector, D and G between the value and the density; each
-// result equals the reference's separate Eval / Pdf for the same inputs.
+// rough_glass (rough_glass.cpp:22-221), disney (disney.cpp:28-613),
+// perfect_mirror (perfect_mirror.cpp:17-70), perfect_glass (perfect_glass.cpp:17-87),
+// plastic (plastic.cpp:16-139), rough_plastic (rough_plastic.cpp:17-241) and the
+// wrappers two_side (two_side.cpp:64-129) and mask (mask.cpp:10-69). Eval and Pdf
+// are fused into one call that shares the half vector, D and G between the value
+// and the density; each result equals the reference's separate Eval / Pdf for the
+// same inputs.
 #pragma once
 #include "dmath.cuh"
 
@@ -452,6 +455,156 @@ RD BsdfSampleRes DisneySample(const MatRec& m, V3 wi, float lobeXi, V2 dirXi) {
   return r;
 }
 
+// ---------------------------------------------------------- perfect_mirror
+// perfect_mirror.cpp:27-48; Eval and Pdf are 0 (:50-62).
+RD BsdfSampleRes MirrorSample(const MatRec& m, V3 wi) {
+  BsdfSampleRes r{};
+  if (wi.z <= 0.f) return r;
+  r.wo = V3{-wi.x, -wi.y, wi.z};
+  r.eta = 1.f;
+  r.type = m.flags;
+  r.pdf = 1.f;
+  r.f = cmul(ld3(m.p), FresnelConductor(wi.z, ld3(m.p + 3), ld3(m.p + 6)));
+  return r;
+}
+
+// ----------------------------------------------------------- perfect_glass
+// perfect_glass.cpp:29-72 (radiance transport); Eval and Pdf are 0.
+RD BsdfSampleRes PerfectGlassSample(const MatRec& m, V3 wi, float lobeXi) {
+  BsdfSampleRes r{};
+  Dielectric fr = FresnelDielectric(wi.z, m.p[6]);
+  float ti = 1.f - fr.r;
+  if (lobeXi <= fr.r) {
+    r.wo = V3{-wi.x, -wi.y, wi.z};
+    r.eta = 1.f;
+    r.pdf = fr.r;
+    r.type = BT_DELTA | BT_REFLECTION;
+    r.f = ld3(m.p) * fr.r;
+  } else {
+    r.wo = V3{-fr.etaTI * wi.x, -fr.etaTI * wi.y, fr.cosThetaT};
+    r.eta = fr.etaIT;
+    r.pdf = ti;
+    r.type = BT_DELTA | BT_TRANSMISSION;
+    r.f = (ld3(m.p + 3) * ti) * Sqr(fr.etaTI);
+  }
+  return r;
+}
+
+// ------------------------------------------------- plastic / rough_plastic
+// Shared layout: p0..2 diffuse, p3..5 specular, p6 eta, p7 1/eta^2, p8 the
+// internal diffuse Fresnel reflectance, p13 specular sampling weight, p14 no_linear.
+// The diffuse term of plastic.cpp:80-88 / rough_plastic.cpp:143-153.
+RD V3 PlasticDiffuse(const MatRec& m, float fi, float fo, float cosThetaO) {
+  V3 diff = ld3(m.p);
+  float a = 1.f - fi, b = 1.f - fo;
+  V3 num{((((diff.x * (1.f / kPi)) * m.p[7]) * a) * b) * cosThetaO,
+         ((((diff.y * (1.f / kPi)) * m.p[7]) * a) * b) * cosThetaO,
+         ((((diff.z * (1.f / kPi)) * m.p[7]) * a) * b) * cosThetaO};
+  if (m.p[14] != 0.f)
+    return V3{num.x * Rcp(1.f - diff.x * m.p[8]), num.y * Rcp(1.f - diff.y * m.p[8]),
+              num.z * Rcp(1.f - diff.z * m.p[8])};
+  float den = 1.f - m.p[8];
+  return V3{num.x / den, num.y / den, num.z / den};
+}
+// Probability of the specular lobe (plastic.cpp:58-66, rough_plastic.cpp:72-80).
+RD float PlasticSpecProb(const MatRec& m, float fi) {
+  float probSpec = fi * m.p[13];
+  float probDiff = (1.f - fi) * (1.f - m.p[13]);
+  return probSpec / (probSpec + probDiff);
+}
+// plastic.cpp:93-139: only the diffuse lobe has a density.
+RD void PlasticEvalPdf(const MatRec& m, V3 wi, V3 wo, V3& f, float& pdf) {
+  float cosThetaI = wi.z, cosThetaO = wo.z;
+  if (cosThetaI <= 0.f || cosThetaO <= 0.f) {
+    f = v3s(0.f);
+    pdf = 0.f;
+    return;
+  }
+  float fi = FresnelDielectric(cosThetaI, m.p[6]).r;
+  float fo = FresnelDielectric(cosThetaO, m.p[6]).r;
+  f = PlasticDiffuse(m, fi, fo, cosThetaO);
+  float probSpec = fi * m.p[13];
+  float probDiff = (1.f - fi) * (1.f - m.p[13]);
+  probDiff = probDiff / (probDiff + probSpec);
+  pdf = SquareToCosineHemispherePdf(wo) * probDiff;
+}
+// plastic.cpp:47-91
+RD BsdfSampleRes PlasticSample(const MatRec& m, V3 wi, float lobeXi, V2 dirXi) {
+  BsdfSampleRes r{};
+  float cosThetaI = wi.z;
+  if (cosThetaI <= 0.f) return r;
+  float fi = FresnelDielectric(cosThetaI, m.p[6]).r;
+  float probSpec = PlasticSpecProb(m, fi);
+  float probDiff = 1.f - probSpec;
+  r.eta = 1.f;
+  if (lobeXi < probSpec) {
+    r.wo = V3{-wi.x, -wi.y, wi.z};
+    r.pdf = probSpec;
+    r.type = BT_REFLECTION | BT_DELTA;
+    r.f = ld3(m.p + 3) * fi;
+  } else {
+    r.wo = SquareToCosineHemisphere(dirXi);
+    r.pdf = SquareToCosineHemispherePdf(r.wo) * probDiff;
+    r.type = BT_REFLECTION | BT_DIFFUSE;
+    float cosThetaO = r.wo.z;
+    float fo = FresnelDielectric(cosThetaO, m.p[6]).r;
+    r.f = PlasticDiffuse(m, fi, fo, cosThetaO);
+  }
+  return r;
+}
+// rough_plastic.cpp:122-158 (value) and :183-214 (density) for one (wi, wo).
+RD void RoughPlasticEvalPdf(const MatRec& m, V3 wi, V3 wo, V3& f, float& pdf) {
+  float cosThetaI = wi.z, cosThetaO = wo.z;
+  if (cosThetaI <= 0.f || cosThetaO <= 0.f) {
+    f = v3s(0.f);
+    pdf = 0.f;
+    return;
+  }
+  Microfacet d = MatDist(m);
+  V3 wh = normalized(wo + wi);
+  float F = FresnelDielectric(dot(wi, wh), m.p[6]).r;
+  float D = MfD(d, wh);
+  float G = MfG(d, wi, wo, wh);
+  V3 spec = ld3(m.p + 3);
+  float den = 4.f * cosThetaI;
+  V3 specular{(((spec.x * D) * G) * F) / den, (((spec.y * D) * G) * F) / den, (((spec.z * D) * G) * F) / den};
+  float fo = FresnelDielectric(dot(wo, wh), m.p[6]).r;
+  f = specular + PlasticDiffuse(m, F, fo, cosThetaO);
+  float fi = FresnelDielectric(cosThetaI, m.p[6]).r;
+  float probSpec = PlasticSpecProb(m, fi);
+  float probDiff = 1.f - probSpec;
+  float specPdf = MfPdf(d, wi, wh) / (4.f * dot(wo, wh)) * probSpec;
+  float diffPdf = SquareToCosineHemispherePdf(wo) * probDiff;
+  pdf = specPdf + diffPdf;
+}
+// rough_plastic.cpp:58-98
+RD BsdfSampleRes RoughPlasticSample(const MatRec& m, V3 wi, float lobeXi, V2 dirXi) {
+  BsdfSampleRes r{};
+  float cosThetaI = wi.z;
+  if (cosThetaI <= 0.f) return r;
+  float fi = FresnelDielectric(cosThetaI, m.p[6]).r;
+  float probSpec = PlasticSpecProb(m, fi);
+  r.eta = 1.f;
+  if (lobeXi < probSpec) {
+    Microfacet d = MatDist(m);
+    float mpdf;
+    V3 wh = MfSample(d, wi, dirXi, mpdf);
+    if (mpdf <= 0.f) return r;
+    r.wo = Reflect(wi, wh);
+    r.type = BT_GLOSSY | BT_REFLECTION;
+  } else {
+    r.wo = SquareToCosineHemisphere(dirXi);
+    r.type = BT_DIFFUSE | BT_REFLECTION;
+  }
+  V3 f;
+  float pdf;
+  RoughPlasticEvalPdf(m, wi, r.wo, f, pdf);
+  r.pdf = pdf;
+  if (pdf <= 0.f) return r;
+  r.f = f;
+  return r;
+}
+
 // ---------------------------------------------------------------- dispatch
 RD void LeafEvalPdf(const MatRec& m, V3 wi, V3 wo, V3& f, float& pdf) {
   switch (m.kind) {
@@ -459,7 +612,9 @@ RD void LeafEvalPdf(const MatRec& m, V3 wi, V3 wo, V3& f, float& pdf) {
     case MAT_ROUGH_METAL: MetalEvalPdf(m, wi, wo, f, pdf); return;
     case MAT_ROUGH_GLASS: GlassEvalPdf(m, wi, wo, f, pdf); return;
     case MAT_DISNEY: DisneyEvalPdf(m, wi, wo, f, pdf); return;
-    default: f = v3s(0.f); pdf = 0.f; return;
+    case MAT_PLASTIC: PlasticEvalPdf(m, wi, wo, f, pdf); return;
+    case MAT_ROUGH_PLASTIC: RoughPlasticEvalPdf(m, wi, wo, f, pdf); return;
+    default: f = v3s(0.f); pdf = 0.f; return;  // delta-only BSDFs: Eval = Pdf = 0
   }
 }
 RD BsdfSampleRes LeafSample(const MatRec& m, V3 wi, float lobeXi, V2 dirXi) {
@@ -468,35 +623,92 @@ RD BsdfSampleRes LeafSample(const MatRec& m, V3 wi, float lobeXi, V2 dirXi) {
     case MAT_ROUGH_METAL: return MetalSample(m, wi, dirXi);
     case MAT_ROUGH_GLASS: return GlassSample(m, wi, lobeXi, dirXi);
     case MAT_DISNEY: return DisneySample(m, wi, lobeXi, dirXi);
+    case MAT_PERFECT_MIRROR: return MirrorSample(m, wi);
+    case MAT_PERFECT_GLASS: return PerfectGlassSample(m, wi, lobeXi);
+    case MAT_PLASTIC: return PlasticSample(m, wi, lobeXi, dirXi);
+    case MAT_ROUGH_PLASTIC: return RoughPlasticSample(m, wi, lobeXi, dirXi);
     default: return BsdfSampleRes{};
   }
 }
-// two_side.cpp:64-129 resolves to a leaf with z flips.
+// Wrappers resolve to a leaf: two_side (two_side.cpp:64-129) picks the outside
+// or inside BSDF by the sign of wi.z and mirrors z for the inside one; mask
+// (mask.cpp:24-60) scales the nested BSDF by its opacity, or, for the share of
+// samples beyond the opacity, passes the ray straight through (a Null event).
+// Scales are applied innermost first, as the nested calls would apply them; the
+// host limits wrapper nesting to kMaxBsdfNest levels.
 RD void BsdfEvalPdf(const MatRec* mats, uint32_t mi, V3 wi, V3 wo, V3& f, float& pdf) {
-  const MatRec& m = mats[mi];
-  if (m.kind != MAT_TWO_SIDE) {
-    LeafEvalPdf(m, wi, wo, f, pdf);
-    return;
+  float ops[kMaxBsdfNest];
+  int nops = 0;
+  f = v3s(0.f);
+  pdf = 0.f;
+  for (int lvl = 0; lvl <= kMaxBsdfNest; lvl++) {
+    const MatRec& m = mats[mi];
+    if (m.kind == MAT_TWO_SIDE) {
+      if (wi.z > 0.f) {
+        mi = m.ref0;
+      } else if (wi.z < 0.f) {
+        mi = m.ref1;
+        wi.z = -wi.z;
+        wo.z = -wo.z;
+      } else {
+        break;
+      }
+    } else if (m.kind == MAT_MASK) {
+      if (nops == kMaxBsdfNest) break;
+      ops[nops++] = m.p[0];
+      mi = m.ref0;
+    } else {
+      LeafEvalPdf(m, wi, wo, f, pdf);
+      break;
+    }
   }
-  if (wi.z > 0.f) {
-    LeafEvalPdf(mats[m.ref0], wi, wo, f, pdf);
-  } else if (wi.z < 0.f) {
-    LeafEvalPdf(mats[m.ref1], V3{wi.x, wi.y, -wi.z}, V3{wo.x, wo.y, -wo.z}, f, pdf);
-  } else {
-    f = v3s(0.f);
-    pdf = 0.f;
+  for (int k = nops - 1; k >= 0; k--) {
+    f = f * ops[k];
+    pdf = pdf * ops[k];
   }
 }
 RD BsdfSampleRes BsdfSample(const MatRec* mats, uint32_t mi, V3 wi, float lobeXi, V2 dirXi) {
-  const MatRec& m = mats[mi];
-  if (m.kind != MAT_TWO_SIDE) return LeafSample(m, wi, lobeXi, dirXi);
-  if (wi.z > 0.f) return LeafSample(mats[m.ref0], wi, lobeXi, dirXi);
-  if (wi.z < 0.f) {
-    BsdfSampleRes r = LeafSample(mats[m.ref1], V3{wi.x, wi.y, -wi.z}, lobeXi, dirXi);
-    r.wo.z *= -1.f;
-    return r;
+  float ops[kMaxBsdfNest];
+  int nops = 0;
+  bool flip = false;
+  BsdfSampleRes r{};
+  for (int lvl = 0; lvl <= kMaxBsdfNest; lvl++) {
+    const MatRec& m = mats[mi];
+    if (m.kind == MAT_TWO_SIDE) {
+      if (wi.z > 0.f) {
+        mi = m.ref0;
+      } else if (wi.z < 0.f) {
+        mi = m.ref1;
+        wi.z = -wi.z;
+        flip = !flip;
+      } else {
+        break;
+      }
+    } else if (m.kind == MAT_MASK) {
+      float op = m.p[0];
+      if (lobeXi < op && nops < kMaxBsdfNest) {
+        lobeXi /= op;
+        ops[nops++] = op;
+        mi = m.ref0;
+      } else {
+        r.f = v3s(1.f);
+        r.pdf = 1.f - op;
+        r.eta = 1.f;
+        r.wo = -wi;
+        r.type = BT_NULL;
+        break;
+      }
+    } else {
+      r = LeafSample(m, wi, lobeXi, dirXi);
+      break;
+    }
   }
-  return BsdfSampleRes{};
+  for (int k = nops - 1; k >= 0; k--) {
+    r.pdf *= ops[k];
+    r.f = r.f * ops[k];
+  }
+  if (flip) r.wo.z = -r.wo.z;
+  return r;
 }
 
 }  // namespace rad
@@ -524,6 +736,10 @@ RD BsdfSampleRes LeafSampleK(const MatRec& m, V3 wi, float lobeXi, V2 dirXi) {
 }
 template <int K>
 RD void ClassEvalPdf(const MatRec* mats, uint32_t mi, V3 wi, V3 wo, V3& f, float& pdf) {
+  if constexpr (K == SC_GENERIC) {
+    BsdfEvalPdf(mats, mi, wi, wo, f, pdf);
+    return;
+  }
   const MatRec& m = mats[mi];
   if (m.kind != MAT_TWO_SIDE) {
     LeafEvalPdfK<K>(m, wi, wo, f, pdf);
@@ -538,6 +754,7 @@ RD void ClassEvalPdf(const MatRec* mats, uint32_t mi, V3 wi, V3 wo, V3& f, float
 }
 template <int K>
 RD BsdfSampleRes ClassSample(const MatRec* mats, uint32_t mi, V3 wi, float lobeXi, V2 dirXi) {
+  if constexpr (K == SC_GENERIC) return BsdfSample(mats, mi, wi, lobeXi, dirXi);
   const MatRec& m = mats[mi];
   if (m.kind != MAT_TWO_SIDE) return LeafSampleK<K>(m, wi, lobeXi, dirXi);
   if (wi.z > 0.f) return LeafSampleK<K>(mats[m.ref0], wi, lobeXi, dirXi);

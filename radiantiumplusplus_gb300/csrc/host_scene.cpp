@@ -381,6 +381,24 @@ bool DisneyHas(const JValue* c, const char* k) {  // disney.cpp:459-471
   return true;
 }
 
+// fresnel.cpp:79-84 (the polynomial fits of the internal diffuse reflectance).
+float DiffuseReflectance(float eta) {
+  float invEta = 1.f / eta;
+  if (eta < 1.f) return std::fma(0.0636f, invEta, std::fma(eta, std::fma(eta, -1.4399f, 0.7099f), 0.6681f));
+  const float c[6] = {0.919317f, -3.4793f, 6.75335f, -7.80989f, 4.98554f, -1.36881f};
+  float acc = c[5];
+  for (int i = 4; i >= 0; i--) acc = std::fma(invEta, acc, c[i]);
+  return acc;
+}
+float LuminanceF(F3 c) { return (c.x * 0.212671f) + (c.y * 0.715160f) + (c.z * 0.072169f); }  // color.h:33
+// Wrapper levels (two_side, mask) above the leaves of material i.
+int WrapDepth(const std::vector<MatRec>& v, uint32_t i) {
+  const MatRec& m = v[i];
+  if (m.kind == MAT_TWO_SIDE) return 1 + std::max(WrapDepth(v, m.ref0), WrapDepth(v, m.ref1));
+  if (m.kind == MAT_MASK) return 1 + WrapDepth(v, m.ref0);
+  return 0;
+}
+
 uint32_t AddMaterial(const JValue* c, std::vector<MatRec>& out) {
   MatRec m;
   std::memset(&m, 0, sizeof(m));
@@ -446,6 +464,47 @@ uint32_t AddMaterial(const JValue* c, std::vector<MatRec>& out) {
     m.flags = BT_DIFFUSE | BT_REFLECTION;
     if (m.dflags & DF_CLEARCOAT) m.flags |= BT_GLOSSY;
     if (hasST) m.flags |= BT_TRANSMISSION;
+  } else if (type == "perfect_mirror") {  // perfect_mirror.cpp:19-25
+    m.kind = MAT_PERFECT_MIRROR;
+    m.flags = BT_DELTA | BT_REFLECTION;
+    put3(0, Color(c, "reflectance", F3(1, 1, 1)));
+    put3(3, Color(c, "eta", F3(0, 0, 0)));
+    put3(6, Color(c, "k", F3(1, 1, 1)));
+  } else if (type == "perfect_glass") {  // perfect_glass.cpp:19-26
+    m.kind = MAT_PERFECT_GLASS;
+    m.flags = BT_DELTA | BT_REFLECTION | BT_TRANSMISSION;
+    put3(0, Color(c, "reflectance", F3(1, 1, 1)));
+    put3(3, Color(c, "transmittance", F3(1, 1, 1)));
+    m.p[6] = RF(c, "int_ior", 1.5046f) / RF(c, "ext_ior", 1.000277f);
+  } else if (type == "plastic" || type == "rough_plastic") {  // plastic.cpp:18-44, rough_plastic.cpp:20-56
+    bool rough = type == "rough_plastic";
+    m.kind = rough ? MAT_ROUGH_PLASTIC : MAT_PLASTIC;
+    m.flags = BT_DIFFUSE | BT_REFLECTION | BT_DELTA;
+    float eta = RF(c, "int_ior", 1.49f) / RF(c, "ext_ior", 1.000277f);
+    F3 diff = Color(c, "diffuse", F3(0.5f, 0.5f, 0.5f));
+    F3 spec = Color(c, "specular", F3(1, 1, 1));
+    put3(0, diff);
+    put3(3, spec);
+    m.p[6] = eta;
+    m.p[7] = 1.f / (eta * eta);
+    m.p[8] = DiffuseReflectance(1.f / eta);
+    // mean luminance of each (constant, 1x1) texture, accumulated in double
+    double diffMean = (double)LuminanceF(diff) / 1.0, specMean = (double)LuminanceF(spec) / 1.0;
+    m.p[13] = (float)(specMean / (diffMean + specMean));
+    m.p[14] = RB(c, "no_linear", false) ? 1.f : 0.f;
+    if (rough) {
+      std::string dist = RS(c, "distribution", "ggx");
+      m.p[11] = dist == "beckmann" ? 0.f : 1.f;  // unknown names fall back to GGX (rough_plastic.cpp:31-38)
+      m.p[9] = m.p[10] = Mono(c, "alpha", 0.1f);
+      m.p[12] = RB(c, "sample_visible", true) ? 1.f : 0.f;
+    }
+  } else if (type == "mask") {  // mask.cpp:12-21
+    m.kind = MAT_MASK;
+    float op = Mono(c, "opacity", 0.5f);
+    m.p[0] = op < 0.f ? 0.f : (1.f < op ? 1.f : op);  // EvalOpacity clamps (mask.cpp:63-65)
+    if (!c->has("nested")) throw ConfigError("mask needs a nested bsdf");
+    m.ref0 = AddMaterial(c->get("nested"), out);
+    m.flags = out[m.ref0].flags;
   } else if (type == "two_side") {  // two_side.cpp:18-62
     m.kind = MAT_TWO_SIDE;
     if (c->has("two_side")) {
@@ -460,6 +519,7 @@ uint32_t AddMaterial(const JValue* c, std::vector<MatRec>& out) {
     throw FactoryError("cannot find factory: " + type);
   }
   out[index] = m;
+  if (WrapDepth(out, index) > kMaxBsdfNest) throw ConfigError("two_side / mask BSDFs nest more than 4 levels deep");
   return index;
 }
 

@@ -197,7 +197,7 @@ __device__ __forceinline__ bool GuidedScatter(const DevScene& S, const PathBuffe
   V2 xd = Next2D(rng);
   V3 f, wiW;
   float pm, bpdf, etaS = 1.f;
-  bool delta = false, ok;
+  bool delta = false, discrete = false, ok;
   if (us < gc) {
     wiW = GuideMixSamplePacked(gmix, xl, xd);
     V3 wl = ToLocal(si.sh, wiW);
@@ -210,8 +210,10 @@ __device__ __forceinline__ bool GuidedScatter(const DevScene& S, const PathBuffe
     bpdf = bs.pdf;
     etaS = bs.eta;
     delta = (bs.type & BT_DELTA) != 0u;
+    // delta lobes and mask pass-through are point masses the guide never draws
+    discrete = (bs.type & (BT_DELTA | BT_NULL)) != 0u;
     wiW = ToWorld(si.sh, bs.wo);
-    pm = delta ? (1.f - gc) * bs.pdf : gc * GuideMixPdfPacked(gmix, wiW) + (1.f - gc) * bs.pdf;
+    pm = discrete ? (1.f - gc) * bs.pdf : gc * GuideMixPdfPacked(gmix, wiW) + (1.f - gc) * bs.pdf;
     ok = bs.pdf > 0.f && pm > 0.f;
   }
   if (!ok) return false;
@@ -231,7 +233,7 @@ __device__ __forceinline__ bool GuidedScatter(const DevScene& S, const PathBuffe
   B.rng[p] = make_uint2((uint32_t)rng.state, (uint32_t)(rng.state >> 32));
   float4 L4 = B.L[p];
   B.L[p] = make_float4(L4.x, L4.y, L4.z, pm);
-  if (G.train && !delta && (uint32_t)depth < G.trainDepth &&
+  if (G.train && !discrete && (uint32_t)depth < G.trainDepth &&
       (G.trainShift == 0u || (GuideHash32(B.pixel[p] ^ G.trainSalt) >> (32u - G.trainShift)) == 0u)) {
     uint32_t slot = atomicAdd(G.ctl, 1u);
     if (slot < G.recCap) {
@@ -320,7 +322,8 @@ __global__ void __launch_bounds__(kBlock) KShadeClass(DevScene S, PathBuffers B,
         float gc = 0.f;
         if constexpr (GUIDED) {
           gmix = G.mix + (size_t)p * kGMixF4;
-          gc = gmix[10].x;
+          // a BSDF with only delta lobes gives the guide nothing to propose
+          gc = (mats[bsdf].flags & BT_NODELTA) ? gmix[10].x : 0.f;
         }
         if (mats[bsdf].flags & BT_NODELTA) {
           float xl = Next1D(rng);

@@ -15,11 +15,12 @@ namespace rad {
 
 // ---------------------------------------------------------------- BSDFs
 enum MatKind : uint32_t { MAT_NONE = 0, MAT_DIFFUSE = 1, MAT_ROUGH_METAL = 2, MAT_ROUGH_GLASS = 3, MAT_DISNEY = 4,
-                          MAT_TWO_SIDE = 5 };
+                          MAT_TWO_SIDE = 5, MAT_PERFECT_MIRROR = 6, MAT_PERFECT_GLASS = 7, MAT_PLASTIC = 8,
+                          MAT_ROUGH_PLASTIC = 9, MAT_MASK = 10 };
 
 // BsdfType bits (rad.offline/include/rad/offline/render/bsdf.h:32-50)
 enum : uint32_t { BT_DIFFUSE = 1, BT_GLOSSY = 2, BT_DELTA = 4, BT_REFLECTION = 8, BT_TRANSMISSION = 16,
-                  BT_NODELTA = 3 };
+                  BT_NULL = 32, BT_NODELTA = 3 };
 
 // Disney "present" flags (disney.cpp:459-471)
 enum : uint32_t { DF_ANISO = 1, DF_SPECTRANS = 2, DF_SHEEN = 4, DF_SHEENTINT = 8, DF_FLATNESS = 16,
@@ -32,17 +33,25 @@ enum : uint32_t { DF_ANISO = 1, DF_SPECTRANS = 2, DF_SHEEN = 4, DF_SHEENTINT = 8
 //  disney:      p0..2 baseColor, p3 roughness, p4 anisotropic, p5 specTrans, p6 sheen, p7 sheenTint,
 //               p8 flatness, p9 specTint, p10 metallic, p11 clearcoat, p12 clearcoatGloss, p13 eta,
 //               p14 specularSample, p15 clearcoatSample; aux = diffuseReflectSample
+//  perfect_mirror: p0..2 reflectance, p3..5 eta, p6..8 k
+//  perfect_glass:  p0..2 R, p3..5 T, p6 eta
+//  plastic, rough_plastic: p0..2 diffuse, p3..5 specular, p6 eta, p7 1/eta^2, p8 internal diffuse
+//               Fresnel reflectance, p9..12 microfacet (rough_plastic), p13 specular sampling
+//               weight, p14 no_linear
 //  two_side:    ref0 outside material index, ref1 inside material index
+//  mask:        p0 opacity clamped to [0, 1], ref0 nested material index
 struct alignas(16) MatRec {
   uint32_t kind;
   uint32_t flags;      // BsdfType bits of the instance
   uint32_t dflags;     // Disney present flags
-  uint32_t ref0, ref1; // two_side children
+  uint32_t ref0, ref1; // two_side / mask children
   float aux;           // disney: diffuse_reflectance_sampling_rate
   uint32_t pad[2];
   float p[16];
 };
 static_assert(sizeof(MatRec) == 96, "MatRec must stay 96 bytes");
+// Deepest chain of wrapper BSDFs (two_side, mask) above a leaf BSDF.
+constexpr int kMaxBsdfNest = 4;
 
 // ---------------------------------------------------------------- shapes
 enum ShapeKind : uint32_t { SHAPE_MESH = 0, SHAPE_RECT = 1, SHAPE_SPHERE = 2 };

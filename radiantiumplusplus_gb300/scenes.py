@@ -71,6 +71,26 @@ def box_room(width=256, height=256, spp=64, seed=1, max_depth=8, rr_depth=3):
     }
 
 
+
+def materials_room(width=256, height=256, spp=64, seed=1, max_depth=8, rr_depth=3):
+    """Box room with the delta and layered BSDFs: plastic floor, rough_plastic back
+    wall, a perfect_mirror sphere, a perfect_glass sphere, a masked diffuse box and a
+    two-sided plastic / rough_plastic ceiling panel."""
+    sc = box_room(width, height, spp, seed, max_depth, rr_depth)
+    ents = sc["scene"]
+    ents[0]["bsdf"] = {"type": "plastic", "diffuse": [0.55, 0.5, 0.45], "int_ior": 1.5}
+    ents[2]["bsdf"] = {"type": "rough_plastic", "diffuse": [0.3, 0.4, 0.6], "alpha": 0.15}
+    ents[5]["bsdf"] = {"type": "mask", "opacity": 0.6,
+                       "nested": {"type": "diffuse", "reflectance": [0.8, 0.8, 0.8]}}
+    ents[6]["bsdf"] = {"type": "two_side", "out_side": {"type": "plastic", "no_linear": True},
+                       "in_side": {"type": "rough_plastic", "alpha": 0.3, "distribution": "beckmann"}}
+    ents.append({"shape": {"type": "sphere", "center": [0.45, 0.85, 0.35], "radius": 0.25},
+                 "bsdf": {"type": "perfect_mirror", "reflectance": [0.95, 0.95, 0.95],
+                          "eta": [0.2, 0.92, 1.1], "k": [3.9, 2.45, 2.14]}})
+    ents.append({"shape": {"type": "sphere", "center": [-0.4, 0.35, 0.45], "radius": 0.3},
+                 "bsdf": {"type": "perfect_glass", "int_ior": 1.5}})
+    return sc
+
 def icosphere(subdiv=2):
     """Unit icosphere: (positions, triangles) with outward counter-clockwise winding."""
     t = (1.0 + 5.0 ** 0.5) / 2.0

@@ -23,6 +23,10 @@ def spheres(dirpath, n=300, emitters=5, w=96, h=64, spp=4):
     return write(dirpath, "spheres_%d_%dx%d" % (n, w, h), sc, assets)
 
 
+def materials(dirpath, w=48, h=48, spp=4, seed=1):
+    return write(dirpath, "materials_%dx%d_%d_%d" % (w, h, spp, seed), scenes.materials_room(w, h, spp, seed))
+
+
 def volume(dirpath, w=48, h=48, spp=4, grid=32, max_depth=32):
     sc, assets = scenes.volume_box(width=w, height=h, spp=spp, grid=grid, max_depth=max_depth)
     return write(dirpath, "vol_%dx%d_%d" % (w, h, grid), sc, assets)
@@ -48,6 +52,20 @@ BSDFS = [
     {"type": "disney", "base_color": [0.5, 0.5, 0.5], "roughness": 0.7},
     {"type": "disney", "base_color": [0.9, 0.8, 0.1], "roughness": 0.2, "metallic": 1.0, "specular": 0.8},
     {"type": "two_side", "two_side": {"type": "rough_metal", "alpha": 0.3}},
+    {"type": "perfect_mirror"},
+    {"type": "perfect_mirror", "reflectance": [0.9, 0.7, 0.5], "eta": [0.2, 0.92, 1.1], "k": [3.9, 2.45, 2.14]},
+    {"type": "perfect_glass"},
+    {"type": "perfect_glass", "int_ior": 1.33, "ext_ior": 1.0, "reflectance": [0.9, 0.8, 0.7],
+     "transmittance": [0.6, 0.8, 1.0]},
+    {"type": "plastic", "diffuse": [0.2, 0.5, 0.8]},
+    {"type": "plastic", "diffuse": [0.6, 0.3, 0.1], "specular": 0.5, "no_linear": True, "int_ior": 1.6},
+    {"type": "rough_plastic", "diffuse": [0.2, 0.5, 0.8], "alpha": 0.2},
+    {"type": "rough_plastic", "alpha": 0.3, "distribution": "beckmann", "no_linear": True},
+    {"type": "rough_plastic", "alpha": 0.15, "sample_visible": False},
+    {"type": "mask", "opacity": 0.4, "nested": {"type": "rough_metal", "alpha": 0.2}},
+    {"type": "mask", "opacity": 0.7, "nested": {"type": "two_side", "two_side": {"type": "plastic"}}},
+    {"type": "two_side", "out_side": {"type": "mask", "opacity": 0.5, "nested": {"type": "diffuse"}},
+     "in_side": {"type": "perfect_glass"}},
 ]
 
 

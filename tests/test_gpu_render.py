@@ -10,7 +10,7 @@ relative (absolute floor 1e-4), and the mean over all samples within 2%.
 import numpy as np
 import pytest
 
-from helpers import box, spheres, volume
+from helpers import box, materials, spheres, volume
 
 pytestmark = pytest.mark.gpu
 
@@ -34,6 +34,15 @@ def test_path_samples_box(rad, oracle, scene_dir):
     path, text, d = box(scene_dir, 48, 48, 4)
     g, o = rad.Scene.from_file(path), oracle.OracleScene(text, d)
     frac, _, _ = _sample_parity(g, o, 4, 0.98)
+    g.close()
+
+
+def test_path_samples_materials(rad, oracle, scene_dir):
+    """Delta BSDFs (mirror, glass, plastic's specular lobe), mask pass-through and
+    two-sided layered materials in one room."""
+    path, text, d = materials(scene_dir, 48, 48, 4)
+    g, o = rad.Scene.from_file(path), oracle.OracleScene(text, d)
+    _sample_parity(g, o, 4, 0.97)
     g.close()
 
 

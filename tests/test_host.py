@@ -4,7 +4,7 @@ import os
 
 import numpy as np
 
-from helpers import box, spheres, volume
+from helpers import box, materials, spheres, volume
 from radiantiumplusplus_gb300 import exr, scenes
 
 
@@ -28,7 +28,8 @@ def test_icosphere_counts_and_winding():
 
 
 def test_generated_scenes_load_in_oracle(oracle, scene_dir):
-    for path, text, d in (box(scene_dir), spheres(scene_dir, 50, 3), volume(scene_dir, 16, 16, 1, grid=16)):
+    for path, text, d in (box(scene_dir), spheres(scene_dir, 50, 3), volume(scene_dir, 16, 16, 1, grid=16),
+                          materials(scene_dir, 16, 16, 1)):
         o = oracle.OracleScene(text, d)
         assert o.width > 0 and o.n_prims > 0
         o.close()

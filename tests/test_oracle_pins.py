@@ -55,9 +55,10 @@ def test_microfacet_normalisation(oracle, ggx, alpha):
     assert abs(total - 1.0) < 0.03
 
 
-@pytest.mark.parametrize("bsdf", BSDFS[:8], ids=lambda b: b["type"])
+@pytest.mark.parametrize("bsdf", BSDFS, ids=lambda b: b["type"] + "_" + str(abs(hash(bsdf_json(b))) % 1000))
 def test_sample_matches_eval_and_pdf(oracle, bsdf):
-    """Sample() returns f and pdf consistent with Eval()/Pdf() at the sampled direction."""
+    """Sample() returns f and pdf consistent with Eval()/Pdf() at the sampled direction
+    (for the lobes that have a density: delta lobes and mask pass-through do not)."""
     rng = np.random.default_rng(5)
     n = 4096
     wi = directions(rng, n)
@@ -65,7 +66,7 @@ def test_sample_matches_eval_and_pdf(oracle, bsdf):
     u = rng.uniform(size=(n, 3)).astype(np.float32)
     js = bsdf_json(bsdf)
     wo, pdf, f, eta, typ = oracle.bsdf_sample(js, wi, u)
-    ok = pdf > 0
+    ok = (pdf > 0) & ((typ & (4 | 32)) == 0)
     f2, pdf2 = oracle.bsdf_eval(js, wi[ok], wo[ok])
     assert np.allclose(pdf[ok], pdf2, rtol=2e-3, atol=1e-6)
     assert np.allclose(f[ok], f2, rtol=2e-3, atol=1e-6)
@@ -86,7 +87,7 @@ def test_pdf_integrates_to_at_most_one(oracle):
     rng = np.random.default_rng(3)
     n = 200000
     wo = directions(rng, n)
-    for b in BSDFS[:8]:
+    for b in BSDFS:
         wi = np.tile(np.array([[0.2, -0.3, 0.932738]], np.float32), (n, 1))
         _, pdf = oracle.bsdf_eval(bsdf_json(b), wi, wo)
         integral = pdf.mean() * 4 * math.pi
@@ -129,3 +130,99 @@ def test_box_room_energy_is_plausible(oracle, scene_dir):
     m = film.mean(axis=(0, 1))
     assert 0.05 < m[0] < 1.0 and m[0] > m[2]  # warm emitter: red dominates blue
     assert stats[2] == 32 * 32 * 16
+
+
+def _fresnel_dielectric(c, eta):
+    """Unpolarised dielectric Fresnel reflectance for light arriving from outside (numpy)."""
+    c = np.asarray(c, np.float64)
+    st2 = (1 - c * c) / eta ** 2
+    ct = np.sqrt(np.maximum(0, 1 - st2))
+    rs = (c - eta * ct) / (c + eta * ct)
+    rp = (eta * c - ct) / (eta * c + ct)
+    r = 0.5 * (rs ** 2 + rp ** 2)
+    return np.where(st2 >= 1, 1.0, r)
+
+
+def test_perfect_mirror_closed_forms(oracle):
+    """Mirror direction, unit pdf; f = R * F with F = 1 for the default purely imaginary
+    index (eta 0, k 1) and ((n-1)^2+k^2)/((n+1)^2+k^2) at normal incidence."""
+    rng = np.random.default_rng(8)
+    wi = directions(rng, 512)
+    wi[:, 2] = np.abs(wi[:, 2]) + 1e-3
+    wi /= np.linalg.norm(wi, axis=1, keepdims=True)
+    u = rng.uniform(size=(512, 3)).astype(np.float32)
+    wo, pdf, f, _, typ = oracle.bsdf_sample('{"type":"perfect_mirror","reflectance":[0.9,0.7,0.5]}', wi, u)
+    assert np.allclose(wo, wi * np.array([-1, -1, 1], np.float32))
+    assert (pdf == 1).all() and (typ == (4 | 8)).all()
+    assert np.allclose(f, [0.9, 0.7, 0.5], rtol=1e-5)
+    n, k = np.array([0.2, 0.92, 1.1]), np.array([3.9, 2.45, 2.14])
+    js = json.dumps({"type": "perfect_mirror", "eta": n.tolist(), "k": k.tolist()})
+    _, _, f, _, _ = oracle.bsdf_sample(js, np.array([[0, 0, 1]], np.float32), u[:1])
+    assert np.allclose(f[0], ((n - 1) ** 2 + k ** 2) / ((n + 1) ** 2 + k ** 2), rtol=1e-5)
+    f, p = oracle.bsdf_eval(js, wi, directions(rng, 512))
+    assert (f == 0).all() and (p == 0).all()
+
+
+def test_perfect_glass_fresnel_and_snell(oracle):
+    """Reflection is chosen with probability F (numpy closed form), the refracted
+    direction obeys Snell's law, and f / pdf is 1 (reflection) or 1 / eta^2 (refraction)."""
+    rng = np.random.default_rng(9)
+    n = 4096
+    wi = directions(rng, n)
+    wi[:, 2] = np.abs(wi[:, 2]) + 1e-3
+    wi /= np.linalg.norm(wi, axis=1, keepdims=True)
+    u = rng.uniform(size=(n, 3)).astype(np.float32)
+    eta = 1.5 / 1.0
+    wo, pdf, f, e, typ = oracle.bsdf_sample('{"type":"perfect_glass","int_ior":1.5,"ext_ior":1.0}', wi, u)
+    F = _fresnel_dielectric(wi[:, 2], eta)
+    refl = (typ & 8) != 0
+    assert np.mean(refl == (u[:, 0] <= F)) > 0.999
+    assert np.allclose(pdf[refl], F[refl], rtol=1e-4)
+    assert np.allclose(pdf[~refl], 1 - F[~refl], rtol=1e-4, atol=1e-6)
+    sin_i = np.hypot(wi[~refl, 0], wi[~refl, 1])
+    sin_t = np.hypot(wo[~refl, 0], wo[~refl, 1])
+    assert np.allclose(sin_t, sin_i / eta, atol=1e-5) and (wo[~refl, 2] < 0).all()
+    assert np.allclose(f[refl, 0] / pdf[refl], 1.0, rtol=1e-5)
+    assert np.allclose(f[~refl, 0] / pdf[~refl], 1 / eta ** 2, rtol=1e-5)
+    assert np.allclose(e[~refl], eta, rtol=1e-6) and (e[refl] == 1).all()
+
+
+def test_plastic_diffuse_lobe_closed_form(oracle):
+    """plastic Eval = R / pi * (1 - F(wi)) (1 - F(wo)) cos(wo) / (eta^2 (1 - Fdr)), with the
+    internal diffuse Fresnel reflectance Fdr integrated numerically (the reference's
+    polynomial fit agrees within 0.2%)."""
+    rng = np.random.default_rng(10)
+    wi, wo = directions(rng, 2048), directions(rng, 2048)
+    wi[:, 2] = np.abs(wi[:, 2]) + 1e-3
+    wo[:, 2] = np.abs(wo[:, 2]) + 1e-3
+    wi /= np.linalg.norm(wi, axis=1, keepdims=True)
+    wo /= np.linalg.norm(wo, axis=1, keepdims=True)
+    eta = 1.49 / 1.000277
+    th = np.linspace(0, np.pi / 2, 200001)
+    fdr = np.trapezoid(_fresnel_dielectric(np.cos(th), 1 / eta) * 2 * np.sin(th) * np.cos(th), th)
+    R = np.array([0.2, 0.5, 0.8])
+    f, pdf = oracle.bsdf_eval(json.dumps({"type": "plastic", "diffuse": R.tolist()}), wi, wo)
+    fi, fo = _fresnel_dielectric(wi[:, 2], eta), _fresnel_dielectric(wo[:, 2], eta)
+    want = R[None] / np.pi * ((1 - fi) * (1 - fo) * wo[:, 2] / (eta ** 2 * (1 - fdr)))[:, None]
+    assert np.allclose(f, want, rtol=2e-3)
+    w = 1.0 / (1.0 + (R @ [0.212671, 0.715160, 0.072169]))  # specular share of the mean luminance
+    pd = (1 - fi) * (1 - w)
+    assert np.allclose(pdf, wo[:, 2] / np.pi * pd / (pd + fi * w), rtol=1e-4)
+
+
+def test_mask_pass_through(oracle):
+    """mask: lobeXi >= opacity passes the ray through (Null, pdf 1 - opacity, f 1); otherwise
+    the nested BSDF scaled by the opacity; Eval and Pdf scale by the opacity."""
+    rng = np.random.default_rng(12)
+    n = 2048
+    wi = directions(rng, n)
+    u = rng.uniform(size=(n, 3)).astype(np.float32)
+    js = '{"type":"mask","opacity":0.35,"nested":{"type":"diffuse","reflectance":0.8}}'
+    wo, pdf, f, _, typ = oracle.bsdf_sample(js, wi, u)
+    through = u[:, 0] >= np.float32(0.35)
+    assert (typ[through] == 32).all() and np.allclose(wo[through], -wi[through])
+    assert np.allclose(pdf[through], 0.65) and (f[through] == 1).all()
+    wo2 = directions(rng, n)
+    f1, p1 = oracle.bsdf_eval(js, wi, wo2)
+    f0, p0 = oracle.bsdf_eval('{"type":"diffuse","reflectance":0.8}', wi, wo2)
+    assert np.allclose(f1, f0 * np.float32(0.35), rtol=1e-6) and np.allclose(p1, p0 * np.float32(0.35), rtol=1e-6)
