@@ -865,6 +865,33 @@ std::unique_ptr<Scene> Scene::FromJson(const std::string& text, const std::strin
       } else if (type == "skybox") {
         L.kind = Light::Skybox;
         L.radiance = color("radiance", V3(1));
+      } else if (type == "point") {  // point.cpp:19-26
+        L.kind = Light::Point;
+        L.worldPos = L.toWorld.ApplyAffineToWorld(ReadV3(ln, "position", V3(0, 0, 0)));
+        L.radiance = ReadV3(ln, "intensity", V3(1, 1, 1));
+      } else if (type == "projection") {  // projection.cpp:19-45
+        L.kind = Light::Projection;
+        L.radiance = color("irradiance", V3(1));
+        L.scale = ReadV3(ln, "scale", V3(1, 1, 1));
+        Float fov = ReadF(ln, "fov", Float(90));
+        Float aspect = 1 / (Float)1;  // Width / Height of a constant texture
+        Float farZ = 10000;
+        Float nearZ = Float(0.0001);
+        Float recip = 1 / (farZ - nearZ);
+        Float cot = 1 / std::tan(Radian(fov / 2));
+        M4 persp{}, scale{}, translate = M4::Identity();
+        persp.m[0][0] = cot;
+        persp.m[1][1] = cot;
+        persp.m[2][2] = farZ * recip;
+        persp.m[2][3] = -nearZ * farZ * recip;
+        persp.m[3][2] = 1;
+        scale.m[0][0] = -Float(0.5);
+        scale.m[1][1] = -Float(0.5) * aspect;
+        scale.m[2][2] = 1;
+        scale.m[3][3] = 1;
+        translate.m[0][3] = -1;
+        translate.m[1][3] = -1 / aspect;
+        L.toClip = Transform(scale * translate * persp);
       } else if (type == "directional") {
         L.kind = Light::Directional;
         L.radiance = color("irradiance", V3(1));
@@ -1391,7 +1418,8 @@ Spectrum Scene::EvalLight(int l, const SurfaceInteraction& si) const {
   return Spectrum(0);
 }
 
-// scene.cpp:87-96 with area.cpp:47-75, skybox.cpp:65-86 and the directional extension
+// scene.cpp:87-96 with area.cpp:47-75, skybox.cpp:65-86, point.cpp:33-49,
+// projection.cpp:52-74 and the directional extension
 std::pair<DirectionSample, Spectrum> Scene::SampleLightDirection(const V3& refP, Float xiL, const V2& xi) const {
   int index;
   Float pdf;
@@ -1415,6 +1443,32 @@ std::pair<DirectionSample, Spectrum> Scene::SampleLightDirection(const V3& refP,
     dsr.Dist = dist;
     dsr.IsDelta = false;
     li = L.radiance;
+  } else if (L.kind == Light::Point) {  // point.cpp:33-49
+    dsr.P = L.worldPos;
+    dsr.N = V3(0);
+    dsr.Pdf = 1;
+    dsr.IsDelta = true;
+    dsr.Dir = dsr.P - refP;
+    Float dist2 = sqnorm(dsr.Dir);
+    dsr.Dist = std::sqrt(dist2);
+    Float invDist = Rcp(dsr.Dist);
+    dsr.Dir = dsr.Dir * invDist;
+    li = L.radiance * Sqr(invDist);
+  } else if (L.kind == Light::Projection) {  // projection.cpp:52-74
+    V3 local = L.toWorld.ApplyAffineToLocal(refP);
+    V3 c = L.toClip.ApplyAffineToWorld(local);
+    bool inRange = c.x >= 0 && c.x <= 1 && c.y >= 0 && c.y <= 1 && local.z > 0;
+    if (inRange) {
+      dsr.P = V3(L.toWorld.ToWorld.m[0][3], L.toWorld.ToWorld.m[1][3], L.toWorld.ToWorld.m[2][3]);
+      dsr.N = normalized(L.toWorld.ApplyLinearToWorld(V3(0, 0, 1)));
+      dsr.Pdf = 1;
+      dsr.IsDelta = true;
+      dsr.Dir = dsr.P - refP;
+      Float squaredNorm = sqnorm(dsr.Dir);
+      dsr.Dist = std::sqrt(squaredNorm);
+      dsr.Dir = dsr.Dir * Rcp(dsr.Dist);
+      li = cmul(L.radiance, L.scale) * PI / (Sqr(local.z) * dot(-dsr.Dir, dsr.N));
+    }
   } else {
     Float radius = std::max(L.worldRadius, norm(refP - L.worldCenter));
     Float dist = 2 * radius;

@@ -102,15 +102,19 @@ struct Shape {
 };
 
 struct Light {
-  enum Kind { Area, Skybox, Directional } kind = Area;
+  enum Kind { Area, Skybox, Directional, Point, Projection } kind = Area;
   int shape = -1;
-  Spectrum radiance;  // area radiance, skybox constant radiance, directional irradiance
+  Spectrum radiance;  // area radiance, skybox constant radiance, directional irradiance,
+                      // point intensity, projection irradiance (constant texture)
   Transform toWorld;
   V3 direction;  // directional: world direction the light travels
+  V3 worldPos;   // point: world position (point.cpp:22-23)
+  Spectrum scale;      // projection: irradiance scale
+  Transform toClip;    // projection: light space -> [0,1]^2 image plane (projection.cpp:27-41)
   V3 worldCenter;
   Float worldRadius = 0;
   bool IsEnv() const { return kind == Skybox; }
-  bool IsDelta() const { return kind == Directional; }
+  bool IsDelta() const { return kind == Directional || kind == Point || kind == Projection; }
 };
 
 struct Medium {

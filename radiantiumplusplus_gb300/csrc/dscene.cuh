@@ -245,6 +245,30 @@ RD DirSample SampleLightDirection(const DevScene& S, V3 refP, float xiL, V2 xi, 
   if (L.kind == LIGHT_AREA) {
     d = ShapeSampleDirection(S, S.shapes[L.shape], refP, xi);
     li = dot(-d.Dir, d.N) >= 0.f ? rad : v3s(0.f);
+  } else if (L.kind == LIGHT_POINT) {  // point.cpp:33-49
+    d.P = V3{L.dir[0], L.dir[1], L.dir[2]};
+    d.N = v3s(0.f);
+    d.Pdf = 1.f;
+    d.IsDelta = true;
+    V3 dir = d.P - refP;
+    d.Dist = sqrtf(sqnorm(dir));
+    float invDist = Rcp(d.Dist);
+    d.Dir = dir * invDist;
+    li = rad * Sqr(invDist);
+  } else if (L.kind == LIGHT_PROJECTION) {  // projection.cpp:52-74 (constant irradiance)
+    V3 local = Affine4(L.m, refP);
+    V3 uv = Affine4(L.m + 16, local);
+    bool inRange = uv.x >= 0.f && uv.x <= 1.f && uv.y >= 0.f && uv.y <= 1.f && local.z > 0.f;
+    if (!inRange) return d;  // Pdf 0: no light sample
+    d.P = V3{L.dir[0], L.dir[1], L.dir[2]};
+    d.N = ld3(L.m + 32);
+    d.Pdf = 1.f;
+    d.IsDelta = true;
+    V3 dir = d.P - refP;
+    d.Dist = sqrtf(sqnorm(dir));
+    d.Dir = dir * Rcp(d.Dist);
+    float den = Sqr(local.z) * dot(-d.Dir, d.N);
+    li = V3{(rad.x * kPi) / den, (rad.y * kPi) / den, (rad.z * kPi) / den};
   } else {
     V3 wc{L.world[0], L.world[1], L.world[2]};
     float radius = fmaxr(L.world[3], norm(refP - wc));
@@ -284,7 +308,8 @@ RD float PdfLightDirection(const DevScene& S, int light, V3 refP, V3 dir, V3 n, 
   return p * S.lightPdf;
 }
 
-// area.cpp:42-45 / skybox.cpp:53-63 (constant radiance)
+// area.cpp:42-45 / skybox.cpp:53-63 (constant radiance); point and projection
+// lights have no surface to hit and evaluate to 0 (point.cpp:29-31, projection.cpp:48-50).
 RD V3 EvalLightAt(const DevScene& S, int light, const SurfInt* si) {
   const LightRec& L = S.lights[light];
   V3 rad{L.radiance[0], L.radiance[1], L.radiance[2]};

@@ -949,6 +949,49 @@ void BuildHostScene(const std::string& json, const std::string& baseDir, HostSce
         L.kind = LIGHT_SKYBOX;
         rad = col("radiance", F3(1, 1, 1));
         RowsOf(t.w, L.lin);
+      } else if (type == "point") {  // point.cpp:19-26
+        L.kind = LIGHT_POINT;
+        F3 p = t.AffW(RV(ln, "position", F3(0, 0, 0)));
+        L.dir[0] = p.x;
+        L.dir[1] = p.y;
+        L.dir[2] = p.z;
+        rad = RV(ln, "intensity", F3(1, 1, 1));
+      } else if (type == "projection") {  // projection.cpp:19-45 (constant irradiance: a 1x1 texture)
+        L.kind = LIGHT_PROJECTION;
+        F3 irr = col("irradiance", F3(1, 1, 1));
+        F3 sc = RV(ln, "scale", F3(1, 1, 1));
+        rad = F3(irr.x * sc.x, irr.y * sc.y, irr.z * sc.z);  // irradiance.cwiseProduct(scale)
+        float fov = RF(ln, "fov", 90.f);
+        float aspect = 1 / (float)1;
+        float farZ = 10000, nearZ = 0.0001f;
+        M4f persp{}, scale{}, translate = M4f::Identity();
+        std::memset(&persp, 0, sizeof(persp));
+        std::memset(&scale, 0, sizeof(scale));
+        float recip = 1 / (farZ - nearZ);
+        float cot = 1 / std::tan((fov / 2) * (kPiF / 180.f));
+        persp.m[0][0] = cot;
+        persp.m[1][1] = cot;
+        persp.m[2][2] = farZ * recip;
+        persp.m[2][3] = -nearZ * farZ * recip;
+        persp.m[3][2] = 1;
+        scale.m[0][0] = -0.5f;
+        scale.m[1][1] = -0.5f * aspect;
+        scale.m[2][2] = 1;
+        scale.m[3][3] = 1;
+        translate.m[0][3] = -1;
+        translate.m[1][3] = -1 / aspect;
+        M4f toClip = scale * translate * persp;
+        for (int i = 0; i < 16; i++) {
+          L.m[i] = t.l.m[i / 4][i % 4];
+          L.m[16 + i] = toClip.m[i / 4][i % 4];
+        }
+        L.dir[0] = t.w.m[0][3];  // TranslationToWorld
+        L.dir[1] = t.w.m[1][3];
+        L.dir[2] = t.w.m[2][3];
+        F3 n = Normalize(t.LinW(F3(0, 0, 1)));
+        L.m[32] = n.x;
+        L.m[33] = n.y;
+        L.m[34] = n.z;
       } else if (type == "directional") {  // extension: no reference factory
         L.kind = LIGHT_DIRECTIONAL;
         rad = col("irradiance", F3(1, 1, 1));

@@ -73,17 +73,21 @@ struct alignas(16) ShapeRec {
 static_assert(sizeof(ShapeRec) == 208, "ShapeRec size");
 
 // ---------------------------------------------------------------- lights
-enum LightKind : uint32_t { LIGHT_AREA = 0, LIGHT_SKYBOX = 1, LIGHT_DIRECTIONAL = 2 };
+enum LightKind : uint32_t { LIGHT_AREA = 0, LIGHT_SKYBOX = 1, LIGHT_DIRECTIONAL = 2, LIGHT_POINT = 3,
+                            LIGHT_PROJECTION = 4 };
 struct alignas(16) LightRec {
   uint32_t kind;
   int32_t shape;
   uint32_t pad[2];
-  float radiance[4];   // rgb (area radiance, sky radiance, directional irradiance)
-  float dir[4];        // directional: world direction the light travels
+  float radiance[4];   // rgb: area radiance, sky radiance, directional irradiance, point intensity,
+                       // projection irradiance x scale
+  float dir[4];        // directional: world direction the light travels; point / projection: world position
   float world[4];      // world bounding sphere center xyz, radius w (skybox.cpp:139-144)
   float lin[12];       // skybox toWorld linear part, rows of 4
+  float m[36];         // projection: world -> light 4x4 (m[0..15]), light -> clip 4x4 (m[16..31]),
+                       // world-space normal (m[32..34])
 };
-static_assert(sizeof(LightRec) == 112, "LightRec size");
+static_assert(sizeof(LightRec) == 256, "LightRec size");
 
 // ---------------------------------------------------------------- media
 enum MediumKind : uint32_t { MED_HOMOGENEOUS = 0, MED_HETEROGENEOUS = 1 };

@@ -91,6 +91,19 @@ def materials_room(width=256, height=256, spp=64, seed=1, max_depth=8, rr_depth=
                  "bsdf": {"type": "perfect_glass", "int_ior": 1.5}})
     return sc
 
+
+def lights_room(width=256, height=256, spp=64, seed=1, max_depth=8, rr_depth=3):
+    """Box room lit by a point light, a projection light shining onto the back wall
+    and a dimmed area light (delta lights next to an MIS-weighted emitter)."""
+    sc = box_room(width, height, spp, seed, max_depth, rr_depth)
+    ents = sc["scene"]
+    ents[-1]["light"]["radiance"] = [4.0, 3.0, 1.0]
+    ents.append({"light": {"type": "point", "position": [0.3, 1.6, 0.2], "intensity": [1.5, 1.3, 1.0]}})
+    ents.append({"to_world": {"translate": [0.2, 1.3, 2.2], "rotate": {"axis": [0, 1, 0], "angle": 180.0}},
+                 "light": {"type": "projection", "fov": 28.0, "irradiance": [2.0, 1.6, 1.2],
+                           "scale": [1.0, 0.8, 1.2]}})
+    return sc
+
 def icosphere(subdiv=2):
     """Unit icosphere: (positions, triangles) with outward counter-clockwise winding."""
     t = (1.0 + 5.0 ** 0.5) / 2.0

@@ -27,6 +27,10 @@ def materials(dirpath, w=48, h=48, spp=4, seed=1):
     return write(dirpath, "materials_%dx%d_%d_%d" % (w, h, spp, seed), scenes.materials_room(w, h, spp, seed))
 
 
+def lights(dirpath, w=48, h=48, spp=4, seed=1):
+    return write(dirpath, "lights_%dx%d_%d_%d" % (w, h, spp, seed), scenes.lights_room(w, h, spp, seed))
+
+
 def volume(dirpath, w=48, h=48, spp=4, grid=32, max_depth=32):
     sc, assets = scenes.volume_box(width=w, height=h, spp=spp, grid=grid, max_depth=max_depth)
     return write(dirpath, "vol_%dx%d_%d" % (w, h, grid), sc, assets)

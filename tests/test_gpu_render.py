@@ -7,10 +7,12 @@ oracle uses glibc's, so a path can diverge when a Russian-roulette or lobe
 decision sits on a 1-ulp boundary. Required: >= 97% of samples within 1e-3
 relative (absolute floor 1e-4), and the mean over all samples within 2%.
 """
+
 import numpy as np
 import pytest
 
-from helpers import box, materials, spheres, volume
+from helpers import box, lights, materials, spheres, volume, write
+from radiantiumplusplus_gb300 import scenes
 
 pytestmark = pytest.mark.gpu
 
@@ -55,6 +57,28 @@ def test_path_samples_spheres(rad, oracle, scene_dir):
 
 def test_volpath_samples(rad, oracle, scene_dir):
     path, text, d = volume(scene_dir, 32, 32, 2, grid=24)
+    g, o = rad.Scene.from_file(path), oracle.OracleScene(text, d)
+    _sample_parity(g, o, 2, 0.93)
+    g.close()
+
+
+def test_path_samples_lights(rad, oracle, scene_dir):
+    """Point and projection lights (delta lights: no MIS weight on their samples) beside
+    an area emitter."""
+    path, text, d = lights(scene_dir, 48, 48, 4)
+    g, o = rad.Scene.from_file(path), oracle.OracleScene(text, d)
+    _sample_parity(g, o, 4, 0.97)
+    g.close()
+
+
+def test_volpath_samples_point_light(rad, oracle, scene_dir):
+    """vol_path with a point light and a projection light in place of the distant light:
+    their samples are attenuated through the medium like any other."""
+    sc, assets = scenes.volume_box(width=32, height=32, spp=2, grid=24)
+    sc["scene"][2] = {"light": {"type": "point", "position": [1.5, 3.0, 1.0], "intensity": [30.0, 30.0, 30.0]}}
+    sc["scene"].append({"to_world": {"translate": [0.0, 1.0, 3.0], "rotate": {"axis": [0, 1, 0], "angle": 180.0}},
+                        "light": {"type": "projection", "fov": 30.0, "irradiance": [4.0, 3.0, 2.0]}})
+    path, text, d = write(scene_dir, "vol_point_32", sc, assets)
     g, o = rad.Scene.from_file(path), oracle.OracleScene(text, d)
     _sample_parity(g, o, 2, 0.93)
     g.close()

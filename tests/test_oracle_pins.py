@@ -226,3 +226,62 @@ def test_mask_pass_through(oracle):
     f1, p1 = oracle.bsdf_eval(js, wi, wo2)
     f0, p0 = oracle.bsdf_eval('{"type":"diffuse","reflectance":0.8}', wi, wo2)
     assert np.allclose(f1, f0 * np.float32(0.35), rtol=1e-6) and np.allclose(p1, p0 * np.float32(0.35), rtol=1e-6)
+
+
+def _direct_light_scene(light_entity, res=48):
+    """Camera looking straight down at a large Lambertian plane (y = 0, reflectance
+    0.5); max_depth 2 keeps only the light sample at the first hit."""
+    return {
+        "camera": {"type": "perspective", "fov": 60.0, "resolution": [res, res],
+                   "origin": [0.0, 6.0, 0.0], "target": [0.0, 0.0, 0.0], "up": [0.0, 0.0, -1.0]},
+        "sampler": {"type": "independent", "sample_count": 1, "seed": 4},
+        "scene": [{"to_world": {"rotate": {"axis": [1, 0, 0], "angle": -90.0}, "scale": [20, 20, 1]},
+                   "shape": {"type": "rectangle"}, "bsdf": {"type": "diffuse", "reflectance": 0.5}},
+                  light_entity],
+        "accel": {"type": "embree"},
+        "renderer": {"type": "path", "max_depth": 2, "rr_depth": 8},
+    }
+
+
+def _plane_hits(o, n):
+    r = o.camera_rays(np.arange(n, dtype=np.uint32), 0).astype(np.float64)
+    t = -r[:, 1] / r[:, 5]
+    return r[:, :3] + t[:, None] * r[:, 4:7]
+
+
+def test_point_light_direct_closed_form(oracle):
+    """A point light of intensity I at height h over a Lambertian plane: the first-hit
+    radiance is R / pi * I * cos(theta) / d^2 (inverse-square falloff, point.cpp:33-49)."""
+    I = np.array([2.0, 1.0, 0.5])
+    sc = _direct_light_scene({"light": {"type": "point", "position": [0.5, 2.0, -0.3], "intensity": I.tolist()}})
+    o = oracle.OracleScene(json.dumps(sc), "")
+    n = o.width * o.height
+    L = o.render_samples(np.arange(n, dtype=np.uint32), np.zeros(n, np.uint32))
+    P = _plane_hits(o, n)
+    d = np.array([0.5, 2.0, -0.3]) - P
+    d2 = (d * d).sum(1)
+    want = 0.5 / np.pi * I[None] * (d[:, 1] / np.sqrt(d2) / d2)[:, None]
+    assert np.allclose(L, want, rtol=1e-4)
+    o.close()
+
+
+def test_projection_light_footprint(oracle):
+    """A projection light at height h aimed straight down lights the square
+    |x|, |z| <= h tan(fov / 2) of the plane; inside it the first-hit radiance is the
+    constant R * E / h^2 (the cos(theta) / cos(alpha) of projection.cpp:70-72 cancel on a
+    plane facing the light), outside it is 0."""
+    h, fov = 2.0, 40.0
+    E = np.array([3.0, 2.0, 1.0])
+    sc = _direct_light_scene({"to_world": {"translate": [0, h, 0], "rotate": {"axis": [1, 0, 0], "angle": 90.0}},
+                              "light": {"type": "projection", "fov": fov, "irradiance": E.tolist()}})
+    o = oracle.OracleScene(json.dumps(sc), "")
+    n = o.width * o.height
+    L = o.render_samples(np.arange(n, dtype=np.uint32), np.zeros(n, np.uint32))
+    P = _plane_hits(o, n)
+    half = h * math.tan(math.radians(fov / 2))
+    inside = (np.abs(P[:, 0]) < half * 0.98) & (np.abs(P[:, 2]) < half * 0.98)
+    outside = (np.abs(P[:, 0]) > half * 1.02) | (np.abs(P[:, 2]) > half * 1.02)
+    assert inside.sum() > 50 and outside.sum() > 50
+    assert np.allclose(L[inside], 0.5 * E[None] / h ** 2, rtol=1e-4)
+    assert (L[outside] == 0).all()
+    o.close()
