@@ -162,6 +162,13 @@ RAD_API int rad_bsdf_sample_batch(const char* bsdf_json, const float* wi, const 
  * each sample's own stream. pixels: n (x + y * width); out: n x 8 rays. */
 RAD_API int rad_camera_rays(rad_scene* scene, const uint32_t* pixels, int64_t n, uint32_t sample, uint32_t seed,
                             float* rays);
+/* Texture<T>::Eval (texture.h:57-62) of the scene's texture number `texture`
+ * (textures are numbered in the order the scene file creates them: BSDF
+ * parameters in each factory's reading order, a chessboard before its two
+ * children). uv: n x 2; duv: n x 4 (du/dx, dv/dx, du/dy, dv/dy); out: n x 3
+ * (mono textures fill the first column). Host memory. */
+RAD_API int rad_scene_texture_eval(rad_scene* scene, uint32_t texture, const float* uv, const float* duv, int64_t n,
+                                   float* out);
 /* Radiance of individual pixel samples (Li), n x 3, through the same kernels
  * as a job. */
 RAD_API int rad_render_samples(rad_scene* scene, const uint32_t* pixels, const uint32_t* samples, int64_t n,

@@ -259,41 +259,46 @@ std::pair<V3, Float> Microfacet::Sample(const V3& wi, const V2& xi) const {
 }
 
 // ----------------------------------------------------------------- helpers
-static Spectrum ReadColor(const Json* cfg, const char* k, const Spectrum& def) {
-  const Json* j = cfg ? cfg->find(k) : nullptr;
-  if (!j) return def;
-  if (j->is_number() || j->is_array()) return JVec3(*j);
-  throw std::runtime_error(std::string("textured parameter not supported: ") + k);
-}
-static Float ReadMono(const Json* cfg, const char* k, Float def) {
-  const Json* j = cfg ? cfg->find(k) : nullptr;
-  if (!j) return def;
-  if (j->is_number()) return (Float)j->num;
-  throw std::runtime_error(std::string("textured parameter not supported: ") + k);
-}
-static Microfacet ReadDist(const Json* cfg) {
-  Microfacet d;
+// Microfacet parameters (rough_metal.cpp:30-45, rough_glass.cpp:35-50) with
+// textured alpha / alpha_u / alpha_v recorded as TexParams of the owning BSDF.
+template <class T>
+static void DistParam(T* self, const Json* cfg, Microfacet T::*m, TexEnv* env) {
+  Microfacet& d = self->*m;
   std::string dist = ReadS(cfg, "distribution", "ggx");
   d.ggx = dist != "beckmann";
+  auto alpha = [&](const char* k, int which) {
+    const Json* j = cfg ? cfg->find(k) : nullptr;
+    if (j && !j->is_number()) {
+      self->texParams.push_back(TexParam{MakeTexture(*j, 1, env), [m, which](Bsdf& b, const V3& v) {
+                                           Microfacet& x = static_cast<T&>(b).*m;
+                                           if (which != 2) x.alphaX = v.x;
+                                           if (which != 1) x.alphaY = v.x;
+                                         }});
+      return;
+    }
+    Float a = j ? (Float)j->num : Float(0.1f);
+    if (which != 2) d.alphaX = a;
+    if (which != 1) d.alphaY = a;
+  };
   if (cfg && cfg->has("alpha")) {
-    d.alphaX = d.alphaY = ReadMono(cfg, "alpha", 0.1f);
+    alpha("alpha", 0);
   } else {
-    d.alphaX = ReadMono(cfg, "alpha_u", 0.1f);
-    d.alphaY = ReadMono(cfg, "alpha_v", 0.1f);
+    alpha("alpha_u", 1);
+    alpha("alpha_v", 2);
   }
   d.sampleVisible = ReadB(cfg, "sample_visible", true);
-  return d;
 }
 
 // ----------------------------------------------------------------- diffuse
 // diffuse.cpp:46-99
 struct DiffuseBsdf final : Bsdf {
   Spectrum R;
-  explicit DiffuseBsdf(const Json* cfg) {
+  explicit DiffuseBsdf(const Json* cfg, TexEnv* env) {
     flags = BT_Diffuse | BT_Reflection;
-    R = ReadColor(cfg, "reflectance", V3(0.5f));
+    ColorParam(cfg, "reflectance", V3(0.5f), &DiffuseBsdf::R, env);
   }
-  std::pair<BsdfSample, Spectrum> Sample(const V3& wi, Float, const V2& dirXi) const override {
+  std::unique_ptr<Bsdf> Clone() const override { return std::make_unique<DiffuseBsdf>(*this); }
+  std::pair<BsdfSample, Spectrum> SampleImpl(const V3& wi, Float, const V2& dirXi, const TexSi*) const override {
     Float cosThetaI = wi.z;
     if (cosThetaI <= 0) return {{}, Spectrum(0)};
     BsdfSample bsr;
@@ -304,11 +309,11 @@ struct DiffuseBsdf final : Bsdf {
     Float cosThetaO = bsr.Wo.z;
     return {bsr, R * (1 / PI) * cosThetaO};
   }
-  Spectrum Eval(const V3& wi, const V3& wo) const override {
+  Spectrum EvalImpl(const V3& wi, const V3& wo, const TexSi*) const override {
     if (wi.z <= 0 || wo.z <= 0) return Spectrum(0);
     return R * (1 / PI) * wo.z;
   }
-  Float Pdf(const V3& wi, const V3& wo) const override {
+  Float PdfImpl(const V3& wi, const V3& wo, const TexSi*) const override {
     if (wi.z <= 0 || wo.z <= 0) return 0;
     return SquareToCosineHemispherePdf(wo);
   }
@@ -319,14 +324,15 @@ struct DiffuseBsdf final : Bsdf {
 struct RoughMetalBsdf final : Bsdf {
   Spectrum R, eta, k;
   Microfacet dist;
-  explicit RoughMetalBsdf(const Json* cfg) {
+  explicit RoughMetalBsdf(const Json* cfg, TexEnv* env) {
     flags = BT_Glossy | BT_Reflection;
-    R = ReadColor(cfg, "reflectance", V3(1));
-    eta = ReadColor(cfg, "eta", V3(0.1999899f, 0.9220823f, 1.0998751f));
-    k = ReadColor(cfg, "k", V3(3.9046354f, 2.4476316f, 2.1376500f));
-    dist = ReadDist(cfg);
+    ColorParam(cfg, "reflectance", V3(1), &RoughMetalBsdf::R, env);
+    ColorParam(cfg, "eta", V3(0.1999899f, 0.9220823f, 1.0998751f), &RoughMetalBsdf::eta, env);
+    ColorParam(cfg, "k", V3(3.9046354f, 2.4476316f, 2.1376500f), &RoughMetalBsdf::k, env);
+    DistParam(this, cfg, &RoughMetalBsdf::dist, env);
   }
-  std::pair<BsdfSample, Spectrum> Sample(const V3& wi, Float, const V2& dirXi) const override {
+  std::unique_ptr<Bsdf> Clone() const override { return std::make_unique<RoughMetalBsdf>(*this); }
+  std::pair<BsdfSample, Spectrum> SampleImpl(const V3& wi, Float, const V2& dirXi, const TexSi*) const override {
     Float cosThetaI = wi.z;
     if (cosThetaI <= 0) return {{}, Spectrum(0)};
     BsdfSample bsr;
@@ -345,7 +351,7 @@ struct RoughMetalBsdf final : Bsdf {
     Spectrum brdf((F.x * Dv * Gv) / denom, (F.y * Dv * Gv) / denom, (F.z * Dv * Gv) / denom);
     return {bsr, cmul(R, brdf) * bsr.Wo.z};
   }
-  Spectrum Eval(const V3& wi, const V3& wo) const override {
+  Spectrum EvalImpl(const V3& wi, const V3& wo, const TexSi*) const override {
     Float cosThetaI = wi.z, cosThetaO = wo.z;
     if (cosThetaI <= 0 || cosThetaO <= 0) return Spectrum(0);
     V3 wh = normalized(wo + wi);
@@ -357,7 +363,7 @@ struct RoughMetalBsdf final : Bsdf {
                   std::abs(F.z * Dv * Gv) / denom);
     return cmul(R, brdf) * cosThetaO;
   }
-  Float Pdf(const V3& wi, const V3& wo) const override {
+  Float PdfImpl(const V3& wi, const V3& wo, const TexSi*) const override {
     if (wi.z <= 0 || wo.z <= 0) return 0;
     V3 wh = normalized(wo + wi);
     return dist.Pdf(wi, wh) / (4 * dot(wo, wh));
@@ -370,17 +376,18 @@ struct RoughGlassBsdf final : Bsdf {
   Spectrum R, T;
   Float eta, invEta;
   Microfacet dist;
-  explicit RoughGlassBsdf(const Json* cfg) {
+  explicit RoughGlassBsdf(const Json* cfg, TexEnv* env) {
     flags = BT_Glossy | BT_Reflection | BT_Transmission;
-    R = ReadColor(cfg, "reflectance", V3(1));
-    T = ReadColor(cfg, "transmittance", V3(1));
+    ColorParam(cfg, "reflectance", V3(1), &RoughGlassBsdf::R, env);
+    ColorParam(cfg, "transmittance", V3(1), &RoughGlassBsdf::T, env);
     Float intIor = ReadF(cfg, "int_ior", Float(1.5046));
     Float extIor = ReadF(cfg, "ext_ior", Float(1.000277));
     eta = intIor / extIor;
     invEta = extIor / intIor;
-    dist = ReadDist(cfg);
+    DistParam(this, cfg, &RoughGlassBsdf::dist, env);
   }
-  std::pair<BsdfSample, Spectrum> Sample(const V3& wi, Float lobeXi, const V2& dirXi) const override {
+  std::unique_ptr<Bsdf> Clone() const override { return std::make_unique<RoughGlassBsdf>(*this); }
+  std::pair<BsdfSample, Spectrum> SampleImpl(const V3& wi, Float lobeXi, const V2& dirXi, const TexSi*) const override {
     BsdfSample bsr;
     Float cosThetaI = wi.z;
     if (cosThetaI == 0) return {{}, Spectrum(0)};
@@ -398,7 +405,7 @@ struct RoughGlassBsdf final : Bsdf {
     if (bsr.Pdf <= 0) return {{}, Spectrum(0)};
     return {bsr, Eval(wi, bsr.Wo)};
   }
-  Spectrum Eval(const V3& wi, const V3& wo) const override {
+  Spectrum EvalImpl(const V3& wi, const V3& wo, const TexSi*) const override {
     Float cosThetaI = wi.z, cosThetaO = wo.z;
     if (cosThetaI == 0) return Spectrum(0);
     bool reflect = cosThetaI * cosThetaO > 0;
@@ -423,7 +430,7 @@ struct RoughGlassBsdf final : Bsdf {
     }
     return result;
   }
-  Float Pdf(const V3& wi, const V3& wo) const override {
+  Float PdfImpl(const V3& wi, const V3& wo, const TexSi*) const override {
     Float cosThetaI = wi.z, cosThetaO = wo.z;
     if (cosThetaI == 0) return 0;
     bool reflect = cosThetaI * cosThetaO > 0;
@@ -460,26 +467,26 @@ struct DisneyBsdf final : Bsdf {
     return true;
   }
 
-  explicit DisneyBsdf(const Json* cfg) {
-    baseColor = ReadColor(cfg, "base_color", V3(0.5f));
-    roughness = ReadMono(cfg, "roughness", 0.5f);
+  explicit DisneyBsdf(const Json* cfg, TexEnv* env) {
+    ColorParam(cfg, "base_color", V3(0.5f), &DisneyBsdf::baseColor, env);
+    MonoParam(cfg, "roughness", 0.5f, &DisneyBsdf::roughness, env);
     hasAnisotropic = HasValue(cfg, "anisotropic");
-    anisotropic = ReadMono(cfg, "anisotropic", 0);
+    MonoParam(cfg, "anisotropic", 0, &DisneyBsdf::anisotropic, env);
     hasSpecTrans = HasValue(cfg, "spec_trans");
-    specTrans = ReadMono(cfg, "spec_trans", 0);
+    MonoParam(cfg, "spec_trans", 0, &DisneyBsdf::specTrans, env);
     hasSheen = HasValue(cfg, "sheen");
-    sheen = ReadMono(cfg, "sheen", 0);
+    MonoParam(cfg, "sheen", 0, &DisneyBsdf::sheen, env);
     hasSheenTint = HasValue(cfg, "sheen_tint");
-    sheenTint = ReadMono(cfg, "sheen_tint", 0);
+    MonoParam(cfg, "sheen_tint", 0, &DisneyBsdf::sheenTint, env);
     hasFlatness = HasValue(cfg, "flatness");
-    flatness = ReadMono(cfg, "flatness", 0);
+    MonoParam(cfg, "flatness", 0, &DisneyBsdf::flatness, env);
     hasSpecTint = HasValue(cfg, "spec_tint");
-    specTint = ReadMono(cfg, "spec_tint", 0);
+    MonoParam(cfg, "spec_tint", 0, &DisneyBsdf::specTint, env);
     hasMetallic = HasValue(cfg, "metallic");
-    metallic = ReadMono(cfg, "metallic", 0);
+    MonoParam(cfg, "metallic", 0, &DisneyBsdf::metallic, env);
     hasClearcoat = HasValue(cfg, "clearcoat");
-    clearcoat = ReadMono(cfg, "clearcoat", 0);
-    clearcoatGloss = ReadMono(cfg, "clearcoat_gloss", 0);
+    MonoParam(cfg, "clearcoat", 0, &DisneyBsdf::clearcoat, env);
+    MonoParam(cfg, "clearcoat_gloss", 0, &DisneyBsdf::clearcoatGloss, env);
     specularSample = ReadF(cfg, "main_specular_sampling_rate", 1);
     clearcoatSample = ReadF(cfg, "clearcoat_sampling_rate", 1);
     diffuseReflectSample = ReadF(cfg, "diffuse_reflectance_sampling_rate", 1);
@@ -498,6 +505,7 @@ struct DisneyBsdf final : Bsdf {
     if (hasClearcoat) flags |= BT_Glossy;
     if (hasSpecTrans) flags |= BT_Transmission;
   }
+  std::unique_ptr<Bsdf> Clone() const override { return std::make_unique<DisneyBsdf>(*this); }
 
   // disney.cpp:474-486
   void RoughnessToAlpha(Float& ax, Float& ay) const {
@@ -599,7 +607,7 @@ struct DisneyBsdf final : Bsdf {
   };
 
   // disney.cpp:113-235
-  std::pair<BsdfSample, Spectrum> Sample(const V3& wi, Float lobeXi, const V2& dirXi) const override {
+  std::pair<BsdfSample, Spectrum> SampleImpl(const V3& wi, Float lobeXi, const V2& dirXi, const TexSi*) const override {
     Float cosThetaI = wi.z;
     BsdfSample bsr;
     if (cosThetaI == 0) return {bsr, Spectrum(0)};
@@ -679,7 +687,7 @@ struct DisneyBsdf final : Bsdf {
   }
 
   // disney.cpp:237-361
-  Spectrum Eval(const V3& wi, const V3& wo) const override {
+  Spectrum EvalImpl(const V3& wi, const V3& wo, const TexSi*) const override {
     Float cosThetaI = wi.z;
     if (cosThetaI == 0) return Spectrum(0);
     Float rough = roughness;
@@ -772,7 +780,7 @@ struct DisneyBsdf final : Bsdf {
   }
 
   // disney.cpp:363-456
-  Float Pdf(const V3& wi, const V3& wo) const override {
+  Float PdfImpl(const V3& wi, const V3& wo, const TexSi*) const override {
     Float cosThetaI = wi.z;
     if (cosThetaI == 0) return 0;
     Float st = hasSpecTrans ? specTrans : Float(0);
@@ -833,13 +841,14 @@ struct DisneyBsdf final : Bsdf {
 // perfect_mirror.cpp:17-62
 struct PerfectMirrorBsdf final : Bsdf {
   Spectrum R, eta, k;
-  explicit PerfectMirrorBsdf(const Json* cfg) {
+  explicit PerfectMirrorBsdf(const Json* cfg, TexEnv* env) {
     flags = BT_Delta | BT_Reflection;
-    R = ReadColor(cfg, "reflectance", V3(1));
-    eta = ReadColor(cfg, "eta", V3(0));
-    k = ReadColor(cfg, "k", V3(1));
+    ColorParam(cfg, "reflectance", V3(1), &PerfectMirrorBsdf::R, env);
+    ColorParam(cfg, "eta", V3(0), &PerfectMirrorBsdf::eta, env);
+    ColorParam(cfg, "k", V3(1), &PerfectMirrorBsdf::k, env);
   }
-  std::pair<BsdfSample, Spectrum> Sample(const V3& wi, Float, const V2&) const override {
+  std::unique_ptr<Bsdf> Clone() const override { return std::make_unique<PerfectMirrorBsdf>(*this); }
+  std::pair<BsdfSample, Spectrum> SampleImpl(const V3& wi, Float, const V2&, const TexSi*) const override {
     Float cosThetaI = wi.z;
     if (cosThetaI <= 0) return {{}, Spectrum(0)};
     BsdfSample bsr;
@@ -850,8 +859,8 @@ struct PerfectMirrorBsdf final : Bsdf {
     Spectrum F = FresnelConductor(wi.z, eta, k);
     return {bsr, cmul(R, F)};
   }
-  Spectrum Eval(const V3&, const V3&) const override { return Spectrum(0); }
-  Float Pdf(const V3&, const V3&) const override { return 0; }
+  Spectrum EvalImpl(const V3&, const V3&, const TexSi*) const override { return Spectrum(0); }
+  Float PdfImpl(const V3&, const V3&, const TexSi*) const override { return 0; }
 };
 
 // ---------------------------------------------------------- perfect_glass
@@ -859,15 +868,16 @@ struct PerfectMirrorBsdf final : Bsdf {
 struct PerfectGlassBsdf final : Bsdf {
   Spectrum R, T;
   Float eta;
-  explicit PerfectGlassBsdf(const Json* cfg) {
+  std::unique_ptr<Bsdf> Clone() const override { return std::make_unique<PerfectGlassBsdf>(*this); }
+  explicit PerfectGlassBsdf(const Json* cfg, TexEnv* env) {
     flags = BT_Delta | BT_Reflection | BT_Transmission;
-    R = ReadColor(cfg, "reflectance", V3(1));
-    T = ReadColor(cfg, "transmittance", V3(1));
+    ColorParam(cfg, "reflectance", V3(1), &PerfectGlassBsdf::R, env);
+    ColorParam(cfg, "transmittance", V3(1), &PerfectGlassBsdf::T, env);
     Float intIor = ReadF(cfg, "int_ior", Float(1.5046));
     Float extIor = ReadF(cfg, "ext_ior", Float(1.000277));
     eta = intIor / extIor;
   }
-  std::pair<BsdfSample, Spectrum> Sample(const V3& wi, Float lobeXi, const V2&) const override {
+  std::pair<BsdfSample, Spectrum> SampleImpl(const V3& wi, Float lobeXi, const V2&, const TexSi*) const override {
     Float ri, cosThetaT, etaIT, etaTI;
     FresnelDielectric(wi.z, eta, ri, cosThetaT, etaIT, etaTI);
     Float ti = 1 - ri;
@@ -889,8 +899,8 @@ struct PerfectGlassBsdf final : Bsdf {
     }
     return {bsr, f};
   }
-  Spectrum Eval(const V3&, const V3&) const override { return Spectrum(0); }
-  Float Pdf(const V3&, const V3&) const override { return 0; }
+  Spectrum EvalImpl(const V3&, const V3&, const TexSi*) const override { return Spectrum(0); }
+  Float PdfImpl(const V3&, const V3&, const TexSi*) const override { return 0; }
 };
 
 // ------------------------------------------------- plastic / rough_plastic
@@ -917,22 +927,26 @@ struct PlasticBase : Bsdf {
   Float eta, fdrInt, invEta2, specularSampleWeight;
   Spectrum diffuse, specular;
   bool noLinear;
-  explicit PlasticBase(const Json* cfg) {
+  PlasticBase(const Json* cfg, TexEnv* env) {
     flags = BT_Diffuse | BT_Reflection | BT_Delta;
     Float intIor = ReadF(cfg, "int_ior", Float(1.49f));
     Float extIor = ReadF(cfg, "ext_ior", Float(1.000277f));
     eta = intIor / extIor;
-    diffuse = ReadColor(cfg, "diffuse", V3(0.5f));
-    specular = ReadColor(cfg, "specular", V3(1));
+    std::shared_ptr<Texture> dt = ColorParam(cfg, "diffuse", V3(0.5f), &PlasticBase::diffuse, env);
+    std::shared_ptr<Texture> st = ColorParam(cfg, "specular", V3(1), &PlasticBase::specular, env);
     noLinear = ReadB(cfg, "no_linear", false);
     fdrInt = DiffuseReflectance(Float(1) / eta);
     invEta2 = Float(1) / (eta * eta);
-    // the mean luminance over each texture's texels; constant textures are 1x1
+    // the mean luminance of Texture::Read over each texture's texels
+    // (constants and chessboards are 1 x 1; a chessboard reads 0)
+    std::shared_ptr<Texture> dc = dt ? dt : ConstTexture(diffuse, 3), sc = st ? st : ConstTexture(specular, 3);
     double diffMean = 0, specMean = 0;
-    diffMean += Luminance(diffuse);
-    diffMean /= (1 * 1);
-    specMean += Luminance(specular);
-    specMean /= (1 * 1);
+    for (uint32_t y = 0; y < dc->height; y++)
+      for (uint32_t x = 0; x < dc->width; x++) diffMean += Luminance(dc->Read(x, y));
+    diffMean /= (dc->height * dc->width);
+    for (uint32_t y = 0; y < sc->height; y++)
+      for (uint32_t x = 0; x < sc->width; x++) specMean += Luminance(sc->Read(x, y));
+    specMean /= (sc->height * sc->width);
     specularSampleWeight = (Float)(specMean / (diffMean + specMean));
   }
   Spectrum DiffuseTerm(Float fi, Float fo, Float cosThetaO) const {  // plastic.cpp:83-88
@@ -947,8 +961,9 @@ struct PlasticBase : Bsdf {
 
 // plastic.cpp:16-139
 struct PlasticBsdf final : PlasticBase {
-  explicit PlasticBsdf(const Json* cfg) : PlasticBase(cfg) {}
-  std::pair<BsdfSample, Spectrum> Sample(const V3& wi, Float lobeXi, const V2& dirXi) const override {
+  PlasticBsdf(const Json* cfg, TexEnv* env) : PlasticBase(cfg, env) {}
+  std::unique_ptr<Bsdf> Clone() const override { return std::make_unique<PlasticBsdf>(*this); }
+  std::pair<BsdfSample, Spectrum> SampleImpl(const V3& wi, Float lobeXi, const V2& dirXi, const TexSi*) const override {
     Float cosThetaI = wi.z;
     if (cosThetaI <= 0) return {{}, Spectrum(0)};
     Float fi = DielectricR(cosThetaI, eta);
@@ -974,14 +989,14 @@ struct PlasticBsdf final : PlasticBase {
     }
     return {bsr, f};
   }
-  Spectrum Eval(const V3& wi, const V3& wo) const override {
+  Spectrum EvalImpl(const V3& wi, const V3& wo, const TexSi*) const override {
     Float cosThetaI = wi.z, cosThetaO = wo.z;
     if (cosThetaI <= 0 || cosThetaO <= 0) return Spectrum(0);
     Float fi = DielectricR(cosThetaI, eta);
     Float fo = DielectricR(cosThetaO, eta);
     return DiffuseTerm(fi, fo, cosThetaO);
   }
-  Float Pdf(const V3& wi, const V3& wo) const override {
+  Float PdfImpl(const V3& wi, const V3& wo, const TexSi*) const override {
     Float cosThetaI = wi.z, cosThetaO = wo.z;
     if (cosThetaI <= 0 || cosThetaO <= 0) return 0;
     Float fi = DielectricR(cosThetaI, eta);
@@ -995,13 +1010,22 @@ struct PlasticBsdf final : PlasticBase {
 // rough_plastic.cpp:17-241 (default context: Glossy and Diffuse both enabled)
 struct RoughPlasticBsdf final : PlasticBase {
   Microfacet dist;
-  explicit RoughPlasticBsdf(const Json* cfg) : PlasticBase(cfg) {
+  std::unique_ptr<Bsdf> Clone() const override { return std::make_unique<RoughPlasticBsdf>(*this); }
+  RoughPlasticBsdf(const Json* cfg, TexEnv* env) : PlasticBase(cfg, env) {
     std::string d = ReadS(cfg, "distribution", "ggx");
     dist.ggx = d != "beckmann";
-    dist.alphaX = dist.alphaY = ReadMono(cfg, "alpha", 0.1f);
+    const Json* aj = cfg ? cfg->find("alpha") : nullptr;
+    if (aj && !aj->is_number()) {  // one alpha texture for both axes (rough_plastic.cpp:28, :104-118)
+      texParams.push_back(TexParam{MakeTexture(*aj, 1, env), [](Bsdf& b, const V3& v) {
+                                     auto& r = static_cast<RoughPlasticBsdf&>(b);
+                                     r.dist.alphaX = r.dist.alphaY = v.x;
+                                   }});
+    } else {
+      dist.alphaX = dist.alphaY = aj ? (Float)aj->num : Float(0.1f);
+    }
     dist.sampleVisible = ReadB(cfg, "sample_visible", true);
   }
-  std::pair<BsdfSample, Spectrum> Sample(const V3& wi, Float lobeXi, const V2& dirXi) const override {
+  std::pair<BsdfSample, Spectrum> SampleImpl(const V3& wi, Float lobeXi, const V2& dirXi, const TexSi*) const override {
     Float cosThetaI = wi.z;
     if (cosThetaI <= 0) return {{}, Spectrum(0)};
     Float fi = DielectricR(cosThetaI, eta);
@@ -1023,7 +1047,7 @@ struct RoughPlasticBsdf final : PlasticBase {
     if (bsr.Pdf <= 0) return {bsr, Spectrum(0)};
     return {bsr, Eval(wi, bsr.Wo)};
   }
-  Spectrum Eval(const V3& wi, const V3& wo) const override {
+  Spectrum EvalImpl(const V3& wi, const V3& wo, const TexSi*) const override {
     Float cosThetaI = wi.z, cosThetaO = wo.z;
     if (cosThetaI <= 0 || cosThetaO <= 0) return Spectrum(0);
     V3 wh = normalized(wo + wi);
@@ -1035,7 +1059,7 @@ struct RoughPlasticBsdf final : PlasticBase {
     Spectrum diff = DiffuseTerm(F, fo, cosThetaO);
     return spec + diff;
   }
-  Float Pdf(const V3& wi, const V3& wo) const override {
+  Float PdfImpl(const V3& wi, const V3& wo, const TexSi*) const override {
     Float cosThetaI = wi.z, cosThetaO = wo.z;
     if (cosThetaI <= 0 || cosThetaO <= 0) return 0;
     Float fi = DielectricR(cosThetaI, eta);
@@ -1054,21 +1078,23 @@ struct RoughPlasticBsdf final : PlasticBase {
 // mask.cpp:10-69
 struct MaskBsdf final : Bsdf {
   Float opacity;
-  std::unique_ptr<Bsdf> nested;
-  explicit MaskBsdf(const Json* cfg) {
-    opacity = ReadMono(cfg, "opacity", 0.5f);
+  std::shared_ptr<Bsdf> nested;
+  MaskBsdf(const Json* cfg, TexEnv* env) {
+    MonoParam(cfg, "opacity", 0.5f, &MaskBsdf::opacity, env);
     if (!cfg || !cfg->has("nested")) throw std::runtime_error("mask needs a nested bsdf");
-    nested = MakeBsdf(cfg->find("nested"));
+    nested = MakeBsdf(cfg->find("nested"), env);
     flags = nested->flags;
   }
+  std::unique_ptr<Bsdf> Clone() const override { return std::make_unique<MaskBsdf>(*this); }
   Float EvalOpacity() const { return std::clamp(opacity, Float(0), Float(1)); }
-  std::pair<BsdfSample, Spectrum> Sample(const V3& wi, Float lobeXi, const V2& dirXi) const override {
+  std::pair<BsdfSample, Spectrum> SampleImpl(const V3& wi, Float lobeXi, const V2& dirXi,
+                                             const TexSi* ts) const override {
     Float op = EvalOpacity();
     BsdfSample bsr;
     Spectrum result;
     if (lobeXi < op) {
       lobeXi /= op;
-      auto r = nested->Sample(wi, lobeXi, dirXi);
+      auto r = nested->Sample(wi, lobeXi, dirXi, ts);
       bsr = r.first;
       bsr.Pdf *= op;
       result = r.second * op;
@@ -1081,66 +1107,67 @@ struct MaskBsdf final : Bsdf {
     }
     return {bsr, result};
   }
-  Spectrum Eval(const V3& wi, const V3& wo) const override { return nested->Eval(wi, wo) * EvalOpacity(); }
-  Float Pdf(const V3& wi, const V3& wo) const override { return nested->Pdf(wi, wo) * EvalOpacity(); }
+  Spectrum EvalImpl(const V3& wi, const V3& wo, const TexSi* ts) const override {
+    return nested->Eval(wi, wo, ts) * EvalOpacity();
+  }
+  Float PdfImpl(const V3& wi, const V3& wo, const TexSi* ts) const override {
+    return nested->Pdf(wi, wo, ts) * EvalOpacity();
+  }
 };
 
 // --------------------------------------------------------------- two_side
 // two_side.cpp:64-129
 struct TwoSideBsdf final : Bsdf {
-  std::unique_ptr<Bsdf> resA, resB;
-  const Bsdf* outside = nullptr;
-  const Bsdf* inside = nullptr;
-  explicit TwoSideBsdf(const Json* cfg) {
+  std::shared_ptr<Bsdf> outside, inside;
+  TwoSideBsdf(const Json* cfg, TexEnv* env) {
     if (cfg && cfg->has("two_side")) {
-      resA = MakeBsdf(cfg->find("two_side"));
-      outside = inside = resA.get();
+      outside = inside = MakeBsdf(cfg->find("two_side"), env);
     } else {
       // two_side.cpp:34-52: the out_side / in_side form. The reference reads its
       // (uninitialised) pointers before assigning them; the intent, kept here,
       // is outside = out_side and inside = in_side, both required.
-      if (cfg && cfg->has("out_side")) resA = MakeBsdf(cfg->find("out_side"));
-      if (cfg && cfg->has("in_side")) resB = MakeBsdf(cfg->find("in_side"));
-      if (!resA || !resB) throw std::runtime_error("config must contains out_side and in_side");
-      outside = resA.get();
-      inside = resB.get();
+      if (cfg && cfg->has("out_side")) outside = MakeBsdf(cfg->find("out_side"), env);
+      if (cfg && cfg->has("in_side")) inside = MakeBsdf(cfg->find("in_side"), env);
+      if (!outside || !inside) throw std::runtime_error("config must contains out_side and in_side");
     }
     flags = inside->flags | outside->flags;
   }
-  std::pair<BsdfSample, Spectrum> Sample(const V3& wi, Float lobeXi, const V2& dirXi) const override {
-    if (wi.z > 0) return outside->Sample(wi, lobeXi, dirXi);
+  std::unique_ptr<Bsdf> Clone() const override { return std::make_unique<TwoSideBsdf>(*this); }
+  std::pair<BsdfSample, Spectrum> SampleImpl(const V3& wi, Float lobeXi, const V2& dirXi,
+                                             const TexSi* ts) const override {
+    if (wi.z > 0) return outside->Sample(wi, lobeXi, dirXi, ts);
     if (wi.z < 0) {
       V3 twi(wi.x, wi.y, -wi.z);
-      auto r = inside->Sample(twi, lobeXi, dirXi);
+      auto r = inside->Sample(twi, lobeXi, dirXi, ts);
       r.first.Wo.z *= -1;
       return r;
     }
     return {BsdfSample{}, Spectrum(0)};
   }
-  Spectrum Eval(const V3& wi, const V3& wo) const override {
-    if (wi.z > 0) return outside->Eval(wi, wo);
-    if (wi.z < 0) return inside->Eval(V3(wi.x, wi.y, -wi.z), V3(wo.x, wo.y, -wo.z));
+  Spectrum EvalImpl(const V3& wi, const V3& wo, const TexSi* ts) const override {
+    if (wi.z > 0) return outside->Eval(wi, wo, ts);
+    if (wi.z < 0) return inside->Eval(V3(wi.x, wi.y, -wi.z), V3(wo.x, wo.y, -wo.z), ts);
     return Spectrum(0);
   }
-  Float Pdf(const V3& wi, const V3& wo) const override {
-    if (wi.z > 0) return outside->Pdf(wi, wo);
-    if (wi.z < 0) return inside->Pdf(V3(wi.x, wi.y, -wi.z), V3(wo.x, wo.y, -wo.z));
+  Float PdfImpl(const V3& wi, const V3& wo, const TexSi* ts) const override {
+    if (wi.z > 0) return outside->Pdf(wi, wo, ts);
+    if (wi.z < 0) return inside->Pdf(V3(wi.x, wi.y, -wi.z), V3(wo.x, wo.y, -wo.z), ts);
     return 0;
   }
 };
 
-std::unique_ptr<Bsdf> MakeBsdf(const Json* cfg) {
+std::unique_ptr<Bsdf> MakeBsdf(const Json* cfg, TexEnv* env) {
   std::string type = ReadS(cfg, "type", "");
-  if (type == "diffuse") return std::make_unique<DiffuseBsdf>(cfg);
-  if (type == "rough_metal") return std::make_unique<RoughMetalBsdf>(cfg);
-  if (type == "rough_glass") return std::make_unique<RoughGlassBsdf>(cfg);
-  if (type == "disney") return std::make_unique<DisneyBsdf>(cfg);
-  if (type == "two_side") return std::make_unique<TwoSideBsdf>(cfg);
-  if (type == "perfect_mirror") return std::make_unique<PerfectMirrorBsdf>(cfg);
-  if (type == "perfect_glass") return std::make_unique<PerfectGlassBsdf>(cfg);
-  if (type == "plastic") return std::make_unique<PlasticBsdf>(cfg);
-  if (type == "rough_plastic") return std::make_unique<RoughPlasticBsdf>(cfg);
-  if (type == "mask") return std::make_unique<MaskBsdf>(cfg);
+  if (type == "diffuse") return std::make_unique<DiffuseBsdf>(cfg, env);
+  if (type == "rough_metal") return std::make_unique<RoughMetalBsdf>(cfg, env);
+  if (type == "rough_glass") return std::make_unique<RoughGlassBsdf>(cfg, env);
+  if (type == "disney") return std::make_unique<DisneyBsdf>(cfg, env);
+  if (type == "two_side") return std::make_unique<TwoSideBsdf>(cfg, env);
+  if (type == "perfect_mirror") return std::make_unique<PerfectMirrorBsdf>(cfg, env);
+  if (type == "perfect_glass") return std::make_unique<PerfectGlassBsdf>(cfg, env);
+  if (type == "plastic") return std::make_unique<PlasticBsdf>(cfg, env);
+  if (type == "rough_plastic") return std::make_unique<RoughPlasticBsdf>(cfg, env);
+  if (type == "mask") return std::make_unique<MaskBsdf>(cfg, env);
   throw std::runtime_error("cannot find factory: " + type);
 }
 

@@ -3,7 +3,10 @@
 // src/bsdf/{diffuse,rough_metal,rough_glass,disney,two_side,perfect_mirror,perfect_glass,
 // plastic,rough_plastic,mask}.cpp.
 #pragma once
+#include <functional>
+
 #include "ref_core.h"
+#include "ref_texture.h"
 
 namespace orc {
 
@@ -27,20 +30,80 @@ struct BsdfSample {
   uint32_t Type = BT_Empty;
 };
 
+struct Bsdf;
+// A textured parameter (ConfigNodeReadTexture, config_node_ext.h:17-45): the
+// texture and how its value is written into a copy of the BSDF.
+struct TexParam {
+  std::shared_ptr<Texture> tex;
+  std::function<void(Bsdf&, const V3&)> set;
+};
+
 // The integrators only ever use the default BsdfContext (Radiance, All lobes),
 // path.cpp:139 and vol_path.cpp:38, so the context is not a parameter here.
+// The reference evaluates a BSDF's textures inside Sample / Eval / Pdf at the
+// SurfaceInteraction's UV; here the public calls take that UV (ts, null = no
+// surface point) and run the constant-parameter code on a copy whose textured
+// parameters hold the looked-up values -- the same values, in the same order
+// of arithmetic.
 struct Bsdf {
   uint32_t flags = 0;
+  std::vector<TexParam> texParams;
   virtual ~Bsdf() = default;
   bool HasAnyTypeExceptDelta() const { return (flags & BT_NoDelta) != 0; }
-  virtual std::pair<BsdfSample, Spectrum> Sample(const V3& wi, Float lobeXi, const V2& dirXi) const = 0;
-  virtual Spectrum Eval(const V3& wi, const V3& wo) const = 0;
-  virtual Float Pdf(const V3& wi, const V3& wo) const = 0;
+  std::pair<BsdfSample, Spectrum> Sample(const V3& wi, Float lobeXi, const V2& dirXi, const TexSi* ts = nullptr) const {
+    if (ts && !texParams.empty()) return Bound(*ts)->SampleImpl(wi, lobeXi, dirXi, ts);
+    return SampleImpl(wi, lobeXi, dirXi, ts);
+  }
+  Spectrum Eval(const V3& wi, const V3& wo, const TexSi* ts = nullptr) const {
+    if (ts && !texParams.empty()) return Bound(*ts)->EvalImpl(wi, wo, ts);
+    return EvalImpl(wi, wo, ts);
+  }
+  Float Pdf(const V3& wi, const V3& wo, const TexSi* ts = nullptr) const {
+    if (ts && !texParams.empty()) return Bound(*ts)->PdfImpl(wi, wo, ts);
+    return PdfImpl(wi, wo, ts);
+  }
+
+ protected:
+  virtual std::unique_ptr<Bsdf> Clone() const = 0;
+  virtual std::pair<BsdfSample, Spectrum> SampleImpl(const V3& wi, Float lobeXi, const V2& dirXi,
+                                                     const TexSi* ts) const = 0;
+  virtual Spectrum EvalImpl(const V3& wi, const V3& wo, const TexSi* ts) const = 0;
+  virtual Float PdfImpl(const V3& wi, const V3& wo, const TexSi* ts) const = 0;
+  std::unique_ptr<Bsdf> Bound(const TexSi& ts) const {
+    std::unique_ptr<Bsdf> b = Clone();
+    for (const TexParam& p : texParams) p.set(*b, p.tex->Eval(ts));
+    return b;
+  }
+  // An RGB / mono parameter: a constant is stored in the member, a texture is
+  // recorded (the member is then filled per lookup). Returns the texture or null.
+  template <class T>
+  std::shared_ptr<Texture> ColorParam(const Json* cfg, const char* k, const V3& def, Spectrum T::*m, TexEnv* env) {
+    const Json* j = cfg ? cfg->find(k) : nullptr;
+    if (j && !(j->is_number() || j->is_array())) {
+      TexParam p{MakeTexture(*j, 3, env), [m](Bsdf& b, const V3& v) { static_cast<T&>(b).*m = v; }};
+      texParams.push_back(p);
+      return p.tex;
+    }
+    static_cast<T*>(this)->*m = j ? JVec3(*j) : def;
+    return nullptr;
+  }
+  template <class T>
+  std::shared_ptr<Texture> MonoParam(const Json* cfg, const char* k, Float def, Float T::*m, TexEnv* env) {
+    const Json* j = cfg ? cfg->find(k) : nullptr;
+    if (j && !j->is_number()) {
+      TexParam p{MakeTexture(*j, 1, env), [m](Bsdf& b, const V3& v) { static_cast<T&>(b).*m = v.x; }};
+      texParams.push_back(p);
+      return p.tex;
+    }
+    static_cast<T*>(this)->*m = j ? (Float)j->num : def;
+    return nullptr;
+  }
 };
 
 // Factory by the reference's names: diffuse, rough_metal, rough_glass, disney, two_side,
-// perfect_mirror, perfect_glass, plastic, rough_plastic, mask.
-std::unique_ptr<Bsdf> MakeBsdf(const Json* cfg);
+// perfect_mirror, perfect_glass, plastic, rough_plastic, mask. env: the scene's
+// image assets (null: textured parameters are an error).
+std::unique_ptr<Bsdf> MakeBsdf(const Json* cfg, TexEnv* env = nullptr);
 
 // Warps: rad.offline/src/warp.cpp:10-99
 V2 SquareToUniformDisk(const V2& u);

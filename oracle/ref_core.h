@@ -301,6 +301,12 @@ struct Json {
   bool is_array() const { return kind == Array; }
   bool is_object() const { return kind == Object; }
   static Json parse(const std::string& text);
+  static Json Num(double v) {
+    Json j;
+    j.kind = Number;
+    j.num = v;
+    return j;
+  }
 };
 
 // ConfigNode helpers: rad.core/include/rad/core/config_node.h:10-170

@@ -32,8 +32,9 @@ static bool Occl(const Scene& S, const V3& P, const V3& N, const V3& p) {
 }
 
 // ------------------------------------------------------------------ path
-Spectrum PathLi(const Scene& S, const Ray& ray0, Pcg32& rng) {
+Spectrum PathLi(const Scene& S, const Ray& ray0, const RayDiff& diff0, Pcg32& rng) {
   Ray ray = ray0;
+  RayDiff diff = diff0;  // only the camera ray has differentials (path.cpp:132, :208)
   Spectrum throughput(1), result(0);
   Float eta = 1;
   int depth = 0;
@@ -67,6 +68,8 @@ Spectrum PathLi(const Scene& S, const Ray& ray0, Pcg32& rng) {
     if (sh.light >= 0) break;
     if (sh.bsdf < 0) break;  // the reference dereferences a null BSDF here
     const Bsdf& bsdf = *S.bsdfs[sh.bsdf];
+    si.ComputeDifferentials(diff);  // si.BSDF(ray) (path.cpp:172)
+    TexSi ts = si.Tex();
     if (bsdf.HasAnyTypeExceptDelta()) {
       Float xl = rng.Next1D();
       V2 xd = rng.Next2D();
@@ -74,8 +77,8 @@ Spectrum PathLi(const Scene& S, const Ray& ray0, Pcg32& rng) {
       const DirectionSample& dsr = dl.first;
       if (dsr.Pdf > 0) {
         V3 wo = si.ToLocal(dsr.Dir);
-        Spectrum f = bsdf.Eval(si.Wi, wo);
-        Float bsdfPdf = bsdf.Pdf(si.Wi, wo);
+        Spectrum f = bsdf.Eval(si.Wi, wo, &ts);
+        Float bsdfPdf = bsdf.Pdf(si.Wi, wo, &ts);
         if (!Occl(S, si.P, si.N, dsr.P)) {
           Float weight = dsr.IsDelta ? 1 : MisWeight(dsr.Pdf, bsdfPdf);
           result = result + cmul(cmul(throughput, f), dl.second) * weight / dsr.Pdf;
@@ -85,11 +88,12 @@ Spectrum PathLi(const Scene& S, const Ray& ray0, Pcg32& rng) {
     {
       Float xl = rng.Next1D();
       V2 xd = rng.Next2D();
-      auto bs = bsdf.Sample(si.Wi, xl, xd);
+      auto bs = bsdf.Sample(si.Wi, xl, xd, &ts);
       if (bs.first.Pdf <= 0) break;
       throughput = cmul(throughput, bs.second) / bs.first.Pdf;
       eta *= bs.first.Eta;
       ray = SpawnRay(si.P, si.N, si.ToWorld(bs.first.Wo));
+      diff.has = false;
       prevBsdfPdf = bs.first.Pdf;
       prevP = si.P;
       isSpecularPath = (bs.first.Type & BT_Delta) != 0;
@@ -357,20 +361,21 @@ Spectrum VolPathLi(const Scene& S, const Ray& ray0, Pcg32& rng) {
         continue;
       }
       const Bsdf& bsdf = *S.bsdfs[sh.bsdf];
+      TexSi ts = si.Tex();  // vol_path traces plain rays: uv derivatives stay 0 (vol_path.cpp:28, :177)
       if (bsdf.HasAnyTypeExceptDelta()) {
         auto sl = VolSampleLight(S, rng, medium, channel, si.P, si.N);
         const DirectionSample& dsr = sl.second;
         if (dsr.Pdf > 0) {
           V3 wo = si.ToLocal(dsr.Dir);
-          Spectrum f = bsdf.Eval(si.Wi, wo);
-          Float bsdfPdf = bsdf.Pdf(si.Wi, wo);
+          Spectrum f = bsdf.Eval(si.Wi, wo, &ts);
+          Float bsdfPdf = bsdf.Pdf(si.Wi, wo, &ts);
           Float weight = dsr.IsDelta ? 1 : MisWeight(dsr.Pdf, bsdfPdf);
           result = result + cmul(cmul(throughput, f), sl.first) * weight / dsr.Pdf;
         }
       }
       Float xl = rng.Next1D();
       V2 xd = rng.Next2D();
-      auto bs = bsdf.Sample(si.Wi, xl, xd);
+      auto bs = bsdf.Sample(si.Wi, xl, xd, &ts);
       if (bs.first.Pdf <= 0) break;
       throughput = cmul(throughput, bs.second) / bs.first.Pdf;
       eta *= bs.first.Eta;
@@ -392,8 +397,9 @@ static Spectrum RenderSample(const Scene& S, uint32_t x, uint32_t y, uint32_t s,
   Float jx = rng.Next1D();
   Float jy = rng.Next1D();
   V2 scr(Float(x) + jx, Float(y) + jy);
-  Ray ray = S.camera.SampleRay(scr);
-  return S.renderer == "vol_path" ? VolPathLi(S, ray, rng) : PathLi(S, ray, rng);
+  RayDiff diff;
+  Ray ray = S.camera.SampleRayDifferential(scr, diff);
+  return S.renderer == "vol_path" ? VolPathLi(S, ray, rng) : PathLi(S, ray, diff, rng);
 }
 
 // sample_renderer.cpp:101-105: HasInfinity / HasNegative test only the first
@@ -560,6 +566,47 @@ int orc_render_samples(void* sp, const uint32_t* pix, const uint32_t* smp, int64
       out[i * 3] = li.x;
       out[i * 3 + 1] = li.y;
       out[i * 3 + 2] = li.z;
+    }
+  } catch (const std::exception& e) {
+    g_err = e.what();
+    return -1;
+  }
+  return 0;
+}
+
+// Texture<T>::Eval of the scene's texture number `tex` (creation order), at
+// uv (n x 2) with derivatives duv (n x 4: du/dx, dv/dx, du/dy, dv/dy); out n x 3.
+int orc_texture_eval(void* sp, uint32_t tex, const float* uv, const float* duv, int64_t n, float* out) {
+  Scene& S = *(Scene*)sp;
+  if (tex >= S.textures.size()) {
+    g_err = "texture index out of range";
+    return -1;
+  }
+  const Texture* t = S.textures[tex];
+  for (int64_t i = 0; i < n; i++) {
+    TexSi si{V2(uv[2 * i], uv[2 * i + 1]), V2(duv[4 * i], duv[4 * i + 1]), V2(duv[4 * i + 2], duv[4 * i + 3])};
+    V3 v = t->Eval(si);
+    out[3 * i] = v.x;
+    out[3 * i + 1] = v.y;
+    out[3 * i + 2] = v.z;
+  }
+  return 0;
+}
+int orc_texture_count(void* sp) { return (int)((Scene*)sp)->textures.size(); }
+
+// An image asset as the texture factory sees it (type: image_default /
+// image_hdr / image_exr, options as the asset's JSON). Writes width, height,
+// channels to dims and, when px is not null, the texels (at most cap floats).
+int orc_image_load(const char* assetJson, const char* path, int32_t* dims, float* px, int64_t cap) {
+  try {
+    Json a = Json::parse(assetJson);
+    ImageAsset im = LoadImageAsset(a, ReadS(&a, "type", ""), path);
+    dims[0] = im.width;
+    dims[1] = im.height;
+    dims[2] = im.channels;
+    if (px) {
+      if ((int64_t)im.px.size() > cap) throw std::runtime_error("buffer too small");
+      std::memcpy(px, im.px.data(), im.px.size() * sizeof(float));
     }
   } catch (const std::exception& e) {
     g_err = e.what();

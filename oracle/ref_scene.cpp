@@ -439,6 +439,33 @@ Ray Camera::SampleRay(const V2& screen) const {
   return r;
 }
 
+Ray Camera::SampleRayDifferential(const V2& screen, RayDiff& diff) const {
+  V2 t(screen.x * (1 / Float(width)), screen.y * (1 / Float(height)));
+  V3 ndc(t.x, t.y, 0);
+  V3 nearP = cameraToClip.ApplyAffineToLocal(ndc);
+  Ray r = SampleRay(screen);
+  diff.has = true;
+  diff.Ox = diff.Oy = r.O;
+  diff.Dx = cameraToWorld.ApplyLinearToWorld(normalized(nearP + dx));
+  diff.Dy = cameraToWorld.ApplyLinearToWorld(normalized(nearP + dy));
+  return r;
+}
+
+void SurfaceInteraction::ComputeDifferentials(const RayDiff& ray) {
+  if (!(ray.has && dUVdX.x == 0 && dUVdX.y == 0 && dUVdY.x == 0 && dUVdY.y == 0)) return;
+  Float d = dot(N, P);
+  Float tx = (d - dot(N, ray.Ox)) / dot(N, ray.Dx);
+  Float ty = (d - dot(N, ray.Oy)) / dot(N, ray.Dy);
+  V3 dpdx = (ray.Dx * tx + ray.Ox) - P;
+  V3 dpdy = (ray.Dy * ty + ray.Oy) - P;
+  Float a00 = dot(dPdU, dPdU), a01 = dot(dPdU, dPdV), a11 = dot(dPdV, dPdV),
+        invDet = Rcp(Fmadd(a00, a11, -(a01 * a01)));
+  Float b0x = dot(dPdU, dpdx), b1x = dot(dPdV, dpdx), b0y = dot(dPdU, dpdy), b1y = dot(dPdV, dpdy);
+  invDet = std::isfinite(invDet) ? invDet : 0;
+  dUVdX = V2(Fmadd(a11, b0x, -(a01 * b1x)) * invDet, Fmadd(a00, b1x, -(a01 * b0x)) * invDet);
+  dUVdY = V2(Fmadd(a11, b0y, -(a01 * b1y)) * invDet, Fmadd(a00, b1y, -(a01 * b0y)) * invDet);
+}
+
 // math_ext.h:65-75
 static M4 LookAtLeftHand(const V3& origin, const V3& target, const V3& up) {
   V3 dir = normalized(target - origin);
@@ -488,6 +515,9 @@ static Camera MakeCamera(const Json& cfg) {
   translate.m[0][3] = -1;
   translate.m[1][3] = -1 / aspect;
   c.cameraToClip = Transform(scale * translate * persp);
+  V3 o = c.cameraToClip.ApplyAffineToLocal(V3(0, 0, 0));
+  c.dx = c.cameraToClip.ApplyAffineToLocal(V3(Float(1) / c.width, 0, 0)) - o;
+  c.dy = c.cameraToClip.ApplyAffineToLocal(V3(0, Float(1) / c.height, 0)) - o;
   return c;
 }
 
@@ -705,11 +735,14 @@ std::unique_ptr<Scene> Scene::FromJson(const std::string& text, const std::strin
         Medium md;
         ReadVol(JoinPath(baseDir, loc), md);
         assets.vols.emplace(name, std::move(md));
+      } else if (type == "image_default" || type == "image_hdr" || type == "image_exr") {
+        S.images[name] = LoadImageAsset(a, type, JoinPath(baseDir, loc));
       } else {
         throw std::runtime_error("cannot find factory: " + type);
       }
     }
   }
+  TexEnv env{&S.images, &S.textures};
   const Json* cam = root.find("camera");
   if (!cam) throw std::runtime_error("no child: camera");
   S.camera = MakeCamera(*cam);
@@ -730,7 +763,7 @@ std::unique_ptr<Scene> Scene::FromJson(const std::string& text, const std::strin
       const Json* def = v.find("bsdf");
       if (!def) throw std::runtime_error("no child: bsdf");
       if (bsdfVars.count(name)) throw std::runtime_error("duplicate bsdf var name: " + name);
-      S.bsdfs.push_back(MakeBsdf(def));
+      S.bsdfs.push_back(MakeBsdf(def, &env));
       bsdfVars[name] = (int)S.bsdfs.size() - 1;
     }
   }
@@ -908,7 +941,7 @@ std::unique_ptr<Scene> Scene::FromJson(const std::string& text, const std::strin
         if (it == bsdfVars.end()) throw std::runtime_error("unknown bsdf var: " + ref->str);
         bsdfIdx = it->second;
       } else {
-        S.bsdfs.push_back(MakeBsdf(bn));
+        S.bsdfs.push_back(MakeBsdf(bn, &env));
         bsdfIdx = (int)S.bsdfs.size() - 1;
       }
     }
@@ -934,7 +967,7 @@ std::unique_ptr<Scene> Scene::FromJson(const std::string& text, const std::strin
       t.kind = Json::String;
       t.str = "diffuse";
       def.obj.push_back({"type", t});
-      S.bsdfs.push_back(MakeBsdf(&def));
+      S.bsdfs.push_back(MakeBsdf(&def, &env));
       bsdfIdx = (int)S.bsdfs.size() - 1;
     }
     if (shapeIdx >= 0) {

@@ -7,6 +7,7 @@
 // ray/triangle test of Woop, Benthin and Wald (JCGT 2013).
 #pragma once
 #include "ref_bsdf.h"
+#include "ref_texture.h"
 
 namespace orc {
 
@@ -39,6 +40,12 @@ struct DirectionSample : PositionSample {  // sample_result.h:15-18
   Float Dist = 0;
 };
 
+// RayDifferential (ray.h:35-57): a camera ray's pixel-offset rays
+struct RayDiff {
+  bool has = false;
+  V3 Ox, Oy, Dx, Dy;
+};
+
 struct SurfaceInteraction {  // interaction.h:44-110
   Float T = std::numeric_limits<Float>::infinity();
   V3 P, N;
@@ -46,7 +53,12 @@ struct SurfaceInteraction {  // interaction.h:44-110
   Frame Shading;
   V2 UV;
   V3 dPdU, dPdV;
+  V2 dUVdX, dUVdY;
   V3 Wi;
+  // SurfaceInteraction::BSDF(ray) (interaction.cpp:83-109): uv derivatives from
+  // a ray's differentials, when it has them.
+  void ComputeDifferentials(const RayDiff& rd);
+  TexSi Tex() const { return TexSi{UV, dUVdX, dUVdY}; }
   bool IsValid() const { return T != std::numeric_limits<Float>::infinity(); }
   V3 ToWorld(const V3& v) const { return Shading.ToWorld(v); }
   V3 ToLocal(const V3& v) const { return Shading.ToLocal(v); }
@@ -153,7 +165,9 @@ struct Camera {  // perspective.cpp:15-70
   int width = 1280, height = 720;
   Float nearZ = 0.001f, farZ = 100;
   Transform cameraToWorld, cameraToClip;
+  V3 dx, dy;  // perspective.cpp:56-59
   Ray SampleRay(const V2& screen) const;
+  Ray SampleRayDifferential(const V2& screen, RayDiff& diff) const;  // perspective.cpp:84-97
 };
 
 struct BvhNode {
@@ -167,6 +181,8 @@ struct PrimRef {
 
 struct Scene {
   std::vector<std::unique_ptr<Bsdf>> bsdfs;
+  std::map<std::string, ImageAsset> images;  // image assets by name
+  std::vector<const Texture*> textures;      // every texture, in creation order
   std::vector<Shape> shapes;
   std::vector<Light> lights;
   std::vector<Medium> media;

@@ -108,6 +108,16 @@ class Scene:
                                     self.seed if seed is None else seed, _p(out)))
         return out
 
+    def texture_eval(self, texture, uv, duv=None):
+        """Texture number `texture` (creation order) at uv (n, 2) with uv derivatives
+        duv (n, 4: du/dx, dv/dx, du/dy, dv/dy; default 0) -> (n, 3)."""
+        uv = np.ascontiguousarray(uv, dtype=np.float32).reshape(-1, 2)
+        n = uv.shape[0]
+        duv = np.zeros((n, 4), np.float32) if duv is None else np.ascontiguousarray(duv, dtype=np.float32)
+        out = np.zeros((n, 3), dtype=np.float32)
+        check(lib().rad_scene_texture_eval(self._h, texture, _p(uv), _p(duv), n, _p(out)))
+        return out
+
     def render_samples(self, pixels, samples, seed=None):
         """Li of individual (pixel, sample) pairs through the job kernels -> (n, 3)."""
         pixels = np.ascontiguousarray(pixels, dtype=np.uint32)

@@ -41,7 +41,7 @@ EXPORTS = [
     "rad_scene_load_json", "rad_scene_load_file", "rad_scene_destroy", "rad_scene_info_get",
     "rad_scene_footprint", "rad_job_submit", "rad_job_wait", "rad_job_cancel", "rad_job_progress",
     "rad_job_film", "rad_job_stats", "rad_job_destroy", "rad_trace_batch", "rad_trace_batch_device",
-    "rad_bsdf_eval_batch", "rad_bsdf_sample_batch", "rad_camera_rays", "rad_render_samples",
+    "rad_bsdf_eval_batch", "rad_bsdf_sample_batch", "rad_camera_rays", "rad_scene_texture_eval", "rad_render_samples",
     "rad_render_samples_noalloc", "rad_guide_enable", "rad_guide_info", "rad_guide_checkpoint",
     "rad_guide_load", "rad_guide_forward", "rad_guide_mix_eval", "rad_guide_grad", "rad_autotune",
 ]
@@ -128,6 +128,7 @@ def load(path=LIB_PATH):
         "rad_bsdf_eval_batch": [ctypes.c_char_p, P, P, I64, P, P],
         "rad_bsdf_sample_batch": [ctypes.c_char_p, P, P, I64, P, P, P, P, P],
         "rad_camera_rays": [P, P, I64, ctypes.c_uint32, ctypes.c_uint32, P],
+        "rad_scene_texture_eval": [P, ctypes.c_uint32, P, P, I64, P],
         "rad_render_samples": [P, P, P, I64, ctypes.c_uint32, P],
         "rad_render_samples_noalloc": [P, P, P, I64, ctypes.c_uint32, P, P],
         "rad_guide_enable": [P, ctypes.c_char_p],

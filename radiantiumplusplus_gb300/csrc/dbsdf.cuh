@@ -8,6 +8,7 @@
 // same inputs.
 #pragma once
 #include "dmath.cuh"
+#include "dtex.cuh"
 
 namespace rad {
 
@@ -635,8 +636,9 @@ RD BsdfSampleRes LeafSample(const MatRec& m, V3 wi, float lobeXi, V2 dirXi) {
 // (mask.cpp:24-60) scales the nested BSDF by its opacity, or, for the share of
 // samples beyond the opacity, passes the ray straight through (a Null event).
 // Scales are applied innermost first, as the nested calls would apply them; the
-// host limits wrapper nesting to kMaxBsdfNest levels.
-RD void BsdfEvalPdf(const MatRec* mats, uint32_t mi, V3 wi, V3 wo, V3& f, float& pdf) {
+// host limits wrapper nesting to kMaxBsdfNest levels. With a texture context,
+// textured parameters are looked up at its uv (dtex.cuh).
+RD void BsdfEvalPdf(const MatRec* mats, uint32_t mi, V3 wi, V3 wo, V3& f, float& pdf, const TexCtx* tc = nullptr) {
   float ops[kMaxBsdfNest];
   int nops = 0;
   f = v3s(0.f);
@@ -655,10 +657,12 @@ RD void BsdfEvalPdf(const MatRec* mats, uint32_t mi, V3 wi, V3 wo, V3& f, float&
       }
     } else if (m.kind == MAT_MASK) {
       if (nops == kMaxBsdfNest) break;
-      ops[nops++] = m.p[0];
+      MatRec tmp;
+      ops[nops++] = TexturedMat(m, tc, tmp).p[0];
       mi = m.ref0;
     } else {
-      LeafEvalPdf(m, wi, wo, f, pdf);
+      MatRec tmp;
+      LeafEvalPdf(TexturedMat(m, tc, tmp), wi, wo, f, pdf);
       break;
     }
   }
@@ -667,7 +671,8 @@ RD void BsdfEvalPdf(const MatRec* mats, uint32_t mi, V3 wi, V3 wo, V3& f, float&
     pdf = pdf * ops[k];
   }
 }
-RD BsdfSampleRes BsdfSample(const MatRec* mats, uint32_t mi, V3 wi, float lobeXi, V2 dirXi) {
+RD BsdfSampleRes BsdfSample(const MatRec* mats, uint32_t mi, V3 wi, float lobeXi, V2 dirXi,
+                            const TexCtx* tc = nullptr) {
   float ops[kMaxBsdfNest];
   int nops = 0;
   bool flip = false;
@@ -685,7 +690,8 @@ RD BsdfSampleRes BsdfSample(const MatRec* mats, uint32_t mi, V3 wi, float lobeXi
         break;
       }
     } else if (m.kind == MAT_MASK) {
-      float op = m.p[0];
+      MatRec tmp;
+      float op = TexturedMat(m, tc, tmp).p[0];
       if (lobeXi < op && nops < kMaxBsdfNest) {
         lobeXi /= op;
         ops[nops++] = op;
@@ -699,7 +705,8 @@ RD BsdfSampleRes BsdfSample(const MatRec* mats, uint32_t mi, V3 wi, float lobeXi
         break;
       }
     } else {
-      r = LeafSample(m, wi, lobeXi, dirXi);
+      MatRec tmp;
+      r = LeafSample(TexturedMat(m, tc, tmp), wi, lobeXi, dirXi);
       break;
     }
   }
@@ -735,9 +742,9 @@ RD BsdfSampleRes LeafSampleK(const MatRec& m, V3 wi, float lobeXi, V2 dirXi) {
   else return LeafSample(m, wi, lobeXi, dirXi);
 }
 template <int K>
-RD void ClassEvalPdf(const MatRec* mats, uint32_t mi, V3 wi, V3 wo, V3& f, float& pdf) {
+RD void ClassEvalPdf(const MatRec* mats, uint32_t mi, V3 wi, V3 wo, V3& f, float& pdf, const TexCtx* tc = nullptr) {
   if constexpr (K == SC_GENERIC) {
-    BsdfEvalPdf(mats, mi, wi, wo, f, pdf);
+    BsdfEvalPdf(mats, mi, wi, wo, f, pdf, tc);
     return;
   }
   const MatRec& m = mats[mi];
@@ -753,8 +760,9 @@ RD void ClassEvalPdf(const MatRec* mats, uint32_t mi, V3 wi, V3 wo, V3& f, float
   }
 }
 template <int K>
-RD BsdfSampleRes ClassSample(const MatRec* mats, uint32_t mi, V3 wi, float lobeXi, V2 dirXi) {
-  if constexpr (K == SC_GENERIC) return BsdfSample(mats, mi, wi, lobeXi, dirXi);
+RD BsdfSampleRes ClassSample(const MatRec* mats, uint32_t mi, V3 wi, float lobeXi, V2 dirXi,
+                             const TexCtx* tc = nullptr) {
+  if constexpr (K == SC_GENERIC) return BsdfSample(mats, mi, wi, lobeXi, dirXi, tc);
   const MatRec& m = mats[mi];
   if (m.kind != MAT_TWO_SIDE) return LeafSampleK<K>(m, wi, lobeXi, dirXi);
   if (wi.z > 0.f) return LeafSampleK<K>(mats[m.ref0], wi, lobeXi, dirXi);

@@ -96,6 +96,93 @@ RD SurfInt ComputeSI(const DevScene& S, V3 O, V3 D, const TraceHit& h) {
   return si;
 }
 
+// uv and position derivatives of a hit (mesh_base.cpp:38-66, rectangle.cpp:204-218,
+// sphere.cpp:215-240); needed only where textures are looked up.
+struct SurfUV {
+  V2 uv;
+  V3 dPdU, dPdV;
+};
+RD SurfUV ComputeUV(const DevScene& S, const TraceHit& h, const SurfInt& si) {
+  SurfUV r;
+  const ShapeRec& sh = S.shapes[h.shape];
+  if (sh.kind == SHAPE_MESH) {
+    if (!sh.hasUV) {
+      r.uv = V2{h.u, h.v};
+      CoordinateSystem(si.N, r.dPdU, r.dPdV);
+      return r;
+    }
+    uint32_t tri = (h.prim - sh.primOffset) + sh.triOffset;
+    uint32_t f0 = __ldg(S.idx + 3 * (size_t)tri), f1 = __ldg(S.idx + 3 * (size_t)tri + 1),
+             f2 = __ldg(S.idx + 3 * (size_t)tri + 2);
+    V3 p0 = ld3(S.pos + 3 * (size_t)f0), p1 = ld3(S.pos + 3 * (size_t)f1), p2 = ld3(S.pos + 3 * (size_t)f2);
+    V3 dp0 = p1 - p0, dp1 = p2 - p0;
+    float b0 = 1.f - h.u - h.v, b1 = h.u, b2 = h.v;
+    const float* uvp = S.uv;
+    float u0x = uvp[2 * f0], u0y = uvp[2 * f0 + 1], u1x = uvp[2 * f1], u1y = uvp[2 * f1 + 1];
+    float u2x = uvp[2 * f2], u2y = uvp[2 * f2 + 1];
+    r.uv = V2{u0x * b0 + (u1x * b1 + (u2x * b2)), u0y * b0 + (u1y * b1 + (u2y * b2))};
+    float d0x = u1x - u0x, d0y = u1y - u0y, d1x = u2x - u0x, d1y = u2y - u0y;
+    float det = d0x * d1y - (d0y * d1x);
+    float invDet = det == 0.f ? 0.f : Rcp(det);
+    if (invDet == 0.f) {
+      r.dPdU = r.dPdV = v3s(0.f);
+    } else {
+      r.dPdU = (d1y * dp0 - (d0y * dp1)) * invDet;
+      r.dPdV = (-d1x * dp0 + (d0x * dp1)) * invDet;
+    }
+  } else if (sh.kind == SHAPE_RECT) {
+    r.uv = V2{h.u * 0.5f + 0.5f, h.v * 0.5f + 0.5f};
+    r.dPdU = ShapeM3(sh, 12);
+    r.dPdV = ShapeM3(sh, 15);
+  } else {
+    V3 local = AffineRows(sh.m + 4, si.P);
+    float rd2 = Sqr(local.x) + Sqr(local.y);
+    // UnitAngleZ (math_ext.h:101-104)
+    float temp = asinf(0.5f * norm(V3{local.x, local.y, local.z - MulSign(1.f, local.z)})) * 2.f;
+    float theta = local.z >= 0.f ? temp : kPi - temp;
+    float phi = atan2f(local.y, local.x);
+    if (phi < 0.f) phi += 2.f * kPi;
+    r.uv = V2{phi / (2.f * kPi), theta / kPi};
+    V3 du{-local.y, local.x, 0.f};
+    float rd = sqrtf(rd2);
+    float invRd = Rcp(rd);
+    float cosPhi = local.x * invRd, sinPhi = local.y * invRd;
+    V3 dv{local.z * cosPhi, local.z * sinPhi, -rd};
+    if (rd == 0.f) dv = V3{1.f, 0.f, 0.f};
+    r.dPdU = LinearRows(sh.m + 16, du * (2.f * kPi));
+    r.dPdV = LinearRows(sh.m + 16, dv * kPi);
+  }
+  return r;
+}
+
+// uv derivatives of the first hit of a camera ray: the pixel-offset rays of
+// Perspective::SampleRayDifferential (perspective.cpp:84-97) intersected with
+// the tangent plane, then solved for (du, dv) as SurfaceInteraction::BSDF(ray)
+// does (interaction.cpp:83-109). (sx, sy): the ray's screen position; O: its origin.
+RD void CameraUVDerivs(const CameraRec& c, float sx, float sy, V3 O, const SurfInt& si, const SurfUV& su, V2& duvdx,
+                       V2& duvdy) {
+  float tx = sx * (1.f / (float)c.width), ty = sy * (1.f / (float)c.height);
+  V3 nearP = Affine4(c.clipToCamera, V3{tx, ty, 0.f});
+  V3 ax = normalized(nearP + V3{c.dx[0], c.dx[1], c.dx[2]});
+  V3 ay = normalized(nearP + V3{c.dy[0], c.dy[1], c.dy[2]});
+  const float* m = c.camToWorld;
+  V3 Dx{(m[0] * ax.x + m[1] * ax.y) + m[2] * ax.z, (m[4] * ax.x + m[5] * ax.y) + m[6] * ax.z,
+        (m[8] * ax.x + m[9] * ax.y) + m[10] * ax.z};
+  V3 Dy{(m[0] * ay.x + m[1] * ay.y) + m[2] * ay.z, (m[4] * ay.x + m[5] * ay.y) + m[6] * ay.z,
+        (m[8] * ay.x + m[9] * ay.y) + m[10] * ay.z};
+  float d = dot(si.N, si.P);
+  float tX = (d - dot(si.N, O)) / dot(si.N, Dx);
+  float tY = (d - dot(si.N, O)) / dot(si.N, Dy);
+  V3 dpdx = (Dx * tX + O) - si.P;
+  V3 dpdy = (Dy * tY + O) - si.P;
+  float a00 = dot(su.dPdU, su.dPdU), a01 = dot(su.dPdU, su.dPdV), a11 = dot(su.dPdV, su.dPdV);
+  float invDet = Rcp(fmaf(a00, a11, -(a01 * a01)));
+  float b0x = dot(su.dPdU, dpdx), b1x = dot(su.dPdV, dpdx), b0y = dot(su.dPdU, dpdy), b1y = dot(su.dPdV, dpdy);
+  invDet = isfinite(invDet) ? invDet : 0.f;
+  duvdx = V2{fmaf(a11, b0x, -(a01 * b1x)) * invDet, fmaf(a00, b1x, -(a01 * b0x)) * invDet};
+  duvdy = V2{fmaf(a11, b0y, -(a01 * b1y)) * invDet, fmaf(a00, b1y, -(a01 * b0y)) * invDet};
+}
+
 // ---------------------------------------------------------------- lights
 struct DirSample {
   V3 P, N, Dir;

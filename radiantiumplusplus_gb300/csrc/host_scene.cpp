@@ -4,6 +4,8 @@
 // produces from the same JSON.
 #include "host_scene.h"
 
+#include "host_image.h"
+
 #include <algorithm>
 #include <cmath>
 #include <cstring>
@@ -350,30 +352,260 @@ std::string Join(const std::string& base, const std::string& loc) {
   return base + "/" + loc;
 }
 
-// ---- BSDF records
-F3 Color(const JValue* c, const char* k, F3 def) {
-  const JValue* v = c ? c->get(k) : nullptr;
-  if (!v) return def;
-  if (v->isNum() || v->isArr()) return Vec3(*v, k);
-  throw FactoryError(std::string("textured parameters are not supported: ") + k);
+// ---- image assets (rad.core asset/image_stb.cpp:12-104, image_hdr.cpp:12-57,
+// image_exr.cpp:12-95): decoded (host_image.cpp) and converted to float texels.
+struct ImageAsset {
+  int width = 0, height = 0, channels = 0;  // channels: 1 (mono) or 3 (rgb)
+  std::vector<float> px;                    // texel (x, y) at (y * width + x) * channels
+  std::string type;
+};
+
+std::string ReadAll(const std::string& path) {
+  std::ifstream in(path, std::ios::binary);
+  if (!in) throw IoError("cannot open " + path);
+  std::stringstream ss;
+  ss << in.rdbuf();
+  return ss.str();
 }
-float Mono(const JValue* c, const char* k, float def) {
-  const JValue* v = c ? c->get(k) : nullptr;
-  if (!v) return def;
-  if (v->isNum()) return (float)v->n;
-  throw FactoryError(std::string("textured parameters are not supported: ") + k);
-}
-void SetDist(const JValue* c, MatRec& m) {
-  std::string dist = RS(c, "distribution", "ggx");
-  m.p[11] = dist == "beckmann" ? 0.f : 1.f;  // unknown names fall back to GGX (rough_metal.cpp:36-39)
-  if (c && c->has("alpha")) {
-    m.p[9] = m.p[10] = Mono(c, "alpha", 0.1f);
-  } else {
-    m.p[9] = Mono(c, "alpha_u", 0.1f);
-    m.p[10] = Mono(c, "alpha_v", 0.1f);
+
+// Color24f::ToLinear (color.h:41-46)
+float SrgbToLinear(float v) { return v <= 0.04045f ? v * (1.0f / 12.92f) : std::pow((v + 0.055f) * (1.0f / 1.055f), 2.4f); }
+
+ImageAsset LoadImageAsset(const JValue& a, const std::string& type, const std::string& path) {
+  ImageAsset im;
+  im.type = type;
+  std::string bytes = ReadAll(path);
+  try {
+    if (type == "image_default") {
+      int ch = RI(&a, "channel", 3);
+      bool flip = RB(&a, "is_flip_y", true);
+      bool lin = RB(&a, "is_to_linear", ch == 3);
+      if (ch != 1 && ch != 3) throw ConfigError("channel must be 1 or 3");
+      img::Ldr l = img::LoadLdr(bytes, ch, flip);
+      im.width = l.width;
+      im.height = l.height;
+      im.channels = ch;
+      im.px.resize(l.px.size());
+      for (size_t i = 0; i < l.px.size(); i++) {
+        float v = (float)l.px[i] / 255.f;  // color /= 255 (image_stb.cpp:59-69, :84-85)
+        im.px[i] = (ch == 3 && lin) ? SrgbToLinear(v) : v;
+      }
+    } else {
+      img::Hdr h = type == "image_hdr" ? img::LoadHdr(bytes, RB(&a, "is_flip_y", false)) : img::LoadExr(bytes);
+      im.width = h.width;
+      im.height = h.height;
+      im.channels = 3;
+      im.px = std::move(h.px);
+    }
+  } catch (const std::runtime_error& e) {
+    if (dynamic_cast<const ConfigError*>(&e)) throw;
+    throw IoError(std::string(e.what()) + ": " + path);
   }
-  m.p[12] = RB(c, "sample_visible", true) ? 1.f : 0.f;
+  return im;
 }
+
+// ---- textures (texture.h:47-90, config_node_ext.h:17-45, bitmap.cpp, chessboard.cpp)
+struct TexEnv {
+  HostScene* hs = nullptr;  // null: records built without a scene (no textures)
+  const std::map<std::string, ImageAsset>* images = nullptr;
+};
+
+// MipMap::FilterBilinear (bitmap.cpp:200-214) on an explicit level
+void MipBilinear(const float* img, uint32_t W, uint32_t H, int C, uint32_t pu, uint32_t pv, float fu, float fv,
+                 float* out) {
+  int32_t dpu = (fu > pu + 0.5f) ? 1 : -1;
+  int32_t dpv = (fv > pv + 0.5f) ? 1 : -1;
+  uint32_t apu = std::min(pu + (uint32_t)dpu, W - 1), apv = std::min(pv + (uint32_t)dpv, H - 1);
+  float du = std::min(std::abs(fu - pu - 0.5f), 1.f);
+  float dv = std::min(std::abs(fv - pv - 0.5f), 1.f);
+  for (int c = 0; c < C; c++) {
+    float a = img[((size_t)pv * W + pu) * C + c], b = img[((size_t)pv * W + apu) * C + c];
+    float d = img[((size_t)apv * W + pu) * C + c], e = img[((size_t)apv * W + apu) * C + c];
+    out[c] = (a * (1 - du) + b * du) * (1 - dv) + (d * (1 - du) + e * du) * dv;
+  }
+}
+
+// MipMap construction (bitmap.cpp:27-64): each coarser texel averages four
+// bilinear lookups at the integer texel corners of the finer level.
+void BuildMips(TexRec& t, std::vector<float> level0, int maxLevel, std::vector<float>& pool) {
+  uint32_t W = t.width, H = t.height;
+  int C = (int)t.channels;
+  if (maxLevel != 0 && ((W % 2 != 0) || (H % 2 != 0))) maxLevel = 0;  // bitmap.cpp:30-33
+  uint32_t real = maxLevel < 0 ? 1 + (uint32_t)std::log2((double)std::max(W, H)) : (uint32_t)maxLevel;
+  real = std::max(real, 1u);
+  if (real > (uint32_t)kMaxMipLevels) throw ConfigError("bitmap: more than 16 mip levels");
+  t.levels = real;
+  std::vector<float> last = std::move(level0);
+  uint32_t lw = W, lh = H;
+  for (uint32_t a = 0; a < real; a++) {
+    if (a > 0) {
+      uint32_t nw = std::max(1u, lw / 2), nh = std::max(1u, lh / 2);
+      std::vector<float> next((size_t)nw * nh * C);
+      auto corner = [&](uint32_t u, uint32_t v, float* o) {
+        uint32_t pu = t.wrap ? u % lw : std::min(u, lw - 1);
+        uint32_t pv = t.wrap ? v % lh : std::min(v, lh - 1);
+        MipBilinear(last.data(), lw, lh, C, pu, pv, pu + 1.f, pv + 1.f, o);
+      };
+      for (uint32_t j = 0; j < nh; j++)
+        for (uint32_t i = 0; i < nw; i++) {
+          float a0[3], a1[3], a2[3], a3[3];
+          corner(i * 2, j * 2, a0);
+          corner(i * 2 + 1, j * 2, a1);
+          corner(i * 2, j * 2 + 1, a2);
+          corner(i * 2 + 1, j * 2 + 1, a3);
+          for (int c = 0; c < C; c++) next[((size_t)j * nw + i) * C + c] = (a0[c] + a1[c] + a2[c] + a3[c]) * 0.25f;
+        }
+      last = std::move(next);
+      lw = nw;
+      lh = nh;
+    }
+    if (pool.size() + last.size() > 0xffffffffull) throw ConfigError("texture pool exceeds 2^32 texels");
+    t.levelOffset[a] = (uint32_t)pool.size();
+    pool.insert(pool.end(), last.begin(), last.end());
+  }
+}
+
+// ConfigNodeReadTexture for a texture node (a number / array is a constant).
+uint32_t AddTexture(const JValue& v, int channels, TexEnv& env) {
+  HostScene& hs = *env.hs;
+  TexRec t;
+  std::memset(&t, 0, sizeof(t));
+  t.channels = (uint32_t)channels;
+  uint32_t index = (uint32_t)hs.tex.size();
+  hs.tex.push_back(t);
+  if (v.isNum() || v.isArr()) {
+    t.kind = TEX_CONST;
+    if (channels == 3) {
+      F3 c = Vec3(v, "texture");
+      t.value[0] = c.x;
+      t.value[1] = c.y;
+      t.value[2] = c.z;
+    } else {
+      t.value[0] = Num(v, "texture");
+    }
+  } else {
+    std::string type = TypeOf(v);
+    if (type == "bitmap") {  // bitmap.cpp:273-316
+      t.kind = TEX_BITMAP;
+      const JValue* an = v.get("asset_name");
+      if (!an || !an->isStr()) throw ConfigError("no child: asset_name");
+      auto it = env.images->find(an->s);
+      if (it == env.images->end()) throw ConfigError("unknown asset: " + an->s);
+      const ImageAsset& im = it->second;
+      if (im.channels != channels) {
+        if (im.type != "image_default") throw ConfigError(im.type + " does not support single channel");
+        throw ConfigError(std::string("loaded image ") + an->s + (im.channels == 1 ? " is mono" : " is rgb"));
+      }
+      std::string f = RS(&v, "filter", "bilinear");
+      t.filter = f == "nearest" ? TF_NEAREST : f == "trilinear" ? TF_TRILINEAR : f == "anisotropic" ? TF_ANISO : TF_BILINEAR;
+      t.wrap = RS(&v, "wrap", "clamp") == "repeat" ? 1u : 0u;
+      bool mip = t.filter == TF_TRILINEAR || t.filter == TF_ANISO;
+      int maxLevel = RI(&v, "max_level", mip ? -1 : 0);
+      t.aniso = RF(&v, "anisotropic_level", t.filter == TF_ANISO ? 8.f : 0.f);
+      if (!mip && maxLevel < 0) maxLevel = 0;
+      t.width = (uint32_t)im.width;
+      t.height = (uint32_t)im.height;
+      BuildMips(t, im.px, maxLevel, hs.texels);
+      if (mip) hs.needDiff = true;
+    } else if (type == "chessboard") {  // chessboard.cpp:18-32
+      t.kind = TEX_CHESS;
+      M4f toUV = M4f::Identity();
+      if (const JValue* n = v.get("to_uv")) toUV = Transform(*n);
+      Xf check(toUV);  // Transform(toUV) inverts the matrix
+      for (int i = 0; i < 16; i++) t.toUV[i] = toUV.m[i / 4][i % 4];
+      const JValue* a = v.get("color_a");
+      const JValue* b = v.get("color_b");
+      JValue da, db;
+      da.type = db.type = JValue::kNum;
+      da.n = 0.4f;
+      db.n = 0.2f;
+      t.childA = AddTexture(a ? *a : da, channels, env);
+      t.childB = AddTexture(b ? *b : db, channels, env);
+      t.remap = RB(&v, "remap", false) ? 1u : 0u;
+    } else {
+      throw FactoryError("cannot find factory: " + type);
+    }
+  }
+  hs.tex[index] = t;
+  return index;
+}
+
+// Texture::Read averaged over the texels as Plastic's constructor does
+// (plastic.cpp:29-42): constant -> its value, bitmap -> level 0, chessboard ->
+// Read() returns 0 (chessboard.cpp:60-62).
+double MeanLuminance(const HostScene& hs, uint32_t id) {
+  const TexRec& t = hs.tex[id];
+  auto lum = [](const float* c) { return (c[0] * 0.212671f) + (c[1] * 0.715160f) + (c[2] * 0.072169f); };
+  if (t.kind == TEX_CONST) return (double)lum(t.value) / 1.0;
+  if (t.kind == TEX_CHESS) return 0.0;
+  double sum = 0;
+  const float* p = hs.texels.data() + t.levelOffset[0];
+  for (uint32_t y = 0; y < t.height; y++)
+    for (uint32_t x = 0; x < t.width; x++) sum += lum(p + ((size_t)y * t.width + x) * 3);
+  return sum / (double)(t.height * t.width);
+}
+
+// ---- BSDF records
+// Parameter reader for one BSDF record: constants go into p[], textured
+// parameters become TexBind entries (their p[] slots are filled per lookup).
+struct MatParams {
+  MatRec& m;
+  TexEnv* env;
+  std::vector<TexBind> binds;
+  uint32_t Tex(const JValue& v, int channels) {
+    if (!env || !env->hs) throw FactoryError("textured parameters need a scene");
+    return AddTexture(v, channels, *env);
+  }
+  void Bind(int slot, int channels, uint32_t tex, bool clamp01 = false) {
+    TexBind b;
+    b.slot = (uint16_t)slot;
+    b.channels = (uint8_t)channels;
+    b.clamp01 = clamp01 ? 1 : 0;
+    b.tex = tex;
+    binds.push_back(b);
+  }
+  // returns the texture index of a textured parameter, or -1
+  int64_t Color(const JValue* c, const char* k, F3 def, int slot) {
+    const JValue* v = c ? c->get(k) : nullptr;
+    F3 x = def;
+    if (v && !(v->isNum() || v->isArr())) {
+      uint32_t t = Tex(*v, 3);
+      Bind(slot, 3, t);
+      return t;
+    }
+    if (v) x = Vec3(*v, k);
+    m.p[slot] = x.x;
+    m.p[slot + 1] = x.y;
+    m.p[slot + 2] = x.z;
+    return -1;
+  }
+  int64_t Mono(const JValue* c, const char* k, float def, int slot, bool clamp01 = false) {
+    const JValue* v = c ? c->get(k) : nullptr;
+    if (v && !v->isNum()) {
+      uint32_t t = Tex(*v, 1);
+      Bind(slot, 1, t, clamp01);
+      return t;
+    }
+    float x = v ? (float)v->n : def;
+    if (clamp01) x = x < 0.f ? 0.f : (1.f < x ? 1.f : x);
+    m.p[slot] = x;
+    return -1;
+  }
+  // microfacet distribution (rough_metal.cpp:30-45, rough_glass.cpp:35-50)
+  void Dist(const JValue* c) {
+    std::string dist = RS(c, "distribution", "ggx");
+    m.p[11] = dist == "beckmann" ? 0.f : 1.f;  // unknown names fall back to GGX
+    if (c && c->has("alpha")) {
+      int64_t t = Mono(c, "alpha", 0.1f, 9);
+      if (t >= 0) Bind(10, 1, (uint32_t)t);
+      else m.p[10] = m.p[9];
+    } else {
+      Mono(c, "alpha_u", 0.1f, 9);
+      Mono(c, "alpha_v", 0.1f, 10);
+    }
+    m.p[12] = RB(c, "sample_visible", true) ? 1.f : 0.f;
+  }
+};
 bool DisneyHas(const JValue* c, const char* k) {  // disney.cpp:459-471
   const JValue* v = c ? c->get(k) : nullptr;
   if (!v) return false;
@@ -399,42 +631,38 @@ int WrapDepth(const std::vector<MatRec>& v, uint32_t i) {
   return 0;
 }
 
-uint32_t AddMaterial(const JValue* c, std::vector<MatRec>& out) {
+uint32_t AddMaterial(const JValue* c, std::vector<MatRec>& out, TexEnv* env) {
   MatRec m;
   std::memset(&m, 0, sizeof(m));
   std::string type = c ? TypeOf(*c) : std::string("diffuse");
   uint32_t index = (uint32_t)out.size();
   out.push_back(m);
-  auto put3 = [&](int at, F3 v) {
-    m.p[at] = v.x;
-    m.p[at + 1] = v.y;
-    m.p[at + 2] = v.z;
-  };
-  if (type == "diffuse") {  // diffuse.cpp:48-51
+  MatParams P{m, env, {}};
+  if (type == "diffuse") {  // diffuse.cpp:40-43
     m.kind = MAT_DIFFUSE;
     m.flags = BT_DIFFUSE | BT_REFLECTION;
-    put3(0, Color(c, "reflectance", F3(0.5f, 0.5f, 0.5f)));
+    P.Color(c, "reflectance", F3(0.5f, 0.5f, 0.5f), 0);
   } else if (type == "rough_metal") {  // rough_metal.cpp:24-43
     m.kind = MAT_ROUGH_METAL;
     m.flags = BT_GLOSSY | BT_REFLECTION;
-    put3(0, Color(c, "reflectance", F3(1, 1, 1)));
-    put3(3, Color(c, "eta", F3(0.1999899f, 0.9220823f, 1.0998751f)));
-    put3(6, Color(c, "k", F3(3.9046354f, 2.4476316f, 2.1376500f)));
-    SetDist(c, m);
+    P.Color(c, "reflectance", F3(1, 1, 1), 0);
+    P.Color(c, "eta", F3(0.1999899f, 0.9220823f, 1.0998751f), 3);
+    P.Color(c, "k", F3(3.9046354f, 2.4476316f, 2.1376500f), 6);
+    P.Dist(c);
   } else if (type == "rough_glass") {  // rough_glass.cpp:24-47
     m.kind = MAT_ROUGH_GLASS;
     m.flags = BT_GLOSSY | BT_REFLECTION | BT_TRANSMISSION;
-    put3(0, Color(c, "reflectance", F3(1, 1, 1)));
-    put3(3, Color(c, "transmittance", F3(1, 1, 1)));
+    P.Color(c, "reflectance", F3(1, 1, 1), 0);
+    P.Color(c, "transmittance", F3(1, 1, 1), 3);
     float intIor = RF(c, "int_ior", 1.5046f);
     float extIor = RF(c, "ext_ior", 1.000277f);
     m.p[6] = intIor / extIor;
     m.p[7] = extIor / intIor;
-    SetDist(c, m);
+    P.Dist(c);
   } else if (type == "disney") {  // disney.cpp:62-111
     m.kind = MAT_DISNEY;
-    put3(0, Color(c, "base_color", F3(0.5f, 0.5f, 0.5f)));
-    m.p[3] = Mono(c, "roughness", 0.5f);
+    P.Color(c, "base_color", F3(0.5f, 0.5f, 0.5f), 0);
+    P.Mono(c, "roughness", 0.5f, 3);
     const char* keys[] = {"anisotropic", "spec_trans", "sheen", "sheen_tint", "flatness", "spec_tint", "metallic",
                           "clearcoat"};
     const uint32_t fl[] = {DF_ANISO, DF_SPECTRANS, DF_SHEEN, DF_SHEENTINT, DF_FLATNESS, DF_SPECTINT, DF_METALLIC,
@@ -442,9 +670,9 @@ uint32_t AddMaterial(const JValue* c, std::vector<MatRec>& out) {
     const int slot[] = {4, 5, 6, 7, 8, 9, 10, 11};
     for (int k = 0; k < 8; k++) {
       if (DisneyHas(c, keys[k])) m.dflags |= fl[k];
-      m.p[slot[k]] = Mono(c, keys[k], 0.f);
+      P.Mono(c, keys[k], 0.f, slot[k]);
     }
-    m.p[12] = Mono(c, "clearcoat_gloss", 0.f);
+    P.Mono(c, "clearcoat_gloss", 0.f, 12);
     m.p[14] = RF(c, "main_specular_sampling_rate", 1.f);
     m.p[15] = RF(c, "clearcoat_sampling_rate", 1.f);
     m.aux = RF(c, "diffuse_reflectance_sampling_rate", 1.f);
@@ -467,60 +695,73 @@ uint32_t AddMaterial(const JValue* c, std::vector<MatRec>& out) {
   } else if (type == "perfect_mirror") {  // perfect_mirror.cpp:19-25
     m.kind = MAT_PERFECT_MIRROR;
     m.flags = BT_DELTA | BT_REFLECTION;
-    put3(0, Color(c, "reflectance", F3(1, 1, 1)));
-    put3(3, Color(c, "eta", F3(0, 0, 0)));
-    put3(6, Color(c, "k", F3(1, 1, 1)));
+    P.Color(c, "reflectance", F3(1, 1, 1), 0);
+    P.Color(c, "eta", F3(0, 0, 0), 3);
+    P.Color(c, "k", F3(1, 1, 1), 6);
   } else if (type == "perfect_glass") {  // perfect_glass.cpp:19-26
     m.kind = MAT_PERFECT_GLASS;
     m.flags = BT_DELTA | BT_REFLECTION | BT_TRANSMISSION;
-    put3(0, Color(c, "reflectance", F3(1, 1, 1)));
-    put3(3, Color(c, "transmittance", F3(1, 1, 1)));
+    P.Color(c, "reflectance", F3(1, 1, 1), 0);
+    P.Color(c, "transmittance", F3(1, 1, 1), 3);
     m.p[6] = RF(c, "int_ior", 1.5046f) / RF(c, "ext_ior", 1.000277f);
   } else if (type == "plastic" || type == "rough_plastic") {  // plastic.cpp:18-44, rough_plastic.cpp:20-56
     bool rough = type == "rough_plastic";
     m.kind = rough ? MAT_ROUGH_PLASTIC : MAT_PLASTIC;
     m.flags = BT_DIFFUSE | BT_REFLECTION | BT_DELTA;
     float eta = RF(c, "int_ior", 1.49f) / RF(c, "ext_ior", 1.000277f);
-    F3 diff = Color(c, "diffuse", F3(0.5f, 0.5f, 0.5f));
-    F3 spec = Color(c, "specular", F3(1, 1, 1));
-    put3(0, diff);
-    put3(3, spec);
+    int64_t td = P.Color(c, "diffuse", F3(0.5f, 0.5f, 0.5f), 0);
+    int64_t ts = P.Color(c, "specular", F3(1, 1, 1), 3);
     m.p[6] = eta;
     m.p[7] = 1.f / (eta * eta);
     m.p[8] = DiffuseReflectance(1.f / eta);
-    // mean luminance of each (constant, 1x1) texture, accumulated in double
-    double diffMean = (double)LuminanceF(diff) / 1.0, specMean = (double)LuminanceF(spec) / 1.0;
+    // mean luminance over each texture's texels, accumulated in double
+    double diffMean = td >= 0 ? MeanLuminance(*env->hs, (uint32_t)td) : (double)LuminanceF(F3(m.p[0], m.p[1], m.p[2])) / 1.0;
+    double specMean = ts >= 0 ? MeanLuminance(*env->hs, (uint32_t)ts) : (double)LuminanceF(F3(m.p[3], m.p[4], m.p[5])) / 1.0;
     m.p[13] = (float)(specMean / (diffMean + specMean));
     m.p[14] = RB(c, "no_linear", false) ? 1.f : 0.f;
     if (rough) {
       std::string dist = RS(c, "distribution", "ggx");
       m.p[11] = dist == "beckmann" ? 0.f : 1.f;  // unknown names fall back to GGX (rough_plastic.cpp:31-38)
-      m.p[9] = m.p[10] = Mono(c, "alpha", 0.1f);
+      int64_t t = P.Mono(c, "alpha", 0.1f, 9);
+      if (t >= 0) P.Bind(10, 1, (uint32_t)t);
+      else m.p[10] = m.p[9];
       m.p[12] = RB(c, "sample_visible", true) ? 1.f : 0.f;
     }
   } else if (type == "mask") {  // mask.cpp:12-21
     m.kind = MAT_MASK;
-    float op = Mono(c, "opacity", 0.5f);
-    m.p[0] = op < 0.f ? 0.f : (1.f < op ? 1.f : op);  // EvalOpacity clamps (mask.cpp:63-65)
+    P.Mono(c, "opacity", 0.5f, 0, true);  // EvalOpacity clamps (mask.cpp:66-68)
     if (!c->has("nested")) throw ConfigError("mask needs a nested bsdf");
-    m.ref0 = AddMaterial(c->get("nested"), out);
+    m.ref0 = AddMaterial(c->get("nested"), out, env);
     m.flags = out[m.ref0].flags;
   } else if (type == "two_side") {  // two_side.cpp:18-62
     m.kind = MAT_TWO_SIDE;
     if (c->has("two_side")) {
-      m.ref0 = m.ref1 = AddMaterial(c->get("two_side"), out);
+      m.ref0 = m.ref1 = AddMaterial(c->get("two_side"), out, env);
     } else {
       if (!c->has("out_side") || !c->has("in_side")) throw ConfigError("config must contains out_side and in_side");
-      m.ref0 = AddMaterial(c->get("out_side"), out);
-      m.ref1 = AddMaterial(c->get("in_side"), out);
+      m.ref0 = AddMaterial(c->get("out_side"), out, env);
+      m.ref1 = AddMaterial(c->get("in_side"), out, env);
     }
     m.flags = out[m.ref0].flags | out[m.ref1].flags;
   } else {
     throw FactoryError("cannot find factory: " + type);
   }
+  if (!P.binds.empty()) {
+    m.texFirst = (uint32_t)env->hs->texBind.size();
+    m.texCount = (uint32_t)P.binds.size();
+    env->hs->texBind.insert(env->hs->texBind.end(), P.binds.begin(), P.binds.end());
+  }
   out[index] = m;
   if (WrapDepth(out, index) > kMaxBsdfNest) throw ConfigError("two_side / mask BSDFs nest more than 4 levels deep");
   return index;
+}
+// true when material i or a material it wraps has textured parameters
+bool HasTextures(const std::vector<MatRec>& v, uint32_t i) {
+  const MatRec& m = v[i];
+  if (m.texCount) return true;
+  if (m.kind == MAT_TWO_SIDE) return HasTextures(v, m.ref0) || HasTextures(v, m.ref1);
+  if (m.kind == MAT_MASK) return HasTextures(v, m.ref0);
+  return false;
 }
 
 // ---- camera (perspective.cpp:15-70, math_ext.h:65-75)
@@ -578,6 +819,15 @@ CameraRec MakeCamera(const JValue& c) {
     cam.clipToCamera[i] = toClip.l.m[i / 4][i % 4];
     cam.camToWorld[i] = camToWorld.w.m[i / 4][i % 4];
   }
+  F3 o = Xf::Aff(toClip.l, F3(0, 0, 0));
+  F3 dx = Xf::Aff(toClip.l, F3(1.f / cam.width, 0, 0)) - o;
+  F3 dy = Xf::Aff(toClip.l, F3(0, 1.f / cam.height, 0)) - o;
+  cam.dx[0] = dx.x;
+  cam.dx[1] = dx.y;
+  cam.dx[2] = dx.z;
+  cam.dy[0] = dy.x;
+  cam.dy[1] = dy.y;
+  cam.dy[2] = dy.z;
   return cam;
 }
 
@@ -635,7 +885,7 @@ bool InvertM4f(const M4f& a, M4f& out) {
 
 void BuildMaterialRecords(const JValue& bsdf, std::vector<MatRec>& out) {
   out.clear();
-  AddMaterial(&bsdf, out);
+  AddMaterial(&bsdf, out, nullptr);
 }
 
 static MediumRec MakeMedium(const JValue& c, const M4f& toWorld, const std::map<std::string, VolData>& vols,
@@ -747,6 +997,8 @@ void BuildHostScene(const std::string& json, const std::string& baseDir, HostSce
   if (!root.isObj()) throw ConfigError("scene root must be an object");
   std::map<std::string, ObjData> objs;
   std::map<std::string, VolData> vols;
+  std::map<std::string, ImageAsset> images;
+  TexEnv env{&hs, &images};
   if (const JValue* an = root.get("assets")) {  // asset.cpp:17-38
     if (!an->isArr()) throw ConfigError("assets must be an array");
     for (const JValue& a : an->a) {
@@ -755,6 +1007,8 @@ void BuildHostScene(const std::string& json, const std::string& baseDir, HostSce
         objs[name] = LoadObj(Join(baseDir, loc));
       } else if (type == "volume_data_mitsuba_vol") {
         vols[name] = LoadVol(Join(baseDir, loc));
+      } else if (type == "image_default" || type == "image_hdr" || type == "image_exr") {
+        images[name] = LoadImageAsset(a, type, Join(baseDir, loc));
       } else {
         throw FactoryError("cannot find factory: " + type);
       }
@@ -780,7 +1034,7 @@ void BuildHostScene(const std::string& json, const std::string& baseDir, HostSce
       const JValue* def = v.get("bsdf");
       if (!def) throw ConfigError("no child: bsdf");
       if (bsdfVars.count(name)) throw ConfigError("duplicate bsdf var name: " + name);
-      bsdfVars[name] = AddMaterial(def, hs.mats);
+      bsdfVars[name] = AddMaterial(def, hs.mats, &env);
     }
   }
   const JValue* sceneNode = root.get("scene");
@@ -1015,7 +1269,7 @@ void BuildHostScene(const std::string& json, const std::string& baseDir, HostSce
         if (it == bsdfVars.end()) throw ConfigError("unknown bsdf var: " + ref->s);
         bsdfIdx = (int)it->second;
       } else {
-        bsdfIdx = (int)AddMaterial(bn, hs.mats);
+        bsdfIdx = (int)AddMaterial(bn, hs.mats, &env);
       }
     }
     int inMed = -1, outMed = -1;
@@ -1033,7 +1287,7 @@ void BuildHostScene(const std::string& json, const std::string& baseDir, HostSce
         outMed = (int)hs.media.size() - 1;
       }
     }
-    if (lightIdx >= 0 && shapeIdx >= 0 && bsdfIdx < 0) bsdfIdx = (int)AddMaterial(nullptr, hs.mats);  // :243-246
+    if (lightIdx >= 0 && shapeIdx >= 0 && bsdfIdx < 0) bsdfIdx = (int)AddMaterial(nullptr, hs.mats, &env);  // :243-246
     if (shapeIdx >= 0) {
       ShapeRec& sh = hs.shapes[shapeIdx];
       sh.light = lightIdx;
@@ -1073,6 +1327,8 @@ void BuildHostScene(const std::string& json, const std::string& baseDir, HostSce
         uint32_t a = hs.mats[m.ref0].kind, b = hs.mats[m.ref1].kind;
         kind = (a == b && a != MAT_TWO_SIDE) ? a : MAT_NONE;
       }
+      // textured materials are shaded by the generic class, which evaluates textures
+      if (HasTextures(hs.mats, (uint32_t)sh.bsdf)) kind = MAT_NONE;
       cls = (kind >= MAT_DIFFUSE && kind <= MAT_DISNEY) ? (uint8_t)kind : (uint8_t)SC_GENERIC;
     }
     hs.shapeClass.push_back(cls);

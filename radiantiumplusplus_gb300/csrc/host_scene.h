@@ -45,6 +45,10 @@ struct HostScene {
   std::vector<float> rectToObject;  // per rect shape: 12 floats (world -> object rows)
   std::vector<uint32_t> rectIndexOfShape;
   std::vector<uint8_t> shapeClass;  // see records.h SC_*
+  std::vector<TexRec> tex;          // textures, in creation order
+  std::vector<float> texels;        // mip chains of the bitmap textures
+  std::vector<TexBind> texBind;     // textured BSDF parameters
+  bool needDiff = false;            // a trilinear / anisotropic bitmap is in use
   int envLight = -1, globalMedium = -1;
   float lightPdf = 0.f;
   uint64_t nPrims = 0;

@@ -86,7 +86,26 @@ __global__ void KCamera(DevScene S, const uint32_t* pix, int64_t n, uint32_t sam
   o[7] = tmax;
 }
 
+// Texture<T>::Eval at given uv and uv derivatives (texture.h:57-62).
+__global__ void KTexEval(DevScene S, uint32_t tex, const float* uv, const float* duv, int64_t n, float* out) {
+  int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  TexCtx x{S.tex, S.texels, S.texBind, V2{uv[2 * i], uv[2 * i + 1]}, V2{duv[4 * i], duv[4 * i + 1]},
+           V2{duv[4 * i + 2], duv[4 * i + 3]}};
+  TexVal v = TexEval(x, tex, x.uv);
+  out[3 * i] = v.c[0];
+  out[3 * i + 1] = v.c[1];
+  out[3 * i + 2] = v.c[2];
+}
+
 static unsigned Blocks(int64_t n, int b) { return (unsigned)((n + b - 1) / b); }
+
+cudaError_t LaunchTexEval(const DevScene& S, uint32_t tex, const float* uv, const float* duv, int64_t n, float* out,
+                          cudaStream_t st) {
+  if (n <= 0) return cudaSuccess;
+  KTexEval<<<Blocks(n, 128), 128, 0, st>>>(S, tex, uv, duv, n, out);
+  return cudaGetLastError();
+}
 
 cudaError_t LaunchBsdfEval(const MatRec* mats, const float* wi, const float* wo, int64_t n, float* f, float* pdf,
                            cudaStream_t st) {

@@ -76,7 +76,9 @@ __global__ void __launch_bounds__(kBlock) KGenerate(DevScene S, PathBuffers B, W
   B.rayD[i] = make_float4(D.x, D.y, D.z, tmax);
   B.thr[i] = make_float4(1.f, 1.f, 1.f, 1.f);
   B.L[i] = make_float4(0.f, 0.f, 0.f, 1.f);
-  B.prev[i] = make_float4(0.f, 0.f, 0.f, __uint_as_float(1u));
+  // the first shading point has no previous vertex: the slot carries the screen
+  // position, from which textured materials rebuild the camera ray differentials
+  B.prev[i] = make_float4((float)x + jx, (float)y + jy, 0.f, __uint_as_float(1u));
   B.rng[i] = make_uint2((uint32_t)rng.state, (uint32_t)(rng.state >> 32));
   B.pixel[i] = pix;
   B.q[0][i] = i;
@@ -191,7 +193,7 @@ template <int K>
 __device__ __forceinline__ bool GuidedScatter(const DevScene& S, const PathBuffers& B, const GuideDev& G, int depth,
                                               uint32_t p, const SurfInt& si, V3 D, const MatRec* mats, uint32_t bsdf,
                                               const float4* gmix, float gc, V3 thr, float eta, Pcg32& rng,
-                                              bool shadow, float4& shC) {
+                                              bool shadow, float4& shC, const TexCtx* tc) {
   float us = Next1D(rng);
   float xl = Next1D(rng);
   V2 xd = Next2D(rng);
@@ -201,11 +203,11 @@ __device__ __forceinline__ bool GuidedScatter(const DevScene& S, const PathBuffe
   if (us < gc) {
     wiW = GuideMixSamplePacked(gmix, xl, xd);
     V3 wl = ToLocal(si.sh, wiW);
-    ClassEvalPdf<K>(mats, bsdf, si.Wi, wl, f, bpdf);
+    ClassEvalPdf<K>(mats, bsdf, si.Wi, wl, f, bpdf, tc);
     pm = gc * GuideMixPdfPacked(gmix, wiW) + (1.f - gc) * bpdf;
     ok = pm > 0.f && !is_zero(f);
   } else {
-    BsdfSampleRes bs = ClassSample<K>(mats, bsdf, si.Wi, xl, xd);
+    BsdfSampleRes bs = ClassSample<K>(mats, bsdf, si.Wi, xl, xd, tc);
     f = bs.f;
     bpdf = bs.pdf;
     etaS = bs.eta;
@@ -318,6 +320,21 @@ __global__ void __launch_bounds__(kBlock) KShadeClass(DevScene S, PathBuffers B,
         SurfInt si = ComputeSI(S, O, D, th);
         uint32_t bsdf = (uint32_t)S.shapes[h.shape].bsdf;
         const MatRec* mats = S.mats;
+        // textured materials are all in the generic class: uv (and, on camera
+        // rays, uv derivatives) for their lookups
+        TexCtx tcx;
+        const TexCtx* tc = nullptr;
+        if constexpr (K == SC_GENERIC) {
+          if (S.nTex) {
+            SurfUV su = ComputeUV(S, th, si);
+            tcx = TexCtx{S.tex, S.texels, S.texBind, su.uv, V2{0.f, 0.f}, V2{0.f, 0.f}};
+            if (depth == 0 && S.needDiff) {
+              float4 pv = B.prev[p];
+              CameraUVDerivs(S.cam, pv.x, pv.y, O, si, su, tcx.duvdx, tcx.duvdy);
+            }
+            tc = &tcx;
+          }
+        }
         const float4* gmix = nullptr;
         float gc = 0.f;
         if constexpr (GUIDED) {
@@ -334,7 +351,7 @@ __global__ void __launch_bounds__(kBlock) KShadeClass(DevScene S, PathBuffers B,
             V3 wo = ToLocal(si.sh, dsr.Dir);
             V3 f;
             float bsdfPdf;
-            ClassEvalPdf<K>(mats, bsdf, si.Wi, wo, f, bsdfPdf);
+            ClassEvalPdf<K>(mats, bsdf, si.Wi, wo, f, bsdfPdf, tc);
             if constexpr (GUIDED) bsdfPdf = gc * GuideMixPdfPacked(gmix, dsr.Dir) + (1.f - gc) * bsdfPdf;
             // Scene::IsOcclude (scene.cpp:53-63)
             V3 so = OffsetP(si.P, si.N, dsr.P - si.P);
@@ -352,11 +369,11 @@ __global__ void __launch_bounds__(kBlock) KShadeClass(DevScene S, PathBuffers B,
           }
         }
         if constexpr (GUIDED) {
-          keep = GuidedScatter<K>(S, B, G, depth, p, si, D, mats, bsdf, gmix, gc, thr, eta, rng, shadow, shC);
+          keep = GuidedScatter<K>(S, B, G, depth, p, si, D, mats, bsdf, gmix, gc, thr, eta, rng, shadow, shC, tc);
         } else {
         float xl = Next1D(rng);
         V2 xd = Next2D(rng);
-        BsdfSampleRes bs = ClassSample<K>(mats, bsdf, si.Wi, xl, xd);
+        BsdfSampleRes bs = ClassSample<K>(mats, bsdf, si.Wi, xl, xd, tc);
         if (bs.pdf > 0.f) {
           thr = cmul(thr, bs.f) / bs.pdf;
           eta *= bs.eta;

@@ -69,7 +69,7 @@ RD float VMis(float a, float b) {
   return isfinite(w) ? w : 0.f;
 }
 
-RD bool VTrace(const DevScene& S, const VRay& ray, SurfInt& si, uint32_t* err) {
+RD bool VTrace(const DevScene& S, const VRay& ray, SurfInt& si, uint32_t* err, V2* uv) {
   RayPre r = MakeRayPre(ray.O, ray.D, ray.MinT);
   TraceHit h;
   if (!TraceBvh8<false>(S, r, ray.MaxT, h, err)) {
@@ -82,6 +82,7 @@ RD bool VTrace(const DevScene& S, const VRay& ray, SurfInt& si, uint32_t* err) {
     return false;
   }
   si = ComputeSI(S, ray.O, ray.D, h);
+  if (uv) *uv = ComputeUV(S, h, si).uv;
   return true;
 }
 
@@ -94,12 +95,15 @@ RD VRay Spawn(V3 P, V3 N, V3 d) { return VRay{OffsetP(P, N, d), d, 0.f, kFloatMa
 #else
 #define RDN __device__ __noinline__
 #endif
-RDN bool VTraceCall(const DevScene& S, const VRay& ray, SurfInt& si, uint32_t* err) { return VTrace(S, ray, si, err); }
-RDN void VBsdfEvalPdf(const MatRec* mats, uint32_t b, V3 wi, V3 wo, V3& f, float& pdf) {
-  BsdfEvalPdf(mats, b, wi, wo, f, pdf);
+// uv: where to put the hit's texture coordinates, or null.
+RDN bool VTraceCall(const DevScene& S, const VRay& ray, SurfInt& si, uint32_t* err, V2* uv) {
+  return VTrace(S, ray, si, err, uv);
 }
-RDN BsdfSampleRes VBsdfSample(const MatRec* mats, uint32_t b, V3 wi, float xl, V2 xd) {
-  return BsdfSample(mats, b, wi, xl, xd);
+RDN void VBsdfEvalPdf(const MatRec* mats, uint32_t b, V3 wi, V3 wo, V3& f, float& pdf, const TexCtx* tc) {
+  BsdfEvalPdf(mats, b, wi, wo, f, pdf, tc);
+}
+RDN BsdfSampleRes VBsdfSample(const MatRec* mats, uint32_t b, V3 wi, float xl, V2 xd, const TexCtx* tc) {
+  return BsdfSample(mats, b, wi, xl, xd, tc);
 }
 
 RD int MediumOfHit(const DevScene& S, const SurfInt& si, V3 D) {
@@ -140,7 +144,7 @@ RDN V3 VolSampleLight(const DevScene& S, Pcg32& rng, int medium, int channel, V3
       MedInt mei = SampleInteraction<BRICKS, HALF>(S, md, ray, Next1D(rng), channel);
       if (md.kind == MED_HOMOGENEOUS && mei.T != kInf) ray.MaxT = fminr(mei.T, remainingDist);
       if (needsIntersection) {
-        VTraceCall(S, ray, si, err);
+        VTraceCall(S, ray, si, err, nullptr);
         nRays++;
       }
       if (si.T < mei.T) mei.T = kInf;
@@ -177,7 +181,7 @@ RDN V3 VolSampleLight(const DevScene& S, Pcg32& rng, int medium, int channel, V3
     }
     bool intersect = activeSurface && needsIntersection;
     if (intersect) {
-      VTraceCall(S, ray, si, err);
+      VTraceCall(S, ray, si, err, nullptr);
       nRays++;
     }
     needsIntersection = needsIntersection && !intersect;
@@ -286,7 +290,7 @@ RD bool VolTop(const DevScene& S, VolPathState& p, uint32_t mode, uint32_t* err)
   MedInt mei = SampleInteraction<BRICKS, HALF>(S, md, ray, Next1D(rng), channel);
   if (md.kind == MED_HOMOGENEOUS && mei.T != kInf) ray.MaxT = mei.T;
   if (!(BRICKS && p.siValid)) {
-    VTraceCall(S, ray, si, err);
+    VTraceCall(S, ray, si, err, nullptr);
     p.nRays++;
   }
   p.siValid = false;
@@ -369,7 +373,17 @@ RD bool VolSurface(const DevScene& S, VolPathState& p, uint32_t mode, uint32_t* 
   VRay& ray = p.ray;
   SurfInt& si = p.si;
   V3& thr = p.thr;
-  bool hit = VTraceCall(S, ray, si, err);
+  // texture coordinates of the hit, for scenes with textures (vol_path traces
+  // plain rays: no differentials, uv derivatives 0)
+  const bool textured = S.nTex != 0u;
+  V2 uvHit;
+  bool hit = VTraceCall(S, ray, si, err, textured ? &uvHit : nullptr);
+  TexCtx tcx;
+  const TexCtx* tc = nullptr;
+  if (textured && hit) {
+    tcx = TexCtx{S.tex, S.texels, S.texBind, uvHit, V2{0.f, 0.f}, V2{0.f, 0.f}};
+    tc = &tcx;
+  }
   p.nRays++;
   int hitLight = hit ? S.shapes[si.shape].light : S.envLight;
   if (hitLight >= 0) {
@@ -406,14 +420,14 @@ RD bool VolSurface(const DevScene& S, VolPathState& p, uint32_t mode, uint32_t* 
       V3 wo = ToLocal(si.sh, dsr.Dir);
       V3 f;
       float bsdfPdf;
-      VBsdfEvalPdf(mats, (uint32_t)shp.bsdf, si.Wi, wo, f, bsdfPdf);
+      VBsdfEvalPdf(mats, (uint32_t)shp.bsdf, si.Wi, wo, f, bsdfPdf, tc);
       float weight = dsr.IsDelta ? 1.f : VMis(dsr.Pdf, bsdfPdf);
       p.result = p.result + cmul(cmul(thr, f), li) * weight / dsr.Pdf;
     }
   }
   float xl = Next1D(p.rng);
   V2 xd = Next2D(p.rng);
-  BsdfSampleRes bs = VBsdfSample(mats, (uint32_t)shp.bsdf, si.Wi, xl, xd);
+  BsdfSampleRes bs = VBsdfSample(mats, (uint32_t)shp.bsdf, si.Wi, xl, xd, tc);
   if (bs.pdf <= 0.f) return false;
   thr = cmul(thr, bs.f) / bs.pdf;
   p.eta *= bs.eta;

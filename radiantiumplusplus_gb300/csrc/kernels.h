@@ -49,6 +49,8 @@ struct FilmView {
 };
 
 // ---- parity kernels (k_parity.cu)
+cudaError_t LaunchTexEval(const DevScene& S, uint32_t tex, const float* uv, const float* duv, int64_t n, float* out,
+                          cudaStream_t st);
 cudaError_t LaunchBsdfEval(const MatRec* mats, const float* wi, const float* wo, int64_t n, float* f, float* pdf,
                            cudaStream_t st);
 cudaError_t LaunchBsdfSample(const MatRec* mats, const float* wi, const float* u, int64_t n, float* wo, float* pdf,

@@ -46,12 +46,44 @@ struct alignas(16) MatRec {
   uint32_t dflags;     // Disney present flags
   uint32_t ref0, ref1; // two_side / mask children
   float aux;           // disney: diffuse_reflectance_sampling_rate
-  uint32_t pad[2];
+  uint32_t texFirst;   // textured parameters: first TexBind of this record
+  uint32_t texCount;   //   and their number (0: all parameters constant)
   float p[16];
 };
 static_assert(sizeof(MatRec) == 96, "MatRec must stay 96 bytes");
 // Deepest chain of wrapper BSDFs (two_side, mask) above a leaf BSDF.
 constexpr int kMaxBsdfNest = 4;
+
+// ---------------------------------------------------------------- textures
+// Texture records (texture.h:47-90, bitmap.cpp:24-344, chessboard.cpp:15-63).
+// A constant texture holds its value; a bitmap holds its mip chain in the texel
+// pool (level l: max(1, w >> l) x max(1, h >> l) texels of `channels` floats, rows
+// of increasing y, from levelOffset[l]); a chessboard holds its uv transform and
+// the two textures it picks between.
+enum TexKind : uint32_t { TEX_CONST = 0, TEX_BITMAP = 1, TEX_CHESS = 2 };
+enum TexFilter : uint32_t { TF_NEAREST = 0, TF_BILINEAR = 1, TF_TRILINEAR = 2, TF_ANISO = 3 };
+constexpr int kMaxMipLevels = 16;
+constexpr int kMaxTexNest = 8;  // deepest chessboard chain above a leaf texture
+struct alignas(16) TexRec {
+  uint32_t kind, channels, filter, wrap;  // wrap: 0 clamp, 1 repeat
+  uint32_t width, height, levels, remap;
+  float value[3];
+  float aniso;                            // anisotropic_level
+  uint32_t childA, childB, pad[2];
+  union {
+    uint32_t levelOffset[kMaxMipLevels];  // bitmap: first float of each level
+    float toUV[16];                       // chessboard: uv transform, row-major 4x4
+  };
+};
+static_assert(sizeof(TexRec) == 128, "TexRec size");
+// One textured BSDF parameter: p[slot .. slot+channels) comes from texture `tex`.
+struct TexBind {
+  uint16_t slot;
+  uint8_t channels;
+  uint8_t clamp01;  // mask opacity is clamped to [0, 1] after the lookup (mask.cpp:66-68)
+  uint32_t tex;
+};
+static_assert(sizeof(TexBind) == 8, "TexBind size");
 
 // ---------------------------------------------------------------- shapes
 enum ShapeKind : uint32_t { SHAPE_MESH = 0, SHAPE_RECT = 1, SHAPE_SPHERE = 2 };
@@ -113,6 +145,7 @@ struct alignas(16) CameraRec {
   float camToWorld[16];    // cameraToWorld.ToWorld
   float nearZ, farZ;
   int32_t width, height;
+  float dx[4], dy[4];      // camera-space offsets of one pixel step (perspective.cpp:56-59)
 };
 
 // ---------------------------------------------------------------- BVH8
@@ -164,8 +197,12 @@ struct DevScene {
   const uint16_t* volumeHalf;  // fp16 copy of the density grids (bit patterns)
   const float* brickMaj;       // per-medium 16^3-brick majorants (scale applied)
   const uint8_t* shapeClass;   // shade class per shape
+  const TexRec* tex;           // textures
+  const float* texels;         // texel pool
+  const TexBind* texBind;      // textured BSDF parameters
   uint32_t nNodes, nPrims, nShapes, nLights;
   uint32_t nMedia, nMats;
+  uint32_t nTex, needDiff;     // needDiff: a trilinear / anisotropic texture reads ray differentials
   int32_t envLight, globalMedium;
   float lightPdf;
   int32_t maxDepth, rrDepth, isVol;

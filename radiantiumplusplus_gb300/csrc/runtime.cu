@@ -756,6 +756,9 @@ uint64_t SceneUpload(const HostScene& hs, rad_scene* sc) {
   uint16_t* volHalf = DevAlloc<uint16_t>(hs.volume.size(), o, b);
   float* bricks = DevAlloc<float>(hs.brickMaj.size(), o, b);
   uint8_t* scls = DevAlloc<uint8_t>(hs.shapeClass.size(), o, b);
+  TexRec* tex = DevAlloc<TexRec>(hs.tex.size(), o, b);
+  float* texels = DevAlloc<float>(hs.texels.size(), o, b);
+  TexBind* tbind = DevAlloc<TexBind>(hs.texBind.size(), o, b);
   up(nodes, hs.nodes);
   up(prims, hs.prims);
   up(pinfo, hs.primInfo);
@@ -775,6 +778,9 @@ uint64_t SceneUpload(const HostScene& hs, rad_scene* sc) {
     Check(cudaDeviceSynchronize(), "sync");
   }
   up(scls, hs.shapeClass);
+  up(tex, hs.tex);
+  up(texels, hs.texels);
+  up(tbind, hs.texBind);
   D.nodes = nodes;
   D.prims = prims;
   D.primInfo = pinfo;
@@ -791,6 +797,11 @@ uint64_t SceneUpload(const HostScene& hs, rad_scene* sc) {
   D.volumeHalf = volHalf;
   D.brickMaj = bricks;
   D.shapeClass = scls;
+  D.tex = tex;
+  D.texels = texels;
+  D.texBind = tbind;
+  D.nTex = (uint32_t)hs.tex.size();
+  D.needDiff = hs.needDiff ? 1u : 0u;
   D.nNodes = (uint32_t)hs.nodes.size();
   D.nPrims = (uint32_t)hs.prims.size();
   D.nShapes = (uint32_t)hs.shapes.size();
@@ -1206,6 +1217,23 @@ int rad_camera_rays(rad_scene* scene, const uint32_t* pixels, int64_t n, uint32_
     Check(cudaMemcpyAsync(dp.p, pixels, 4 * n, cudaMemcpyHostToDevice, lib.stream), "copy");
     Check(LaunchCameraRays(scene->dev, dp.p, n, sample, seed, dr.p, lib.stream), "camera");
     Check(cudaMemcpyAsync(rays, dr.p, 32 * n, cudaMemcpyDeviceToHost, lib.stream), "copy");
+    Check(cudaStreamSynchronize(lib.stream), "sync");
+  });
+}
+
+int rad_scene_texture_eval(rad_scene* scene, uint32_t texture, const float* uv, const float* duv, int64_t n,
+                           float* out) {
+  if (!scene || n < 0 || (n > 0 && (!uv || !duv || !out))) return Fail(RAD_ERR_INVALID_ARG, "bad argument");
+  if (texture >= scene->dev.nTex) return Fail(RAD_ERR_INVALID_ARG, "texture index out of range");
+  if (n == 0) return RAD_OK;
+  return Guard([&] {
+    Lib& lib = L();
+    std::lock_guard<std::mutex> g(lib.gpuMu);
+    DevBuf<float> du(2 * n), dd(4 * n), dout(3 * n);
+    Check(cudaMemcpyAsync(du.p, uv, 8 * n, cudaMemcpyHostToDevice, lib.stream), "copy");
+    Check(cudaMemcpyAsync(dd.p, duv, 16 * n, cudaMemcpyHostToDevice, lib.stream), "copy");
+    Check(LaunchTexEval(scene->dev, texture, du.p, dd.p, n, dout.p, lib.stream), "texture eval");
+    Check(cudaMemcpyAsync(out, dout.p, 12 * n, cudaMemcpyDeviceToHost, lib.stream), "copy");
     Check(cudaStreamSynchronize(lib.stream), "sync");
   });
 }

@@ -31,6 +31,56 @@ def lights(dirpath, w=48, h=48, spp=4, seed=1):
     return write(dirpath, "lights_%dx%d_%d_%d" % (w, h, spp, seed), scenes.lights_room(w, h, spp, seed))
 
 
+def textured_room_scene(w=48, h=48, spp=4, seed=1, renderer="path"):
+    """Box room whose materials read textures of every kind: bitmaps from PNG
+    (RGB and mono), Radiance HDR and OpenEXR assets with nearest / bilinear /
+    trilinear / anisotropic filters and clamp / repeat wrapping, nested
+    chessboards, a textured mask opacity and textured microfacet roughness.
+    Returns (scene dict, {file name: bytes})."""
+    import imgenc
+    rng = np.random.default_rng(11)
+    yy, xx = np.mgrid[0:64, 0:64]
+    tiles = ((xx // 8 + yy // 8) % 2)[..., None] * np.array([180, 60, 40]) + rng.integers(0, 60, (64, 64, 3))
+    grain = (96 + 80 * np.sin(xx / 5.0) * np.cos(yy / 7.0))[..., None].astype(np.int64)
+    hdr_img = np.stack([0.2 + 0.6 * xx / 63, 0.3 + 0.0 * yy, 0.8 - 0.5 * yy / 63], axis=2)[:32, :48]
+    exr_img = {k: (0.3 + 0.6 * rng.random((16, 16))).astype(np.float16) for k in "RGB"}
+    assets = {"tiles.png": imgenc.png(tiles.clip(0, 255)), "grain.png": imgenc.png(grain.clip(0, 255)),
+              "sky.hdr": imgenc.hdr(hdr_img), "metal.exr": imgenc.exr(exr_img, 3)}
+    sc = scenes.box_room(w, h, spp, seed)
+    if renderer == "vol_path":
+        sc["renderer"] = {"type": "vol_path", "max_depth": 8, "rr_depth": 3}
+    sc["assets"] = [
+        {"name": "tiles", "type": "image_default", "location": "tiles.png"},
+        {"name": "grain", "type": "image_default", "location": "grain.png", "channel": 1},
+        {"name": "sky", "type": "image_hdr", "location": "sky.hdr", "is_flip_y": True},
+        {"name": "metal", "type": "image_exr", "location": "metal.exr"},
+    ]
+    e = sc["scene"]
+    e[0]["bsdf"] = {"type": "diffuse", "reflectance": {"type": "bitmap", "asset_name": "tiles", "filter": "trilinear",
+                                                       "wrap": "repeat"}}
+    e[0]["to_world"]["scale"] = [1.0, 1.0, 1.0]
+    e[2]["bsdf"] = {"type": "rough_plastic", "alpha": 0.2, "diffuse": {
+        "type": "chessboard", "to_uv": {"scale": [6, 6, 1]}, "remap": True,
+        "color_a": {"type": "bitmap", "asset_name": "tiles", "filter": "anisotropic", "anisotropic_level": 4},
+        "color_b": {"type": "chessboard", "color_a": [0.1, 0.5, 0.2], "color_b": 0.7, "to_uv": {"scale": [3, 3, 1]}}}}
+    e[3]["bsdf"] = {"type": "plastic", "diffuse": [0.6, 0.1, 0.1],
+                    "specular": {"type": "bitmap", "asset_name": "sky", "filter": "bilinear"}}
+    e[5]["bsdf"] = {"type": "disney", "base_color": {"type": "bitmap", "asset_name": "tiles", "filter": "nearest"},
+                    "roughness": {"type": "bitmap", "asset_name": "grain", "wrap": "repeat"}, "metallic": 0.3}
+    e[6]["bsdf"] = {"type": "mask", "opacity": {"type": "chessboard", "color_a": 0.9, "color_b": 0.2,
+                                                "to_uv": {"scale": [4, 2, 1]}},
+                    "nested": {"type": "diffuse", "reflectance": 0.8}}
+    e.append({"shape": {"type": "sphere", "center": [0.45, 0.85, 0.35], "radius": 0.25},
+              "bsdf": {"type": "rough_metal", "reflectance": {"type": "bitmap", "asset_name": "metal"},
+                       "alpha": {"type": "bitmap", "asset_name": "grain", "filter": "trilinear"}}})
+    return sc, assets
+
+
+def textured(dirpath, w=48, h=48, spp=4, seed=1, renderer="path"):
+    sc, assets = textured_room_scene(w, h, spp, seed, renderer)
+    return write(dirpath, "textured_%s_%dx%d_%d_%d" % (renderer, w, h, spp, seed), sc, assets)
+
+
 def volume(dirpath, w=48, h=48, spp=4, grid=32, max_depth=32):
     sc, assets = scenes.volume_box(width=w, height=h, spp=spp, grid=grid, max_depth=max_depth)
     return write(dirpath, "vol_%dx%d_%d" % (w, h, grid), sc, assets)

@@ -37,6 +37,9 @@ def lib():
                                  ctypes.c_int, ctypes.c_int, P, P]
         L.orc_render_samples.argtypes = [P, P, P, ctypes.c_int64, ctypes.c_uint32, P]
         L.orc_bsdf_eval.argtypes = [ctypes.c_char_p, P, P, ctypes.c_int64, P, P]
+        L.orc_texture_eval.argtypes = [P, ctypes.c_uint32, P, P, ctypes.c_int64, P]
+        L.orc_texture_count.argtypes = [P]
+        L.orc_image_load.argtypes = [ctypes.c_char_p, ctypes.c_char_p, P, P, ctypes.c_int64]
         L.orc_bsdf_sample.argtypes = [ctypes.c_char_p, P, P, ctypes.c_int64, P, P, P, P, P]
         L.orc_fresnel_dielectric.argtypes = [ctypes.c_float, ctypes.c_float, P]
         L.orc_fresnel_conductor.argtypes = [ctypes.c_float, P, P, P]
@@ -113,6 +116,18 @@ class OracleScene:
         if rc != 0:
             raise RuntimeError(lib().orc_last_error().decode())
         return film, stats
+
+    def texture_count(self):
+        return lib().orc_texture_count(self.h)
+
+    def texture_eval(self, texture, uv, duv=None):
+        uv = np.ascontiguousarray(uv, dtype=np.float32).reshape(-1, 2)
+        n = uv.shape[0]
+        duv = np.zeros((n, 4), np.float32) if duv is None else np.ascontiguousarray(duv, dtype=np.float32)
+        out = np.zeros((n, 3), dtype=np.float32)
+        if lib().orc_texture_eval(self.h, texture, _p(uv), _p(duv), n, _p(out)) != 0:
+            raise RuntimeError(lib().orc_last_error().decode())
+        return out
 
     def render_samples(self, pixels, samples, seed=None):
         pixels = np.ascontiguousarray(pixels, dtype=np.uint32)
@@ -250,3 +265,17 @@ def guide_random_records(n, lo, hi, seed, w_max=2.0):
     rec[:, 8:11] = q[:, 6:9]
     rec[:, 12:15], rec[:, 15] = wi, w
     return rec
+
+
+def image_load(asset, path):
+    """An image asset decoded and converted as the bitmap texture sees it -> (h, w, c) float32."""
+    import json as _json
+    dims = np.zeros(3, np.int32)
+    js = _json.dumps(asset).encode()
+    if lib().orc_image_load(js, str(path).encode(), _p(dims), None, 0) != 0:
+        raise RuntimeError(lib().orc_last_error().decode())
+    w, h, c = (int(x) for x in dims)
+    px = np.zeros(w * h * c, np.float32)
+    if lib().orc_image_load(js, str(path).encode(), _p(dims), _p(px), px.size) != 0:
+        raise RuntimeError(lib().orc_last_error().decode())
+    return px.reshape(h, w, c)
