@@ -895,9 +895,33 @@ std::unique_ptr<Scene> Scene::FromJson(const std::string& text, const std::strin
       if (type == "area") {
         L.kind = Light::Area;
         L.radiance = color("radiance", V3(1));
-      } else if (type == "skybox") {
+      } else if (type == "skybox") {  // skybox.cpp:24-50
         L.kind = Light::Skybox;
-        L.radiance = color("radiance", V3(1));
+        const Json* rj = ln->find("radiance");
+        if (rj && rj->is_object()) {
+          L.map = MakeTexture(*rj, 3, &env);
+          uint32_t width = L.map->width, height = L.map->height;
+          L.uniformMap = width == 1 && height == 1;
+          if (!L.uniformMap) {
+            std::vector<Float> luminance(width * height);
+            for (uint32_t y = 0; y < height; y++) {
+              Float sinTheta = std::sin((y + Float(0.5)) / height * PI);
+              Float v = y / (Float)height;
+              uint32_t start = y * width;
+              for (uint32_t x = 0; x < width; x++) {
+                Float u = x / (Float)width;
+                TexSi si{V2(u, v), V2(), V2()};
+                V3 color = L.map->Eval(si);
+                Float lum = Luminance(color);
+                lum *= sinTheta;
+                luminance[start + x] = lum;
+              }
+            }
+            L.dist.Build(luminance.data(), width, height);
+          }
+        } else {
+          L.radiance = color("radiance", V3(1));
+        }
       } else if (type == "point") {  // point.cpp:19-26
         L.kind = Light::Point;
         L.worldPos = L.toWorld.ApplyAffineToWorld(ReadV3(ln, "position", V3(0, 0, 0)));
@@ -1444,10 +1468,62 @@ int Scene::LightOf(const SurfaceInteraction& si) const {
 }
 
 // area.cpp:42-45, skybox.cpp:53-63 (constant map)
+// distribution.cpp:55-68
+void Continuous1D::Build(const Float* f, size_t size) {
+  pdf.assign(f, f + size);
+  cdf.resize(size + 1);
+  cdf[0] = 0;
+  size_t count = pdf.size();
+  for (size_t i = 1; i < count + 1; ++i) cdf[i] = cdf[i - 1] + pdf[i - 1] / count;
+  sum = cdf[count];
+  for (size_t i = 1; i < count + 1; i++) cdf[i] /= sum;
+  normalization = Float(1.0 / sum);
+}
+// distribution.cpp:84-97
+std::tuple<size_t, Float, Float> Continuous1D::Sample(Float xi) const {
+  auto iter = std::lower_bound(cdf.begin(), cdf.end(), xi);
+  size_t index = std::distance(cdf.begin(), iter);
+  index = std::clamp(index - 1, size_t(0), cdf.size() - 2);
+  Float du = xi - cdf[index];
+  if ((cdf[index + 1] - cdf[index]) > 0) du /= (cdf[index + 1] - cdf[index]);
+  Float p = pdf[index] * normalization;
+  Float c = (index + du) / Count();
+  return {index, c, p};
+}
+// distribution.cpp:103-129
+void Continuous2D::Build(const Float* data, size_t nu, size_t nv) {
+  conditional.resize(nv);
+  for (size_t v = 0; v < nv; v++) conditional[v].Build(data + v * nu, nu);
+  std::vector<Float> m(nv);
+  for (size_t v = 0; v < nv; v++) m[v] = conditional[v].sum;
+  marginal.Build(m.data(), m.size());
+}
+std::tuple<size_t, size_t, Float> Continuous2D::Sample(const V2& xi) const {
+  auto [vj, d1, pdf1] = marginal.Sample(xi.y);
+  auto [vi, d0, pdf0] = conditional[vj].Sample(xi.x);
+  (void)d0;
+  (void)d1;
+  return {vi, vj, pdf0 * pdf1};
+}
+Float Continuous2D::Pdf(const V2& uv) const {
+  size_t iu = std::clamp(size_t(uv.x * conditional[0].Count()), size_t(0), conditional[0].Count() - 1);
+  size_t iv = std::clamp(size_t(uv.y * marginal.Count()), size_t(0), marginal.Count() - 1);
+  return conditional[iv].pdf[iu] / marginal.sum;
+}
+
+// area.cpp:42-45, skybox.cpp:53-63
 Spectrum Scene::EvalLight(int l, const SurfaceInteraction& si) const {
   const Light& L = lights[l];
   if (L.kind == Light::Area) return dot(si.ToWorld(si.Wi), si.N) >= 0 ? L.radiance : Spectrum(0);
-  if (L.kind == Light::Skybox) return L.radiance;
+  if (L.kind == Light::Skybox) {
+    if (!L.map) return L.radiance;
+    V3 v = L.toWorld.ApplyLinearToLocal(-si.Wi);
+    Float phi = std::atan2(v.x, -v.z);
+    phi = (phi < 0) ? (phi + 2 * PI) : phi;
+    Float theta = std::acos(std::clamp(v.y, Float(-1), Float(1)));
+    TexSi tsi{V2(phi / (2 * PI), theta / PI), si.dUVdX, si.dUVdY};
+    return L.map->Eval(tsi);
+  }
   return Spectrum(0);
 }
 
@@ -1464,18 +1540,51 @@ std::pair<DirectionSample, Spectrum> Scene::SampleLightDirection(const V3& refP,
   if (L.kind == Light::Area) {
     dsr = shapes[L.shape].SampleDirection(refP, xi);
     li = dot(-dsr.Dir, dsr.N) >= 0 ? L.radiance : Spectrum(0);
-  } else if (L.kind == Light::Skybox) {
+  } else if (L.kind == Light::Skybox) {  // skybox.cpp:65-106
     Float radius = std::max(L.worldRadius, norm(refP - L.worldCenter));
     Float dist = 2 * radius;
-    V3 dir = normalized(SquareToUniformSphere(xi));
-    V3 worldDir = L.toWorld.ApplyLinearToWorld(dir);
-    dsr.P = worldDir * dist + refP;
-    dsr.N = -worldDir;
-    dsr.Pdf = SquareToUniformSpherePdf();
-    dsr.Dir = worldDir;
-    dsr.Dist = dist;
-    dsr.IsDelta = false;
-    li = L.radiance;
+    if (L.uniformMap) {
+      V3 dir = normalized(SquareToUniformSphere(xi));
+      Float phi = std::atan2(dir.x, -dir.z);
+      phi = (phi < 0) ? (phi + 2 * PI) : phi;
+      Float theta = std::acos(std::clamp(dir.y, Float(-1), Float(1)));
+      V2 uv(phi / (2 * PI), theta / PI);
+      V3 worldDir = L.toWorld.ApplyLinearToWorld(dir);
+      dsr.P = worldDir * dist + refP;
+      dsr.N = -worldDir;
+      dsr.Pdf = SquareToUniformSpherePdf();
+      dsr.Dir = worldDir;
+      dsr.Dist = dist;
+      dsr.IsDelta = false;
+      li = L.map ? L.map->Eval(TexSi{uv, V2(), V2()}) : L.radiance;
+    } else {
+      // SampleLightDir (skybox.cpp:213-233)
+      auto [iu, iv, pdf0] = L.dist.Sample(xi);
+      Float pdfDir = pdf0;
+      bool ok = pdfDir > 0;
+      Float y = iv / (Float)L.map->height;
+      Float x = iu / (Float)L.map->width;
+      V2 uv(x, y);
+      Float theta = y * PI;
+      Float phi = x * 2 * PI;
+      Float sinTheta = std::sin(theta);
+      if (ok && sinTheta == 0) ok = false;
+      if (!ok) {
+        dsr.Pdf = 0;
+        return {dsr, Spectrum(0)};
+      }
+      pdfDir /= (2 * PI * PI * sinTheta);
+      V3 sph(std::cos(phi) * sinTheta, std::sin(phi) * sinTheta, std::cos(theta));  // SphericalCoordinates
+      V3 dir(sph.y, sph.z, -sph.x);
+      V3 worldDir = L.toWorld.ApplyLinearToWorld(dir);
+      dsr.P = worldDir * dist + refP;
+      dsr.N = -worldDir;
+      dsr.Pdf = pdfDir;
+      dsr.Dir = worldDir;
+      dsr.Dist = dist;
+      dsr.IsDelta = false;
+      li = L.map->Eval(TexSi{uv, V2(), V2()});
+    }
   } else if (L.kind == Light::Point) {  // point.cpp:33-49
     dsr.P = L.worldPos;
     dsr.N = V3(0);
@@ -1525,7 +1634,22 @@ Float Scene::PdfLightDirection(int l, const V3& refP, const DirectionSample& dsr
   if (L.kind == Light::Area) {
     p = dot(-dsr.Dir, dsr.N) >= 0 ? shapes[L.shape].PdfDirection(refP, dsr) : 0;
   } else if (L.kind == Light::Skybox) {
-    p = SquareToUniformSpherePdf();
+    if (L.uniformMap) {
+      p = SquareToUniformSpherePdf();
+    } else {  // skybox.cpp:108-127
+      V3 v = L.toWorld.ApplyAffineToLocal(dsr.Dir);
+      Float theta = std::acos(std::clamp(v.y, Float(-1), Float(1)));
+      Float sinTheta = std::sin(theta);
+      if (sinTheta == 0) {
+        p = 0;
+      } else {
+        Float phi = std::atan2(v.x, -v.z);
+        phi = (phi < 0) ? (phi + 2 * PI) : phi;
+        V2 uv(phi / (2 * PI), theta / PI);
+        Float pdf = L.dist.Pdf(uv);
+        p = pdf / (2 * PI * PI * sinTheta);
+      }
+    }
   }
   return p * lightPdf;
 }

@@ -6,6 +6,8 @@
 // (src/accel/embree.cpp) with a binned-SAH BVH2 and the watertight
 // ray/triangle test of Woop, Benthin and Wald (JCGT 2013).
 #pragma once
+#include <tuple>
+
 #include "ref_bsdf.h"
 #include "ref_texture.h"
 
@@ -89,6 +91,24 @@ struct Discrete1D {
   std::pair<size_t, Float> SampleReuse(Float xi) const;
 };
 
+// distribution.cpp:55-129
+struct Continuous1D {
+  std::vector<Float> pdf, cdf;
+  Float sum = 0, normalization = 0;
+  void Build(const Float* f, size_t n);
+  size_t Count() const { return pdf.size(); }
+  // (index, cdf, pdf) of the sample
+  std::tuple<size_t, Float, Float> Sample(Float xi) const;
+};
+struct Continuous2D {
+  std::vector<Continuous1D> conditional;
+  Continuous1D marginal;
+  void Build(const Float* data, size_t nu, size_t nv);
+  // (index u, index v, pdf)
+  std::tuple<size_t, size_t, Float> Sample(const V2& xi) const;
+  Float Pdf(const V2& uv) const;
+};
+
 struct Shape {
   enum Kind { Mesh, Rect, Sphere } kind = Mesh;
   int bsdf = -1, light = -1, inMedium = -1, outMedium = -1;
@@ -123,6 +143,9 @@ struct Light {
   V3 worldPos;   // point: world position (point.cpp:22-23)
   Spectrum scale;      // projection: irradiance scale
   Transform toClip;    // projection: light space -> [0,1]^2 image plane (projection.cpp:27-41)
+  std::shared_ptr<Texture> map;  // skybox: radiance texture (null: constant radiance)
+  bool uniformMap = true;        // skybox: 1 x 1 map, uniform sphere sampling
+  Continuous2D dist;             // skybox: luminance distribution of a bitmap map
   V3 worldCenter;
   Float worldRadius = 0;
   bool IsEnv() const { return kind == Skybox; }

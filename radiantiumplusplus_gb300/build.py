@@ -23,7 +23,7 @@ CSRC = os.path.join(PKG, "csrc")
 BUILD = os.path.join(PKG, "_build")
 LIB = os.path.join(PKG, "librad_gpu.so")
 
-HOST_SOURCES = ["host_scene.cpp", "host_bvh.cpp", "host_image.cpp"]
+HOST_SOURCES = ["host_scene.cpp", "host_bvh.cpp", "host_image.cpp", "host_texeval.cpp"]
 CUDA_SOURCES = ["runtime.cu", "k_path.cu", "k_vol.cu", "k_parity.cu", "k_noalloc.cu", "k_guide.cu", "guide_host.cu"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 
@@ -63,8 +63,9 @@ def build(verbose=False, force=False):
         o = os.path.join(BUILD, src + ".o")
         objs.append(o)
         if force or _stale(o, [s] + headers):
+            cuda_inc = ["-I" + os.path.join(os.path.dirname(os.path.dirname(nvcc)), "include")]
             jobs.append(["g++", "-O2", "-std=c++17", "-fPIC", "-ffp-contract=off", "-pthread", "-Wall",
-                         "-Wno-unused-function", *inc, "-c", s, "-o", o])
+                         "-Wno-unused-function", *inc, *cuda_inc, "-c", s, "-o", o])
     for src in CUDA_SOURCES:
         s = os.path.join(CSRC, src)
         o = os.path.join(BUILD, src + ".o")

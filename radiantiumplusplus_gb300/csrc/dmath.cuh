@@ -13,7 +13,9 @@
 #include <cmath>
 #include <cstring>
 #define RD inline
+#undef __global__
 #define __global__
+#undef __launch_bounds__
 #define __launch_bounds__(x)
 inline float __uint_as_float(uint32_t u) { float f; std::memcpy(&f, &u, 4); return f; }
 inline uint32_t __float_as_uint(float f) { uint32_t u; std::memcpy(&u, &f, 4); return u; }

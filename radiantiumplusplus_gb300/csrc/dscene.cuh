@@ -4,6 +4,7 @@
 // sphere.cpp:265-328), spawn offsets (interaction.cpp:10-26) and the
 // perspective camera (perspective.cpp:73-82).
 #pragma once
+#include "dtex.cuh"
 #include "dtrace.cuh"
 
 namespace rad {
@@ -307,6 +308,80 @@ RD float ShapePdfDirection(const ShapeRec& sh, V3 refP, V3 dir, V3 n, float dist
   return pdf;
 }
 
+// ContinuousDistribution1D::Sample (distribution.cpp:84-97) over one row of a
+// 2D distribution laid out as pdf[n], cdf[n + 1], normalization. The bin is
+// lower_bound(cdf, xi) - 1 in unsigned arithmetic clamped to n - 1, so xi = 0
+// (lower_bound 0) selects the last bin, as in the reference.
+RD uint32_t Dist1DSample(const float* row, uint32_t n, float xi, float& pdf) {
+  const float* cdf = row + n;
+  uint32_t lo = 0, len = n + 1;
+  while (len > 0) {
+    uint32_t half = len >> 1, mid = lo + half;
+    if (cdf[mid] < xi) {
+      lo = mid + 1;
+      len = len - half - 1;
+    } else {
+      len = half;
+    }
+  }
+  uint32_t idx = lo == 0u ? n - 1u : (lo - 1u < n - 1u ? lo - 1u : n - 1u);
+  pdf = row[idx] * row[2 * n + 1];
+  return idx;
+}
+// Skybox::SampleLightDir / PdfDirection on a bitmap radiance map (skybox.cpp:112-131,
+// 213-233) with ContinuousDistribution2D (distribution.cpp:103-129): rows of
+// 2 nu + 2 floats, then the marginal (pdf, cdf, normalization, sum).
+RD bool EnvSampleDir(const DevScene& S, const LightRec& L, V2 xi, V3& worldDir, float& pdf, V2& uv) {
+  const uint32_t nu = L.distW, nv = L.distH;
+  const float* base = S.lightDist + L.dist;
+  const float* marg = base + (size_t)nv * (2 * nu + 2);
+  float pdf1, pdf0;
+  uint32_t vj = Dist1DSample(marg, nv, xi.y, pdf1);
+  uint32_t vi = Dist1DSample(base + (size_t)vj * (2 * nu + 2), nu, xi.x, pdf0);
+  pdf = pdf0 * pdf1;
+  if (pdf <= 0.f) return false;
+  float y = (float)vj / (float)nv, x = (float)vi / (float)nu;
+  uv = V2{x, y};
+  float theta = y * kPi, phi = x * 2.f * kPi;
+  float sinTheta = sinf(theta);
+  if (sinTheta == 0.f) return false;
+  pdf /= (2.f * kPi * kPi * sinTheta);
+  float cosTheta = cosf(theta), sinPhi = sinf(phi), cosPhi = cosf(phi);
+  V3 sph{cosPhi * sinTheta, sinPhi * sinTheta, cosTheta};
+  worldDir = LinearRows(L.lin, V3{sph.y, sph.z, -sph.x});
+  return true;
+}
+RD float EnvDirPdf(const DevScene& S, const LightRec& L, V3 dir) {
+  V3 v = Affine4(L.m, dir);
+  float theta = acosf(clampr(v.y, -1.f, 1.f));
+  float sinTheta = sinf(theta);
+  if (sinTheta == 0.f) return 0.f;
+  float phi = atan2f(v.x, -v.z);
+  phi = phi < 0.f ? phi + 2.f * kPi : phi;
+  V2 uv{phi / (2.f * kPi), theta / kPi};
+  const uint32_t nu = L.distW, nv = L.distH;
+  const float* base = S.lightDist + L.dist;
+  const float* marg = base + (size_t)nv * (2 * nu + 2);
+  float fu = uv.x * (float)nu, fv = uv.y * (float)nv;
+  uint32_t iu = fu >= 0.f ? (uint32_t)fu : 0u, iv = fv >= 0.f ? (uint32_t)fv : 0u;
+  iu = iu < nu - 1u ? iu : nu - 1u;
+  iv = iv < nv - 1u ? iv : nv - 1u;
+  float pdf = base[(size_t)iv * (2 * nu + 2) + iu] / marg[2 * nv + 2];
+  return pdf / (2.f * kPi * kPi * sinTheta);
+}
+// The sky's radiance towards world direction d (skybox.cpp:53-63): the map's
+// value at the direction's latitude-longitude uv.
+RD V3 EnvRadiance(const DevScene& S, const LightRec& L, V3 d) {
+  if (!L.tex) return V3{L.radiance[0], L.radiance[1], L.radiance[2]};
+  V3 v = LinearRows(L.m, d);
+  float phi = atan2f(v.x, -v.z);
+  phi = phi < 0.f ? phi + 2.f * kPi : phi;
+  float theta = acosf(clampr(v.y, -1.f, 1.f));
+  TexCtx x{S.tex, S.texels, S.texBind, V2{phi / (2.f * kPi), theta / kPi}, V2{0.f, 0.f}, V2{0.f, 0.f}};
+  TexVal r = TexEval(x, L.tex - 1u, x.uv);
+  return V3{r.c[0], r.c[1], r.c[2]};
+}
+
 // scene.cpp:65-96: uniform light pick, then the light's direction sample.
 RD DirSample SampleLightDirection(const DevScene& S, V3 refP, float xiL, V2 xi, V3& li) {
   DirSample d{};
@@ -348,7 +423,7 @@ RD DirSample SampleLightDirection(const DevScene& S, V3 refP, float xiL, V2 xi, 
     bool inRange = uv.x >= 0.f && uv.x <= 1.f && uv.y >= 0.f && uv.y <= 1.f && local.z > 0.f;
     if (!inRange) return d;  // Pdf 0: no light sample
     d.P = V3{L.dir[0], L.dir[1], L.dir[2]};
-    d.N = ld3(L.m + 32);
+    d.N = ld3(L.lin);
     d.Pdf = 1.f;
     d.IsDelta = true;
     V3 dir = d.P - refP;
@@ -362,10 +437,31 @@ RD DirSample SampleLightDirection(const DevScene& S, V3 refP, float xiL, V2 xi, 
     float dist = 2.f * radius;
     V3 worldDir;
     if (L.kind == LIGHT_SKYBOX) {
-      V3 dir = normalized(SquareToUniformSphere(xi));
-      worldDir = LinearRows(L.lin, dir);
+      if (L.distW) {  // bitmap radiance: luminance importance sampling (skybox.cpp:88-103)
+        float pdf;
+        V2 uv;
+        if (!EnvSampleDir(S, L, xi, worldDir, pdf, uv)) {
+          d.Pdf = 0.f;
+          return d;
+        }
+        d.Pdf = pdf;
+        TexCtx x{S.tex, S.texels, S.texBind, uv, V2{0.f, 0.f}, V2{0.f, 0.f}};
+        TexVal r = TexEval(x, L.tex - 1u, uv);
+        rad = V3{r.c[0], r.c[1], r.c[2]};
+      } else {  // skybox.cpp:70-87
+        V3 dir = normalized(SquareToUniformSphere(xi));
+        worldDir = LinearRows(L.lin, dir);
+        d.Pdf = SquareToUniformSpherePdf();
+        if (L.tex) {
+          float phi = atan2f(dir.x, -dir.z);
+          phi = phi < 0.f ? phi + 2.f * kPi : phi;
+          float theta = acosf(clampr(dir.y, -1.f, 1.f));
+          TexCtx x{S.tex, S.texels, S.texBind, V2{phi / (2.f * kPi), theta / kPi}, V2{0.f, 0.f}, V2{0.f, 0.f}};
+          TexVal r = TexEval(x, L.tex - 1u, x.uv);
+          rad = V3{r.c[0], r.c[1], r.c[2]};
+        }
+      }
       d.N = -worldDir;
-      d.Pdf = SquareToUniformSpherePdf();
       d.IsDelta = false;
     } else {
       V3 ld{L.dir[0], L.dir[1], L.dir[2]};
@@ -390,18 +486,18 @@ RD float PdfLightDirection(const DevScene& S, int light, V3 refP, V3 dir, V3 n, 
   if (L.kind == LIGHT_AREA) {
     p = dot(-dir, n) >= 0.f ? ShapePdfDirection(S.shapes[L.shape], refP, dir, n, dist) : 0.f;
   } else if (L.kind == LIGHT_SKYBOX) {
-    p = SquareToUniformSpherePdf();
+    p = L.distW ? EnvDirPdf(S, L, dir) : SquareToUniformSpherePdf();
   }
   return p * S.lightPdf;
 }
 
-// area.cpp:42-45 / skybox.cpp:53-63 (constant radiance); point and projection
+// area.cpp:42-45 / skybox.cpp:53-63; point and projection
 // lights have no surface to hit and evaluate to 0 (point.cpp:29-31, projection.cpp:48-50).
 RD V3 EvalLightAt(const DevScene& S, int light, const SurfInt* si) {
   const LightRec& L = S.lights[light];
   V3 rad{L.radiance[0], L.radiance[1], L.radiance[2]};
   if (L.kind == LIGHT_AREA) return dot(ToWorld(si->sh, si->Wi), si->N) >= 0.f ? rad : v3s(0.f);
-  if (L.kind == LIGHT_SKYBOX) return rad;
+  if (L.kind == LIGHT_SKYBOX) return EnvRadiance(S, L, -si->Wi);
   return v3s(0.f);
 }
 

@@ -545,6 +545,46 @@ double MeanLuminance(const HostScene& hs, uint32_t id) {
   return sum / (double)(t.height * t.width);
 }
 
+// ContinuousDistribution1D (distribution.cpp:55-68) appended to `pool` as
+// pdf[n], cdf[n + 1], normalization; returns the unnormalised sum.
+float AppendDist1D(const float* f, size_t n, std::vector<float>& pool) {
+  std::vector<float> cdf(n + 1);
+  cdf[0] = 0;
+  for (size_t i = 1; i < n + 1; ++i) cdf[i] = cdf[i - 1] + f[i - 1] / (float)n;
+  float sum = cdf[n];
+  for (size_t i = 1; i < n + 1; i++) cdf[i] /= sum;
+  pool.insert(pool.end(), f, f + n);
+  pool.insert(pool.end(), cdf.begin(), cdf.end());
+  pool.push_back((float)(1.0 / sum));
+  return sum;
+}
+
+// Skybox luminance grid and ContinuousDistribution2D (skybox.cpp:27-47,
+// distribution.cpp:103-118): the map read at texel corners (x / W, y / H),
+// luminance weighted by sin of the row's centre latitude.
+void BuildEnvDistribution(HostScene& hs, uint32_t tex, uint32_t W, uint32_t H, LightRec& L) {
+  std::vector<float> lum((size_t)W * H);
+  for (uint32_t y = 0; y < H; y++) {
+    float sinTheta = std::sin((y + 0.5f) / H * kPiF);
+    float v = y / (float)H;
+    for (uint32_t x = 0; x < W; x++) {
+      float u = x / (float)W;
+      float c[3];
+      HostTexEval(hs, tex, u, v, c);
+      float l = (c[0] * 0.212671f) + (c[1] * 0.715160f) + (c[2] * 0.072169f);
+      lum[(size_t)y * W + x] = l * sinTheta;
+    }
+  }
+  if (hs.lightDist.size() + lum.size() * 2 + 4 * H + 8 > 0xffffffffull) throw ConfigError("environment map too large");
+  L.dist = (uint32_t)hs.lightDist.size();
+  L.distW = W;
+  L.distH = H;
+  std::vector<float> marginal(H);
+  for (uint32_t y = 0; y < H; y++) marginal[y] = AppendDist1D(lum.data() + (size_t)y * W, W, hs.lightDist);
+  float msum = AppendDist1D(marginal.data(), H, hs.lightDist);
+  hs.lightDist.push_back(msum);
+}
+
 // ---- BSDF records
 // Parameter reader for one BSDF record: constants go into p[], textured
 // parameters become TexBind entries (their p[] slots are filled per lookup).
@@ -1199,10 +1239,20 @@ void BuildHostScene(const std::string& json, const std::string& baseDir, HostSce
       if (type == "area") {  // area.cpp:20-40
         L.kind = LIGHT_AREA;
         rad = col("radiance", F3(1, 1, 1));
-      } else if (type == "skybox") {  // skybox.cpp:24-50 (constant radiance)
+      } else if (type == "skybox") {  // skybox.cpp:24-50
         L.kind = LIGHT_SKYBOX;
-        rad = col("radiance", F3(1, 1, 1));
+        const JValue* rn = ln->get("radiance");
+        if (rn && rn->isObj()) {
+          uint32_t tid = AddTexture(*rn, 3, env);
+          L.tex = tid + 1;
+          const TexRec& tr = hs.tex[tid];
+          uint32_t W = tr.kind == TEX_BITMAP ? tr.width : 1u, H = tr.kind == TEX_BITMAP ? tr.height : 1u;
+          if (!(W == 1 && H == 1)) BuildEnvDistribution(hs, tid, W, H, L);
+        } else {
+          rad = col("radiance", F3(1, 1, 1));
+        }
         RowsOf(t.w, L.lin);
+        for (int i = 0; i < 16; i++) L.m[i] = t.l.m[i / 4][i % 4];
       } else if (type == "point") {  // point.cpp:19-26
         L.kind = LIGHT_POINT;
         F3 p = t.AffW(RV(ln, "position", F3(0, 0, 0)));
@@ -1243,9 +1293,9 @@ void BuildHostScene(const std::string& json, const std::string& baseDir, HostSce
         L.dir[1] = t.w.m[1][3];
         L.dir[2] = t.w.m[2][3];
         F3 n = Normalize(t.LinW(F3(0, 0, 1)));
-        L.m[32] = n.x;
-        L.m[33] = n.y;
-        L.m[34] = n.z;
+        L.lin[0] = n.x;
+        L.lin[1] = n.y;
+        L.lin[2] = n.z;
       } else if (type == "directional") {  // extension: no reference factory
         L.kind = LIGHT_DIRECTIONAL;
         rad = col("irradiance", F3(1, 1, 1));

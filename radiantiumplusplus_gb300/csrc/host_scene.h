@@ -49,6 +49,7 @@ struct HostScene {
   std::vector<float> texels;        // mip chains of the bitmap textures
   std::vector<TexBind> texBind;     // textured BSDF parameters
   bool needDiff = false;            // a trilinear / anisotropic bitmap is in use
+  std::vector<float> lightDist;     // 2D luminance distributions of textured skyboxes
   int envLight = -1, globalMedium = -1;
   float lightPdf = 0.f;
   uint64_t nPrims = 0;
@@ -58,6 +59,9 @@ struct HostScene {
   std::vector<PrimRec> prims;
   std::vector<uint32_t> primInfo;  // 2 words per leaf-order primitive
 };
+
+// Texture `tex` of the scene at (u, v) with zero uv derivatives (host_texeval.cpp).
+void HostTexEval(const HostScene& hs, uint32_t tex, float u, float v, float out[3]);
 
 // Parses `json` (scene text) resolving asset locations against `baseDir`.
 void BuildHostScene(const std::string& json, const std::string& baseDir, HostScene& out);

@@ -110,14 +110,17 @@ enum LightKind : uint32_t { LIGHT_AREA = 0, LIGHT_SKYBOX = 1, LIGHT_DIRECTIONAL 
 struct alignas(16) LightRec {
   uint32_t kind;
   int32_t shape;
-  uint32_t pad[2];
+  uint32_t tex;        // skybox: radiance texture + 1 (0: constant radiance)
+  uint32_t dist;       // skybox with a bitmap: first float of its 2D luminance distribution
   float radiance[4];   // rgb: area radiance, sky radiance, directional irradiance, point intensity,
                        // projection irradiance x scale
   float dir[4];        // directional: world direction the light travels; point / projection: world position
   float world[4];      // world bounding sphere center xyz, radius w (skybox.cpp:139-144)
-  float lin[12];       // skybox toWorld linear part, rows of 4
-  float m[36];         // projection: world -> light 4x4 (m[0..15]), light -> clip 4x4 (m[16..31]),
-                       // world-space normal (m[32..34])
+  float lin[12];       // skybox toWorld linear part, rows of 4; projection: world-space normal (lin[0..2])
+  float m[32];         // projection: world -> light 4x4 (m[0..15]), light -> clip 4x4 (m[16..31]);
+                       // skybox: world -> light 4x4 (m[0..15])
+  uint32_t distW, distH;  // skybox with a bitmap: distribution size (texels); 0: uniform sphere sampling
+  uint32_t pad2[2];
 };
 static_assert(sizeof(LightRec) == 256, "LightRec size");
 
@@ -200,6 +203,7 @@ struct DevScene {
   const TexRec* tex;           // textures
   const float* texels;         // texel pool
   const TexBind* texBind;      // textured BSDF parameters
+  const float* lightDist;      // 2D luminance distributions of textured skyboxes
   uint32_t nNodes, nPrims, nShapes, nLights;
   uint32_t nMedia, nMats;
   uint32_t nTex, needDiff;     // needDiff: a trilinear / anisotropic texture reads ray differentials

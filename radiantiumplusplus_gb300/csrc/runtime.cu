@@ -759,6 +759,7 @@ uint64_t SceneUpload(const HostScene& hs, rad_scene* sc) {
   TexRec* tex = DevAlloc<TexRec>(hs.tex.size(), o, b);
   float* texels = DevAlloc<float>(hs.texels.size(), o, b);
   TexBind* tbind = DevAlloc<TexBind>(hs.texBind.size(), o, b);
+  float* ldist = DevAlloc<float>(hs.lightDist.size(), o, b);
   up(nodes, hs.nodes);
   up(prims, hs.prims);
   up(pinfo, hs.primInfo);
@@ -781,6 +782,7 @@ uint64_t SceneUpload(const HostScene& hs, rad_scene* sc) {
   up(tex, hs.tex);
   up(texels, hs.texels);
   up(tbind, hs.texBind);
+  up(ldist, hs.lightDist);
   D.nodes = nodes;
   D.prims = prims;
   D.primInfo = pinfo;
@@ -800,6 +802,7 @@ uint64_t SceneUpload(const HostScene& hs, rad_scene* sc) {
   D.tex = tex;
   D.texels = texels;
   D.texBind = tbind;
+  D.lightDist = ldist;
   D.nTex = (uint32_t)hs.tex.size();
   D.needDiff = hs.needDiff ? 1u : 0u;
   D.nNodes = (uint32_t)hs.nodes.size();

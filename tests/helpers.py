@@ -73,6 +73,9 @@ def textured_room_scene(w=48, h=48, spp=4, seed=1, renderer="path"):
     e.append({"shape": {"type": "sphere", "center": [0.45, 0.85, 0.35], "radius": 0.25},
               "bsdf": {"type": "rough_metal", "reflectance": {"type": "bitmap", "asset_name": "metal"},
                        "alpha": {"type": "bitmap", "asset_name": "grain", "filter": "trilinear"}}})
+    # environment map seen through the open front of the room: importance-sampled HDR sky
+    e.append({"to_world": {"rotate": {"axis": [0, 1, 0], "angle": 30.0}},
+              "light": {"type": "skybox", "radiance": {"type": "bitmap", "asset_name": "sky"}}})
     return sc, assets
 
 

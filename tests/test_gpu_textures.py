@@ -29,7 +29,7 @@ def test_texture_lookups_match(rad, oracle, scene_dir):
     path, text, d = textured(scene_dir, 16, 16, 1)
     g, o = rad.Scene.from_file(path), oracle.OracleScene(text, d)
     n = o.texture_count()
-    assert n == 14
+    assert n == 15
     uv, duv = _uv_batch(20000, 3)
     # textures 0 and 13 are trilinear, 2 anisotropic, 1 a chessboard over 2; the
     # others (nearest / bilinear bitmaps, chessboards, constants) are bit-exact

@@ -137,3 +137,40 @@ def test_camera_uv_derivatives_of_a_facing_plane(oracle, tmp_path):
     far_tri, far_bi = render("trilinear", 3.6, 8), render("bilinear", 3.6, 8)
     assert np.allclose(near_tri, near_bi, rtol=1e-6)
     assert far_tri.std() < 0.5 * far_bi.std()
+
+
+def _sky_plane(tmp_path, name, radiance, assets=None):
+    sc = {"camera": {"type": "perspective", "fov": 30.0, "resolution": [8, 8], "origin": [0, 3, 0.01],
+                     "target": [0, 0, 0]},
+          "sampler": {"type": "independent", "sample_count": 1, "seed": 1},
+          "assets": [{"name": "s", "type": "image_hdr", "location": "s.hdr"}] if assets else [],
+          "scene": [{"to_world": {"rotate": {"axis": [1, 0, 0], "angle": -90.0}, "scale": [50, 50, 1]},
+                     "shape": {"type": "rectangle"}, "bsdf": {"type": "diffuse", "reflectance": 0.5}},
+                    {"to_world": {"rotate": {"axis": [0, 1, 0], "angle": 20.0}},
+                     "light": {"type": "skybox", "radiance": radiance}}],
+          "accel": {"type": "embree"}, "renderer": {"type": "path", "max_depth": 2}}
+    _, text, d = write(tmp_path, name, sc, assets)
+    return text, d
+
+
+def test_env_map_sampling(oracle, tmp_path):
+    """A bitmap skybox is importance sampled by luminance (skybox.cpp:27-47, 213-233):
+    under a uniform map the lit plane's radiance approaches the constant sky's
+    R * L (the sampled directions are texel corners, so within a few percent), and
+    doubling the map doubles it."""
+    import imgenc
+    ones = np.ones((32, 64, 3))
+    text_c, d_c = _sky_plane(tmp_path, "const", 1.0)
+    text_m, d_m = _sky_plane(tmp_path, "map", {"type": "bitmap", "asset_name": "s"}, {"s.hdr": imgenc.hdr(ones)})
+    text_2, d_2 = _sky_plane(tmp_path, "map2", {"type": "bitmap", "asset_name": "s"}, {"s.hdr": imgenc.hdr(2 * ones)})
+    n = 64
+    pix = np.repeat(np.arange(n, dtype=np.uint32), 512)
+    smp = np.tile(np.arange(512, dtype=np.uint32), n)
+    vals = []
+    for text, d in ((text_c, d_c), (text_m, d_m), (text_2, d_2)):
+        o = oracle.OracleScene(text, d)
+        vals.append(o.render_samples(pix, smp)[:, 0].mean())
+        o.close()
+    assert abs(vals[0] - 0.5) < 0.01
+    assert abs(vals[1] - vals[0]) < 0.05 * vals[0]
+    assert abs(vals[2] - 2 * vals[1]) < 1e-3 * vals[2]
