@@ -390,6 +390,20 @@ Spectrum VolPathLi(const Scene& S, const Ray& ray0, Pcg32& rng) {
   return result;
 }
 
+// ao.cpp:22-36
+Spectrum AOLi(const Scene& S, const Ray& ray, Pcg32& rng) {
+  SurfaceInteraction si;
+  if (!Trace(S, ray, si)) return Spectrum(0);
+  V3 wo = SquareToCosineHemisphere(rng.Next2D());
+  Float pdf = SquareToCosineHemispherePdf(wo);
+  Ray shadowRay = SpawnRay(si.P, si.N, si.ToWorld(wo));
+  if (g_rays) g_rays->shadow++;
+  bool visibility = S.Occluded(shadowRay);
+  Spectrum l(0);
+  if (!visibility && wo.z > 0) l = Spectrum(wo.z / PI / pdf);
+  return l;
+}
+
 // sample_renderer.cpp:93-106: one pixel sample. The jitter takes the first two
 // draws of the sample's stream (the reference uses a separate per-tile mt19937).
 static Spectrum RenderSample(const Scene& S, uint32_t x, uint32_t y, uint32_t s, uint32_t seed) {
@@ -399,6 +413,7 @@ static Spectrum RenderSample(const Scene& S, uint32_t x, uint32_t y, uint32_t s,
   V2 scr(Float(x) + jx, Float(y) + jy);
   RayDiff diff;
   Ray ray = S.camera.SampleRayDifferential(scr, diff);
+  if (S.renderer == "ao") return AOLi(S, ray, rng);
   return S.renderer == "vol_path" ? VolPathLi(S, ray, rng) : PathLi(S, ray, diff, rng);
 }
 

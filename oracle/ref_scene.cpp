@@ -1008,7 +1008,8 @@ std::unique_ptr<Scene> Scene::FromJson(const std::string& text, const std::strin
   const Json* rn = root.find("renderer");
   if (!rn) throw std::runtime_error("no child: renderer");
   S.renderer = ReadS(rn, "type", "");
-  if (S.renderer != "path" && S.renderer != "vol_path") throw std::runtime_error("cannot find factory: " + S.renderer);
+  if (S.renderer != "path" && S.renderer != "vol_path" && S.renderer != "ao")
+    throw std::runtime_error("cannot find factory: " + S.renderer);
   S.maxDepth = ReadI(rn, "max_depth", -1);
   S.rrDepth = ReadI(rn, "rr_depth", S.renderer == "path" ? 3 : 5);
   if (const Json* an = root.find("accel")) {

@@ -1354,8 +1354,9 @@ void BuildHostScene(const std::string& json, const std::string& baseDir, HostSce
   const JValue* rn = root.get("renderer");
   if (!rn) throw ConfigError("no child: renderer");
   std::string rt = TypeOf(*rn);
-  if (rt != "path" && rt != "vol_path") throw FactoryError("cannot find factory: " + rt);
+  if (rt != "path" && rt != "vol_path" && rt != "ao") throw FactoryError("cannot find factory: " + rt);
   hs.isVol = rt == "vol_path";
+  hs.isAO = rt == "ao";
   hs.maxDepth = RI(rn, "max_depth", -1);
   hs.rrDepth = RI(rn, "rr_depth", hs.isVol ? 5 : 3);
   if (const JValue* an = root.get("accel")) {

@@ -32,6 +32,7 @@ struct HostScene {
   int spp = 16;
   uint32_t seed = 0;
   bool isVol = false;
+  bool isAO = false;  // renderer "ao"
   int maxDepth = -1, rrDepth = 3;
   std::vector<MatRec> mats;
   std::vector<ShapeRec> shapes;

@@ -128,6 +128,12 @@ extern "C" RAD_API int rad_render_samples_noalloc(rad_scene* scene, const uint32
     int grid = std::max(1, std::min(sms * 8, (int)((count + 127) / 128)));
     int iters = S.maxDepth >= 0 ? std::max(1, S.maxDepth) : kMaxBounce;
     if (iters > kMaxBounce) iters = kMaxBounce;
+    if (S.isAO) {  // renderer "ao": first hit and one visibility ray
+      if (LaunchExtend(S, B, 0, grid, st) != cudaSuccess || LaunchShadeAO(S, B, grid, st) != cudaSuccess ||
+          LaunchShadow(S, B, 0, grid, st) != cudaSuccess)
+        return done(RAD_ERR_CUDA, "ao launch failed");
+      iters = 0;
+    }
     for (int d = 0; d < iters; d++) {
       if (LaunchExtend(S, B, d, grid, st) != cudaSuccess || LaunchShade(S, B, d, grid, st) != cudaSuccess ||
           LaunchShadow(S, B, d, grid, st) != cudaSuccess)

@@ -416,6 +416,49 @@ __global__ void __launch_bounds__(kBlock) KShadeClass(DevScene S, PathBuffers B,
   }
 }
 
+// AO::Li (ao.cpp:22-36) after the first hit: a cosine-weighted direction and a
+// visibility ray of unbounded length; the shadow stage adds cos / pi / pdf when
+// nothing blocks it. Misses contribute 0.
+__global__ void __launch_bounds__(kBlock) KShadeAO(DevScene S, PathBuffers B) {
+  uint32_t count = B.counters[0];
+  uint32_t* cntSh = B.counters + kShadowBase;
+  uint32_t stride = gridDim.x * blockDim.x;
+  for (uint32_t base = blockIdx.x * blockDim.x; base < count; base += stride) {
+    uint32_t i = base + threadIdx.x;
+    bool shadow = false;
+    float4 shO = make_float4(0, 0, 0, 0), shD = shO, shC = shO;
+    if (i < count) {
+      uint32_t p = B.q[0][i];
+      HitRec h = B.hit[p];
+      if (h.prim != kNoPrim) {
+        float4 ro = B.rayO[p], rd = B.rayD[p];
+        TraceHit th{h.t, h.u, h.v, h.prim, h.shape, h.front};
+        SurfInt si = ComputeSI(S, V3{ro.x, ro.y, ro.z}, V3{rd.x, rd.y, rd.z}, th);
+        uint2 rs = B.rng[p];
+        Pcg32 rng;
+        rng.state = ((uint64_t)rs.y << 32) | rs.x;
+        V3 wo = SquareToCosineHemisphere(Next2D(rng));
+        float pdf = SquareToCosineHemispherePdf(wo);
+        if (wo.z > 0.f) {
+          V3 d = ToWorld(si.sh, wo);
+          V3 o = OffsetP(si.P, si.N, d);
+          float l = wo.z / kPi / pdf;
+          shadow = true;
+          shO = make_float4(o.x, o.y, o.z, kFloatMax);
+          shD = make_float4(d.x, d.y, d.z, __uint_as_float(p));
+          shC = make_float4(l, l, l, 0.f);
+        }
+      }
+    }
+    uint32_t sslot = WarpAppend(cntSh, shadow);
+    if (shadow) {
+      B.shO[sslot] = shO;
+      B.shD[sslot] = shD;
+      B.shC[sslot] = shC;
+    }
+  }
+}
+
 template <bool COUNT>
 __global__ void __launch_bounds__(kBlock, 8)
     KShadow(DevScene S, PathBuffers B, int depth, unsigned long long* trav, int refillBusy, int leafFrac8) {
@@ -579,6 +622,10 @@ cudaError_t LaunchShade(const DevScene& S, const PathBuffers& B, int depth, int 
     KShadeClass<SC_DISNEY, false><<<grid, kBlock, 0, st>>>(S, B, none, depth);
     KShadeClass<SC_GENERIC, false><<<grid, kBlock, 0, st>>>(S, B, none, depth);
   }
+  return cudaGetLastError();
+}
+cudaError_t LaunchShadeAO(const DevScene& S, const PathBuffers& B, int grid, cudaStream_t st) {
+  KShadeAO<<<grid, kBlock, 0, st>>>(S, B);
   return cudaGetLastError();
 }
 cudaError_t LaunchShadow(const DevScene& S, const PathBuffers& B, int depth, int grid, cudaStream_t st,

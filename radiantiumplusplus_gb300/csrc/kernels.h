@@ -101,6 +101,8 @@ cudaError_t LaunchExtend(const DevScene& S, const PathBuffers& B, int depth, int
 // G (optional): guide network; its classes then sample the one-sample MIS mixture.
 cudaError_t LaunchShade(const DevScene& S, const PathBuffers& B, int depth, int grid, cudaStream_t st,
                         const GuideDev* G = nullptr);
+// renderer "ao": for every path of bounce 0 with a hit, one cosine-sampled visibility ray
+cudaError_t LaunchShadeAO(const DevScene& S, const PathBuffers& B, int grid, cudaStream_t st);
 cudaError_t LaunchShadow(const DevScene& S, const PathBuffers& B, int depth, int grid, cudaStream_t st,
                          unsigned long long* trav = nullptr, int refillBusy = 20, int leafFrac8 = 4);
 // spw: samples per wave of the generate stage (per pixel, in sample order, as

@@ -210,6 +210,7 @@ struct DevScene {
   int32_t envLight, globalMedium;
   float lightPdf;
   int32_t maxDepth, rrDepth, isVol;
+  int32_t isAO;                // renderer "ao" (ao.cpp): one hit, one cosine-sampled visibility ray
   CameraRec cam;
 };
 

@@ -275,6 +275,19 @@ uint64_t LaunchBounces(const DevScene& S, const TraceTune& tu, uint32_t count, P
   int tgrid = std::max(1, std::min(lib.sms * tu.blocksPerSm, (int)((count + 127) / 128)));
   int iters = S.maxDepth >= 0 ? std::max(1, S.maxDepth) : kMaxBounce;
   if (iters > kMaxBounce) iters = kMaxBounce;
+  if (S.isAO) {  // ao.cpp:22-36: first hit, one visibility ray
+    cudaEvent_t a = nullptr;
+    ps.Begin(1, a);
+    Check(LaunchExtend(S, lib.paths, 0, tgrid, lib.stream, trav, tu.refillBusy, tu.leafFrac8), "extend");
+    ps.End(1, a);
+    ps.Begin(2, a);
+    Check(LaunchShadeAO(S, lib.paths, grid, lib.stream), "ao");
+    ps.End(2, a);
+    ps.Begin(3, a);
+    Check(LaunchShadow(S, lib.paths, 0, tgrid, lib.stream, trav, tu.refillBusy, tu.leafFrac8), "shadow");
+    ps.End(3, a);
+    return 3;
+  }
   for (int d = 0; d < iters; d++) {
     cudaEvent_t a = nullptr;
     ps.Begin(1, a);
@@ -817,6 +830,7 @@ uint64_t SceneUpload(const HostScene& hs, rad_scene* sc) {
   D.maxDepth = hs.maxDepth;
   D.rrDepth = hs.rrDepth;
   D.isVol = hs.isVol ? 1 : 0;
+  D.isAO = hs.isAO ? 1 : 0;
   D.cam = hs.cam;
   return b;
 }

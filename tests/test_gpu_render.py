@@ -62,6 +62,19 @@ def test_volpath_samples(rad, oracle, scene_dir):
     g.close()
 
 
+def test_ao_samples(rad, oracle, scene_dir):
+    """Renderer `ao` (ao.cpp): the first hit and one cosine-sampled visibility ray."""
+    sc = scenes.box_room(48, 48, 4)
+    sc["renderer"] = {"type": "ao"}
+    path, text, d = write(scene_dir, "ao_box", sc)
+    g, o = rad.Scene.from_file(path), oracle.OracleScene(text, d)
+    _sample_parity(g, o, 4, 0.99)
+    film = g.render()
+    ref, _ = o.render()
+    assert abs(film.mean() - ref.mean()) < 1e-3 * ref.mean()
+    g.close()
+
+
 def test_path_samples_lights(rad, oracle, scene_dir):
     """Point and projection lights (delta lights: no MIS weight on their samples) beside
     an area emitter."""

@@ -285,3 +285,29 @@ def test_projection_light_footprint(oracle):
     assert np.allclose(L[inside], 0.5 * E[None] / h ** 2, rtol=1e-4)
     assert (L[outside] == 0).all()
     o.close()
+
+
+def test_ao_closed_forms(oracle, scene_dir):
+    """ao.cpp:22-36: 1 on an open plane, 1/2 next to a (large) wall — every direction
+    towards the wall's side of the hemisphere hits it — and 0 for misses."""
+    from helpers import write
+    sc = {"camera": {"type": "perspective", "fov": 20.0, "resolution": [16, 16], "origin": [0, 5, 0.01],
+                     "target": [0, 0, 0]},
+          "sampler": {"type": "independent", "sample_count": 1, "seed": 2},
+          "scene": [{"to_world": {"rotate": {"axis": [1, 0, 0], "angle": -90.0}, "scale": [1000, 1000, 1]},
+                     "shape": {"type": "rectangle"}}],
+          "accel": {"type": "embree"}, "renderer": {"type": "ao"}}
+    _, text, d = write(scene_dir, "ao_open", sc)
+    o = oracle.OracleScene(text, d)
+    n = 256 * 64
+    pix = np.repeat(np.arange(256, dtype=np.uint32), 64)
+    smp = np.tile(np.arange(64, dtype=np.uint32), 256)
+    v = o.render_samples(pix, smp)
+    assert np.allclose(v, 1.0, rtol=1e-6)
+    o.close()
+    sc["scene"].append({"to_world": {"translate": [0, 0, -0.3], "scale": [1000, 1000, 1]}, "shape": {"type": "rectangle"}})
+    _, text, d = write(scene_dir, "ao_wall", sc)
+    o = oracle.OracleScene(text, d)
+    v = o.render_samples(pix, smp)[:, 0]
+    assert abs(v.mean() - 0.5) < 0.01, v.mean()
+    o.close()
