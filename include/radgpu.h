@@ -250,7 +250,7 @@ RAD_API int rad_guide_grad(rad_scene* scene, const float* records, int64_t n, fl
  * depend on it. config_json may be NULL; keys: leaf_frac8 (list, default
  * [2,3,4,5,6]), refill_busy (list, default [16,20,24,28,32]), blocks_per_sm
  * (list, default [4,6,8]), reps (timed waves per candidate, 2).
- * RAD_ERR_UNSUPPORTED for `vol_path` scenes. */
+ * RAD_ERR_UNSUPPORTED for `vol_path` and `particle_tracer` scenes. */
 typedef struct rad_tune_result {
   int32_t refill_busy, blocks_per_sm; /* chosen */
   int32_t candidates;                 /* configurations timed */

@@ -387,7 +387,7 @@ struct RoughGlassBsdf final : Bsdf {
     DistParam(this, cfg, &RoughGlassBsdf::dist, env);
   }
   std::unique_ptr<Bsdf> Clone() const override { return std::make_unique<RoughGlassBsdf>(*this); }
-  std::pair<BsdfSample, Spectrum> SampleImpl(const V3& wi, Float lobeXi, const V2& dirXi, const TexSi*) const override {
+  std::pair<BsdfSample, Spectrum> SampleImpl(const V3& wi, Float lobeXi, const V2& dirXi, const TexSi* ts) const override {
     BsdfSample bsr;
     Float cosThetaI = wi.z;
     if (cosThetaI == 0) return {{}, Spectrum(0)};
@@ -401,11 +401,11 @@ struct RoughGlassBsdf final : Bsdf {
     bool isReflect = Frame::IsSameHemisphere(wi, bsr.Wo);
     bsr.Eta = isReflect ? 1 : etaIT;
     bsr.Type = BT_Glossy | (isReflect ? BT_Reflection : BT_Transmission);
-    bsr.Pdf = Pdf(wi, bsr.Wo);
+    bsr.Pdf = PdfImpl(wi, bsr.Wo, ts);
     if (bsr.Pdf <= 0) return {{}, Spectrum(0)};
-    return {bsr, Eval(wi, bsr.Wo)};
+    return {bsr, EvalImpl(wi, bsr.Wo, ts)};
   }
-  Spectrum EvalImpl(const V3& wi, const V3& wo, const TexSi*) const override {
+  Spectrum EvalImpl(const V3& wi, const V3& wo, const TexSi* ts) const override {
     Float cosThetaI = wi.z, cosThetaO = wo.z;
     if (cosThetaI == 0) return Spectrum(0);
     bool reflect = cosThetaI * cosThetaO > 0;
@@ -422,7 +422,7 @@ struct RoughGlassBsdf final : Bsdf {
       Float brdf = std::abs(F * Dv * Gv / (cosThetaI * 4));
       result = R * brdf;
     } else {
-      Float scale = Sqr(ie);
+      Float scale = (ts && ts->importance) ? Float(1) : Sqr(ie);  // rough_glass.cpp:143
       Float idm = dot(wi, m);
       Float odm = dot(wo, m);
       Float btdf = std::abs((scale * (1 - F) * Dv * Gv * e * e * idm * odm) / (cosThetaI * Sqr(idm + e * odm)));
@@ -607,7 +607,7 @@ struct DisneyBsdf final : Bsdf {
   };
 
   // disney.cpp:113-235
-  std::pair<BsdfSample, Spectrum> SampleImpl(const V3& wi, Float lobeXi, const V2& dirXi, const TexSi*) const override {
+  std::pair<BsdfSample, Spectrum> SampleImpl(const V3& wi, Float lobeXi, const V2& dirXi, const TexSi* ts) const override {
     Float cosThetaI = wi.z;
     BsdfSample bsr;
     if (cosThetaI == 0) return {bsr, Spectrum(0)};
@@ -681,13 +681,13 @@ struct DisneyBsdf final : Bsdf {
       bool reflect = cosThetaI * wo.z > Float(0);
       if (!reflect) return {bsr, Spectrum(0)};
     }
-    bsr.Pdf = Pdf(wi, bsr.Wo);
+    bsr.Pdf = PdfImpl(wi, bsr.Wo, ts);
     if (bsr.Pdf <= 0) return {bsr, Spectrum(0)};
-    return {bsr, Eval(wi, bsr.Wo)};
+    return {bsr, EvalImpl(wi, bsr.Wo, ts)};
   }
 
   // disney.cpp:237-361
-  Spectrum EvalImpl(const V3& wi, const V3& wo, const TexSi*) const override {
+  Spectrum EvalImpl(const V3& wi, const V3& wo, const TexSi* ts) const override {
     Float cosThetaI = wi.z;
     if (cosThetaI == 0) return Spectrum(0);
     Float rough = roughness;
@@ -731,7 +731,7 @@ struct DisneyBsdf final : Bsdf {
       value = value + Spectrum(dF.x * Dv * Gv / den, dF.y * Dv * Gv / den, dF.z * Dv * Gv / den);
     }
     if (hasSpecTrans && hasSpecTransLobe) {
-      Float scale = Sqr(invEtaPath);
+      Float scale = (ts && ts->importance) ? Float(1) : Sqr(invEtaPath);  // disney.cpp:304
       Float idh = dot(wi, wh), odh = dot(wo, wh);
       Float t = std::abs((scale * (Float(1) - frSpecDielectric) * Dv * Gv * etaPath * etaPath * idh * odh) /
                          (cosThetaI * Sqr(idh + etaPath * odh)));
@@ -877,7 +877,7 @@ struct PerfectGlassBsdf final : Bsdf {
     Float extIor = ReadF(cfg, "ext_ior", Float(1.000277));
     eta = intIor / extIor;
   }
-  std::pair<BsdfSample, Spectrum> SampleImpl(const V3& wi, Float lobeXi, const V2&, const TexSi*) const override {
+  std::pair<BsdfSample, Spectrum> SampleImpl(const V3& wi, Float lobeXi, const V2&, const TexSi* ts) const override {
     Float ri, cosThetaT, etaIT, etaTI;
     FresnelDielectric(wi.z, eta, ri, cosThetaT, etaIT, etaTI);
     Float ti = 1 - ri;
@@ -895,7 +895,8 @@ struct PerfectGlassBsdf final : Bsdf {
       bsr.Pdf = ti;
       bsr.Type = BT_Delta | BT_Transmission;
       f = T * ti;
-      f = f * Sqr(etaTI);
+      Float factor = (ts && ts->importance) ? Float(1) : etaTI;  // perfect_glass.cpp:64-65
+      f = f * Sqr(factor);
     }
     return {bsr, f};
   }
@@ -1025,7 +1026,7 @@ struct RoughPlasticBsdf final : PlasticBase {
     }
     dist.sampleVisible = ReadB(cfg, "sample_visible", true);
   }
-  std::pair<BsdfSample, Spectrum> SampleImpl(const V3& wi, Float lobeXi, const V2& dirXi, const TexSi*) const override {
+  std::pair<BsdfSample, Spectrum> SampleImpl(const V3& wi, Float lobeXi, const V2& dirXi, const TexSi* ts) const override {
     Float cosThetaI = wi.z;
     if (cosThetaI <= 0) return {{}, Spectrum(0)};
     Float fi = DielectricR(cosThetaI, eta);
@@ -1043,9 +1044,9 @@ struct RoughPlasticBsdf final : PlasticBase {
       bsr.Wo = SquareToCosineHemisphere(dirXi);
       bsr.Type = BT_Diffuse | BT_Reflection;
     }
-    bsr.Pdf = Pdf(wi, bsr.Wo);
+    bsr.Pdf = PdfImpl(wi, bsr.Wo, ts);
     if (bsr.Pdf <= 0) return {bsr, Spectrum(0)};
-    return {bsr, Eval(wi, bsr.Wo)};
+    return {bsr, EvalImpl(wi, bsr.Wo, ts)};
   }
   Spectrum EvalImpl(const V3& wi, const V3& wo, const TexSi*) const override {
     Float cosThetaI = wi.z, cosThetaO = wo.z;

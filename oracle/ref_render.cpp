@@ -404,6 +404,122 @@ Spectrum AOLi(const Scene& S, const Ray& ray, Pcg32& rng) {
   return l;
 }
 
+// ------------------------------------------------------ particle tracer
+// particle_tracer.cpp:135-175
+static void ConnectCamera(const Scene& S, const SurfaceInteraction& si, bool hasShape, const Bsdf* bsdf,
+                          const TexSi* ts, const DirectionSample& cam, const Spectrum& weight, Float sampleScale,
+                          std::vector<Spectrum>& image) {
+  if (cam.Pdf <= 0 || is_zero(weight)) return;
+  if (Occl(S, si.P, si.N, cam.P)) return;
+  V3 o = OffsetP(si.P, si.N, cam.P - si.P);  // SpawnRayTo (interaction.cpp:20-26)
+  V3 toCamera = cam.P - o;
+  toCamera = toCamera / norm(toCamera);
+  V3 wo = si.ToLocal(toCamera);
+  Spectrum fs(1);
+  if (!hasShape) {
+    if (wo.z <= 0) fs = Spectrum(0);
+  } else if (!bsdf) {
+    fs = fs * std::max(Float(0), wo.z);
+  } else {
+    Float idn = dot(si.N, si.ToWorld(si.Wi));
+    Float odn = dot(si.N, toCamera);
+    if (idn * si.Wi.z <= 0 || odn * wo.z <= 0) {
+      fs = Spectrum(0);
+    } else {
+      Float correction = (si.Wi.z * odn) / (wo.z * idn);
+      Spectrum bsdfVal = bsdf->Eval(si.Wi, wo, ts);
+      fs = cmul(fs, bsdfVal) * std::abs(correction) / cam.Pdf;
+    }
+  }
+  Spectrum ij = cmul(weight, fs) * sampleScale;
+  int x = (int)cam.UV.x, y = (int)cam.UV.y;
+  Spectrum& px = image[(size_t)y * S.camera.width + x];
+  px = px + ij;
+}
+
+// One light path (particle_tracer.cpp:97-226): the emitter point seen by the
+// camera, then the emitted ray with a camera connection at every vertex.
+static void ParticleSample(const Scene& S, uint64_t id, uint32_t seed, Float sampleScale, std::vector<Spectrum>& image) {
+  Pcg32 rng = Pcg32::ForSample((uint32_t)id, (uint32_t)(id >> 32), seed);
+  if (S.lights.empty()) return;
+  if (S.maxDepth != 0) {  // SampleLight (:104-133)
+    int index;
+    Float lightPdf;
+    S.SampleLight(rng.Next1D(), index, lightPdf);
+    const Light& L = S.lights[index];
+    if (!L.IsDelta()) {
+      SurfaceInteraction si;
+      Spectrum li;
+      bool hasShape = L.kind == Light::Area;
+      if (!hasShape) {
+        V3 camPos = S.camera.cameraToWorld.ApplyAffineToWorld(V3(0, 0, 0));
+        auto r = S.SampleOneLightDirection(index, camPos, rng.Next2D());
+        li = r.second;
+        lightPdf *= r.first.Pdf > 0 ? (r.first.Pdf * Sqr(r.first.Dist)) : 0;
+        si.P = r.first.P;
+        si.N = r.first.N;
+      } else {
+        PositionSample psr = S.shapes[L.shape].SamplePosition(rng.Next2D());
+        lightPdf *= psr.Pdf;
+        si.P = psr.P;
+        si.N = psr.N;
+        li = L.radiance;
+      }
+      si.Shading = Frame(si.N);
+      rng.Next2D();  // Perspective::SampleDirection's sample
+      DirectionSample cam;
+      Float we = S.camera.SampleDirection(si.P, cam);
+      Spectrum weight = li * we / lightPdf;
+      si.Wi = si.ToLocal(cam.Dir);
+      ConnectCamera(S, si, hasShape, nullptr, nullptr, cam, weight, sampleScale, image);
+    }
+  }
+  int index;
+  Float lightPdf;
+  S.SampleLight(rng.Next1D(), index, lightPdf);
+  V2 xi2 = rng.Next2D(), xi3 = rng.Next2D();
+  Ray ray;
+  Spectrum li;
+  if (!S.LightSampleRay(index, xi2, xi3, ray, li)) return;
+  Spectrum throughput = li / lightPdf;
+  // TraceLightRay (:177-226)
+  Float eta = 1;
+  int depth = 1;
+  SurfaceInteraction si;
+  bool isHit = Trace(S, ray, si);
+  if (!isHit || S.shapes[si.shape].bsdf < 0) return;
+  if (S.maxDepth >= 0 && depth >= S.maxDepth) return;
+  for (;;) {
+    const Bsdf& bsdf = *S.bsdfs[S.shapes[si.shape].bsdf];
+    TexSi ts = si.Tex();
+    ts.importance = true;
+    rng.Next2D();
+    DirectionSample cam;
+    Float we = S.camera.SampleDirection(si.P, cam);
+    ConnectCamera(S, si, true, &bsdf, &ts, cam, throughput * we, sampleScale, image);
+    Float bl = rng.Next1D();
+    V2 bd = rng.Next2D();
+    auto bs = bsdf.Sample(si.Wi, bl, bd, &ts);
+    V3 woW = si.ToWorld(bs.first.Wo);
+    Float idn = dot(si.N, -ray.D), odn = dot(si.N, woW);
+    if (idn * si.Wi.z <= 0 || odn * bs.first.Wo.z <= 0) break;
+    Float correction = (si.Wi.z * odn) / (bs.first.Wo.z * idn);
+    throughput = cmul(throughput, bs.second) * std::abs(correction) / bs.first.Pdf;
+    eta *= bs.first.Eta;
+    if (is_zero(throughput)) break;
+    ray = SpawnRay(si.P, si.N, woW);
+    isHit = Trace(S, ray, si);
+    depth++;
+    if (!isHit || S.shapes[si.shape].bsdf < 0) break;
+    if (S.maxDepth >= 0 && depth >= S.maxDepth) return;
+    if (depth >= S.rrDepth) {
+      Float rr = std::min(max_comp(throughput) * Sqr(eta), Float(0.95));
+      if (rng.Next1D() > rr) break;
+      throughput = throughput * Rcp(rr);
+    }
+  }
+}
+
 // sample_renderer.cpp:93-106: one pixel sample. The jitter takes the first two
 // draws of the sample's stream (the reference uses a separate per-tile mt19937).
 static Spectrum RenderSample(const Scene& S, uint32_t x, uint32_t y, uint32_t s, uint32_t seed) {
@@ -567,6 +683,27 @@ int orc_render(void* sp, int row0, int row1, int rowStep, int s0, int s1, int se
     stats[1] = nS;
     stats[2] = nSamp;
     stats[3] = nBad;
+  }
+  return 0;
+}
+
+// particle_tracer: light paths [first, first + count) of `spp` splatted into
+// film (W x H x 3, accumulated onto its contents).
+int orc_render_particle(void* sp, uint64_t first, uint64_t count, uint64_t spp, uint32_t seed, float* film) {
+  Scene& S = *(Scene*)sp;
+  try {
+    size_t npix = (size_t)S.camera.width * S.camera.height;
+    std::vector<Spectrum> image(npix, Spectrum(0));
+    Float sampleScale = npix / ((Float)spp);
+    for (uint64_t i = 0; i < count; i++) ParticleSample(S, first + i, seed, sampleScale, image);
+    for (size_t p = 0; p < npix; p++) {
+      film[3 * p] += image[p].x;
+      film[3 * p + 1] += image[p].y;
+      film[3 * p + 2] += image[p].z;
+    }
+  } catch (const std::exception& e) {
+    g_err = e.what();
+    return -1;
   }
   return 0;
 }

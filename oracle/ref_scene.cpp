@@ -451,6 +451,34 @@ Ray Camera::SampleRayDifferential(const V2& screen, RayDiff& diff) const {
   return r;
 }
 
+Float Camera::SampleDirection(const V3& ref, DirectionSample& dsr) const {
+  V3 refP = cameraToWorld.ApplyAffineToLocal(ref);
+  dsr = DirectionSample();
+  dsr.Pdf = 0;
+  if (refP.z < nearZ || refP.z > farZ) return 0;
+  V3 ndcPos = cameraToClip.ApplyAffineToWorld(refP);
+  if (ndcPos.x < 0 || ndcPos.x >= 1 || ndcPos.y < 0 || ndcPos.y >= 1) return 0;
+  dsr.UV = V2(ndcPos.x * Float(width), ndcPos.y * Float(height));
+  Float dist = norm(refP);
+  Float invDist = Rcp(dist);
+  V3 dir = refP * invDist;
+  dsr.P = cameraToWorld.ApplyAffineToWorld(V3(0, 0, 0));
+  dsr.Dir = (dsr.P - ref) * invDist;
+  dsr.Dist = dist;
+  dsr.N = cameraToWorld.ApplyLinearToWorld(V3(0, 0, 1));
+  dsr.Pdf = 1;
+  // Importance (perspective.cpp:124-135)
+  Float importance = 0;
+  Float cosTheta = dir.z;
+  if (cosTheta > 0) {
+    Float invCosTheta = Rcp(cosTheta);
+    V2 p(dir.x * invCosTheta, dir.y * invCosTheta);
+    if (rectMin.x <= p.x && rectMin.y <= p.y && p.x <= rectMax.x && p.y <= rectMax.y)
+      importance = normalization * invCosTheta * invCosTheta * invCosTheta;
+  }
+  return importance * invDist * invDist;
+}
+
 void SurfaceInteraction::ComputeDifferentials(const RayDiff& ray) {
   if (!(ray.has && dUVdX.x == 0 && dUVdX.y == 0 && dUVdY.x == 0 && dUVdY.y == 0)) return;
   Float d = dot(N, P);
@@ -518,6 +546,12 @@ static Camera MakeCamera(const Json& cfg) {
   V3 o = c.cameraToClip.ApplyAffineToLocal(V3(0, 0, 0));
   c.dx = c.cameraToClip.ApplyAffineToLocal(V3(Float(1) / c.width, 0, 0)) - o;
   c.dy = c.cameraToClip.ApplyAffineToLocal(V3(0, Float(1) / c.height, 0)) - o;
+  V3 pMin = c.cameraToClip.ApplyAffineToLocal(V3(0, 0, 0));
+  V3 pMax = c.cameraToClip.ApplyAffineToLocal(V3(1, 1, 0));
+  V2 a(pMin.x / pMin.z, pMin.y / pMin.z), b(pMax.x / pMax.z, pMax.y / pMax.z);
+  c.rectMin = V2(std::min(a.x, b.x), std::min(a.y, b.y));  // BoundingBox2::extend
+  c.rectMax = V2(std::max(a.x, b.x), std::max(a.y, b.y));
+  c.normalization = 1 / ((c.rectMax.x - c.rectMin.x) * (c.rectMax.y - c.rectMin.y));
   return c;
 }
 
@@ -949,6 +983,9 @@ std::unique_ptr<Scene> Scene::FromJson(const std::string& text, const std::strin
         translate.m[0][3] = -1;
         translate.m[1][3] = -1 / aspect;
         L.toClip = Transform(scale * translate * persp);
+        V3 pMin = L.toClip.ApplyAffineToLocal(V3(0, 0, 0)), pMax = L.toClip.ApplyAffineToLocal(V3(1, 1, 0));
+        Float ax = pMin.x / pMin.z, ay = pMin.y / pMin.z, bx = pMax.x / pMax.z, by = pMax.y / pMax.z;
+        L.cameraArea = 1 / ((bx - ax) * (by - ay));  // BoundingBox2(min, max).volume()
       } else if (type == "directional") {
         L.kind = Light::Directional;
         L.radiance = color("irradiance", V3(1));
@@ -1008,7 +1045,7 @@ std::unique_ptr<Scene> Scene::FromJson(const std::string& text, const std::strin
   const Json* rn = root.find("renderer");
   if (!rn) throw std::runtime_error("no child: renderer");
   S.renderer = ReadS(rn, "type", "");
-  if (S.renderer != "path" && S.renderer != "vol_path" && S.renderer != "ao")
+  if (S.renderer != "path" && S.renderer != "vol_path" && S.renderer != "ao" && S.renderer != "particle_tracer")
     throw std::runtime_error("cannot find factory: " + S.renderer);
   S.maxDepth = ReadI(rn, "max_depth", -1);
   S.rrDepth = ReadI(rn, "rr_depth", S.renderer == "path" ? 3 : 5);
@@ -1534,9 +1571,16 @@ std::pair<DirectionSample, Spectrum> Scene::SampleLightDirection(const V3& refP,
   int index;
   Float pdf;
   SampleLight(xiL, index, pdf);
+  if (index < 0) return {DirectionSample(), Spectrum(0)};
+  auto r = SampleOneLightDirection(index, refP, xi);
+  r.first.Pdf *= pdf;
+  return r;
+}
+
+// Light::SampleDirection of light l.
+std::pair<DirectionSample, Spectrum> Scene::SampleOneLightDirection(int index, const V3& refP, const V2& xi) const {
   DirectionSample dsr;
   Spectrum li(0);
-  if (index < 0) return {dsr, li};
   const Light& L = lights[index];
   if (L.kind == Light::Area) {
     dsr = shapes[L.shape].SampleDirection(refP, xi);
@@ -1624,7 +1668,6 @@ std::pair<DirectionSample, Spectrum> Scene::SampleLightDirection(const V3& refP,
     dsr.IsDelta = true;
     li = L.radiance;
   }
-  dsr.Pdf *= pdf;
   return {dsr, li};
 }
 
@@ -1653,6 +1696,87 @@ Float Scene::PdfLightDirection(int l, const V3& refP, const DirectionSample& dsr
     }
   }
   return p * lightPdf;
+}
+
+}  // namespace orc
+
+namespace orc {
+
+// Light::SampleRay
+bool Scene::LightSampleRay(int l, const V2& xi2, const V2& xi3, Ray& ray, Spectrum& li) const {
+  const Light& L = lights[l];
+  ray = Ray();
+  ray.MinT = 0;
+  ray.MaxT = std::numeric_limits<Float>::max();
+  if (L.kind == Light::Area) {  // area.cpp:120-128
+    PositionSample psr = shapes[L.shape].SamplePosition(xi2);
+    Float pdf = psr.Pdf;
+    V3 local = SquareToCosineHemisphere(xi3);
+    Frame fr(psr.N);  // SurfaceInteraction(psr)
+    V3 d = fr.ToWorld(local);
+    ray = SpawnRay(psr.P, psr.N, d);
+    Spectrum eval = L.radiance;  // Eval(si) with no incident direction: dot(0, N) >= 0
+    li = eval * PI / pdf;
+    return true;
+  }
+  if (L.kind == Light::Point) {  // point.cpp:67-71
+    ray.O = L.worldPos;
+    ray.D = SquareToUniformSphere(xi3);
+    li = L.radiance * 4 * PI;
+    return true;
+  }
+  if (L.kind == Light::Projection) {  // projection.cpp:93-104
+    V2 uv = xi3;
+    V3 nearP = L.toClip.ApplyAffineToLocal(V3(uv.x, uv.y, 0));
+    V3 nearDir = normalized(nearP);
+    ray.O = V3(L.toWorld.ToWorld.m[0][3], L.toWorld.ToWorld.m[1][3], L.toWorld.ToWorld.m[2][3]);
+    ray.D = L.toWorld.ApplyLinearToWorld(nearDir);
+    li = cmul(L.radiance, L.scale) * PI * L.cameraArea;
+    return true;
+  }
+  Float R = L.worldRadius;
+  // SquareToUniformDiskConcentric (warp.cpp:80-95)
+  Float x = Fmadd(2, xi2.x, -1), y = Fmadd(2, xi2.y, -1);
+  bool quadrant = std::abs(x) < std::abs(y);
+  Float r = quadrant ? y : x, rp = quadrant ? x : y;
+  Float phi0 = Float(0.25) * PI * rp / r;
+  if (quadrant) phi0 = Float(0.5) * PI - phi0;
+  if (x == 0 && y == 0) phi0 = 0;
+  V2 offset(r * std::cos(phi0), r * std::sin(phi0));
+  if (L.kind == Light::Skybox) {  // skybox.cpp:135-163
+    Float pdfDir;
+    V2 uv;
+    if (L.uniformMap) {
+      pdfDir = SquareToUniformSpherePdf();
+      uv = xi3;
+    } else {
+      auto [iu, iv, pdf0] = L.dist.Sample(xi3);
+      pdfDir = pdf0;
+      if (pdf0 <= 0) return false;
+      Float vy = iv / (Float)L.map->height, vx = iu / (Float)L.map->width;
+      uv = V2(vx, vy);
+      Float sinTheta = std::sin(vy * PI);
+      if (sinTheta == 0) return false;
+      pdfDir /= (2 * PI * PI * sinTheta);
+    }
+    if (pdfDir <= 0) return false;
+    Float theta = uv.y * PI, phi = uv.x * PI * 2;
+    V3 sph(std::cos(phi) * std::sin(theta), std::sin(phi) * std::sin(theta), std::cos(theta));
+    V3 d(sph.y, sph.z, -sph.x);
+    V3 worldD = L.toWorld.ApplyAffineToWorld(-d);
+    V3 perp = Frame(d).ToWorld(V3(offset.x, offset.y, 0));
+    ray.O = L.worldCenter + (perp - worldD) * R;
+    ray.D = worldD;
+    Spectrum c = L.map ? L.map->Eval(TexSi{uv, V2(), V2()}) : L.radiance;
+    li = c * PI * Sqr(R) / pdfDir;
+    return true;
+  }
+  // directional (extension): parallel rays through a disk covering the world sphere
+  V3 perp = Frame(L.direction).ToWorld(V3(offset.x, offset.y, 0));
+  ray.O = L.worldCenter + (perp - L.direction) * R;
+  ray.D = L.direction;
+  li = L.radiance * PI * Sqr(R);
+  return true;
 }
 
 }  // namespace orc

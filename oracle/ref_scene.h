@@ -146,6 +146,7 @@ struct Light {
   std::shared_ptr<Texture> map;  // skybox: radiance texture (null: constant radiance)
   bool uniformMap = true;        // skybox: 1 x 1 map, uniform sphere sampling
   Continuous2D dist;             // skybox: luminance distribution of a bitmap map
+  Float cameraArea = 0;          // projection: 1 / area of the image rectangle (projection.cpp:41-44)
   V3 worldCenter;
   Float worldRadius = 0;
   bool IsEnv() const { return kind == Skybox; }
@@ -189,7 +190,12 @@ struct Camera {  // perspective.cpp:15-70
   Float nearZ = 0.001f, farZ = 100;
   Transform cameraToWorld, cameraToClip;
   V3 dx, dy;  // perspective.cpp:56-59
+  V2 rectMin, rectMax;  // _imageRect (perspective.cpp:61-65)
+  Float normalization = 0;
   Ray SampleRay(const V2& screen) const;
+  // Perspective::SampleDirection + Importance (perspective.cpp:101-137): dsr.UV is the pixel position,
+  // dsr.Pdf 0 outside the frustum; returns the importance
+  Float SampleDirection(const V3& ref, DirectionSample& dsr) const;
   Ray SampleRayDifferential(const V2& screen, RayDiff& diff) const;  // perspective.cpp:84-97
 };
 
@@ -235,6 +241,10 @@ struct Scene {
   void SampleLight(Float xi, int& index, Float& pdf) const;
   int LightOf(const SurfaceInteraction& si) const;  // scene.cpp:105-113, -1 if none
   std::pair<DirectionSample, Spectrum> SampleLightDirection(const V3& refP, Float xiL, const V2& xi) const;
+  std::pair<DirectionSample, Spectrum> SampleOneLightDirection(int light, const V3& refP, const V2& xi) const;
+  // Light::SampleRay (area.cpp:120-128, skybox.cpp:135-163, point.cpp:67-71, projection.cpp:93-104);
+  // false when the light emits nothing for this sample
+  bool LightSampleRay(int light, const V2& xi2, const V2& xi3, Ray& ray, Spectrum& li) const;
   Float PdfLightDirection(int light, const V3& refP, const DirectionSample& dsr) const;
   Spectrum EvalLight(int light, const SurfaceInteraction& si) const;
   uint64_t PrimCount() const { return prims.size(); }

@@ -17,6 +17,9 @@ namespace orc {
 // screen-space derivatives (interaction.h: UV, dUVdX, dUVdY).
 struct TexSi {
   V2 uv, duvdx, duvdy;
+  // BsdfContext::Mode == TransportMode::Importance (light tracing, particle_tracer.cpp:161, :199); BSDF calls
+  // carry it with the surface point
+  bool importance = false;
 };
 
 // RGB textures return (r, g, b); mono textures return (v, 0, 0).

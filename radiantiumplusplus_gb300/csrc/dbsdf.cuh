@@ -93,7 +93,7 @@ RD BsdfSampleRes MetalSample(const MatRec& m, V3 wi, V2 dirXi) {
 }
 
 // ------------------------------------------------------------- rough_glass
-RD void GlassEvalPdf(const MatRec& m, V3 wi, V3 wo, V3& f, float& pdf) {
+RD void GlassEvalPdf(const MatRec& m, V3 wi, V3 wo, V3& f, float& pdf, bool imp = false) {
   f = v3s(0.f);
   pdf = 0.f;
   float cosThetaI = wi.z, cosThetaO = wo.z;
@@ -114,7 +114,7 @@ RD void GlassEvalPdf(const MatRec& m, V3 wi, V3 wo, V3& f, float& pdf) {
     float brdf = fabsf(F * D * G / (cosThetaI * 4.f));
     f = ld3(m.p) * brdf;
   } else {
-    float scale = Sqr(ie);
+    float scale = imp ? 1.f : Sqr(ie);  // TransportMode::Importance: no eta^2 (rough_glass.cpp:143)
     float btdf = fabsf((scale * (1.f - F) * D * G * e * e * idm * odm) / (cosThetaI * Sqr(idm + e * odm)));
     f = ld3(m.p + 3) * btdf;
   }
@@ -126,7 +126,7 @@ RD void GlassEvalPdf(const MatRec& m, V3 wi, V3 wo, V3& f, float& pdf) {
   p *= reflect ? Fp : (1.f - Fp);
   pdf = fabsf(p * dwhdwo);
 }
-RD BsdfSampleRes GlassSample(const MatRec& m, V3 wi, float lobeXi, V2 dirXi) {
+RD BsdfSampleRes GlassSample(const MatRec& m, V3 wi, float lobeXi, V2 dirXi, bool imp = false) {
   BsdfSampleRes r{};
   float cosThetaI = wi.z;
   if (cosThetaI == 0.f) return r;
@@ -140,7 +140,7 @@ RD BsdfSampleRes GlassSample(const MatRec& m, V3 wi, float lobeXi, V2 dirXi) {
   bool isReflect = wi.z * wo.z > 0.f;
   V3 f;
   float pdf;
-  GlassEvalPdf(m, wi, wo, f, pdf);
+  GlassEvalPdf(m, wi, wo, f, pdf, imp);
   if (pdf <= 0.f) return BsdfSampleRes{};
   r.wo = wo;
   r.eta = isReflect ? 1.f : fr.etaIT;
@@ -244,7 +244,7 @@ RD float SmithGGX1(V3 v, V3 wh, float alpha) {  // disney.cpp:596-612
 }
 
 // disney.cpp:237-456: value and density for one (wi, wo).
-RD void DisneyEvalPdf(const MatRec& m, V3 wi, V3 wo, V3& f, float& pdf) {
+RD void DisneyEvalPdf(const MatRec& m, V3 wi, V3 wo, V3& f, float& pdf, bool imp = false) {
   f = v3s(0.f);
   pdf = 0.f;
   float cosThetaI = wi.z;
@@ -305,7 +305,7 @@ RD void DisneyEvalPdf(const MatRec& m, V3 wi, V3 wo, V3& f, float& pdf) {
     value = value + V3{dF.x * D * G / den, dF.y * D * G / den, dF.z * D * G / den};
   }
   if (hasST && lobeST) {
-    float scale = Sqr(invEtaPath);
+    float scale = imp ? 1.f : Sqr(invEtaPath);  // disney.cpp:304
     float idh = dot(wi, wh), odh = dot(wo, wh);
     float t = fabsf((scale * (1.f - frD) * D * G * etaPath * etaPath * idh * odh) /
                     (cosThetaI * Sqr(idh + etaPath * odh)));
@@ -382,7 +382,7 @@ RD void DisneyEvalPdf(const MatRec& m, V3 wi, V3 wo, V3& f, float& pdf) {
 }
 
 // disney.cpp:113-235
-RD BsdfSampleRes DisneySample(const MatRec& m, V3 wi, float lobeXi, V2 dirXi) {
+RD BsdfSampleRes DisneySample(const MatRec& m, V3 wi, float lobeXi, V2 dirXi, bool imp = false) {
   BsdfSampleRes r{};
   float cosThetaI = wi.z;
   if (cosThetaI == 0.f) return r;
@@ -445,7 +445,7 @@ RD BsdfSampleRes DisneySample(const MatRec& m, V3 wi, float lobeXi, V2 dirXi) {
   }
   V3 f;
   float pdf;
-  DisneyEvalPdf(m, wi, wo, f, pdf);
+  DisneyEvalPdf(m, wi, wo, f, pdf, imp);
   r.wo = wo;
   r.pdf = pdf;
   if (pdf <= 0.f) {
@@ -471,7 +471,7 @@ RD BsdfSampleRes MirrorSample(const MatRec& m, V3 wi) {
 
 // ----------------------------------------------------------- perfect_glass
 // perfect_glass.cpp:29-72 (radiance transport); Eval and Pdf are 0.
-RD BsdfSampleRes PerfectGlassSample(const MatRec& m, V3 wi, float lobeXi) {
+RD BsdfSampleRes PerfectGlassSample(const MatRec& m, V3 wi, float lobeXi, bool imp = false) {
   BsdfSampleRes r{};
   Dielectric fr = FresnelDielectric(wi.z, m.p[6]);
   float ti = 1.f - fr.r;
@@ -486,7 +486,8 @@ RD BsdfSampleRes PerfectGlassSample(const MatRec& m, V3 wi, float lobeXi) {
     r.eta = fr.etaIT;
     r.pdf = ti;
     r.type = BT_DELTA | BT_TRANSMISSION;
-    r.f = (ld3(m.p + 3) * ti) * Sqr(fr.etaTI);
+    r.f = ld3(m.p + 3) * ti;
+    if (!imp) r.f = r.f * Sqr(fr.etaTI);  // radiance transport (perfect_glass.cpp:63-65)
   }
   return r;
 }
@@ -607,25 +608,25 @@ RD BsdfSampleRes RoughPlasticSample(const MatRec& m, V3 wi, float lobeXi, V2 dir
 }
 
 // ---------------------------------------------------------------- dispatch
-RD void LeafEvalPdf(const MatRec& m, V3 wi, V3 wo, V3& f, float& pdf) {
+RD void LeafEvalPdf(const MatRec& m, V3 wi, V3 wo, V3& f, float& pdf, bool imp = false) {
   switch (m.kind) {
     case MAT_DIFFUSE: DiffuseEvalPdf(m, wi, wo, f, pdf); return;
     case MAT_ROUGH_METAL: MetalEvalPdf(m, wi, wo, f, pdf); return;
-    case MAT_ROUGH_GLASS: GlassEvalPdf(m, wi, wo, f, pdf); return;
-    case MAT_DISNEY: DisneyEvalPdf(m, wi, wo, f, pdf); return;
+    case MAT_ROUGH_GLASS: GlassEvalPdf(m, wi, wo, f, pdf, imp); return;
+    case MAT_DISNEY: DisneyEvalPdf(m, wi, wo, f, pdf, imp); return;
     case MAT_PLASTIC: PlasticEvalPdf(m, wi, wo, f, pdf); return;
     case MAT_ROUGH_PLASTIC: RoughPlasticEvalPdf(m, wi, wo, f, pdf); return;
     default: f = v3s(0.f); pdf = 0.f; return;  // delta-only BSDFs: Eval = Pdf = 0
   }
 }
-RD BsdfSampleRes LeafSample(const MatRec& m, V3 wi, float lobeXi, V2 dirXi) {
+RD BsdfSampleRes LeafSample(const MatRec& m, V3 wi, float lobeXi, V2 dirXi, bool imp = false) {
   switch (m.kind) {
     case MAT_DIFFUSE: return DiffuseSample(m, wi, dirXi);
     case MAT_ROUGH_METAL: return MetalSample(m, wi, dirXi);
-    case MAT_ROUGH_GLASS: return GlassSample(m, wi, lobeXi, dirXi);
-    case MAT_DISNEY: return DisneySample(m, wi, lobeXi, dirXi);
+    case MAT_ROUGH_GLASS: return GlassSample(m, wi, lobeXi, dirXi, imp);
+    case MAT_DISNEY: return DisneySample(m, wi, lobeXi, dirXi, imp);
     case MAT_PERFECT_MIRROR: return MirrorSample(m, wi);
-    case MAT_PERFECT_GLASS: return PerfectGlassSample(m, wi, lobeXi);
+    case MAT_PERFECT_GLASS: return PerfectGlassSample(m, wi, lobeXi, imp);
     case MAT_PLASTIC: return PlasticSample(m, wi, lobeXi, dirXi);
     case MAT_ROUGH_PLASTIC: return RoughPlasticSample(m, wi, lobeXi, dirXi);
     default: return BsdfSampleRes{};
@@ -638,7 +639,8 @@ RD BsdfSampleRes LeafSample(const MatRec& m, V3 wi, float lobeXi, V2 dirXi) {
 // Scales are applied innermost first, as the nested calls would apply them; the
 // host limits wrapper nesting to kMaxBsdfNest levels. With a texture context,
 // textured parameters are looked up at its uv (dtex.cuh).
-RD void BsdfEvalPdf(const MatRec* mats, uint32_t mi, V3 wi, V3 wo, V3& f, float& pdf, const TexCtx* tc = nullptr) {
+RD void BsdfEvalPdf(const MatRec* mats, uint32_t mi, V3 wi, V3 wo, V3& f, float& pdf, const TexCtx* tc = nullptr,
+                    bool imp = false) {
   float ops[kMaxBsdfNest];
   int nops = 0;
   f = v3s(0.f);
@@ -662,7 +664,7 @@ RD void BsdfEvalPdf(const MatRec* mats, uint32_t mi, V3 wi, V3 wo, V3& f, float&
       mi = m.ref0;
     } else {
       MatRec tmp;
-      LeafEvalPdf(TexturedMat(m, tc, tmp), wi, wo, f, pdf);
+      LeafEvalPdf(TexturedMat(m, tc, tmp), wi, wo, f, pdf, imp);
       break;
     }
   }
@@ -672,7 +674,7 @@ RD void BsdfEvalPdf(const MatRec* mats, uint32_t mi, V3 wi, V3 wo, V3& f, float&
   }
 }
 RD BsdfSampleRes BsdfSample(const MatRec* mats, uint32_t mi, V3 wi, float lobeXi, V2 dirXi,
-                            const TexCtx* tc = nullptr) {
+                            const TexCtx* tc = nullptr, bool imp = false) {
   float ops[kMaxBsdfNest];
   int nops = 0;
   bool flip = false;
@@ -706,7 +708,7 @@ RD BsdfSampleRes BsdfSample(const MatRec* mats, uint32_t mi, V3 wi, float lobeXi
       }
     } else {
       MatRec tmp;
-      r = LeafSample(TexturedMat(m, tc, tmp), wi, lobeXi, dirXi);
+      r = LeafSample(TexturedMat(m, tc, tmp), wi, lobeXi, dirXi, imp);
       break;
     }
   }

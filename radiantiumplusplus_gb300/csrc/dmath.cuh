@@ -221,6 +221,18 @@ RD V3 SquareToUniformSphere(V2 u) {
   return V3{r * cosf(a), r * sinf(a), z};
 }
 RD float SquareToUniformSpherePdf() { return 1.f / (4.f * kPi); }
+// warp.cpp:80-95 (Shirley-Chiu concentric mapping)
+RD V2 SquareToUniformDiskConcentric(V2 u) {
+  float x = fmaf(2.f, u.x, -1.f);
+  float y = fmaf(2.f, u.y, -1.f);
+  bool quadrant = fabsf(x) < fabsf(y);
+  float r = quadrant ? y : x;
+  float rp = quadrant ? x : y;
+  float phi = 0.25f * kPi * rp / r;
+  if (quadrant) phi = 0.5f * kPi - phi;
+  if (x == 0.f && y == 0.f) phi = 0.f;
+  return V2{r * cosf(phi), r * sinf(phi)};
+}
 RD float SquareToUniformConePdf(float cosCutoff) { return 1.f / (2.f * kPi) / (1.f - cosCutoff); }
 
 // ---------------------------------------------------------------- fresnel

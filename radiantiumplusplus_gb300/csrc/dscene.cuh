@@ -207,6 +207,44 @@ RD uint32_t CdfLowerBound(const float* cdf, uint32_t n, float value) {
   return lo;
 }
 
+// Shape::SamplePosition (mesh_base.cpp:84-110, rectangle.cpp:221-230,
+// sphere.cpp:250-258): position, normal, area density.
+RD void ShapeSamplePosition(const DevScene& S, const ShapeRec& sh, V2 xi, V3& P, V3& N, float& pdf) {
+  if (sh.kind == SHAPE_SPHERE) {
+    V3 local = SquareToUniformSphere(xi);
+    P = Fmadd(local, v3s(sh.m[3]), V3{sh.m[0], sh.m[1], sh.m[2]});
+    N = local;
+    pdf = 1.f / sh.surfaceArea;
+    return;
+  }
+  if (sh.kind == SHAPE_MESH) {
+    const float* cdf = S.cdf + 2 * (size_t)sh.cdfOffset;
+    float value = xi.y * sh.cdfSum;
+    uint32_t idx = CdfLowerBound(cdf, sh.primCount, value);
+    float pm = cdf[2 * (size_t)idx + 1] * sh.cdfNorm;
+    float cd = idx == 0 ? 0.f : cdf[2 * (size_t)(idx - 1)] * sh.cdfNorm;
+    V2 txi{xi.x, (xi.y - cd) / pm};
+    uint32_t tri = idx + sh.triOffset;
+    uint32_t f0 = S.idx[3 * (size_t)tri], f1 = S.idx[3 * (size_t)tri + 1], f2 = S.idx[3 * (size_t)tri + 2];
+    V3 p0 = ld3(S.pos + 3 * (size_t)f0), p1 = ld3(S.pos + 3 * (size_t)f1), p2 = ld3(S.pos + 3 * (size_t)f2);
+    V3 e0 = p1 - p0, e1 = p2 - p0;
+    V2 b = SquareToUniformTriangle(txi);
+    P = e0 * b.x + (e1 * b.y + p0);
+    pdf = sh.cdfNorm;
+    if (!sh.hasNormals) {
+      N = normalized(cross(e0, e1));
+    } else {
+      V3 n0 = ld3(S.nrm + 3 * (size_t)f0), n1 = ld3(S.nrm + 3 * (size_t)f1), n2 = ld3(S.nrm + 3 * (size_t)f2);
+      N = normalized(n0 * (1.f - b.x - b.y) + (n1 * b.x + (n2 * b.y)));
+    }
+  } else {
+    float sx = xi.x * 2.f - 1.f, sy = xi.y * 2.f - 1.f;
+    P = AffineRows(sh.m, V3{sx, sy, 0.f});
+    N = ShapeM3(sh, 18);
+    pdf = 1.f / sh.surfaceArea;
+  }
+}
+
 // Shape::SamplePosition + SampleDirection (shape.cpp:7-19, mesh_base.cpp:84-110,
 // rectangle.cpp:204-214, sphere.cpp:251-320).
 RD DirSample ShapeSampleDirection(const DevScene& S, const ShapeRec& sh, V3 refP, V2 xi) {
@@ -214,32 +252,7 @@ RD DirSample ShapeSampleDirection(const DevScene& S, const ShapeRec& sh, V3 refP
   if (sh.kind != SHAPE_SPHERE) {
     V3 P, N;
     float pdf;
-    if (sh.kind == SHAPE_MESH) {
-      const float* cdf = S.cdf + 2 * (size_t)sh.cdfOffset;
-      float value = xi.y * sh.cdfSum;
-      uint32_t idx = CdfLowerBound(cdf, sh.primCount, value);
-      float pm = cdf[2 * (size_t)idx + 1] * sh.cdfNorm;
-      float cd = idx == 0 ? 0.f : cdf[2 * (size_t)(idx - 1)] * sh.cdfNorm;
-      V2 txi{xi.x, (xi.y - cd) / pm};
-      uint32_t tri = idx + sh.triOffset;
-      uint32_t f0 = S.idx[3 * (size_t)tri], f1 = S.idx[3 * (size_t)tri + 1], f2 = S.idx[3 * (size_t)tri + 2];
-      V3 p0 = ld3(S.pos + 3 * (size_t)f0), p1 = ld3(S.pos + 3 * (size_t)f1), p2 = ld3(S.pos + 3 * (size_t)f2);
-      V3 e0 = p1 - p0, e1 = p2 - p0;
-      V2 b = SquareToUniformTriangle(txi);
-      P = e0 * b.x + (e1 * b.y + p0);
-      pdf = sh.cdfNorm;
-      if (!sh.hasNormals) {
-        N = normalized(cross(e0, e1));
-      } else {
-        V3 n0 = ld3(S.nrm + 3 * (size_t)f0), n1 = ld3(S.nrm + 3 * (size_t)f1), n2 = ld3(S.nrm + 3 * (size_t)f2);
-        N = normalized(n0 * (1.f - b.x - b.y) + (n1 * b.x + (n2 * b.y)));
-      }
-    } else {
-      float sx = xi.x * 2.f - 1.f, sy = xi.y * 2.f - 1.f;
-      P = AffineRows(sh.m, V3{sx, sy, 0.f});
-      N = ShapeM3(sh, 18);
-      pdf = 1.f / sh.surfaceArea;
-    }
+    ShapeSamplePosition(S, sh, xi, P, N, pdf);
     d.P = P;
     d.N = N;
     d.IsDelta = false;
@@ -382,27 +395,25 @@ RD V3 EnvRadiance(const DevScene& S, const LightRec& L, V3 d) {
   return V3{r.c[0], r.c[1], r.c[2]};
 }
 
-// scene.cpp:65-96: uniform light pick, then the light's direction sample.
-RD DirSample SampleLightDirection(const DevScene& S, V3 refP, float xiL, V2 xi, V3& li) {
+// Scene::SampleLight (scene.cpp:65-77): uniform pick; false without lights.
+RD bool PickLight(const DevScene& S, float xiL, int& index, float& pick) {
+  if (S.nLights < 2) {
+    index = 0;
+    pick = 1.f;
+    return S.nLights == 1;
+  }
+  float lf = xiL * (float)S.nLights;
+  uint32_t iu = (uint32_t)lf;
+  index = (int)(iu < S.nLights - 1 ? iu : S.nLights - 1);
+  pick = S.lightPdf;
+  return true;
+}
+
+// Light::SampleDirection of one light (area.cpp:47-75, skybox.cpp:65-106,
+// point.cpp:33-49, projection.cpp:52-74, the directional extension).
+RD DirSample LightSampleDirection(const DevScene& S, const LightRec& L, V3 refP, V2 xi, V3& li) {
   DirSample d{};
   li = v3s(0.f);
-  int index;
-  float pick;
-  if (S.nLights < 2) {
-    if (S.nLights == 1) {
-      index = 0;
-      pick = 1.f;
-    } else {
-      d.Pdf = 0.f;
-      return d;
-    }
-  } else {
-    float lf = xiL * (float)S.nLights;
-    uint32_t iu = (uint32_t)lf;
-    index = (int)(iu < S.nLights - 1 ? iu : S.nLights - 1);
-    pick = S.lightPdf;
-  }
-  const LightRec& L = S.lights[index];
   V3 rad{L.radiance[0], L.radiance[1], L.radiance[2]};
   if (L.kind == LIGHT_AREA) {
     d = ShapeSampleDirection(S, S.shapes[L.shape], refP, xi);
@@ -475,6 +486,21 @@ RD DirSample SampleLightDirection(const DevScene& S, V3 refP, float xiL, V2 xi, 
     d.Dist = dist;
     li = rad;
   }
+  return d;
+}
+
+
+// scene.cpp:87-96: uniform light pick, then the light's direction sample.
+RD DirSample SampleLightDirection(const DevScene& S, V3 refP, float xiL, V2 xi, V3& li) {
+  int index;
+  float pick;
+  if (!PickLight(S, xiL, index, pick)) {
+    DirSample d{};
+    li = v3s(0.f);
+    d.Pdf = 0.f;
+    return d;
+  }
+  DirSample d = LightSampleDirection(S, S.lights[index], refP, xi, li);
   d.Pdf *= pick;
   return d;
 }
@@ -499,6 +525,105 @@ RD V3 EvalLightAt(const DevScene& S, int light, const SurfInt* si) {
   if (L.kind == LIGHT_AREA) return dot(ToWorld(si->sh, si->Wi), si->N) >= 0.f ? rad : v3s(0.f);
   if (L.kind == LIGHT_SKYBOX) return EnvRadiance(S, L, -si->Wi);
   return v3s(0.f);
+}
+
+// ------------------------------------------------------- light tracing parts
+// Perspective::SampleDirection + Importance (perspective.cpp:101-137): the
+// camera seen from a world point. Returns false (pdf 0) outside the frustum.
+RD bool CameraSampleDirection(const CameraRec& c, V3 ref, V3& camP, V3& dir, float& dist, V2& pixel,
+                              float& importance) {
+  V3 refP = Affine4(c.worldToCam, ref);
+  if (refP.z < c.nearZ || refP.z > c.farZ) return false;
+  V3 ndc = Affine4(c.camToClip, refP);
+  if (ndc.x < 0.f || ndc.x >= 1.f || ndc.y < 0.f || ndc.y >= 1.f) return false;
+  pixel = V2{ndc.x * (float)c.width, ndc.y * (float)c.height};
+  dist = norm(refP);
+  float invDist = Rcp(dist);
+  V3 d = refP * invDist;
+  camP = Affine4(c.camToWorld, v3s(0.f));
+  dir = (camP - ref) * invDist;
+  float imp = 0.f;
+  float cosTheta = d.z;
+  if (cosTheta > 0.f) {
+    float invCosTheta = Rcp(cosTheta);
+    float px = d.x * invCosTheta, py = d.y * invCosTheta;
+    if (c.rect[0] <= px && c.rect[1] <= py && px <= c.rect[2] && py <= c.rect[3])
+      imp = c.normalization * invCosTheta * invCosTheta * invCosTheta;
+  }
+  importance = imp * invDist * invDist;
+  return true;
+}
+
+// Light::SampleRay (area.cpp:120-128, skybox.cpp:135-163, point.cpp:67-71,
+// projection.cpp:93-104): an emitted ray and its weight. `ok` false when the
+// light cannot emit (a map with zero density). The `directional` extension
+// emits parallel rays through a disk covering the world sphere.
+RD bool LightSampleRay(const DevScene& S, const LightRec& L, V2 xi2, V2 xi3, V3& O, V3& D, V3& li) {
+  V3 rad{L.radiance[0], L.radiance[1], L.radiance[2]};
+  if (L.kind == LIGHT_AREA) {
+    V3 P, N;
+    float pdf;
+    ShapeSamplePosition(S, S.shapes[L.shape], xi2, P, N, pdf);
+    Frame fr = FrameFromN(N);
+    V3 local = SquareToCosineHemisphere(xi3);
+    D = ToWorld(fr, local);
+    O = OffsetP(P, N, D);
+    li = rad * kPi / pdf;  // Eval(si) of a point with no incident direction: the radiance
+    return true;
+  }
+  if (L.kind == LIGHT_POINT) {
+    O = V3{L.dir[0], L.dir[1], L.dir[2]};
+    D = SquareToUniformSphere(xi3);
+    li = rad * 4.f * kPi;
+    return true;
+  }
+  if (L.kind == LIGHT_PROJECTION) {
+    V3 nearP = Affine4(L.m2, V3{xi3.x, xi3.y, 0.f});
+    V3 nearDir = normalized(nearP);
+    O = V3{L.dir[0], L.dir[1], L.dir[2]};
+    D = LinearRows(L.m2 + 16, nearDir);
+    li = rad * kPi * L.m2[28];
+    return true;
+  }
+  V3 wc{L.world[0], L.world[1], L.world[2]};
+  float R = L.world[3];
+  V2 off = SquareToUniformDiskConcentric(xi2);
+  if (L.kind == LIGHT_SKYBOX) {
+    float pdfDir;
+    V2 uv;
+    if (!L.distW) {
+      pdfDir = SquareToUniformSpherePdf();
+      uv = xi3;
+    } else {
+      V3 unused;
+      if (!EnvSampleDir(S, L, xi3, unused, pdfDir, uv)) return false;
+    }
+    float theta = uv.y * kPi, phi = uv.x * kPi * 2.f;
+    float sinTheta = sinf(theta), cosTheta = cosf(theta), sinPhi = sinf(phi), cosPhi = cosf(phi);
+    V3 sph{cosPhi * sinTheta, sinPhi * sinTheta, cosTheta};
+    V3 d{sph.y, sph.z, -sph.x};
+    V3 worldD = AffineRows(L.lin, -d);  // ApplyAffineToWorld of a direction, as the reference writes it
+    Frame fr = FrameFromN(d);
+    V3 perp = ToWorld(fr, V3{off.x, off.y, 0.f});
+    O = wc + (perp - worldD) * R;
+    D = worldD;
+    V3 c = rad;
+    if (L.tex) {
+      TexCtx x{S.tex, S.texels, S.texBind, uv, V2{0.f, 0.f}, V2{0.f, 0.f}};
+      TexVal r = TexEval(x, L.tex - 1u, uv);
+      c = V3{r.c[0], r.c[1], r.c[2]};
+    }
+    li = ((c * kPi) * Sqr(R)) / pdfDir;
+    return true;
+  }
+  // directional (extension): parallel rays along the light's direction
+  V3 ld{L.dir[0], L.dir[1], L.dir[2]};
+  Frame fr = FrameFromN(ld);
+  V3 perp = ToWorld(fr, V3{off.x, off.y, 0.f});
+  O = wc + (perp - ld) * R;
+  D = ld;
+  li = rad * kPi * Sqr(R);
+  return true;
 }
 
 // ---------------------------------------------------------------- camera

@@ -868,6 +868,17 @@ CameraRec MakeCamera(const JValue& c) {
   cam.dy[0] = dy.x;
   cam.dy[1] = dy.y;
   cam.dy[2] = dy.z;
+  for (int i = 0; i < 16; i++) {
+    cam.worldToCam[i] = camToWorld.l.m[i / 4][i % 4];
+    cam.camToClip[i] = toClip.w.m[i / 4][i % 4];
+  }
+  F3 pMin = Xf::Aff(toClip.l, F3(0, 0, 0)), pMax = Xf::Aff(toClip.l, F3(1, 1, 0));
+  float ax = pMin.x / pMin.z, ay = pMin.y / pMin.z, bx = pMax.x / pMax.z, by = pMax.y / pMax.z;
+  cam.rect[0] = std::min(ax, bx);
+  cam.rect[1] = std::min(ay, by);
+  cam.rect[2] = std::max(ax, bx);
+  cam.rect[3] = std::max(ay, by);
+  cam.normalization = 1 / ((cam.rect[2] - cam.rect[0]) * (cam.rect[3] - cam.rect[1]));
   return cam;
 }
 
@@ -1285,10 +1296,16 @@ void BuildHostScene(const std::string& json, const std::string& baseDir, HostSce
         translate.m[0][3] = -1;
         translate.m[1][3] = -1 / aspect;
         M4f toClip = scale * translate * persp;
+        Xf clip(toClip);
         for (int i = 0; i < 16; i++) {
           L.m[i] = t.l.m[i / 4][i % 4];
           L.m[16 + i] = toClip.m[i / 4][i % 4];
+          L.m2[i] = clip.l.m[i / 4][i % 4];
         }
+        RowsOf(t.w, L.m2 + 16);
+        F3 pMin = Xf::Aff(clip.l, F3(0, 0, 0)), pMax = Xf::Aff(clip.l, F3(1, 1, 0));
+        float ax = pMin.x / pMin.z, ay = pMin.y / pMin.z, bx = pMax.x / pMax.z, by = pMax.y / pMax.z;
+        L.m2[28] = 1 / ((std::max(ax, bx) - std::min(ax, bx)) * (std::max(ay, by) - std::min(ay, by)));
         L.dir[0] = t.w.m[0][3];  // TranslationToWorld
         L.dir[1] = t.w.m[1][3];
         L.dir[2] = t.w.m[2][3];
@@ -1354,9 +1371,11 @@ void BuildHostScene(const std::string& json, const std::string& baseDir, HostSce
   const JValue* rn = root.get("renderer");
   if (!rn) throw ConfigError("no child: renderer");
   std::string rt = TypeOf(*rn);
-  if (rt != "path" && rt != "vol_path" && rt != "ao") throw FactoryError("cannot find factory: " + rt);
+  if (rt != "path" && rt != "vol_path" && rt != "ao" && rt != "particle_tracer")
+    throw FactoryError("cannot find factory: " + rt);
   hs.isVol = rt == "vol_path";
   hs.isAO = rt == "ao";
+  hs.isParticle = rt == "particle_tracer";  // max_depth -1, rr_depth 3 (particle_tracer.cpp:24-25)
   hs.maxDepth = RI(rn, "max_depth", -1);
   hs.rrDepth = RI(rn, "rr_depth", hs.isVol ? 5 : 3);
   if (const JValue* an = root.get("accel")) {

@@ -33,6 +33,7 @@ struct HostScene {
   uint32_t seed = 0;
   bool isVol = false;
   bool isAO = false;  // renderer "ao"
+  bool isParticle = false;  // renderer "particle_tracer"
   int maxDepth = -1, rrDepth = 3;
   std::vector<MatRec> mats;
   std::vector<ShapeRec> shapes;

@@ -91,6 +91,7 @@ extern "C" RAD_API int rad_render_samples_noalloc(rad_scene* scene, const uint32
                        "rad_render_samples_noalloc: n exceeds the fixed scratch capacity of 16384 samples");
   if (n == 0) return RAD_OK;
   const DevScene& S = *SceneDevice(scene);
+  if (S.isParticle) return ReportError(RAD_ERR_UNSUPPORTED, "particle_tracer has no per-pixel samples");
   int dev = SceneDeviceIndex();
   if (dev < 0 || dev >= kMaxDevices) return ReportError(RAD_ERR_INVALID_ARG, "device index out of range");
   int prevDev = 0;

@@ -101,6 +101,14 @@ cudaError_t LaunchExtend(const DevScene& S, const PathBuffers& B, int depth, int
 // G (optional): guide network; its classes then sample the one-sample MIS mixture.
 cudaError_t LaunchShade(const DevScene& S, const PathBuffers& B, int depth, int grid, cudaStream_t st,
                         const GuideDev* G = nullptr);
+// renderer "particle_tracer": light paths [first, first + count), splatted into `film`
+struct ParticleParams {
+  uint64_t first, count;
+  uint32_t seed;
+  float sampleScale;  // pixels / light paths of the job (particle_tracer.cpp:55)
+};
+cudaError_t LaunchParticle(const DevScene& S, const FilmView& film, const ParticleParams& pp, uint32_t* err, int grid,
+                           cudaStream_t st);
 // renderer "ao": for every path of bounce 0 with a hit, one cosine-sampled visibility ray
 cudaError_t LaunchShadeAO(const DevScene& S, const PathBuffers& B, int grid, cudaStream_t st);
 cudaError_t LaunchShadow(const DevScene& S, const PathBuffers& B, int depth, int grid, cudaStream_t st,

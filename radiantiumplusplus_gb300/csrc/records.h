@@ -121,8 +121,10 @@ struct alignas(16) LightRec {
                        // skybox: world -> light 4x4 (m[0..15])
   uint32_t distW, distH;  // skybox with a bitmap: distribution size (texels); 0: uniform sphere sampling
   uint32_t pad2[2];
+  float m2[32];        // projection: clip -> light 4x4 (m2[0..15]), light -> world linear rows of 4 (m2[16..27]),
+                       // 1 / image-rectangle area (m2[28]; projection.cpp:41-44)
 };
-static_assert(sizeof(LightRec) == 256, "LightRec size");
+static_assert(sizeof(LightRec) == 384, "LightRec size");
 
 // ---------------------------------------------------------------- media
 enum MediumKind : uint32_t { MED_HOMOGENEOUS = 0, MED_HETEROGENEOUS = 1 };
@@ -149,6 +151,11 @@ struct alignas(16) CameraRec {
   float nearZ, farZ;
   int32_t width, height;
   float dx[4], dy[4];      // camera-space offsets of one pixel step (perspective.cpp:56-59)
+  float worldToCam[16];    // cameraToWorld.ToLocal
+  float camToClip[16];     // cameraToClip.ToWorld
+  float rect[4];           // image-plane rectangle at z = 1 (min x, min y, max x, max y), perspective.cpp:61-65
+  float normalization;     // 1 / its area
+  float pad[3];
 };
 
 // ---------------------------------------------------------------- BVH8
@@ -211,6 +218,7 @@ struct DevScene {
   float lightPdf;
   int32_t maxDepth, rrDepth, isVol;
   int32_t isAO;                // renderer "ao" (ao.cpp): one hit, one cosine-sampled visibility ray
+  int32_t isParticle;          // renderer "particle_tracer": light paths splatted into the film
   CameraRec cam;
 };
 

@@ -485,8 +485,32 @@ void RunWaveGraph(rad_job* j) {
   j->launched += npix * spw;
 }
 
+// particle_tracer jobs: the next batch of light paths (ParticleTracer::Render,
+// particle_tracer.cpp:39-83; one "sample" = one light path for the whole film).
+void RunWaveParticle(rad_job* j) {
+  Lib& lib = L();
+  const DevScene& S = j->scene->dev;
+  uint64_t npix = (uint64_t)S.cam.width * S.cam.height;
+  const uint32_t k = std::min<uint32_t>(lib.maxPaths, j->spp - j->nextSample);
+  ParticleParams pp{(uint64_t)j->first + j->nextSample, k, j->seed, (float)npix / (float)j->spp};
+  FilmView film{j->accum, S.cam.width, S.cam.height, j->dStats};
+  ProfSink ps{j};
+  cudaEvent_t a = nullptr;
+  ps.Begin(5, a);
+  int grid = std::max(1, std::min(lib.sms * 8, (int)((k + 127) / 128)));
+  Check(LaunchParticle(S, film, pp, lib.paths.counters + kMiscBase + 1, grid, lib.stream), "particle_tracer");
+  ps.End(5, a);
+  j->stats.kernel_launches += 1;
+  j->nextSample += k;
+  j->launched += k;
+}
+
 // Runs wave(s) for the job's next sample index over all its pixels.
 void RunWave(rad_job* j) {
+  if (j->scene->dev.isParticle) {
+    RunWaveParticle(j);
+    return;
+  }
   const uint32_t spw = WaveSamples(j);
   if (GraphEligible(j) && j->spp - j->nextSample >= spw) {
     RunWaveGraph(j);
@@ -831,6 +855,7 @@ uint64_t SceneUpload(const HostScene& hs, rad_scene* sc) {
   D.rrDepth = hs.rrDepth;
   D.isVol = hs.isVol ? 1 : 0;
   D.isAO = hs.isAO ? 1 : 0;
+  D.isParticle = hs.isParticle ? 1 : 0;
   D.cam = hs.cam;
   return b;
 }
@@ -1024,7 +1049,7 @@ int rad_job_submit(rad_scene* scene, const rad_job_desc* desc, rad_job** out) {
     if (j->flags & RAD_JOB_GUIDE)
       j->trainSamples = (uint32_t)std::ceil((double)scene->guideCfg.trainFraction * (double)j->spp);
     uint64_t npix = (uint64_t)scene->info.width * scene->info.height;
-    j->total = npix * j->spp;
+    j->total = scene->dev.isParticle ? j->spp : npix * j->spp;  // particle_tracer: spp = light paths
     j->filmBytes = npix * sizeof(float4) + 64;
     j->tSubmit = NowMs();
     scene->jobs++;
@@ -1105,7 +1130,8 @@ int rad_job_film(rad_job* job, float* rgb, int32_t width, int32_t height) {
     std::lock_guard<std::mutex> g(lib.gpuMu);
     size_t n = (size_t)width * height * 3;
     if (!job->resolve) Check(cudaMalloc(&job->resolve, n * sizeof(float)), "cudaMalloc");
-    float scale = 1.0f / (float)job->spp;  // sample_renderer.cpp:109-114
+    // sample_renderer.cpp:109-114; a particle film already carries pixels / light paths
+    float scale = S.isParticle ? 1.0f : 1.0f / (float)job->spp;
     Check(LaunchResolveFilm(FilmView{job->accum, width, height, nullptr}, scale, job->resolve, lib.stream), "resolve");
     Check(cudaMemcpyAsync(rgb, job->resolve, n * sizeof(float), cudaMemcpyDeviceToHost, lib.stream), "film copy");
     Check(cudaStreamSynchronize(lib.stream), "sync");
@@ -1258,6 +1284,8 @@ int rad_scene_texture_eval(rad_scene* scene, uint32_t texture, const float* uv, 
 int rad_render_samples(rad_scene* scene, const uint32_t* pixels, const uint32_t* samples, int64_t n, uint32_t seed,
                        float* radiance) {
   if (!scene || n < 0 || (n > 0 && (!pixels || !samples || !radiance))) return Fail(RAD_ERR_INVALID_ARG, "bad argument");
+  if (scene->dev.isParticle)
+    return Fail(RAD_ERR_UNSUPPORTED, "particle_tracer splats light paths: it has no per-pixel samples");
   if (n == 0) return RAD_OK;
   uint64_t npix = (uint64_t)scene->info.width * scene->info.height;
   for (int64_t i = 0; i < n; i++)
@@ -1464,7 +1492,8 @@ int rad_guide_info(rad_scene* scene, rad_guide_info_t* info) {
 // configuration and keeps the fastest in the scene.
 int rad_autotune(rad_scene* scene, const char* config_json, rad_tune_result* out) {
   if (!scene) return Fail(RAD_ERR_INVALID_ARG, "null scene");
-  if (scene->dev.isVol) return Fail(RAD_ERR_UNSUPPORTED, "the autotuner covers the `path` traversal kernels");
+  if (scene->dev.isVol || scene->dev.isParticle)
+    return Fail(RAD_ERR_UNSUPPORTED, "the autotuner covers the `path` traversal kernels");
   return Guard([&] {
     EnsureInit();
     int reps = 2;

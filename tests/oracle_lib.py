@@ -38,6 +38,7 @@ def lib():
         L.orc_render_samples.argtypes = [P, P, P, ctypes.c_int64, ctypes.c_uint32, P]
         L.orc_bsdf_eval.argtypes = [ctypes.c_char_p, P, P, ctypes.c_int64, P, P]
         L.orc_texture_eval.argtypes = [P, ctypes.c_uint32, P, P, ctypes.c_int64, P]
+        L.orc_render_particle.argtypes = [P, ctypes.c_uint64, ctypes.c_uint64, ctypes.c_uint64, ctypes.c_uint32, P]
         L.orc_texture_count.argtypes = [P]
         L.orc_image_load.argtypes = [ctypes.c_char_p, ctypes.c_char_p, P, P, ctypes.c_int64]
         L.orc_bsdf_sample.argtypes = [ctypes.c_char_p, P, P, ctypes.c_int64, P, P, P, P, P]
@@ -116,6 +117,15 @@ class OracleScene:
         if rc != 0:
             raise RuntimeError(lib().orc_last_error().decode())
         return film, stats
+
+    def render_particle(self, spp=None, first=0, count=None, seed=None):
+        """particle_tracer film: light paths [first, first + count) of a job of `spp` light paths."""
+        spp = self.spp if spp is None else spp
+        count = spp - first if count is None else count
+        film = np.zeros((self.height, self.width, 3), np.float32)
+        if lib().orc_render_particle(self.h, first, count, spp, self.seed if seed is None else seed, _p(film)) != 0:
+            raise RuntimeError(lib().orc_last_error().decode())
+        return film
 
     def texture_count(self):
         return lib().orc_texture_count(self.h)

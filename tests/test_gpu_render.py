@@ -75,6 +75,33 @@ def test_ao_samples(rad, oracle, scene_dir):
     g.close()
 
 
+@pytest.mark.parametrize("light", ["area", "sky", "point"])
+def test_particle_tracer_film(rad, oracle, scene_dir, light):
+    """Renderer `particle_tracer`: the job's film (light paths splatted with atomics)
+    against the oracle's film of the same light paths. Splat order differs, and a
+    path can take the other branch on a 1-ulp transcendental difference, so the
+    check is per pixel within 2% for >= 90% of lit pixels and the film mean
+    within 1%."""
+    sc = scenes.materials_room(24, 24, 1)
+    if light == "sky":
+        sc["scene"].append({"light": {"type": "skybox", "radiance": [0.4, 0.5, 0.6]}})
+    elif light == "point":
+        sc["scene"].append({"light": {"type": "point", "position": [0.2, 1.5, 0.3], "intensity": [2, 2, 2]}})
+    sc["renderer"] = {"type": "particle_tracer", "max_depth": 6}
+    sc["sampler"]["sample_count"] = 60000
+    path, text, d = write(scene_dir, "particle_" + light, sc)
+    g, o = rad.Scene.from_file(path), oracle.OracleScene(text, d)
+    film = g.render()
+    ref = o.render_particle()
+    lit = ref.sum(axis=2) > 1e-3
+    close = (np.abs(film - ref) <= 0.02 * np.abs(ref) + 1e-6).all(axis=2)
+    assert close[lit].mean() >= 0.9, close[lit].mean()
+    assert abs(film.mean() - ref.mean()) < 0.01 * ref.mean()
+    with pytest.raises(rad.RadError):
+        g.render_samples(np.zeros(1, np.uint32), np.zeros(1, np.uint32))
+    g.close()
+
+
 def test_path_samples_lights(rad, oracle, scene_dir):
     """Point and projection lights (delta lights: no MIS weight on their samples) beside
     an area emitter."""

@@ -311,3 +311,23 @@ def test_ao_closed_forms(oracle, scene_dir):
     v = o.render_samples(pix, smp)[:, 0]
     assert abs(v.mean() - 0.5) < 0.01, v.mean()
     o.close()
+
+
+def test_particle_tracer_agrees_with_path_tracer(oracle, scene_dir):
+    """particle_tracer (particle_tracer.cpp) and path estimate the same image: on the
+    Lambertian box room their film means agree to within the light tracer's noise."""
+    from helpers import write
+    from radiantiumplusplus_gb300 import scenes
+    sc = scenes.box_room(16, 16, 256, max_depth=8)
+    _, text, d = write(scene_dir, "pt_path", sc)
+    o = oracle.OracleScene(text, d)
+    ref, _ = o.render()
+    o.close()
+    sc["renderer"] = {"type": "particle_tracer", "max_depth": 8}
+    sc["sampler"]["sample_count"] = 200000
+    _, text, d = write(scene_dir, "pt_particle", sc)
+    o = oracle.OracleScene(text, d)
+    film = o.render_particle()
+    o.close()
+    m, r = film.reshape(-1, 3).mean(0), ref.reshape(-1, 3).mean(0)
+    assert np.all(np.abs(m - r) < 0.04 * r), (m, r)
