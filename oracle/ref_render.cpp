@@ -500,6 +500,10 @@ static void ParticleSample(const Scene& S, uint64_t id, uint32_t seed, Float sam
     Float bl = rng.Next1D();
     V2 bd = rng.Next2D();
     auto bs = bsdf.Sample(si.Wi, bl, bd, &ts);
+    // Decision kept with the GPU path: a failed sample (pdf 0) ends the light path,
+    // where the reference divides by the zero pdf (particle_tracer.cpp:206) and
+    // writes NaN into the film.
+    if (!(bs.first.Pdf > 0)) break;
     V3 woW = si.ToWorld(bs.first.Wo);
     Float idn = dot(si.N, -ray.D), odn = dot(si.N, woW);
     if (idn * si.Wi.z <= 0 || odn * bs.first.Wo.z <= 0) break;

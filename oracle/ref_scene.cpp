@@ -1048,7 +1048,7 @@ std::unique_ptr<Scene> Scene::FromJson(const std::string& text, const std::strin
   if (S.renderer != "path" && S.renderer != "vol_path" && S.renderer != "ao" && S.renderer != "particle_tracer")
     throw std::runtime_error("cannot find factory: " + S.renderer);
   S.maxDepth = ReadI(rn, "max_depth", -1);
-  S.rrDepth = ReadI(rn, "rr_depth", S.renderer == "path" ? 3 : 5);
+  S.rrDepth = ReadI(rn, "rr_depth", S.renderer == "vol_path" ? 5 : 3);  // path.cpp, particle_tracer.cpp: 3; vol_path.cpp: 5
   if (const Json* an = root.find("accel")) {
     std::string at = ReadS(an, "type", "");
     if (at != "embree" && at != "gpu_bvh8") throw std::runtime_error("cannot find factory: " + at);

@@ -23,6 +23,7 @@ inline int __ffs(uint32_t x) { return __builtin_ffs((int)x); }
 inline int __popc(uint32_t x) { return __builtin_popcount(x); }
 template <typename T> inline T __ldg(const T* p) { return *p; }
 inline uint32_t atomicOr(uint32_t* p, uint32_t v) { uint32_t o = *p; *p |= v; return o; }
+inline float atomicAdd(float* p, float v) { float o = *p; *p += v; return o; }
 inline uint2 make_uint2(uint32_t a, uint32_t b) { uint2 r; r.x = a; r.y = b; return r; }
 using std::isfinite;
 using std::isnan;
