@@ -64,7 +64,9 @@ typedef struct rad_scene_info {
 
 /* One render request. spp = 0 takes the scene's sample_count; seed = UINT32_MAX
  * takes the scene's sampler seed. first_sample lets a job continue an earlier
- * one with disjoint sample indices (resumable accumulation). */
+ * one with disjoint sample indices (resumable accumulation). For the
+ * particle_tracer renderer a sample is one light path over the whole film
+ * (particle_tracer.cpp:52-83), so spp counts light paths. */
 typedef struct rad_job_desc {
   uint32_t spp;
   uint32_t seed;
