@@ -4,7 +4,8 @@
  * Drop-in replacement for the RadiantiumPlusPlus offline hot path: the
  * `path` and `vol_path` renderers (module/rad.offline/src/renderer/path.cpp,
  * vol_path.cpp), their sample-renderer driver (sample_renderer.cpp) and the
- * Embree accelerator (src/accel/embree.cpp). Scenes are the reference's JSON
+ * Embree accelerator (src/accel/embree.cpp); also the `ao`, `particle_tracer`
+ * and `bdpt` renderers (ao.cpp, particle_tracer.cpp, bdpt.cpp). Scenes are the reference's JSON
  * format with the same factory names. Plain pointers and sizes only: no C++
  * or torch types cross this boundary, and no exception escapes it.
  *
@@ -66,7 +67,8 @@ typedef struct rad_scene_info {
  * takes the scene's sampler seed. first_sample lets a job continue an earlier
  * one with disjoint sample indices (resumable accumulation). For the
  * particle_tracer renderer a sample is one light path over the whole film
- * (particle_tracer.cpp:52-83), so spp counts light paths. */
+ * (particle_tracer.cpp:52-83), so spp counts light paths. A bdpt sample is one
+ * camera subpath and one light subpath (bdpt.cpp:261-305). */
 typedef struct rad_job_desc {
   uint32_t spp;
   uint32_t seed;
@@ -172,7 +174,9 @@ RAD_API int rad_camera_rays(rad_scene* scene, const uint32_t* pixels, int64_t n,
 RAD_API int rad_scene_texture_eval(rad_scene* scene, uint32_t texture, const float* uv, const float* duv, int64_t n,
                                    float* out);
 /* Radiance of individual pixel samples (Li), n x 3, through the same kernels
- * as a job. */
+ * as a job. For bdpt: the camera-side sum (connections with t >= 2 camera
+ * vertices); its t = 1 connections land on other pixels and are left out.
+ * RAD_ERR_UNSUPPORTED for particle_tracer. */
 RAD_API int rad_render_samples(rad_scene* scene, const uint32_t* pixels, const uint32_t* samples, int64_t n,
                                uint32_t seed, float* radiance);
 
@@ -252,7 +256,7 @@ RAD_API int rad_guide_grad(rad_scene* scene, const float* records, int64_t n, fl
  * depend on it. config_json may be NULL; keys: leaf_frac8 (list, default
  * [2,3,4,5,6]), refill_busy (list, default [16,20,24,28,32]), blocks_per_sm
  * (list, default [4,6,8]), reps (timed waves per candidate, 2).
- * RAD_ERR_UNSUPPORTED for `vol_path` and `particle_tracer` scenes. */
+ * RAD_ERR_UNSUPPORTED for `vol_path`, `particle_tracer` and `bdpt` scenes. */
 typedef struct rad_tune_result {
   int32_t refill_busy, blocks_per_sm; /* chosen */
   int32_t candidates;                 /* configurations timed */

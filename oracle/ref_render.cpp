@@ -524,9 +524,12 @@ static void ParticleSample(const Scene& S, uint64_t id, uint32_t seed, Float sam
   }
 }
 
+Spectrum BdptSample(const Scene& S, uint32_t x, uint32_t y, uint32_t s, uint32_t seed, std::vector<Spectrum>* film);
+
 // sample_renderer.cpp:93-106: one pixel sample. The jitter takes the first two
 // draws of the sample's stream (the reference uses a separate per-tile mt19937).
 static Spectrum RenderSample(const Scene& S, uint32_t x, uint32_t y, uint32_t s, uint32_t seed) {
+  if (S.renderer == "bdpt") return BdptSample(S, x, y, s, seed, nullptr);  // camera side only
   Pcg32 rng = Pcg32::ForSample(x + y * (uint32_t)S.camera.width, s, seed);
   Float jx = rng.Next1D();
   Float jy = rng.Next1D();
@@ -708,6 +711,57 @@ int orc_render_particle(void* sp, uint64_t first, uint64_t count, uint64_t spp, 
   } catch (const std::exception& e) {
     g_err = e.what();
     return -1;
+  }
+  return 0;
+}
+
+// bdpt: samples [s0, s1) of every pixel; film (W x H x 3) receives, per pixel,
+// (sum of valid camera-side samples + the t = 1 splats landing there) / spp
+// (bdpt.cpp:261-305).
+int orc_render_bdpt(void* sp, int s0, int s1, uint32_t seed, int threads, float* film) {
+  Scene& S = *(Scene*)sp;
+  if (S.renderer != "bdpt") {
+    g_err = "orc_render_bdpt: the scene's renderer is not bdpt";
+    return -1;
+  }
+  const int W = S.camera.width, H = S.camera.height;
+  const size_t npix = (size_t)W * H;
+  int nt = threads > 0 ? threads : (int)std::thread::hardware_concurrency();
+  std::vector<std::vector<Spectrum>> images(nt, std::vector<Spectrum>(npix, Spectrum(0)));
+  std::atomic<int> next{0};
+  std::atomic<bool> failed{false};
+  auto worker = [&](int w) {
+    try {
+      std::vector<Spectrum>& img = images[w];
+      for (;;) {
+        int y = next.fetch_add(1);
+        if (y >= H) break;
+        for (int x = 0; x < W; x++) {
+          Spectrum acc(0);
+          for (int s = s0; s < s1; s++) {
+            Spectrum li = BdptSample(S, (uint32_t)x, (uint32_t)y, (uint32_t)s, seed, &img);
+            if (!InvalidSample(li)) acc = acc + li;
+          }
+          img[(size_t)y * W + x] = img[(size_t)y * W + x] + acc;
+        }
+      }
+    } catch (const std::exception& e) {
+      g_err = e.what();
+      failed = true;
+    }
+  };
+  std::vector<std::thread> ts;
+  for (int i = 1; i < nt; i++) ts.emplace_back(worker, i);
+  worker(0);
+  for (auto& t : ts) t.join();
+  if (failed) return -1;
+  Float coeff = Float(1) / (Float)S.spp;
+  for (size_t p = 0; p < npix; p++) {
+    Spectrum sum(0);
+    for (int i = 0; i < nt; i++) sum = sum + images[i][p];
+    film[3 * p] = sum.x * coeff;
+    film[3 * p + 1] = sum.y * coeff;
+    film[3 * p + 2] = sum.z * coeff;
   }
   return 0;
 }

@@ -467,17 +467,19 @@ Float Camera::SampleDirection(const V3& ref, DirectionSample& dsr) const {
   dsr.Dist = dist;
   dsr.N = cameraToWorld.ApplyLinearToWorld(V3(0, 0, 1));
   dsr.Pdf = 1;
-  // Importance (perspective.cpp:124-135)
-  Float importance = 0;
-  Float cosTheta = dir.z;
-  if (cosTheta > 0) {
-    Float invCosTheta = Rcp(cosTheta);
-    V2 p(dir.x * invCosTheta, dir.y * invCosTheta);
-    if (rectMin.x <= p.x && rectMin.y <= p.y && p.x <= rectMax.x && p.y <= rectMax.y)
-      importance = normalization * invCosTheta * invCosTheta * invCosTheta;
-  }
-  return importance * invDist * invDist;
+  return Importance(dir) * invDist * invDist;
 }
+
+Float Camera::Importance(const V3& d) const {
+  Float cosTheta = d.z;
+  if (cosTheta <= 0) return 0;
+  Float invCosTheta = Rcp(cosTheta);
+  V2 p(d.x * invCosTheta, d.y * invCosTheta);
+  if (!(rectMin.x <= p.x && rectMin.y <= p.y && p.x <= rectMax.x && p.y <= rectMax.y)) return 0;
+  return normalization * invCosTheta * invCosTheta * invCosTheta;
+}
+
+Float Camera::PdfWe(const V3& worldDir) const { return Importance(cameraToWorld.ApplyLinearToLocal(worldDir)); }
 
 void SurfaceInteraction::ComputeDifferentials(const RayDiff& ray) {
   if (!(ray.has && dUVdX.x == 0 && dUVdX.y == 0 && dUVdY.x == 0 && dUVdY.y == 0)) return;
@@ -1045,10 +1047,17 @@ std::unique_ptr<Scene> Scene::FromJson(const std::string& text, const std::strin
   const Json* rn = root.find("renderer");
   if (!rn) throw std::runtime_error("no child: renderer");
   S.renderer = ReadS(rn, "type", "");
-  if (S.renderer != "path" && S.renderer != "vol_path" && S.renderer != "ao" && S.renderer != "particle_tracer")
+  if (S.renderer != "path" && S.renderer != "vol_path" && S.renderer != "ao" && S.renderer != "particle_tracer" &&
+      S.renderer != "bdpt")
     throw std::runtime_error("cannot find factory: " + S.renderer);
   S.maxDepth = ReadI(rn, "max_depth", -1);
-  S.rrDepth = ReadI(rn, "rr_depth", S.renderer == "vol_path" ? 5 : 3);  // path.cpp, particle_tracer.cpp: 3; vol_path.cpp: 5
+  // path.cpp, particle_tracer.cpp: 3; vol_path.cpp, bdpt.cpp: 5
+  S.rrDepth = ReadI(rn, "rr_depth", S.renderer == "vol_path" || S.renderer == "bdpt" ? 5 : 3);
+  if (S.renderer == "bdpt") {
+    if (const Json* um = rn->find("use_mis")) S.useMis = um->b;
+    for (const Light& L : S.lights)
+      if (L.kind == Light::Directional) throw std::runtime_error("bdpt: the directional light is not supported");
+  }
   if (const Json* an = root.find("accel")) {
     std::string at = ReadS(an, "type", "");
     if (at != "embree" && at != "gpu_bvh8") throw std::runtime_error("cannot find factory: " + at);
@@ -1671,6 +1680,20 @@ std::pair<DirectionSample, Spectrum> Scene::SampleOneLightDirection(int index, c
   return {dsr, li};
 }
 
+// Skybox::PdfDirection (skybox.cpp:108-127)
+static Float SkyPdfDirection(const Light& L, const V3& dir) {
+  if (L.uniformMap) return SquareToUniformSpherePdf();
+  V3 v = L.toWorld.ApplyAffineToLocal(dir);
+  Float theta = std::acos(std::clamp(v.y, Float(-1), Float(1)));
+  Float sinTheta = std::sin(theta);
+  if (sinTheta == 0) return 0;
+  Float phi = std::atan2(v.x, -v.z);
+  phi = (phi < 0) ? (phi + 2 * PI) : phi;
+  V2 uv(phi / (2 * PI), theta / PI);
+  Float pdf = L.dist.Pdf(uv);
+  return pdf / (2 * PI * PI * sinTheta);
+}
+
 // scene.cpp:98-103 with area.cpp:77-91, skybox.cpp:88-106
 Float Scene::PdfLightDirection(int l, const V3& refP, const DirectionSample& dsr) const {
   const Light& L = lights[l];
@@ -1678,22 +1701,7 @@ Float Scene::PdfLightDirection(int l, const V3& refP, const DirectionSample& dsr
   if (L.kind == Light::Area) {
     p = dot(-dsr.Dir, dsr.N) >= 0 ? shapes[L.shape].PdfDirection(refP, dsr) : 0;
   } else if (L.kind == Light::Skybox) {
-    if (L.uniformMap) {
-      p = SquareToUniformSpherePdf();
-    } else {  // skybox.cpp:108-127
-      V3 v = L.toWorld.ApplyAffineToLocal(dsr.Dir);
-      Float theta = std::acos(std::clamp(v.y, Float(-1), Float(1)));
-      Float sinTheta = std::sin(theta);
-      if (sinTheta == 0) {
-        p = 0;
-      } else {
-        Float phi = std::atan2(v.x, -v.z);
-        phi = (phi < 0) ? (phi + 2 * PI) : phi;
-        V2 uv(phi / (2 * PI), theta / PI);
-        Float pdf = L.dist.Pdf(uv);
-        p = pdf / (2 * PI * PI * sinTheta);
-      }
-    }
+    p = SkyPdfDirection(L, dsr.Dir);
   }
   return p * lightPdf;
 }
@@ -1701,6 +1709,17 @@ Float Scene::PdfLightDirection(int l, const V3& refP, const DirectionSample& dsr
 }  // namespace orc
 
 namespace orc {
+
+// SquareToUniformDiskConcentric (warp.cpp:80-95)
+static V2 SquareToUniformDiskConcentric(const V2& xi2) {
+  Float x = Fmadd(2, xi2.x, -1), y = Fmadd(2, xi2.y, -1);
+  bool quadrant = std::abs(x) < std::abs(y);
+  Float r = quadrant ? y : x, rp = quadrant ? x : y;
+  Float phi0 = Float(0.25) * PI * rp / r;
+  if (quadrant) phi0 = Float(0.5) * PI - phi0;
+  if (x == 0 && y == 0) phi0 = 0;
+  return V2(r * std::cos(phi0), r * std::sin(phi0));
+}
 
 // Light::SampleRay
 bool Scene::LightSampleRay(int l, const V2& xi2, const V2& xi3, Ray& ray, Spectrum& li) const {
@@ -1731,18 +1750,11 @@ bool Scene::LightSampleRay(int l, const V2& xi2, const V2& xi3, Ray& ray, Spectr
     V3 nearDir = normalized(nearP);
     ray.O = V3(L.toWorld.ToWorld.m[0][3], L.toWorld.ToWorld.m[1][3], L.toWorld.ToWorld.m[2][3]);
     ray.D = L.toWorld.ApplyLinearToWorld(nearDir);
-    li = cmul(L.radiance, L.scale) * PI * L.cameraArea;
+    li = L.radiance * PI * L.cameraArea;  // SampleRay leaves out the light's scale
     return true;
   }
   Float R = L.worldRadius;
-  // SquareToUniformDiskConcentric (warp.cpp:80-95)
-  Float x = Fmadd(2, xi2.x, -1), y = Fmadd(2, xi2.y, -1);
-  bool quadrant = std::abs(x) < std::abs(y);
-  Float r = quadrant ? y : x, rp = quadrant ? x : y;
-  Float phi0 = Float(0.25) * PI * rp / r;
-  if (quadrant) phi0 = Float(0.5) * PI - phi0;
-  if (x == 0 && y == 0) phi0 = 0;
-  V2 offset(r * std::cos(phi0), r * std::sin(phi0));
+  V2 offset = SquareToUniformDiskConcentric(xi2);
   if (L.kind == Light::Skybox) {  // skybox.cpp:135-163
     Float pdfDir;
     V2 uv;
@@ -1777,6 +1789,111 @@ bool Scene::LightSampleRay(int l, const V2& xi2, const V2& xi3, Ray& ray, Spectr
   ray.D = L.direction;
   li = L.radiance * PI * Sqr(R);
   return true;
+}
+
+// SampleLe of each light. The directional extension has none: scenes pairing it
+// with bdpt are rejected when loaded.
+Scene::LeSample Scene::LightSampleLe(int l, const V2& xi2, const V2& xi3) const {
+  const Light& L = lights[l];
+  LeSample r;
+  r.ray.MinT = 0;
+  r.ray.MaxT = std::numeric_limits<Float>::max();
+  if (L.kind == Light::Area) {  // area.cpp:130-140 (constant radiance)
+    r.psr = shapes[L.shape].SamplePosition(xi2);
+    r.pdfPos = r.psr.Pdf > 0 ? r.psr.Pdf : 0;
+    V3 local = SquareToCosineHemisphere(xi3);
+    r.pdfDir = SquareToCosineHemispherePdf(local);
+    Frame fr(r.psr.N);  // SurfaceInteraction(psr)
+    r.ray = SpawnRay(r.psr.P, r.psr.N, fr.ToWorld(local));
+    r.le = L.radiance;  // Eval(si) with no incident direction: dot(0, N) >= 0
+  } else if (L.kind == Light::Point) {  // point.cpp:75-85
+    r.psr.P = L.worldPos;
+    r.psr.N = V3(0);
+    r.psr.UV = V2(0, 0);
+    r.psr.Pdf = 1;
+    r.psr.IsDelta = true;
+    r.pdfPos = 1;
+    V3 local = SquareToUniformSphere(xi3);
+    r.pdfDir = SquareToUniformSpherePdf();
+    Frame fr(r.psr.N);
+    r.ray = SpawnRay(r.psr.P, r.psr.N, fr.ToWorld(local));
+    r.le = L.radiance;
+  } else if (L.kind == Light::Projection) {  // projection.cpp:107-120
+    r.psr.P = V3(L.toWorld.ToWorld.m[0][3], L.toWorld.ToWorld.m[1][3], L.toWorld.ToWorld.m[2][3]);
+    r.psr.N = normalized(L.toWorld.ApplyLinearToWorld(V3(0, 0, 1)));
+    r.psr.UV = V2(Float(0.5), Float(0.5));
+    r.psr.Pdf = 1;
+    r.psr.IsDelta = true;
+    r.pdfPos = 1;
+    V3 nearP = L.toClip.ApplyAffineToLocal(V3(xi3.x, xi3.y, 0));
+    V3 nearDir = normalized(nearP);
+    r.ray.O = r.psr.P;
+    r.ray.D = L.toWorld.ApplyLinearToWorld(nearDir);
+    r.le = L.radiance;  // the irradiance without the light's scale
+    r.pdfDir = 1 / (L.cameraArea * PI);
+  } else if (L.kind == Light::Skybox) {  // skybox.cpp:170-204
+    Float R = L.worldRadius;
+    V2 offset = SquareToUniformDiskConcentric(xi2);
+    Float pdfDir;
+    V2 uv;
+    if (L.uniformMap) {
+      pdfDir = SquareToUniformSpherePdf();
+      uv = xi3;
+    } else {
+      auto [iu, iv, pdf0] = L.dist.Sample(xi3);
+      pdfDir = pdf0;
+      if (pdf0 <= 0) return LeSample();
+      Float vy = iv / (Float)L.map->height, vx = iu / (Float)L.map->width;
+      uv = V2(vx, vy);
+      Float sinTheta = std::sin(vy * PI);
+      if (sinTheta == 0) return LeSample();
+      pdfDir /= (2 * PI * PI * sinTheta);
+    }
+    if (pdfDir <= 0) return LeSample();
+    Float theta = uv.y * PI, phi = uv.x * PI * 2;
+    V3 sph(std::cos(phi) * std::sin(theta), std::sin(phi) * std::sin(theta), std::cos(theta));
+    V3 d(sph.y, sph.z, -sph.x);
+    V3 worldD = L.toWorld.ApplyAffineToWorld(-d);
+    V3 perp = Frame(d).ToWorld(V3(offset.x, offset.y, 0));
+    r.ray.O = L.worldCenter + (perp - worldD) * R;
+    r.ray.D = worldD;
+    r.le = L.map ? L.map->Eval(TexSi{uv, V2(), V2()}) : L.radiance;
+    r.pdfPos = 1 / (PI * Sqr(R));
+    r.pdfDir = pdfDir;
+    r.psr.P = r.ray.O;
+    r.psr.N = r.ray.D;
+    r.psr.UV = uv;
+    r.psr.Pdf = r.pdfPos;
+    r.psr.IsDelta = false;
+  } else {
+    throw std::runtime_error("bdpt: the directional light is not supported");
+  }
+  return r;
+}
+
+std::pair<Float, Float> Scene::LightPdfLe(int l, const PositionSample& psr, const V3& dir) const {
+  const Light& L = lights[l];
+  if (L.kind == Light::Area) {  // area.cpp:142-147
+    Frame fr(psr.N);
+    Float pdfPos = shapes[L.shape].PdfPosition();
+    Float pdfDir = SquareToCosineHemispherePdf(fr.ToLocal(dir));
+    return {pdfPos, std::abs(pdfDir)};
+  }
+  if (L.kind == Light::Point) return {Float(0), std::abs(SquareToUniformSpherePdf())};  // point.cpp:87-91
+  if (L.kind == Light::Projection) {  // projection.cpp:122-133
+    V3 refP = L.toWorld.ApplyAffineToLocal(psr.P);
+    V3 ndcPos = L.toClip.ApplyAffineToWorld(refP);
+    Float pdfDir;
+    if (ndcPos.x < 0 || ndcPos.x >= 1 || ndcPos.y < 0 || ndcPos.y >= 1 || ndcPos.z <= 0)
+      pdfDir = 0;
+    else
+      pdfDir = 1 / (L.cameraArea * PI);
+    return {Float(0), std::abs(pdfDir)};
+  }
+  if (L.kind == Light::Skybox) {  // skybox.cpp:206-212
+    return {1 / (PI * Sqr(L.worldRadius)), SkyPdfDirection(L, dir)};
+  }
+  throw std::runtime_error("bdpt: the directional light is not supported");
 }
 
 }  // namespace orc

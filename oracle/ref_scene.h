@@ -197,6 +197,8 @@ struct Camera {  // perspective.cpp:15-70
   // dsr.Pdf 0 outside the frustum; returns the importance
   Float SampleDirection(const V3& ref, DirectionSample& dsr) const;
   Ray SampleRayDifferential(const V2& screen, RayDiff& diff) const;  // perspective.cpp:84-97
+  Float Importance(const V3& d) const;      // perspective.cpp:124-139, d in camera space
+  Float PdfWe(const V3& worldDir) const;    // perspective.cpp:141-146: the direction density
 };
 
 struct BvhNode {
@@ -221,6 +223,7 @@ struct Scene {
   Camera camera;
   std::string renderer = "path";
   int maxDepth = -1, rrDepth = 3;
+  bool useMis = true;  // bdpt.cpp:226 (use_mis)
   int spp = 16;
   uint32_t seed = 0;
   std::vector<PrimRef> prims;
@@ -246,6 +249,18 @@ struct Scene {
   // false when the light emits nothing for this sample
   bool LightSampleRay(int light, const V2& xi2, const V2& xi3, Ray& ray, Spectrum& li) const;
   Float PdfLightDirection(int light, const V3& refP, const DirectionSample& dsr) const;
+  // Light::SampleLe (area.cpp:130-140, point.cpp:75-85, projection.cpp:107-120, skybox.cpp:170-204): an
+  // emitted ray, its radiance, the emitting position and the position / direction densities (0 when the
+  // light cannot emit this sample)
+  struct LeSample {
+    Ray ray;
+    Spectrum le = Spectrum(0);
+    PositionSample psr;
+    Float pdfPos = 0, pdfDir = 0;
+  };
+  LeSample LightSampleLe(int light, const V2& xi2, const V2& xi3) const;
+  // Light::PdfLe (area.cpp:142-147, point.cpp:87-91, projection.cpp:122-133, skybox.cpp:206-212)
+  std::pair<Float, Float> LightPdfLe(int light, const PositionSample& psr, const V3& dir) const;
   Spectrum EvalLight(int light, const SurfaceInteraction& si) const;
   uint64_t PrimCount() const { return prims.size(); }
 };

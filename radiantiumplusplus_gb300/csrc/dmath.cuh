@@ -13,6 +13,7 @@
 #include <cmath>
 #include <cstring>
 #define RD inline
+#define RDN inline
 #undef __global__
 #define __global__
 #undef __launch_bounds__
@@ -31,6 +32,8 @@ using std::isinf;
 #else
 #include <cuda_runtime.h>
 #define RD __device__ __forceinline__
+// large device functions called from several places: one copy in the code
+#define RDN __device__ __noinline__
 #endif
 
 #include "records.h"

@@ -528,6 +528,16 @@ RD V3 EvalLightAt(const DevScene& S, int light, const SurfInt* si) {
 }
 
 // ------------------------------------------------------- light tracing parts
+// Perspective::Importance (perspective.cpp:124-139) of camera-space direction d.
+RD float CameraImportance(const CameraRec& c, V3 d) {
+  float cosTheta = d.z;
+  if (cosTheta <= 0.f) return 0.f;
+  float invCosTheta = Rcp(cosTheta);
+  float px = d.x * invCosTheta, py = d.y * invCosTheta;
+  if (!(c.rect[0] <= px && c.rect[1] <= py && px <= c.rect[2] && py <= c.rect[3])) return 0.f;
+  return c.normalization * invCosTheta * invCosTheta * invCosTheta;
+}
+
 // Perspective::SampleDirection + Importance (perspective.cpp:101-137): the
 // camera seen from a world point. Returns false (pdf 0) outside the frustum.
 RD bool CameraSampleDirection(const CameraRec& c, V3 ref, V3& camP, V3& dir, float& dist, V2& pixel,
@@ -542,15 +552,7 @@ RD bool CameraSampleDirection(const CameraRec& c, V3 ref, V3& camP, V3& dir, flo
   V3 d = refP * invDist;
   camP = Affine4(c.camToWorld, v3s(0.f));
   dir = (camP - ref) * invDist;
-  float imp = 0.f;
-  float cosTheta = d.z;
-  if (cosTheta > 0.f) {
-    float invCosTheta = Rcp(cosTheta);
-    float px = d.x * invCosTheta, py = d.y * invCosTheta;
-    if (c.rect[0] <= px && c.rect[1] <= py && px <= c.rect[2] && py <= c.rect[3])
-      imp = c.normalization * invCosTheta * invCosTheta * invCosTheta;
-  }
-  importance = imp * invDist * invDist;
+  importance = CameraImportance(c, d) * invDist * invDist;
   return true;
 }
 
@@ -582,7 +584,7 @@ RD bool LightSampleRay(const DevScene& S, const LightRec& L, V2 xi2, V2 xi3, V3&
     V3 nearDir = normalized(nearP);
     O = V3{L.dir[0], L.dir[1], L.dir[2]};
     D = LinearRows(L.m2 + 16, nearDir);
-    li = rad * kPi * L.m2[28];
+    li = V3{L.m2[29], L.m2[30], L.m2[31]} * kPi * L.m2[28];  // SampleRay leaves out the light's scale
     return true;
   }
   V3 wc{L.world[0], L.world[1], L.world[2]};

@@ -1306,6 +1306,9 @@ void BuildHostScene(const std::string& json, const std::string& baseDir, HostSce
         F3 pMin = Xf::Aff(clip.l, F3(0, 0, 0)), pMax = Xf::Aff(clip.l, F3(1, 1, 0));
         float ax = pMin.x / pMin.z, ay = pMin.y / pMin.z, bx = pMax.x / pMax.z, by = pMax.y / pMax.z;
         L.m2[28] = 1 / ((std::max(ax, bx) - std::min(ax, bx)) * (std::max(ay, by) - std::min(ay, by)));
+        L.m2[29] = irr.x;
+        L.m2[30] = irr.y;
+        L.m2[31] = irr.z;
         L.dir[0] = t.w.m[0][3];  // TranslationToWorld
         L.dir[1] = t.w.m[1][3];
         L.dir[2] = t.w.m[2][3];
@@ -1371,13 +1374,19 @@ void BuildHostScene(const std::string& json, const std::string& baseDir, HostSce
   const JValue* rn = root.get("renderer");
   if (!rn) throw ConfigError("no child: renderer");
   std::string rt = TypeOf(*rn);
-  if (rt != "path" && rt != "vol_path" && rt != "ao" && rt != "particle_tracer")
+  if (rt != "path" && rt != "vol_path" && rt != "ao" && rt != "particle_tracer" && rt != "bdpt")
     throw FactoryError("cannot find factory: " + rt);
   hs.isVol = rt == "vol_path";
   hs.isAO = rt == "ao";
   hs.isParticle = rt == "particle_tracer";  // max_depth -1, rr_depth 3 (particle_tracer.cpp:24-25)
+  hs.isBdpt = rt == "bdpt";                 // max_depth -1, rr_depth 5, use_mis true (bdpt.cpp:223-227)
   hs.maxDepth = RI(rn, "max_depth", -1);
-  hs.rrDepth = RI(rn, "rr_depth", hs.isVol ? 5 : 3);
+  hs.rrDepth = RI(rn, "rr_depth", hs.isVol || hs.isBdpt ? 5 : 3);
+  if (hs.isBdpt) {
+    hs.bdptMis = RB(rn, "use_mis", true);
+    for (const LightRec& L : hs.lights)
+      if (L.kind == LIGHT_DIRECTIONAL) throw ConfigError("bdpt: the directional light is not supported");
+  }
   if (const JValue* an = root.get("accel")) {
     std::string at = TypeOf(*an);
     if (at != "embree" && at != "gpu_bvh8") throw FactoryError("cannot find factory: " + at);

@@ -34,6 +34,7 @@ struct HostScene {
   bool isVol = false;
   bool isAO = false;  // renderer "ao"
   bool isParticle = false;  // renderer "particle_tracer"
+  bool isBdpt = false, bdptMis = true;  // renderer "bdpt" and its use_mis
   int maxDepth = -1, rrDepth = 3;
   std::vector<MatRec> mats;
   std::vector<ShapeRec> shapes;

@@ -107,6 +107,10 @@ struct ParticleParams {
   uint32_t seed;
   float sampleScale;  // pixels / light paths of the job (particle_tracer.cpp:55)
 };
+// Renderer "bdpt" (k_light.cu): the wave's pixel samples; per-sample camera-side
+// radiance into `out` (n x 3) when set, valid samples and splats into film.accum when set.
+cudaError_t LaunchBdpt(const DevScene& S, const FilmView& film, const WaveParams& w, float* out, uint32_t* err,
+                       int grid, cudaStream_t st);
 cudaError_t LaunchParticle(const DevScene& S, const FilmView& film, const ParticleParams& pp, uint32_t* err, int grid,
                            cudaStream_t st);
 // renderer "ao": for every path of bounce 0 with a hit, one cosine-sampled visibility ray

@@ -122,7 +122,8 @@ struct alignas(16) LightRec {
   uint32_t distW, distH;  // skybox with a bitmap: distribution size (texels); 0: uniform sphere sampling
   uint32_t pad2[2];
   float m2[32];        // projection: clip -> light 4x4 (m2[0..15]), light -> world linear rows of 4 (m2[16..27]),
-                       // 1 / image-rectangle area (m2[28]; projection.cpp:41-44)
+                       // 1 / image-rectangle area (m2[28]; projection.cpp:41-44), irradiance without the
+                       // scale (m2[29..31]: SampleRay / SampleLe, projection.cpp:93-120)
 };
 static_assert(sizeof(LightRec) == 384, "LightRec size");
 
@@ -219,6 +220,7 @@ struct DevScene {
   int32_t maxDepth, rrDepth, isVol;
   int32_t isAO;                // renderer "ao" (ao.cpp): one hit, one cosine-sampled visibility ray
   int32_t isParticle;          // renderer "particle_tracer": light paths splatted into the film
+  int32_t isBdpt, bdptMis;     // renderer "bdpt"; its use_mis flag
   CameraRec cam;
 };
 

@@ -505,10 +505,40 @@ void RunWaveParticle(rad_job* j) {
   j->launched += k;
 }
 
+// bdpt jobs: one thread per pixel sample over the wave's pixels (BDPT::Render,
+// bdpt.cpp:261-305), camera-side radiance and splats added into the film.
+void RunWaveBdpt(rad_job* j) {
+  Lib& lib = L();
+  const DevScene& S = j->scene->dev;
+  uint64_t npix = (uint64_t)S.cam.width * S.cam.height;
+  const uint32_t spw = WaveSamples(j);
+  const uint32_t k = std::min(spw, j->spp - j->nextSample);
+  FilmView film{j->accum, S.cam.width, S.cam.height, j->dStats};
+  ProfSink ps{j};
+  int grid = lib.sms * 4;
+  for (uint64_t p0 = 0; p0 < npix; p0 += lib.maxPaths) {
+    uint32_t count = (uint32_t)std::min<uint64_t>(lib.maxPaths, npix - p0) * k;
+    WaveParams w{(uint32_t)p0, count, j->first + j->nextSample, j->seed, nullptr, nullptr, nullptr, k};
+    cudaEvent_t a = nullptr;
+    ps.Begin(5, a);
+    Check(LaunchBdpt(S, film, w, nullptr, lib.paths.counters + kMiscBase + 1, std::max(1, std::min(grid, (int)((count + 127) / 128))),
+                     lib.stream),
+          "bdpt");
+    ps.End(5, a);
+    j->stats.kernel_launches += 1;
+  }
+  j->nextSample += k;
+  j->launched += npix * k;
+}
+
 // Runs wave(s) for the job's next sample index over all its pixels.
 void RunWave(rad_job* j) {
   if (j->scene->dev.isParticle) {
     RunWaveParticle(j);
+    return;
+  }
+  if (j->scene->dev.isBdpt) {
+    RunWaveBdpt(j);
     return;
   }
   const uint32_t spw = WaveSamples(j);
@@ -856,6 +886,8 @@ uint64_t SceneUpload(const HostScene& hs, rad_scene* sc) {
   D.isVol = hs.isVol ? 1 : 0;
   D.isAO = hs.isAO ? 1 : 0;
   D.isParticle = hs.isParticle ? 1 : 0;
+  D.isBdpt = hs.isBdpt ? 1 : 0;
+  D.bdptMis = hs.bdptMis ? 1 : 0;
   D.cam = hs.cam;
   return b;
 }
@@ -1303,6 +1335,13 @@ int rad_render_samples(rad_scene* scene, const uint32_t* pixels, const uint32_t*
       uint32_t count = (uint32_t)std::min<int64_t>(lib.maxPaths, n - b);
       WaveParams w{0, count, 0, seed, dp.p + b, ds.p + b};
       ProfSink ps{nullptr};
+      if (scene->dev.isBdpt) {
+        int grid = std::max(1, std::min(lib.sms * 4, (int)((count + 127) / 128)));
+        Check(LaunchBdpt(scene->dev, FilmView{}, w, dout.p + 3 * b, lib.paths.counters + kMiscBase + 1, grid,
+                         lib.stream),
+              "bdpt");
+        continue;
+      }
       Check(LaunchGenerate(scene->dev, lib.paths, w, lib.stream), "generate");
       if (scene->dev.isVol) {
         Check(LaunchVolPath(scene->dev, lib.paths, w, lib.paths.counters + kMiscBase + 1, lib.stream), "vol_path");
@@ -1492,7 +1531,7 @@ int rad_guide_info(rad_scene* scene, rad_guide_info_t* info) {
 // configuration and keeps the fastest in the scene.
 int rad_autotune(rad_scene* scene, const char* config_json, rad_tune_result* out) {
   if (!scene) return Fail(RAD_ERR_INVALID_ARG, "null scene");
-  if (scene->dev.isVol || scene->dev.isParticle)
+  if (scene->dev.isVol || scene->dev.isParticle || scene->dev.isBdpt)
     return Fail(RAD_ERR_UNSUPPORTED, "the autotuner covers the `path` traversal kernels");
   return Guard([&] {
     EnsureInit();

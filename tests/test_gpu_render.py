@@ -102,6 +102,41 @@ def test_particle_tracer_film(rad, oracle, scene_dir, light):
     g.close()
 
 
+@pytest.mark.parametrize("light", ["area", "sky", "point", "projection", "textured", "nomis"])
+def test_bdpt_samples_and_film(rad, oracle, scene_dir, light):
+    """Renderer `bdpt` (bdpt.cpp): each pixel sample's camera-side radiance (the
+    MIS-weighted t >= 2 connections) through rad_render_samples against the oracle
+    on identical streams; then the job film (camera side plus the t = 1 splats,
+    added with atomics) against the oracle's film: mean within 2%, and most lit
+    pixels within 5% (a sample can take the other branch on a 1-ulp
+    transcendental difference, and splat order differs)."""
+    from helpers import textured_room_scene
+    assets = None
+    if light == "textured":
+        sc, assets = textured_room_scene(24, 24, 16)
+    else:
+        sc = scenes.materials_room(24, 24, 16)
+    if light == "sky":
+        sc["scene"].append({"light": {"type": "skybox", "radiance": [0.4, 0.5, 0.6]}})
+    elif light == "point":
+        sc["scene"].append({"light": {"type": "point", "position": [0.2, 1.5, 0.3], "intensity": [2, 2, 2]}})
+    elif light == "projection":
+        sc["scene"].append({"to_world": {"translate": [0.2, 1.3, 2.2], "rotate": {"axis": [0, 1, 0], "angle": 180.0}},
+                            "light": {"type": "projection", "fov": 28.0, "irradiance": [2.0, 1.6, 1.2],
+                                      "scale": [1.5, 1.5, 1.5]}})
+    sc["renderer"] = {"type": "bdpt", "max_depth": 6, "use_mis": light != "nomis"}
+    path, text, d = write(scene_dir, "bdpt_" + light, sc, assets)
+    g, o = rad.Scene.from_file(path), oracle.OracleScene(text, d)
+    _sample_parity(g, o, 4, 0.95)
+    film = g.render()
+    ref = o.render_bdpt()
+    lit = ref.sum(axis=2) > 1e-3
+    close = (np.abs(film - ref) <= 0.05 * np.abs(ref) + 1e-5).all(axis=2)
+    assert close[lit].mean() >= 0.6, close[lit].mean()
+    assert abs(film.mean() - ref.mean()) < 0.02 * ref.mean(), (film.mean(), ref.mean())
+    g.close()
+
+
 def test_path_samples_lights(rad, oracle, scene_dir):
     """Point and projection lights (delta lights: no MIS weight on their samples) beside
     an area emitter."""

@@ -331,3 +331,39 @@ def test_particle_tracer_agrees_with_path_tracer(oracle, scene_dir):
     o.close()
     m, r = film.reshape(-1, 3).mean(0), ref.reshape(-1, 3).mean(0)
     assert np.all(np.abs(m - r) < 0.04 * r), (m, r)
+
+
+@pytest.mark.parametrize("room,mis", [("box_room", True), ("box_room", False), ("materials_room", True)])
+def test_bdpt_agrees_with_path_tracer(oracle, scene_dir, room, mis):
+    """bdpt (bdpt.cpp) and path estimate the same image when every strategy can
+    reach every path (area light, unbounded depth): the MIS weights (balance
+    heuristic, or uniform with use_mis false) sum to one over the strategies, so
+    the film means agree to within the noise. materials_room adds delta (mirror,
+    glass, plastic) and layered lobes and the importance-transport BSDF calls."""
+    from helpers import write
+    from radiantiumplusplus_gb300 import scenes
+    w = 16 if room == "box_room" else 24
+    sc = getattr(scenes, room)(w, w, 4096, max_depth=-1)
+    _, text, d = write(scene_dir, "bd_path_" + room, sc)
+    o = oracle.OracleScene(text, d)
+    ref, _ = o.render()
+    o.close()
+    sc["renderer"] = {"type": "bdpt", "use_mis": mis}
+    sc["sampler"]["sample_count"] = 2048 if room == "box_room" else 1024
+    _, text, d = write(scene_dir, "bd_bdpt_" + room, sc)
+    o = oracle.OracleScene(text, d)
+    film = o.render_bdpt()
+    o.close()
+    m, r = film.reshape(-1, 3).mean(0), ref.reshape(-1, 3).mean(0)
+    assert np.all(np.abs(m - r) < 0.03 * r), (m, r)
+
+
+def test_bdpt_rejects_directional_light(oracle):
+    """The directional light is an extension with no SampleLe; bdpt scenes with one
+    are refused when loaded."""
+    from radiantiumplusplus_gb300 import scenes
+    sc = scenes.box_room(8, 8, 1)
+    sc["scene"].append({"light": {"type": "directional", "direction": [0, -1, 0], "irradiance": [1, 1, 1]}})
+    sc["renderer"] = {"type": "bdpt"}
+    with pytest.raises(RuntimeError, match="directional"):
+        oracle.OracleScene(json.dumps(sc), "")
