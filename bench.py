@@ -376,6 +376,84 @@ def run_volume(args, world, rank, local):
     print(json.dumps(line), flush=True)
 
 
+def run_renderers(args, world, rank, local):
+    """The other renderers on the many-spheres 1080p frame: bdpt (the line's value), particle_tracer and ao,
+    each one job of `steps` whole-frame passes timed on the device, and the CPU oracle of each on a bounded
+    sample with all host threads."""
+    import torch
+    import radiantiumplusplus_gb300 as rad
+    from radiantiumplusplus_gb300 import scenes
+    torch.cuda.set_device(local)
+    rad.init({"device": local})
+    npix = W * H
+    out = {}
+    clk = None
+    with tempfile.TemporaryDirectory(prefix="rad_bench_r_") as tmp:
+        sc, assets = scenes.many_spheres(n_spheres=10000, width=W, height=H, spp=1, max_depth=MAX_DEPTH, seed=2)
+        for name, renderer in (("bdpt", {"type": "bdpt", "max_depth": args.bdpt_depth}),
+                               ("particle_tracer", {"type": "particle_tracer", "max_depth": MAX_DEPTH}),
+                               ("ao", {"type": "ao"})):
+            sc["renderer"] = renderer
+            d = os.path.join(tmp, name)
+            path = scenes.write_scene(d, sc, assets)
+            scene = rad.Scene.from_file(path)
+            per = npix  # samples (light paths for particle_tracer) per whole-frame pass
+            j = scene.submit(spp=max(1, args.warmup) * (per if name == "particle_tracer" else 1), first_sample=20_000)
+            j.wait()
+            j.close()
+            clocks = ClockSampler(local) if name == "bdpt" else None
+            torch.cuda.synchronize()
+            if clocks:
+                clocks.start()
+            job = scene.submit(spp=args.steps * (per if name == "particle_tracer" else 1), profile=True)
+            job.wait()
+            torch.cuda.synchronize()
+            if clocks:
+                clk = clocks.stop()
+            st = job.stats()
+            job.close()
+            r = {"samples_per_s": st["samples"] / (st["gpu_ms"] / 1000.0), "gpu_ms": st["gpu_ms"],
+                 "samples": st["samples"], "gpu_launches": st["kernel_launches"],
+                 "unit": "light paths/s" if name == "particle_tracer" else "samples/s"}
+            if rank == 0 and not args.no_cpu:
+                sys.path.insert(0, os.path.join(ROOT, "tests"))
+                import oracle_lib
+                o = oracle_lib.OracleScene.from_file(path)
+                threads = os.cpu_count() or 1
+                t0 = time.perf_counter()
+                if name == "bdpt":
+                    _, n = o.render_bdpt(rows=(0, H, args.bdpt_cpu_row_step), samples=(0, 1), threads=threads,
+                                         count=True)
+                    what = "rows 0..%d step %d at 1 spp" % (H, args.bdpt_cpu_row_step)
+                elif name == "particle_tracer":
+                    n = 200_000
+                    o.render_particle(spp=npix, first=0, count=n)  # one thread
+                    threads = 1
+                    what = "%d light paths of a %d-path frame, one thread" % (n, npix)
+                else:
+                    _, cs = o.render(rows=(0, H, 16), samples=(0, 1), threads=threads)
+                    n = int(cs[2])
+                    what = "rows 0..%d step 16 at 1 spp" % H
+                dt = time.perf_counter() - t0
+                r["cpu_baseline"] = {"value": n / dt, "unit": r["unit"], "cores": threads, "kind": "port",
+                                     "sample": "%s (%d, %.1f s)" % (what, n, dt)}
+                o.close()
+            scene.close()
+            out[name] = r
+    b = out["bdpt"]
+    line = {"metric": "samples/s (bdpt, many-spheres 1920x1080, depth %d)" % args.bdpt_depth,
+            "value": b["samples_per_s"], "unit": "samples/s", "n_gpus": 1, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": b["gpu_ms"] / args.steps, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded generator, no dataset)",
+            "config": {"workload": "many_spheres_1080p_renderers", "spheres": 10000, "triangles": 3200000,
+                       "width": W, "height": H, "bdpt_max_depth": args.bdpt_depth, "bdpt_rr_depth": 5,
+                       "particle_max_depth": MAX_DEPTH, "l2": "inputs larger than L2: resident scene > 129 MB"},
+            "gpu_launches": b["gpu_launches"], "clocks": clk, "renderers": out}
+    if "cpu_baseline" in b:
+        line["cpu_baseline"] = b["cpu_baseline"]
+    print(json.dumps(line), flush=True)
+
+
 def run_guided(args, world, rank, local):
     """Learned proposal vs plain BSDF sampling on the guided room (the sphere field in
     a closed room lit only through a ceiling opening), 1920x1080, depth 16. relMSE
@@ -535,7 +613,10 @@ def main():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline leg")
     ap.add_argument("--cpu-row-step", type=int, default=4)
-    ap.add_argument("--workload", default="many_spheres", choices=["many_spheres", "volume", "serving", "guided"])
+    ap.add_argument("--workload", default="many_spheres",
+                    choices=["many_spheres", "volume", "serving", "guided", "renderers"])
+    ap.add_argument("--bdpt-depth", type=int, default=MAX_DEPTH, help="renderers: bdpt max_depth")
+    ap.add_argument("--bdpt-cpu-row-step", type=int, default=8, help="renderers: oracle bdpt row sample")
     ap.add_argument("--guided-res", type=int, nargs=2, default=[1920, 1080])
     ap.add_argument("--guided-spheres", type=int, default=10000)
     ap.add_argument("--guided-ref-spp", type=int, default=1024)
@@ -558,6 +639,8 @@ def main():
         run_guided(args, world, rank, local)
     elif args.workload == "serving":
         run_serving(args, world, rank, local)
+    elif args.workload == "renderers":
+        run_renderers(args, world, rank, local)
     else:
         run_ours(args, world, rank, local)
     if world > 1:

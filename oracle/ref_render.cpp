@@ -715,10 +715,12 @@ int orc_render_particle(void* sp, uint64_t first, uint64_t count, uint64_t spp, 
   return 0;
 }
 
-// bdpt: samples [s0, s1) of every pixel; film (W x H x 3) receives, per pixel,
-// (sum of valid camera-side samples + the t = 1 splats landing there) / spp
-// (bdpt.cpp:261-305).
-int orc_render_bdpt(void* sp, int s0, int s1, uint32_t seed, int threads, float* film) {
+// bdpt: samples [s0, s1) of the pixels of rows [row0, row1) step rowStep; film
+// (W x H x 3) receives, per pixel, (sum of valid camera-side samples + the t = 1
+// splats landing there) / spp (bdpt.cpp:261-305). Returns the number of samples
+// run, or -1.
+int64_t orc_render_bdpt(void* sp, int row0, int row1, int rowStep, int s0, int s1, uint32_t seed, int threads,
+                        float* film) {
   Scene& S = *(Scene*)sp;
   if (S.renderer != "bdpt") {
     g_err = "orc_render_bdpt: the scene's renderer is not bdpt";
@@ -728,14 +730,17 @@ int orc_render_bdpt(void* sp, int s0, int s1, uint32_t seed, int threads, float*
   const size_t npix = (size_t)W * H;
   int nt = threads > 0 ? threads : (int)std::thread::hardware_concurrency();
   std::vector<std::vector<Spectrum>> images(nt, std::vector<Spectrum>(npix, Spectrum(0)));
-  std::atomic<int> next{0};
+  std::vector<int> rows;
+  for (int y = row0; y < row1 && y < H; y += rowStep) rows.push_back(y);
+  std::atomic<size_t> next{0};
   std::atomic<bool> failed{false};
   auto worker = [&](int w) {
     try {
       std::vector<Spectrum>& img = images[w];
       for (;;) {
-        int y = next.fetch_add(1);
-        if (y >= H) break;
+        size_t k = next.fetch_add(1);
+        if (k >= rows.size()) break;
+        int y = rows[k];
         for (int x = 0; x < W; x++) {
           Spectrum acc(0);
           for (int s = s0; s < s1; s++) {
@@ -763,7 +768,7 @@ int orc_render_bdpt(void* sp, int s0, int s1, uint32_t seed, int threads, float*
     film[3 * p + 1] = sum.y * coeff;
     film[3 * p + 2] = sum.z * coeff;
   }
-  return 0;
+  return (int64_t)rows.size() * W * (s1 - s0);
 }
 
 // Per-sample radiance for a list of (pixel, sample) pairs: out n x 3.

@@ -24,7 +24,7 @@ BUILD = os.path.join(PKG, "_build")
 LIB = os.path.join(PKG, "librad_gpu.so")
 
 HOST_SOURCES = ["host_scene.cpp", "host_bvh.cpp", "host_image.cpp", "host_texeval.cpp"]
-CUDA_SOURCES = ["runtime.cu", "k_path.cu", "k_vol.cu", "k_light.cu", "k_parity.cu", "k_noalloc.cu", "k_guide.cu",
+CUDA_SOURCES = ["runtime.cu", "k_path.cu", "k_vol.cu", "k_light.cu", "k_bdpt.cu", "k_parity.cu", "k_noalloc.cu", "k_guide.cu",
                 "guide_host.cu"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 

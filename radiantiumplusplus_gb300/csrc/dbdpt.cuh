@@ -4,18 +4,20 @@
 // have made the same path. Connections with one camera vertex (t = 1) project
 // to another pixel and are splatted into the film there.
 //
-// One thread runs one pixel sample; both subpaths live in the thread's local
-// memory (kMaxBdptVertices each; a subpath stops there).
+// The functions here are the per-sample steps of that algorithm; the kernels
+// (k_bdpt.cu) run them as a wavefront: each subpath bounce between two
+// launches of the BVH8 closest-hit kernel, the connections of one camera
+// vertex index per launch, their visibility rays through the any-hit kernel.
+// A subpath's vertices live in device memory strided by the wave size; a
+// subpath stops at kMaxBdptVertices vertices.
 #pragma once
 #include "dlight.cuh"
 
 namespace rad {
 
-constexpr int kMaxBdptVertices = 64;
-
 enum : uint32_t { BV_CAMERA = 0, BV_LIGHT = 1, BV_SURFACE = 2 };
 
-struct BVert {  // bdpt.cpp:29-44
+struct BVert {  // bdpt.cpp:29-44, 112 bytes
   V3 P, N;     // position, geometric normal (zero: not on a surface)
   Frame sh;    // shading frame
   V3 Wi;       // surface: local incident direction
@@ -25,6 +27,13 @@ struct BVert {  // bdpt.cpp:29-44
   int32_t id;  // surface: shape; light: light
   uint32_t type;
   uint32_t delta;
+};
+
+// One sample's subpath: vertex k at v[k * stride].
+struct VPath {
+  BVert* v;
+  uint32_t stride;
+  RD BVert& operator[](int k) const { return v[(size_t)k * stride]; }
 };
 
 RD bool VIsOnSurface(const BVert& v) { return !(v.N.x == 0.f && v.N.y == 0.f && v.N.z == 0.f); }
@@ -192,80 +201,118 @@ RDN float VPdf(const DevScene& S, const BVert& v, const BVert* prev, const BVert
   return ConvertDensity(S, v, pdf, next);
 }
 
-// BDPT::RandomWalk (bdpt.cpp:409-476)
-RDN void RandomWalk(const DevScene& S, Pcg32& rng, V3 O, V3 D, float tmin, float tmax, V3 thr, float pdf, bool imp,
-                   BVert* path, int& n, uint32_t* err) {
-  float pdfFwd = pdf, pdfRev = 0.f;
-  float rr = 1.f, eta = 1.f;
-  for (int depth = 0;; depth++) {
-    if (thr.x == 0.f && thr.y == 0.f && thr.z == 0.f) break;
-    if (depth >= S.rrDepth) {
-      float rrVal = fminr(max_comp(thr) * Sqr(eta), 0.95f);
-      if (Next1D(rng) > rrVal) break;
-      thr = thr * Rcp(rrVal);
-      rr *= rrVal;
+// Walk state of one subpath between two traces (BDPT::RandomWalk's locals).
+struct WalkState {
+  V3 thr;
+  float eta, pdfFwd, rr;
+  int n;  // vertices so far
+};
+
+RD bool IsBlack(V3 v) { return v.x == 0.f && v.y == 0.f && v.z == 0.f; }
+
+// Top of RandomWalk's loop for bounce `depth` (bdpt.cpp:418-428): a black
+// throughput ends the walk, then Russian roulette from rr_depth.
+RD bool WalkContinue(const DevScene& S, Pcg32& rng, WalkState& w, int depth) {
+  if (IsBlack(w.thr)) return false;
+  if (depth >= S.rrDepth) {
+    float rrVal = fminr(max_comp(w.thr) * Sqr(w.eta), 0.95f);
+    if (Next1D(rng) > rrVal) return false;
+    w.thr = w.thr * Rcp(rrVal);
+    w.rr *= rrVal;
+  }
+  return true;
+}
+
+// The rest of RandomWalk's bounce `depth` (bdpt.cpp:429-475) once ray (O, D)
+// has been traced: the miss (an environment vertex on camera subpaths) or the
+// surface vertex, the BSDF sample and the reverse density of the previous
+// vertex. Returns true with the next ray in (O, D) when the walk goes on.
+RDN bool WalkStep(const DevScene& S, Pcg32& rng, VPath path, int cap, WalkState& w, int depth, bool imp, bool hit,
+                  const TraceHit& h, V3& O, V3& D) {
+  if (!hit) {
+    if (S.envLight >= 0 && !imp && w.n < cap) {
+      BVert e{};
+      e.type = BV_LIGHT;
+      e.id = S.envLight;
+      e.P = D * -1.f + O;  // ray(-1)
+      e.N = -D;
+      e.thr = w.thr;
+      e.pdfFwd = w.pdfFwd;
+      path[w.n++] = e;
     }
-    RayPre r = MakeRayPre(O, D, tmin);
-    TraceHit h;
-    if (!TraceBvh8<false>(S, r, tmax, h, err)) {
-      if (S.envLight >= 0 && !imp && n < kMaxBdptVertices) {
-        BVert& e = path[n++];
-        e = BVert{};
-        e.type = BV_LIGHT;
-        e.id = S.envLight;
-        e.P = D * -1.f + O;  // ray(-1)
-        e.N = -D;
-        e.thr = thr;
-        e.pdfFwd = pdfFwd;
-      }
-      break;
-    }
-    SurfInt si = ComputeSI(S, O, D, h);
-    const ShapeRec& shp = S.shapes[si.shape];
-    if (shp.bsdf < 0) break;
-    if (n >= kMaxBdptVertices) break;
-    BVert& now = path[n];
-    now.type = BV_SURFACE;
-    now.id = si.shape;
-    now.P = si.P;
-    now.N = si.N;
-    now.sh = si.sh;
-    now.Wi = si.Wi;
-    now.uv = S.nTex ? ComputeUV(S, h, si).uv : V2{0.f, 0.f};
-    now.thr = thr;
-    now.pdfRev = 0.f;
-    now.delta = 0u;
-    now.pdfFwd = ConvertDensity(S, path[n - 1], pdfFwd * rr, now);
-    BVert& prev = path[n - 1];
-    n++;
-    if (S.maxDepth >= 0 && (depth + 1) > S.maxDepth) break;
-    if (shp.light >= 0) break;
-    const uint32_t mi = (uint32_t)shp.bsdf;
-    TexCtx tcx = VTex(S, now);
-    const TexCtx* tc = S.nTex ? &tcx : nullptr;
+    return false;
+  }
+  SurfInt si = ComputeSI(S, O, D, h);
+  const ShapeRec& shp = S.shapes[si.shape];
+  if (shp.bsdf < 0) return false;
+  if (w.n >= cap) return false;
+  BVert now;
+  now.type = BV_SURFACE;
+  now.id = si.shape;
+  now.P = si.P;
+  now.N = si.N;
+  now.sh = si.sh;
+  now.Wi = si.Wi;
+  now.uv = S.nTex ? ComputeUV(S, h, si).uv : V2{0.f, 0.f};
+  now.thr = w.thr;
+  now.pdfRev = 0.f;
+  now.delta = 0u;
+  const BVert prev = path[w.n - 1];
+  now.pdfFwd = ConvertDensity(S, prev, w.pdfFwd * w.rr, now);
+  const int k = w.n++;
+  bool go = !(S.maxDepth >= 0 && (depth + 1) > S.maxDepth) && shp.light < 0;
+  BsdfSampleRes bs{};
+  const uint32_t mi = (uint32_t)shp.bsdf;
+  TexCtx tcx = VTex(S, now);
+  const TexCtx* tc = S.nTex ? &tcx : nullptr;
+  if (go) {
     float bl = Next1D(rng);
     V2 bd = Next2D(rng);
-    BsdfSampleRes bs = BsdfSample(S.mats, mi, si.Wi, bl, bd, tc, imp);
-    if (bs.pdf <= 0.f) break;
-    bool isDelta = (bs.type & BT_DELTA) != 0u;
-    float correction = imp ? CorrectShadingNormal(now, bs.wo) : 1.f;
-    thr = cmul(thr, bs.f) * correction / bs.pdf;
-    eta *= bs.eta;
-    D = ToWorld(si.sh, bs.wo);
-    O = OffsetP(si.P, si.N, D);
-    tmin = 0.f;
-    tmax = kFloatMax;
-    pdfFwd = bs.pdf;
-    if (isDelta) {
-      pdfRev = pdfFwd;
-      now.delta = 1u;
-    } else {
-      V3 f;
-      BsdfEvalPdf(S.mats, mi, bs.wo, si.Wi, f, pdfRev, tc, imp);  // BsdfRevPdf (bdpt.cpp:647-651)
-      now.delta = 0u;
-    }
-    prev.pdfRev = ConvertDensity(S, now, pdfRev * rr, prev);
+    bs = BsdfSample(S.mats, mi, si.Wi, bl, bd, tc, imp);
+    go = !(bs.pdf <= 0.f);
   }
+  if (!go) {
+    path[k] = now;
+    return false;
+  }
+  bool isDelta = (bs.type & BT_DELTA) != 0u;
+  float correction = imp ? CorrectShadingNormal(now, bs.wo) : 1.f;
+  w.thr = cmul(w.thr, bs.f) * correction / bs.pdf;
+  w.eta *= bs.eta;
+  D = ToWorld(si.sh, bs.wo);
+  O = OffsetP(si.P, si.N, D);
+  w.pdfFwd = bs.pdf;
+  float pdfRev;
+  if (isDelta) {
+    pdfRev = w.pdfFwd;
+    now.delta = 1u;
+  } else {
+    V3 f;
+    BsdfEvalPdf(S.mats, mi, bs.wo, si.Wi, f, pdfRev, tc, imp);  // BsdfRevPdf (bdpt.cpp:647-651)
+  }
+  path[k] = now;
+  path[k - 1].pdfRev = ConvertDensity(S, now, pdfRev * w.rr, prev);
+  return true;
+}
+
+// BDPT::GenerateCameraPath (bdpt.cpp:351-369) up to its first trace: the
+// jittered camera ray of pixel sample (pix, smp) and the camera vertex.
+RD void CameraPathStart(const DevScene& S, Pcg32& rng, uint32_t pix, VPath path, WalkState& w, V3& O, V3& D,
+                        float& tmin, float& tmax) {
+  uint32_t x = pix % (uint32_t)S.cam.width, y = pix / (uint32_t)S.cam.width;
+  float jx = Next1D(rng);
+  float jy = Next1D(rng);
+  CameraRay(S.cam, (float)x + jx, (float)y + jy, O, D, tmin, tmax);
+  BVert c{};
+  c.type = BV_CAMERA;
+  c.thr = v3s(1.f);
+  c.P = O;
+  path[0] = c;
+  w.thr = v3s(1.f);
+  w.eta = 1.f;
+  w.pdfFwd = CameraPdfWe(S.cam, D);
+  w.rr = 1.f;
+  w.n = 1;
 }
 
 // Light::SampleLe (area.cpp:130-140, point.cpp:75-85, projection.cpp:107-120,
@@ -349,37 +396,62 @@ RDN LeSample LightSampleLe(const DevScene& S, const LightRec& L, V2 xi2, V2 xi3)
   return r;
 }
 
-// BDPT::GenerateLightPath (bdpt.cpp:371-407); a scene without lights has no light subpath
-RD void GenerateLightPath(const DevScene& S, Pcg32& rng, BVert* path, int& n, uint32_t* err) {
-  if (S.nLights == 0) return;
+// Direction and position density of the emitted ray, kept for the fix-up of
+// infinite-light subpaths once the walk is over (bdpt.cpp:398-406).
+struct LightFix {
+  V3 D;
+  float pdfPos;
+};
+
+// BDPT::GenerateLightPath (bdpt.cpp:371-397) up to its first trace: the light
+// pick, the emitted ray and the light vertex. False when there is no light
+// subpath (no light, or a zero density or radiance).
+RD bool LightPathStart(const DevScene& S, Pcg32& rng, VPath path, WalkState& w, V3& O, V3& D, LightFix& fix) {
+  w.n = 0;
+  if (S.nLights == 0) return false;
   int index;
   float selectPdf;
   PickLight(S, Next1D(rng), index, selectPdf);
   V2 xi2 = Next2D(rng);
   V2 xi3 = Next2D(rng);
   LeSample r = LightSampleLe(S, S.lights[index], xi2, xi3);
-  if (r.pdfPos <= 0.f || r.pdfDir <= 0.f || (r.le.x == 0.f && r.le.y == 0.f && r.le.z == 0.f)) return;
-  V3 thr = r.le * AbsDot(r.N, r.D) / (selectPdf * r.pdfPos * r.pdfDir);
-  BVert& lv = path[n++];
-  lv = VFromPsr(BV_LIGHT, r.P, r.N);
+  if (r.pdfPos <= 0.f || r.pdfDir <= 0.f || IsBlack(r.le)) return false;
+  BVert lv = VFromPsr(BV_LIGHT, r.P, r.N);
   lv.thr = r.le;
   lv.pdfFwd = r.pdfPos * selectPdf;
   lv.pdfRev = 0.f;
   lv.delta = r.delta ? 1u : 0u;
   lv.id = index;
-  RandomWalk(S, rng, r.O, r.D, 0.f, kFloatMax, thr, r.pdfDir, true, path, n, err);
-  if (VIsInfinite(S, path[0])) {
-    if (n > 1) {
-      path[1].pdfFwd = r.pdfPos;
-      if (VIsOnSurface(path[1])) path[1].pdfFwd *= AbsDot(r.D, path[1].N);
-    }
-    path[0].pdfFwd = InfiniteLightDensity(S, r.D);
-  }
+  path[0] = lv;
+  w.thr = r.le * AbsDot(r.N, r.D) / (selectPdf * r.pdfPos * r.pdfDir);
+  w.eta = 1.f;
+  w.pdfFwd = r.pdfDir;
+  w.rr = 1.f;
+  w.n = 1;
+  O = r.O;
+  D = r.D;
+  fix.D = r.D;
+  fix.pdfPos = r.pdfPos;
+  return true;
 }
 
-// BDPT::MISWeight (bdpt.cpp:555-634): the strategy's vertex values are set in
-// place and restored before returning, as the reference's scoped assignments do.
-RDN float MISWeight(const DevScene& S, BVert* lightV, BVert* camV, const BVert& sampled, int s, int t) {
+// bdpt.cpp:398-406: an infinite light's subpath takes area densities that
+// the walk could not know.
+RD void LightPathFinish(const DevScene& S, VPath path, int n, const LightFix& fix) {
+  if (n == 0 || !VIsInfinite(S, path[0])) return;
+  if (n > 1) {
+    float pf = fix.pdfPos;
+    if (VIsOnSurface(path[1])) pf *= AbsDot(fix.D, path[1].N);
+    path[1].pdfFwd = pf;
+  }
+  path[0].pdfFwd = InfiniteLightDensity(S, fix.D);
+}
+
+// BDPT::MISWeight (bdpt.cpp:555-634). The reference assigns the strategy's
+// values into the subpaths (the sampled end vertex, the connection vertices'
+// delta flags and the four reverse densities) and restores them afterwards;
+// here they are overrides read in place of the stored values.
+RDN float MISWeight(const DevScene& S, VPath lightV, VPath camV, const BVert& sampled, int s, int t) {
   if (s + t == 2) return 1.f;
   float sumRi = 0.f;
   if (!S.bdptMis) {
@@ -391,53 +463,59 @@ RDN float MISWeight(const DevScene& S, BVert* lightV, BVert* camV, const BVert& 
     }
     return 1.f / (1.f + sumRi);
   }
-  BVert* qs = s > 0 ? &lightV[s - 1] : nullptr;
-  BVert* pt = t > 0 ? &camV[t - 1] : nullptr;
-  BVert* qsMinus = s > 1 ? &lightV[s - 2] : nullptr;
-  BVert* ptMinus = t > 1 ? &camV[t - 2] : nullptr;
-  BVert saveQs, savePt, saveQsMinus, savePtMinus;
-  if (qs) saveQs = *qs;
-  if (pt) savePt = *pt;
-  if (qsMinus) saveQsMinus = *qsMinus;
-  if (ptMinus) savePtMinus = *ptMinus;
-  if (s == 1)
-    *qs = sampled;
-  else if (t == 1)
-    *pt = sampled;
-  if (pt) pt->delta = 0u;
-  if (qs) qs->delta = 0u;
-  if (pt) pt->pdfRev = s > 0 ? VPdf(S, *qs, qsMinus, *pt) : PdfLightOrigin(S, *pt, *ptMinus);
-  if (ptMinus) ptMinus->pdfRev = s > 0 ? VPdf(S, *pt, qs, *ptMinus) : PdfLightV(S, *pt, *ptMinus);
-  if (qs) qs->pdfRev = VPdf(S, *pt, ptMinus, *qs);
-  if (qsMinus) qsMinus->pdfRev = VPdf(S, *qs, pt, *qsMinus);
+  const BVert* qs = s > 0 ? (s == 1 ? &sampled : &lightV[s - 1]) : nullptr;
+  const BVert* pt = t > 0 ? (t == 1 ? &sampled : &camV[t - 1]) : nullptr;
+  const BVert* qsMinus = s > 1 ? &lightV[s - 2] : nullptr;
+  const BVert* ptMinus = t > 1 ? &camV[t - 2] : nullptr;
+  float ptRev = 0.f, ptMinusRev = 0.f, qsRev = 0.f, qsMinusRev = 0.f;
+  if (pt) ptRev = s > 0 ? VPdf(S, *qs, qsMinus, *pt) : PdfLightOrigin(S, *pt, *ptMinus);
+  if (ptMinus) ptMinusRev = s > 0 ? VPdf(S, *pt, qs, *ptMinus) : PdfLightV(S, *pt, *ptMinus);
+  if (qs) qsRev = VPdf(S, *pt, ptMinus, *qs);
+  if (qsMinus) qsMinusRev = VPdf(S, *qs, pt, *qsMinus);
   float ri = 1.f;
   for (int i = t - 1; i > 0; --i) {
-    float rv = camV[i].pdfRev != 0.f ? camV[i].pdfRev : 1.f, fw = camV[i].pdfFwd != 0.f ? camV[i].pdfFwd : 1.f;
-    ri *= rv / fw;
-    if (!camV[i].delta && !camV[i - 1].delta) sumRi += ri;
+    const BVert& v = camV[i];
+    float rev = i == t - 1 ? ptRev : (i == t - 2 ? ptMinusRev : v.pdfRev);
+    rev = rev != 0.f ? rev : 1.f;
+    float fwd = v.pdfFwd != 0.f ? v.pdfFwd : 1.f;
+    ri *= rev / fwd;
+    bool dI = i == t - 1 ? false : v.delta != 0u;
+    if (!dI && !camV[i - 1].delta) sumRi += ri;
   }
   ri = 1.f;
   for (int i = s - 1; i >= 0; --i) {
-    float rv = lightV[i].pdfRev != 0.f ? lightV[i].pdfRev : 1.f, fw = lightV[i].pdfFwd != 0.f ? lightV[i].pdfFwd : 1.f;
-    ri *= rv / fw;
-    bool deltaLightvertex = i > 0 ? lightV[i - 1].delta != 0u : lightV[0].delta != 0u;
-    if (!lightV[i].delta && !deltaLightvertex) sumRi += ri;
+    const BVert& v = (s == 1 && i == 0) ? sampled : lightV[i];
+    float rev = i == s - 1 ? qsRev : (i == s - 2 ? qsMinusRev : v.pdfRev);
+    rev = rev != 0.f ? rev : 1.f;
+    float fwd = v.pdfFwd != 0.f ? v.pdfFwd : 1.f;
+    ri *= rev / fwd;
+    bool dI = i == s - 1 ? false : v.delta != 0u;
+    bool deltaLightvertex = i > 0 ? lightV[i - 1].delta != 0u : dI;
+    if (!dI && !deltaLightvertex) sumRi += ri;
   }
-  if (qsMinus) *qsMinus = saveQsMinus;
-  if (ptMinus) *ptMinus = savePtMinus;
-  if (qs) *qs = saveQs;
-  if (pt) *pt = savePt;
   return 1.f / (1.f + sumRi);
 }
 
-RD bool IsBlack(V3 v) { return v.x == 0.f && v.y == 0.f && v.z == 0.f; }
+// One connection's result: contribution c (MIS-weighted); with `vis`, it
+// counts only if the segment from (P, N) to `target` is unoccluded
+// (Scene::IsOcclude, scene.cpp:53-63); `splat` connections (t = 1) land on
+// film position `pixel` instead of the sample's own pixel.
+struct ConnOut {
+  V3 c, P, N, target;
+  V2 pixel;
+  bool vis, splat;
+};
 
-// BDPT::ConnectBdpt (bdpt.cpp:478-553)
-RDN V3 ConnectBdpt(const DevScene& S, Pcg32& rng, BVert* lightV, BVert* camV, int s, int t, V2& scrPos,
-                  uint32_t* err) {
-  V3 l = v3s(0.f);
-  if (t > 1 && s != 0 && camV[t - 1].type == BV_LIGHT) return l;
+// BDPT::ConnectBdpt (bdpt.cpp:478-553) with the visibility test deferred:
+// false when the connection contributes nothing whatever the visibility. The
+// weight is computed for every candidate; the reference computes it only for
+// unoccluded ones, to the same value.
+RDN bool ConnectBdpt(const DevScene& S, Pcg32& rng, VPath lightV, VPath camV, int s, int t, ConnOut& o) {
+  if (t > 1 && s != 0 && camV[t - 1].type == BV_LIGHT) return false;
   BVert sampled{};
+  V3 l = v3s(0.f);
+  o.vis = false;
+  o.splat = false;
   if (s == 0) {
     const BVert& pt = camV[t - 1];
     if (VIsLight(S, pt)) {
@@ -448,18 +526,24 @@ RDN V3 ConnectBdpt(const DevScene& S, Pcg32& rng, BVert* lightV, BVert* camV, in
     const BVert& qs = lightV[s - 1];
     if (VConnectible(S, qs)) {
       Next2D(rng);  // Perspective::SampleDirection's sample (unused by a pinhole)
-      V3 camP, camDir, camN;
+      V3 camP, camDir;
       float camDist, we;
       V2 pixel;
       if (CameraSampleDirection(S.cam, qs.P, camP, camDir, camDist, pixel, we)) {
-        camN = LinearRows(S.cam.camToWorld, V3{0.f, 0.f, 1.f});
-        sampled = VFromPsr(BV_CAMERA, camP, camN);
-        sampled.thr = v3s(we / 1.f);
+        sampled = VFromPsr(BV_CAMERA, camP, LinearRows(S.cam.camToWorld, V3{0.f, 0.f, 1.f}));
+        sampled.thr = v3s(we / 1.f);  // dsr.Pdf is 1
         sampled.delta = 1u;
         V3 fs = VFs(S, qs, sampled, true);
         V3 result = cmul(cmul(qs.thr, fs), sampled.thr);
-        scrPos = pixel;
-        if (!IsBlack(result) && !LOccluded(S, qs.P, qs.N, camP, err)) l = l + result;
+        if (!IsBlack(result)) {
+          l = l + result;
+          o.vis = true;
+          o.splat = true;
+          o.pixel = pixel;
+          o.P = qs.P;
+          o.N = qs.N;
+          o.target = camP;
+        }
       }
     }
   } else if (s == 1) {
@@ -481,7 +565,13 @@ RDN V3 ConnectBdpt(const DevScene& S, Pcg32& rng, BVert* lightV, BVert* camV, in
           sampled.pdfFwd = PdfLightOrigin(S, sampled, pt);
           V3 fs = VFs(S, pt, sampled, false);
           V3 result = cmul(cmul(pt.thr, fs), sampled.thr);
-          if (!IsBlack(result) && !LOccluded(S, pt.P, pt.N, dsr.P, err)) l = l + result;
+          if (!IsBlack(result)) {
+            l = l + result;
+            o.vis = true;
+            o.P = pt.P;
+            o.N = pt.N;
+            o.target = dsr.P;
+          }
         }
       }
     }
@@ -493,52 +583,31 @@ RDN V3 ConnectBdpt(const DevScene& S, Pcg32& rng, BVert* lightV, BVert* camV, in
       V3 cameraFs = VFs(S, pt, qs, false);
       float g = 1.f / sqnorm(qs.P - pt.P);  // BDPT::G (bdpt.cpp:652-656)
       V3 result = cmul(cmul(cmul(qs.thr, lightFs), cameraFs), pt.thr) * g;
-      if (!IsBlack(result) && !LOccluded(S, pt.P, pt.N, qs.P, err)) l = l + result;
-    }
-  }
-  if (IsBlack(l)) return l;
-  float mis = MISWeight(S, lightV, camV, sampled, s, t);
-  return l * mis;
-}
-
-// One pixel sample (BDPT::Render + Li, bdpt.cpp:261-349): returns the camera-side
-// sum (t >= 2); t = 1 connections are splatted into `film` when it is set.
-RDN V3 BdptSample(const DevScene& S, const ParticleFilm* film, uint32_t pix, uint32_t smp, uint32_t seed,
-                 uint32_t* err) {
-  Pcg32 rng = PcgForSample(pix, smp, seed);
-  uint32_t x = pix % (uint32_t)S.cam.width, y = pix / (uint32_t)S.cam.width;
-  float jx = Next1D(rng);
-  float jy = Next1D(rng);
-  V3 O, D;
-  float tmin, tmax;
-  CameraRay(S.cam, (float)x + jx, (float)y + jy, O, D, tmin, tmax);
-  BVert camV[kMaxBdptVertices];
-  BVert lightV[kMaxBdptVertices];
-  int nc = 0, nl = 0;
-  // BDPT::GenerateCameraPath (bdpt.cpp:351-369)
-  float pdfDir = CameraPdfWe(S.cam, D);
-  camV[0] = BVert{};
-  camV[0].type = BV_CAMERA;
-  camV[0].thr = v3s(1.f);
-  camV[0].P = O;
-  nc = 1;
-  RandomWalk(S, rng, O, D, tmin, tmax, v3s(1.f), pdfDir, false, camV, nc, err);
-  GenerateLightPath(S, rng, lightV, nl, err);
-  V3 l = v3s(0.f);
-  for (int t = 1; t <= nc; ++t) {
-    for (int s = 0; s <= nl; ++s) {
-      int depth = t + s - 2;
-      if ((s == 1 && t == 1) || depth < 0) continue;
-      V2 scrPos{(float)x, (float)y};
-      V3 pathL = ConnectBdpt(S, rng, lightV, camV, s, t, scrPos, err);
-      if (t == 1) {
-        if (film && !IsBlack(pathL)) Splat(*film, scrPos, pathL);
-      } else {
-        l = l + pathL;
+      if (!IsBlack(result)) {
+        l = l + result;
+        o.vis = true;
+        o.P = pt.P;
+        o.N = pt.N;
+        o.target = qs.P;
       }
     }
   }
-  return l;
+  if (IsBlack(l)) return false;
+  float mis = MISWeight(S, lightV, camV, sampled, s, t);
+  o.c = l * mis;
+  return true;
+}
+
+// The visibility ray of Scene::IsOcclude (scene.cpp:53-63) from (P, N) to
+// target: false when the points are closer than the shadow epsilon (occluded).
+RD bool ShadowRay(V3 P, V3 N, V3 target, V3& o, V3& d, float& tmax) {
+  o = OffsetP(P, N, target - P);
+  d = target - o;
+  float dist = norm(d);
+  if (dist < kShadowEps) return false;
+  d = d / dist;
+  tmax = dist * (1.f - kShadowEps);
+  return true;
 }
 
 }  // namespace rad

@@ -92,6 +92,7 @@ extern "C" RAD_API int rad_render_samples_noalloc(rad_scene* scene, const uint32
   if (n == 0) return RAD_OK;
   const DevScene& S = *SceneDevice(scene);
   if (S.isParticle) return ReportError(RAD_ERR_UNSUPPORTED, "particle_tracer has no per-pixel samples");
+  if (S.isBdpt) return ReportError(RAD_ERR_UNSUPPORTED, "bdpt keeps its subpaths in device scratch it allocates");
   int dev = SceneDeviceIndex();
   if (dev < 0 || dev >= kMaxDevices) return ReportError(RAD_ERR_INVALID_ARG, "device index out of range");
   int prevDev = 0;
@@ -119,20 +120,6 @@ extern "C" RAD_API int rad_render_samples_noalloc(rad_scene* scene, const uint32
   if (cudaMemsetAsync(addr->counters + kMiscBase + 1, 0, sizeof(uint32_t), st) != cudaSuccess)
     return done(RAD_ERR_CUDA, "cudaMemsetAsync failed");
   WaveParams w{0, count, 0, seed, d_pixels, d_samples};
-  if (S.isBdpt) {  // one thread per sample, no path buffers
-    int sms = 148;
-    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-    int grid = std::max(1, std::min(sms * 4, (int)((count + 127) / 128)));
-    if (LaunchBdpt(S, FilmView{}, w, d_radiance, addr->counters + kMiscBase + 1, grid, st) != cudaSuccess)
-      return done(RAD_ERR_CUDA, "bdpt launch failed");
-    uint32_t err = 0;
-    if (cudaMemcpyAsync(&err, addr->counters + kMiscBase + 1, sizeof(uint32_t), cudaMemcpyDeviceToHost, st) !=
-            cudaSuccess ||
-        cudaStreamSynchronize(st) != cudaSuccess)
-      return done(RAD_ERR_CUDA, "stream synchronisation failed");
-    if (err) return done(RAD_ERR_DEVICE_CHECK, "a device-side bound was exceeded");
-    return done(RAD_OK, "");
-  }
   if (LaunchGenerate(S, B, w, st) != cudaSuccess) return done(RAD_ERR_CUDA, "generate launch failed");
   if (S.isVol) {
     if (LaunchVolPath(S, B, w, addr->counters + kMiscBase + 1, st) != cudaSuccess)

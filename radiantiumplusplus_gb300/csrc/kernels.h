@@ -107,10 +107,41 @@ struct ParticleParams {
   uint32_t seed;
   float sampleScale;  // pixels / light paths of the job (particle_tracer.cpp:55)
 };
-// Renderer "bdpt" (k_light.cu): the wave's pixel samples; per-sample camera-side
-// radiance into `out` (n x 3) when set, valid samples and splats into film.accum when set.
-cudaError_t LaunchBdpt(const DevScene& S, const FilmView& film, const WaveParams& w, float* out, uint32_t* err,
-                       int grid, cudaStream_t st);
+// ---- renderer "bdpt" (k_bdpt.cu): wavefront stages of one wave of pixel samples
+struct BVert;
+constexpr size_t kBVertBytes = 112;  // sizeof(BVert) (dbdpt.cuh)
+struct BdptBuffers {
+  BVert* vert;         // [2 * cap][nw]: camera subpath vertices, then light subpath vertices
+  float4* walkA;       // per sample: walk throughput rgb, eta
+  float4* walkB;       // per sample: pdfFwd, rr, vertex count (bits)
+  float4* fix;         // per sample: emitted direction xyz, position density (light subpath fix-up)
+  uint32_t* nCam;      // per sample: camera / light subpath vertex counts
+  uint32_t* nLight;
+  float4 *shO, *shD, *shC;  // visibility rays of one connection round: origin + tmax, direction + tag, contribution
+  uint32_t cap, nw, shCap;
+};
+// Camera subpaths: jittered camera rays of the wave's samples into queue 0.
+cudaError_t LaunchBdptCamera(const DevScene& S, const PathBuffers& B, const BdptBuffers& V, const WaveParams& w,
+                             cudaStream_t st);
+// Light subpaths: light pick and emitted rays of the wave's `count` samples into queue 0.
+cudaError_t LaunchBdptLight(const DevScene& S, const PathBuffers& B, const BdptBuffers& V, uint32_t count,
+                            cudaStream_t st);
+// One subpath bounce for the queue of `depth` (after LaunchExtend): vertex, BSDF sample, next ray.
+// Longest camera subpath of the wave: B.counters[kMiscBase] (atomic max).
+cudaError_t LaunchBdptWalk(const DevScene& S, const PathBuffers& B, const BdptBuffers& V, int depth, bool light,
+                           int grid, cudaStream_t st);
+// Infinite-light fix-up of the light subpaths.
+cudaError_t LaunchBdptLightFix(const DevScene& S, const BdptBuffers& V, uint32_t count, cudaStream_t st);
+// The connections of camera vertex t - 1 of every sample (all light vertices): direct contributions
+// into B.L, visibility rays into V.sh* (count in B.counters[kShadowBase + t - 1]); splats only with `splats`.
+cudaError_t LaunchBdptConnect(const DevScene& S, const PathBuffers& B, const BdptBuffers& V, uint32_t count, int t,
+                              bool splats, int grid, cudaStream_t st);
+// Visibility rays of round t: unoccluded contributions into B.L (atomic) or the film (splats).
+cudaError_t LaunchBdptShadow(const DevScene& S, const PathBuffers& B, const BdptBuffers& V, int t, float4* film,
+                             int grid, cudaStream_t st, int refillBusy, int leafFrac8);
+// Per sample: camera-side radiance into `out` (n x 3) and / or valid samples into the film.
+cudaError_t LaunchBdptAccumulate(const PathBuffers& B, const FilmView& film, uint32_t count, float* out,
+                                 cudaStream_t st);
 cudaError_t LaunchParticle(const DevScene& S, const FilmView& film, const ParticleParams& pp, uint32_t* err, int grid,
                            cudaStream_t st);
 // renderer "ao": for every path of bounce 0 with a hit, one cosine-sampled visibility ray

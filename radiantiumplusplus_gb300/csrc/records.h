@@ -127,6 +127,9 @@ struct alignas(16) LightRec {
 };
 static_assert(sizeof(LightRec) == 384, "LightRec size");
 
+// bdpt: vertices of one subpath at most (camera or light vertex included)
+constexpr int kMaxBdptVertices = 64;
+
 // ---------------------------------------------------------------- media
 enum MediumKind : uint32_t { MED_HOMOGENEOUS = 0, MED_HETEROGENEOUS = 1 };
 struct alignas(16) MediumRec {

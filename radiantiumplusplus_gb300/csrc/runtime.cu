@@ -77,6 +77,11 @@ double NowMs() {
   return duration<double, std::milli>(steady_clock::now().time_since_epoch()).count();
 }
 
+void FreeAll(std::vector<void*>& v) {
+  for (void* p : v) cudaFree(p);
+  v.clear();
+}
+
 template <typename T>
 T* DevAlloc(size_t count, std::vector<void*>& owner, uint64_t& bytes) {
   if (count == 0) return nullptr;
@@ -165,6 +170,10 @@ struct Lib {
   float4* guideRec = nullptr;
   uint32_t guideRecCap = 0;
   uint64_t guideBytes = 0;
+  // bdpt wavefront scratch, allocated with the first bdpt wave for its scene's vertex cap
+  BdptBuffers bdpt{};
+  std::vector<void*> bdptAllocs;
+  uint64_t bdptBytes = 0;
 };
 
 // Never destroyed: at process exit the worker thread may still be parked on
@@ -265,6 +274,124 @@ struct ProfSink {
     job->profKind.push_back(kind);
   }
 };
+
+// ---- bdpt ---------------------------------------------------------------------
+// Device bytes the bdpt scratch may take: the wave size follows from the
+// scene's vertex cap (2 subpaths x cap vertices + cap visibility rays a sample).
+constexpr uint64_t kBdptScratchBytes = 4ull << 30;
+
+int BdptCap(const DevScene& S) {
+  return S.maxDepth >= 0 ? std::min(kMaxBdptVertices, S.maxDepth + 2) : kMaxBdptVertices;
+}
+
+const BdptBuffers& EnsureBdpt(int cap) {
+  Lib& lib = L();
+  if (lib.bdpt.vert && (int)lib.bdpt.cap == cap) return lib.bdpt;
+  Check(cudaStreamSynchronize(lib.stream), "sync");
+  FreeAll(lib.bdptAllocs);
+  lib.used -= lib.bdptBytes;
+  lib.bdptBytes = 0;
+  uint64_t per = 2ull * cap * kBVertBytes + (uint64_t)cap * 3 * sizeof(float4) + 3 * sizeof(float4) + 8;
+  uint32_t nw = (uint32_t)std::min<uint64_t>(lib.maxPaths, std::max<uint64_t>(1024, kBdptScratchBytes / per));
+  BdptBuffers V{};
+  auto& o = lib.bdptAllocs;
+  uint64_t& b = lib.bdptBytes;
+  V.vert = reinterpret_cast<BVert*>(DevAlloc<uint8_t>(2ull * cap * nw * kBVertBytes, o, b));
+  V.walkA = DevAlloc<float4>(nw, o, b);
+  V.walkB = DevAlloc<float4>(nw, o, b);
+  V.fix = DevAlloc<float4>(nw, o, b);
+  V.nCam = DevAlloc<uint32_t>(nw, o, b);
+  V.nLight = DevAlloc<uint32_t>(nw, o, b);
+  V.shCap = (uint32_t)std::min<uint64_t>(0xffffffffu, (uint64_t)nw * cap);
+  V.shO = DevAlloc<float4>(V.shCap, o, b);
+  V.shD = DevAlloc<float4>(V.shCap, o, b);
+  V.shC = DevAlloc<float4>(V.shCap, o, b);
+  V.cap = (uint32_t)cap;
+  V.nw = nw;
+  lib.bdpt = V;
+  lib.used += b;
+  return lib.bdpt;
+}
+
+// Zeroes the wave counters; keeps the device-error word and, with keepMaxCam,
+// the longest-camera-subpath word.
+void ResetCounters(const PathBuffers& B, bool keepMaxCam, cudaStream_t st) {
+  size_t head = keepMaxCam ? (size_t)kMiscBase : (size_t)kMiscBase + 1;
+  Check(cudaMemsetAsync(B.counters, 0, head * sizeof(uint32_t), st), "cudaMemsetAsync");
+  Check(cudaMemsetAsync(B.counters + kMiscBase + 2, 0, (kCounterWords - kMiscBase - 2) * sizeof(uint32_t), st),
+        "cudaMemsetAsync");
+}
+
+// One subpath bounce loop: extend + walk per depth until the queue empties.
+uint64_t BdptWalks(const DevScene& S, const TraceTune& tu, uint32_t count, bool light, int cap, ProfSink& ps) {
+  Lib& lib = L();
+  const PathBuffers& B = lib.paths;
+  const BdptBuffers& V = lib.bdpt;
+  int grid = std::max(1, std::min(lib.sms * 8, (int)((count + 127) / 128)));
+  int tgrid = std::max(1, std::min(lib.sms * tu.blocksPerSm, (int)((count + 127) / 128)));
+  int iters = S.maxDepth >= 0 ? std::min(cap, S.maxDepth + 1) : cap;
+  uint64_t launches = 0;
+  for (int d = 0; d < iters; d++) {
+    cudaEvent_t a = nullptr;
+    ps.Begin(1, a);
+    Check(LaunchExtend(S, B, d, tgrid, lib.stream, nullptr, tu.refillBusy, tu.leafFrac8), "extend");
+    ps.End(1, a);
+    ps.Begin(2, a);
+    Check(LaunchBdptWalk(S, B, V, d, light, grid, lib.stream), "bdpt walk");
+    ps.End(2, a);
+    launches += 2;
+    if (S.maxDepth < 0 && (d % 8) == 7) {
+      uint32_t next = 0;
+      Check(cudaMemcpyAsync(&next, B.counters + d + 1, sizeof(uint32_t), cudaMemcpyDeviceToHost, lib.stream), "copy");
+      Check(cudaStreamSynchronize(lib.stream), "sync");
+      if (next == 0) break;
+    }
+  }
+  return launches;
+}
+
+// The bdpt stages for `w.count` (<= the scratch's wave size) pixel samples:
+// film (splats and valid samples) and / or per-sample camera-side radiance `out`.
+uint64_t RunBdptWave(const DevScene& S, const TraceTune& tu, const WaveParams& w, const FilmView& film, float* out,
+                     ProfSink& ps) {
+  Lib& lib = L();
+  const int cap = BdptCap(S);
+  const BdptBuffers& V = EnsureBdpt(cap);
+  const PathBuffers& B = lib.paths;
+  const uint32_t count = w.count;
+  uint64_t launches = 0;
+  cudaEvent_t a = nullptr;
+  ResetCounters(B, false, lib.stream);
+  ps.Begin(0, a);
+  Check(LaunchBdptCamera(S, B, V, w, lib.stream), "bdpt camera");
+  ps.End(0, a);
+  launches += 1 + BdptWalks(S, tu, count, false, cap, ps);
+  ResetCounters(B, true, lib.stream);
+  ps.Begin(0, a);
+  Check(LaunchBdptLight(S, B, V, count, lib.stream), "bdpt light");
+  ps.End(0, a);
+  launches += 1 + BdptWalks(S, tu, count, true, cap, ps);
+  Check(LaunchBdptLightFix(S, V, count, lib.stream), "bdpt light fix-up");
+  uint32_t maxCam = 0;
+  Check(cudaMemcpyAsync(&maxCam, B.counters + kMiscBase, sizeof(uint32_t), cudaMemcpyDeviceToHost, lib.stream), "copy");
+  Check(cudaStreamSynchronize(lib.stream), "sync");
+  launches += 1;
+  int grid = lib.sms * 8;
+  int tgrid = std::max(1, std::min(lib.sms * tu.blocksPerSm, (int)((count + 127) / 128)));
+  for (int t = 1; t <= (int)maxCam && t <= cap; t++) {
+    ps.Begin(2, a);
+    Check(LaunchBdptConnect(S, B, V, count, t, film.accum != nullptr, grid, lib.stream), "bdpt connect");
+    ps.End(2, a);
+    ps.Begin(3, a);
+    Check(LaunchBdptShadow(S, B, V, t, film.accum, tgrid, lib.stream, tu.refillBusy, tu.leafFrac8), "bdpt shadow");
+    ps.End(3, a);
+    launches += 2;
+  }
+  ps.Begin(4, a);
+  Check(LaunchBdptAccumulate(B, film, count, out, lib.stream), "bdpt accumulate");
+  ps.End(4, a);
+  return launches + 1;
+}
 
 // Launches the bounce loop for `count` generated paths. Returns kernels launched.
 uint64_t LaunchBounces(const DevScene& S, const TraceTune& tu, uint32_t count, ProfSink& ps,
@@ -505,27 +632,20 @@ void RunWaveParticle(rad_job* j) {
   j->launched += k;
 }
 
-// bdpt jobs: one thread per pixel sample over the wave's pixels (BDPT::Render,
-// bdpt.cpp:261-305), camera-side radiance and splats added into the film.
+// bdpt jobs (BDPT::Render, bdpt.cpp:261-305): the wavefront stages over the
+// job's pixels, as many consecutive samples per wave as the scratch holds.
 void RunWaveBdpt(rad_job* j) {
-  Lib& lib = L();
   const DevScene& S = j->scene->dev;
-  uint64_t npix = (uint64_t)S.cam.width * S.cam.height;
-  const uint32_t spw = WaveSamples(j);
-  const uint32_t k = std::min(spw, j->spp - j->nextSample);
+  const uint64_t npix = (uint64_t)S.cam.width * S.cam.height;
+  const uint32_t nw = EnsureBdpt(BdptCap(S)).nw;
+  const uint32_t k = npix * 2 > nw ? 1u : (uint32_t)std::min<uint64_t>(j->spp - j->nextSample, nw / npix);
   FilmView film{j->accum, S.cam.width, S.cam.height, j->dStats};
   ProfSink ps{j};
-  int grid = lib.sms * 4;
-  for (uint64_t p0 = 0; p0 < npix; p0 += lib.maxPaths) {
-    uint32_t count = (uint32_t)std::min<uint64_t>(lib.maxPaths, npix - p0) * k;
+  const uint64_t chunk = nw / k;
+  for (uint64_t p0 = 0; p0 < npix; p0 += chunk) {
+    uint32_t count = (uint32_t)std::min<uint64_t>(chunk, npix - p0) * k;
     WaveParams w{(uint32_t)p0, count, j->first + j->nextSample, j->seed, nullptr, nullptr, nullptr, k};
-    cudaEvent_t a = nullptr;
-    ps.Begin(5, a);
-    Check(LaunchBdpt(S, film, w, nullptr, lib.paths.counters + kMiscBase + 1, std::max(1, std::min(grid, (int)((count + 127) / 128))),
-                     lib.stream),
-          "bdpt");
-    ps.End(5, a);
-    j->stats.kernel_launches += 1;
+    j->stats.kernel_launches += RunBdptWave(S, j->scene->tune, w, film, nullptr, ps);
   }
   j->nextSample += k;
   j->launched += npix * k;
@@ -892,11 +1012,6 @@ uint64_t SceneUpload(const HostScene& hs, rad_scene* sc) {
   return b;
 }
 
-void FreeAll(std::vector<void*>& v) {
-  for (void* p : v) cudaFree(p);
-  v.clear();
-}
-
 std::string ReadFile(const std::string& path) {
   std::ifstream in(path, std::ios::binary);
   if (!in) throw IoError("cannot open " + path);
@@ -956,6 +1071,10 @@ int rad_shutdown(void) {
     lib.guideRec = nullptr;
     lib.guideRecCap = 0;
     lib.guideBytes = 0;
+    FreeAll(lib.bdptAllocs);
+    lib.used -= lib.bdptBytes;
+    lib.bdptBytes = 0;
+    lib.bdpt = BdptBuffers{};
     if (lib.hCounters) cudaFreeHost(lib.hCounters);
     lib.hCounters = nullptr;
     for (cudaEvent_t e : lib.evPool) cudaEventDestroy(e);
@@ -1331,15 +1450,13 @@ int rad_render_samples(rad_scene* scene, const uint32_t* pixels, const uint32_t*
     Check(cudaMemcpyAsync(ds.p, samples, 4 * n, cudaMemcpyHostToDevice, lib.stream), "copy");
     uint32_t zero = 0;
     Check(cudaMemcpyAsync(lib.paths.counters + kMiscBase + 1, &zero, 4, cudaMemcpyHostToDevice, lib.stream), "copy");
-    for (int64_t b = 0; b < n; b += lib.maxPaths) {
-      uint32_t count = (uint32_t)std::min<int64_t>(lib.maxPaths, n - b);
+    const int64_t step = scene->dev.isBdpt ? (int64_t)EnsureBdpt(BdptCap(scene->dev)).nw : (int64_t)lib.maxPaths;
+    for (int64_t b = 0; b < n; b += step) {
+      uint32_t count = (uint32_t)std::min<int64_t>(step, n - b);
       WaveParams w{0, count, 0, seed, dp.p + b, ds.p + b};
       ProfSink ps{nullptr};
       if (scene->dev.isBdpt) {
-        int grid = std::max(1, std::min(lib.sms * 4, (int)((count + 127) / 128)));
-        Check(LaunchBdpt(scene->dev, FilmView{}, w, dout.p + 3 * b, lib.paths.counters + kMiscBase + 1, grid,
-                         lib.stream),
-              "bdpt");
+        RunBdptWave(scene->dev, scene->tune, w, FilmView{}, dout.p + 3 * b, ps);
         continue;
       }
       Check(LaunchGenerate(scene->dev, lib.paths, w, lib.stream), "generate");

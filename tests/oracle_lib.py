@@ -39,7 +39,9 @@ def lib():
         L.orc_bsdf_eval.argtypes = [ctypes.c_char_p, P, P, ctypes.c_int64, P, P]
         L.orc_texture_eval.argtypes = [P, ctypes.c_uint32, P, P, ctypes.c_int64, P]
         L.orc_render_particle.argtypes = [P, ctypes.c_uint64, ctypes.c_uint64, ctypes.c_uint64, ctypes.c_uint32, P]
-        L.orc_render_bdpt.argtypes = [P, ctypes.c_int, ctypes.c_int, ctypes.c_uint32, ctypes.c_int, P]
+        L.orc_render_bdpt.argtypes = [P, ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_int,
+                                      ctypes.c_uint32, ctypes.c_int, P]
+        L.orc_render_bdpt.restype = ctypes.c_int64
         L.orc_texture_count.argtypes = [P]
         L.orc_image_load.argtypes = [ctypes.c_char_p, ctypes.c_char_p, P, P, ctypes.c_int64]
         L.orc_bsdf_sample.argtypes = [ctypes.c_char_p, P, P, ctypes.c_int64, P, P, P, P, P]
@@ -128,13 +130,16 @@ class OracleScene:
             raise RuntimeError(lib().orc_last_error().decode())
         return film
 
-    def render_bdpt(self, samples=None, seed=None, threads=0):
-        """bdpt film: per pixel (valid camera-side samples + t = 1 splats landing there) / spp."""
+    def render_bdpt(self, samples=None, seed=None, threads=0, rows=None, count=False):
+        """bdpt film: per pixel (valid camera-side samples + t = 1 splats landing there) / spp.
+        rows = (row0, row1, step) renders a subset of the pixels; count=True also returns the samples run."""
         s0, s1 = samples if samples is not None else (0, self.spp)
+        r0, r1, rs = rows if rows is not None else (0, self.height, 1)
         film = np.zeros((self.height, self.width, 3), np.float32)
-        if lib().orc_render_bdpt(self.h, s0, s1, self.seed if seed is None else seed, threads, _p(film)) != 0:
+        n = lib().orc_render_bdpt(self.h, r0, r1, rs, s0, s1, self.seed if seed is None else seed, threads, _p(film))
+        if n < 0:
             raise RuntimeError(lib().orc_last_error().decode())
-        return film
+        return (film, n) if count else film
 
     def texture_count(self):
         return lib().orc_texture_count(self.h)
