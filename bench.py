@@ -414,7 +414,11 @@ def run_renderers(args, world, rank, local):
             job.close()
             r = {"samples_per_s": st["samples"] / (st["gpu_ms"] / 1000.0), "gpu_ms": st["gpu_ms"],
                  "samples": st["samples"], "gpu_launches": st["kernel_launches"],
-                 "unit": "light paths/s" if name == "particle_tracer" else "samples/s"}
+                 "unit": "light paths/s" if name == "particle_tracer" else "samples/s",
+                 # profiled stage times (events around every launch); bdpt: generate = subpath starts,
+                 # extend = closest-hit bounces, shade = walks + connections, shadow = visibility rays
+                 "kernel_ms": {k: round(st["ms_" + k], 3) for k in
+                               ("generate", "extend", "shade", "shadow", "accumulate", "volpath")}}
             if rank == 0 and not args.no_cpu:
                 sys.path.insert(0, os.path.join(ROOT, "tests"))
                 import oracle_lib

@@ -152,22 +152,44 @@ __global__ void __launch_bounds__(kBdptBlock) KBdptWalk(DevScene S, PathBuffers 
   }
 }
 
+RD uint32_t SortKey(const BdptBuffers& V, uint32_t p) { return V.nCam[p] * (V.cap + 1u) + V.nLight[p]; }
+
 __global__ void __launch_bounds__(kBdptBlock) KBdptLightFix(DevScene S, BdptBuffers V, uint32_t count) {
   for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < count; i += gridDim.x * blockDim.x) {
     uint32_t n = V.nLight[i];
+    atomicAdd(V.keyFill + SortKey(V, i), 1u);
     if (n == 0u) continue;
     float4 f = V.fix[i];
     LightPathFinish(S, LightPathOf(V, i), (int)n, LightFix{V3{f.x, f.y, f.z}, f.w});
   }
 }
 
+// Exclusive scan of the key counts (at most 65^2 keys: one thread suffices),
+// which become the scatter cursors.
+__global__ void KBdptKeyScan(BdptBuffers V) {
+  const uint32_t nk = (V.cap + 1u) * (V.cap + 1u);
+  uint32_t acc = 0;
+  for (uint32_t k = 0; k < nk; k++) {
+    uint32_t c = V.keyFill[k];
+    V.keyStart[k] = acc;
+    V.keyFill[k] = acc;
+    acc += c;
+  }
+  V.keyStart[nk] = acc;
+}
+
+__global__ void __launch_bounds__(kBdptBlock) KBdptKeyScatter(BdptBuffers V, uint32_t count) {
+  for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < count; i += gridDim.x * blockDim.x)
+    V.order[atomicAdd(V.keyFill + SortKey(V, i), 1u)] = i;
+}
+
 __global__ void __launch_bounds__(kBdptBlock)
     KBdptConnect(DevScene S, PathBuffers B, BdptBuffers V, uint32_t count, int t, bool splats) {
   uint32_t* nsh = B.counters + kShadowBase + (t - 1);
   uint32_t* err = B.counters + kMiscBase + 1;
-  for (uint32_t p = blockIdx.x * blockDim.x + threadIdx.x; p < count; p += gridDim.x * blockDim.x) {
-    const int nc = (int)V.nCam[p];
-    if (nc < t) continue;
+  const uint32_t first = V.keyStart[(uint32_t)t * (V.cap + 1u)];  // samples with nc < t come first
+  for (uint32_t j = first + blockIdx.x * blockDim.x + threadIdx.x; j < count; j += gridDim.x * blockDim.x) {
+    const uint32_t p = V.order[j];
     const int nl = (int)V.nLight[p];
     Pcg32 rng = LoadRng(B, p);
     VPath cam = CamPath(V, p), lig = LightPathOf(V, p);
@@ -329,6 +351,8 @@ cudaError_t LaunchBdptWalk(const DevScene& S, const PathBuffers& B, const BdptBu
 cudaError_t LaunchBdptLightFix(const DevScene& S, const BdptBuffers& V, uint32_t count, cudaStream_t st) {
   if (count == 0) return cudaSuccess;
   KBdptLightFix<<<GridFor(count, 1 << 16), kBdptBlock, 0, st>>>(S, V, count);
+  KBdptKeyScan<<<1, 1, 0, st>>>(V);
+  KBdptKeyScatter<<<GridFor(count, 1 << 16), kBdptBlock, 0, st>>>(V, count);
   return cudaGetLastError();
 }
 cudaError_t LaunchBdptConnect(const DevScene& S, const PathBuffers& B, const BdptBuffers& V, uint32_t count, int t,

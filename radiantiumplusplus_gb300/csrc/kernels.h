@@ -118,6 +118,11 @@ struct BdptBuffers {
   uint32_t* nCam;      // per sample: camera / light subpath vertex counts
   uint32_t* nLight;
   float4 *shO, *shD, *shC;  // visibility rays of one connection round: origin + tmax, direction + tag, contribution
+  // samples ordered by (camera, light) subpath length, so that a connection round runs over the
+  // suffix of samples with a long enough camera subpath, neighbours looping over as many light vertices
+  uint32_t* order;     // nw sample slots
+  uint32_t* keyStart;  // (cap + 1)^2 + 1: first slot of each key (exclusive scan of the key counts)
+  uint32_t* keyFill;   // (cap + 1)^2: per-key counts, then scatter cursors
   uint32_t cap, nw, shCap;
 };
 // Camera subpaths: jittered camera rays of the wave's samples into queue 0.
@@ -130,7 +135,8 @@ cudaError_t LaunchBdptLight(const DevScene& S, const PathBuffers& B, const BdptB
 // Longest camera subpath of the wave: B.counters[kMiscBase] (atomic max).
 cudaError_t LaunchBdptWalk(const DevScene& S, const PathBuffers& B, const BdptBuffers& V, int depth, bool light,
                            int grid, cudaStream_t st);
-// Infinite-light fix-up of the light subpaths.
+// Infinite-light fix-up of the light subpaths, then the samples' order by subpath lengths
+// (V.keyFill zeroed beforehand).
 cudaError_t LaunchBdptLightFix(const DevScene& S, const BdptBuffers& V, uint32_t count, cudaStream_t st);
 // The connections of camera vertex t - 1 of every sample (all light vertices): direct contributions
 // into B.L, visibility rays into V.sh* (count in B.counters[kShadowBase + t - 1]); splats only with `splats`.

@@ -291,7 +291,7 @@ const BdptBuffers& EnsureBdpt(int cap) {
   FreeAll(lib.bdptAllocs);
   lib.used -= lib.bdptBytes;
   lib.bdptBytes = 0;
-  uint64_t per = 2ull * cap * kBVertBytes + (uint64_t)cap * 3 * sizeof(float4) + 3 * sizeof(float4) + 8;
+  uint64_t per = 2ull * cap * kBVertBytes + (uint64_t)cap * 3 * sizeof(float4) + 3 * sizeof(float4) + 12;
   uint32_t nw = (uint32_t)std::min<uint64_t>(lib.maxPaths, std::max<uint64_t>(1024, kBdptScratchBytes / per));
   BdptBuffers V{};
   auto& o = lib.bdptAllocs;
@@ -306,6 +306,9 @@ const BdptBuffers& EnsureBdpt(int cap) {
   V.shO = DevAlloc<float4>(V.shCap, o, b);
   V.shD = DevAlloc<float4>(V.shCap, o, b);
   V.shC = DevAlloc<float4>(V.shCap, o, b);
+  V.order = DevAlloc<uint32_t>(nw, o, b);
+  V.keyStart = DevAlloc<uint32_t>((size_t)(cap + 1) * (cap + 1) + 1, o, b);
+  V.keyFill = DevAlloc<uint32_t>((size_t)(cap + 1) * (cap + 1), o, b);
   V.cap = (uint32_t)cap;
   V.nw = nw;
   lib.bdpt = V;
@@ -371,11 +374,12 @@ uint64_t RunBdptWave(const DevScene& S, const TraceTune& tu, const WaveParams& w
   Check(LaunchBdptLight(S, B, V, count, lib.stream), "bdpt light");
   ps.End(0, a);
   launches += 1 + BdptWalks(S, tu, count, true, cap, ps);
+  Check(cudaMemsetAsync(V.keyFill, 0, (size_t)(cap + 1) * (cap + 1) * sizeof(uint32_t), lib.stream), "cudaMemsetAsync");
   Check(LaunchBdptLightFix(S, V, count, lib.stream), "bdpt light fix-up");
   uint32_t maxCam = 0;
   Check(cudaMemcpyAsync(&maxCam, B.counters + kMiscBase, sizeof(uint32_t), cudaMemcpyDeviceToHost, lib.stream), "copy");
   Check(cudaStreamSynchronize(lib.stream), "sync");
-  launches += 1;
+  launches += 3;
   int grid = lib.sms * 8;
   int tgrid = std::max(1, std::min(lib.sms * tu.blocksPerSm, (int)((count + 127) / 128)));
   for (int t = 1; t <= (int)maxCam && t <= cap; t++) {
