@@ -208,8 +208,6 @@ struct WalkState {
   int n;  // vertices so far
 };
 
-RD bool IsBlack(V3 v) { return v.x == 0.f && v.y == 0.f && v.z == 0.f; }
-
 // Top of RandomWalk's loop for bounce `depth` (bdpt.cpp:418-428): a black
 // throughput ends the walk, then Russian roulette from rr_depth.
 RD bool WalkContinue(const DevScene& S, Pcg32& rng, WalkState& w, int depth) {
@@ -595,18 +593,6 @@ RDN bool ConnectBdpt(const DevScene& S, Pcg32& rng, VPath lightV, VPath camV, in
   if (IsBlack(l)) return false;
   float mis = MISWeight(S, lightV, camV, sampled, s, t);
   o.c = l * mis;
-  return true;
-}
-
-// The visibility ray of Scene::IsOcclude (scene.cpp:53-63) from (P, N) to
-// target: false when the points are closer than the shadow epsilon (occluded).
-RD bool ShadowRay(V3 P, V3 N, V3 target, V3& o, V3& d, float& tmax) {
-  o = OffsetP(P, N, target - P);
-  d = target - o;
-  float dist = norm(d);
-  if (dist < kShadowEps) return false;
-  d = d / dist;
-  tmax = dist * (1.f - kShadowEps);
   return true;
 }
 

@@ -148,8 +148,13 @@ cudaError_t LaunchBdptShadow(const DevScene& S, const PathBuffers& B, const Bdpt
 // Per sample: camera-side radiance into `out` (n x 3) and / or valid samples into the film.
 cudaError_t LaunchBdptAccumulate(const PathBuffers& B, const FilmView& film, uint32_t count, float* out,
                                  cudaStream_t st);
-cudaError_t LaunchParticle(const DevScene& S, const FilmView& film, const ParticleParams& pp, uint32_t* err, int grid,
-                           cudaStream_t st);
+// Renderer "particle_tracer" (k_light.cu): light path starts (emitter connections into
+// visibility round 0 of B.sh*, emitted rays into queue 0) and one bounce per launch after
+// LaunchExtend (camera connections into round d + 1); the rounds are traced by LaunchBdptShadow.
+cudaError_t LaunchParticleStart(const DevScene& S, const PathBuffers& B, const ParticleParams& pp,
+                                unsigned long long* stats, cudaStream_t st);
+cudaError_t LaunchParticleBounce(const DevScene& S, const PathBuffers& B, int d, float sampleScale, int grid,
+                                 cudaStream_t st);
 // renderer "ao": for every path of bounce 0 with a hit, one cosine-sampled visibility ray
 cudaError_t LaunchShadeAO(const DevScene& S, const PathBuffers& B, int grid, cudaStream_t st);
 cudaError_t LaunchShadow(const DevScene& S, const PathBuffers& B, int depth, int grid, cudaStream_t st,

@@ -129,6 +129,8 @@ static_assert(sizeof(LightRec) == 384, "LightRec size");
 
 // bdpt: vertices of one subpath at most (camera or light vertex included)
 constexpr int kMaxBdptVertices = 64;
+// particle_tracer: bounces of one light path at most (max_depth -1 is capped like camera paths)
+constexpr int kMaxLightBounces = 256;
 
 // ---------------------------------------------------------------- media
 enum MediumKind : uint32_t { MED_HOMOGENEOUS = 0, MED_HETEROGENEOUS = 1 };

@@ -617,21 +617,57 @@ void RunWaveGraph(rad_job* j) {
 }
 
 // particle_tracer jobs: the next batch of light paths (ParticleTracer::Render,
-// particle_tracer.cpp:39-83; one "sample" = one light path for the whole film).
+// particle_tracer.cpp:39-83; one "sample" = one light path for the whole film),
+// as a wavefront: starts, then per bounce closest hit, bounce and the round's
+// camera-connection visibility rays.
 void RunWaveParticle(rad_job* j) {
   Lib& lib = L();
   const DevScene& S = j->scene->dev;
+  const TraceTune& tu = j->scene->tune;
+  const PathBuffers& B = lib.paths;
   uint64_t npix = (uint64_t)S.cam.width * S.cam.height;
   const uint32_t k = std::min<uint32_t>(lib.maxPaths, j->spp - j->nextSample);
-  ParticleParams pp{(uint64_t)j->first + j->nextSample, k, j->seed, (float)npix / (float)j->spp};
-  FilmView film{j->accum, S.cam.width, S.cam.height, j->dStats};
+  const float scale = (float)npix / (float)j->spp;
+  ParticleParams pp{(uint64_t)j->first + j->nextSample, k, j->seed, scale};
+  BdptBuffers sh{};  // the visibility rays of a round live in the path state's shadow records
+  sh.shO = B.shO;
+  sh.shD = B.shD;
+  sh.shC = B.shC;
+  sh.shCap = B.capacity;
   ProfSink ps{j};
   cudaEvent_t a = nullptr;
-  ps.Begin(5, a);
   int grid = std::max(1, std::min(lib.sms * 8, (int)((k + 127) / 128)));
-  Check(LaunchParticle(S, film, pp, lib.paths.counters + kMiscBase + 1, grid, lib.stream), "particle_tracer");
-  ps.End(5, a);
-  j->stats.kernel_launches += 1;
+  int tgrid = std::max(1, std::min(lib.sms * tu.blocksPerSm, (int)((k + 127) / 128)));
+  ResetCounters(B, false, lib.stream);
+  ps.Begin(0, a);
+  Check(LaunchParticleStart(S, B, pp, j->dStats, lib.stream), "particle start");
+  ps.End(0, a);
+  ps.Begin(3, a);
+  Check(LaunchBdptShadow(S, B, sh, 1, j->accum, tgrid, lib.stream, tu.refillBusy, tu.leafFrac8), "particle splats");
+  ps.End(3, a);
+  uint64_t launches = 2;
+  // bounce d tests depth d + 1 against max_depth before it does anything
+  const int iters = S.maxDepth >= 0 ? std::min(kMaxLightBounces, std::max(0, S.maxDepth - 1)) : kMaxLightBounces;
+  for (int d = 0; d < iters; d++) {
+    ps.Begin(1, a);
+    Check(LaunchExtend(S, B, d, tgrid, lib.stream, nullptr, tu.refillBusy, tu.leafFrac8), "extend");
+    ps.End(1, a);
+    ps.Begin(2, a);
+    Check(LaunchParticleBounce(S, B, d, scale, grid, lib.stream), "particle bounce");
+    ps.End(2, a);
+    ps.Begin(3, a);
+    Check(LaunchBdptShadow(S, B, sh, d + 2, j->accum, tgrid, lib.stream, tu.refillBusy, tu.leafFrac8),
+          "particle splats");
+    ps.End(3, a);
+    launches += 3;
+    if (S.maxDepth < 0 && (d % 8) == 7) {
+      uint32_t next = 0;
+      Check(cudaMemcpyAsync(&next, B.counters + d + 1, sizeof(uint32_t), cudaMemcpyDeviceToHost, lib.stream), "copy");
+      Check(cudaStreamSynchronize(lib.stream), "sync");
+      if (next == 0) break;
+    }
+  }
+  j->stats.kernel_launches += launches;
   j->nextSample += k;
   j->launched += k;
 }
