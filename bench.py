@@ -430,10 +430,9 @@ def run_renderers(args, world, rank, local):
                                          count=True)
                     what = "rows 0..%d step %d at 1 spp" % (H, args.bdpt_cpu_row_step)
                 elif name == "particle_tracer":
-                    n = 200_000
-                    o.render_particle(spp=npix, first=0, count=n)  # one thread
-                    threads = 1
-                    what = "%d light paths of a %d-path frame, one thread" % (n, npix)
+                    n = 2_000_000
+                    o.render_particle(spp=npix, first=0, count=n, threads=threads)
+                    what = "%d light paths of a %d-path frame" % (n, npix)
                 else:
                     _, cs = o.render(rows=(0, H, 16), samples=(0, 1), threads=threads)
                     n = int(cs[2])

@@ -696,21 +696,36 @@ int orc_render(void* sp, int row0, int row1, int rowStep, int s0, int s1, int se
 
 // particle_tracer: light paths [first, first + count) of `spp` splatted into
 // film (W x H x 3, accumulated onto its contents).
-int orc_render_particle(void* sp, uint64_t first, uint64_t count, uint64_t spp, uint32_t seed, float* film) {
+// `threads` workers (0: all host threads) take contiguous ranges of light paths.
+int orc_render_particle(void* sp, uint64_t first, uint64_t count, uint64_t spp, uint32_t seed, int threads,
+                        float* film) {
   Scene& S = *(Scene*)sp;
-  try {
-    size_t npix = (size_t)S.camera.width * S.camera.height;
-    std::vector<Spectrum> image(npix, Spectrum(0));
-    Float sampleScale = npix / ((Float)spp);
-    for (uint64_t i = 0; i < count; i++) ParticleSample(S, first + i, seed, sampleScale, image);
-    for (size_t p = 0; p < npix; p++) {
-      film[3 * p] += image[p].x;
-      film[3 * p + 1] += image[p].y;
-      film[3 * p + 2] += image[p].z;
+  size_t npix = (size_t)S.camera.width * S.camera.height;
+  int nt = threads > 0 ? threads : (int)std::thread::hardware_concurrency();
+  if (nt < 1) nt = 1;
+  std::vector<std::vector<Spectrum>> images(nt, std::vector<Spectrum>(npix, Spectrum(0)));
+  Float sampleScale = npix / ((Float)spp);
+  std::atomic<bool> failed{false};
+  auto worker = [&](int w) {
+    try {
+      uint64_t a = count * (uint64_t)w / (uint64_t)nt, b = count * (uint64_t)(w + 1) / (uint64_t)nt;
+      for (uint64_t i = a; i < b; i++) ParticleSample(S, first + i, seed, sampleScale, images[w]);
+    } catch (const std::exception& e) {
+      g_err = e.what();
+      failed = true;
     }
-  } catch (const std::exception& e) {
-    g_err = e.what();
-    return -1;
+  };
+  std::vector<std::thread> ts;
+  for (int i = 1; i < nt; i++) ts.emplace_back(worker, i);
+  worker(0);
+  for (auto& t : ts) t.join();
+  if (failed) return -1;
+  for (size_t p = 0; p < npix; p++) {
+    for (int w = 0; w < nt; w++) {
+      film[3 * p] += images[w][p].x;
+      film[3 * p + 1] += images[w][p].y;
+      film[3 * p + 2] += images[w][p].z;
+    }
   }
   return 0;
 }

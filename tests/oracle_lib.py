@@ -38,7 +38,8 @@ def lib():
         L.orc_render_samples.argtypes = [P, P, P, ctypes.c_int64, ctypes.c_uint32, P]
         L.orc_bsdf_eval.argtypes = [ctypes.c_char_p, P, P, ctypes.c_int64, P, P]
         L.orc_texture_eval.argtypes = [P, ctypes.c_uint32, P, P, ctypes.c_int64, P]
-        L.orc_render_particle.argtypes = [P, ctypes.c_uint64, ctypes.c_uint64, ctypes.c_uint64, ctypes.c_uint32, P]
+        L.orc_render_particle.argtypes = [P, ctypes.c_uint64, ctypes.c_uint64, ctypes.c_uint64, ctypes.c_uint32,
+                                          ctypes.c_int, P]
         L.orc_render_bdpt.argtypes = [P, ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_int,
                                       ctypes.c_uint32, ctypes.c_int, P]
         L.orc_render_bdpt.restype = ctypes.c_int64
@@ -121,12 +122,14 @@ class OracleScene:
             raise RuntimeError(lib().orc_last_error().decode())
         return film, stats
 
-    def render_particle(self, spp=None, first=0, count=None, seed=None):
-        """particle_tracer film: light paths [first, first + count) of a job of `spp` light paths."""
+    def render_particle(self, spp=None, first=0, count=None, seed=None, threads=1):
+        """particle_tracer film: light paths [first, first + count) of a job of `spp` light paths
+        (threads 0: all host threads; the sum order then depends on the split)."""
         spp = self.spp if spp is None else spp
         count = spp - first if count is None else count
         film = np.zeros((self.height, self.width, 3), np.float32)
-        if lib().orc_render_particle(self.h, first, count, spp, self.seed if seed is None else seed, _p(film)) != 0:
+        if lib().orc_render_particle(self.h, first, count, spp, self.seed if seed is None else seed, threads,
+                                     _p(film)) != 0:
             raise RuntimeError(lib().orc_last_error().decode())
         return film
 

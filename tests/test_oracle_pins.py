@@ -327,7 +327,7 @@ def test_particle_tracer_agrees_with_path_tracer(oracle, scene_dir):
     sc["sampler"]["sample_count"] = 200000
     _, text, d = write(scene_dir, "pt_particle", sc)
     o = oracle.OracleScene(text, d)
-    film = o.render_particle()
+    film = o.render_particle(threads=0)
     o.close()
     m, r = film.reshape(-1, 3).mean(0), ref.reshape(-1, 3).mean(0)
     assert np.all(np.abs(m - r) < 0.04 * r), (m, r)
