@@ -385,11 +385,12 @@ def run_renderers(args, world, rank, local):
     from radiantiumplusplus_gb300 import scenes
     torch.cuda.set_device(local)
     rad.init({"device": local})
-    npix = W * H
+    Wr, Hr = args.renderers_res
+    npix = Wr * Hr
     out = {}
     clk = None
     with tempfile.TemporaryDirectory(prefix="rad_bench_r_") as tmp:
-        sc, assets = scenes.many_spheres(n_spheres=10000, width=W, height=H, spp=1, max_depth=MAX_DEPTH, seed=2)
+        sc, assets = scenes.many_spheres(n_spheres=10000, width=Wr, height=Hr, spp=1, max_depth=MAX_DEPTH, seed=2)
         for name, renderer in (("bdpt", {"type": "bdpt", "max_depth": args.bdpt_depth}),
                                ("particle_tracer", {"type": "particle_tracer", "max_depth": MAX_DEPTH}),
                                ("ao", {"type": "ao"})):
@@ -426,17 +427,17 @@ def run_renderers(args, world, rank, local):
                 threads = os.cpu_count() or 1
                 t0 = time.perf_counter()
                 if name == "bdpt":
-                    _, n = o.render_bdpt(rows=(0, H, args.bdpt_cpu_row_step), samples=(0, 1), threads=threads,
+                    _, n = o.render_bdpt(rows=(0, Hr, args.bdpt_cpu_row_step), samples=(0, 1), threads=threads,
                                          count=True)
-                    what = "rows 0..%d step %d at 1 spp" % (H, args.bdpt_cpu_row_step)
+                    what = "rows 0..%d step %d at 1 spp" % (Hr, args.bdpt_cpu_row_step)
                 elif name == "particle_tracer":
                     n = 2_000_000
                     o.render_particle(spp=npix, first=0, count=n, threads=threads)
                     what = "%d light paths of a %d-path frame" % (n, npix)
                 else:
-                    _, cs = o.render(rows=(0, H, 16), samples=(0, 1), threads=threads)
+                    _, cs = o.render(rows=(0, Hr, 16), samples=(0, 1), threads=threads)
                     n = int(cs[2])
-                    what = "rows 0..%d step 16 at 1 spp" % H
+                    what = "rows 0..%d step 16 at 1 spp" % Hr
                 dt = time.perf_counter() - t0
                 r["cpu_baseline"] = {"value": n / dt, "unit": r["unit"], "cores": threads, "kind": "port",
                                      "sample": "%s (%d, %.1f s)" % (what, n, dt)}
@@ -444,12 +445,12 @@ def run_renderers(args, world, rank, local):
             scene.close()
             out[name] = r
     b = out["bdpt"]
-    line = {"metric": "samples/s (bdpt, many-spheres 1920x1080, depth %d)" % args.bdpt_depth,
+    line = {"metric": "samples/s (bdpt, many-spheres %dx%d, depth %d)" % (Wr, Hr, args.bdpt_depth),
             "value": b["samples_per_s"], "unit": "samples/s", "n_gpus": 1, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": b["gpu_ms"] / args.steps, "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded generator, no dataset)",
-            "config": {"workload": "many_spheres_1080p_renderers", "spheres": 10000, "triangles": 3200000,
-                       "width": W, "height": H, "bdpt_max_depth": args.bdpt_depth, "bdpt_rr_depth": 5,
+            "config": {"workload": "many_spheres_renderers", "spheres": 10000, "triangles": 3200000,
+                       "width": Wr, "height": Hr, "bdpt_max_depth": args.bdpt_depth, "bdpt_rr_depth": 5,
                        "particle_max_depth": MAX_DEPTH, "l2": "inputs larger than L2: resident scene > 129 MB"},
             "gpu_launches": b["gpu_launches"], "clocks": clk, "renderers": out}
     if "cpu_baseline" in b:
@@ -619,6 +620,7 @@ def main():
     ap.add_argument("--workload", default="many_spheres",
                     choices=["many_spheres", "volume", "serving", "guided", "renderers"])
     ap.add_argument("--bdpt-depth", type=int, default=MAX_DEPTH, help="renderers: bdpt max_depth")
+    ap.add_argument("--renderers-res", type=int, nargs=2, default=[W, H], help="renderers: frame size")
     ap.add_argument("--bdpt-cpu-row-step", type=int, default=8, help="renderers: oracle bdpt row sample")
     ap.add_argument("--guided-res", type=int, nargs=2, default=[1920, 1080])
     ap.add_argument("--guided-spheres", type=int, default=10000)
