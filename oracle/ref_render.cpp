@@ -54,6 +54,7 @@ Spectrum PathLi(const Scene& S, const Ray& ray0, const RayDiff& diff0, Pcg32& rn
         DirectionSample dsr;
         dsr.P = si.P;
         dsr.N = si.Shading.N;
+        dsr.UV = si.UV;
         V3 rel = si.P - prevP;
         dsr.Dist = norm(rel);
         dsr.Dir = si.IsValid() ? rel / dsr.Dist : -si.Wi;
@@ -342,6 +343,7 @@ Spectrum VolPathLi(const Scene& S, const Ray& ray0, Pcg32& rng) {
           DirectionSample dsr;
           dsr.P = si.P;
           dsr.N = si.Shading.N;
+          dsr.UV = si.UV;
           V3 rel = si.P - prevP;
           dsr.Dist = norm(rel);
           dsr.Dir = si.IsValid() ? rel / dsr.Dist : -si.Wi;
@@ -458,12 +460,13 @@ static void ParticleSample(const Scene& S, uint64_t id, uint32_t seed, Float sam
         lightPdf *= r.first.Pdf > 0 ? (r.first.Pdf * Sqr(r.first.Dist)) : 0;
         si.P = r.first.P;
         si.N = r.first.N;
-      } else {
-        PositionSample psr = S.shapes[L.shape].SamplePosition(rng.Next2D());
-        lightPdf *= psr.Pdf;
-        si.P = psr.P;
-        si.N = psr.N;
-        li = L.radiance;
+      } else {  // Light::SamplePosition, then Eval(SurfaceInteraction(psr))
+        auto pp = S.LightSamplePosition(index, rng.Next2D());
+        lightPdf *= pp.second;
+        si.P = pp.first.P;
+        si.N = pp.first.N;
+        si.UV = pp.first.UV;
+        li = S.AreaRadiance(L, si.UV);
       }
       si.Shading = Frame(si.N);
       rng.Next2D();  // Perspective::SampleDirection's sample

@@ -928,9 +928,31 @@ std::unique_ptr<Scene> Scene::FromJson(const std::string& text, const std::strin
         if (j->is_number() || j->is_array()) return JVec3(*j);
         throw std::runtime_error("textured lights are not supported");
       };
-      if (type == "area") {
+      if (type == "area") {  // area.cpp:20-41
         L.kind = Light::Area;
-        L.radiance = color("radiance", V3(1));
+        const Json* rj = ln->find("radiance");
+        if (rj && rj->is_object()) {
+          if (ReadS(rj, "type", "") == "chessboard") throw std::runtime_error("area: chessboard radiance is not supported");
+          L.map = MakeTexture(*rj, 3, &env);
+          uint32_t width = L.map->width, height = L.map->height;
+          if (width == 1 && height == 1) {  // _isUniform: the map is one constant
+            L.radiance = L.map->Eval(TexSi{V2(0, 0), V2(), V2()});
+            L.map = nullptr;
+          } else {
+            std::vector<Float> luminance(width * height);
+            for (uint32_t y = 0; y < height; y++) {
+              Float v = y / (Float)height;
+              uint32_t start = y * width;
+              for (uint32_t x = 0; x < width; x++) {
+                Float u = x / (Float)width;
+                luminance[start + x] = Luminance(L.map->Eval(TexSi{V2(u, v), V2(), V2()}));
+              }
+            }
+            L.dist.Build(luminance.data(), width, height);
+          }
+        } else {
+          L.radiance = color("radiance", V3(1));
+        }
       } else if (type == "skybox") {  // skybox.cpp:24-50
         L.kind = Light::Skybox;
         const Json* rj = ln->find("radiance");
@@ -1041,7 +1063,13 @@ std::unique_ptr<Scene> Scene::FromJson(const std::string& text, const std::strin
       sh.inMedium = inMed;
       sh.outMedium = outMed;
     }
-    if (lightIdx >= 0) S.lights[lightIdx].shape = shapeIdx;
+    if (lightIdx >= 0) {
+      S.lights[lightIdx].shape = shapeIdx;
+      // only the rectangle has EvalParamSurface (shape.cpp:27-29)
+      if (S.lights[lightIdx].kind == Light::Area && S.lights[lightIdx].map &&
+          (shapeIdx < 0 || S.shapes[shapeIdx].kind != Shape::Rect))
+        throw std::runtime_error("no impl EvalParamSurface(): a textured area light needs a rectangle");
+    }
   }
   // renderer (path.cpp:26-29, vol_path.cpp:22-25)
   const Json* rn = root.find("renderer");
@@ -1558,10 +1586,47 @@ Float Continuous2D::Pdf(const V2& uv) const {
   return conditional[iv].pdf[iu] / marginal.sum;
 }
 
+Spectrum Scene::AreaRadiance(const Light& L, const V2& uv) const {
+  return L.map ? L.map->Eval(TexSi{uv, V2(), V2()}) : L.radiance;
+}
+
+// Rectangle::EvalParamSurface (rectangle.cpp:236-250): position, normal and the
+// norm of dPdU x dPdV (the unit frame axes) at uv
+static void RectParam(const Shape& sh, const V2& uv, V3& P, V3& N, Float& dA) {
+  V2 tmp(uv.x * 2 - 1, uv.y * 2 - 1);
+  P = sh.toWorld.ApplyAffineToWorld(V3(tmp.x, tmp.y, 0));
+  N = sh.frame.N;
+  dA = norm(cross(sh.frame.S, sh.frame.T));
+}
+
+std::pair<PositionSample, Float> Scene::LightSamplePosition(int l, const V2& xi) const {
+  const Light& L = lights[l];
+  const Shape& sh = shapes[L.shape];
+  if (!L.map) {
+    PositionSample psr = sh.SamplePosition(xi);
+    return {psr, psr.Pdf > 0 ? psr.Pdf : 0};
+  }
+  auto [iu, iv, pdf] = L.dist.Sample(xi);
+  if (pdf <= 0) return {PositionSample(), Float(0)};
+  Float y = iv / (Float)L.map->height;
+  Float x = iu / (Float)L.map->width;
+  PositionSample psr;
+  Float dA;
+  psr.UV = V2(x, y);
+  RectParam(sh, psr.UV, psr.P, psr.N, dA);
+  pdf /= dA;
+  psr.Pdf = pdf;
+  psr.IsDelta = false;
+  return {psr, psr.Pdf > 0 ? psr.Pdf : 0};
+}
+
 // area.cpp:42-45, skybox.cpp:53-63
 Spectrum Scene::EvalLight(int l, const SurfaceInteraction& si) const {
   const Light& L = lights[l];
-  if (L.kind == Light::Area) return dot(si.ToWorld(si.Wi), si.N) >= 0 ? L.radiance : Spectrum(0);
+  if (L.kind == Light::Area) {
+    if (dot(si.ToWorld(si.Wi), si.N) < 0) return Spectrum(0);
+    return L.map ? L.map->Eval(TexSi{si.UV, si.dUVdX, si.dUVdY}) : L.radiance;
+  }
   if (L.kind == Light::Skybox) {
     if (!L.map) return L.radiance;
     V3 v = L.toWorld.ApplyLinearToLocal(-si.Wi);
@@ -1591,7 +1656,20 @@ std::pair<DirectionSample, Spectrum> Scene::SampleOneLightDirection(int index, c
   DirectionSample dsr;
   Spectrum li(0);
   const Light& L = lights[index];
-  if (L.kind == Light::Area) {
+  if (L.kind == Light::Area && L.map) {  // area.cpp:59-72: SurfaceInteraction::ToDsr leaves Pdf 0
+    auto [iu, iv, pdf] = L.dist.Sample(xi);
+    if (pdf <= 0) return {DirectionSample(), Spectrum(0)};
+    V2 uv(iu / (Float)L.map->width, iv / (Float)L.map->height);
+    Float dA;
+    RectParam(shapes[L.shape], uv, dsr.P, dsr.N, dA);
+    dsr.UV = uv;
+    dsr.Pdf = 0;
+    dsr.IsDelta = false;
+    V3 rel = dsr.P - refP;
+    dsr.Dist = norm(rel);
+    dsr.Dir = rel / dsr.Dist;
+    li = dot(-dsr.Dir, dsr.N) >= 0 ? L.map->Eval(TexSi{uv, V2(), V2()}) : Spectrum(0);
+  } else if (L.kind == Light::Area) {
     dsr = shapes[L.shape].SampleDirection(refP, xi);
     li = dot(-dsr.Dir, dsr.N) >= 0 ? L.radiance : Spectrum(0);
   } else if (L.kind == Light::Skybox) {  // skybox.cpp:65-106
@@ -1698,7 +1776,16 @@ static Float SkyPdfDirection(const Light& L, const V3& dir) {
 Float Scene::PdfLightDirection(int l, const V3& refP, const DirectionSample& dsr) const {
   const Light& L = lights[l];
   Float p = 0;
-  if (L.kind == Light::Area) {
+  if (L.kind == Light::Area && L.map) {  // area.cpp:81-90
+    Float pdf = L.dist.Pdf(dsr.UV);
+    if (pdf > 0) {
+      V3 P, N;
+      Float dA;
+      RectParam(shapes[L.shape], dsr.UV, P, N, dA);
+      Float dp = dot(dsr.Dir, dsr.N);
+      p = pdf * Sqr(dsr.Dist) / (dA * -dp);
+    }
+  } else if (L.kind == Light::Area) {
     p = dot(-dsr.Dir, dsr.N) >= 0 ? shapes[L.shape].PdfDirection(refP, dsr) : 0;
   } else if (L.kind == Light::Skybox) {
     p = SkyPdfDirection(L, dsr.Dir);
@@ -1728,13 +1815,14 @@ bool Scene::LightSampleRay(int l, const V2& xi2, const V2& xi3, Ray& ray, Spectr
   ray.MinT = 0;
   ray.MaxT = std::numeric_limits<Float>::max();
   if (L.kind == Light::Area) {  // area.cpp:120-128
-    PositionSample psr = shapes[L.shape].SamplePosition(xi2);
-    Float pdf = psr.Pdf;
+    auto pp = LightSamplePosition(l, xi2);
+    const PositionSample& psr = pp.first;
+    Float pdf = pp.second;
     V3 local = SquareToCosineHemisphere(xi3);
     Frame fr(psr.N);  // SurfaceInteraction(psr)
     V3 d = fr.ToWorld(local);
     ray = SpawnRay(psr.P, psr.N, d);
-    Spectrum eval = L.radiance;  // Eval(si) with no incident direction: dot(0, N) >= 0
+    Spectrum eval = AreaRadiance(L, psr.UV);  // Eval(si) with no incident direction: dot(0, N) >= 0
     li = eval * PI / pdf;
     return true;
   }
@@ -1798,14 +1886,15 @@ Scene::LeSample Scene::LightSampleLe(int l, const V2& xi2, const V2& xi3) const 
   LeSample r;
   r.ray.MinT = 0;
   r.ray.MaxT = std::numeric_limits<Float>::max();
-  if (L.kind == Light::Area) {  // area.cpp:130-140 (constant radiance)
-    r.psr = shapes[L.shape].SamplePosition(xi2);
-    r.pdfPos = r.psr.Pdf > 0 ? r.psr.Pdf : 0;
+  if (L.kind == Light::Area) {  // area.cpp:130-140
+    auto pp = LightSamplePosition(l, xi2);
+    r.psr = pp.first;
+    r.pdfPos = pp.second;
     V3 local = SquareToCosineHemisphere(xi3);
     r.pdfDir = SquareToCosineHemispherePdf(local);
     Frame fr(r.psr.N);  // SurfaceInteraction(psr)
     r.ray = SpawnRay(r.psr.P, r.psr.N, fr.ToWorld(local));
-    r.le = L.radiance;  // Eval(si) with no incident direction: dot(0, N) >= 0
+    r.le = AreaRadiance(L, r.psr.UV);  // Eval(si) with no incident direction: dot(0, N) >= 0
   } else if (L.kind == Light::Point) {  // point.cpp:75-85
     r.psr.P = L.worldPos;
     r.psr.N = V3(0);

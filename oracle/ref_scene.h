@@ -143,9 +143,9 @@ struct Light {
   V3 worldPos;   // point: world position (point.cpp:22-23)
   Spectrum scale;      // projection: irradiance scale
   Transform toClip;    // projection: light space -> [0,1]^2 image plane (projection.cpp:27-41)
-  std::shared_ptr<Texture> map;  // skybox: radiance texture (null: constant radiance)
+  std::shared_ptr<Texture> map;  // skybox / area: radiance texture (null: constant radiance)
   bool uniformMap = true;        // skybox: 1 x 1 map, uniform sphere sampling
-  Continuous2D dist;             // skybox: luminance distribution of a bitmap map
+  Continuous2D dist;             // skybox / area: luminance distribution of a bitmap map
   Float cameraArea = 0;          // projection: 1 / area of the image rectangle (projection.cpp:41-44)
   V3 worldCenter;
   Float worldRadius = 0;
@@ -262,6 +262,11 @@ struct Scene {
   // Light::PdfLe (area.cpp:142-147, point.cpp:87-91, projection.cpp:122-133, skybox.cpp:206-212)
   std::pair<Float, Float> LightPdfLe(int light, const PositionSample& psr, const V3& dir) const;
   Spectrum EvalLight(int light, const SurfaceInteraction& si) const;
+  // DiffuseArea::SamplePosition (area.cpp:93-115): (position sample, density); a textured light samples its
+  // luminance distribution at texel corners of the rectangle (Rectangle::EvalParamSurface, rectangle.cpp:236-250)
+  std::pair<PositionSample, Float> LightSamplePosition(int light, const V2& xi) const;
+  // the area light's radiance texture at uv (constant radiance without one)
+  Spectrum AreaRadiance(const Light& L, const V2& uv) const;
   uint64_t PrimCount() const { return prims.size(); }
 };
 

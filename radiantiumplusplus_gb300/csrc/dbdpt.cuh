@@ -110,12 +110,12 @@ RD V3 VLe(const DevScene& S, const BVert& v, const BVert& other) {
     si.sh = v.sh;
     si.Wi = ToLocal(v.sh, toV);
   }
-  return EvalLightAt(S, l, &si);
+  return EvalLightAt(S, l, &si, v.uv);
 }
 
 // BDPT::InfiniteLightDensity (bdpt.cpp:658-663)
 RD float InfiniteLightDensity(const DevScene& S, V3 w) {
-  return PdfLightDirection(S, S.envLight, v3s(0.f), -w, v3s(0.f), 0.f);
+  return PdfLightDirection(S, S.envLight, v3s(0.f), -w, v3s(0.f), 0.f, V2{0.f, 0.f});
 }
 
 // Shape::PdfPosition (mesh_base.cpp, rectangle.cpp, sphere.cpp): uniform by area
@@ -322,18 +322,17 @@ struct LeSample {
 };
 RDN LeSample LightSampleLe(const DevScene& S, const LightRec& L, V2 xi2, V2 xi3) {
   LeSample r{};
-  if (L.kind == LIGHT_AREA) {  // constant radiance
+  if (L.kind == LIGHT_AREA) {
     const ShapeRec& sh = S.shapes[L.shape];
-    float pdf;
-    ShapeSamplePosition(S, sh, xi2, r.P, r.N, pdf);
-    r.delta = sh.kind == SHAPE_SPHERE && sh.m[3] == 0.f;
-    r.pdfPos = pdf > 0.f ? pdf : 0.f;
+    V2 uv;
+    AreaSamplePosition(S, L, xi2, r.P, r.N, uv, r.pdfPos);
+    r.delta = !L.tex && sh.kind == SHAPE_SPHERE && sh.m[3] == 0.f;
     V3 local = SquareToCosineHemisphere(xi3);
     r.pdfDir = SquareToCosineHemispherePdf(local);
     Frame fr = FrameFromN(r.N);
     r.D = ToWorld(fr, local);
     r.O = OffsetP(r.P, r.N, r.D);
-    r.le = V3{L.radiance[0], L.radiance[1], L.radiance[2]};
+    r.le = AreaRadiance(S, L, uv);  // Eval(si) with no incident direction: dot(0, N) >= 0
   } else if (L.kind == LIGHT_POINT) {
     r.P = V3{L.dir[0], L.dir[1], L.dir[2]};
     r.N = v3s(0.f);

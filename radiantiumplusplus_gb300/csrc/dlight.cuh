@@ -101,11 +101,12 @@ RD bool ParticleStart(const DevScene& S, uint64_t id, uint32_t seed, float sampl
         lightPdf *= dsr.Pdf > 0.f ? (dsr.Pdf * Sqr(dsr.Dist)) : 0.f;
         si.P = dsr.P;
         si.N = dsr.N;
-      } else {  // area: a point on the emitter, radiance Eval(si) (area.cpp:42-45)
+      } else {  // area: Light::SamplePosition, radiance Eval(si) (area.cpp:42-45)
         float pdf;
-        ShapeSamplePosition(S, S.shapes[L.shape], xi, si.P, si.N, pdf);
+        V2 uv;
+        AreaSamplePosition(S, L, xi, si.P, si.N, uv, pdf);
         lightPdf *= pdf;
-        le = V3{L.radiance[0], L.radiance[1], L.radiance[2]};
+        le = AreaRadiance(S, L, uv);
       }
       si.sh = FrameFromN(si.N);  // SurfaceInteraction(psr) (interaction.cpp:30-41)
       V3 camP, camDir;

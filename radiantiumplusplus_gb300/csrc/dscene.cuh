@@ -344,16 +344,33 @@ RD uint32_t Dist1DSample(const float* row, uint32_t n, float xi, float& pdf) {
 // Skybox::SampleLightDir / PdfDirection on a bitmap radiance map (skybox.cpp:112-131,
 // 213-233) with ContinuousDistribution2D (distribution.cpp:103-129): rows of
 // 2 nu + 2 floats, then the marginal (pdf, cdf, normalization, sum).
-RD bool EnvSampleDir(const DevScene& S, const LightRec& L, V2 xi, V3& worldDir, float& pdf, V2& uv) {
+// ContinuousDistribution2D::Sample / Pdf (distribution.cpp:103-129) of a
+// light's luminance distribution (a bitmap skybox or area light).
+RD float Dist2DSample(const DevScene& S, const LightRec& L, V2 xi, uint32_t& iu, uint32_t& iv) {
   const uint32_t nu = L.distW, nv = L.distH;
   const float* base = S.lightDist + L.dist;
   const float* marg = base + (size_t)nv * (2 * nu + 2);
   float pdf1, pdf0;
-  uint32_t vj = Dist1DSample(marg, nv, xi.y, pdf1);
-  uint32_t vi = Dist1DSample(base + (size_t)vj * (2 * nu + 2), nu, xi.x, pdf0);
-  pdf = pdf0 * pdf1;
+  iv = Dist1DSample(marg, nv, xi.y, pdf1);
+  iu = Dist1DSample(base + (size_t)iv * (2 * nu + 2), nu, xi.x, pdf0);
+  return pdf0 * pdf1;
+}
+RD float Dist2DPdf(const DevScene& S, const LightRec& L, V2 uv) {
+  const uint32_t nu = L.distW, nv = L.distH;
+  const float* base = S.lightDist + L.dist;
+  const float* marg = base + (size_t)nv * (2 * nu + 2);
+  float fu = uv.x * (float)nu, fv = uv.y * (float)nv;
+  uint32_t iu = fu >= 0.f ? (uint32_t)fu : 0u, iv = fv >= 0.f ? (uint32_t)fv : 0u;
+  iu = iu < nu - 1u ? iu : nu - 1u;
+  iv = iv < nv - 1u ? iv : nv - 1u;
+  return base[(size_t)iv * (2 * nu + 2) + iu] / marg[2 * nv + 2];
+}
+
+RD bool EnvSampleDir(const DevScene& S, const LightRec& L, V2 xi, V3& worldDir, float& pdf, V2& uv) {
+  uint32_t vi, vj;
+  pdf = Dist2DSample(S, L, xi, vi, vj);
   if (pdf <= 0.f) return false;
-  float y = (float)vj / (float)nv, x = (float)vi / (float)nu;
+  float y = (float)vj / (float)L.distH, x = (float)vi / (float)L.distW;
   uv = V2{x, y};
   float theta = y * kPi, phi = x * 2.f * kPi;
   float sinTheta = sinf(theta);
@@ -372,14 +389,7 @@ RD float EnvDirPdf(const DevScene& S, const LightRec& L, V3 dir) {
   float phi = atan2f(v.x, -v.z);
   phi = phi < 0.f ? phi + 2.f * kPi : phi;
   V2 uv{phi / (2.f * kPi), theta / kPi};
-  const uint32_t nu = L.distW, nv = L.distH;
-  const float* base = S.lightDist + L.dist;
-  const float* marg = base + (size_t)nv * (2 * nu + 2);
-  float fu = uv.x * (float)nu, fv = uv.y * (float)nv;
-  uint32_t iu = fu >= 0.f ? (uint32_t)fu : 0u, iv = fv >= 0.f ? (uint32_t)fv : 0u;
-  iu = iu < nu - 1u ? iu : nu - 1u;
-  iv = iv < nv - 1u ? iv : nv - 1u;
-  float pdf = base[(size_t)iv * (2 * nu + 2) + iu] / marg[2 * nv + 2];
+  float pdf = Dist2DPdf(S, L, uv);
   return pdf / (2.f * kPi * kPi * sinTheta);
 }
 // The sky's radiance towards world direction d (skybox.cpp:53-63): the map's
@@ -393,6 +403,40 @@ RD V3 EnvRadiance(const DevScene& S, const LightRec& L, V3 d) {
   TexCtx x{S.tex, S.texels, S.texBind, V2{phi / (2.f * kPi), theta / kPi}, V2{0.f, 0.f}, V2{0.f, 0.f}};
   TexVal r = TexEval(x, L.tex - 1u, x.uv);
   return V3{r.c[0], r.c[1], r.c[2]};
+}
+
+// An area light's radiance at uv: its bitmap, else the constant (area.cpp:42-45).
+RD V3 AreaRadiance(const DevScene& S, const LightRec& L, V2 uv) {
+  if (!L.tex) return V3{L.radiance[0], L.radiance[1], L.radiance[2]};
+  TexCtx x{S.tex, S.texels, S.texBind, uv, V2{0.f, 0.f}, V2{0.f, 0.f}};
+  TexVal r = TexEval(x, L.tex - 1u, uv);
+  return V3{r.c[0], r.c[1], r.c[2]};
+}
+
+// DiffuseArea::SamplePosition (area.cpp:93-115): a bitmap light samples its
+// luminance distribution at texel corners uv of its rectangle
+// (Rectangle::EvalParamSurface, rectangle.cpp:236-250; |dPdU x dPdV| is the
+// rectangle's area). pdf is the area density, 0 for a failed sample.
+RD void AreaSamplePosition(const DevScene& S, const LightRec& L, V2 xi, V3& P, V3& N, V2& uv, float& pdf) {
+  const ShapeRec& sh = S.shapes[L.shape];
+  uv = V2{0.f, 0.f};
+  if (!L.tex) {
+    ShapeSamplePosition(S, sh, xi, P, N, pdf);
+    pdf = pdf > 0.f ? pdf : 0.f;
+    return;
+  }
+  uint32_t iu, iv;
+  float p = Dist2DSample(S, L, xi, iu, iv);
+  if (p <= 0.f) {
+    P = N = v3s(0.f);
+    pdf = 0.f;
+    return;
+  }
+  uv = V2{(float)iu / (float)L.distW, (float)iv / (float)L.distH};
+  P = AffineRows(sh.m, V3{uv.x * 2.f - 1.f, uv.y * 2.f - 1.f, 0.f});
+  N = ShapeM3(sh, 18);
+  p /= sh.surfaceArea;
+  pdf = p > 0.f ? p : 0.f;
 }
 
 // Scene::SampleLight (scene.cpp:65-77): uniform pick; false without lights.
@@ -416,6 +460,7 @@ RD DirSample LightSampleDirection(const DevScene& S, const LightRec& L, V3 refP,
   li = v3s(0.f);
   V3 rad{L.radiance[0], L.radiance[1], L.radiance[2]};
   if (L.kind == LIGHT_AREA) {
+    if (L.tex) return d;  // area.cpp:59-72: the bitmap branch's SurfaceInteraction::ToDsr leaves Pdf 0
     d = ShapeSampleDirection(S, S.shapes[L.shape], refP, xi);
     li = dot(-d.Dir, d.N) >= 0.f ? rad : v3s(0.f);
   } else if (L.kind == LIGHT_POINT) {  // point.cpp:33-49
@@ -506,10 +551,13 @@ RD DirSample SampleLightDirection(const DevScene& S, V3 refP, float xiL, V2 xi, 
 }
 
 // scene.cpp:98-103
-RD float PdfLightDirection(const DevScene& S, int light, V3 refP, V3 dir, V3 n, float dist) {
+RD float PdfLightDirection(const DevScene& S, int light, V3 refP, V3 dir, V3 n, float dist, V2 uv) {
   const LightRec& L = S.lights[light];
   float p = 0.f;
-  if (L.kind == LIGHT_AREA) {
+  if (L.kind == LIGHT_AREA && L.tex) {  // area.cpp:81-90 (no facing test)
+    float pdf = Dist2DPdf(S, L, uv);
+    if (pdf > 0.f) p = pdf * Sqr(dist) / (S.shapes[L.shape].surfaceArea * -dot(dir, n));
+  } else if (L.kind == LIGHT_AREA) {
     p = dot(-dir, n) >= 0.f ? ShapePdfDirection(S.shapes[L.shape], refP, dir, n, dist) : 0.f;
   } else if (L.kind == LIGHT_SKYBOX) {
     p = L.distW ? EnvDirPdf(S, L, dir) : SquareToUniformSpherePdf();
@@ -519,10 +567,9 @@ RD float PdfLightDirection(const DevScene& S, int light, V3 refP, V3 dir, V3 n, 
 
 // area.cpp:42-45 / skybox.cpp:53-63; point and projection
 // lights have no surface to hit and evaluate to 0 (point.cpp:29-31, projection.cpp:48-50).
-RD V3 EvalLightAt(const DevScene& S, int light, const SurfInt* si) {
+RD V3 EvalLightAt(const DevScene& S, int light, const SurfInt* si, V2 uv) {
   const LightRec& L = S.lights[light];
-  V3 rad{L.radiance[0], L.radiance[1], L.radiance[2]};
-  if (L.kind == LIGHT_AREA) return dot(ToWorld(si->sh, si->Wi), si->N) >= 0.f ? rad : v3s(0.f);
+  if (L.kind == LIGHT_AREA) return dot(ToWorld(si->sh, si->Wi), si->N) >= 0.f ? AreaRadiance(S, L, uv) : v3s(0.f);
   if (L.kind == LIGHT_SKYBOX) return EnvRadiance(S, L, -si->Wi);
   return v3s(0.f);
 }
@@ -564,13 +611,14 @@ RD bool LightSampleRay(const DevScene& S, const LightRec& L, V2 xi2, V2 xi3, V3&
   V3 rad{L.radiance[0], L.radiance[1], L.radiance[2]};
   if (L.kind == LIGHT_AREA) {
     V3 P, N;
+    V2 uv;
     float pdf;
-    ShapeSamplePosition(S, S.shapes[L.shape], xi2, P, N, pdf);
+    AreaSamplePosition(S, L, xi2, P, N, uv, pdf);
     Frame fr = FrameFromN(N);
     V3 local = SquareToCosineHemisphere(xi3);
     D = ToWorld(fr, local);
     O = OffsetP(P, N, D);
-    li = rad * kPi / pdf;  // Eval(si) of a point with no incident direction: the radiance
+    li = AreaRadiance(S, L, uv) * kPi / pdf;  // Eval(si) of a point with no incident direction
     return true;
   }
   if (L.kind == LIGHT_POINT) {

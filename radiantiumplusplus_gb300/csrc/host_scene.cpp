@@ -562,7 +562,10 @@ float AppendDist1D(const float* f, size_t n, std::vector<float>& pool) {
 // Skybox luminance grid and ContinuousDistribution2D (skybox.cpp:27-47,
 // distribution.cpp:103-118): the map read at texel corners (x / W, y / H),
 // luminance weighted by sin of the row's centre latitude.
-void BuildEnvDistribution(HostScene& hs, uint32_t tex, uint32_t W, uint32_t H, LightRec& L) {
+// Luminance distribution of a bitmap light over its texel corners: weighted by
+// sin(theta) of the row for a skybox (skybox.cpp:28-48), unweighted for an
+// area light (area.cpp:25-40).
+void BuildEnvDistribution(HostScene& hs, uint32_t tex, uint32_t W, uint32_t H, LightRec& L, bool sinWeight = true) {
   std::vector<float> lum((size_t)W * H);
   for (uint32_t y = 0; y < H; y++) {
     float sinTheta = std::sin((y + 0.5f) / H * kPiF);
@@ -572,7 +575,7 @@ void BuildEnvDistribution(HostScene& hs, uint32_t tex, uint32_t W, uint32_t H, L
       float c[3];
       HostTexEval(hs, tex, u, v, c);
       float l = (c[0] * 0.212671f) + (c[1] * 0.715160f) + (c[2] * 0.072169f);
-      lum[(size_t)y * W + x] = l * sinTheta;
+      lum[(size_t)y * W + x] = sinWeight ? l * sinTheta : l;
     }
   }
   if (hs.lightDist.size() + lum.size() * 2 + 4 * H + 8 > 0xffffffffull) throw ConfigError("environment map too large");
@@ -1249,7 +1252,23 @@ void BuildHostScene(const std::string& json, const std::string& baseDir, HostSce
       F3 rad;
       if (type == "area") {  // area.cpp:20-40
         L.kind = LIGHT_AREA;
-        rad = col("radiance", F3(1, 1, 1));
+        const JValue* rn = ln->get("radiance");
+        if (rn && rn->isObj()) {
+          uint32_t tid = AddTexture(*rn, 3, env);
+          const TexRec& tr = hs.tex[tid];
+          uint32_t W = tr.kind == TEX_BITMAP ? tr.width : 1u, H = tr.kind == TEX_BITMAP ? tr.height : 1u;
+          if (tr.kind == TEX_CHESS) throw FactoryError("area: chessboard radiance is not supported");
+          if (W == 1 && H == 1) {  // _isUniform: one constant
+            float c[3];
+            HostTexEval(hs, tid, 0.f, 0.f, c);
+            rad = F3(c[0], c[1], c[2]);
+          } else {
+            L.tex = tid + 1;
+            BuildEnvDistribution(hs, tid, W, H, L, false);
+          }
+        } else {
+          rad = col("radiance", F3(1, 1, 1));
+        }
       } else if (type == "skybox") {  // skybox.cpp:24-50
         L.kind = LIGHT_SKYBOX;
         const JValue* rn = ln->get("radiance");
@@ -1369,6 +1388,9 @@ void BuildHostScene(const std::string& json, const std::string& baseDir, HostSce
     if (lightIdx >= 0) {
       hs.lights[lightIdx].shape = shapeIdx;
       if (hs.lights[lightIdx].kind == LIGHT_AREA && shapeIdx < 0) throw ConfigError("area light needs a shape");
+      // only the rectangle has EvalParamSurface (shape.cpp:27-29)
+      if (hs.lights[lightIdx].kind == LIGHT_AREA && hs.lights[lightIdx].tex && hs.shapes[shapeIdx].kind != SHAPE_RECT)
+        throw ConfigError("no impl EvalParamSurface(): a textured area light needs a rectangle");
     }
   }
   const JValue* rn = root.get("renderer");

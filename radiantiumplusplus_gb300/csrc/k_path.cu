@@ -294,6 +294,11 @@ __global__ void __launch_bounds__(kBlock) KShadeClass(DevScene S, PathBuffers B,
             si.sh.S = si.sh.T = si.sh.N = v3s(0.f);
             si.Wi = -D;  // scene.cpp:45-47: world-space -D on a miss
           }
+          V2 uvL{0.f, 0.f};  // a bitmap area light reads its radiance at the hit's uv
+          if (anyHit && S.lights[hitLight].tex && S.lights[hitLight].kind == LIGHT_AREA) {
+            TraceHit th{h.t, h.u, h.v, h.prim, h.shape, h.front};
+            uvL = ComputeUV(S, th, si).uv;
+          }
           float4 pv = B.prev[p];
           bool specular = __float_as_uint(pv.w) & 1u;
           float weight;
@@ -305,9 +310,9 @@ __global__ void __launch_bounds__(kBlock) KShadeClass(DevScene S, PathBuffers B,
             V3 rel = si.P - prevP;
             float dist = norm(rel);
             V3 dir = anyHit ? rel / dist : -si.Wi;
-            weight = MisWeight(L4.w, PdfLightDirection(S, hitLight, prevP, dir, si.sh.N, dist));
+            weight = MisWeight(L4.w, PdfLightDirection(S, hitLight, prevP, dir, si.sh.N, dist, uvL));
           }
-          V3 li = EvalLightAt(S, hitLight, &si);
+          V3 li = EvalLightAt(S, hitLight, &si, uvL);
           V3 L = V3{L4.x, L4.y, L4.z} + cmul(thr, li) * weight;
           B.L[p] = make_float4(L.x, L.y, L.z, L4.w);
         }

@@ -376,7 +376,7 @@ RD bool VolSurface(const DevScene& S, VolPathState& p, uint32_t mode, uint32_t* 
   // texture coordinates of the hit, for scenes with textures (vol_path traces
   // plain rays: no differentials, uv derivatives 0)
   const bool textured = S.nTex != 0u;
-  V2 uvHit;
+  V2 uvHit{0.f, 0.f};
   bool hit = VTraceCall(S, ray, si, err, textured ? &uvHit : nullptr);
   TexCtx tcx;
   const TexCtx* tc = nullptr;
@@ -394,9 +394,9 @@ RD bool VolSurface(const DevScene& S, VolPathState& p, uint32_t mode, uint32_t* 
       V3 rel = si.P - p.prevP;
       float dist = norm(rel);
       V3 dir = hit ? rel / dist : -si.Wi;
-      weight = VMis(p.prevPdf, PdfLightDirection(S, hitLight, p.prevP, dir, si.sh.N, dist));
+      weight = VMis(p.prevPdf, PdfLightDirection(S, hitLight, p.prevP, dir, si.sh.N, dist, uvHit));
     }
-    V3 li = EvalLightAt(S, hitLight, &si);
+    V3 li = EvalLightAt(S, hitLight, &si, uvHit);
     p.result = p.result + cmul(thr, li) * weight;
   }
   if (!hit) return false;

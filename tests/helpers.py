@@ -79,6 +79,23 @@ def textured_room_scene(w=48, h=48, spp=4, seed=1, renderer="path"):
     return sc, assets
 
 
+def textured_light_room(w=48, h=48, spp=4, seed=1, renderer="path"):
+    """Box room lit by its ceiling rectangle with a bitmap radiance (an 8 x 6
+    Radiance HDR pattern with a black row): the light's luminance distribution
+    drives its position samples (area.cpp:93-115). Returns (scene dict, assets)."""
+    import imgenc
+    yy, xx = np.mgrid[0:6, 0:8]
+    img = np.stack([4.0 + 20.0 * xx / 7, 2.0 + 14.0 * yy / 5, 8.0 * ((xx + yy) % 2) + 1.0], axis=2)
+    img[2] = 0.0
+    sc = scenes.box_room(w, h, spp, seed)
+    sc["assets"] = [{"name": "glow", "type": "image_hdr", "location": "glow.hdr"}]
+    sc["scene"][-1]["light"] = {"type": "area", "radiance": {"type": "bitmap", "asset_name": "glow",
+                                                               "filter": "nearest"}}
+    if renderer != "path":
+        sc["renderer"] = {"type": renderer, "max_depth": 6}
+    return sc, {"glow.hdr": imgenc.hdr(img)}
+
+
 def textured(dirpath, w=48, h=48, spp=4, seed=1, renderer="path"):
     sc, assets = textured_room_scene(w, h, spp, seed, renderer)
     return write(dirpath, "textured_%s_%dx%d_%d_%d" % (renderer, w, h, spp, seed), sc, assets)

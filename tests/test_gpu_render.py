@@ -137,6 +137,30 @@ def test_bdpt_samples_and_film(rad, oracle, scene_dir, light):
     g.close()
 
 
+@pytest.mark.parametrize("renderer", ["path", "vol_path", "bdpt", "particle_tracer"])
+def test_textured_area_light(rad, oracle, scene_dir, renderer):
+    """A bitmap radiance on the emitter rectangle: its texels seen at hits, the
+    luminance distribution behind position samples (light paths), the
+    reference's zero-density direction samples (no next-event estimation from a
+    bitmap light) and its direction density in the MIS weights."""
+    from helpers import textured_light_room
+    sc, assets = textured_light_room(24, 24, 4, renderer=renderer)
+    if renderer == "particle_tracer":
+        sc["sampler"]["sample_count"] = 60000
+    path, text, d = write(scene_dir, "texlight_" + renderer, sc, assets)
+    g, o = rad.Scene.from_file(path), oracle.OracleScene(text, d)
+    if renderer == "particle_tracer":
+        film = g.render()
+        ref = o.render_particle()
+        lit = ref.sum(axis=2) > 1e-3
+        close = (np.abs(film - ref) <= 0.02 * np.abs(ref) + 1e-6).all(axis=2)
+        assert close[lit].mean() >= 0.9, close[lit].mean()
+        assert abs(film.mean() - ref.mean()) < 0.01 * ref.mean()
+    else:
+        _sample_parity(g, o, 4, 0.95)
+    g.close()
+
+
 def test_path_samples_lights(rad, oracle, scene_dir):
     """Point and projection lights (delta lights: no MIS weight on their samples) beside
     an area emitter."""

@@ -367,3 +367,39 @@ def test_bdpt_rejects_directional_light(oracle):
     sc["renderer"] = {"type": "bdpt"}
     with pytest.raises(RuntimeError, match="directional"):
         oracle.OracleScene(json.dumps(sc), "")
+
+
+def test_textured_area_light_seen_directly(oracle, scene_dir):
+    """area.cpp:42-45 with a bitmap: a camera facing the emitter sees its texels
+    (nearest filter: texel floor(u (w - 1)), bitmap.cpp:181-191), laid out by the
+    rectangle's uv (rectangle.cpp:202-217); an emitter shape other than a
+    rectangle is refused (only the rectangle has EvalParamSurface,
+    shape.cpp:27-29)."""
+    import imgenc
+    from helpers import write
+    texels = np.full((3, 3, 3), 0.5)
+    texels[:2, :2] = [[[1.0, 0.0, 0.0], [0.0, 2.0, 0.0]], [[0.0, 0.0, 3.0], [4.0, 4.0, 4.0]]]
+    sc = {"camera": {"type": "perspective", "fov": 10.0, "resolution": [16, 16], "origin": [0, 0, 5],
+                     "target": [0, 0, 0]},
+          "sampler": {"type": "independent", "sample_count": 1, "seed": 2},
+          "assets": [{"name": "q", "type": "image_hdr", "location": "q.hdr"}],
+          "scene": [{"to_world": {"scale": [2, 2, 1]}, "shape": {"type": "rectangle"},
+                     "light": {"type": "area", "radiance": {"type": "bitmap", "asset_name": "q",
+                                                            "filter": "nearest"}}}],
+          "accel": {"type": "embree"}, "renderer": {"type": "path", "max_depth": 1}}
+    hdr = imgenc.hdr(texels, rle=False)  # scanlines narrower than 8 are stored flat
+    _, text, d = write(scene_dir, "tex_light_direct", sc, {"q.hdr": hdr})
+    o = oracle.OracleScene(text, d)
+    film, _ = o.render()
+    o.close()
+    q = imgenc.rgbe(texels)
+    dec = q[..., :3] * np.ldexp(1.0, q[..., 3:4].astype(int) - 136)  # the RGBE values the decoder returns
+    corners = film[[1, 1, 14, 14], [1, 14, 1, 14]]
+    got = {tuple(np.round(c, 3)) for c in corners}
+    want = {tuple(np.round(c, 3)) for c in dec[:2, :2].reshape(-1, 3)}
+    assert got == want, (got, want)
+    sc["scene"][0]["shape"] = {"type": "sphere", "radius": 1.0}
+    sc["scene"][0]["to_world"] = {"translate": [0, 0, 0]}
+    _, text, d = write(scene_dir, "tex_light_sphere", sc, {"q.hdr": hdr})
+    with pytest.raises(RuntimeError, match="EvalParamSurface"):
+        oracle.OracleScene(text, d)
