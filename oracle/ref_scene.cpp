@@ -986,10 +986,16 @@ std::unique_ptr<Scene> Scene::FromJson(const std::string& text, const std::strin
         L.radiance = ReadV3(ln, "intensity", V3(1, 1, 1));
       } else if (type == "projection") {  // projection.cpp:19-45
         L.kind = Light::Projection;
-        L.radiance = color("irradiance", V3(1));
+        const Json* ij = ln->find("irradiance");
+        Float aspect = 1 / (Float)1;  // Width / Height of the irradiance texture (1 x 1 when constant)
+        if (ij && ij->is_object()) {
+          L.map = MakeTexture(*ij, 3, &env);
+          aspect = L.map->width / (Float)L.map->height;
+        } else {
+          L.radiance = color("irradiance", V3(1));
+        }
         L.scale = ReadV3(ln, "scale", V3(1, 1, 1));
         Float fov = ReadF(ln, "fov", Float(90));
-        Float aspect = 1 / (Float)1;  // Width / Height of a constant texture
         Float farZ = 10000;
         Float nearZ = Float(0.0001);
         Float recip = 1 / (farZ - nearZ);
@@ -1741,7 +1747,9 @@ std::pair<DirectionSample, Spectrum> Scene::SampleOneLightDirection(int index, c
       Float squaredNorm = sqnorm(dsr.Dir);
       dsr.Dist = std::sqrt(squaredNorm);
       dsr.Dir = dsr.Dir * Rcp(dsr.Dist);
-      li = cmul(L.radiance, L.scale) * PI / (Sqr(local.z) * dot(-dsr.Dir, dsr.N));
+      dsr.UV = V2(c.x, c.y);
+      Spectrum irr = L.map ? L.map->Eval(TexSi{dsr.UV, V2(), V2()}) : L.radiance;
+      li = cmul(irr, L.scale) * PI / (Sqr(local.z) * dot(-dsr.Dir, dsr.N));
     }
   } else {
     Float radius = std::max(L.worldRadius, norm(refP - L.worldCenter));
@@ -1838,7 +1846,8 @@ bool Scene::LightSampleRay(int l, const V2& xi2, const V2& xi3, Ray& ray, Spectr
     V3 nearDir = normalized(nearP);
     ray.O = V3(L.toWorld.ToWorld.m[0][3], L.toWorld.ToWorld.m[1][3], L.toWorld.ToWorld.m[2][3]);
     ray.D = L.toWorld.ApplyLinearToWorld(nearDir);
-    li = L.radiance * PI * L.cameraArea;  // SampleRay leaves out the light's scale
+    Spectrum irr = L.map ? L.map->Eval(TexSi{uv, V2(), V2()}) : L.radiance;
+    li = irr * PI * L.cameraArea;  // SampleRay leaves out the light's scale
     return true;
   }
   Float R = L.worldRadius;
@@ -1918,7 +1927,7 @@ Scene::LeSample Scene::LightSampleLe(int l, const V2& xi2, const V2& xi3) const 
     V3 nearDir = normalized(nearP);
     r.ray.O = r.psr.P;
     r.ray.D = L.toWorld.ApplyLinearToWorld(nearDir);
-    r.le = L.radiance;  // the irradiance without the light's scale
+    r.le = L.map ? L.map->Eval(TexSi{xi3, V2(), V2()}) : L.radiance;  // the irradiance without the light's scale
     r.pdfDir = 1 / (L.cameraArea * PI);
   } else if (L.kind == Light::Skybox) {  // skybox.cpp:170-204
     Float R = L.worldRadius;

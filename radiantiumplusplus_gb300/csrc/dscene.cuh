@@ -486,6 +486,11 @@ RD DirSample LightSampleDirection(const DevScene& S, const LightRec& L, V3 refP,
     d.Dist = sqrtf(sqnorm(dir));
     d.Dir = dir * Rcp(d.Dist);
     float den = Sqr(local.z) * dot(-d.Dir, d.N);
+    if (L.tex) {  // irradiance texture at the light-space uv, times the scale
+      TexCtx x{S.tex, S.texels, S.texBind, V2{uv.x, uv.y}, V2{0.f, 0.f}, V2{0.f, 0.f}};
+      TexVal t = TexEval(x, L.tex - 1u, x.uv);
+      rad = cmul(V3{t.c[0], t.c[1], t.c[2]}, rad);
+    }
     li = V3{(rad.x * kPi) / den, (rad.y * kPi) / den, (rad.z * kPi) / den};
   } else {
     V3 wc{L.world[0], L.world[1], L.world[2]};
@@ -632,7 +637,13 @@ RD bool LightSampleRay(const DevScene& S, const LightRec& L, V2 xi2, V2 xi3, V3&
     V3 nearDir = normalized(nearP);
     O = V3{L.dir[0], L.dir[1], L.dir[2]};
     D = LinearRows(L.m2 + 16, nearDir);
-    li = V3{L.m2[29], L.m2[30], L.m2[31]} * kPi * L.m2[28];  // SampleRay leaves out the light's scale
+    V3 irr{L.m2[29], L.m2[30], L.m2[31]};
+    if (L.tex) {
+      TexCtx x{S.tex, S.texels, S.texBind, xi3, V2{0.f, 0.f}, V2{0.f, 0.f}};
+      TexVal t = TexEval(x, L.tex - 1u, xi3);
+      irr = V3{t.c[0], t.c[1], t.c[2]};
+    }
+    li = irr * kPi * L.m2[28];  // SampleRay leaves out the light's scale
     return true;
   }
   V3 wc{L.world[0], L.world[1], L.world[2]};

@@ -1292,11 +1292,22 @@ void BuildHostScene(const std::string& json, const std::string& baseDir, HostSce
         rad = RV(ln, "intensity", F3(1, 1, 1));
       } else if (type == "projection") {  // projection.cpp:19-45 (constant irradiance: a 1x1 texture)
         L.kind = LIGHT_PROJECTION;
-        F3 irr = col("irradiance", F3(1, 1, 1));
         F3 sc = RV(ln, "scale", F3(1, 1, 1));
-        rad = F3(irr.x * sc.x, irr.y * sc.y, irr.z * sc.z);  // irradiance.cwiseProduct(scale)
+        F3 irr(1, 1, 1);
+        float aspect = 1 / (float)1;  // Width / Height of the irradiance texture (1 x 1 when constant)
+        const JValue* in = ln->get("irradiance");
+        if (in && in->isObj()) {  // a texture: looked up per sample; radiance holds the scale
+          uint32_t tid = AddTexture(*in, 3, env);
+          L.tex = tid + 1;
+          const TexRec& tr = hs.tex[tid];
+          uint32_t W = tr.kind == TEX_BITMAP ? tr.width : 1u, H = tr.kind == TEX_BITMAP ? tr.height : 1u;
+          aspect = W / (float)H;
+          rad = sc;
+        } else {
+          irr = col("irradiance", F3(1, 1, 1));
+          rad = F3(irr.x * sc.x, irr.y * sc.y, irr.z * sc.z);  // irradiance.cwiseProduct(scale)
+        }
         float fov = RF(ln, "fov", 90.f);
-        float aspect = 1 / (float)1;
         float farZ = 10000, nearZ = 0.0001f;
         M4f persp{}, scale{}, translate = M4f::Identity();
         std::memset(&persp, 0, sizeof(persp));

@@ -96,6 +96,24 @@ def textured_light_room(w=48, h=48, spp=4, seed=1, renderer="path"):
     return sc, {"glow.hdr": imgenc.hdr(img)}
 
 
+def textured_projection_room(w=48, h=48, spp=4, seed=1, renderer="path"):
+    """Box room with a dimmed area light and a projection light whose irradiance
+    is a 16 x 12 PNG slide (aspect 4:3 sets the projector's frustum,
+    projection.cpp:23-39). Returns (scene dict, assets)."""
+    import imgenc
+    yy, xx = np.mgrid[0:12, 0:16]
+    img = np.stack([40 + 200 * (xx // 4 % 2), 60 + 15 * yy, 220 - 12 * xx], axis=2)
+    sc = scenes.box_room(w, h, spp, seed)
+    sc["assets"] = [{"name": "slide", "type": "image_default", "location": "slide.png"}]
+    sc["scene"][-1]["light"]["radiance"] = [2.0, 1.5, 0.5]
+    sc["scene"].append({"to_world": {"translate": [0.2, 1.3, 2.2], "rotate": {"axis": [0, 1, 0], "angle": 180.0}},
+                        "light": {"type": "projection", "fov": 35.0, "scale": [1.5, 1.2, 1.0],
+                                  "irradiance": {"type": "bitmap", "asset_name": "slide", "filter": "bilinear"}}})
+    if renderer != "path":
+        sc["renderer"] = {"type": renderer, "max_depth": 6}
+    return sc, {"slide.png": imgenc.png(img.clip(0, 255))}
+
+
 def textured(dirpath, w=48, h=48, spp=4, seed=1, renderer="path"):
     sc, assets = textured_room_scene(w, h, spp, seed, renderer)
     return write(dirpath, "textured_%s_%dx%d_%d_%d" % (renderer, w, h, spp, seed), sc, assets)

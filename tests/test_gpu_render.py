@@ -137,17 +137,20 @@ def test_bdpt_samples_and_film(rad, oracle, scene_dir, light):
     g.close()
 
 
+@pytest.mark.parametrize("light", ["area", "projection"])
 @pytest.mark.parametrize("renderer", ["path", "vol_path", "bdpt", "particle_tracer"])
-def test_textured_area_light(rad, oracle, scene_dir, renderer):
-    """A bitmap radiance on the emitter rectangle: its texels seen at hits, the
-    luminance distribution behind position samples (light paths), the
+def test_textured_light(rad, oracle, scene_dir, renderer, light):
+    """area: a bitmap radiance on the emitter rectangle: its texels seen at hits,
+    the luminance distribution behind position samples (light paths), the
     reference's zero-density direction samples (no next-event estimation from a
-    bitmap light) and its direction density in the MIS weights."""
-    from helpers import textured_light_room
-    sc, assets = textured_light_room(24, 24, 4, renderer=renderer)
+    bitmap light) and its direction density in the MIS weights. projection: a
+    bitmap slide looked up at the light-space uv of each direction or emitted ray."""
+    from helpers import textured_light_room, textured_projection_room
+    make = textured_light_room if light == "area" else textured_projection_room
+    sc, assets = make(24, 24, 4, renderer=renderer)
     if renderer == "particle_tracer":
         sc["sampler"]["sample_count"] = 60000
-    path, text, d = write(scene_dir, "texlight_" + renderer, sc, assets)
+    path, text, d = write(scene_dir, "texlight_%s_%s" % (light, renderer), sc, assets)
     g, o = rad.Scene.from_file(path), oracle.OracleScene(text, d)
     if renderer == "particle_tracer":
         film = g.render()

@@ -287,6 +287,39 @@ def test_projection_light_footprint(oracle):
     o.close()
 
 
+def test_textured_projection_footprint(oracle, scene_dir):
+    """A bitmap irradiance (an 8 x 4 slide, left half E1, right half E2) sets the
+    projector's aspect (projection.cpp:23-39): the lit footprint is twice as long
+    along one axis as along the other, and inside it the first-hit radiance is
+    R * E(uv) * scale / h^2 with E one of the two halves (nearest filter)."""
+    import imgenc
+    from helpers import write
+    h, fov = 2.0, 40.0
+    E1, E2 = np.array([200, 40, 40]), np.array([20, 60, 220])
+    slide = np.zeros((4, 8, 3), np.int64)
+    slide[:, :4], slide[:, 4:] = E1, E2
+    sc = _direct_light_scene({"to_world": {"translate": [0, h, 0], "rotate": {"axis": [1, 0, 0], "angle": 90.0}},
+                              "light": {"type": "projection", "fov": fov, "scale": [2.0, 2.0, 2.0],
+                                        "irradiance": {"type": "bitmap", "asset_name": "slide",
+                                                       "filter": "nearest"}}})
+    sc["assets"] = [{"name": "slide", "type": "image_default", "location": "slide.png"}]
+    _, text, d = write(scene_dir, "proj_slide", sc, {"slide.png": imgenc.png(slide)})
+    o = oracle.OracleScene(text, d)
+    n = o.width * o.height
+    L = o.render_samples(np.arange(n, dtype=np.uint32), np.zeros(n, np.uint32))
+    P = _plane_hits(o, n)
+    lit = L.sum(axis=1) > 0
+    ext = np.abs(P[lit][:, [0, 2]]).max(axis=0)
+    assert abs(ext.max() / ext.min() - 2.0) < 0.1, ext
+    half = h * math.tan(math.radians(fov / 2))
+    assert abs(ext.max() / half - 1.0) < 0.05, (ext, half)
+    lin = lambda c: np.where(c / 255.0 <= 0.04045, c / 255.0 / 12.92, ((c / 255.0 + 0.055) / 1.055) ** 2.4)
+    want = [0.5 * 2.0 * lin(E) / h ** 2 for E in (E1, E2)]
+    near = [np.isclose(L[lit], w[None], rtol=2e-3).all(axis=1) for w in want]
+    assert (near[0] | near[1]).all() and near[0].sum() > 20 and near[1].sum() > 20
+    o.close()
+
+
 def test_ao_closed_forms(oracle, scene_dir):
     """ao.cpp:22-36: 1 on an open plane, 1/2 next to a (large) wall — every direction
     towards the wall's side of the hemisphere hits it — and 0 for misses."""
