@@ -164,6 +164,37 @@ def test_textured_light(rad, oracle, scene_dir, renderer, light):
     g.close()
 
 
+@pytest.mark.parametrize("case", ["depth0", "depth1", "depth2", "rr0", "nolight", "onlysky"])
+def test_bdpt_edge_cases(rad, oracle, scene_dir, case):
+    """bdpt at the edges of its loops: max_depth 0-2 (the camera subpath stops
+    after its first vertices, connections are not limited by max_depth), Russian
+    roulette from the first bounce, a scene without lights (no light subpath, the
+    reference would index light -1) and a sky as the only light (infinite-light
+    subpaths and their density fix-up)."""
+    sc = scenes.box_room(16, 16, 8)
+    sc["renderer"] = {"type": "bdpt"}
+    if case.startswith("depth"):
+        sc["renderer"]["max_depth"] = int(case[-1])
+    elif case == "rr0":
+        sc["renderer"]["rr_depth"] = 0
+    elif case == "nolight":
+        del sc["scene"][-1]["light"]
+    elif case == "onlysky":
+        del sc["scene"][-1]["light"]
+        sc["scene"][2]["to_world"]["translate"] = [0, 1, -3]  # open the back of the room a little
+        sc["scene"].append({"light": {"type": "skybox", "radiance": [0.8, 0.9, 1.0]}})
+    path, text, d = write(scene_dir, "bdpt_edge_" + case, sc)
+    g, o = rad.Scene.from_file(path), oracle.OracleScene(text, d)
+    frac, lg, lo = _sample_parity(g, o, 8, 0.95)
+    film = g.render()
+    ref = o.render_bdpt()
+    if case == "nolight":
+        assert not lo.any() and not lg.any() and not film.any() and not ref.any()
+    else:
+        assert abs(film.mean() - ref.mean()) < 0.02 * ref.mean(), (film.mean(), ref.mean())
+    g.close()
+
+
 def test_path_samples_lights(rad, oracle, scene_dir):
     """Point and projection lights (delta lights: no MIS weight on their samples) beside
     an area emitter."""

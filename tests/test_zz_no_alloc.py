@@ -50,3 +50,18 @@ def test_noalloc_rejects_oversize(rad, scene_dir):
                                               ctypes.c_void_p(1), None)
     assert st == 1 and "16384" in rad._capi.last_error()
     scene.close()
+
+
+@pytest.mark.parametrize("renderer", ["particle_tracer", "bdpt"])
+def test_noalloc_refuses_splatting_renderers(rad, scene_dir, renderer):
+    """particle_tracer has no per-pixel samples and bdpt needs its allocated
+    subpath scratch: both answer RAD_ERR_UNSUPPORTED before touching the buffers."""
+    from helpers import write
+    from radiantiumplusplus_gb300 import scenes
+    sc = scenes.box_room(8, 8, 1)
+    sc["renderer"] = {"type": renderer}
+    scene = rad.Scene.from_file(write(scene_dir, "noalloc_" + renderer, sc)[0])
+    st = rad.lib().rad_render_samples_noalloc(scene.handle, ctypes.c_void_p(1), ctypes.c_void_p(1), 1, 0,
+                                              ctypes.c_void_p(1), None)
+    assert st == rad._capi.RAD_ERR_UNSUPPORTED
+    scene.close()
