@@ -168,14 +168,17 @@ __global__ void __launch_bounds__(kBdptBlock) KBdptLightFix(DevScene S, BdptBuff
 // which become the scatter cursors.
 __global__ void KBdptKeyScan(BdptBuffers V) {
   const uint32_t nk = (V.cap + 1u) * (V.cap + 1u);
-  uint32_t acc = 0;
+  uint32_t acc = 0, items = 0;
   for (uint32_t k = 0; k < nk; k++) {
-    uint32_t c = V.keyFill[k];
+    uint32_t c = V.keyFill[k], nl = k % (V.cap + 1u);
     V.keyStart[k] = acc;
+    V.itemStart[k] = items;
     V.keyFill[k] = acc;
     acc += c;
+    items += nl > 1u ? c * (nl - 1u) : 0u;
   }
   V.keyStart[nk] = acc;
+  V.itemStart[nk] = items;
 }
 
 __global__ void __launch_bounds__(kBdptBlock) KBdptKeyScatter(BdptBuffers V, uint32_t count) {
@@ -224,6 +227,81 @@ __global__ void __launch_bounds__(kBdptBlock)
     }
     B.L[p] = make_float4(acc.x, acc.y, acc.z, 0.f);
     StoreRng(B, p, rng);
+  }
+}
+
+// Queues the visibility ray of connection `o` of sample p (round t).
+__device__ __forceinline__ void EmitConnection(const DevScene& S, const BdptBuffers& V, uint32_t* nsh, uint32_t* err,
+                                               uint32_t p, const ConnOut& o, bool splats) {
+  uint32_t tag = p;
+  if (o.splat) {
+    if (!splats) return;
+    int x = (int)o.pixel.x, y = (int)o.pixel.y;
+    if (x < 0 || y < 0 || x >= S.cam.width || y >= S.cam.height) return;
+    tag = 0x80000000u | (uint32_t)(y * S.cam.width + x);
+  }
+  V3 ro, rd;
+  float tmax;
+  if (!ShadowRay(o.P, o.N, o.target, ro, rd, tmax)) return;
+  uint32_t slot = atomicAdd(nsh, 1u);
+  if (slot >= V.shCap) {
+    atomicOr(err, 8u);  // more visibility rays than the round's buffer holds
+    return;
+  }
+  V.shO[slot] = make_float4(ro.x, ro.y, ro.z, tmax);
+  V.shD[slot] = make_float4(rd.x, rd.y, rd.z, __uint_as_float(tag));
+  V.shC[slot] = make_float4(o.c.x, o.c.y, o.c.z, 0.f);
+}
+
+// Round t >= 2, the s = 0 and s = 1 connections of each sample of the suffix
+// (the only ones of the round that draw random numbers: s = 1's light sample).
+__global__ void __launch_bounds__(kBdptBlock) KBdptConnectHead(DevScene S, PathBuffers B, BdptBuffers V, uint32_t count,
+                                                              int t) {
+  uint32_t* nsh = B.counters + kShadowBase + (t - 1);
+  uint32_t* err = B.counters + kMiscBase + 1;
+  const uint32_t first = V.keyStart[(uint32_t)t * (V.cap + 1u)];
+  for (uint32_t j = first + blockIdx.x * blockDim.x + threadIdx.x; j < count; j += gridDim.x * blockDim.x) {
+    const uint32_t p = V.order[j];
+    const int nl = (int)V.nLight[p];
+    Pcg32 rng = LoadRng(B, p);
+    VPath cam = CamPath(V, p), lig = LightPathOf(V, p);
+    float4 L4 = B.L[p];
+    V3 acc{L4.x, L4.y, L4.z};
+    for (int s = 0; s <= nl && s <= 1; ++s) {
+      ConnOut o;
+      if (!ConnectBdpt(S, rng, lig, cam, s, t, o)) continue;
+      if (!o.vis)
+        acc = acc + o.c;
+      else
+        EmitConnection(S, V, nsh, err, p, o, true);
+    }
+    B.L[p] = make_float4(acc.x, acc.y, acc.z, 0.f);
+    StoreRng(B, p, rng);
+  }
+}
+
+// Round t >= 2, the s >= 2 connections, one per thread: item g of the round is
+// found by a binary search over the per-key item starts (samples of one key
+// have the same light subpath length nl, hence nl - 1 such connections).
+__global__ void __launch_bounds__(kBdptBlock) KBdptConnectTail(DevScene S, PathBuffers B, BdptBuffers V, int t) {
+  uint32_t* nsh = B.counters + kShadowBase + (t - 1);
+  uint32_t* err = B.counters + kMiscBase + 1;
+  const uint32_t c1 = V.cap + 1u, nk = c1 * c1;
+  const uint32_t k0 = (uint32_t)t * c1;
+  const uint32_t g0 = V.itemStart[k0], g1 = V.itemStart[nk];
+  for (uint32_t g = g0 + blockIdx.x * blockDim.x + threadIdx.x; g < g1; g += gridDim.x * blockDim.x) {
+    uint32_t lo = k0, hi = nk;  // the last key with itemStart <= g
+    while (hi - lo > 1u) {
+      uint32_t mid = (lo + hi) >> 1;
+      if (V.itemStart[mid] <= g) lo = mid; else hi = mid;
+    }
+    const uint32_t nl = lo % c1, local = g - V.itemStart[lo];
+    const uint32_t p = V.order[V.keyStart[lo] + local / (nl - 1u)];
+    const int s = 2 + (int)(local % (nl - 1u));
+    Pcg32 rng;  // these connections draw no random numbers
+    rng.state = 0;
+    ConnOut o;
+    if (ConnectBdpt(S, rng, LightPathOf(V, p), CamPath(V, p), s, t, o)) EmitConnection(S, V, nsh, err, p, o, true);
   }
 }
 
@@ -359,6 +437,13 @@ cudaError_t LaunchBdptConnect(const DevScene& S, const PathBuffers& B, const Bdp
                               bool splats, int grid, cudaStream_t st) {
   if (count == 0) return cudaSuccess;
   KBdptConnect<<<GridFor(count, grid), kBdptBlock, 0, st>>>(S, B, V, count, t, splats);
+  return cudaGetLastError();
+}
+cudaError_t LaunchBdptConnectSplit(const DevScene& S, const PathBuffers& B, const BdptBuffers& V, uint32_t count,
+                                   int t, int grid, cudaStream_t st) {
+  if (count == 0) return cudaSuccess;
+  KBdptConnectHead<<<GridFor(count, grid), kBdptBlock, 0, st>>>(S, B, V, count, t);
+  KBdptConnectTail<<<grid, kBdptBlock, 0, st>>>(S, B, V, t);
   return cudaGetLastError();
 }
 cudaError_t LaunchBdptShadow(const DevScene& S, const PathBuffers& B, const BdptBuffers& V, int t, float4* film,

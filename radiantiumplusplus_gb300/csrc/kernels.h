@@ -123,6 +123,7 @@ struct BdptBuffers {
   uint32_t* order;     // nw sample slots
   uint32_t* keyStart;  // (cap + 1)^2 + 1: first slot of each key (exclusive scan of the key counts)
   uint32_t* keyFill;   // (cap + 1)^2: per-key counts, then scatter cursors
+  uint32_t* itemStart; // (cap + 1)^2 + 1: exclusive scan over keys of the s >= 2 connections (nl - 1 a sample)
   uint32_t cap, nw, shCap;
 };
 // Camera subpaths: jittered camera rays of the wave's samples into queue 0.
@@ -142,6 +143,10 @@ cudaError_t LaunchBdptLightFix(const DevScene& S, const BdptBuffers& V, uint32_t
 // into B.L, visibility rays into V.sh* (count in B.counters[kShadowBase + t - 1]); splats only with `splats`.
 cudaError_t LaunchBdptConnect(const DevScene& S, const PathBuffers& B, const BdptBuffers& V, uint32_t count, int t,
                               bool splats, int grid, cudaStream_t st);
+// Round t >= 2 with splats enabled, split: s = 0 / 1 per sample (they draw the round's random
+// numbers), then the s >= 2 connections one per thread.
+cudaError_t LaunchBdptConnectSplit(const DevScene& S, const PathBuffers& B, const BdptBuffers& V, uint32_t count,
+                                   int t, int grid, cudaStream_t st);
 // Visibility rays of round t: unoccluded contributions into B.L (atomic) or the film (splats).
 cudaError_t LaunchBdptShadow(const DevScene& S, const PathBuffers& B, const BdptBuffers& V, int t, float4* film,
                              int grid, cudaStream_t st, int refillBusy, int leafFrac8);

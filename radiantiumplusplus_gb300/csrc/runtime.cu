@@ -309,6 +309,7 @@ const BdptBuffers& EnsureBdpt(int cap) {
   V.order = DevAlloc<uint32_t>(nw, o, b);
   V.keyStart = DevAlloc<uint32_t>((size_t)(cap + 1) * (cap + 1) + 1, o, b);
   V.keyFill = DevAlloc<uint32_t>((size_t)(cap + 1) * (cap + 1), o, b);
+  V.itemStart = DevAlloc<uint32_t>((size_t)(cap + 1) * (cap + 1) + 1, o, b);
   V.cap = (uint32_t)cap;
   V.nw = nw;
   lib.bdpt = V;
@@ -384,12 +385,15 @@ uint64_t RunBdptWave(const DevScene& S, const TraceTune& tu, const WaveParams& w
   int tgrid = std::max(1, std::min(lib.sms * tu.blocksPerSm, (int)((count + 127) / 128)));
   for (int t = 1; t <= (int)maxCam && t <= cap; t++) {
     ps.Begin(2, a);
-    Check(LaunchBdptConnect(S, B, V, count, t, film.accum != nullptr, grid, lib.stream), "bdpt connect");
+    if (t >= 2)
+      Check(LaunchBdptConnectSplit(S, B, V, count, t, grid, lib.stream), "bdpt connect");
+    else
+      Check(LaunchBdptConnect(S, B, V, count, t, film.accum != nullptr, grid, lib.stream), "bdpt connect");
     ps.End(2, a);
     ps.Begin(3, a);
     Check(LaunchBdptShadow(S, B, V, t, film.accum, tgrid, lib.stream, tu.refillBusy, tu.leafFrac8), "bdpt shadow");
     ps.End(3, a);
-    launches += 2;
+    launches += t >= 2 ? 3 : 2;
   }
   ps.Begin(4, a);
   Check(LaunchBdptAccumulate(B, film, count, out, lib.stream), "bdpt accumulate");
