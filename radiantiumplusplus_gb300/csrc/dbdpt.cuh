@@ -498,6 +498,16 @@ RDN float MISWeight(const DevScene& S, VPath lightV, VPath camV, const BVert& sa
   return 1.f / (1.f + sumRi);
 }
 
+// Random numbers the t = 1 connections (s = 2 .. sEnd - 1) draw before
+// connection sEnd: Perspective::SampleDirection's 2D sample for each light
+// vertex s - 1 that can connect (ConnectBdpt, bdpt.cpp:500-503).
+RD uint64_t Round1Draws(const DevScene& S, VPath lightV, int sEnd) {
+  uint64_t n = 0;
+  for (int s = 2; s < sEnd; ++s)
+    if (VConnectible(S, lightV[s - 1])) n += 2u;
+  return n;
+}
+
 // One connection's result: contribution c (MIS-weighted); with `vis`, it
 // counts only if the segment from (P, N) to `target` is unoccluded
 // (Scene::IsOcclude, scene.cpp:53-63); `splat` connections (t = 1) land on

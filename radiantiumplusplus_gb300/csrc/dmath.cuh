@@ -195,6 +195,21 @@ RD Pcg32 PcgForSample(uint32_t pixel, uint32_t sample, uint32_t seed) {
   PcgNext(r);
   return r;
 }
+// Advances the stream by `delta` draws in O(log delta) (Brown, "Random Number
+// Generation with Arbitrary Strides", 1994: the LCG's k-step map is again affine).
+RD void PcgAdvance(Pcg32& r, uint64_t delta) {
+  uint64_t curMult = 6364136223846793005ULL, curPlus = 1442695040888963407ULL, accMult = 1u, accPlus = 0u;
+  while (delta) {
+    if (delta & 1u) {
+      accMult *= curMult;
+      accPlus = accPlus * curMult + curPlus;
+    }
+    curPlus = (curMult + 1u) * curPlus;
+    curMult *= curMult;
+    delta >>= 1;
+  }
+  r.state = accMult * r.state + accPlus;
+}
 RD float Next1D(Pcg32& r) { return (float)(PcgNext(r) >> 8) * 5.9604644775390625e-08f; }
 RD V2 Next2D(Pcg32& r) {
   float a = Next1D(r);

@@ -3,12 +3,15 @@
 //   camera subpaths: KBdptCamera, then per bounce the BVH8 closest-hit kernel
 //     (KExtend) and KBdptWalk;
 //   light subpaths: KBdptLight, the same bounce loop, KBdptLightFix;
-//   connections, one round per camera vertex index t: KBdptConnect evaluates
-//     every (s, t) connection of each sample in the reference's order (so the
-//     sample's random numbers are drawn in that order) and queues the
-//     visibility rays; KBdptShadow traces them with the persistent any-hit
-//     traversal and adds the unoccluded contributions (atomics: a sample has
-//     several) to the sample or, for t = 1, to the film pixel they land on;
+//   connections, one round per camera vertex index t, over the samples ordered
+//     by subpath lengths: round 1 (t = 1, splats) one thread per connection,
+//     each starting from the sample's stream advanced past the draws of the
+//     connections before it; rounds t >= 2 the s <= 1 connections per sample
+//     (s = 1 draws the round's random numbers) and the s >= 2 ones one per
+//     thread. Every connection queues its visibility ray; KBdptShadow traces
+//     them with the persistent any-hit traversal and adds the unoccluded
+//     contributions (atomics: a sample has several) to the sample or, for
+//     t = 1, to the film pixel they land on;
 //   KBdptAccumulate adds each valid sample into the film.
 #include <algorithm>
 
@@ -186,50 +189,6 @@ __global__ void __launch_bounds__(kBdptBlock) KBdptKeyScatter(BdptBuffers V, uin
     V.order[atomicAdd(V.keyFill + SortKey(V, i), 1u)] = i;
 }
 
-__global__ void __launch_bounds__(kBdptBlock)
-    KBdptConnect(DevScene S, PathBuffers B, BdptBuffers V, uint32_t count, int t, bool splats) {
-  uint32_t* nsh = B.counters + kShadowBase + (t - 1);
-  uint32_t* err = B.counters + kMiscBase + 1;
-  const uint32_t first = V.keyStart[(uint32_t)t * (V.cap + 1u)];  // samples with nc < t come first
-  for (uint32_t j = first + blockIdx.x * blockDim.x + threadIdx.x; j < count; j += gridDim.x * blockDim.x) {
-    const uint32_t p = V.order[j];
-    const int nl = (int)V.nLight[p];
-    Pcg32 rng = LoadRng(B, p);
-    VPath cam = CamPath(V, p), lig = LightPathOf(V, p);
-    float4 L4 = B.L[p];
-    V3 acc{L4.x, L4.y, L4.z};
-    for (int s = 0; s <= nl; ++s) {
-      if ((s == 1 && t == 1) || t + s - 2 < 0) continue;
-      ConnOut o;
-      if (!ConnectBdpt(S, rng, lig, cam, s, t, o)) continue;
-      if (!o.vis) {
-        acc = acc + o.c;
-        continue;
-      }
-      uint32_t tag = p;
-      if (o.splat) {
-        if (!splats) continue;
-        int x = (int)o.pixel.x, y = (int)o.pixel.y;
-        if (x < 0 || y < 0 || x >= S.cam.width || y >= S.cam.height) continue;
-        tag = 0x80000000u | (uint32_t)(y * S.cam.width + x);
-      }
-      V3 ro, rd;
-      float tmax;
-      if (!ShadowRay(o.P, o.N, o.target, ro, rd, tmax)) continue;
-      uint32_t slot = atomicAdd(nsh, 1u);
-      if (slot >= V.shCap) {
-        atomicOr(err, 8u);  // more visibility rays than the round's buffer holds
-        continue;
-      }
-      V.shO[slot] = make_float4(ro.x, ro.y, ro.z, tmax);
-      V.shD[slot] = make_float4(rd.x, rd.y, rd.z, __uint_as_float(tag));
-      V.shC[slot] = make_float4(o.c.x, o.c.y, o.c.z, 0.f);
-    }
-    B.L[p] = make_float4(acc.x, acc.y, acc.z, 0.f);
-    StoreRng(B, p, rng);
-  }
-}
-
 // Queues the visibility ray of connection `o` of sample p (round t).
 __device__ __forceinline__ void EmitConnection(const DevScene& S, const BdptBuffers& V, uint32_t* nsh, uint32_t* err,
                                                uint32_t p, const ConnOut& o, bool splats) {
@@ -302,6 +261,45 @@ __global__ void __launch_bounds__(kBdptBlock) KBdptConnectTail(DevScene S, PathB
     rng.state = 0;
     ConnOut o;
     if (ConnectBdpt(S, rng, LightPathOf(V, p), CamPath(V, p), s, t, o)) EmitConnection(S, V, nsh, err, p, o, true);
+  }
+}
+
+// Round t = 1, per sample: keep the stream's state for the connections and
+// advance the sample's stream past all of them.
+__global__ void __launch_bounds__(kBdptBlock) KBdptRound1Head(DevScene S, PathBuffers B, BdptBuffers V, uint32_t count) {
+  for (uint32_t p = blockIdx.x * blockDim.x + threadIdx.x; p < count; p += gridDim.x * blockDim.x) {
+    const int nl = (int)V.nLight[p];
+    uint2 st = B.rng[p];
+    V.rng1[p] = st;
+    Pcg32 rng = LoadRng(B, p);
+    PcgAdvance(rng, Round1Draws(S, LightPathOf(V, p), nl + 1));
+    StoreRng(B, p, rng);
+  }
+}
+
+// Round t = 1, one thread per connection (s >= 2, the only ones of the round).
+__global__ void __launch_bounds__(kBdptBlock) KBdptRound1Tail(DevScene S, PathBuffers B, BdptBuffers V) {
+  uint32_t* nsh = B.counters + kShadowBase;
+  uint32_t* err = B.counters + kMiscBase + 1;
+  const uint32_t c1 = V.cap + 1u, nk = c1 * c1;
+  const uint32_t k0 = c1;  // every sample has a camera vertex
+  const uint32_t g0 = V.itemStart[k0], g1 = V.itemStart[nk];
+  for (uint32_t g = g0 + blockIdx.x * blockDim.x + threadIdx.x; g < g1; g += gridDim.x * blockDim.x) {
+    uint32_t lo = k0, hi = nk;
+    while (hi - lo > 1u) {
+      uint32_t mid = (lo + hi) >> 1;
+      if (V.itemStart[mid] <= g) lo = mid; else hi = mid;
+    }
+    const uint32_t nl = lo % c1, local = g - V.itemStart[lo];
+    const uint32_t p = V.order[V.keyStart[lo] + local / (nl - 1u)];
+    const int s = 2 + (int)(local % (nl - 1u));
+    VPath lig = LightPathOf(V, p);
+    uint2 st = V.rng1[p];
+    Pcg32 rng;
+    rng.state = (uint64_t)st.x | ((uint64_t)st.y << 32);
+    PcgAdvance(rng, Round1Draws(S, lig, s));
+    ConnOut o;
+    if (ConnectBdpt(S, rng, lig, CamPath(V, p), s, 1, o)) EmitConnection(S, V, nsh, err, p, o, true);
   }
 }
 
@@ -433,17 +431,18 @@ cudaError_t LaunchBdptLightFix(const DevScene& S, const BdptBuffers& V, uint32_t
   KBdptKeyScatter<<<GridFor(count, 1 << 16), kBdptBlock, 0, st>>>(V, count);
   return cudaGetLastError();
 }
-cudaError_t LaunchBdptConnect(const DevScene& S, const PathBuffers& B, const BdptBuffers& V, uint32_t count, int t,
-                              bool splats, int grid, cudaStream_t st) {
-  if (count == 0) return cudaSuccess;
-  KBdptConnect<<<GridFor(count, grid), kBdptBlock, 0, st>>>(S, B, V, count, t, splats);
-  return cudaGetLastError();
-}
 cudaError_t LaunchBdptConnectSplit(const DevScene& S, const PathBuffers& B, const BdptBuffers& V, uint32_t count,
                                    int t, int grid, cudaStream_t st) {
   if (count == 0) return cudaSuccess;
   KBdptConnectHead<<<GridFor(count, grid), kBdptBlock, 0, st>>>(S, B, V, count, t);
   KBdptConnectTail<<<grid, kBdptBlock, 0, st>>>(S, B, V, t);
+  return cudaGetLastError();
+}
+cudaError_t LaunchBdptRound1(const DevScene& S, const PathBuffers& B, const BdptBuffers& V, uint32_t count,
+                             bool splats, int grid, cudaStream_t st) {
+  if (count == 0) return cudaSuccess;
+  KBdptRound1Head<<<GridFor(count, grid), kBdptBlock, 0, st>>>(S, B, V, count);
+  if (splats) KBdptRound1Tail<<<grid, kBdptBlock, 0, st>>>(S, B, V);
   return cudaGetLastError();
 }
 cudaError_t LaunchBdptShadow(const DevScene& S, const PathBuffers& B, const BdptBuffers& V, int t, float4* film,

@@ -124,6 +124,7 @@ struct BdptBuffers {
   uint32_t* keyStart;  // (cap + 1)^2 + 1: first slot of each key (exclusive scan of the key counts)
   uint32_t* keyFill;   // (cap + 1)^2: per-key counts, then scatter cursors
   uint32_t* itemStart; // (cap + 1)^2 + 1: exclusive scan over keys of the s >= 2 connections (nl - 1 a sample)
+  uint2* rng1;         // per sample: PCG state before connection round t = 1
   uint32_t cap, nw, shCap;
 };
 // Camera subpaths: jittered camera rays of the wave's samples into queue 0.
@@ -139,14 +140,16 @@ cudaError_t LaunchBdptWalk(const DevScene& S, const PathBuffers& B, const BdptBu
 // Infinite-light fix-up of the light subpaths, then the samples' order by subpath lengths
 // (V.keyFill zeroed beforehand).
 cudaError_t LaunchBdptLightFix(const DevScene& S, const BdptBuffers& V, uint32_t count, cudaStream_t st);
-// The connections of camera vertex t - 1 of every sample (all light vertices): direct contributions
-// into B.L, visibility rays into V.sh* (count in B.counters[kShadowBase + t - 1]); splats only with `splats`.
-cudaError_t LaunchBdptConnect(const DevScene& S, const PathBuffers& B, const BdptBuffers& V, uint32_t count, int t,
-                              bool splats, int grid, cudaStream_t st);
-// Round t >= 2 with splats enabled, split: s = 0 / 1 per sample (they draw the round's random
-// numbers), then the s >= 2 connections one per thread.
+// Round t >= 2 of the connections (camera vertex t - 1 with every light vertex): s = 0 / 1 per
+// sample (s = 1 draws the round's random numbers; s = 0 adds into B.L directly), then the s >= 2
+// ones one per thread; visibility rays into V.sh* (count in B.counters[kShadowBase + t - 1]).
 cudaError_t LaunchBdptConnectSplit(const DevScene& S, const PathBuffers& B, const BdptBuffers& V, uint32_t count,
                                    int t, int grid, cudaStream_t st);
+// Round t = 1 (splats), one thread per connection: each starts from the sample's stream advanced past the
+// draws of the connections before it; the sample's stream is advanced past them all. Without splats
+// only the advance runs.
+cudaError_t LaunchBdptRound1(const DevScene& S, const PathBuffers& B, const BdptBuffers& V, uint32_t count,
+                             bool splats, int grid, cudaStream_t st);
 // Visibility rays of round t: unoccluded contributions into B.L (atomic) or the film (splats).
 cudaError_t LaunchBdptShadow(const DevScene& S, const PathBuffers& B, const BdptBuffers& V, int t, float4* film,
                              int grid, cudaStream_t st, int refillBusy, int leafFrac8);

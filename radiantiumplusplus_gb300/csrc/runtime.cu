@@ -291,7 +291,7 @@ const BdptBuffers& EnsureBdpt(int cap) {
   FreeAll(lib.bdptAllocs);
   lib.used -= lib.bdptBytes;
   lib.bdptBytes = 0;
-  uint64_t per = 2ull * cap * kBVertBytes + (uint64_t)cap * 3 * sizeof(float4) + 3 * sizeof(float4) + 12;
+  uint64_t per = 2ull * cap * kBVertBytes + (uint64_t)cap * 3 * sizeof(float4) + 3 * sizeof(float4) + 20;
   uint32_t nw = (uint32_t)std::min<uint64_t>(lib.maxPaths, std::max<uint64_t>(1024, kBdptScratchBytes / per));
   BdptBuffers V{};
   auto& o = lib.bdptAllocs;
@@ -310,6 +310,7 @@ const BdptBuffers& EnsureBdpt(int cap) {
   V.keyStart = DevAlloc<uint32_t>((size_t)(cap + 1) * (cap + 1) + 1, o, b);
   V.keyFill = DevAlloc<uint32_t>((size_t)(cap + 1) * (cap + 1), o, b);
   V.itemStart = DevAlloc<uint32_t>((size_t)(cap + 1) * (cap + 1) + 1, o, b);
+  V.rng1 = DevAlloc<uint2>(nw, o, b);
   V.cap = (uint32_t)cap;
   V.nw = nw;
   lib.bdpt = V;
@@ -388,12 +389,12 @@ uint64_t RunBdptWave(const DevScene& S, const TraceTune& tu, const WaveParams& w
     if (t >= 2)
       Check(LaunchBdptConnectSplit(S, B, V, count, t, grid, lib.stream), "bdpt connect");
     else
-      Check(LaunchBdptConnect(S, B, V, count, t, film.accum != nullptr, grid, lib.stream), "bdpt connect");
+      Check(LaunchBdptRound1(S, B, V, count, film.accum != nullptr, grid, lib.stream), "bdpt connect");
     ps.End(2, a);
     ps.Begin(3, a);
     Check(LaunchBdptShadow(S, B, V, t, film.accum, tgrid, lib.stream, tu.refillBusy, tu.leafFrac8), "bdpt shadow");
     ps.End(3, a);
-    launches += t >= 2 ? 3 : 2;
+    launches += 3;
   }
   ps.Begin(4, a);
   Check(LaunchBdptAccumulate(B, film, count, out, lib.stream), "bdpt accumulate");
