@@ -119,15 +119,16 @@ __global__ void __launch_bounds__(kBdptBlock) KBdptLight(DevScene S, PathBuffers
 
 template <bool LIGHT>
 __global__ void __launch_bounds__(kBdptBlock) KBdptWalk(DevScene S, PathBuffers B, BdptBuffers V, int depth) {
-  const uint32_t count = B.counters[depth];
-  const uint32_t* qin = B.q[depth & 1];
+  uint32_t start[kShadeClasses + 1];  // the hits class by class (neighbours sample the same kind of BSDF)
+  ClassQueueStarts(B, depth, start);
+  const uint32_t count = start[kShadeClasses];
   uint32_t* maxCam = B.counters + kMiscBase;
   for (uint32_t base = blockIdx.x * blockDim.x; base < count; base += gridDim.x * blockDim.x) {
     const uint32_t i = base + threadIdx.x;
     bool push = false;
     uint32_t p = 0;
     if (i < count) {
-      p = qin[i];
+      p = ClassQueueEntry(B, start, i);
       Pcg32 rng = LoadRng(B, p);
       WalkState ws = LoadWalk(V, p);
       float4 o4 = B.rayO[p], d4 = B.rayD[p];

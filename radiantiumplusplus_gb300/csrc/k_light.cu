@@ -52,18 +52,20 @@ __global__ void __launch_bounds__(128) KParticleStart(DevScene S, PathBuffers B,
   }
 }
 
-// Bounce d of the queued light paths (after the closest-hit kernel): camera
-// connection into visibility round d + 1, next ray into the next queue.
+// Bounce d of the queued light paths (after the closest-hit kernel, taken class
+// by class from its shade-class queues): camera connection into visibility
+// round d + 1, next ray into the next queue.
 __global__ void __launch_bounds__(128) KParticleBounce(DevScene S, PathBuffers B, int d, float sampleScale) {
-  const uint32_t count = B.counters[d];
-  const uint32_t* qin = B.q[d & 1];
+  uint32_t start[kShadeClasses + 1];
+  ClassQueueStarts(B, d, start);
+  const uint32_t count = start[kShadeClasses];
   uint32_t* nsh = B.counters + kShadowBase + d + 1;
   for (uint32_t base = blockIdx.x * blockDim.x; base < count; base += gridDim.x * blockDim.x) {
     const uint32_t i = base + threadIdx.x;
     bool push = false;
     uint32_t p = 0;
     if (i < count) {
-      p = qin[i];
+      p = ClassQueueEntry(B, start, i);
       uint2 rs = B.rng[p];
       Pcg32 rng;
       rng.state = (uint64_t)rs.x | ((uint64_t)rs.y << 32);

@@ -40,6 +40,23 @@ constexpr int kClassBase = kMiscBase + 8;
 constexpr int kFetchBase = kClassBase + (kMaxBounce + 1) * kShadeClasses;
 constexpr int kCounterWords = kFetchBase + 2 * (kMaxBounce + 1);
 
+#if defined(__CUDACC__)
+// Entry i of bounce `depth`'s hits taken class by class from the shade-class
+// queues the closest-hit kernel fills (each queued path appears in exactly one),
+// so that neighbouring threads shade the same kind of material. `start` holds
+// the classes' prefix sums (ClassQueueStarts).
+__device__ __forceinline__ void ClassQueueStarts(const PathBuffers& B, int depth, uint32_t* start) {
+  const uint32_t* cc = B.counters + kClassBase + depth * kShadeClasses;
+  start[0] = 0;
+  for (int c = 0; c < kShadeClasses; c++) start[c + 1] = start[c] + cc[c];
+}
+__device__ __forceinline__ uint32_t ClassQueueEntry(const PathBuffers& B, const uint32_t* start, uint32_t i) {
+  int c = 0;
+  while (c + 1 < kShadeClasses && i >= start[c + 1]) c++;
+  return B.classQ[(size_t)c * B.capacity + (i - start[c])];
+}
+#endif
+
 struct FilmView {
   float4* accum;  // rgb sum, sample count in w
   int32_t width, height;
