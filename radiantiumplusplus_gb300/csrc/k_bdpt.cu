@@ -240,28 +240,88 @@ __global__ void __launch_bounds__(kBdptBlock) KBdptConnectHead(DevScene S, PathB
   }
 }
 
-// Round t >= 2, the s >= 2 connections, one per thread: item g of the round is
-// found by a binary search over the per-key item starts (samples of one key
-// have the same light subpath length nl, hence nl - 1 such connections).
+// The s >= 2 connections of round t, item g (counted over the samples with
+// at least t camera vertices): a binary search over the per-key item starts
+// (samples of one key have the same light subpath length nl, hence nl - 1
+// such connections) gives the sample and s.
+RD void RoundItem(const BdptBuffers& V, uint32_t k0, uint32_t g, uint32_t& p, int& s) {
+  const uint32_t c1 = V.cap + 1u, nk = c1 * c1;
+  uint32_t lo = k0, hi = nk;  // the last key with itemStart <= g
+  while (hi - lo > 1u) {
+    uint32_t mid = (lo + hi) >> 1;
+    if (V.itemStart[mid] <= g) lo = mid; else hi = mid;
+  }
+  const uint32_t nl = lo % c1, local = g - V.itemStart[lo];
+  p = V.order[V.keyStart[lo] + local / (nl - 1u)];
+  s = 2 + (int)(local % (nl - 1u));
+}
+RD uint32_t VClass(const DevScene& S, const BVert& v) { return v.type == BV_SURFACE ? S.shapeClass[v.id] : 0u; }
+// Bucket of connection (p, s) of round t: the shade classes of its camera and light vertices.
+RD uint32_t ItemBucket(const DevScene& S, const BdptBuffers& V, uint32_t p, int s, int t) {
+  return VClass(S, CamPath(V, p)[t - 1]) * (uint32_t)kShadeClasses + VClass(S, LightPathOf(V, p)[s - 1]);
+}
+
+// Round t's s >= 2 connections counted per bucket (pass 0) or scattered into
+// V.items bucket by bucket (pass 1), with warp-aggregated atomics.
+__global__ void __launch_bounds__(kBdptBlock) KBdptItemSort(DevScene S, BdptBuffers V, int t, int pass) {
+  const uint32_t c1 = V.cap + 1u, nk = c1 * c1;
+  const uint32_t k0 = (uint32_t)t * c1;
+  const uint32_t g0 = V.itemStart[k0], n = V.itemStart[nk] - g0;
+  const uint32_t lane = threadIdx.x & 31u;
+  uint32_t* cnt = V.bucket + (pass == 0 ? 0 : 2 * kBdptBuckets);
+  for (uint32_t base = blockIdx.x * blockDim.x; base < n; base += gridDim.x * blockDim.x) {
+    const uint32_t j = base + threadIdx.x;
+    const bool ok = j < n;
+    uint32_t p = 0, key = 0xffffffffu;
+    int s = 0;
+    if (ok) {
+      RoundItem(V, k0, g0 + j, p, s);
+      key = ItemBucket(S, V, p, s, t);
+    }
+    const uint32_t grp = __match_any_sync(0xffffffffu, key);
+    const int leader = __ffs(grp) - 1;
+    uint32_t slot = 0;
+    if (ok && (int)lane == leader) slot = atomicAdd(cnt + key, (uint32_t)__popc(grp));
+    slot = __shfl_sync(0xffffffffu, slot, leader);
+    if (ok && pass == 1) V.items[slot + __popc(grp & ((1u << lane) - 1u))] = p | ((uint32_t)s << 24);
+  }
+}
+// Bucket starts (exclusive scan of the counts, copied into the scatter cursors);
+// zeroes the counts for the next round.
+__global__ void KBdptItemScan(BdptBuffers V) {
+  uint32_t acc = 0;
+  for (int b = 0; b < kBdptBuckets; b++) {
+    uint32_t c = V.bucket[b];
+    V.bucket[kBdptBuckets + b] = acc;
+    V.bucket[2 * kBdptBuckets + b] = acc;
+    V.bucket[b] = 0;
+    acc += c;
+  }
+  V.bucket[3 * kBdptBuckets] = acc;
+}
+
+// Round t's s >= 2 connections, one per thread in bucket order (t >= 2: no
+// random numbers; t = 1: each starts from the sample's stream advanced past the
+// draws of the connections before it).
 __global__ void __launch_bounds__(kBdptBlock) KBdptConnectTail(DevScene S, PathBuffers B, BdptBuffers V, int t) {
   uint32_t* nsh = B.counters + kShadowBase + (t - 1);
   uint32_t* err = B.counters + kMiscBase + 1;
   const uint32_t c1 = V.cap + 1u, nk = c1 * c1;
-  const uint32_t k0 = (uint32_t)t * c1;
-  const uint32_t g0 = V.itemStart[k0], g1 = V.itemStart[nk];
-  for (uint32_t g = g0 + blockIdx.x * blockDim.x + threadIdx.x; g < g1; g += gridDim.x * blockDim.x) {
-    uint32_t lo = k0, hi = nk;  // the last key with itemStart <= g
-    while (hi - lo > 1u) {
-      uint32_t mid = (lo + hi) >> 1;
-      if (V.itemStart[mid] <= g) lo = mid; else hi = mid;
+  const uint32_t n = V.itemStart[nk] - V.itemStart[(uint32_t)t * c1];
+  for (uint32_t j = blockIdx.x * blockDim.x + threadIdx.x; j < n; j += gridDim.x * blockDim.x) {
+    const uint32_t it = V.items[j];
+    const uint32_t p = it & 0xffffffu;
+    const int s = (int)(it >> 24);
+    VPath lig = LightPathOf(V, p);
+    Pcg32 rng;
+    rng.state = 0;  // rounds t >= 2: these connections draw no random numbers
+    if (t == 1) {
+      uint2 st = V.rng1[p];
+      rng.state = (uint64_t)st.x | ((uint64_t)st.y << 32);
+      PcgAdvance(rng, Round1Draws(S, lig, s));
     }
-    const uint32_t nl = lo % c1, local = g - V.itemStart[lo];
-    const uint32_t p = V.order[V.keyStart[lo] + local / (nl - 1u)];
-    const int s = 2 + (int)(local % (nl - 1u));
-    Pcg32 rng;  // these connections draw no random numbers
-    rng.state = 0;
     ConnOut o;
-    if (ConnectBdpt(S, rng, LightPathOf(V, p), CamPath(V, p), s, t, o)) EmitConnection(S, V, nsh, err, p, o, true);
+    if (ConnectBdpt(S, rng, lig, CamPath(V, p), s, t, o)) EmitConnection(S, V, nsh, err, p, o, true);
   }
 }
 
@@ -275,32 +335,6 @@ __global__ void __launch_bounds__(kBdptBlock) KBdptRound1Head(DevScene S, PathBu
     Pcg32 rng = LoadRng(B, p);
     PcgAdvance(rng, Round1Draws(S, LightPathOf(V, p), nl + 1));
     StoreRng(B, p, rng);
-  }
-}
-
-// Round t = 1, one thread per connection (s >= 2, the only ones of the round).
-__global__ void __launch_bounds__(kBdptBlock) KBdptRound1Tail(DevScene S, PathBuffers B, BdptBuffers V) {
-  uint32_t* nsh = B.counters + kShadowBase;
-  uint32_t* err = B.counters + kMiscBase + 1;
-  const uint32_t c1 = V.cap + 1u, nk = c1 * c1;
-  const uint32_t k0 = c1;  // every sample has a camera vertex
-  const uint32_t g0 = V.itemStart[k0], g1 = V.itemStart[nk];
-  for (uint32_t g = g0 + blockIdx.x * blockDim.x + threadIdx.x; g < g1; g += gridDim.x * blockDim.x) {
-    uint32_t lo = k0, hi = nk;
-    while (hi - lo > 1u) {
-      uint32_t mid = (lo + hi) >> 1;
-      if (V.itemStart[mid] <= g) lo = mid; else hi = mid;
-    }
-    const uint32_t nl = lo % c1, local = g - V.itemStart[lo];
-    const uint32_t p = V.order[V.keyStart[lo] + local / (nl - 1u)];
-    const int s = 2 + (int)(local % (nl - 1u));
-    VPath lig = LightPathOf(V, p);
-    uint2 st = V.rng1[p];
-    Pcg32 rng;
-    rng.state = (uint64_t)st.x | ((uint64_t)st.y << 32);
-    PcgAdvance(rng, Round1Draws(S, lig, s));
-    ConnOut o;
-    if (ConnectBdpt(S, rng, lig, CamPath(V, p), s, 1, o)) EmitConnection(S, V, nsh, err, p, o, true);
   }
 }
 
@@ -432,18 +466,26 @@ cudaError_t LaunchBdptLightFix(const DevScene& S, const BdptBuffers& V, uint32_t
   KBdptKeyScatter<<<GridFor(count, 1 << 16), kBdptBlock, 0, st>>>(V, count);
   return cudaGetLastError();
 }
+// The s >= 2 connections of round t: sorted into buckets, then one per thread.
+static void LaunchTail(const DevScene& S, const PathBuffers& B, const BdptBuffers& V, int t, int grid,
+                       cudaStream_t st) {
+  KBdptItemSort<<<grid, kBdptBlock, 0, st>>>(S, V, t, 0);
+  KBdptItemScan<<<1, 1, 0, st>>>(V);
+  KBdptItemSort<<<grid, kBdptBlock, 0, st>>>(S, V, t, 1);
+  KBdptConnectTail<<<grid, kBdptBlock, 0, st>>>(S, B, V, t);
+}
 cudaError_t LaunchBdptConnectSplit(const DevScene& S, const PathBuffers& B, const BdptBuffers& V, uint32_t count,
                                    int t, int grid, cudaStream_t st) {
   if (count == 0) return cudaSuccess;
   KBdptConnectHead<<<GridFor(count, grid), kBdptBlock, 0, st>>>(S, B, V, count, t);
-  KBdptConnectTail<<<grid, kBdptBlock, 0, st>>>(S, B, V, t);
+  LaunchTail(S, B, V, t, grid, st);
   return cudaGetLastError();
 }
 cudaError_t LaunchBdptRound1(const DevScene& S, const PathBuffers& B, const BdptBuffers& V, uint32_t count,
                              bool splats, int grid, cudaStream_t st) {
   if (count == 0) return cudaSuccess;
   KBdptRound1Head<<<GridFor(count, grid), kBdptBlock, 0, st>>>(S, B, V, count);
-  if (splats) KBdptRound1Tail<<<grid, kBdptBlock, 0, st>>>(S, B, V);
+  if (splats) LaunchTail(S, B, V, 1, grid, st);
   return cudaGetLastError();
 }
 cudaError_t LaunchBdptShadow(const DevScene& S, const PathBuffers& B, const BdptBuffers& V, int t, float4* film,

@@ -127,6 +127,7 @@ struct ParticleParams {
 // ---- renderer "bdpt" (k_bdpt.cu): wavefront stages of one wave of pixel samples
 struct BVert;
 constexpr size_t kBVertBytes = 112;  // sizeof(BVert) (dbdpt.cuh)
+constexpr int kBdptBuckets = kShadeClasses * kShadeClasses;  // (camera vertex class, light vertex class)
 struct BdptBuffers {
   BVert* vert;         // [2 * cap][nw]: camera subpath vertices, then light subpath vertices
   float4* walkA;       // per sample: walk throughput rgb, eta
@@ -142,6 +143,9 @@ struct BdptBuffers {
   uint32_t* keyFill;   // (cap + 1)^2: per-key counts, then scatter cursors
   uint32_t* itemStart; // (cap + 1)^2 + 1: exclusive scan over keys of the s >= 2 connections (nl - 1 a sample)
   uint2* rng1;         // per sample: PCG state before connection round t = 1
+  // the s >= 2 connections of one round ordered by the shade classes of their two vertices
+  uint32_t* items;     // nw * cap: sample | s << 24, bucket by bucket
+  uint32_t* bucket;    // 2 * kBdptBuckets + 1: counts, then starts, then scatter cursors
   uint32_t cap, nw, shCap;
 };
 // Camera subpaths: jittered camera rays of the wave's samples into queue 0.

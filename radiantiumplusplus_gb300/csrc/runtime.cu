@@ -291,8 +291,10 @@ const BdptBuffers& EnsureBdpt(int cap) {
   FreeAll(lib.bdptAllocs);
   lib.used -= lib.bdptBytes;
   lib.bdptBytes = 0;
-  uint64_t per = 2ull * cap * kBVertBytes + (uint64_t)cap * 3 * sizeof(float4) + 3 * sizeof(float4) + 20;
-  uint32_t nw = (uint32_t)std::min<uint64_t>(lib.maxPaths, std::max<uint64_t>(1024, kBdptScratchBytes / per));
+  uint64_t per = 2ull * cap * kBVertBytes + (uint64_t)cap * (3 * sizeof(float4) + 4) + 3 * sizeof(float4) + 20;
+  // at most 2^24 samples a wave: a sorted connection packs its sample slot in 24 bits
+  uint32_t nw = (uint32_t)std::min<uint64_t>(std::min<uint64_t>(lib.maxPaths, 1u << 24),
+                                             std::max<uint64_t>(1024, kBdptScratchBytes / per));
   BdptBuffers V{};
   auto& o = lib.bdptAllocs;
   uint64_t& b = lib.bdptBytes;
@@ -311,6 +313,8 @@ const BdptBuffers& EnsureBdpt(int cap) {
   V.keyFill = DevAlloc<uint32_t>((size_t)(cap + 1) * (cap + 1), o, b);
   V.itemStart = DevAlloc<uint32_t>((size_t)(cap + 1) * (cap + 1) + 1, o, b);
   V.rng1 = DevAlloc<uint2>(nw, o, b);
+  V.items = DevAlloc<uint32_t>((size_t)nw * cap, o, b);
+  V.bucket = DevAlloc<uint32_t>(3 * kBdptBuckets + 1, o, b);
   V.cap = (uint32_t)cap;
   V.nw = nw;
   lib.bdpt = V;
@@ -377,6 +381,7 @@ uint64_t RunBdptWave(const DevScene& S, const TraceTune& tu, const WaveParams& w
   ps.End(0, a);
   launches += 1 + BdptWalks(S, tu, count, true, cap, ps);
   Check(cudaMemsetAsync(V.keyFill, 0, (size_t)(cap + 1) * (cap + 1) * sizeof(uint32_t), lib.stream), "cudaMemsetAsync");
+  Check(cudaMemsetAsync(V.bucket, 0, kBdptBuckets * sizeof(uint32_t), lib.stream), "cudaMemsetAsync");
   Check(LaunchBdptLightFix(S, V, count, lib.stream), "bdpt light fix-up");
   uint32_t maxCam = 0;
   Check(cudaMemcpyAsync(&maxCam, B.counters + kMiscBase, sizeof(uint32_t), cudaMemcpyDeviceToHost, lib.stream), "copy");
@@ -394,7 +399,7 @@ uint64_t RunBdptWave(const DevScene& S, const TraceTune& tu, const WaveParams& w
     ps.Begin(3, a);
     Check(LaunchBdptShadow(S, B, V, t, film.accum, tgrid, lib.stream, tu.refillBusy, tu.leafFrac8), "bdpt shadow");
     ps.End(3, a);
-    launches += 3;
+    launches += 6;
   }
   ps.Begin(4, a);
   Check(LaunchBdptAccumulate(B, film, count, out, lib.stream), "bdpt accumulate");
