@@ -355,9 +355,7 @@ RDN LeSample LightSampleLe(const DevScene& S, const LightRec& L, V2 xi2, V2 xi3)
     r.D = LinearRows(L.m2 + 16, nearDir);
     r.le = V3{L.m2[29], L.m2[30], L.m2[31]};  // irradiance without the light's scale
     if (L.tex) {
-      TexCtx x{S.tex, S.texels, S.texBind, xi3, V2{0.f, 0.f}, V2{0.f, 0.f}};
-      TexVal t = TexEval(x, L.tex - 1u, xi3);
-      r.le = V3{t.c[0], t.c[1], t.c[2]};
+      r.le = LightTex(S, L.tex, xi3);
     }
     r.pdfDir = 1.f / (L.m2[28] * kPi);
   } else if (L.kind == LIGHT_SKYBOX) {
@@ -385,9 +383,7 @@ RDN LeSample LightSampleLe(const DevScene& S, const LightRec& L, V2 xi2, V2 xi3)
     r.D = worldD;
     r.le = V3{L.radiance[0], L.radiance[1], L.radiance[2]};
     if (L.tex) {
-      TexCtx x{S.tex, S.texels, S.texBind, uv, V2{0.f, 0.f}, V2{0.f, 0.f}};
-      TexVal t = TexEval(x, L.tex - 1u, uv);
-      r.le = V3{t.c[0], t.c[1], t.c[2]};
+      r.le = LightTex(S, L.tex, uv);
     }
     r.pdfPos = 1.f / (kPi * Sqr(R));
     r.pdfDir = pdfDir;

@@ -392,6 +392,15 @@ RD float EnvDirPdf(const DevScene& S, const LightRec& L, V3 dir) {
   float pdf = Dist2DPdf(S, L, uv);
   return pdf / (2.f * kPi * kPi * sinTheta);
 }
+// A light's texture at uv with zero derivatives (lights are looked up without
+// ray differentials). One out-of-line copy serves every light lookup, so the
+// texture filters' code is not repeated inside each kernel's light sampling.
+static RDN V3 LightTex(const DevScene& S, uint32_t tex1, V2 uv) {
+  TexCtx x{S.tex, S.texels, S.texBind, uv, V2{0.f, 0.f}, V2{0.f, 0.f}};
+  TexVal r = TexEval(x, tex1 - 1u, uv);
+  return V3{r.c[0], r.c[1], r.c[2]};
+}
+
 // The sky's radiance towards world direction d (skybox.cpp:53-63): the map's
 // value at the direction's latitude-longitude uv.
 RD V3 EnvRadiance(const DevScene& S, const LightRec& L, V3 d) {
@@ -400,17 +409,13 @@ RD V3 EnvRadiance(const DevScene& S, const LightRec& L, V3 d) {
   float phi = atan2f(v.x, -v.z);
   phi = phi < 0.f ? phi + 2.f * kPi : phi;
   float theta = acosf(clampr(v.y, -1.f, 1.f));
-  TexCtx x{S.tex, S.texels, S.texBind, V2{phi / (2.f * kPi), theta / kPi}, V2{0.f, 0.f}, V2{0.f, 0.f}};
-  TexVal r = TexEval(x, L.tex - 1u, x.uv);
-  return V3{r.c[0], r.c[1], r.c[2]};
+  return LightTex(S, L.tex, V2{phi / (2.f * kPi), theta / kPi});
 }
 
 // An area light's radiance at uv: its bitmap, else the constant (area.cpp:42-45).
 RD V3 AreaRadiance(const DevScene& S, const LightRec& L, V2 uv) {
   if (!L.tex) return V3{L.radiance[0], L.radiance[1], L.radiance[2]};
-  TexCtx x{S.tex, S.texels, S.texBind, uv, V2{0.f, 0.f}, V2{0.f, 0.f}};
-  TexVal r = TexEval(x, L.tex - 1u, uv);
-  return V3{r.c[0], r.c[1], r.c[2]};
+  return LightTex(S, L.tex, uv);
 }
 
 // DiffuseArea::SamplePosition (area.cpp:93-115): a bitmap light samples its
@@ -487,9 +492,7 @@ RD DirSample LightSampleDirection(const DevScene& S, const LightRec& L, V3 refP,
     d.Dir = dir * Rcp(d.Dist);
     float den = Sqr(local.z) * dot(-d.Dir, d.N);
     if (L.tex) {  // irradiance texture at the light-space uv, times the scale
-      TexCtx x{S.tex, S.texels, S.texBind, V2{uv.x, uv.y}, V2{0.f, 0.f}, V2{0.f, 0.f}};
-      TexVal t = TexEval(x, L.tex - 1u, x.uv);
-      rad = cmul(V3{t.c[0], t.c[1], t.c[2]}, rad);
+      rad = cmul(LightTex(S, L.tex, V2{uv.x, uv.y}), rad);
     }
     li = V3{(rad.x * kPi) / den, (rad.y * kPi) / den, (rad.z * kPi) / den};
   } else {
@@ -506,9 +509,7 @@ RD DirSample LightSampleDirection(const DevScene& S, const LightRec& L, V3 refP,
           return d;
         }
         d.Pdf = pdf;
-        TexCtx x{S.tex, S.texels, S.texBind, uv, V2{0.f, 0.f}, V2{0.f, 0.f}};
-        TexVal r = TexEval(x, L.tex - 1u, uv);
-        rad = V3{r.c[0], r.c[1], r.c[2]};
+        rad = LightTex(S, L.tex, uv);
       } else {  // skybox.cpp:70-87
         V3 dir = normalized(SquareToUniformSphere(xi));
         worldDir = LinearRows(L.lin, dir);
@@ -517,9 +518,7 @@ RD DirSample LightSampleDirection(const DevScene& S, const LightRec& L, V3 refP,
           float phi = atan2f(dir.x, -dir.z);
           phi = phi < 0.f ? phi + 2.f * kPi : phi;
           float theta = acosf(clampr(dir.y, -1.f, 1.f));
-          TexCtx x{S.tex, S.texels, S.texBind, V2{phi / (2.f * kPi), theta / kPi}, V2{0.f, 0.f}, V2{0.f, 0.f}};
-          TexVal r = TexEval(x, L.tex - 1u, x.uv);
-          rad = V3{r.c[0], r.c[1], r.c[2]};
+          rad = LightTex(S, L.tex, V2{phi / (2.f * kPi), theta / kPi});
         }
       }
       d.N = -worldDir;
@@ -639,9 +638,7 @@ RD bool LightSampleRay(const DevScene& S, const LightRec& L, V2 xi2, V2 xi3, V3&
     D = LinearRows(L.m2 + 16, nearDir);
     V3 irr{L.m2[29], L.m2[30], L.m2[31]};
     if (L.tex) {
-      TexCtx x{S.tex, S.texels, S.texBind, xi3, V2{0.f, 0.f}, V2{0.f, 0.f}};
-      TexVal t = TexEval(x, L.tex - 1u, xi3);
-      irr = V3{t.c[0], t.c[1], t.c[2]};
+      irr = LightTex(S, L.tex, xi3);
     }
     li = irr * kPi * L.m2[28];  // SampleRay leaves out the light's scale
     return true;
@@ -670,9 +667,7 @@ RD bool LightSampleRay(const DevScene& S, const LightRec& L, V2 xi2, V2 xi3, V3&
     D = worldD;
     V3 c = rad;
     if (L.tex) {
-      TexCtx x{S.tex, S.texels, S.texBind, uv, V2{0.f, 0.f}, V2{0.f, 0.f}};
-      TexVal r = TexEval(x, L.tex - 1u, uv);
-      c = V3{r.c[0], r.c[1], r.c[2]};
+      c = LightTex(S, L.tex, uv);
     }
     li = ((c * kPi) * Sqr(R)) / pdfDir;
     return true;

@@ -111,96 +111,126 @@ RD int MediumOfHit(const DevScene& S, const SurfInt& si, V3 D) {
   return dot(D, si.N) > 0.f ? sh.outMedium : sh.inMedium;
 }
 
-// vol_path.cpp:224-342. stable: RelTr ratios instead of the reference's (see RelTr).
-template <bool BRICKS, bool HALF>
-RDN V3 VolSampleLight(const DevScene& S, Pcg32& rng, int medium, int channel, V3 refP, V3 refN, DirSample& dsr,
-                     uint32_t* err, uint64_t& nRays, bool stable) {
+// Next-event estimation of vol_path (vol_path.cpp:224-342) as resumable steps:
+// NeeBegin draws the light sample, each NeeStep is one iteration of the
+// transmittance loop (a ratio-tracking step in a medium, or a surface segment),
+// so that a warp can run the loop's iterations of many lanes together.
+// stable: RelTr ratios instead of the reference's (see RelTr).
+struct NeeState {
+  DirSample dsr;
+  V3 li, tr;        // the light's radiance, the transmittance so far
+  VRay ray;
+  float total;      // distance covered
+  int medium, guard;
+  bool active, needsIsect;
+  float siT;        // the last surface hit of the shadow ray (SurfInt fields the loop reads)
+  V3 siP, siN;
+  int siShape;
+};
+
+RD void NeeBegin(const DevScene& S, Pcg32& rng, int medium, V3 refP, V3 refN, NeeState& n) {
   float xl = Next1D(rng);
   V2 xd = Next2D(rng);
-  V3 li;
-  dsr = SampleLightDirection(S, refP, xl, xd, li);
-  if (dsr.Pdf <= 0.f) return v3s(0.f);
-  VRay ray = Spawn(refP, refN, dsr.Dir);
-  float totalDist = 0.f;
-  V3 resultTr = v3s(1.f);
-  bool active = true, needsIntersection = true;
+  n.dsr = SampleLightDirection(S, refP, xl, xd, n.li);
+  n.active = n.dsr.Pdf > 0.f;
+  if (!n.active) return;
+  n.ray = Spawn(refP, refN, n.dsr.Dir);
+  n.total = 0.f;
+  n.tr = v3s(1.f);
+  n.needsIsect = true;
+  n.siT = kInf;
+  n.siShape = -1;
+  n.medium = medium;
+  n.guard = 0;
+}
+
+// One iteration of the transmittance loop; false once it has ended.
+template <bool BRICKS, bool HALF>
+RDN bool NeeStep(const DevScene& S, Pcg32& rng, int channel, NeeState& n, uint32_t* err, uint32_t& nRays,
+                 bool stable) {
+  if (n.guard++ >= kMaxTrLoop) {
+    atomicOr(err, 2u);
+    n.tr = v3s(0.f);
+    return n.active = false;
+  }
+  VRay& ray = n.ray;
   SurfInt si;
-  si.T = kInf;
-  si.shape = -1;
-  for (int guard = 0; active; guard++) {
-    if (guard >= kMaxTrLoop) {
-      atomicOr(err, 2u);
-      return v3s(0.f);
-    }
-    float remainingDist = dsr.Dist * (1.f - kShadowEps) - totalDist;
-    ray.MaxT = remainingDist;
-    active = active && remainingDist > 0.f;
-    if (!active) break;
-    bool escapedMedium = false;
-    bool activeMedium = active && medium >= 0;
-    bool activeSurface = active && !activeMedium;
-    if (activeMedium) {
-      const MediumRec& md = S.media[medium];
-      MedInt mei = SampleInteraction<BRICKS, HALF>(S, md, ray, Next1D(rng), channel);
-      if (md.kind == MED_HOMOGENEOUS && mei.T != kInf) ray.MaxT = fminr(mei.T, remainingDist);
-      if (needsIntersection) {
-        VTraceCall(S, ray, si, err, nullptr);
-        nRays++;
-      }
-      if (si.T < mei.T) mei.T = kInf;
-      bool isSpectral = true;
-      {
-        float t = fminr(remainingDist, fminr(mei.T, si.T)) - mei.MinT;
-        if (t >= 0.f) {
-          bool pass = si.T < mei.T || mei.T > remainingDist;
-          V3 mTr;
-          if (stable) {
-            float m = comp(mei.cE, channel);
-            V3 rel = RelTr(mei.cE, channel, t);
-            mTr = pass ? rel : (m > 0.f ? rel / m : v3s(0.f));
-          } else {
-            V3 tr = ExpV(mei.cE * -t);
-            V3 ffp = pass ? tr : cmul(tr, mei.cE);
-            float trPdf = comp(ffp, channel);
-            mTr = trPdf > 0.f ? tr / trPdf : v3s(0.f);
-          }
-          resultTr = cmul(resultTr, mTr);
-        }
-      }
-      if ((mei.T > remainingDist) && mei.T != kInf) totalDist = dsr.Dist;
-      if (mei.T > remainingDist) mei.T = kInf;
-      escapedMedium = mei.T == kInf;
-      activeMedium = mei.T != kInf;
-      isSpectral = isSpectral && activeMedium;
-      if (activeMedium) {
-        totalDist += mei.T;
-        ray.O = mei.P;
-        si.T = si.T - mei.T;
-        if (isSpectral) resultTr = cmul(resultTr, mei.sN);
-      }
-    }
-    bool intersect = activeSurface && needsIntersection;
-    if (intersect) {
+  si.T = n.siT;
+  si.P = n.siP;
+  si.N = n.siN;
+  si.shape = n.siShape;
+  float remainingDist = n.dsr.Dist * (1.f - kShadowEps) - n.total;
+  ray.MaxT = remainingDist;
+  bool active = remainingDist > 0.f;
+  if (!active) return n.active = false;
+  bool escapedMedium = false;
+  bool activeMedium = active && n.medium >= 0;
+  bool activeSurface = active && !activeMedium;
+  if (activeMedium) {
+    const MediumRec& md = S.media[n.medium];
+    MedInt mei = SampleInteraction<BRICKS, HALF>(S, md, ray, Next1D(rng), channel);
+    if (md.kind == MED_HOMOGENEOUS && mei.T != kInf) ray.MaxT = fminr(mei.T, remainingDist);
+    if (n.needsIsect) {
       VTraceCall(S, ray, si, err, nullptr);
       nRays++;
     }
-    needsIntersection = needsIntersection && !intersect;
-    activeSurface = activeSurface || escapedMedium;
-    if (activeSurface) totalDist += si.T;
-    activeSurface = activeSurface && si.T != kInf && active && !activeMedium;
-    if (activeSurface) {
-      if (S.shapes[si.shape].bsdf >= 0) resultTr = v3s(0.f);
-      ray = Spawn(si.P, si.N, ray.D);
+    if (si.T < mei.T) mei.T = kInf;
+    bool isSpectral = true;
+    {
+      float t = fminr(remainingDist, fminr(mei.T, si.T)) - mei.MinT;
+      if (t >= 0.f) {
+        bool pass = si.T < mei.T || mei.T > remainingDist;
+        V3 mTr;
+        if (stable) {
+          float m = comp(mei.cE, channel);
+          V3 rel = RelTr(mei.cE, channel, t);
+          mTr = pass ? rel : (m > 0.f ? rel / m : v3s(0.f));
+        } else {
+          V3 tr = ExpV(mei.cE * -t);
+          V3 ffp = pass ? tr : cmul(tr, mei.cE);
+          float trPdf = comp(ffp, channel);
+          mTr = trPdf > 0.f ? tr / trPdf : v3s(0.f);
+        }
+        n.tr = cmul(n.tr, mTr);
+      }
     }
-    ray.MaxT = remainingDist;
-    needsIntersection = needsIntersection || activeSurface;
-    active = active && (activeMedium || activeSurface) && !is_zero(resultTr);
-    if (activeSurface) {
-      const ShapeRec& sh = S.shapes[si.shape];
-      if (sh.inMedium >= 0 || sh.outMedium >= 0) medium = MediumOfHit(S, si, ray.D);
+    if ((mei.T > remainingDist) && mei.T != kInf) n.total = n.dsr.Dist;
+    if (mei.T > remainingDist) mei.T = kInf;
+    escapedMedium = mei.T == kInf;
+    activeMedium = mei.T != kInf;
+    isSpectral = isSpectral && activeMedium;
+    if (activeMedium) {
+      n.total += mei.T;
+      ray.O = mei.P;
+      si.T = si.T - mei.T;
+      if (isSpectral) n.tr = cmul(n.tr, mei.sN);
     }
   }
-  return cmul(li, resultTr);
+  bool intersect = activeSurface && n.needsIsect;
+  if (intersect) {
+    VTraceCall(S, ray, si, err, nullptr);
+    nRays++;
+  }
+  n.needsIsect = n.needsIsect && !intersect;
+  activeSurface = activeSurface || escapedMedium;
+  if (activeSurface) n.total += si.T;
+  activeSurface = activeSurface && si.T != kInf && active && !activeMedium;
+  if (activeSurface) {
+    if (S.shapes[si.shape].bsdf >= 0) n.tr = v3s(0.f);
+    ray = Spawn(si.P, si.N, ray.D);
+  }
+  ray.MaxT = remainingDist;
+  n.needsIsect = n.needsIsect || activeSurface;
+  active = active && (activeMedium || activeSurface) && !is_zero(n.tr);
+  if (activeSurface) {
+    const ShapeRec& sh = S.shapes[si.shape];
+    if (sh.inMedium >= 0 || sh.outMedium >= 0) n.medium = MediumOfHit(S, si, ray.D);
+  }
+  n.siT = si.T;
+  n.siP = si.P;
+  n.siN = si.N;
+  n.siShape = si.shape;
+  return n.active = active;
 }
 
 // Per-path state of the `vol_path` loop (VolPath::Li's locals), so that a lane
@@ -212,18 +242,25 @@ struct VolPathState {
   float eta, prevPdf;
   int medium, channel, depth, guard;
   bool isSpecular, siValid, afterNull;
-  int act;      // next part of the loop iteration: kActTop, kActScatter or kActSurface
-  V3 scatterP;  // kActScatter: the real collision
+  int act;      // next part of the loop iteration (kAct*)
+  V3 scatterP;  // kActScatter / kActScatterEnd: the real collision
   SurfInt si;
   Pcg32 rng;
   uint32_t nRays, nShadow;
+  NeeState nee;  // kActNee: the next-event estimation in progress
+  int neeRet;    // the part that follows it
+  V2 uvHit;      // kActSurfaceEnd: the hit's texture coordinates
 };
 // Parts of one iteration of the VolPath::Li loop (vol_path.cpp:40-215): the top
-// (Russian roulette, depth test, free flight, null / real decision), the medium
-// scatter (phase NEE + phase sampling) and the surface part (trace, emission,
-// BSDF NEE and sampling). A path runs them in this order, so its arithmetic and
-// random numbers are those of the loop; KVolPath runs one kind per warp step.
-constexpr int kActTop = 0, kActScatter = 1, kActSurface = 2;
+// (Russian roulette, depth test, free flight, null / real decision); the medium
+// scatter (the light sample of the phase NEE), its transmittance steps and its
+// end (NEE contribution, phase sampling); the surface part (trace, emission,
+// the light sample of the BSDF NEE), its transmittance steps and its end (NEE
+// contribution, BSDF sampling). A path runs them in this order, so its
+// arithmetic and random numbers are those of the loop; KVolPath runs one kind
+// per warp step.
+constexpr int kActTop = 0, kActScatter = 1, kActSurface = 2, kActNee = 3, kActScatterEnd = 4, kActSurfaceEnd = 5;
+constexpr int kActs = 6;
 
 RD void VolInit(const DevScene& S, VolPathState& p, VRay ray, Pcg32 rng) {
   p.ray = ray;
@@ -340,20 +377,24 @@ RD bool VolTop(const DevScene& S, VolPathState& p, uint32_t mode, uint32_t* err)
   return true;
 }
 
-// Medium scatter: phase-function NEE and the next direction.
-template <bool BRICKS, bool HALF>
-RD bool VolScatter(const DevScene& S, VolPathState& p, uint32_t mode, uint32_t* err) {
-  const bool realDepth = BRICKS || (mode & kVolRealDepth);
+// Medium scatter: the light sample of the phase-function NEE.
+RD bool VolScatter(const DevScene& S, VolPathState& p) {
+  NeeBegin(S, p.rng, p.medium, p.scatterP, v3s(0.f), p.nee);
+  p.neeRet = kActScatterEnd;
+  p.act = p.nee.active ? kActNee : kActScatterEnd;
+  return true;
+}
+
+// After the NEE: its contribution and the next direction.
+RD bool VolScatterEnd(const DevScene& S, VolPathState& p) {
   const MediumRec& md = S.media[p.medium];
   MedInt mei;  // the phase functions read the incident direction and its frame
   mei.Wi = -p.ray.D;
   mei.sh = FrameFromN(mei.Wi);
   mei.P = p.scatterP;
-  DirSample dsr;
-  uint64_t ns = 0;
-  V3 li = VolSampleLight<BRICKS, HALF>(S, p.rng, p.medium, p.channel, mei.P, v3s(0.f), dsr, err, ns, realDepth);
-  p.nShadow += (uint32_t)ns;
+  const DirSample& dsr = p.nee.dsr;
   if (dsr.Pdf > 0.f) {
+    V3 li = cmul(p.nee.li, p.nee.tr);
     float phaseVal = PhaseEval(md, mei, dsr.Dir);
     float weight = dsr.IsDelta ? 1.f : VMis(dsr.Pdf, phaseVal);
     p.result = p.result + cmul(p.thr, li) * weight * phaseVal / dsr.Pdf;
@@ -366,10 +407,17 @@ RD bool VolScatter(const DevScene& S, VolPathState& p, uint32_t mode, uint32_t* 
   return VolNextIteration(p);
 }
 
-// Surface part: trace, emission with MIS, BSDF NEE, BSDF sampling.
+// One step of the NEE's transmittance loop.
+template <bool BRICKS, bool HALF>
+RD bool VolNee(const DevScene& S, VolPathState& p, uint32_t mode, uint32_t* err) {
+  const bool realDepth = BRICKS || (mode & kVolRealDepth);
+  if (!NeeStep<BRICKS, HALF>(S, p.rng, p.channel, p.nee, err, p.nShadow, realDepth)) p.act = p.neeRet;
+  return true;
+}
+
+// Surface part: trace, emission with MIS, the light sample of the BSDF NEE.
 template <bool BRICKS, bool HALF>
 RD bool VolSurface(const DevScene& S, VolPathState& p, uint32_t mode, uint32_t* err) {
-  const bool realDepth = BRICKS || (mode & kVolRealDepth);
   VRay& ray = p.ray;
   SurfInt& si = p.si;
   V3& thr = p.thr;
@@ -378,12 +426,6 @@ RD bool VolSurface(const DevScene& S, VolPathState& p, uint32_t mode, uint32_t* 
   const bool textured = S.nTex != 0u;
   V2 uvHit{0.f, 0.f};
   bool hit = VTraceCall(S, ray, si, err, textured ? &uvHit : nullptr);
-  TexCtx tcx;
-  const TexCtx* tc = nullptr;
-  if (textured && hit) {
-    tcx = TexCtx{S.tex, S.texels, S.texBind, uvHit, V2{0.f, 0.f}, V2{0.f, 0.f}};
-    tc = &tcx;
-  }
   p.nRays++;
   int hitLight = hit ? S.shapes[si.shape].light : S.envLight;
   if (hitLight >= 0) {
@@ -410,20 +452,40 @@ RD bool VolSurface(const DevScene& S, VolPathState& p, uint32_t mode, uint32_t* 
     p.act = kActTop;
     return true;
   }
+  p.uvHit = uvHit;
+  p.neeRet = kActSurfaceEnd;
+  if (S.mats[shp.bsdf].flags & BT_NODELTA) {
+    NeeBegin(S, p.rng, p.medium, si.P, si.N, p.nee);
+    p.act = p.nee.active ? kActNee : kActSurfaceEnd;
+  } else {
+    p.nee.dsr.Pdf = 0.f;  // no NEE at a delta-only BSDF
+    p.act = kActSurfaceEnd;
+  }
+  return true;
+}
+
+// After the NEE: its contribution, BSDF sampling.
+RD bool VolSurfaceEnd(const DevScene& S, VolPathState& p) {
+  VRay& ray = p.ray;
+  SurfInt& si = p.si;
+  V3& thr = p.thr;
+  const ShapeRec& shp = S.shapes[si.shape];
   const MatRec* mats = S.mats;
-  if (mats[shp.bsdf].flags & BT_NODELTA) {
-    DirSample dsr;
-    uint64_t ns = 0;
-    V3 li = VolSampleLight<BRICKS, HALF>(S, p.rng, p.medium, p.channel, si.P, si.N, dsr, err, ns, realDepth);
-    p.nShadow += (uint32_t)ns;
-    if (dsr.Pdf > 0.f) {
-      V3 wo = ToLocal(si.sh, dsr.Dir);
-      V3 f;
-      float bsdfPdf;
-      VBsdfEvalPdf(mats, (uint32_t)shp.bsdf, si.Wi, wo, f, bsdfPdf, tc);
-      float weight = dsr.IsDelta ? 1.f : VMis(dsr.Pdf, bsdfPdf);
-      p.result = p.result + cmul(cmul(thr, f), li) * weight / dsr.Pdf;
-    }
+  TexCtx tcx;
+  const TexCtx* tc = nullptr;
+  if (S.nTex != 0u) {
+    tcx = TexCtx{S.tex, S.texels, S.texBind, p.uvHit, V2{0.f, 0.f}, V2{0.f, 0.f}};
+    tc = &tcx;
+  }
+  const DirSample& dsr = p.nee.dsr;
+  if (dsr.Pdf > 0.f) {
+    V3 li = cmul(p.nee.li, p.nee.tr);
+    V3 wo = ToLocal(si.sh, dsr.Dir);
+    V3 f;
+    float bsdfPdf;
+    VBsdfEvalPdf(mats, (uint32_t)shp.bsdf, si.Wi, wo, f, bsdfPdf, tc);
+    float weight = dsr.IsDelta ? 1.f : VMis(dsr.Pdf, bsdfPdf);
+    p.result = p.result + cmul(cmul(thr, f), li) * weight / dsr.Pdf;
   }
   float xl = Next1D(p.rng);
   V2 xd = Next2D(p.rng);
@@ -443,10 +505,19 @@ RD bool VolSurface(const DevScene& S, VolPathState& p, uint32_t mode, uint32_t* 
 // The next part of the path's current iteration; false when the path has ended
 // (its radiance is in p.result).
 template <bool BRICKS, bool HALF>
+RD bool VolAct(const DevScene& S, VolPathState& p, int act, uint32_t mode, uint32_t* err) {
+  switch (act) {
+    case kActScatter: return VolScatter(S, p);
+    case kActSurface: return VolSurface<BRICKS, HALF>(S, p, mode, err);
+    case kActNee: return VolNee<BRICKS, HALF>(S, p, mode, err);
+    case kActScatterEnd: return VolScatterEnd(S, p);
+    case kActSurfaceEnd: return VolSurfaceEnd(S, p);
+    default: return VolTop<BRICKS, HALF>(S, p, mode, err);
+  }
+}
+template <bool BRICKS, bool HALF>
 RD bool VolStep(const DevScene& S, VolPathState& p, uint32_t mode, uint32_t* err) {
-  if (p.act == kActScatter) return VolScatter<BRICKS, HALF>(S, p, mode, err);
-  if (p.act == kActSurface) return VolSurface<BRICKS, HALF>(S, p, mode, err);
-  return VolTop<BRICKS, HALF>(S, p, mode, err);
+  return VolAct<BRICKS, HALF>(S, p, p.act, mode, err);
 }
 
 // The whole loop for one path (host-side checks and equivalence tests).
@@ -499,20 +570,17 @@ __global__ void __launch_bounds__(kVolBlock)
         }
       }
     }
-    const uint32_t m0 = __ballot_sync(0xffffffffu, live && p.act == kActTop);
-    const uint32_t m1 = __ballot_sync(0xffffffffu, live && p.act == kActScatter);
-    const uint32_t m2 = __ballot_sync(0xffffffffu, live && p.act == kActSurface);
-    if ((m0 | m1 | m2) == 0u) break;
-    const int c0 = __popc(m0), c1 = __popc(m1), c2 = __popc(m2);
-    const int act = (c0 >= c1 && c0 >= c2) ? kActTop : (c1 >= c2 ? kActScatter : kActSurface);
+    int act = -1, best = 0;
+    for (int a = 0; a < kActs; a++) {
+      const int c = __popc(__ballot_sync(0xffffffffu, live && p.act == a));
+      if (c > best) {
+        best = c;
+        act = a;
+      }
+    }
+    if (act < 0) break;
     if (live && p.act == act) {
-      bool alive;
-      if (act == kActTop)
-        alive = VolTop<BRICKS, HALF>(S, p, mode, err);
-      else if (act == kActScatter)
-        alive = VolScatter<BRICKS, HALF>(S, p, mode, err);
-      else
-        alive = VolSurface<BRICKS, HALF>(S, p, mode, err);
+      bool alive = VolAct<BRICKS, HALF>(S, p, act, mode, err);
       if (!alive) {
         B.L[idx] = make_float4(p.result.x, p.result.y, p.result.z, 0.f);
         nRays += p.nRays;
