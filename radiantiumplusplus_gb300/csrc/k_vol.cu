@@ -541,7 +541,7 @@ RD V3 VolLi(const DevScene& S, Pcg32& rng, VRay ray, uint32_t mode, uint32_t* er
 // (top / medium scatter / surface) that most of the warp's live lanes are at, so
 // a warp executes one code path at a time while paths stay in different phases.
 template <bool BRICKS, bool HALF>
-__global__ void __launch_bounds__(kVolBlock, 4)
+__global__ void __launch_bounds__(kVolBlock, 5)
     KVolPath(DevScene S, PathBuffers B, uint32_t count, uint32_t* err, uint32_t mode) {
   uint32_t* next = B.counters + kMiscBase + 4;
   const uint32_t lane = threadIdx.x & 31u;
