@@ -214,14 +214,15 @@ __device__ __forceinline__ void EmitConnection(const DevScene& S, const BdptBuff
 }
 
 // Round t >= 2, the s = 0 and s = 1 connections of each sample of the suffix
-// (the only ones of the round that draw random numbers: s = 1's light sample).
+// (the only ones of the round that draw random numbers: s = 1's light sample),
+// in the order of V.items (by the camera vertex's shade class).
 __global__ void __launch_bounds__(kBdptBlock) KBdptConnectHead(DevScene S, PathBuffers B, BdptBuffers V, uint32_t count,
                                                               int t) {
   uint32_t* nsh = B.counters + kShadowBase + (t - 1);
   uint32_t* err = B.counters + kMiscBase + 1;
   const uint32_t first = V.keyStart[(uint32_t)t * (V.cap + 1u)];
-  for (uint32_t j = first + blockIdx.x * blockDim.x + threadIdx.x; j < count; j += gridDim.x * blockDim.x) {
-    const uint32_t p = V.order[j];
+  for (uint32_t j = blockIdx.x * blockDim.x + threadIdx.x; j < count - first; j += gridDim.x * blockDim.x) {
+    const uint32_t p = V.items[j] & 0xffffffu;
     const int nl = (int)V.nLight[p];
     Pcg32 rng = LoadRng(B, p);
     VPath cam = CamPath(V, p), lig = LightPathOf(V, p);
@@ -261,12 +262,17 @@ RD uint32_t ItemBucket(const DevScene& S, const BdptBuffers& V, uint32_t p, int 
   return VClass(S, CamPath(V, p)[t - 1]) * (uint32_t)kShadeClasses + VClass(S, LightPathOf(V, p)[s - 1]);
 }
 
-// Round t's s >= 2 connections counted per bucket (pass 0) or scattered into
-// V.items bucket by bucket (pass 1), with warp-aggregated atomics.
-__global__ void __launch_bounds__(kBdptBlock) KBdptItemSort(DevScene S, BdptBuffers V, int t, int pass) {
+// Round t's work items counted per bucket (pass 0) or scattered into V.items
+// bucket by bucket (pass 1), with warp-aggregated atomics. head: the samples
+// with at least t camera vertices (their s <= 1 connections), bucketed by the
+// camera vertex's shade class; else the s >= 2 connections, bucketed by both
+// vertices' classes.
+__global__ void __launch_bounds__(kBdptBlock) KBdptItemSort(DevScene S, BdptBuffers V, int t, int pass, int head,
+                                                           uint32_t count) {
   const uint32_t c1 = V.cap + 1u, nk = c1 * c1;
   const uint32_t k0 = (uint32_t)t * c1;
-  const uint32_t g0 = V.itemStart[k0], n = V.itemStart[nk] - g0;
+  const uint32_t g0 = head ? V.keyStart[k0] : V.itemStart[k0];
+  const uint32_t n = head ? count - g0 : V.itemStart[nk] - g0;
   const uint32_t lane = threadIdx.x & 31u;
   uint32_t* cnt = V.bucket + (pass == 0 ? 0 : 2 * kBdptBuckets);
   for (uint32_t base = blockIdx.x * blockDim.x; base < n; base += gridDim.x * blockDim.x) {
@@ -274,7 +280,10 @@ __global__ void __launch_bounds__(kBdptBlock) KBdptItemSort(DevScene S, BdptBuff
     const bool ok = j < n;
     uint32_t p = 0, key = 0xffffffffu;
     int s = 0;
-    if (ok) {
+    if (ok && head) {
+      p = V.order[g0 + j];
+      key = VClass(S, CamPath(V, p)[t - 1]);
+    } else if (ok) {
       RoundItem(V, k0, g0 + j, p, s);
       key = ItemBucket(S, V, p, s, t);
     }
@@ -467,16 +476,21 @@ cudaError_t LaunchBdptLightFix(const DevScene& S, const BdptBuffers& V, uint32_t
   return cudaGetLastError();
 }
 // The s >= 2 connections of round t: sorted into buckets, then one per thread.
+static void LaunchSort(const DevScene& S, const BdptBuffers& V, int t, bool head, uint32_t count, int grid,
+                       cudaStream_t st) {
+  KBdptItemSort<<<grid, kBdptBlock, 0, st>>>(S, V, t, 0, head ? 1 : 0, count);
+  KBdptItemScan<<<1, 1, 0, st>>>(V);
+  KBdptItemSort<<<grid, kBdptBlock, 0, st>>>(S, V, t, 1, head ? 1 : 0, count);
+}
 static void LaunchTail(const DevScene& S, const PathBuffers& B, const BdptBuffers& V, int t, int grid,
                        cudaStream_t st) {
-  KBdptItemSort<<<grid, kBdptBlock, 0, st>>>(S, V, t, 0);
-  KBdptItemScan<<<1, 1, 0, st>>>(V);
-  KBdptItemSort<<<grid, kBdptBlock, 0, st>>>(S, V, t, 1);
+  LaunchSort(S, V, t, false, 0, grid, st);
   KBdptConnectTail<<<grid, kBdptBlock, 0, st>>>(S, B, V, t);
 }
 cudaError_t LaunchBdptConnectSplit(const DevScene& S, const PathBuffers& B, const BdptBuffers& V, uint32_t count,
                                    int t, int grid, cudaStream_t st) {
   if (count == 0) return cudaSuccess;
+  LaunchSort(S, V, t, true, count, grid, st);
   KBdptConnectHead<<<GridFor(count, grid), kBdptBlock, 0, st>>>(S, B, V, count, t);
   LaunchTail(S, B, V, t, grid, st);
   return cudaGetLastError();

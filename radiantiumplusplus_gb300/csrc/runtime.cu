@@ -399,7 +399,7 @@ uint64_t RunBdptWave(const DevScene& S, const TraceTune& tu, const WaveParams& w
     ps.Begin(3, a);
     Check(LaunchBdptShadow(S, B, V, t, film.accum, tgrid, lib.stream, tu.refillBusy, tu.leafFrac8), "bdpt shadow");
     ps.End(3, a);
-    launches += 6;
+    launches += t >= 2 ? 9 : 6;
   }
   ps.Begin(4, a);
   Check(LaunchBdptAccumulate(B, film, count, out, lib.stream), "bdpt accumulate");
