@@ -190,7 +190,9 @@ RAD_API int rad_render_samples(rad_scene* scene, const uint32_t* pixels, const u
  * 16384 (RAD_ERR_INVALID_ARG beyond). Work runs on `stream` (a cudaStream_t,
  * NULL = default stream) and the call returns when it has finished. The first
  * call on a device looks up the array's address; make it before any stream
- * capture. Every call shares the one array: calls that overlap on the GPU race. */
+ * capture. Every call shares the one array: calls that overlap on the GPU race.
+ * RAD_ERR_UNSUPPORTED for particle_tracer (no per-pixel samples) and bdpt (its
+ * subpaths live in scratch the library allocates). */
 RAD_API int rad_render_samples_noalloc(rad_scene* scene, const uint32_t* d_pixels, const uint32_t* d_samples,
                                        int64_t n, uint32_t seed, float* d_radiance, void* stream);
 
