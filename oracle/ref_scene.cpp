@@ -253,7 +253,13 @@ PositionSample Shape::SamplePosition(const V2& xi) const {
     psr.P = e0 * b.x + (e1 * b.y + p0);
     psr.Pdf = dist.normalization;
     psr.IsDelta = false;
-    psr.UV = b;
+    if (!hasUV) {
+      psr.UV = b;
+    } else {
+      V2 uv0 = uv[f0], uv1 = uv[f1], uv2 = uv[f2];
+      Float b0 = 1 - b.x - b.y;
+      psr.UV = V2(uv0.x * b0 + (uv1.x * b.x + (uv2.x * b.y)), uv0.y * b0 + (uv1.y * b.x + (uv2.y * b.y)));
+    }
     if (nrm.empty()) {
       psr.N = normalized(cross(e0, e1));
     } else {
@@ -932,10 +938,13 @@ std::unique_ptr<Scene> Scene::FromJson(const std::string& text, const std::strin
         L.kind = Light::Area;
         const Json* rj = ln->find("radiance");
         if (rj && rj->is_object()) {
-          if (ReadS(rj, "type", "") == "chessboard") throw std::runtime_error("area: chessboard radiance is not supported");
           L.map = MakeTexture(*rj, 3, &env);
           uint32_t width = L.map->width, height = L.map->height;
-          if (width == 1 && height == 1) {  // _isUniform: the map is one constant
+          if (ReadS(rj, "type", "") == "chessboard") {
+            // chessboard.cpp:30-31: width = height = 1, so _isUniform: the shape is sampled and the texture
+            // read at each point's uv (area.cpp:45-58)
+            L.uniformMap = true;
+          } else if (width == 1 && height == 1) {  // _isUniform: the map is one constant
             L.radiance = L.map->Eval(TexSi{V2(0, 0), V2(), V2()});
             L.map = nullptr;
           } else {
@@ -949,6 +958,7 @@ std::unique_ptr<Scene> Scene::FromJson(const std::string& text, const std::strin
               }
             }
             L.dist.Build(luminance.data(), width, height);
+            L.uniformMap = false;
           }
         } else {
           L.radiance = color("radiance", V3(1));
@@ -1072,9 +1082,12 @@ std::unique_ptr<Scene> Scene::FromJson(const std::string& text, const std::strin
     if (lightIdx >= 0) {
       S.lights[lightIdx].shape = shapeIdx;
       // only the rectangle has EvalParamSurface (shape.cpp:27-29)
-      if (S.lights[lightIdx].kind == Light::Area && S.lights[lightIdx].map &&
-          (shapeIdx < 0 || S.shapes[shapeIdx].kind != Shape::Rect))
+      const Light& AL = S.lights[lightIdx];
+      if (AL.kind == Light::Area && AL.map && !AL.uniformMap && (shapeIdx < 0 || S.shapes[shapeIdx].kind != Shape::Rect))
         throw std::runtime_error("no impl EvalParamSurface(): a textured area light needs a rectangle");
+      // sphere.cpp:250-320 leaves the sample's uv unset: a chessboard would be read at an undefined uv
+      if (AL.kind == Light::Area && AL.map && AL.uniformMap && shapeIdx >= 0 && S.shapes[shapeIdx].kind == Shape::Sphere)
+        throw std::runtime_error("area: a chessboard radiance on a sphere is not supported");
     }
   }
   // renderer (path.cpp:26-29, vol_path.cpp:22-25)
@@ -1608,7 +1621,7 @@ static void RectParam(const Shape& sh, const V2& uv, V3& P, V3& N, Float& dA) {
 std::pair<PositionSample, Float> Scene::LightSamplePosition(int l, const V2& xi) const {
   const Light& L = lights[l];
   const Shape& sh = shapes[L.shape];
-  if (!L.map) {
+  if (!L.map || L.uniformMap) {
     PositionSample psr = sh.SamplePosition(xi);
     return {psr, psr.Pdf > 0 ? psr.Pdf : 0};
   }
@@ -1662,7 +1675,7 @@ std::pair<DirectionSample, Spectrum> Scene::SampleOneLightDirection(int index, c
   DirectionSample dsr;
   Spectrum li(0);
   const Light& L = lights[index];
-  if (L.kind == Light::Area && L.map) {  // area.cpp:59-72: SurfaceInteraction::ToDsr leaves Pdf 0
+  if (L.kind == Light::Area && L.map && !L.uniformMap) {  // area.cpp:59-72: SurfaceInteraction::ToDsr leaves Pdf 0
     auto [iu, iv, pdf] = L.dist.Sample(xi);
     if (pdf <= 0) return {DirectionSample(), Spectrum(0)};
     V2 uv(iu / (Float)L.map->width, iv / (Float)L.map->height);
@@ -1677,7 +1690,7 @@ std::pair<DirectionSample, Spectrum> Scene::SampleOneLightDirection(int index, c
     li = dot(-dsr.Dir, dsr.N) >= 0 ? L.map->Eval(TexSi{uv, V2(), V2()}) : Spectrum(0);
   } else if (L.kind == Light::Area) {
     dsr = shapes[L.shape].SampleDirection(refP, xi);
-    li = dot(-dsr.Dir, dsr.N) >= 0 ? L.radiance : Spectrum(0);
+    li = dot(-dsr.Dir, dsr.N) >= 0 ? AreaRadiance(L, dsr.UV) : Spectrum(0);  // a chessboard at the sample's uv
   } else if (L.kind == Light::Skybox) {  // skybox.cpp:65-106
     Float radius = std::max(L.worldRadius, norm(refP - L.worldCenter));
     Float dist = 2 * radius;
@@ -1784,7 +1797,7 @@ static Float SkyPdfDirection(const Light& L, const V3& dir) {
 Float Scene::PdfLightDirection(int l, const V3& refP, const DirectionSample& dsr) const {
   const Light& L = lights[l];
   Float p = 0;
-  if (L.kind == Light::Area && L.map) {  // area.cpp:81-90
+  if (L.kind == Light::Area && L.map && !L.uniformMap) {  // area.cpp:81-90
     Float pdf = L.dist.Pdf(dsr.UV);
     if (pdf > 0) {
       V3 P, N;

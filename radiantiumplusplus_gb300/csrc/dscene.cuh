@@ -208,8 +208,11 @@ RD uint32_t CdfLowerBound(const float* cdf, uint32_t n, float value) {
 }
 
 // Shape::SamplePosition (mesh_base.cpp:84-110, rectangle.cpp:221-230,
-// sphere.cpp:250-258): position, normal, area density.
-RD void ShapeSamplePosition(const DevScene& S, const ShapeRec& sh, V2 xi, V3& P, V3& N, float& pdf) {
+// sphere.cpp:250-258): position, normal, area density and the sample's uv (a
+// mesh's interpolated uv, else its barycentrics; a rectangle's xi; a sphere
+// leaves it unset, here 0).
+RD void ShapeSamplePosition(const DevScene& S, const ShapeRec& sh, V2 xi, V3& P, V3& N, float& pdf, V2& uv) {
+  uv = V2{0.f, 0.f};
   if (sh.kind == SHAPE_SPHERE) {
     V3 local = SquareToUniformSphere(xi);
     P = Fmadd(local, v3s(sh.m[3]), V3{sh.m[0], sh.m[1], sh.m[2]});
@@ -231,6 +234,14 @@ RD void ShapeSamplePosition(const DevScene& S, const ShapeRec& sh, V2 xi, V3& P,
     V2 b = SquareToUniformTriangle(txi);
     P = e0 * b.x + (e1 * b.y + p0);
     pdf = sh.cdfNorm;
+    if (!sh.hasUV) {
+      uv = b;
+    } else {
+      const float* t = S.uv;
+      float b0 = 1.f - b.x - b.y;
+      uv = V2{t[2 * f0] * b0 + (t[2 * f1] * b.x + (t[2 * f2] * b.y)),
+              t[2 * f0 + 1] * b0 + (t[2 * f1 + 1] * b.x + (t[2 * f2 + 1] * b.y))};
+    }
     if (!sh.hasNormals) {
       N = normalized(cross(e0, e1));
     } else {
@@ -242,17 +253,19 @@ RD void ShapeSamplePosition(const DevScene& S, const ShapeRec& sh, V2 xi, V3& P,
     P = AffineRows(sh.m, V3{sx, sy, 0.f});
     N = ShapeM3(sh, 18);
     pdf = 1.f / sh.surfaceArea;
+    uv = xi;
   }
 }
 
 // Shape::SamplePosition + SampleDirection (shape.cpp:7-19, mesh_base.cpp:84-110,
-// rectangle.cpp:204-214, sphere.cpp:251-320).
-RD DirSample ShapeSampleDirection(const DevScene& S, const ShapeRec& sh, V3 refP, V2 xi) {
+// rectangle.cpp:204-214, sphere.cpp:251-320); uv as ShapeSamplePosition's.
+RD DirSample ShapeSampleDirection(const DevScene& S, const ShapeRec& sh, V3 refP, V2 xi, V2& uv) {
   DirSample d;
+  uv = V2{0.f, 0.f};
   if (sh.kind != SHAPE_SPHERE) {
     V3 P, N;
     float pdf;
-    ShapeSamplePosition(S, sh, xi, P, N, pdf);
+    ShapeSamplePosition(S, sh, xi, P, N, pdf, uv);
     d.P = P;
     d.N = N;
     d.IsDelta = false;
@@ -412,7 +425,7 @@ RD V3 EnvRadiance(const DevScene& S, const LightRec& L, V3 d) {
   return LightTex(S, L.tex, V2{phi / (2.f * kPi), theta / kPi});
 }
 
-// An area light's radiance at uv: its bitmap, else the constant (area.cpp:42-45).
+// An area light's radiance at uv: its texture, else the constant (area.cpp:42-45).
 RD V3 AreaRadiance(const DevScene& S, const LightRec& L, V2 uv) {
   if (!L.tex) return V3{L.radiance[0], L.radiance[1], L.radiance[2]};
   return LightTex(S, L.tex, uv);
@@ -421,12 +434,13 @@ RD V3 AreaRadiance(const DevScene& S, const LightRec& L, V2 uv) {
 // DiffuseArea::SamplePosition (area.cpp:93-115): a bitmap light samples its
 // luminance distribution at texel corners uv of its rectangle
 // (Rectangle::EvalParamSurface, rectangle.cpp:236-250; |dPdU x dPdV| is the
-// rectangle's area). pdf is the area density, 0 for a failed sample.
+// rectangle's area). A constant or a chessboard (a 1 x 1 texture,
+// chessboard.cpp:30-31) samples the shape, uv the shape sample's. pdf is the
+// area density, 0 for a failed sample.
 RD void AreaSamplePosition(const DevScene& S, const LightRec& L, V2 xi, V3& P, V3& N, V2& uv, float& pdf) {
   const ShapeRec& sh = S.shapes[L.shape];
-  uv = V2{0.f, 0.f};
-  if (!L.tex) {
-    ShapeSamplePosition(S, sh, xi, P, N, pdf);
+  if (!L.distW) {
+    ShapeSamplePosition(S, sh, xi, P, N, pdf, uv);
     pdf = pdf > 0.f ? pdf : 0.f;
     return;
   }
@@ -434,6 +448,7 @@ RD void AreaSamplePosition(const DevScene& S, const LightRec& L, V2 xi, V3& P, V
   float p = Dist2DSample(S, L, xi, iu, iv);
   if (p <= 0.f) {
     P = N = v3s(0.f);
+    uv = V2{0.f, 0.f};
     pdf = 0.f;
     return;
   }
@@ -465,9 +480,10 @@ RD DirSample LightSampleDirection(const DevScene& S, const LightRec& L, V3 refP,
   li = v3s(0.f);
   V3 rad{L.radiance[0], L.radiance[1], L.radiance[2]};
   if (L.kind == LIGHT_AREA) {
-    if (L.tex) return d;  // area.cpp:59-72: the bitmap branch's SurfaceInteraction::ToDsr leaves Pdf 0
-    d = ShapeSampleDirection(S, S.shapes[L.shape], refP, xi);
-    li = dot(-d.Dir, d.N) >= 0.f ? rad : v3s(0.f);
+    if (L.distW) return d;  // area.cpp:59-72: the bitmap branch's SurfaceInteraction::ToDsr leaves Pdf 0
+    V2 uv;  // area.cpp:55-58: a chessboard is read at the shape sample's uv
+    d = ShapeSampleDirection(S, S.shapes[L.shape], refP, xi, uv);
+    li = dot(-d.Dir, d.N) >= 0.f ? AreaRadiance(S, L, uv) : v3s(0.f);
   } else if (L.kind == LIGHT_POINT) {  // point.cpp:33-49
     d.P = V3{L.dir[0], L.dir[1], L.dir[2]};
     d.N = v3s(0.f);
@@ -558,7 +574,7 @@ RD DirSample SampleLightDirection(const DevScene& S, V3 refP, float xiL, V2 xi, 
 RD float PdfLightDirection(const DevScene& S, int light, V3 refP, V3 dir, V3 n, float dist, V2 uv) {
   const LightRec& L = S.lights[light];
   float p = 0.f;
-  if (L.kind == LIGHT_AREA && L.tex) {  // area.cpp:81-90 (no facing test)
+  if (L.kind == LIGHT_AREA && L.distW) {  // area.cpp:81-90 (no facing test)
     float pdf = Dist2DPdf(S, L, uv);
     if (pdf > 0.f) p = pdf * Sqr(dist) / (S.shapes[L.shape].surfaceArea * -dot(dir, n));
   } else if (L.kind == LIGHT_AREA) {

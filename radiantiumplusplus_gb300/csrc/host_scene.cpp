@@ -1257,8 +1257,11 @@ void BuildHostScene(const std::string& json, const std::string& baseDir, HostSce
           uint32_t tid = AddTexture(*rn, 3, env);
           const TexRec& tr = hs.tex[tid];
           uint32_t W = tr.kind == TEX_BITMAP ? tr.width : 1u, H = tr.kind == TEX_BITMAP ? tr.height : 1u;
-          if (tr.kind == TEX_CHESS) throw FactoryError("area: chessboard radiance is not supported");
-          if (W == 1 && H == 1) {  // _isUniform: one constant
+          if (tr.kind == TEX_CHESS) {
+            // a chessboard is 1 x 1 (chessboard.cpp:30-31): _isUniform, so the light samples its shape and
+            // reads the texture at each point's uv (area.cpp:45-58); no distribution (distW 0)
+            L.tex = tid + 1;
+          } else if (W == 1 && H == 1) {  // _isUniform: one constant
             float c[3];
             HostTexEval(hs, tid, 0.f, 0.f, c);
             rad = F3(c[0], c[1], c[2]);
@@ -1400,8 +1403,13 @@ void BuildHostScene(const std::string& json, const std::string& baseDir, HostSce
       hs.lights[lightIdx].shape = shapeIdx;
       if (hs.lights[lightIdx].kind == LIGHT_AREA && shapeIdx < 0) throw ConfigError("area light needs a shape");
       // only the rectangle has EvalParamSurface (shape.cpp:27-29)
-      if (hs.lights[lightIdx].kind == LIGHT_AREA && hs.lights[lightIdx].tex && hs.shapes[shapeIdx].kind != SHAPE_RECT)
+      const LightRec& AL = hs.lights[lightIdx];
+      if (AL.kind == LIGHT_AREA && AL.distW && hs.shapes[shapeIdx].kind != SHAPE_RECT)
         throw ConfigError("no impl EvalParamSurface(): a textured area light needs a rectangle");
+      // Sphere::SamplePosition / SampleDirection leave the sample's uv unset (sphere.cpp:250-320), so the
+      // reference would read a chessboard radiance at an undefined uv
+      if (AL.kind == LIGHT_AREA && AL.tex && !AL.distW && hs.shapes[shapeIdx].kind == SHAPE_SPHERE)
+        throw ConfigError("area: a chessboard radiance on a sphere is not supported (its samples carry no uv)");
     }
   }
   const JValue* rn = root.get("renderer");

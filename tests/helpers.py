@@ -96,6 +96,29 @@ def textured_light_room(w=48, h=48, spp=4, seed=1, renderer="path"):
     return sc, {"glow.hdr": imgenc.hdr(img)}
 
 
+def chessboard_light_room(w=48, h=48, spp=4, seed=1, renderer="path", shape="rect", a=(30.0, 14.0, 3.0),
+                          b=(3.0, 6.0, 24.0), ceiling=(1.0, 0.8, 0.3)):
+    """Box room lit by an emitter whose radiance is a chessboard (a 1 x 1 texture to
+    the light, chessboard.cpp:30-31): the shape is sampled uniformly and the texture
+    read at each sample's uv (area.cpp:45-58). shape "rect": the ceiling rectangle;
+    "cube": a small cube hanging below the ceiling (a mesh with per-face uvs; its
+    samples carry interpolated uvs; the ceiling rectangle keeps a constant
+    radiance `ceiling`). Returns (scene dict, assets)."""
+    sc = scenes.box_room(w, h, spp, seed)
+    chess = {"type": "chessboard", "color_a": list(a), "color_b": list(b),
+             "to_uv": {"scale": [3.0, 2.0, 1.0]}}
+    if shape == "rect":
+        sc["scene"][-1]["light"] = {"type": "area", "radiance": chess}
+    else:
+        sc["scene"][-1]["light"]["radiance"] = list(ceiling)
+        sc["scene"].append({"to_world": {"translate": [0.1, 1.55, 0.2], "rotate": {"axis": [1, 1, 0], "angle": 30.0},
+                                         "scale": [0.18, 0.18, 0.18]},
+                            "shape": {"type": "cube"}, "light": {"type": "area", "radiance": chess}})
+    if renderer != "path":
+        sc["renderer"] = {"type": renderer, "max_depth": 6}
+    return sc, {}
+
+
 def textured_projection_room(w=48, h=48, spp=4, seed=1, renderer="path"):
     """Box room with a dimmed area light and a projection light whose irradiance
     is a 16 x 12 PNG slide (aspect 4:3 sets the projector's frustum,

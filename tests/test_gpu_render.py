@@ -137,17 +137,22 @@ def test_bdpt_samples_and_film(rad, oracle, scene_dir, light):
     g.close()
 
 
-@pytest.mark.parametrize("light", ["area", "projection"])
+@pytest.mark.parametrize("light", ["area", "projection", "chess_rect", "chess_cube"])
 @pytest.mark.parametrize("renderer", ["path", "vol_path", "bdpt", "particle_tracer"])
 def test_textured_light(rad, oracle, scene_dir, renderer, light):
     """area: a bitmap radiance on the emitter rectangle: its texels seen at hits,
     the luminance distribution behind position samples (light paths), the
     reference's zero-density direction samples (no next-event estimation from a
     bitmap light) and its direction density in the MIS weights. projection: a
-    bitmap slide looked up at the light-space uv of each direction or emitted ray."""
-    from helpers import textured_light_room, textured_projection_room
-    make = textured_light_room if light == "area" else textured_projection_room
-    sc, assets = make(24, 24, 4, renderer=renderer)
+    bitmap slide looked up at the light-space uv of each direction or emitted ray.
+    chess_*: a chessboard radiance on a rectangle or a cube: uniform shape samples
+    (next-event estimation included) read at the sample's uv."""
+    from helpers import chessboard_light_room, textured_light_room, textured_projection_room
+    if light.startswith("chess"):
+        sc, assets = chessboard_light_room(24, 24, 4, renderer=renderer, shape=light[6:])
+    else:
+        make = textured_light_room if light == "area" else textured_projection_room
+        sc, assets = make(24, 24, 4, renderer=renderer)
     if renderer == "particle_tracer":
         sc["sampler"]["sample_count"] = 60000
     path, text, d = write(scene_dir, "texlight_%s_%s" % (light, renderer), sc, assets)

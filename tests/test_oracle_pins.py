@@ -436,3 +436,72 @@ def test_textured_area_light_seen_directly(oracle, scene_dir):
     _, text, d = write(scene_dir, "tex_light_sphere", sc, {"q.hdr": hdr})
     with pytest.raises(RuntimeError, match="EvalParamSurface"):
         oracle.OracleScene(text, d)
+
+
+@pytest.mark.parametrize("shape", ["rect", "cube"])
+def test_chessboard_area_light_is_linear_in_its_colours(oracle, scene_dir, shape):
+    """A chessboard radiance leaves the light's sampling untouched (uniform shape
+    samples, area.cpp:55-58), so the renders with colours (a, b) and (b, a) add up,
+    pixel by pixel, to the render of the constant a + b with the same seed (the
+    cube room's ceiling light is kept at radiance 0, so it is counted once)."""
+    from helpers import chessboard_light_room, write
+    a, b = (30.0, 14.0, 3.0), (3.0, 6.0, 24.0)
+    films = []
+    for i, (ca, cb) in enumerate([(a, b), (b, a)]):
+        sc, _ = chessboard_light_room(16, 16, 16, shape=shape, a=ca, b=cb, ceiling=(0, 0, 0))
+        _, text, d = write(scene_dir, "chess_lin_%s_%d" % (shape, i), sc)
+        o = oracle.OracleScene(text, d)
+        films.append(o.render()[0])
+        o.close()
+    sc, _ = chessboard_light_room(16, 16, 16, shape=shape, ceiling=(0, 0, 0))
+    emitter = sc["scene"][-1]["light"]
+    emitter["radiance"] = [x + y for x, y in zip(a, b)]
+    _, text, d = write(scene_dir, "chess_lin_%s_c" % shape, sc)
+    o = oracle.OracleScene(text, d)
+    ref, _ = o.render()
+    o.close()
+    assert np.allclose(films[0] + films[1], ref, rtol=1e-4, atol=1e-6)
+    assert not np.allclose(films[0], films[1], rtol=0.05)  # the two colourings light the room differently
+
+
+def test_chessboard_area_light_seen_directly(oracle, scene_dir):
+    """A camera facing a chessboard emitter sees colour_a where the fractional
+    parts of the to_uv-mapped uv fall on the same side of 1/2, colour_b elsewhere
+    (chessboard.cpp:35-56). The particle tracer's emitter-point splats, which
+    read the texture at position samples' uvs (rectangle.cpp:221-230), draw the
+    same pattern as the path tracer's hits (rectangle.cpp:202-217). A sphere
+    emitter is refused: its samples carry no uv (sphere.cpp:250-320)."""
+    from helpers import write
+    red, blue = [4.0, 0.0, 0.0], [0.0, 0.0, 4.0]
+    sc = {"camera": {"type": "perspective", "fov": 10.0, "resolution": [16, 16], "origin": [0, 0, 5],
+                     "target": [0, 0, 0]},
+          "sampler": {"type": "independent", "sample_count": 1, "seed": 2},
+          "scene": [{"to_world": {"scale": [2, 2, 1]}, "shape": {"type": "rectangle"},
+                     "light": {"type": "area", "radiance": {"type": "chessboard", "color_a": red,
+                                                            "color_b": blue,
+                                                            "to_uv": {"scale": [2, 2, 1]}}}}],
+          "accel": {"type": "embree"}, "renderer": {"type": "path", "max_depth": 1}}
+    _, text, d = write(scene_dir, "chess_light_direct", sc)
+    o = oracle.OracleScene(text, d)
+    film, _ = o.render()
+    o.close()
+    diag = {tuple(film[i, j]) for i, j in [(1, 1), (14, 14)]}
+    anti = {tuple(film[i, j]) for i, j in [(1, 14), (14, 1)]}  # the view spans tuv 0.78..1.22 on both axes
+    assert len(diag) == 1 and len(anti) == 1 and diag | anti == {tuple(red), tuple(blue)}, (diag, anti)
+    assert {tuple(c) for c in film.reshape(-1, 3)} == {tuple(red), tuple(blue)}
+    sc["renderer"] = {"type": "particle_tracer", "max_depth": 1}
+    sc["sampler"]["sample_count"] = 40000
+    _, text, d = write(scene_dir, "chess_light_particle", sc)
+    o = oracle.OracleScene(text, d)
+    pt = o.render_particle(threads=0)
+    o.close()
+    redder = film[..., 0] > film[..., 2]
+    inner = np.zeros_like(redder)
+    inner[1:-1, 1:-1] = True  # pixels away from the emitter's edge
+    agree = (pt[..., 0] > pt[..., 2]) == redder
+    assert agree[inner].mean() >= 0.9, agree[inner].mean()
+    sc["scene"][0]["shape"] = {"type": "sphere", "radius": 1.0}
+    sc["scene"][0]["to_world"] = {"translate": [0, 0, 0]}
+    _, text, d = write(scene_dir, "chess_light_sphere", sc)
+    with pytest.raises(RuntimeError, match="sphere"):
+        oracle.OracleScene(text, d)
