@@ -450,6 +450,731 @@ Ldr DecodePnm(const std::string& bytes, int req, bool flipY) {
   return out;
 }
 
+// -------------------------------------------------------------------- JPEG
+// ITU-T T.81 Huffman JPEG: sequential (SOF0 / SOF1) and progressive (SOF2)
+// scans, 8-bit samples, 1, 3 or 4 components, sampling factors 1..4 that
+// divide the largest ones, restart intervals. The pixel pipeline restates the
+// choices stb_image makes (stbi_load behind the image_default asset):
+//  * coefficients are kept as 16-bit integers (progressive scans add their
+//    successive-approximation bits to them), multiplied by the quantisation
+//    table with 16-bit wrap-around;
+//  * the inverse DCT is the integer "islow" factorisation of the Independent
+//    JPEG Group (Loeffler-Ligtenberg-Moschytz rotations with constants rounded
+//    to 12 fractional bits): columns first, rounded to keep 2 extra bits,
+//    then rows with the 0.5 rounding and the +128 level shift folded into one
+//    bias before the final shift by 17, clamped to 0..255;
+//  * chroma planes subsampled 2x horizontally and/or vertically are upsampled
+//    with the triangle filter (3/4 nearest + 1/4 next sample, centred between
+//    samples; with both, a 3x3-weighted 2-D version rounded once), the rows
+//    stepped so that output row y blends the chroma rows nearest y/2 - 1/4;
+//    any other ratio replicates samples;
+//  * YCbCr -> RGB in 20-bit fixed point with the constants 1.402, 0.71414,
+//    0.34414, 1.772 rounded to 12 bits, the cb term of green truncated to its
+//    high 16 bits; 3 components named 'R', 'G', 'B' (or an Adobe marker with
+//    transform 0 and no JFIF marker) are RGB already; 4 components are CMYK
+//    (Adobe transform 0) or YCCK (transform 2) combined with K by the rounded
+//    product x * k / 255, else YCbCr with the fourth ignored;
+//  * one requested channel is the Y plane itself for YCbCr files, the integer
+//    luma (77 r + 150 g + 29 b) >> 8 otherwise.
+struct JHuff {
+  bool present = false;
+  uint8_t fastLen[512];  // 9-bit lookahead: code length (0: longer code)
+  uint8_t fastSym[512];
+  int maxcode[18], valptr[17], mincode[17];
+  uint8_t vals[256];
+};
+
+// T.81 C.2 / F.2.2.3: canonical codes from the counts per length.
+void BuildJHuff(JHuff& h, const uint8_t* counts, const uint8_t* vals, int n) {
+  std::memcpy(h.vals, vals, n);
+  std::memset(h.fastLen, 0, sizeof(h.fastLen));
+  int code = 0, k = 0;
+  for (int l = 1; l <= 16; l++) {
+    h.valptr[l] = k;
+    h.mincode[l] = code;
+    for (int i = 0; i < counts[l - 1]; i++, k++, code++) {
+      if (l <= 9) {
+        int first = code << (9 - l);
+        for (int j = 0; j < (1 << (9 - l)); j++) {
+          h.fastLen[first + j] = (uint8_t)l;
+          h.fastSym[first + j] = vals[k];
+        }
+      }
+    }
+    h.maxcode[l] = counts[l - 1] ? code - 1 : -1;
+    if (code > (1 << l)) Fail("jpeg: bad Huffman code lengths");
+    code <<= 1;
+  }
+  h.present = true;
+}
+
+// Entropy-coded segment reader: MSB-first bits, 0xFF 0x00 stuffing removed; a
+// marker ends the data (zeros are read after it).
+struct JBits {
+  const uint8_t* p;
+  size_t n, pos;
+  uint32_t buf = 0;
+  int cnt = 0;
+  int marker = -1;
+  bool nomore = false;
+  uint8_t Byte() { return pos < n ? p[pos++] : 0; }
+  void Fill() {
+    while (cnt <= 24) {
+      uint32_t b = 0;
+      if (!nomore) {
+        b = Byte();
+        if (b == 0xFF) {
+          uint32_t c = Byte();
+          while (c == 0xFF) c = Byte();
+          if (c != 0) {
+            marker = (int)c;
+            nomore = true;
+            b = 0;
+          }
+        }
+      }
+      buf |= b << (24 - cnt);
+      cnt += 8;
+    }
+  }
+  int Bits(int k) {
+    if (k == 0) return 0;
+    Fill();
+    uint32_t v = buf >> (32 - k);
+    buf <<= k;
+    cnt -= k;
+    return (int)v;
+  }
+  // EXTEND(RECEIVE(s)), T.81 F.2.2.1
+  int Receive(int s) {
+    int v = Bits(s);
+    return v < (1 << (s - 1)) ? v - (1 << s) + 1 : v;
+  }
+  int Decode(const JHuff& h) {
+    if (!h.present) Fail("jpeg: scan uses an undefined Huffman table");
+    Fill();
+    uint32_t look = buf >> 23;
+    if (h.fastLen[look]) {
+      int l = h.fastLen[look];
+      buf <<= l;
+      cnt -= l;
+      return h.fastSym[look];
+    }
+    for (int l = 10; l <= 16; l++) {
+      int code = (int)(buf >> (32 - l));
+      if (code <= h.maxcode[l]) {
+        buf <<= l;
+        cnt -= l;
+        return h.vals[h.valptr[l] + code - h.mincode[l]];
+      }
+    }
+    Fail("jpeg: bad Huffman code");
+  }
+};
+
+struct JComp {
+  int id = 0, h = 1, v = 1, tq = 0, td = 0, ta = 0;
+  int x = 0, y = 0;        // plane size in samples
+  int bw = 0, bh = 0;      // blocks per row / column of the MCU-padded plane
+  int dcPred = 0;
+  std::vector<int16_t> coef;  // bw * bh blocks of 64, natural order
+  std::vector<uint8_t> plane;  // bw * 8 x bh * 8 samples
+};
+
+// zigzag index -> natural (row-major) index, T.81 figure A.6
+struct JZigzag {
+  uint8_t nat[64];
+  JZigzag() {
+    int k = 0;
+    for (int s = 0; s < 15; s++) {
+      int lo = s > 7 ? s - 7 : 0, hi = s < 7 ? s : 7;
+      if (s & 1) {
+        for (int r = lo; r <= hi; r++) nat[k++] = (uint8_t)(r * 8 + (s - r));
+      } else {
+        for (int r = hi; r >= lo; r--) nat[k++] = (uint8_t)(r * 8 + (s - r));
+      }
+    }
+  }
+};
+const JZigzag kZz;
+
+inline int F2F(float x) { return (int)(x * 4096.f + 0.5f); }
+
+// One 1-D pass of the islow IDCT on s0..s7 (frequency order); outputs the even
+// part x0..x3 and the odd part t0..t3 (outputs i and 7 - i are x_i +- t_(3-i)).
+inline void Idct1D(int s0, int s1, int s2, int s3, int s4, int s5, int s6, int s7, int& x0, int& x1, int& x2,
+                   int& x3, int& t0, int& t1, int& t2, int& t3) {
+  int p2 = s2, p3 = s6;
+  int p1 = (p2 + p3) * F2F(0.5411961f);
+  t2 = p1 + p3 * F2F(-1.847759065f);
+  t3 = p1 + p2 * F2F(0.765366865f);
+  p2 = s0;
+  p3 = s4;
+  t0 = (p2 + p3) * 4096;
+  t1 = (p2 - p3) * 4096;
+  x0 = t0 + t3;
+  x3 = t0 - t3;
+  x1 = t1 + t2;
+  x2 = t1 - t2;
+  t0 = s7;
+  t1 = s5;
+  t2 = s3;
+  t3 = s1;
+  p3 = t0 + t2;
+  int p4 = t1 + t3;
+  p1 = t0 + t3;
+  p2 = t1 + t2;
+  int p5 = (p3 + p4) * F2F(1.175875602f);
+  t0 = t0 * F2F(0.298631336f);
+  t1 = t1 * F2F(2.053119869f);
+  t2 = t2 * F2F(3.072711026f);
+  t3 = t3 * F2F(1.501321110f);
+  p1 = p5 + p1 * F2F(-0.899976223f);
+  p2 = p5 + p2 * F2F(-2.562915447f);
+  p3 = p3 * F2F(-1.961570560f);
+  p4 = p4 * F2F(-0.390180644f);
+  t3 += p1 + p4;
+  t2 += p2 + p3;
+  t1 += p2 + p4;
+  t0 += p1 + p3;
+}
+
+inline uint8_t Clamp255(int v) { return (uint8_t)(v < 0 ? 0 : v > 255 ? 255 : v); }
+
+// Dequantised block d (natural order) -> 8 x 8 samples at out (row stride).
+void IdctBlock(const int16_t* d, uint8_t* out, int stride) {
+  int val[64];
+  for (int c = 0; c < 8; c++) {  // columns, keeping 2 extra bits
+    int x0, x1, x2, x3, t0, t1, t2, t3;
+    Idct1D(d[c], d[c + 8], d[c + 16], d[c + 24], d[c + 32], d[c + 40], d[c + 48], d[c + 56], x0, x1, x2, x3, t0, t1,
+           t2, t3);
+    x0 += 512;
+    x1 += 512;
+    x2 += 512;
+    x3 += 512;
+    val[c] = (x0 + t3) >> 10;
+    val[c + 56] = (x0 - t3) >> 10;
+    val[c + 8] = (x1 + t2) >> 10;
+    val[c + 48] = (x1 - t2) >> 10;
+    val[c + 16] = (x2 + t1) >> 10;
+    val[c + 40] = (x2 - t1) >> 10;
+    val[c + 24] = (x3 + t0) >> 10;
+    val[c + 32] = (x3 - t0) >> 10;
+  }
+  for (int r = 0; r < 8; r++) {  // rows: remove 12 + 2 + 3 bits, round, shift the level by 128
+    const int* v = val + 8 * r;
+    int x0, x1, x2, x3, t0, t1, t2, t3;
+    Idct1D(v[0], v[1], v[2], v[3], v[4], v[5], v[6], v[7], x0, x1, x2, x3, t0, t1, t2, t3);
+    const int bias = 65536 + (128 << 17);
+    x0 += bias;
+    x1 += bias;
+    x2 += bias;
+    x3 += bias;
+    uint8_t* o = out + (size_t)r * stride;
+    o[0] = Clamp255((x0 + t3) >> 17);
+    o[7] = Clamp255((x0 - t3) >> 17);
+    o[1] = Clamp255((x1 + t2) >> 17);
+    o[6] = Clamp255((x1 - t2) >> 17);
+    o[2] = Clamp255((x2 + t1) >> 17);
+    o[5] = Clamp255((x2 - t1) >> 17);
+    o[3] = Clamp255((x3 + t0) >> 17);
+    o[4] = Clamp255((x3 - t0) >> 17);
+  }
+}
+
+struct JpegDecoder {
+  const uint8_t* b;
+  size_t n, pos = 2;
+  uint16_t q[4][64] = {};  // natural order
+  bool qSet[4] = {};
+  JHuff dc[4], ac[4];
+  std::vector<JComp> comp;
+  int X = 0, Y = 0, hmax = 1, vmax = 1, mcux = 0, mcuy = 0;
+  bool progressive = false, frame = false, jfif = false;
+  int rgbIds = 0, adobe = -1, restart = 0;
+  int eobrun = 0;
+
+  uint8_t U8() {
+    if (pos >= n) Fail("jpeg: truncated");
+    return b[pos++];
+  }
+  int U16() {
+    int hi = U8();
+    return (hi << 8) | U8();
+  }
+  // the next marker: 0xFF then any fill 0xFF bytes; -1 when the byte is not 0xFF
+  int Marker() {
+    if (pos >= n) Fail("jpeg: no EOI marker");
+    if (b[pos] != 0xFF) {
+      pos++;
+      return -1;
+    }
+    while (pos < n && b[pos] == 0xFF) pos++;
+    return U8();
+  }
+
+  void Frame(int m) {
+    if (frame) Fail("jpeg: more than one frame");
+    frame = true;
+    progressive = m == 0xC2;
+    int L = U16();
+    if (U8() != 8) Fail("jpeg: only 8-bit samples are supported");
+    Y = U16();
+    X = U16();
+    if (Y == 0) Fail("jpeg: no height in the frame header (DNL is not supported)");
+    if (X == 0) Fail("jpeg: zero width");
+    int nf = U8();
+    if (nf != 1 && nf != 3 && nf != 4) Fail("jpeg: 1, 3 or 4 components are supported");
+    if (L != 8 + 3 * nf) Fail("jpeg: bad frame header length");
+    comp.resize(nf);
+    for (int i = 0; i < nf; i++) {
+      JComp& c = comp[i];
+      c.id = U8();
+      int hv = U8();
+      c.h = hv >> 4;
+      c.v = hv & 15;
+      c.tq = U8();
+      if (c.h < 1 || c.h > 4 || c.v < 1 || c.v > 4) Fail("jpeg: bad sampling factors");
+      if (c.tq > 3) Fail("jpeg: bad quantisation table index");
+      if (nf == 3 && c.id == "RGB"[i]) rgbIds++;
+      hmax = std::max(hmax, c.h);
+      vmax = std::max(vmax, c.v);
+    }
+    if ((size_t)X * Y * nf > ((size_t)1 << 30)) Fail("jpeg: image too large");
+    for (JComp& c : comp)
+      if (hmax % c.h || vmax % c.v) Fail("jpeg: sampling factors must divide the largest ones");
+    mcux = (X + hmax * 8 - 1) / (hmax * 8);
+    mcuy = (Y + vmax * 8 - 1) / (vmax * 8);
+    for (JComp& c : comp) {
+      c.x = (X * c.h + hmax - 1) / hmax;
+      c.y = (Y * c.v + vmax - 1) / vmax;
+      c.bw = mcux * c.h;
+      c.bh = mcuy * c.v;
+      c.coef.assign((size_t)c.bw * c.bh * 64, 0);
+    }
+  }
+
+  void Tables(int m) {
+    int L = U16() - 2;
+    if (m == 0xDB) {  // DQT
+      while (L > 0) {
+        int pq = U8(), t = pq & 15, p = pq >> 4;
+        if (p > 1 || t > 3) Fail("jpeg: bad DQT");
+        for (int i = 0; i < 64; i++) q[t][kZz.nat[i]] = (uint16_t)(p ? U16() : U8());
+        qSet[t] = true;
+        L -= p ? 129 : 65;
+      }
+    } else if (m == 0xC4) {  // DHT
+      while (L > 0) {
+        int tc = U8(), th = tc & 15;
+        tc >>= 4;
+        if (tc > 1 || th > 3) Fail("jpeg: bad DHT");
+        uint8_t counts[16], vals[256];
+        int total = 0;
+        for (int i = 0; i < 16; i++) total += counts[i] = U8();
+        if (total > 256) Fail("jpeg: bad DHT");
+        for (int i = 0; i < total; i++) vals[i] = U8();
+        BuildJHuff(tc ? ac[th] : dc[th], counts, vals, total);
+        L -= 17 + total;
+      }
+    }
+    if (L != 0) Fail("jpeg: bad table segment length");
+  }
+
+  void Skip(int m) {
+    int L = U16();
+    if (L < 2 || pos + (size_t)(L - 2) > n) Fail("jpeg: bad segment length");
+    const uint8_t* s = b + pos;
+    if (m == 0xE0 && L >= 7 && std::memcmp(s, "JFIF\0", 5) == 0) jfif = true;
+    if (m == 0xEE && L >= 14 && std::memcmp(s, "Adobe\0", 6) == 0) adobe = s[11];
+    pos += L - 2;
+  }
+
+  // T.81 G.1.2: one block of a scan into the coefficients c (zigzag band ss..se).
+  void DecodeBlock(JBits& r, JComp& c, int16_t* d, int ss, int se, int ah, int al) {
+    if (!progressive) {
+      std::memset(d, 0, 64 * sizeof(int16_t));
+      int t = r.Decode(dc[c.td]);
+      if (t > 15) Fail("jpeg: bad DC code");
+      c.dcPred += t ? r.Receive(t) : 0;
+      d[0] = (int16_t)c.dcPred;
+      for (int k = 1; k < 64;) {
+        int rs = r.Decode(ac[c.ta]), s = rs & 15, run = rs >> 4;
+        if (s == 0) {
+          if (rs != 0xF0) break;
+          k += 16;
+        } else {
+          k += run;
+          if (k > 63) Fail("jpeg: AC run past the block");
+          d[kZz.nat[k++]] = (int16_t)r.Receive(s);
+        }
+      }
+      return;
+    }
+    if (ss == 0) {  // DC scans
+      if (ah == 0) {
+        std::memset(d, 0, 64 * sizeof(int16_t));
+        int t = r.Decode(dc[c.td]);
+        if (t > 15) Fail("jpeg: bad DC code");
+        c.dcPred += t ? r.Receive(t) : 0;
+        d[0] = (int16_t)(c.dcPred * (1 << al));
+      } else if (r.Bits(1)) {
+        d[0] = (int16_t)(d[0] + (1 << al));
+      }
+      return;
+    }
+    if (ah == 0) {  // first AC scan of a band
+      if (eobrun > 0) {
+        eobrun--;
+        return;
+      }
+      for (int k = ss; k <= se;) {
+        int rs = r.Decode(ac[c.ta]), s = rs & 15, run = rs >> 4;
+        if (s == 0) {
+          if (run < 15) {
+            eobrun = (1 << run) - 1 + r.Bits(run);
+            break;
+          }
+          k += 16;
+        } else {
+          k += run;
+          if (k > 63) Fail("jpeg: AC run past the block");
+          d[kZz.nat[k++]] = (int16_t)(r.Receive(s) * (1 << al));
+        }
+      }
+      return;
+    }
+    // AC refinement (T.81 G.1.2.3): one correction bit per nonzero coefficient
+    // passed, new coefficients of magnitude 1 << al placed after `run` zeros
+    const int16_t bit = (int16_t)(1 << al);
+    auto refine = [&](int16_t& v) {
+      if (r.Bits(1) && (v & bit) == 0) v = (int16_t)(v > 0 ? v + bit : v - bit);
+    };
+    if (eobrun > 0) {
+      eobrun--;
+      for (int k = ss; k <= se; k++) {
+        int16_t& v = d[kZz.nat[k]];
+        if (v != 0) refine(v);
+      }
+      return;
+    }
+    int k = ss;
+    do {
+      int rs = r.Decode(ac[c.ta]), s = rs & 15, run = rs >> 4;
+      int16_t val = 0;
+      if (s == 0) {
+        if (run < 15) {
+          eobrun = (1 << run) - 1 + r.Bits(run);
+          run = 64;  // the rest of the band only refines
+        }              // else 15 zeros and a zero "coefficient": 16 zeros
+      } else {
+        if (s != 1) Fail("jpeg: bad AC refinement code");
+        val = r.Bits(1) ? bit : (int16_t)-bit;
+      }
+      while (k <= se) {
+        int16_t& v = d[kZz.nat[k++]];
+        if (v != 0) {
+          refine(v);
+        } else {
+          if (run == 0) {
+            v = val;
+            break;
+          }
+          run--;
+        }
+      }
+    } while (k <= se);
+  }
+
+  void Scan() {
+    int L = U16();
+    int ns = U8();
+    if (ns < 1 || ns > 4 || ns > (int)comp.size() || L != 6 + 2 * ns) Fail("jpeg: bad scan header");
+    std::vector<JComp*> sc;
+    for (int i = 0; i < ns; i++) {
+      int id = U8(), tt = U8();
+      JComp* c = nullptr;
+      for (JComp& k : comp)
+        if (k.id == id) c = &k;
+      if (!c) Fail("jpeg: scan names an unknown component");
+      c->td = tt >> 4;
+      c->ta = tt & 15;
+      if (c->td > 3 || c->ta > 3) Fail("jpeg: bad Huffman table index");
+      sc.push_back(c);
+    }
+    int ss = U8(), se = U8(), a = U8(), ah = a >> 4, al = a & 15;
+    if (progressive) {
+      if (ss > 63 || se > 63 || ss > se || ah > 13 || al > 13) Fail("jpeg: bad progressive scan");
+      if ((ss == 0) != (se == 0)) Fail("jpeg: a scan mixes DC and AC coefficients");
+      if (ss > 0 && ns != 1) Fail("jpeg: AC scans have one component");
+    } else {
+      if (ss != 0 || ah != 0 || al != 0) Fail("jpeg: bad sequential scan");
+      se = 63;
+    }
+    JBits r{b, n, pos};
+    int todo = restart ? restart : 0x7fffffff;
+    auto reset = [&]() {
+      r.buf = 0;
+      r.cnt = 0;
+      r.marker = -1;
+      r.nomore = false;
+      for (JComp* c : sc) c->dcPred = 0;
+      eobrun = 0;
+      todo = restart ? restart : 0x7fffffff;
+    };
+    reset();
+    // the segment's remaining bytes (padding bits) up to its marker
+    auto drain = [&]() {
+      while (r.marker < 0 && r.pos < r.n) {
+        r.buf = 0;
+        r.cnt = 0;
+        r.Fill();
+      }
+    };
+    // false: the segment ended without its restart marker (the scan stops)
+    auto step = [&]() {
+      if (--todo > 0) return true;
+      drain();
+      if (r.marker < 0xD0 || r.marker > 0xD7) return false;
+      reset();
+      return true;
+    };
+    bool more = true;
+    if (ns == 1) {  // non-interleaved: the component's own block grid
+      JComp& c = *sc[0];
+      int w = (c.x + 7) >> 3, h = (c.y + 7) >> 3;
+      for (int j = 0; j < h && more; j++)
+        for (int i = 0; i < w && more; i++) {
+          DecodeBlock(r, c, &c.coef[((size_t)j * c.bw + i) * 64], ss, se, ah, al);
+          more = step();
+        }
+    } else {
+      for (int j = 0; j < mcuy && more; j++)
+        for (int i = 0; i < mcux && more; i++) {
+          for (JComp* c : sc)
+            for (int y = 0; y < c->v; y++)
+              for (int x = 0; x < c->h; x++) {
+                size_t blk = (size_t)(j * c->v + y) * c->bw + (i * c->h + x);
+                DecodeBlock(r, *c, &c->coef[blk * 64], ss, se, ah, al);
+              }
+          more = step();
+        }
+    }
+    drain();
+    pos = r.pos;
+    if (r.marker >= 0) pendingMarker = r.marker;
+  }
+  int pendingMarker = -1;
+
+  void Decode() {
+    if (n < 2 || b[0] != 0xFF || b[1] != 0xD8) Fail("jpeg: no SOI marker");
+    for (;;) {
+      int m;
+      if (pendingMarker >= 0) {
+        m = pendingMarker;
+        pendingMarker = -1;
+      } else {
+        m = Marker();
+        if (m < 0) continue;  // padding between segments
+      }
+      if (m == 0xD9) break;  // EOI
+      if (m == 0xC0 || m == 0xC1 || m == 0xC2) {
+        Frame(m);
+      } else if (m >= 0xC3 && m <= 0xCF && m != 0xC4 && m != 0xC8 && m != 0xCC) {
+        Fail("jpeg: only Huffman baseline / extended / progressive frames are supported");
+      } else if (m == 0xDB || m == 0xC4) {
+        Tables(m);
+      } else if (m == 0xDD) {
+        if (U16() != 4) Fail("jpeg: bad DRI length");
+        restart = U16();
+      } else if (m == 0xDA) {
+        if (!frame) Fail("jpeg: scan before the frame header");
+        Scan();
+      } else if ((m >= 0xE0 && m <= 0xEF) || m == 0xFE) {
+        Skip(m);
+      } else if (m >= 0xD0 && m <= 0xD7) {
+        // a stray restart marker between segments
+      } else {
+        Fail("jpeg: unknown marker");
+      }
+    }
+    if (!frame) Fail("jpeg: no frame header");
+    for (JComp& c : comp) {  // dequantise (16-bit wrap) and transform every block
+      if (!qSet[c.tq]) Fail("jpeg: undefined quantisation table");
+      c.plane.assign((size_t)c.bw * 8 * c.bh * 8, 0);
+      const uint16_t* qt = q[c.tq];
+      int16_t blk[64];
+      for (int j = 0; j < c.bh; j++)
+        for (int i = 0; i < c.bw; i++) {
+          const int16_t* d = &c.coef[((size_t)j * c.bw + i) * 64];
+          for (int k = 0; k < 64; k++) blk[k] = (int16_t)(d[k] * qt[k]);
+          IdctBlock(blk, &c.plane[(size_t)j * 8 * c.bw * 8 + (size_t)i * 8], c.bw * 8);
+        }
+    }
+  }
+};
+
+inline uint8_t Div4(int x) { return (uint8_t)(x >> 2); }
+inline uint8_t Div16(int x) { return (uint8_t)(x >> 4); }
+inline uint8_t Blinn(int x, int y) {  // x * y / 255, rounded
+  unsigned t = (unsigned)(x * y + 128);
+  return (uint8_t)((t + (t >> 8)) >> 8);
+}
+inline uint8_t LumaY(int r, int g, int b) { return (uint8_t)((r * 77 + g * 150 + 29 * b) >> 8); }
+
+// One output row of a component plane at hs x vs subsampling (w input samples).
+const uint8_t* Upsample(uint8_t* out, const uint8_t* nearRow, const uint8_t* farRow, int w, int hs, int vs) {
+  if (hs == 1 && vs == 1) return nearRow;
+  if (hs == 1 && vs == 2) {
+    for (int i = 0; i < w; i++) out[i] = Div4(3 * nearRow[i] + farRow[i] + 2);
+  } else if (hs == 2 && vs == 1) {
+    const uint8_t* in = nearRow;
+    if (w == 1) {
+      out[0] = out[1] = in[0];
+      return out;
+    }
+    out[0] = in[0];
+    out[1] = Div4(in[0] * 3 + in[1] + 2);
+    int i = 1;
+    for (; i < w - 1; i++) {
+      int c = 3 * in[i] + 2;
+      out[2 * i] = Div4(c + in[i - 1]);
+      out[2 * i + 1] = Div4(c + in[i + 1]);
+    }
+    out[2 * i] = Div4(in[w - 2] * 3 + in[w - 1] + 2);  // stb's last pair: 3/4 of the left sample (kept)
+    out[2 * i + 1] = in[w - 1];
+  } else if (hs == 2 && vs == 2) {
+    if (w == 1) {
+      out[0] = out[1] = Div4(3 * nearRow[0] + farRow[0] + 2);
+      return out;
+    }
+    int t1 = 3 * nearRow[0] + farRow[0];
+    out[0] = Div4(t1 + 2);
+    for (int i = 1; i < w; i++) {
+      int t0 = t1;
+      t1 = 3 * nearRow[i] + farRow[i];
+      out[2 * i - 1] = Div16(3 * t0 + t1 + 8);
+      out[2 * i] = Div16(3 * t1 + t0 + 8);
+    }
+    out[2 * w - 1] = Div4(t1 + 2);
+  } else {
+    for (int i = 0; i < w; i++)
+      for (int j = 0; j < hs; j++) out[i * hs + j] = nearRow[i];
+  }
+  return out;
+}
+
+void YCbCrRow(uint8_t* out, const uint8_t* y, const uint8_t* cb, const uint8_t* cr, int count) {
+  const int kCr = F2F(1.40200f) << 8, kCrG = F2F(0.71414f) << 8, kCbG = F2F(0.34414f) << 8,
+            kCb = F2F(1.77200f) << 8;
+  for (int i = 0; i < count; i++) {
+    int yf = (y[i] << 20) + (1 << 19);
+    int vr = cr[i] - 128, vb = cb[i] - 128;
+    int r = yf + vr * kCr;
+    int g = (int)((uint32_t)(yf + vr * -kCrG) + ((uint32_t)(vb * -kCbG) & 0xffff0000u));
+    int b = yf + vb * kCb;
+    out[3 * i] = Clamp255(r >> 20);
+    out[3 * i + 1] = Clamp255(g >> 20);
+    out[3 * i + 2] = Clamp255(b >> 20);
+  }
+}
+
+Ldr DecodeJpeg(const std::string& bytes, int req, bool flipY) {
+  JpegDecoder z;
+  z.b = (const uint8_t*)bytes.data();
+  z.n = bytes.size();
+  z.Decode();
+  const int nc = (int)z.comp.size();
+  const bool isRgb = nc == 3 && (z.rgbIds == 3 || (z.adobe == 0 && !z.jfif));
+  const int decodeN = (nc == 3 && req < 3 && !isRgb) ? 1 : nc;
+  struct Line {
+    const uint8_t *l0, *l1;
+    int hs, vs, ystep, ypos, wl;
+    std::vector<uint8_t> buf;
+  };
+  std::vector<Line> ln(decodeN);
+  for (int k = 0; k < decodeN; k++) {
+    const JComp& c = z.comp[k];
+    Line& L = ln[k];
+    L.hs = z.hmax / c.h;
+    L.vs = z.vmax / c.v;
+    L.ystep = L.vs >> 1;
+    L.ypos = 0;
+    L.wl = (z.X + L.hs - 1) / L.hs;
+    L.l0 = L.l1 = c.plane.data();
+    L.buf.resize((size_t)z.X + 3);
+  }
+  Ldr out;
+  out.width = z.X;
+  out.height = z.Y;
+  out.channels = req;
+  out.px.resize((size_t)z.X * z.Y * req);
+  std::vector<uint8_t> rgb((size_t)z.X * 3);
+  const uint8_t* co[4] = {};
+  for (int j = 0; j < z.Y; j++) {
+    for (int k = 0; k < decodeN; k++) {
+      Line& L = ln[k];
+      bool bot = L.ystep >= (L.vs >> 1);
+      co[k] = Upsample(L.buf.data(), bot ? L.l1 : L.l0, bot ? L.l0 : L.l1, L.wl, L.hs, L.vs);
+      if (++L.ystep >= L.vs) {
+        L.ystep = 0;
+        L.l0 = L.l1;
+        if (++L.ypos < z.comp[k].y) L.l1 += (size_t)z.comp[k].bw * 8;
+      }
+    }
+    uint8_t* o = &out.px[(size_t)j * z.X * req];
+    if (req == 3) {
+      if (nc == 3) {
+        if (isRgb) {
+          for (int i = 0; i < z.X; i++) {
+            o[3 * i] = co[0][i];
+            o[3 * i + 1] = co[1][i];
+            o[3 * i + 2] = co[2][i];
+          }
+        } else {
+          YCbCrRow(o, co[0], co[1], co[2], z.X);
+        }
+      } else if (nc == 4) {
+        if (z.adobe == 0) {  // CMYK
+          for (int i = 0; i < z.X; i++) {
+            int m = co[3][i];
+            o[3 * i] = Blinn(co[0][i], m);
+            o[3 * i + 1] = Blinn(co[1][i], m);
+            o[3 * i + 2] = Blinn(co[2][i], m);
+          }
+        } else if (z.adobe == 2) {  // YCCK
+          YCbCrRow(o, co[0], co[1], co[2], z.X);
+          for (int i = 0; i < z.X; i++) {
+            int m = co[3][i];
+            for (int c = 0; c < 3; c++) o[3 * i + c] = Blinn(255 - o[3 * i + c], m);
+          }
+        } else {  // YCbCr, the fourth component ignored
+          YCbCrRow(o, co[0], co[1], co[2], z.X);
+        }
+      } else {
+        for (int i = 0; i < z.X; i++) o[3 * i] = o[3 * i + 1] = o[3 * i + 2] = co[0][i];
+      }
+    } else {
+      if (isRgb) {
+        for (int i = 0; i < z.X; i++) o[i] = LumaY(co[0][i], co[1][i], co[2][i]);
+      } else if (nc == 4 && z.adobe == 0) {
+        for (int i = 0; i < z.X; i++) {
+          int m = co[3][i];
+          o[i] = LumaY(Blinn(co[0][i], m), Blinn(co[1][i], m), Blinn(co[2][i], m));
+        }
+      } else if (nc == 4 && z.adobe == 2) {
+        for (int i = 0; i < z.X; i++) o[i] = Blinn(255 - co[0][i], co[3][i]);
+      } else {
+        for (int i = 0; i < z.X; i++) o[i] = co[0][i];
+      }
+    }
+  }
+  if (flipY) FlipRows(out.px.data(), out.height, (size_t)out.width * req);
+  return out;
+}
+
+bool IsJpeg(const std::string& b) { return b.size() >= 3 && (uint8_t)b[0] == 0xFF && (uint8_t)b[1] == 0xD8 && (uint8_t)b[2] == 0xFF; }
+
 bool IsPng(const std::string& b) { return b.size() >= 8 && std::memcmp(b.data(), "\x89PNG\r\n\x1a\n", 8) == 0; }
 bool IsPnm(const std::string& b) { return b.size() >= 3 && b[0] == 'P' && (b[1] == '5' || b[1] == '6'); }
 
@@ -459,13 +1184,14 @@ Ldr LoadLdr(const std::string& bytes, int reqChannels, bool flipY) {
   if (reqChannels != 1 && reqChannels != 3) Fail("channel must be 1 or 3");
   if (IsPng(bytes)) return DecodePng(bytes, reqChannels, flipY);
   if (IsPnm(bytes)) return DecodePnm(bytes, reqChannels, flipY);
-  Fail("unsupported image format (PNG and binary PNM are read)");
+  if (IsJpeg(bytes)) return DecodeJpeg(bytes, reqChannels, flipY);
+  Fail("unsupported image format (PNG, JPEG and binary PNM are read)");
 }
 
 // --------------------------------------------------------------------- HDR
 Hdr LoadHdr(const std::string& bytes, bool flipY) {
   Hdr out;
-  if (IsPng(bytes) || IsPnm(bytes)) {  // stbi_loadf of an LDR file
+  if (IsPng(bytes) || IsPnm(bytes) || IsJpeg(bytes)) {  // stbi_loadf of an LDR file
     Ldr l = LoadLdr(bytes, 3, flipY);
     out.width = l.width;
     out.height = l.height;

@@ -31,12 +31,25 @@ def lights(dirpath, w=48, h=48, spp=4, seed=1):
     return write(dirpath, "lights_%dx%d_%d_%d" % (w, h, spp, seed), scenes.lights_room(w, h, spp, seed))
 
 
-def textured_room_scene(w=48, h=48, spp=4, seed=1, renderer="path"):
+def _jpeg_rgb(rgb, scans=None, restart=0, sampling=((2, 2), (1, 1), (1, 1))):
+    """An RGB image as a JFIF YCbCr JPEG (imgenc.jpeg) with a mild quantiser."""
+    import imgenc
+    r, g, b = (rgb[..., k].astype(np.float64) for k in range(3))
+    planes = [0.299 * r + 0.587 * g + 0.114 * b, -0.168736 * r - 0.331264 * g + 0.5 * b + 128,
+              0.5 * r - 0.418688 * g - 0.081312 * b + 128]
+    q = [np.full(64, 3), np.full(64, 5), np.full(64, 5)]
+    h, w = rgb.shape[:2]
+    return imgenc.jpeg(planes, list(sampling), q, w, h, scans=scans, restart=restart)[0]
+
+
+def textured_room_scene(w=48, h=48, spp=4, seed=1, renderer="path", jpeg=False):
     """Box room whose materials read textures of every kind: bitmaps from PNG
     (RGB and mono), Radiance HDR and OpenEXR assets with nearest / bilinear /
     trilinear / anisotropic filters and clamp / repeat wrapping, nested
     chessboards, a textured mask opacity and textured microfacet roughness.
-    Returns (scene dict, {file name: bytes})."""
+    jpeg: the two PNG textures become JPEG files (a progressive 4:2:0 colour
+    image, a sequential grey one with restart markers). Returns (scene dict,
+    {file name: bytes})."""
     import imgenc
     rng = np.random.default_rng(11)
     yy, xx = np.mgrid[0:64, 0:64]
@@ -46,6 +59,13 @@ def textured_room_scene(w=48, h=48, spp=4, seed=1, renderer="path"):
     exr_img = {k: (0.3 + 0.6 * rng.random((16, 16))).astype(np.float16) for k in "RGB"}
     assets = {"tiles.png": imgenc.png(tiles.clip(0, 255)), "grain.png": imgenc.png(grain.clip(0, 255)),
               "sky.hdr": imgenc.hdr(hdr_img), "metal.exr": imgenc.exr(exr_img, 3)}
+    if jpeg:
+        prog = [((1, 2, 3), 0, 0, 0, 1), ((1,), 1, 5, 0, 2), ((1,), 6, 63, 0, 2), ((2,), 1, 63, 0, 1),
+                ((3,), 1, 63, 0, 1), ((1,), 1, 63, 2, 1), ((1, 2, 3), 0, 0, 1, 0), ((1,), 1, 63, 1, 0),
+                ((2,), 1, 63, 1, 0), ((3,), 1, 63, 1, 0)]
+        assets["tiles.png"] = _jpeg_rgb(tiles.clip(0, 255), scans=prog)
+        assets["grain.png"] = imgenc.jpeg([grain[..., 0].clip(0, 255)], [(1, 1)], [np.full(64, 2)], 64, 64,
+                                          restart=5)[0]
     sc = scenes.box_room(w, h, spp, seed)
     if renderer == "vol_path":
         sc["renderer"] = {"type": "vol_path", "max_depth": 8, "rr_depth": 3}
@@ -137,9 +157,10 @@ def textured_projection_room(w=48, h=48, spp=4, seed=1, renderer="path"):
     return sc, {"slide.png": imgenc.png(img.clip(0, 255))}
 
 
-def textured(dirpath, w=48, h=48, spp=4, seed=1, renderer="path"):
-    sc, assets = textured_room_scene(w, h, spp, seed, renderer)
-    return write(dirpath, "textured_%s_%dx%d_%d_%d" % (renderer, w, h, spp, seed), sc, assets)
+def textured(dirpath, w=48, h=48, spp=4, seed=1, renderer="path", jpeg=False):
+    sc, assets = textured_room_scene(w, h, spp, seed, renderer, jpeg)
+    return write(dirpath, "textured_%s_%dx%d_%d_%d%s" % (renderer, w, h, spp, seed, "_jpeg" if jpeg else ""), sc,
+                 assets)
 
 
 def volume(dirpath, w=48, h=48, spp=4, grid=32, max_depth=32):

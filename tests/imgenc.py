@@ -1,7 +1,9 @@
 """Image encoders for the decoder tests and textured test scenes, written from the
 format specifications with Python's zlib: PNG (every colour type and bit depth,
 the five row filters, Adam7 interlacing), binary PNM, Radiance RGBE (flat and
-run-length) and OpenEXR scanline files (NONE / RLE / ZIPS / ZIP; HALF / FLOAT).
+run-length), OpenEXR scanline files (NONE / RLE / ZIPS / ZIP; HALF / FLOAT) and
+Huffman JPEG (sequential and progressive, any sampling factors, restart
+intervals).
 """
 import struct
 import zlib
@@ -204,3 +206,341 @@ def exr(channels, compression=0, ymin=0, xmin=0):
         offs.append(pos)
         pos += len(c)
     return header + b"".join(struct.pack("<Q", o) for o in offs) + b"".join(chunks)
+
+
+# ------------------------------------------------------------------- JPEG
+# ITU-T T.81 encoder (Huffman; sequential or progressive): the component planes
+# are given (already in the colour space to store), transformed by a float DCT,
+# quantised and entropy coded with Huffman tables built from the symbol counts
+# (T.81 K.2). jpeg() returns the file and the quantised coefficients, so a test
+# can reconstruct the samples without entropy decoding.
+
+def _zigzag():
+    out = []
+    for s in range(15):
+        rows = range(max(0, s - 7), min(s, 7) + 1)
+        for r in (rows if s % 2 else reversed(rows)):
+            out.append(r * 8 + (s - r))
+    return np.array(out)
+
+
+ZIGZAG = _zigzag()  # zigzag index -> row-major index
+_DCT = np.array([[(np.sqrt(0.5) if u == 0 else 1.0) * 0.5 * np.cos((2 * x + 1) * u * np.pi / 16)
+                  for x in range(8)] for u in range(8)])
+
+
+class _BitWriter:
+    def __init__(self):
+        self.out = bytearray()
+        self.acc = 0
+        self.n = 0
+
+    def bits(self, v, n):
+        for i in range(n - 1, -1, -1):
+            self.acc = (self.acc << 1) | ((v >> i) & 1)
+            self.n += 1
+            if self.n == 8:
+                self.out.append(self.acc)
+                if self.acc == 0xFF:
+                    self.out.append(0)
+                self.acc = self.n = 0
+
+    def flush(self):  # pad with 1 bits
+        if self.n:
+            self.bits((1 << (8 - self.n)) - 1, 8 - self.n)
+
+
+def _huff_table(freq):
+    """Code lengths limited to 16 bits (T.81 K.2) -> (counts[16], symbols, {sym: (code, len)})."""
+    import heapq
+    syms = [s for s in range(256) if freq[s]]
+    if not syms:
+        syms = [0]
+    # Huffman code lengths with a reserved symbol (frequency 1) that takes the all-ones code
+    heap = [(int(freq[s]), i, [s]) for i, s in enumerate(syms)] + [(1, 10 ** 6, [256])]
+    heapq.heapify(heap)
+    size = {s: 0 for s in syms + [256]}
+    tie = 10 ** 6 + 1
+    while len(heap) > 1:
+        f1, _, a = heapq.heappop(heap)
+        f2, _, b = heapq.heappop(heap)
+        for s in a + b:
+            size[s] += 1
+        heapq.heappush(heap, (f1 + f2, tie, a + b))
+        tie += 1
+    bits = [0] * 40
+    for s, l in size.items():
+        bits[l] += 1
+    i = 39
+    while i > 16:
+        while bits[i] > 0:
+            j = i - 2
+            while bits[j] == 0:
+                j -= 1
+            bits[i] -= 2
+            bits[i - 1] += 1
+            bits[j + 1] += 2
+            bits[j] -= 1
+        i -= 1
+    while bits[i] == 0:
+        i -= 1
+    bits[i] -= 1  # the reserved symbol, last of the longest codes
+    order = sorted(syms, key=lambda s: (-int(freq[s]), s))
+    lens = []
+    for l in range(1, 17):
+        lens += [l] * bits[l]
+    codes, code, k = {}, 0, 0
+    for l in range(1, 17):
+        for _ in range(bits[l]):
+            codes[order[k]] = (code, l)
+            code += 1
+            k += 1
+        code <<= 1
+    return bits[1:17], order[:k], codes
+
+
+def _nbits(a):
+    return int(a).bit_length()
+
+
+def _magnitude_bits(v, s):
+    return v if v > 0 else (v - 1) & ((1 << s) - 1)
+
+
+class _ScanCoder:
+    """Emits one scan twice: a counting pass (symbol frequencies) and a writing pass."""
+
+    def __init__(self, dc, ac, w):
+        self.dc, self.ac, self.w = dc, ac, w  # dc / ac: {table: codes} or {table: freq array}
+
+    def sym(self, kind, t, s):
+        tab = (self.dc if kind == 0 else self.ac)[t]
+        if self.w is None:
+            tab[s] += 1
+        else:
+            code, l = tab[s]
+            self.w.bits(code, l)
+
+    def raw(self, v, n):
+        if self.w is not None and n:
+            self.w.bits(v, n)
+
+
+def _encode_scan(sc, comps, coef, scan, mcux, mcuy, X, Y, hmax, vmax, restart, rst):
+    """One scan of the coefficients through coder sc (T.81 G.1.2 for the progressive cases)."""
+    ids, ss, se, ah, al, prog = scan
+    members = [c for c in comps if c["id"] in ids]
+    st = {"eobrun": 0, "be": [], "pred": {c["id"]: 0 for c in members}}
+
+    def flush_eob(t):
+        if st["eobrun"]:
+            n = _nbits(st["eobrun"]) - 1
+            sc.sym(1, t, n << 4)
+            sc.raw(st["eobrun"] - (1 << n), n)
+            for b in st["be"]:
+                sc.raw(b, 1)
+            st["eobrun"], st["be"] = 0, []
+
+    def block(c, blk):
+        d = coef[c["id"]][blk]
+        if not prog:  # sequential
+            diff = int(d[0]) - st["pred"][c["id"]]
+            st["pred"][c["id"]] = int(d[0])
+            s = _nbits(abs(diff))
+            sc.sym(0, c["td"], s)
+            sc.raw(_magnitude_bits(diff, s), s)
+            r = 0
+            for k in range(1, 64):
+                v = int(d[ZIGZAG[k]])
+                if v == 0:
+                    r += 1
+                    continue
+                while r > 15:
+                    sc.sym(1, c["ta"], 0xF0)
+                    r -= 16
+                s = _nbits(abs(v))
+                sc.sym(1, c["ta"], (r << 4) | s)
+                sc.raw(_magnitude_bits(v, s), s)
+                r = 0
+            if r:
+                sc.sym(1, c["ta"], 0)
+            return
+        if ss == 0:  # DC scans
+            v = int(d[0]) >> al
+            if ah == 0:
+                diff = v - st["pred"][c["id"]]
+                st["pred"][c["id"]] = v
+                s = _nbits(abs(diff))
+                sc.sym(0, c["td"], s)
+                sc.raw(_magnitude_bits(diff, s), s)
+            else:
+                sc.raw(v & 1, 1)
+            return
+        t = c["ta"]
+        if ah == 0:  # first AC scan of the band
+            r = 0
+            for k in range(ss, se + 1):
+                v = int(d[ZIGZAG[k]])
+                a = abs(v) >> al
+                if a == 0:
+                    r += 1
+                    continue
+                flush_eob(t)
+                while r > 15:
+                    sc.sym(1, t, 0xF0)
+                    r -= 16
+                s = _nbits(a)
+                sc.sym(1, t, (r << 4) | s)
+                sc.raw(_magnitude_bits(a if v > 0 else -a, s), s)
+                r = 0
+            if r:
+                st["eobrun"] += 1
+                if st["eobrun"] == 0x7FFF:
+                    flush_eob(t)
+            return
+        absv = [abs(int(d[ZIGZAG[k]])) >> al for k in range(ss, se + 1)]
+        eob = max([i for i, a in enumerate(absv) if a == 1], default=-1)
+        r, br = 0, []
+        for i, a in enumerate(absv):
+            if a == 0:
+                r += 1
+                continue
+            while r > 15 and i <= eob:
+                flush_eob(t)
+                sc.sym(1, t, 0xF0)
+                r -= 16
+                for b in br:
+                    sc.raw(b, 1)
+                br = []
+            if a > 1:
+                br.append(a & 1)
+                continue
+            flush_eob(t)
+            sc.sym(1, t, (r << 4) | 1)
+            sc.raw(1 if int(d[ZIGZAG[ss + i]]) > 0 else 0, 1)
+            for b in br:
+                sc.raw(b, 1)
+            br, r = [], 0
+        if r or br:
+            st["eobrun"] += 1
+            st["be"] += br
+            if st["eobrun"] == 0x7FFF or len(st["be"]) > 900:
+                flush_eob(t)
+
+    units = []
+    if len(members) == 1:
+        c = members[0]
+        cx, cy = -(-X * c["h"] // hmax), -(-Y * c["v"] // vmax)
+        for j in range(-(-cy // 8)):
+            for i in range(-(-cx // 8)):
+                units.append([(c, (j, i))])
+    else:
+        for j in range(mcuy):
+            for i in range(mcux):
+                units.append([(c, (j * c["v"] + y, i * c["h"] + x)) for c in members
+                              for y in range(c["v"]) for x in range(c["h"])])
+    ac_t = members[0]["ta"]
+    for u, unit in enumerate(units):
+        if restart and u and u % restart == 0:
+            flush_eob(ac_t)
+            rst(u // restart - 1)
+            st["pred"] = {c["id"]: 0 for c in members}
+        for c, blk in unit:
+            block(c, blk)
+    flush_eob(ac_t)
+
+
+def jpeg(planes, sampling, quant, X, Y, ids=None, scans=None, restart=0, app=(), qtab=None, seed=0):
+    """planes: per component a float array (Y x X, 0..255 samples at full
+    resolution; subsampled components are box-averaged). sampling: (h, v) per
+    component. quant: per component a 64-entry table (row-major). scans: None for
+    one interleaved sequential scan, a list of component-id tuples for
+    sequential scans of those components, or progressive scans
+    (ids, Ss, Se, Ah, Al). Returns (file bytes, {component id: coefficient
+    blocks (by, bx, 64) row-major int}, component records)."""
+    nc = len(planes)
+    ids = ids or list(range(1, nc + 1))
+    hmax = max(h for h, _ in sampling)
+    vmax = max(v for _, v in sampling)
+    mcux, mcuy = -(-X // (8 * hmax)), -(-Y // (8 * vmax))
+    comps, coef = [], {}
+    qtables = []
+    for k in range(nc):
+        h, v = sampling[k]
+        q = np.asarray(quant[k], dtype=np.int64).reshape(64)
+        tq = next((i for i, t in enumerate(qtables) if np.array_equal(t, q)), None)
+        if tq is None:
+            tq = len(qtables)
+            qtables.append(q)
+        c = {"id": ids[k], "h": h, "v": v, "tq": tq, "td": min(k, 1), "ta": min(k, 1)}
+        comps.append(c)
+        fx, fy = hmax // h, vmax // v
+        pw, ph = mcux * 8 * hmax, mcuy * 8 * vmax
+        full = np.pad(np.asarray(planes[k], np.float64), ((0, ph - Y), (0, pw - X)), mode="edge")
+        sub = full.reshape(ph // fy, fy, pw // fx, fx).mean(axis=(1, 3))
+        cx, cy = -(-X * h // hmax), -(-Y * v // vmax)
+        # samples past the component's own size repeat its edge (as encoders pad)
+        sub[:, cx:] = sub[:, cx - 1:cx]
+        sub[cy:, :] = sub[cy - 1:cy, :]
+        blocks = sub.reshape(ph // fy // 8, 8, pw // fx // 8, 8).transpose(0, 2, 1, 3) - 128.0
+        f = np.einsum("ux,abxy,vy->abuv", _DCT, blocks, _DCT)  # [by, bx, vertical u, horizontal v]
+        coef[c["id"]] = np.round(f.reshape(f.shape[0], f.shape[1], 64) / q).astype(np.int64)
+    progressive = scans is not None and len(scans[0]) == 5
+    if scans is None:
+        scans = [tuple(ids)]
+    full_scans = []
+    for s in scans:
+        if progressive:
+            full_scans.append((tuple(s[0]), s[1], s[2], s[3], s[4], True))
+        else:
+            full_scans.append((tuple(s), 0, 63, 0, 0, False))
+    out = bytearray(b"\xff\xd8")
+    for a in app:
+        out += a
+    for t, q in enumerate(qtables):
+        sixteen = int(q.max() > 255)
+        body = bytes([(sixteen << 4) | t]) + b"".join(
+            (int(q[ZIGZAG[i]]).to_bytes(2, "big") if sixteen else bytes([int(q[ZIGZAG[i]])])) for i in range(64))
+        out += b"\xff\xdb" + struct.pack(">H", 2 + len(body)) + body
+    sof = bytes([8]) + struct.pack(">HHB", Y, X, nc) + b"".join(
+        bytes([c["id"], (c["h"] << 4) | c["v"], c["tq"]]) for c in comps)
+    out += (b"\xff\xc2" if progressive else b"\xff\xc0") + struct.pack(">H", 2 + len(sof)) + sof
+    if restart:
+        out += b"\xff\xdd" + struct.pack(">HH", 4, restart)
+    for scan in full_scans:
+        sid = scan[0]
+        members = [c for c in comps if c["id"] in sid]
+        # counting pass: symbol frequencies per table
+        fdc = {c["td"]: np.zeros(257, np.int64) for c in members}
+        fac = {c["ta"]: np.zeros(257, np.int64) for c in members}
+        _encode_scan(_ScanCoder(fdc, fac, None), comps, coef, scan, mcux, mcuy, X, Y, hmax, vmax, restart,
+                     lambda m: None)
+        need_dc = scan[1] == 0 and scan[3] == 0
+        need_ac = scan[2] > 0
+        dht = b""
+        cdc, cac = {}, {}
+        for t, fr in fdc.items():
+            if need_dc:
+                counts, order, cdc[t] = _huff_table(fr)
+                dht += bytes([t]) + bytes(counts) + bytes(order)
+        for t, fr in fac.items():
+            if need_ac:
+                counts, order, cac[t] = _huff_table(fr)
+                dht += bytes([0x10 | t]) + bytes(counts) + bytes(order)
+        if dht:
+            out += b"\xff\xc4" + struct.pack(">H", 2 + len(dht)) + dht
+        sos = bytes([len(members)]) + b"".join(bytes([c["id"], (c["td"] << 4) | c["ta"]]) for c in members)
+        sos += bytes([scan[1], scan[2], (scan[3] << 4) | scan[4]])
+        out += b"\xff\xda" + struct.pack(">H", 2 + len(sos)) + sos
+        w = _BitWriter()
+
+        def rst(m, w=w):
+            w.flush()
+            w.out += bytes([0xFF, 0xD0 + (m & 7)])
+
+        _encode_scan(_ScanCoder(cdc, cac, w), comps, coef, scan, mcux, mcuy, X, Y, hmax, vmax, restart, rst)
+        w.flush()
+        out += w.out
+    out += b"\xff\xd9"
+    qt = {c["id"]: qtables[c["tq"]] for c in comps}
+    return bytes(out), coef, comps, qt

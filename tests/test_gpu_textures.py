@@ -59,9 +59,11 @@ def _sample_parity(g, o, spp, min_frac):
     assert np.all(np.abs(mg - mo) <= 0.02 * np.abs(mo) + 1e-6), (mg, mo)
 
 
-@pytest.mark.parametrize("renderer", ["path", "vol_path"])
-def test_textured_room_samples(rad, oracle, scene_dir, renderer):
-    path, text, d = textured(scene_dir, 48, 48, 4, renderer=renderer)
+@pytest.mark.parametrize("renderer,jpeg", [("path", False), ("vol_path", False), ("path", True)])
+def test_textured_room_samples(rad, oracle, scene_dir, renderer, jpeg):
+    """jpeg: the colour and grey bitmaps are read from JPEG files (progressive
+    4:2:0, sequential grey with restart markers) by the library's decoder."""
+    path, text, d = textured(scene_dir, 48, 48, 4, renderer=renderer, jpeg=jpeg)
     g, o = rad.Scene.from_file(path), oracle.OracleScene(text, d)
     _sample_parity(g, o, 4, 0.97)
     g.close()

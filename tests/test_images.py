@@ -131,5 +131,8 @@ def test_bad_files_are_reported(oracle, tmp_path):
     with pytest.raises(RuntimeError):
         oracle.image_load({"type": "image_default"}, tmp_path / "x.png")
     (tmp_path / "y.jpg").write_bytes(b"\xff\xd8\xff\xe0garbage")
-    with pytest.raises(RuntimeError, match="unsupported image format"):
+    with pytest.raises(RuntimeError, match="jpeg"):
         oracle.image_load({"type": "image_default"}, tmp_path / "y.jpg")
+    (tmp_path / "z.gif").write_bytes(b"GIF89a\x01\x00\x01\x00")
+    with pytest.raises(RuntimeError, match="unsupported image format"):
+        oracle.image_load({"type": "image_default"}, tmp_path / "z.gif")
