@@ -1175,6 +1175,314 @@ Ldr DecodeJpeg(const std::string& bytes, int req, bool flipY) {
 
 bool IsJpeg(const std::string& b) { return b.size() >= 3 && (uint8_t)b[0] == 0xFF && (uint8_t)b[1] == 0xD8 && (uint8_t)b[2] == 0xFF; }
 
+// ---------------------------------------------------------------------- BMP
+// Windows / OS2 bitmaps as stb_image reads them: BITMAPCOREHEADER (12 bytes)
+// and the 40 / 56 / 108 / 124-byte info headers, 1 / 4 / 8-bit palettes,
+// 24-bit BGR, 16 / 32-bit pixels through channel masks (BI_RGB defaults 5-5-5 and
+// 8-8-8-8, or BI_BITFIELDS), each field widened to 8 bits by bit replication;
+// rows are bottom-up unless the height is negative. RLE compression is refused.
+// A 32-bit image whose alpha field is zero everywhere reads as opaque.
+uint32_t LE32(const uint8_t* p) { return p[0] | (p[1] << 8) | (p[2] << 16) | ((uint32_t)p[3] << 24); }
+int LE16(const uint8_t* p) { return p[0] | (p[1] << 8); }
+
+int HighBit(uint32_t z) {
+  int n = -1;
+  while (z) {
+    n++;
+    z >>= 1;
+  }
+  return n;
+}
+int BitCount(uint32_t a) {
+  int n = 0;
+  for (; a; a &= a - 1) n++;
+  return n;
+}
+// the field (v & mask) >> shift, `bits` wide, widened to 8 bits by replicating its bits
+int MaskField(uint32_t v, uint32_t mask, int shift, int bits) {
+  if (!mask) return 0;
+  v &= mask;
+  if (shift < 0)
+    v <<= -shift;
+  else
+    v >>= shift;
+  if (bits >= 8) return (int)(v & 255);
+  v >>= 8 - bits;  // the field's top `bits` bits of the 8-bit window
+  int r = 0;
+  for (int got = 0; got < 8; got += bits) r = (r << bits) | (int)v;  // replicate ...
+  int total = ((8 + bits - 1) / bits) * bits;
+  return r >> (total - 8);  // ... and keep the top 8 bits
+}
+
+Ldr DecodeBmp(const std::string& bytes, int req, bool flipY) {
+  const uint8_t* b = (const uint8_t*)bytes.data();
+  size_t n = bytes.size();
+  if (n < 26) Fail("bmp: truncated header");
+  uint32_t offset = LE32(b + 10), hsz = LE32(b + 14);
+  if (hsz != 12 && hsz != 40 && hsz != 56 && hsz != 108 && hsz != 124) Fail("bmp: unknown header size");
+  if (14 + (size_t)hsz > n) Fail("bmp: truncated header");
+  const uint8_t* h = b + 14;
+  int64_t w, ht;
+  int bpp;
+  uint32_t compress = 0, mr = 0, mg = 0, mb = 0, ma = 0;
+  if (hsz == 12) {
+    w = LE16(h + 4);
+    ht = LE16(h + 6);
+    bpp = LE16(h + 10);
+  } else {
+    w = (int32_t)LE32(h + 4);
+    ht = (int32_t)LE32(h + 8);
+    bpp = LE16(h + 14);
+    compress = LE32(h + 16);
+  }
+  if (LE16(h + (hsz == 12 ? 8 : 12)) != 1) Fail("bmp: planes must be 1");
+  bool topDown = ht < 0;
+  if (topDown) ht = -ht;
+  if (w <= 0 || ht <= 0 || w > (1 << 24) || ht > (1 << 24)) Fail("bmp: bad size");
+  if (compress == 1 || compress == 2) Fail("bmp: RLE compression is not supported");
+  if (compress != 0 && compress != 3) Fail("bmp: unsupported compression");
+  size_t extra = 14 + hsz;
+  if (bpp == 16 || bpp == 32) {
+    if (compress == 0) {
+      if (bpp == 32) {
+        mr = 0xffu << 16;
+        mg = 0xffu << 8;
+        mb = 0xffu;
+        ma = 0xffu << 24;
+      } else {
+        mr = 31u << 10;
+        mg = 31u << 5;
+        mb = 31u;
+      }
+    } else if (hsz == 40) {  // BI_BITFIELDS: three masks follow the header
+      if (extra + 12 > n) Fail("bmp: truncated masks");
+      mr = LE32(b + extra);
+      mg = LE32(b + extra + 4);
+      mb = LE32(b + extra + 8);
+      extra += 12;
+      if (mr == mg && mg == mb) Fail("bmp: bad masks");
+    } else {
+      mr = LE32(h + 40);
+      mg = LE32(h + 44);
+      mb = LE32(h + 48);
+      ma = hsz >= 56 ? LE32(h + 52) : 0;
+    }
+  } else if (bpp != 1 && bpp != 4 && bpp != 8 && bpp != 24) {
+    Fail("bmp: unsupported bit depth");
+  } else if (compress == 3) {
+    Fail("bmp: bitfields need 16 or 32-bit pixels");
+  }
+  const int src = ma ? 4 : 3;  // samples per pixel before the requested conversion
+  std::vector<uint8_t> px((size_t)w * ht * src);
+  uint8_t pal[256][4] = {};
+  if (bpp < 16) {
+    int esz = hsz == 12 ? 3 : 4;
+    int64_t psize = offset > extra ? (int64_t)(offset - extra) / esz : 0;
+    if (psize <= 0 || psize > 256) Fail("bmp: bad palette");
+    if (extra + (size_t)psize * esz > n) Fail("bmp: truncated palette");
+    for (int i = 0; i < psize; i++) {
+      const uint8_t* e = b + extra + (size_t)i * esz;
+      pal[i][0] = e[2];
+      pal[i][1] = e[1];
+      pal[i][2] = e[0];
+      pal[i][3] = 255;
+    }
+  }
+  size_t rowBytes = (((size_t)w * bpp + 31) / 32) * 4;
+  if (offset > n || (size_t)ht * rowBytes > n - offset) Fail("bmp: pixel data truncated");
+  int rs = HighBit(mr) - 7, gs = HighBit(mg) - 7, bs = HighBit(mb) - 7, as = HighBit(ma) - 7;
+  int rc = BitCount(mr), gc = BitCount(mg), bc = BitCount(mb), ac = BitCount(ma);
+  bool anyAlpha = false;
+  for (int64_t y = 0; y < ht; y++) {
+    const uint8_t* row = b + offset + (size_t)y * rowBytes;
+    int64_t oy = topDown ? y : ht - 1 - y;  // output rows top to bottom
+    uint8_t* o = &px[(size_t)oy * w * src];
+    for (int64_t x = 0; x < w; x++, o += src) {
+      if (bpp < 16) {
+        int idx;
+        if (bpp == 8) {
+          idx = row[x];
+        } else if (bpp == 4) {
+          idx = (row[x >> 1] >> ((x & 1) ? 0 : 4)) & 15;
+        } else {
+          idx = (row[x >> 3] >> (7 - (x & 7))) & 1;
+        }
+        o[0] = pal[idx][0];
+        o[1] = pal[idx][1];
+        o[2] = pal[idx][2];
+      } else if (bpp == 24) {
+        const uint8_t* p = row + 3 * x;
+        o[0] = p[2];
+        o[1] = p[1];
+        o[2] = p[0];
+      } else {
+        uint32_t v = bpp == 16 ? (uint32_t)LE16(row + 2 * x) : LE32(row + 4 * x);
+        o[0] = (uint8_t)MaskField(v, mr, rs, rc);
+        o[1] = (uint8_t)MaskField(v, mg, gs, gc);
+        o[2] = (uint8_t)MaskField(v, mb, bs, bc);
+        if (src == 4) {
+          o[3] = (uint8_t)(ma ? MaskField(v, ma, as, ac) : 255);
+          anyAlpha |= o[3] != 0;
+        }
+      }
+    }
+  }
+  if (src == 4 && !anyAlpha)
+    for (size_t i = 3; i < px.size(); i += 4) px[i] = 255;
+  Ldr out;
+  out.width = (int)w;
+  out.height = (int)ht;
+  out.channels = req;
+  ConvertChannels(px, src, req, (size_t)w * ht, out.px);
+  if (flipY) FlipRows(out.px.data(), out.height, (size_t)out.width * req);
+  return out;
+}
+
+// ---------------------------------------------------------------------- TGA
+// Truevision TGA as stb_image reads it: colour-mapped (type 1 / 9), true-colour
+// (2 / 10) and grey (3 / 11) images, run-length packets for the 9..11 types,
+// 8-bit grey or indices, 15 / 16-bit 5-5-5 colour (each field scaled by
+// 255 / 31, no alpha), 24-bit BGR and 32-bit BGRA; rows bottom-up unless the
+// descriptor's top-to-bottom bit is set.
+Ldr DecodeTga(const std::string& bytes, int req, bool flipY) {
+  const uint8_t* b = (const uint8_t*)bytes.data();
+  size_t n = bytes.size();
+  if (n < 18) Fail("tga: truncated header");
+  int idLen = b[0], cmapType = b[1], type = b[2];
+  int cmapFirst = LE16(b + 3), cmapLen = LE16(b + 5), cmapBits = b[7];
+  int w = LE16(b + 12), ht = LE16(b + 14), bits = b[16], desc = b[17];
+  bool rle = type >= 8;
+  int base = rle ? type - 8 : type;
+  if (cmapType > 1 || (base != 1 && base != 2 && base != 3)) Fail("tga: unsupported image type");
+  if ((base == 1) != (cmapType == 1)) Fail("tga: colour map and image type disagree");
+  if (w == 0 || ht == 0) Fail("tga: zero size");
+  auto compOf = [](int bitsPer, bool grey) {  // stbi__tga_get_comp
+    if (bitsPer == 8) return grey ? 1 : 0;
+    if (bitsPer == 15 || bitsPer == 16) return bitsPer == 16 && grey ? 2 : 3;
+    if (bitsPer == 24) return 3;
+    if (bitsPer == 32) return 4;
+    return 0;
+  };
+  int comp;
+  if (base == 1) {
+    if (bits != 8 && bits != 16) Fail("tga: colour-map indices must be 8 or 16 bits");
+    comp = compOf(cmapBits, false);
+  } else {
+    comp = compOf(bits, base == 3);
+  }
+  if (comp == 0 || comp == 2) Fail("tga: unsupported pixel format");
+  size_t pos = 18 + (size_t)idLen;
+  const bool rgb16 = (base == 1 ? cmapBits : bits) == 15 || (base == 1 ? cmapBits : bits) == 16;
+  auto readPixel = [&](const uint8_t* p, int nbits, uint8_t* o) {
+    if (nbits == 15 || nbits == 16) {
+      int v = LE16(p);
+      int r = (v >> 10) & 31, g = (v >> 5) & 31, bl = v & 31;
+      o[0] = (uint8_t)((r * 255) / 31);
+      o[1] = (uint8_t)((g * 255) / 31);
+      o[2] = (uint8_t)((bl * 255) / 31);
+    } else {
+      for (int i = 0; i < nbits / 8; i++) o[i] = p[i];
+    }
+  };
+  std::vector<uint8_t> cmap;
+  int cmapBytes = (cmapBits + 1) >> 3;
+  if (cmapType == 1) {
+    if (pos + (size_t)cmapFirst * 0 + (size_t)cmapLen * cmapBytes > n) Fail("tga: truncated colour map");
+    cmap.resize((size_t)cmapLen * comp);
+    for (int i = 0; i < cmapLen; i++) readPixel(b + pos + (size_t)i * cmapBytes, cmapBits, &cmap[(size_t)i * comp]);
+    pos += (size_t)cmapLen * cmapBytes;
+  }
+  const int pixBytes = (bits + 1) >> 3;
+  std::vector<uint8_t> px((size_t)w * ht * comp);
+  size_t total = (size_t)w * ht;
+  uint8_t cur[4] = {};
+  int runLeft = 0;
+  bool repeat = false, first = true;
+  for (size_t i = 0; i < total; i++) {
+    bool read = true;
+    if (rle) {
+      if (runLeft == 0) {
+        if (pos >= n) Fail("tga: truncated data");
+        int hdr = b[pos++];
+        runLeft = 1 + (hdr & 127);
+        repeat = (hdr & 128) != 0;
+        read = true;
+      } else if (repeat) {
+        read = false;
+      }
+      runLeft--;
+    }
+    if (read || first) {
+      if (pos + pixBytes > n) Fail("tga: truncated data");
+      const uint8_t* p = b + pos;
+      pos += pixBytes;
+      if (base == 1) {
+        int idx = pixBytes == 1 ? p[0] : LE16(p);
+        idx -= cmapFirst;
+        if (idx < 0 || idx >= cmapLen) idx = 0;
+        std::memcpy(cur, &cmap[(size_t)idx * comp], comp);
+      } else {
+        readPixel(p, bits, cur);
+      }
+      first = false;
+    }
+    std::memcpy(&px[i * comp], cur, comp);
+  }
+  if (comp >= 3 && !rgb16)  // BGR(A) -> RGB(A)
+    for (size_t i = 0; i < total; i++) std::swap(px[i * comp], px[i * comp + 2]);
+  if (!((desc >> 5) & 1)) FlipRows(px.data(), ht, (size_t)w * comp);  // stored bottom-up
+  Ldr out;
+  out.width = w;
+  out.height = ht;
+  out.channels = req;
+  ConvertChannels(px, comp, req, total, out.px);
+  if (flipY) FlipRows(out.px.data(), out.height, (size_t)out.width * req);
+  return out;
+}
+
+bool IsBmp(const std::string& b) { return b.size() >= 2 && b[0] == 'B' && b[1] == 'M'; }
+// stbi__tga_test: a plausible header (no magic number)
+bool IsTga(const std::string& s) {
+  if (s.size() < 18) return false;
+  const uint8_t* b = (const uint8_t*)s.data();
+  int cmapType = b[1], type = b[2];
+  if (cmapType > 1) return false;
+  if (cmapType == 1) {
+    if (type != 1 && type != 9) return false;
+    if (b[7] != 8 && b[7] != 15 && b[7] != 16 && b[7] != 24 && b[7] != 32) return false;
+    if (b[16] != 8 && b[16] != 16) return false;
+  } else {
+    if (type != 2 && type != 3 && type != 10 && type != 11) return false;
+    int bits = b[16];
+    if (bits != 8 && bits != 15 && bits != 16 && bits != 24 && bits != 32) return false;
+  }
+  return LE16(b + 12) >= 1 && LE16(b + 14) >= 1;
+}
+
+// stbi_load of a Radiance file (stbi__hdr_load + stbi__hdr_to_ldr): one
+// requested channel is (r + g + b) / 3 of the decoded RGBE values; each value v
+// becomes (v ^ (1 / 2.2)) * 255 + 0.5, clamped to 0..255 and truncated.
+bool IsHdrFile(const std::string& b) { return b.rfind("#?RADIANCE", 0) == 0 || b.rfind("#?RGBE", 0) == 0; }
+Ldr HdrToLdr(const std::string& bytes, int req, bool flipY) {
+  Hdr h = LoadHdr(bytes, flipY);
+  Ldr out;
+  out.width = h.width;
+  out.height = h.height;
+  out.channels = req;
+  size_t npx = (size_t)h.width * h.height;
+  out.px.resize(npx * req);
+  const float gamma = 1.0f / 2.2f;
+  for (size_t i = 0; i < npx; i++)
+    for (int k = 0; k < req; k++) {
+      const float* c = &h.px[i * 3];
+      float v = req == 3 ? c[k] : (c[0] + c[1] + c[2]) / 3;
+      float z = (float)std::pow((double)v, (double)gamma) * 255 + 0.5f;
+      z = z < 0 ? 0 : z > 255 ? 255 : z;
+      out.px[i * req + k] = (uint8_t)z;
+    }
+  return out;
+}
+
 bool IsPng(const std::string& b) { return b.size() >= 8 && std::memcmp(b.data(), "\x89PNG\r\n\x1a\n", 8) == 0; }
 bool IsPnm(const std::string& b) { return b.size() >= 3 && b[0] == 'P' && (b[1] == '5' || b[1] == '6'); }
 
@@ -1185,13 +1493,17 @@ Ldr LoadLdr(const std::string& bytes, int reqChannels, bool flipY) {
   if (IsPng(bytes)) return DecodePng(bytes, reqChannels, flipY);
   if (IsPnm(bytes)) return DecodePnm(bytes, reqChannels, flipY);
   if (IsJpeg(bytes)) return DecodeJpeg(bytes, reqChannels, flipY);
-  Fail("unsupported image format (PNG, JPEG and binary PNM are read)");
+  if (IsBmp(bytes)) return DecodeBmp(bytes, reqChannels, flipY);
+  if (IsHdrFile(bytes)) return HdrToLdr(bytes, reqChannels, flipY);
+  if (IsTga(bytes)) return DecodeTga(bytes, reqChannels, flipY);  // last: TGA has no signature
+  Fail("unsupported image format (PNG, JPEG, BMP, TGA, Radiance HDR and binary PNM are read)");
 }
 
 // --------------------------------------------------------------------- HDR
 Hdr LoadHdr(const std::string& bytes, bool flipY) {
   Hdr out;
-  if (IsPng(bytes) || IsPnm(bytes) || IsJpeg(bytes)) {  // stbi_loadf of an LDR file
+  if (IsPng(bytes) || IsPnm(bytes) || IsJpeg(bytes) || IsBmp(bytes) || (!IsHdrFile(bytes) && IsTga(bytes))) {
+    // stbi_loadf of an LDR file
     Ldr l = LoadLdr(bytes, 3, flipY);
     out.width = l.width;
     out.height = l.height;

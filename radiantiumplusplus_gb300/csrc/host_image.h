@@ -6,6 +6,8 @@
 //    bit depths 1..16, Adam7 interlacing, PLTE / tRNS;
 //  * baseline and progressive Huffman JPEG (ITU-T T.81) with stb_image's
 //    integer IDCT, chroma upsampling and colour conversion;
+//  * BMP (palette, 24-bit, 16 / 32-bit masked; not RLE) and TGA (colour-mapped,
+//    true-colour and grey, raw or run-length);
 //  * binary PNM (P5 / P6, maxval <= 255);
 //  * Radiance RGBE .hdr (flat and adaptive run-length scanlines);
 //  * OpenEXR scanline images with NONE, RLE, ZIPS or ZIP compression and HALF or
@@ -34,7 +36,8 @@ struct Hdr {
   std::vector<float> px;
 };
 
-// stbi_load(..., req_comp) for PNG / JPEG / PNM files: req_comp is 1 or 3.
+// stbi_load(..., req_comp) for PNG / JPEG / BMP / TGA / PNM files (and Radiance
+// files mapped to 8 bits as stb does): req_comp is 1 or 3.
 Ldr LoadLdr(const std::string& bytes, int reqChannels, bool flipY);
 // stbi_loadf(..., 3) for Radiance .hdr files (and, like stb, LDR files mapped
 // through (v / 255) ^ 2.2).

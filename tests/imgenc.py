@@ -544,3 +544,87 @@ def jpeg(planes, sampling, quant, X, Y, ids=None, scans=None, restart=0, app=(),
     out += b"\xff\xd9"
     qt = {c["id"]: qtables[c["tq"]] for c in comps}
     return bytes(out), coef, comps, qt
+
+
+# -------------------------------------------------------------- BMP / TGA
+def bmp(img, bpp=24, hsz=40, masks=None, palette=None, top_down=False, compress=None):
+    """img: (h, w) palette indices for bpp <= 8, else (h, w, 3|4) raw field values
+    for 16 / 32 bits (packed with `masks` (r, g, b[, a]) or the defaults) or RGB
+    bytes for 24. hsz 12 writes the OS/2 core header (3-byte palette entries)."""
+    h, w = img.shape[:2]
+    rows = []
+    for y in (range(h) if top_down else range(h - 1, -1, -1)):
+        r = img[y]
+        if bpp <= 8:
+            bits = "".join(format(int(v), "0%db" % bpp) for v in r)
+            bits += "0" * (-len(bits) % 8)
+            row = bytes(int(bits[i:i + 8], 2) for i in range(0, len(bits), 8))
+        elif bpp == 24:
+            row = bytes(int(c) for px in r for c in (px[2], px[1], px[0]))
+        else:
+            row = b"".join(int(v).to_bytes(bpp // 8, "little") for v in r)
+        rows.append(row + b"\0" * (-len(row) % 4))
+    pix = b"".join(rows)
+    pal = b""
+    if palette is not None:
+        pal = b"".join(bytes([int(c[2]), int(c[1]), int(c[0])]) + (b"" if hsz == 12 else b"\0") for c in palette)
+    if compress is None:
+        compress = 3 if masks is not None else 0
+    if hsz == 12:
+        hdr = struct.pack("<IHHHH", 12, w, h, 1, bpp)
+    else:
+        hdr = struct.pack("<IiiHHIIiiII", hsz, w, -h if top_down else h, 1, bpp, compress, len(pix), 2835, 2835, 0, 0)
+        m = list(masks or (0, 0, 0)) + [0] * 4
+        if hsz >= 56:
+            hdr += struct.pack("<IIII", *m[:4])
+        hdr += b"\0" * (hsz - len(hdr))
+    extra = struct.pack("<III", *m[:3]) if (hsz == 40 and compress == 3) else b""
+    off = 14 + len(hdr) + len(extra) + len(pal)
+    return b"BM" + struct.pack("<IHHI", off + len(pix), 0, 0, off) + hdr + extra + pal + pix
+
+
+def tga(img, kind, bits, rle=False, top_down=False, cmap=None, cmap_bits=24, first=0):
+    """kind 1 (colour-mapped: img = (h, w) indices), 2 (true colour: img = (h, w,
+    3|4) RGB(A) bytes, or (h, w) 16-bit 5-5-5 words for bits 15 / 16), 3 (grey)."""
+    h, w = img.shape[:2]
+
+    def px(v):
+        if kind == 1:
+            return int(v).to_bytes(bits // 8, "little")
+        if kind == 3:
+            return bytes([int(v)])
+        if bits in (15, 16):
+            return int(v).to_bytes(2, "little")
+        c = [int(x) for x in v]
+        return bytes([c[2], c[1], c[0]] + c[3:])
+
+    order = range(h) if top_down else range(h - 1, -1, -1)
+    flat = [px(img[y][x]) for y in order for x in range(w)]
+    if rle:  # alternate repeat and raw packets of up to 128 pixels
+        out, i = [], 0
+        while i < len(flat):
+            j = i
+            while j + 1 < len(flat) and flat[j + 1] == flat[i] and j - i < 127:
+                j += 1
+            if j > i:
+                out.append(bytes([0x80 | (j - i)]) + flat[i])
+                i = j + 1
+            else:
+                k = i
+                while k + 1 < len(flat) and flat[k + 1] != flat[k] and k - i < 127:
+                    k += 1
+                out.append(bytes([k - i]) + b"".join(flat[i:k + 1]))
+                i = k + 1
+        data = b"".join(out)
+    else:
+        data = b"".join(flat)
+    cm = b""
+    if cmap is not None:
+        for c in cmap:
+            cm += (int(c).to_bytes(2, "little") if cmap_bits in (15, 16) else
+                   bytes([int(c[2]), int(c[1]), int(c[0])] + [int(x) for x in c[3:]]))
+    typ = kind + (8 if rle else 0)
+    hdr = struct.pack("<BBBHHBHHHHBB", 0, 1 if cmap is not None else 0, typ, first,
+                      len(cmap) if cmap is not None else 0, cmap_bits if cmap is not None else 0, 0, 0, w, h, bits,
+                      0x20 if top_down else 0)
+    return hdr + cm + data

@@ -136,3 +136,123 @@ def test_bad_files_are_reported(oracle, tmp_path):
     (tmp_path / "z.gif").write_bytes(b"GIF89a\x01\x00\x01\x00")
     with pytest.raises(RuntimeError, match="unsupported image format"):
         oracle.image_load({"type": "image_default"}, tmp_path / "z.gif")
+
+
+def _widen(v, bits):
+    """An n-bit field widened to 8 bits by repeating its bits (stbi__shiftsigned)."""
+    v = np.asarray(v, np.int64)
+    if bits >= 8:
+        return v & 255
+    r, got = np.zeros_like(v), 0
+    while got < 8:
+        r, got = (r << bits) | v, got + bits
+    return r >> (got - 8)
+
+
+def _expect8(rgb, req):
+    rgb = np.asarray(rgb, np.int64)
+    if rgb.shape[-1] == 1:
+        return np.repeat(rgb, 3, axis=-1) if req == 3 else rgb
+    return rgb[..., :3] if req == 3 else _luma(rgb[..., :3])[..., None]
+
+
+def _check8(oracle, tmp_path, name, data, rgb):
+    for req in (3, 1):
+        got = _load(oracle, tmp_path, name, data, {"type": "image_default", "channel": req, "is_to_linear": False,
+                                                   "is_flip_y": False})
+        want = _expect8(rgb, req)
+        assert got.shape == want.shape and np.array_equal(got, (want / np.float32(255)).astype(np.float32)), req
+
+
+BMP_CASES = ["pal1", "pal4", "pal8", "rgb24", "os2_24", "os2_pal8", "rgb555", "rgb565", "argb32", "rgb32_no_alpha",
+             "v4_abgr32", "top_down24"]
+
+
+@pytest.mark.parametrize("case", BMP_CASES)
+def test_bmp_decode(oracle, tmp_path, case):
+    """BMP through stbi_load: palettes, BGR, masked 16 / 32-bit pixels widened by
+    bit replication, OS/2 core headers, bottom-up and top-down rows, 4-byte row
+    padding (odd widths)."""
+    rng = np.random.default_rng(len(case))
+    h, w = 7, 13
+    if case.startswith("pal") or case == "os2_pal8":
+        bpp = 8 if case == "os2_pal8" else int(case[3:])
+        pal = rng.integers(0, 256, size=(1 << bpp, 3))
+        idx = rng.integers(0, 1 << bpp, size=(h, w))
+        data = imgenc.bmp(idx, bpp, hsz=12 if case.startswith("os2") else 40, palette=pal)
+        want = pal[idx]
+    elif case in ("rgb24", "os2_24", "top_down24"):
+        want = rng.integers(0, 256, size=(h, w, 3))
+        data = imgenc.bmp(want, 24, hsz=12 if case == "os2_24" else 40, top_down=case == "top_down24")
+    elif case in ("rgb555", "rgb565"):
+        g6 = case == "rgb565"
+        f = np.stack([rng.integers(0, 32, (h, w)), rng.integers(0, 64 if g6 else 32, (h, w)),
+                      rng.integers(0, 32, (h, w))], axis=-1)
+        words = (f[..., 0] << (11 if g6 else 10)) | (f[..., 1] << 5) | f[..., 2]
+        masks = (0xF800, 0x07E0, 0x001F) if g6 else None
+        data = imgenc.bmp(words, 16, masks=masks)
+        want = np.stack([_widen(f[..., 0], 5), _widen(f[..., 1], 6 if g6 else 5), _widen(f[..., 2], 5)], axis=-1)
+    else:
+        c = rng.integers(0, 256, size=(h, w, 4))
+        if case == "rgb32_no_alpha":
+            c[..., 3] = 0
+        if case == "v4_abgr32":
+            words = c[..., 0] | (c[..., 1] << 8) | (c[..., 2] << 16) | (c[..., 3] << 24)
+            data = imgenc.bmp(words, 32, hsz=108, masks=(0xFF, 0xFF00, 0xFF0000, 0xFF000000))
+        else:
+            words = (c[..., 3] << 24) | (c[..., 0] << 16) | (c[..., 1] << 8) | c[..., 2]
+            data = imgenc.bmp(words, 32)
+        want = c[..., :3]
+    _check8(oracle, tmp_path, case + ".bmp", data, want)
+
+
+TGA_CASES = [(2, 24, False), (2, 32, False), (2, 16, False), (3, 8, False), (1, 8, False), (2, 24, True),
+             (2, 32, True), (3, 8, True), (1, 8, True)]
+
+
+@pytest.mark.parametrize("top_down", [False, True])
+@pytest.mark.parametrize("kind,bits,rle", TGA_CASES, ids=lambda v: str(v))
+def test_tga_decode(oracle, tmp_path, kind, bits, rle, top_down):
+    """TGA through stbi_load: true colour (BGR, BGRA, 5-5-5 scaled by 255 / 31),
+    grey, colour-mapped, each raw and run-length coded, both row orders."""
+    rng = np.random.default_rng(kind * 100 + bits + rle)
+    h, w = 6, 11
+    runs = rng.integers(0, 3, size=(h, w))  # few distinct values: long runs for the RLE packets
+    if kind == 1:
+        cmap = rng.integers(0, 256, size=(40, 3))
+        idx = (runs * 7 + rng.integers(0, 2, size=(h, w))) % 40
+        data = imgenc.tga(idx, 1, 8, rle, top_down, cmap=cmap)
+        want = cmap[idx]
+    elif kind == 3:
+        grey = runs * 60 + 10
+        data = imgenc.tga(grey, 3, 8, rle, top_down)
+        want = grey[..., None]
+    elif bits == 16:
+        f = rng.integers(0, 32, size=(h, w, 3))
+        words = (f[..., 0] << 10) | (f[..., 1] << 5) | f[..., 2]
+        data = imgenc.tga(words, 2, 16, rle, top_down)
+        want = f * 255 // 31
+    else:
+        pal = rng.integers(0, 256, size=(3, bits // 8))
+        img = pal[runs]
+        data = imgenc.tga(img, 2, bits, rle, top_down)
+        want = img[..., :3]
+    _check8(oracle, tmp_path, "t.tga", data, want)
+
+
+def test_hdr_through_image_default(oracle, tmp_path):
+    """stbi_load of a Radiance file: (v ^ (1 / 2.2)) * 255 + 0.5 truncated, the grey
+    request averaging the three decoded channels first."""
+    rng = np.random.default_rng(12)
+    rgb = rng.uniform(0.0, 1.5, size=(5, 9, 3))
+    data = imgenc.hdr(rgb, rle=False)
+    q = imgenc.rgbe(rgb)
+    dec = (q[..., :3] * np.ldexp(1.0, q[..., 3:4].astype(int) - 136)).astype(np.float32)
+    for req in (3, 1):
+        v = dec if req == 3 else ((dec[..., 0] + dec[..., 1] + dec[..., 2]) / np.float32(3))[..., None]
+        z = (np.power(v.astype(np.float64), np.float64(np.float32(1.0) / np.float32(2.2))).astype(np.float32) *
+             np.float32(255) + np.float32(0.5))
+        want = np.clip(z, 0, 255).astype(np.uint8)
+        got = _load(oracle, tmp_path, "h.hdr", data, {"type": "image_default", "channel": req, "is_to_linear": False,
+                                                      "is_flip_y": False})
+        assert np.array_equal(got, (want / np.float32(255)).astype(np.float32)), req
