@@ -98,6 +98,25 @@ constexpr int kJobStatWords = 10;
 
 }  // namespace
 
+// The device buffers of a finished job (film, statistics, resolve target,
+// events) and, for a `path` job, its instantiated per-chunk wave graphs with
+// their wave contexts: kept by the scene for its next job of the same film, so
+// a stream of short jobs does not allocate, free (a device-wide sync) and
+// capture per job. The graphs are reused when the samples per wave and the
+// scene's traversal parameters match; the job's wave contexts are rewritten.
+struct JobSpare {
+  bool valid = false;
+  float4* accum = nullptr;
+  unsigned long long *dStats = nullptr, *hStats = nullptr;
+  float* resolve = nullptr;
+  cudaEvent_t evStart = nullptr, evEnd = nullptr;
+  WaveCtx* ctx = nullptr;
+  std::vector<cudaGraphExec_t> graphs;
+  std::vector<uint64_t> graphKernels;
+  uint32_t spw = 0;
+  uint64_t tuneEpoch = 0;
+};
+
 struct rad_scene {
   DevScene dev{};
   std::vector<void*> allocs;
@@ -108,6 +127,8 @@ struct rad_scene {
   GuideNet* guide = nullptr;  // learned proposal, created by rad_guide_enable / _load or a guided job
   GuideConfig guideCfg;
   TraceTune tune;  // traversal launch parameters (rad_autotune)
+  uint64_t tuneEpoch = 0;  // bumped when `tune` changes (captured graphs bake it in)
+  JobSpare spare;          // guarded by the library's GPU mutex
 };
 
 struct rad_job {
@@ -135,6 +156,7 @@ struct rad_job {
   uint32_t spw = 0;           // samples per wave (0 = not chosen yet; see WaveSamples)
   // CUDA graph per pixel chunk: one captured wave replayed once per sample
   WaveCtx* ctx = nullptr;  // device, one per chunk
+  bool ctxStale = false;   // graphs taken over from an earlier job: contexts not yet written
   std::vector<cudaGraphExec_t> graphs;
   std::vector<uint64_t> graphKernels;
   std::mutex m;
@@ -584,8 +606,7 @@ void RunWaveGraph(rad_job* j) {
   uint64_t npix = (uint64_t)W * H;
   const uint32_t spw = WaveSamples(j);
   size_t nChunks = (size_t)((npix + lib.maxPaths - 1) / lib.maxPaths);
-  if (j->graphs.empty()) {
-    Check(cudaMalloc(&j->ctx, nChunks * sizeof(WaveCtx)), "cudaMalloc");
+  auto uploadCtx = [&]() {
     std::vector<WaveCtx> host(nChunks);
     for (auto& c : host) {
       c = WaveCtx{};
@@ -595,6 +616,14 @@ void RunWaveGraph(rad_job* j) {
       c.seed = j->seed;
     }
     Check(cudaMemcpy(j->ctx, host.data(), nChunks * sizeof(WaveCtx), cudaMemcpyHostToDevice), "ctx upload");
+  };
+  if (j->ctxStale) {
+    uploadCtx();
+    j->ctxStale = false;
+  }
+  if (j->graphs.empty()) {
+    Check(cudaMalloc(&j->ctx, nChunks * sizeof(WaveCtx)), "cudaMalloc");
+    uploadCtx();
     ProfSink none{nullptr};
     FilmView film{j->accum, (int32_t)W, (int32_t)H, j->dStats};
     for (size_t c = 0; c < nChunks; c++) {
@@ -831,9 +860,51 @@ bool AdmitFilm(rad_job* j) {
   return true;
 }
 
+void FreeSpareGraphs(JobSpare& sp) {
+  for (cudaGraphExec_t g : sp.graphs) cudaGraphExecDestroy(g);
+  if (sp.ctx) cudaFree(sp.ctx);
+  sp.graphs.clear();
+  sp.graphKernels.clear();
+  sp.ctx = nullptr;
+}
+
+void FreeSpare(JobSpare& sp) {
+  if (!sp.valid) return;
+  FreeSpareGraphs(sp);
+  if (sp.accum) cudaFree(sp.accum);
+  if (sp.dStats) cudaFree(sp.dStats);
+  if (sp.hStats) cudaFreeHost(sp.hStats);
+  if (sp.resolve) cudaFree(sp.resolve);
+  if (sp.evStart) cudaEventDestroy(sp.evStart);
+  if (sp.evEnd) cudaEventDestroy(sp.evEnd);
+  sp = JobSpare{};
+}
+
 void AllocJobFilm(rad_job* j) {
   const DevScene& S = j->scene->dev;
   size_t npix = (size_t)S.cam.width * S.cam.height;
+  JobSpare& sp = j->scene->spare;
+  if (sp.valid) {  // take over the previous job's buffers (same scene: same film size)
+    j->accum = sp.accum;
+    j->dStats = sp.dStats;
+    j->hStats = sp.hStats;
+    j->resolve = sp.resolve;
+    j->evStart = sp.evStart;
+    j->evEnd = sp.evEnd;
+    if (!sp.graphs.empty() && GraphEligible(j) && sp.spw == WaveSamples(j) && sp.tuneEpoch == j->scene->tuneEpoch) {
+      j->ctx = sp.ctx;
+      j->graphs = std::move(sp.graphs);
+      j->graphKernels = std::move(sp.graphKernels);
+      j->ctxStale = true;
+      sp.ctx = nullptr;
+    }
+    FreeSpareGraphs(sp);
+    sp = JobSpare{};
+    std::memset(j->hStats, 0, kJobStatWords * sizeof(unsigned long long));
+    Check(cudaMemsetAsync(j->accum, 0, npix * sizeof(float4), L().stream), "memset film");
+    Check(cudaMemsetAsync(j->dStats, 0, kJobStatWords * sizeof(unsigned long long), L().stream), "memset stats");
+    return;
+  }
   Check(cudaMalloc(&j->accum, npix * sizeof(float4)), "film");
   Check(cudaMalloc(&j->dStats, kJobStatWords * sizeof(unsigned long long)), "stats");
   Check(cudaMallocHost(&j->hStats, kJobStatWords * sizeof(unsigned long long)), "stats host");
@@ -1213,6 +1284,7 @@ int rad_scene_destroy(rad_scene* scene) {
     Lib& lib = L();
     std::lock_guard<std::mutex> g(lib.gpuMu);
     cudaStreamSynchronize(lib.stream);
+    FreeSpare(scene->spare);
     FreeAll(scene->allocs);
     lib.used -= scene->bytes;
     if (scene->guide) {
@@ -1354,17 +1426,32 @@ int rad_job_destroy(rad_job* job) {
     Lib& lib = L();
     std::lock_guard<std::mutex> g(lib.gpuMu);
     cudaStreamSynchronize(lib.stream);
-    if (job->accum) {
-      cudaFree(job->accum);
-      lib.used -= job->filmBytes;
+    if (job->accum) lib.used -= job->filmBytes;
+    JobSpare& sp = job->scene->spare;
+    if (job->accum && job->dStats && job->hStats && job->evStart && job->evEnd) {  // keep for the scene's next job
+      FreeSpare(sp);
+      sp.valid = true;
+      sp.accum = job->accum;
+      sp.dStats = job->dStats;
+      sp.hStats = job->hStats;
+      sp.resolve = job->resolve;
+      sp.evStart = job->evStart;
+      sp.evEnd = job->evEnd;
+      sp.ctx = job->ctx;
+      sp.graphs = std::move(job->graphs);
+      sp.graphKernels = std::move(job->graphKernels);
+      sp.spw = job->spw;
+      sp.tuneEpoch = job->scene->tuneEpoch;
+    } else {
+      if (job->accum) cudaFree(job->accum);
+      if (job->dStats) cudaFree(job->dStats);
+      if (job->hStats) cudaFreeHost(job->hStats);
+      if (job->resolve) cudaFree(job->resolve);
+      for (cudaGraphExec_t g : job->graphs) cudaGraphExecDestroy(g);
+      if (job->ctx) cudaFree(job->ctx);
+      if (job->evStart) cudaEventDestroy(job->evStart);
+      if (job->evEnd) cudaEventDestroy(job->evEnd);
     }
-    if (job->dStats) cudaFree(job->dStats);
-    if (job->hStats) cudaFreeHost(job->hStats);
-    if (job->resolve) cudaFree(job->resolve);
-    for (cudaGraphExec_t g : job->graphs) cudaGraphExecDestroy(g);
-    if (job->ctx) cudaFree(job->ctx);
-    if (job->evStart) cudaEventDestroy(job->evStart);
-    if (job->evEnd) cudaEventDestroy(job->evEnd);
     job->scene->jobs--;
     delete job;
   });
@@ -1792,6 +1879,7 @@ int rad_autotune(rad_scene* scene, const char* config_json, rad_tune_result* out
       throw Error{RAD_ERR_DEVICE_CHECK, "device-side check fired while tuning"};
     }
     scene->tune = best;
+    scene->tuneEpoch++;
     if (out) *out = res;
   });
 }

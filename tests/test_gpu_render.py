@@ -304,3 +304,30 @@ def test_volpath_modes_keep_the_expectation(rad, scene_dir, base, flags):
     zt = (bm.mean() - am.mean()) / np.sqrt(am.var(ddof=1) / am.size + bm.var(ddof=1) / bm.size)
     assert abs(zt) < 4.0, zt
     s.close()
+
+
+@pytest.mark.gpu
+def test_consecutive_jobs_reuse_buffers_and_graphs(rad, scene_dir):
+    """A finished job's film, statistics buffers and captured wave graphs serve the
+    scene's next job (same film; the graphs when the samples per wave match): a run
+    of jobs with equal and different spp and first samples returns, bit for bit,
+    the film each job gives on a freshly loaded scene."""
+    path, _, _ = write(scene_dir, "reuse_box", scenes.box_room(32, 32, 4))
+    runs = [(4, 0), (4, 100), (2, 7), (4, 100), (1, 3)]
+    sc = rad.Scene.from_file(path)
+    films = []
+    for spp, first in runs:
+        j = sc.submit(spp=spp, first_sample=first)
+        j.wait()
+        films.append(j.film())
+        j.close()
+    sc.close()
+    for (spp, first), f in zip(runs, films):
+        fresh = rad.Scene.from_file(path)
+        j = fresh.submit(spp=spp, first_sample=first)
+        j.wait()
+        ref = j.film()
+        j.close()
+        fresh.close()
+        assert np.array_equal(f, ref), (spp, first)
+    assert np.array_equal(films[1], films[3])
