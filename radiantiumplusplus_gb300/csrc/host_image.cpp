@@ -1387,7 +1387,7 @@ Ldr DecodeTga(const std::string& bytes, int req, bool flipY) {
   std::vector<uint8_t> cmap;
   int cmapBytes = (cmapBits + 1) >> 3;
   if (cmapType == 1) {
-    if (pos + (size_t)cmapFirst * 0 + (size_t)cmapLen * cmapBytes > n) Fail("tga: truncated colour map");
+    if (pos + (size_t)cmapLen * cmapBytes > n) Fail("tga: truncated colour map");
     cmap.resize((size_t)cmapLen * comp);
     for (int i = 0; i < cmapLen; i++) readPixel(b + pos + (size_t)i * cmapBytes, cmapBits, &cmap[(size_t)i * comp]);
     pos += (size_t)cmapLen * cmapBytes;
