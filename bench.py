@@ -69,7 +69,7 @@ class ClockSampler:
     def start(self):
         try:
             self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.gpu), "--query-gpu=" + self.FIELDS,
-                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                          "--format=csv,noheader,nounits", "-lms", "100"],
                                          stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
         except OSError:
             self.proc = None
@@ -221,7 +221,6 @@ def run_ours(args, world, rank, local):
         job.wait()
         torch.cuda.synchronize()
         barrier(world)
-        clk = clocks.stop()
         st = job.stats()
         job.close()
         # per-kernel breakdown (events around every launch, so no graph replay): 2 extra samples, not timed
@@ -247,6 +246,7 @@ def run_ours(args, world, rank, local):
         torch.cuda.synchronize()
         e2e_s = allreduce_max(world, time.perf_counter() - t0)
         barrier(world)
+        clk = clocks.stop()  # sampled through both timed regions (and the 2-spp profile between them)
         e2e_value = args.steps * W * H * spp_step * world / e2e_s
         # ---- roofline for the dominant kernel
         kern = {"extend": pst["ms_extend"], "shade": pst["ms_shade"], "shadow": pst["ms_shadow"],
@@ -612,7 +612,7 @@ def run_serving(args, world, rank, local):
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--steps", type=int, default=40)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline leg")
