@@ -282,7 +282,7 @@ def run_ours(args, world, rank, local):
         "roofline": {"bound": "hbm", "kernel": "extend (BVH8 closest hit)", "achieved": achieved, "peak": hbm_peak,
                      "unit": "GB/s", "frac": achieved / hbm_peak, "traffic": EXTEND_DRAM_BYTES_PER_LAUNCH,
                      "traffic_source": "ncu dram__bytes_read.sum + dram__bytes_write.sum, mean over the 16 extend "
-                                       "launches of one wave of this workload (profiles/extend_many_spheres_1080p.md)",
+                                       "launches of one wave of this workload",
                      "peak_source": peak_src, "dominant_kernel_by_time": dominant,
                      "nodes_per_ray": nodes_per_ray, "prims_per_ray": prims_per_ray,
                      "bytes_per_ray": BYTES_QUEUE + BYTES_RAY + BYTES_HIT + nodes_per_ray * BYTES_NODE

@@ -114,12 +114,17 @@ typedef struct rad_stats {
 /* ---- library ------------------------------------------------------------ */
 /* config_json may be NULL. Keys: "device" (int), "budget_bytes" (admission
  * budget for resident scenes + films, default 150e9), "max_paths" (paths in
- * flight per wave), "block_size". Idempotent. */
+ * flight per wave), "block_size". Idempotent: on a library already
+ * initialised only "budget_bytes" is applied (a new admission budget). */
 RAD_API int rad_init(const char* config_json);
 RAD_API int rad_shutdown(void);
 /* Copies the calling thread's last error message (NUL-terminated). */
 RAD_API int rad_last_error(char* buf, size_t size);
 RAD_API int rad_version(int32_t* major, int32_t* minor);
+/* No counterpart in the reference. Device bytes counted against the admission
+ * budget (resident scenes, job films including films parked with a scene for
+ * its next job, path-state buffers) and the budget itself. */
+RAD_API int rad_device_usage(uint64_t* used_bytes, uint64_t* budget_bytes);
 
 /* ---- scenes (BuildContext::SetFromJson + Build, build_context.cpp:47-321) -- */
 RAD_API int rad_scene_load_json(const char* json_text, const char* base_dir, rad_scene** out);
@@ -187,7 +192,10 @@ RAD_API int rad_render_samples(rad_scene* scene, const uint32_t* pixels, const u
  * synchronise the device): d_pixels, d_samples (n each) and d_radiance (n x 3)
  * are device pointers the caller owns, and the path state lives in a fixed
  * file-scope device array, so this call allocates nothing. n may be at most
- * 16384 (RAD_ERR_INVALID_ARG beyond). Work runs on `stream` (a cudaStream_t,
+ * 16384 (RAD_ERR_INVALID_ARG beyond). The pixel indices are in device memory,
+ * so the host cannot check them: one beyond the film is reported as
+ * RAD_ERR_DEVICE_CHECK after the call (rad_render_samples, which reads them
+ * on the host, answers RAD_ERR_INVALID_ARG). Work runs on `stream` (a cudaStream_t,
  * NULL = default stream) and the call returns when it has finished. The first
  * call on a device looks up the array's address; make it before any stream
  * capture. Every call shares the one array: calls that overlap on the GPU race.

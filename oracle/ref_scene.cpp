@@ -1154,6 +1154,21 @@ static void PrimBounds(const Scene& S, const PrimRef& p, V3& lo, V3& hi) {
   }
 }
 
+// The box the BVH tests for a primitive. Analytic primitives: the rectangle
+// test runs on the float world->object rows, whose plane differs from the one
+// through the corners by rounding, and a grazing ray turns that into a hit
+// point outside the corner box (the sphere's roots likewise). Their boxes grow
+// by 1e-5 of their largest coordinate so traversal never culls a primitive its
+// own test would hit. World bounds and centroids use the unpadded box.
+static void PadAnalytic(const Scene& S, const PrimRef& p, V3& lo, V3& hi) {
+  if (S.shapes[p.shape].kind == Shape::Mesh) return;
+  Float m = 0;
+  for (int a = 0; a < 3; a++) m = std::max(m, std::max(std::abs(lo[a]), std::abs(hi[a])));
+  V3 pad(m * 1e-5f);
+  lo = lo - pad;
+  hi = hi + pad;
+}
+
 void Scene::BuildBvh() {
   size_t n = prims.size();
   std::vector<V3> lo(n), hi(n), ce(n);
@@ -1164,6 +1179,7 @@ void Scene::BuildBvh() {
     ce[i] = (lo[i] + hi[i]) * 0.5f;
     worldLo = vmin(worldLo, lo[i]);
     worldHi = vmax(worldHi, hi[i]);
+    PadAnalytic(*this, prims[i], lo[i], hi[i]);
   }
   order.resize(n);
   for (size_t i = 0; i < n; i++) order[i] = (uint32_t)i;
@@ -1380,16 +1396,21 @@ Hit Scene::Intersect(const Ray& ray) const {
   uint32_t stack[128];
   int sp = 0;
   stack[sp++] = 0;
+  // Nodes are pruned against the best distance widened by the same margin as
+  // the slabs: a node holding a primitive at exactly the best t (an exact tie,
+  // which the lower primitive id wins) is still visited, so the result does not
+  // depend on the order nodes are visited in.
+  const Float margin = 1 + 2 * 3.5762786865234375e-07f;
   while (sp) {
     const BvhNode& n = nodes[stack[--sp]];
     Float tn;
-    if (!BoxHit(n, ray.O, inv, ray.MinT, h.t, tn)) continue;
+    if (!BoxHit(n, ray.O, inv, ray.MinT, h.t * margin, tn)) continue;
     if (n.count) {
       for (uint32_t i = 0; i < n.count; i++) IntersectPrim(order[n.first + i], ray, h);
     } else {
       Float ta, tb;
-      bool ha = BoxHit(nodes[n.left], ray.O, inv, ray.MinT, h.t, ta);
-      bool hb = BoxHit(nodes[n.left + 1], ray.O, inv, ray.MinT, h.t, tb);
+      bool ha = BoxHit(nodes[n.left], ray.O, inv, ray.MinT, h.t * margin, ta);
+      bool hb = BoxHit(nodes[n.left + 1], ray.O, inv, ray.MinT, h.t * margin, tb);
       if (ha && hb) {
         if (ta <= tb) {
           stack[sp++] = n.left + 1;

@@ -27,7 +27,8 @@ import numpy as np
 from . import _capi
 from ._capi import RadError, check
 
-__all__ = ["Scene", "Job", "Renderer", "RadError", "init", "shutdown", "bsdf_eval", "bsdf_sample", "lib"]
+__all__ = ["Scene", "Job", "Renderer", "RadError", "init", "shutdown", "device_usage", "bsdf_eval", "bsdf_sample",
+           "lib"]
 
 
 def _p(a):
@@ -54,6 +55,13 @@ def init(config=None):
 
 def shutdown():
     check(lib().rad_shutdown())
+
+
+def device_usage():
+    """rad_device_usage: (bytes counted against the admission budget, budget)."""
+    u, b = ctypes.c_uint64(), ctypes.c_uint64()
+    check(lib().rad_device_usage(ctypes.byref(u), ctypes.byref(b)))
+    return u.value, b.value
 
 
 class Scene:

@@ -37,7 +37,7 @@ RAD_JOB_VOL_REAL_DEPTH = 64
 
 # Every symbol the header declares (the export test checks this list).
 EXPORTS = [
-    "rad_init", "rad_shutdown", "rad_last_error", "rad_version",
+    "rad_init", "rad_shutdown", "rad_last_error", "rad_version", "rad_device_usage",
     "rad_scene_load_json", "rad_scene_load_file", "rad_scene_destroy", "rad_scene_info_get",
     "rad_scene_footprint", "rad_job_submit", "rad_job_wait", "rad_job_cancel", "rad_job_progress",
     "rad_job_film", "rad_job_stats", "rad_job_destroy", "rad_trace_batch", "rad_trace_batch_device",
@@ -111,6 +111,7 @@ def load(path=LIB_PATH):
         "rad_shutdown": [],
         "rad_last_error": [ctypes.c_char_p, ctypes.c_size_t],
         "rad_version": [P, P],
+        "rad_device_usage": [P, P],
         "rad_scene_load_json": [ctypes.c_char_p, ctypes.c_char_p, P],
         "rad_scene_load_file": [ctypes.c_char_p, P],
         "rad_scene_destroy": [P],

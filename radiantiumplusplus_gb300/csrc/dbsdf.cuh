@@ -12,12 +12,14 @@
 
 namespace rad {
 
+// BsdfSampleResult (bsdf.h:77-98): a sample that fails keeps the defaults,
+// pdf 0 and eta 1.
 struct BsdfSampleRes {
-  V3 wo;
-  float pdf;
-  float eta;
-  uint32_t type;
-  V3 f;
+  V3 wo{0.f, 0.f, 0.f};
+  float pdf = 0.f;
+  float eta = 1.f;
+  uint32_t type = 0;
+  V3 f{0.f, 0.f, 0.f};
 };
 
 RD Microfacet MatDist(const MatRec& m) {

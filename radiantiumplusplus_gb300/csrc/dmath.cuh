@@ -7,9 +7,13 @@
 #include <stdint.h>
 
 #if defined(RAD_HOST_EMULATION)
-// Host build of the device functions: lets a CPU harness run the same
-// traversal, BSDF and scene code to check index arithmetic and BVH8 decoding.
-#include <vector_types.h>
+// Host build of the device functions and kernels: a CPU harness runs the same
+// traversal, BSDF, scene and integrator code (bit for bit the device
+// arithmetic, with the host's libm for transcendentals). A kernel runs as a
+// loop over its grid, one thread at a time, each thread the only active lane
+// of its warp: ballots hold the calling lane's bit, shuffles from the leader
+// return the lane's own value, and warp sums see no other lanes.
+#include <cuda_runtime.h>
 #include <cmath>
 #include <cstring>
 #define RD inline
@@ -17,15 +21,34 @@
 #undef __global__
 #define __global__
 #undef __launch_bounds__
-#define __launch_bounds__(x)
+#define __launch_bounds__(...)
+#undef __device__
+#define __device__
+#undef __forceinline__
+#define __forceinline__ inline
+struct HemuDim3 {
+  unsigned x, y, z;
+};
+inline HemuDim3 threadIdx{0u, 0u, 0u}, blockIdx{0u, 0u, 0u}, blockDim{1u, 1u, 1u}, gridDim{1u, 1u, 1u};
 inline float __uint_as_float(uint32_t u) { float f; std::memcpy(&f, &u, 4); return f; }
 inline uint32_t __float_as_uint(float f) { uint32_t u; std::memcpy(&u, &f, 4); return u; }
 inline int __ffs(uint32_t x) { return __builtin_ffs((int)x); }
 inline int __popc(uint32_t x) { return __builtin_popcount(x); }
 template <typename T> inline T __ldg(const T* p) { return *p; }
+inline uint32_t HemuLane() { return threadIdx.x & 31u; }
+inline uint32_t __ballot_sync(uint32_t, bool p) { return p ? 1u << HemuLane() : 0u; }
+inline uint32_t __match_any_sync(uint32_t, uint32_t) { return 1u << HemuLane(); }
+template <typename T> inline T __shfl_sync(uint32_t, T v, int) { return v; }
+template <typename T> inline T __shfl_down_sync(uint32_t, T, unsigned) { return T(0); }
 inline uint32_t atomicOr(uint32_t* p, uint32_t v) { uint32_t o = *p; *p |= v; return o; }
 inline float atomicAdd(float* p, float v) { float o = *p; *p += v; return o; }
-inline uint2 make_uint2(uint32_t a, uint32_t b) { uint2 r; r.x = a; r.y = b; return r; }
+inline uint32_t atomicAdd(uint32_t* p, uint32_t v) { uint32_t o = *p; *p += v; return o; }
+inline unsigned long long atomicAdd(unsigned long long* p, unsigned long long v) {
+  unsigned long long o = *p;
+  *p += v;
+  return o;
+}
+inline uint32_t atomicMax(uint32_t* p, uint32_t v) { uint32_t o = *p; if (v > o) *p = v; return o; }
 using std::isfinite;
 using std::isnan;
 using std::isinf;

@@ -215,9 +215,24 @@ void BuildBvh8(HostScene& hs) {
           b.hi[i] = sh.m[i] + sh.m[3];
         }
       }
-      pb[g] = b;
       for (int i = 0; i < 3; i++) cen[3 * g + i] = (b.lo[i] + b.hi[i]) * 0.5f;
       world.Grow(b);
+      if (sh.kind != SHAPE_MESH) {
+        // Analytic primitives: the rectangle test runs on the float
+        // world->object rows, whose plane differs from the one through the
+        // corners by rounding, and a grazing ray turns that into a hit point
+        // outside the corner box (the sphere's roots likewise). The boxes the
+        // BVH tests grow by 1e-5 of their largest coordinate so traversal never
+        // culls a primitive its own test would hit; world bounds and centroids
+        // keep the unpadded box.
+        float m = 0.f;
+        for (int i = 0; i < 3; i++) m = std::max(m, std::max(std::fabs(b.lo[i]), std::fabs(b.hi[i])));
+        for (int i = 0; i < 3; i++) {
+          b.lo[i] -= m * 1e-5f;
+          b.hi[i] += m * 1e-5f;
+        }
+      }
+      pb[g] = b;
     }
   }
   for (int i = 0; i < 3; i++) {

@@ -1387,6 +1387,8 @@ Ldr DecodeTga(const std::string& bytes, int req, bool flipY) {
   std::vector<uint8_t> cmap;
   int cmapBytes = (cmapBits + 1) >> 3;
   if (cmapType == 1) {
+    // stb_image refuses an empty palette ("bad palette"); every index would fall back to entry 0
+    if (cmapLen == 0) Fail("tga: empty colour map");
     if (pos + (size_t)cmapLen * cmapBytes > n) Fail("tga: truncated colour map");
     cmap.resize((size_t)cmapLen * comp);
     for (int i = 0; i < cmapLen; i++) readPixel(b + pos + (size_t)i * cmapBytes, cmapBits, &cmap[(size_t)i * comp]);

@@ -48,6 +48,7 @@ namespace {
 constexpr int kMaxDevices = 64;
 std::mutex g_mu;
 NoAllocScratch* g_addr[kMaxDevices] = {nullptr};
+int g_sms[kMaxDevices] = {0};  // SM count per device, read with the address
 
 PathBuffers ScratchBuffers(NoAllocScratch* s) {
   PathBuffers B{};
@@ -74,6 +75,7 @@ PathBuffers ScratchBuffers(NoAllocScratch* s) {
 
 // Scene access and error reporting live with the rest of the C ABI (runtime.cu).
 const DevScene* SceneDevice(const rad_scene* scene);
+const TraceTune* SceneTune(const rad_scene* scene);
 int SceneDeviceIndex();
 int ReportError(int code, const char* msg);
 
@@ -109,10 +111,16 @@ extern "C" RAD_API int rad_render_samples_noalloc(rad_scene* scene, const uint32
       void* p = nullptr;
       cudaError_t e = cudaGetSymbolAddress(&p, g_noallocScratch);
       if (e != cudaSuccess || !p) return done(RAD_ERR_CUDA, "cudaGetSymbolAddress of the scratch array failed");
+      int sms = 0;
+      if (cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess || sms <= 0)
+        return done(RAD_ERR_CUDA, "cudaDeviceGetAttribute failed");
+      g_sms[dev] = sms;
       g_addr[dev] = static_cast<NoAllocScratch*>(p);
     }
     addr = g_addr[dev];
   }
+  const int sms = g_sms[dev];
+  const TraceTune& tu = *SceneTune(scene);
   cudaStream_t st = static_cast<cudaStream_t>(stream);
   PathBuffers B = ScratchBuffers(addr);
   uint32_t count = (uint32_t)n;
@@ -125,20 +133,22 @@ extern "C" RAD_API int rad_render_samples_noalloc(rad_scene* scene, const uint32
     if (LaunchVolPath(S, B, w, addr->counters + kMiscBase + 1, st) != cudaSuccess)
       return done(RAD_ERR_CUDA, "vol_path launch failed");
   } else {
-    int sms = 148;
-    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    // launch shapes and traversal parameters as rad_render_samples uses them (rad_autotune's choice)
     int grid = std::max(1, std::min(sms * 8, (int)((count + 127) / 128)));
+    int tgrid = std::max(1, std::min(sms * tu.blocksPerSm, (int)((count + 127) / 128)));
     int iters = S.maxDepth >= 0 ? std::max(1, S.maxDepth) : kMaxBounce;
     if (iters > kMaxBounce) iters = kMaxBounce;
     if (S.isAO) {  // renderer "ao": first hit and one visibility ray
-      if (LaunchExtend(S, B, 0, grid, st) != cudaSuccess || LaunchShadeAO(S, B, grid, st) != cudaSuccess ||
-          LaunchShadow(S, B, 0, grid, st) != cudaSuccess)
+      if (LaunchExtend(S, B, 0, tgrid, st, nullptr, tu.refillBusy, tu.leafFrac8) != cudaSuccess ||
+          LaunchShadeAO(S, B, grid, st) != cudaSuccess ||
+          LaunchShadow(S, B, 0, tgrid, st, nullptr, tu.refillBusy, tu.leafFrac8) != cudaSuccess)
         return done(RAD_ERR_CUDA, "ao launch failed");
       iters = 0;
     }
     for (int d = 0; d < iters; d++) {
-      if (LaunchExtend(S, B, d, grid, st) != cudaSuccess || LaunchShade(S, B, d, grid, st) != cudaSuccess ||
-          LaunchShadow(S, B, d, grid, st) != cudaSuccess)
+      if (LaunchExtend(S, B, d, tgrid, st, nullptr, tu.refillBusy, tu.leafFrac8) != cudaSuccess ||
+          LaunchShade(S, B, d, grid, st) != cudaSuccess ||
+          LaunchShadow(S, B, d, tgrid, st, nullptr, tu.refillBusy, tu.leafFrac8) != cudaSuccess)
         return done(RAD_ERR_CUDA, "bounce launch failed");
       if (S.maxDepth < 0 && (d % 8) == 7) {
         uint32_t next = 0;
@@ -156,6 +166,7 @@ extern "C" RAD_API int rad_render_samples_noalloc(rad_scene* scene, const uint32
           cudaSuccess ||
       cudaStreamSynchronize(st) != cudaSuccess)
     return done(RAD_ERR_CUDA, "stream synchronisation failed");
+  if (err & kErrPixelRange) return done(RAD_ERR_DEVICE_CHECK, "a pixel index lies outside the film");
   if (err) return done(RAD_ERR_DEVICE_CHECK, "a device-side bound was exceeded");
   return done(RAD_OK, "");
 }

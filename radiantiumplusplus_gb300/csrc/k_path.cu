@@ -21,6 +21,7 @@ namespace rad {
 
 constexpr int kBlock = 128;
 
+#ifndef RAD_HOST_EMULATION
 static int g_gridBlocks = 0;
 int PathGridBlocks() {
   if (g_gridBlocks == 0) {
@@ -31,6 +32,7 @@ int PathGridBlocks() {
   }
   return g_gridBlocks;
 }
+#endif
 
 RD float MisWeight(float a, float b) {  // path.cpp:231-236
   a *= a;
@@ -63,6 +65,12 @@ __global__ void __launch_bounds__(kBlock) KGenerate(DevScene S, PathBuffers B, W
   const uint32_t npc = w.count / spw;  // pixels per sample of this wave
   const uint32_t j = spw > 1u ? i % npc : i, s = spw > 1u ? i / npc : 0u;
   uint32_t pix = w.pixelList ? w.pixelList[i] : w.pixelBegin + j;
+  if (pix >= (uint32_t)S.cam.width * (uint32_t)S.cam.height) {
+    // a caller's device-side pixel list the host could not check: report, and
+    // trace pixel 0 instead so no film write leaves the film
+    atomicOr(B.counters + kMiscBase + 1, kErrPixelRange);
+    pix = 0;
+  }
   uint32_t smp = w.sampleList ? w.sampleList[i] : (w.ctx ? w.ctx->sample : w.sample) + s;
   uint32_t seed = w.ctx ? w.ctx->seed : w.seed;
   uint32_t x = pix % (uint32_t)S.cam.width, y = pix / (uint32_t)S.cam.width;
@@ -598,6 +606,8 @@ __global__ void KResolveFilm(FilmView film, float scale, float* out) {
   out[3 * i + 2] = a.z * scale;
 }
 
+#ifndef RAD_HOST_EMULATION
+// ---- launchers (a host harness runs the kernels above as loops over their grids)
 cudaError_t LaunchGenerate(const DevScene& S, const PathBuffers& B, const WaveParams& w, cudaStream_t st) {
   uint32_t n = w.count > (uint32_t)kCounterWords ? w.count : (uint32_t)kCounterWords;
   KGenerate<<<(n + kBlock - 1) / kBlock, kBlock, 0, st>>>(S, B, w);
@@ -660,5 +670,7 @@ cudaError_t LaunchResolveFilm(const FilmView& film, float scale, float* out, cud
   KResolveFilm<<<(n + 255) / 256, 256, 0, st>>>(film, scale, out);
   return cudaGetLastError();
 }
+
+#endif  // RAD_HOST_EMULATION
 
 }  // namespace rad

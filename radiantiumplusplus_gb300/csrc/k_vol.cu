@@ -10,9 +10,7 @@
 #include "dbsdf.cuh"
 #include "dscene.cuh"
 #include "dvol.cuh"
-#ifndef RAD_HOST_EMULATION
 #include "kernels.h"
-#endif
 
 namespace rad {
 
@@ -534,7 +532,6 @@ RD V3 VolLi(const DevScene& S, Pcg32& rng, VRay ray, uint32_t mode, uint32_t* er
   return p.result;
 }
 
-#ifndef RAD_HOST_EMULATION
 // Persistent lanes: each thread runs its path one part of a loop iteration at a
 // time and takes the next unstarted path (counter B.counters[kMiscBase + 4],
 // reset by the generate stage) when its own ends. Each warp step runs the part
@@ -594,6 +591,7 @@ __global__ void __launch_bounds__(kVolBlock, 5)
   if (nShadow) atomicAdd(B.counters + kMiscBase + 3, (uint32_t)nShadow);
 }
 
+#ifndef RAD_HOST_EMULATION
 cudaError_t LaunchVolPath(const DevScene& S, const PathBuffers& B, const WaveParams& w, uint32_t* err,
                           cudaStream_t st, uint32_t mode) {
   if (w.count == 0) return cudaSuccess;

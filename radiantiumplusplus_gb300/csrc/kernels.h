@@ -35,6 +35,9 @@ constexpr int kShadowBase = kMaxBounce + 1;
 constexpr int kMiscBase = 2 * kMaxBounce + 2;  // [0] spare, [1] device error word (sticky),
                                                // [2] vol closest rays, [3] vol shadow-side rays,
                                                // [4] vol paths taken (KVolPath's refill counter)
+// bits of the device error word: 1 traversal stack, 2 / 4 vol_path iteration
+// bounds, 8 bdpt visibility buffer, kErrPixelRange a pixel index beyond the film
+constexpr uint32_t kErrPixelRange = 16u;
 constexpr int kClassBase = kMiscBase + 8;
 // per-bounce ray-fetch counters of the persistent extend / shadow kernels
 constexpr int kFetchBase = kClassBase + (kMaxBounce + 1) * kShadeClasses;

@@ -115,6 +115,7 @@ struct JobSpare {
   std::vector<uint64_t> graphKernels;
   uint32_t spw = 0;
   uint64_t tuneEpoch = 0;
+  uint64_t bytes = 0;  // film bytes, still counted in the library's used bytes
 };
 
 struct rad_scene {
@@ -172,6 +173,10 @@ struct Lib {
   cudaStream_t stream = nullptr;
   uint64_t budget = 150ull * 1000 * 1000 * 1000;
   std::atomic<uint64_t> used{0};
+  // films parked with their scenes for the next job (JobSpare): counted in
+  // `used`, and released when an admission would otherwise fail
+  std::atomic<uint64_t> spareBytes{0};
+  std::vector<rad_scene*> spareScenes;  // guarded by gpuMu
   uint32_t maxPaths = 1u << 21;
   PathBuffers paths{};
   std::vector<void*> pathAllocs;
@@ -249,7 +254,14 @@ void WorkerMain();
 
 void InitLocked(const char* cfg) {
   Lib& lib = L();
-  if (lib.inited) return;
+  if (lib.inited) {
+    // a running library takes a new admission budget; the other keys are fixed at first init
+    if (cfg && *cfg) {
+      JValue c = JsonReader::Parse(cfg);
+      if (const JValue* v = c.get("budget_bytes")) lib.budget = (uint64_t)v->n;
+    }
+    return;
+  }
   if (cfg && *cfg) {
     JValue c = JsonReader::Parse(cfg);
     if (const JValue* v = c.get("device")) lib.device = (int)v->n;
@@ -868,8 +880,13 @@ void FreeSpareGraphs(JobSpare& sp) {
   sp.ctx = nullptr;
 }
 
-void FreeSpare(JobSpare& sp) {
+void FreeSpare(rad_scene* sc) {
+  JobSpare& sp = sc->spare;
   if (!sp.valid) return;
+  Lib& lib = L();
+  lib.used -= sp.bytes;
+  lib.spareBytes -= sp.bytes;
+  lib.spareScenes.erase(std::find(lib.spareScenes.begin(), lib.spareScenes.end(), sc));
   FreeSpareGraphs(sp);
   if (sp.accum) cudaFree(sp.accum);
   if (sp.dStats) cudaFree(sp.dStats);
@@ -878,6 +895,13 @@ void FreeSpare(JobSpare& sp) {
   if (sp.evStart) cudaEventDestroy(sp.evStart);
   if (sp.evEnd) cudaEventDestroy(sp.evEnd);
   sp = JobSpare{};
+}
+
+// Frees every parked film (caller holds gpuMu). Admission calls this before it
+// refuses a scene or a job, so parked films never keep work out.
+void ReleaseSpares() {
+  Lib& lib = L();
+  while (!lib.spareScenes.empty()) FreeSpare(lib.spareScenes.back());
 }
 
 void AllocJobFilm(rad_job* j) {
@@ -899,6 +923,11 @@ void AllocJobFilm(rad_job* j) {
       sp.ctx = nullptr;
     }
     FreeSpareGraphs(sp);
+    // the job's own admission counted its film: drop the spare's count
+    Lib& lib = L();
+    lib.used -= sp.bytes;
+    lib.spareBytes -= sp.bytes;
+    lib.spareScenes.erase(std::find(lib.spareScenes.begin(), lib.spareScenes.end(), j->scene));
     sp = JobSpare{};
     std::memset(j->hStats, 0, kJobStatWords * sizeof(unsigned long long));
     Check(cudaMemsetAsync(j->accum, 0, npix * sizeof(float4), L().stream), "memset film");
@@ -957,6 +986,7 @@ void WorkerMain() {
       inflight.pop_front();
     }
     rad_job* j = nullptr;
+    bool reclaim = false;  // a pending job waits for memory that parked films hold
     {
       std::unique_lock<std::mutex> lk(lib.qmu);
       // admission: films that fit the budget join the running set
@@ -973,6 +1003,11 @@ void WorkerMain() {
           it = lib.pending.erase(it);
           continue;
         }
+        if (lib.spareBytes.load() > 0) {
+          reclaim = true;
+          ++it;
+          continue;
+        }
         if (lib.running.empty() && completing.empty()) {
           // nothing running can free memory: this job can never be admitted
           it = lib.pending.erase(it);
@@ -981,7 +1016,7 @@ void WorkerMain() {
         }
         ++it;
       }
-      if (lib.running.empty() && completing.empty()) {
+      if (lib.running.empty() && completing.empty() && !reclaim) {
         if (lib.stop) break;
         lib.qcv.wait(lk);
         continue;
@@ -994,6 +1029,11 @@ void WorkerMain() {
         for (rad_job* c : lib.running)
           if (c->launched.load() < j->launched.load()) j = c;
       }
+    }
+    if (reclaim) {
+      std::lock_guard<std::mutex> g(lib.gpuMu);
+      ReleaseSpares();
+      continue;  // admission again, with the parked films' memory free
     }
     if (j) {
       std::lock_guard<std::mutex> g(lib.gpuMu);
@@ -1157,6 +1197,7 @@ struct DevBuf {
 namespace rad {
 // Accessors for other translation units of the C ABI.
 const DevScene* SceneDevice(const rad_scene* scene) { return &scene->dev; }
+const TraceTune* SceneTune(const rad_scene* scene) { return &scene->tune; }
 int SceneDeviceIndex() { return L().device; }
 int ReportError(int code, const char* msg) { return Fail(code, msg); }
 }  // namespace rad
@@ -1218,6 +1259,13 @@ int rad_version(int32_t* major, int32_t* minor) {
   return RAD_OK;
 }
 
+int rad_device_usage(uint64_t* used_bytes, uint64_t* budget_bytes) {
+  Lib& lib = L();
+  if (used_bytes) *used_bytes = lib.used.load();
+  if (budget_bytes) *budget_bytes = lib.budget;
+  return RAD_OK;
+}
+
 int rad_scene_load_json(const char* json_text, const char* base_dir, rad_scene** out) {
   if (!json_text || !out) return Fail(RAD_ERR_INVALID_ARG, "null argument");
   *out = nullptr;
@@ -1234,6 +1282,10 @@ int rad_scene_load_json(const char* json_text, const char* base_dir, rad_scene**
       FreeAll(sc->allocs);
       delete sc;
       throw;
+    }
+    if (lib.used.load() + sc->bytes > lib.budget && lib.spareBytes.load() > 0) {
+      std::lock_guard<std::mutex> g(lib.gpuMu);
+      ReleaseSpares();
     }
     if (lib.used.load() + sc->bytes > lib.budget) {
       FreeAll(sc->allocs);
@@ -1284,7 +1336,7 @@ int rad_scene_destroy(rad_scene* scene) {
     Lib& lib = L();
     std::lock_guard<std::mutex> g(lib.gpuMu);
     cudaStreamSynchronize(lib.stream);
-    FreeSpare(scene->spare);
+    FreeSpare(scene);
     FreeAll(scene->allocs);
     lib.used -= scene->bytes;
     if (scene->guide) {
@@ -1328,6 +1380,10 @@ int rad_job_submit(rad_scene* scene, const rad_job_desc* desc, rad_job** out) {
     scene->jobs++;
     *out = j;
     if (j->flags & RAD_JOB_SYNC) {
+      if (j->filmBytes + lib.used.load() > lib.budget && lib.spareBytes.load() > 0) {
+        std::lock_guard<std::mutex> g(lib.gpuMu);
+        ReleaseSpares();
+      }
       if (j->filmBytes + lib.used.load() > lib.budget) {
         FinishJob(j, RAD_ERR_ADMISSION, "job film exceeds the device budget");
         return;
@@ -1426,10 +1482,13 @@ int rad_job_destroy(rad_job* job) {
     Lib& lib = L();
     std::lock_guard<std::mutex> g(lib.gpuMu);
     cudaStreamSynchronize(lib.stream);
-    if (job->accum) lib.used -= job->filmBytes;
     JobSpare& sp = job->scene->spare;
     if (job->accum && job->dStats && job->hStats && job->evStart && job->evEnd) {  // keep for the scene's next job
-      FreeSpare(sp);
+      FreeSpare(job->scene);
+      // the film stays counted in lib.used while it is parked
+      sp.bytes = job->filmBytes;
+      lib.spareBytes += sp.bytes;
+      lib.spareScenes.push_back(job->scene);
       sp.valid = true;
       sp.accum = job->accum;
       sp.dStats = job->dStats;
@@ -1443,6 +1502,7 @@ int rad_job_destroy(rad_job* job) {
       sp.spw = job->spw;
       sp.tuneEpoch = job->scene->tuneEpoch;
     } else {
+      if (job->accum) lib.used -= job->filmBytes;
       if (job->accum) cudaFree(job->accum);
       if (job->dStats) cudaFree(job->dStats);
       if (job->hStats) cudaFreeHost(job->hStats);

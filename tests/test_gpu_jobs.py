@@ -117,3 +117,80 @@ def test_cli_renders_and_saves(rad, scene_dir):
     s = rad.Scene.from_file(path)
     assert np.allclose(read_exr(out), s.render(), rtol=0, atol=0)
     s.close()
+
+
+def _film_bytes(scene):
+    return scene.width * scene.height * 16 + 64  # float4 per pixel + stats tail (rad_job_submit)
+
+
+def test_parked_film_stays_counted(rad, scene_dir):
+    """A destroyed job's film is parked with its scene for the next job: it is
+    still counted against the budget until the scene (or admission) frees it."""
+    used0, _ = rad.device_usage()
+    s = rad.Scene.from_file(box(scene_dir, 36, 20, 2)[0])
+    used1, _ = rad.device_usage()
+    assert used1 == used0 + s.footprint()
+    j = s.submit(spp=2)
+    j.wait()
+    assert rad.device_usage()[0] == used1 + _film_bytes(s)
+    j.close()
+    assert rad.device_usage()[0] == used1 + _film_bytes(s)  # parked, still counted
+    j2 = s.submit(spp=1)  # takes the parked film over: counted once
+    j2.wait()
+    assert rad.device_usage()[0] == used1 + _film_bytes(s)
+    j2.close()
+    s.close()
+    assert rad.device_usage()[0] == used0
+
+
+def test_admission_refusals_and_parked_film_release(rad, scene_dir):
+    """Against a small budget: a scene that does not fit and a job whose film
+    does not fit are refused with RAD_ERR_ADMISSION; a job that fits only once
+    another scene's parked film is freed is admitted (the film is released)."""
+    used0, budget0 = rad.device_usage()
+    try:
+        a = rad.Scene.from_file(box(scene_dir, 64, 64, 1)[0])
+        j = a.submit(spp=1)
+        j.wait()
+        j.close()  # a's film is now parked
+        b = rad.Scene.from_file(box(scene_dir, 48, 48, 1, seed=3)[0])
+        used = rad.device_usage()[0]
+        # room for b's film only if a's parked film is released
+        rad.init({"budget_bytes": used - _film_bytes(a) + _film_bytes(b)})
+        jb = b.submit(spp=1)
+        jb.wait()
+        assert rad.device_usage()[0] == used - _film_bytes(a) + _film_bytes(b)
+        jb.close()
+        # a film larger than the whole remaining budget: refused, async and sync
+        rad.init({"budget_bytes": rad.device_usage()[0] + 100})
+        for sync in (False, True):
+            jc = a.submit(spp=1, sync=sync)
+            with pytest.raises(rad.RadError) as e:
+                jc.wait()
+            assert e.value.code == 7  # RAD_ERR_ADMISSION
+            jc.close()
+        assert rad.device_usage()[0] == used - _film_bytes(a)  # both films freed: nothing parked
+        rad.init({"budget_bytes": rad.device_usage()[0] + 100})
+        with pytest.raises(rad.RadError) as e:
+            rad.Scene.from_file(box(scene_dir, 16, 16, 1, seed=5)[0])
+        assert e.value.code == 7
+        b.close()
+        a.close()
+    finally:
+        rad.init({"budget_bytes": budget0})
+    assert rad.device_usage()[0] == used0
+
+
+def test_wait_times_out(rad, scene_dir):
+    """rad_job_wait returns RAD_ERR_TIMEOUT while the job runs on; the job still finishes."""
+    s = rad.Scene.from_file(box(scene_dir, 256, 256, 4)[0])
+    j = s.submit(spp=4000)
+    with pytest.raises(rad.RadError) as e:
+        j.wait(timeout_ms=1)
+    assert e.value.code == 8  # RAD_ERR_TIMEOUT
+    j.cancel()
+    with pytest.raises(rad.RadError) as e:
+        j.wait()
+    assert e.value.code == 9
+    j.close()
+    s.close()

@@ -1,0 +1,228 @@
+"""The renderer's device code, compiled for the host (tests/hostemu: the BVH8
+traversal, scene, BSDF and light functions and the wavefront kernels of
+k_path.cu / k_vol.cu, run one lane at a time), against the oracle, bit for bit.
+
+Both sides call the host libm for transcendentals, so any difference here is a
+difference of algorithm. Covered: camera rays; closest and any hits on the
+box room and on the full 3.2 M-triangle many-spheres field; every BSDF's
+eval / pdf / sample on seeded sweeps over the parameter ranges of the
+many-spheres materials (Disney with each key present or absent, rough glass
+down to alpha = 0); per-sample radiance of `path`, `ao` and `vol_path` on the
+small parity scenes, the 256x256 box room, the 1920x1080 many-spheres frame
+and the 256^3 fBm volume.
+"""
+import json
+import os
+
+import numpy as np
+import pytest
+
+import hemu_lib
+from helpers import BSDFS, box, directions, lights, materials, spheres, textured, volume, write
+from radiantiumplusplus_gb300 import scenes
+
+
+def _same(a, b):
+    """Bitwise equality, NaN equal to NaN."""
+    a = np.asarray(a)
+    b = np.asarray(b)
+    if a.dtype == np.float32:
+        return (a.view(np.uint32) == b.view(np.uint32)) | (np.isnan(a) & np.isnan(b))
+    return a == b
+
+
+@pytest.fixture(scope="module")
+def field(tmp_path_factory, oracle):
+    """The many-spheres stress frame: 10,000 icospheres (3.2 M triangles), 1920x1080, depth 16."""
+    d = str(tmp_path_factory.mktemp("field"))
+    sc, assets = scenes.many_spheres(n_spheres=10000, width=1920, height=1080, spp=1, max_depth=16, seed=2)
+    path = scenes.write_scene(d, sc, assets)
+    with open(path) as fh:
+        text = fh.read()
+    h, o = hemu_lib.HemuScene(text, d), oracle.OracleScene(text, d)
+    yield h, o
+    h.close()
+    o.close()
+
+
+def test_camera_rays_bit_exact(oracle, scene_dir, field):
+    path, text, d = box(scene_dir, 64, 48, 1)
+    h, o = hemu_lib.HemuScene(text, d), oracle.OracleScene(text, d)
+    rng = np.random.default_rng(1)
+    for sc_h, sc_o, npix in ((h, o, 64 * 48), field + (1920 * 1080,)):
+        pix = rng.integers(0, npix, 20000).astype(np.uint32)
+        for sample in (0, 7, 123456):
+            assert _same(sc_h.camera_rays(pix, sample, sc_o.seed), sc_o.camera_rays(pix, sample)).all()
+    h.close()
+
+
+def _trace_both(h, o, rays):
+    hh, ho = h.trace(rays), o.trace(rays)
+    assert _same(hh, ho).all(1).mean() == 1.0, "closest hits differ on %d rays" % (~_same(hh, ho).all(1)).sum()
+    po = ho[:, 3].view(np.uint32)
+    short = rays.copy()
+    short[:, 7] = np.where(po != 0xFFFFFFFF, ho[:, 0] * np.float32(0.999), np.float32(1e3))
+    for r in (rays, short):
+        ah, ao = h.trace(r, True), o.trace(r, True)
+        assert np.array_equal(ah[:, 3].view(np.uint32), ao[:, 3].view(np.uint32))
+    return ho
+
+
+def test_trace_many_spheres_field_bit_exact(field):
+    """Closest hit (t, u, v, primitive id, sidedness) and occlusion on the
+    3.2 M-triangle field: camera rays and random rays from inside the field."""
+    h, o = field
+    rng = np.random.default_rng(3)
+    n = 1 << 18
+    cam = o.camera_rays(rng.integers(0, 1920 * 1080, n).astype(np.uint32), 0)
+    org = rng.uniform(0.0, 100.0, (n, 3))
+    rnd = np.concatenate([org, np.zeros((n, 1)), directions(rng, n), np.full((n, 1), 3.4e38)], 1).astype(np.float32)
+    for rays in (cam, rnd):
+        hits = _trace_both(h, o, rays)
+        assert (hits[:, 3].view(np.uint32) != 0xFFFFFFFF).mean() > 0.5
+
+
+def test_trace_box_edge_cases_bit_exact(oracle, scene_dir):
+    path, text, d = box(scene_dir)
+    h, o = hemu_lib.HemuScene(text, d), oracle.OracleScene(text, d)
+    rays = np.array([
+        [0, 1, 0.5, 0, 0, 0, -1, 3.4e38],
+        [0, 1, 0.5, 0, 1, 0, 0, 3.4e38],
+        [0, 1, 5, 0, 0, 0, 1, 3.4e38],
+        [0, 1, 0.5, 0, 0, 0, -1, 0.1],
+        [-1, 1, 0, 0, 1, 0, 0, 3.4e38],
+        [0, 0, 0, 0, 0, -1, 0, 3.4e38],
+        [0, 1, 0, 0, 1e-30, 0, -1, 3.4e38],  # denormal-sized direction component
+        [0.3, 0.4, 0.2, 0, 0, 1, 0, 3.4e38],  # straight up from inside the box
+    ], dtype=np.float32)
+    rng = np.random.default_rng(5)
+    n = 1 << 16
+    org = rng.uniform((-1, 0, -1), (1, 2, 1), (n, 3))
+    rnd = np.concatenate([org, np.zeros((n, 1)), directions(rng, n), np.full((n, 1), 3.4e38)], 1).astype(np.float32)
+    _trace_both(h, o, np.concatenate([rays, rnd]))
+    h.close()
+
+
+def _disney(rng):
+    b = {"type": "disney"}
+    if rng.uniform() < 0.8:
+        b["base_color"] = rng.uniform(0, 1, 3).round(6).tolist()
+    for k in ("metallic", "roughness", "specular", "spec_tint", "spec_trans", "anisotropic", "sheen", "sheen_tint",
+              "clearcoat", "clearcoat_gloss", "flatness"):
+        r = rng.uniform()
+        if r < 0.5:
+            b[k] = float(np.float32(rng.uniform()))
+        elif r < 0.6:
+            b[k] = 0.0  # present but zero: the reference's "present" flags need nonzero
+    return b
+
+
+def _sweep_bsdfs(n_disney, seed=11):
+    """Seeded parameter sets over the many-spheres materials' ranges."""
+    rng = np.random.default_rng(seed)
+    out = [dict(b) for b in BSDFS]
+    out += [_disney(rng) for _ in range(n_disney)]
+    for a in [0.0, 1e-4, 1e-3] + list(rng.uniform(0, 0.3, 40)):
+        out.append({"type": "rough_glass", "int_ior": 1.5, "ext_ior": 1.0, "alpha": float(np.float32(a))})
+    out.append({"type": "rough_glass", "int_ior": 1.33, "ext_ior": 1.0, "alpha": 0.0})
+    for _ in range(60):
+        b = {"type": "rough_metal", "distribution": "ggx" if rng.uniform() < 0.7 else "beckmann",
+             "sample_visible": bool(rng.uniform() < 0.8)}
+        if rng.uniform() < 0.3:
+            b["alpha_u"] = float(np.float32(rng.uniform(0.05, 0.5)))
+            b["alpha_v"] = float(np.float32(rng.uniform(0.05, 0.5)))
+        else:
+            b["alpha"] = float(np.float32(rng.uniform(0.05, 0.5)))
+        out.append(b)
+    for _ in range(20):
+        out.append({"type": "diffuse", "reflectance": rng.uniform(0.1, 0.9, 3).round(6).tolist()})
+    return out
+
+
+def test_bsdf_sweep_bit_exact(oracle):
+    """Eval / pdf / sample of 2,000 Disney parameter sets (every parameter
+    U[0, 1], each key present, present-and-zero or absent), rough glass at
+    alpha in {0, 1e-4, 1e-3} and U[0, 0.3] (alpha = 0 is the degenerate D that
+    microfacet.cpp:151 guards), rough metal and diffuse: 64 direction pairs
+    and 64 samples each, identical bits."""
+    rng = np.random.default_rng(12)
+    bad = []
+    for b in _sweep_bsdfs(2000):
+        js = json.dumps(b)
+        wi, wo = directions(rng, 64), directions(rng, 64)
+        wi[:8, 2] = np.abs(wi[:8, 2])  # a few same-hemisphere pairs for the reflection lobes
+        wo[:8, 2] = np.abs(wo[:8, 2])
+        fh, ph = hemu_lib.bsdf_eval(js, wi, wo)
+        fo, po = oracle.bsdf_eval(js, wi, wo)
+        u = rng.uniform(0, 1, (64, 3)).astype(np.float32)
+        sh = hemu_lib.bsdf_sample(js, wi, u)
+        so = oracle.bsdf_sample(js, wi, u)
+        ok = _same(fh, fo).all() and _same(ph, po).all() and all(_same(x, y).all() for x, y in zip(sh, so))
+        if not ok:
+            bad.append(js)
+    assert not bad, "%d parameter sets differ, e.g. %s" % (len(bad), bad[:3])
+
+
+def _samples_bit_exact(h, o, n, seed=7, npix=None, vol_mode=0):
+    rng = np.random.default_rng(seed)
+    npix = npix or o.width * o.height
+    pix = rng.integers(0, npix, n).astype(np.uint32)
+    smp = rng.integers(0, 1 << 16, n).astype(np.uint32)
+    lh = h.render_samples(pix, smp, o.seed, vol_mode)
+    lo = o.render_samples(pix, smp)
+    same = _same(lh, lo).all(1)
+    assert same.all(), "%d of %d samples differ" % ((~same).sum(), n)
+    assert np.abs(lo).sum() > 0
+
+
+def _ao_box(d):
+    sc = scenes.box_room(48, 48, 4)
+    sc["renderer"] = {"type": "ao"}
+    return write(d, "hemu_ao", sc)
+
+
+def _textured_light(d):
+    from helpers import textured_light_room
+    sc, assets = textured_light_room()
+    return write(d, "hemu_tlight", sc, assets)
+
+
+@pytest.mark.parametrize("which", ["box", "materials", "lights", "spheres", "textured", "textured_light", "ao",
+                                   "volume"])
+def test_render_samples_bit_exact(oracle, scene_dir, which):
+    """Per-sample Li of the wavefront kernels (generate, extend, the shade
+    classes, shadow; or the vol_path kernel) equals the oracle's Path::Li /
+    VolPath::Li bit for bit, 4,096 random (pixel, sample) pairs per scene."""
+    make = {"box": lambda d: box(d, 48, 48, 4), "materials": materials, "lights": lights,
+            "spheres": lambda d: spheres(d, 300, 4, 48, 32, 4), "textured": textured,
+            "textured_light": _textured_light, "ao": _ao_box, "volume": lambda d: volume(d, 32, 32, 4, grid=24)}
+    path, text, d = make[which](scene_dir)
+    h, o = hemu_lib.HemuScene(text, d), oracle.OracleScene(text, d)
+    _samples_bit_exact(h, o, 4096)
+    h.close()
+
+
+def test_render_samples_box_room_256_bit_exact(oracle, scene_dir):
+    """The box room at its stated size: 256x256, depth 8, Russian roulette from 3."""
+    path, text, d = box(scene_dir, 256, 256, 64)
+    h, o = hemu_lib.HemuScene(text, d), oracle.OracleScene(text, d)
+    _samples_bit_exact(h, o, 16384)
+    h.close()
+
+
+def test_render_samples_many_spheres_field_bit_exact(field):
+    h, o = field
+    _samples_bit_exact(h, o, 8192, seed=9)
+
+
+def test_render_samples_fbm_volume_256_bit_exact(oracle, tmp_path):
+    """vol_path on the 256^3 fBm density grid (sigma_t scale 20, albedo 0.9,
+    HG g = 0.6, rough-glass box, depth 32), at a reduced frame."""
+    sc, assets = scenes.volume_box(width=96, height=96, spp=1, max_depth=32, grid=256)
+    path = scenes.write_scene(str(tmp_path), sc, assets)
+    with open(path) as fh:
+        text = fh.read()
+    h, o = hemu_lib.HemuScene(text, str(tmp_path)), oracle.OracleScene(text, str(tmp_path))
+    _samples_bit_exact(h, o, 4096, seed=13)
+    h.close()
+    o.close()

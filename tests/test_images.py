@@ -240,6 +240,21 @@ def test_tga_decode(oracle, tmp_path, kind, bits, rle, top_down):
     _check8(oracle, tmp_path, "t.tga", data, want)
 
 
+@pytest.mark.parametrize("case", ["empty", "truncated"])
+def test_tga_bad_colour_map(oracle, tmp_path, case):
+    """A colour-mapped TGA whose palette is empty, or cut short by the end of
+    the file, is refused with an error instead of read past its end."""
+    idx = np.zeros((2, 3), np.int64)
+    if case == "empty":
+        data = bytearray(imgenc.tga(idx, 1, 8, cmap=np.zeros((0, 3), np.int64)))
+    else:
+        data = bytearray(imgenc.tga(idx, 1, 8, cmap=np.full((40, 3), 7)))
+        data = data[:18 + 10 * 3]  # header, then 10 of the 40 palette entries
+    with pytest.raises(RuntimeError, match="colour map"):
+        _load(oracle, tmp_path, "bad.tga", bytes(data), {"type": "image_default", "channel": 3,
+                                                         "is_to_linear": False, "is_flip_y": False})
+
+
 def test_hdr_through_image_default(oracle, tmp_path):
     """stbi_load of a Radiance file: (v ^ (1 / 2.2)) * 255 + 0.5 truncated, the grey
     request averaging the three decoded channels first."""

@@ -27,10 +27,26 @@ def _noalloc(rad, scene, pixels, samples, seed):
     return out.cpu().numpy()
 
 
-@pytest.mark.parametrize("which", ["box", "spheres"])
+def _scene_path(scene_dir, which):
+    from helpers import volume, write
+    from radiantiumplusplus_gb300 import scenes
+    if which == "box":
+        return box(scene_dir, 40, 30, 4)[0]
+    if which == "spheres":
+        return spheres(scene_dir, 300, 4, 48, 32, 4)[0]
+    if which == "vol_path":
+        return volume(scene_dir, 32, 32, 4, grid=24)[0]
+    sc = scenes.box_room(40, 30, 4)
+    sc["renderer"] = {"type": "ao"}
+    return write(scene_dir, "noalloc_ao", sc)[0]
+
+
+@pytest.mark.parametrize("which", ["box", "spheres", "vol_path", "ao"])
 def test_noalloc_matches_render_samples_twice(rad, scene_dir, which):
-    path = box(scene_dir, 40, 30, 4)[0] if which == "box" else spheres(scene_dir, 300, 4, 48, 32, 4)[0]
-    scene = rad.Scene.from_file(path)
+    """The same kernels on the same per-sample PCG streams: every sample's
+    radiance is bit-identical to rad_render_samples', on two calls in a row
+    (the second smaller, over the first call's leftover scratch contents)."""
+    scene = rad.Scene.from_file(_scene_path(scene_dir, which))
     rng = np.random.default_rng(4)
     for call in range(2):
         n = 16384 if call == 0 else 5000
@@ -38,8 +54,24 @@ def test_noalloc_matches_render_samples_twice(rad, scene_dir, which):
         smp = rng.integers(0, 64, n).astype(np.uint32)
         ref = scene.render_samples(pix, smp)
         got = _noalloc(rad, scene, pix, smp, scene.seed)
-        close = np.abs(got - ref) <= 1e-3 * np.maximum(np.abs(ref), 1e-1)
-        assert close.all(), "call %d: %d samples differ" % (call, (~close.all(1)).sum())
+        same = (got == ref) | (np.isnan(got) & np.isnan(ref))
+        assert same.all(), "call %d: %d samples differ" % (call, (~same.all(1)).sum())
+        assert np.abs(ref).sum() > 0
+    scene.close()
+
+
+def test_noalloc_reports_pixels_beyond_the_film(rad, scene_dir):
+    """Pixel indices sit in device memory, so the check is on the device: an
+    index past the film gives RAD_ERR_DEVICE_CHECK, and the next call is clean."""
+    scene = rad.Scene.from_file(box(scene_dir, 8, 8, 1)[0])
+    pix = np.array([0, 5, 64, 3], np.uint32)
+    smp = np.zeros(4, np.uint32)
+    with pytest.raises(rad.RadError) as e:
+        _noalloc(rad, scene, pix, smp, 0)
+    assert e.value.code == rad._capi.RAD_ERR_DEVICE_CHECK
+    pix[2] = 63
+    got = _noalloc(rad, scene, pix, smp, 0)
+    assert np.array_equal(got, scene.render_samples(pix, smp, seed=0))
     scene.close()
 
 
