@@ -129,6 +129,24 @@ RD V3 Fmadd(V3 a, V3 b, V3 c) { return V3{fmaf(a.x, b.x, c.x), fmaf(a.y, b.y, c.
 RD float Luminance(V3 c) { return (c.x * 0.212671f) + (c.y * 0.715160f) + (c.z * 0.072169f); }
 RD float fminr(float a, float b) { return (b < a) ? b : a; }  // std::min
 RD float fmaxr(float a, float b) { return (a < b) ? b : a; }  // std::max
+// fmaxf(fmaxf(a, b), c) and fminf(fminf(a, b), c) as one instruction each
+// (three-input max.f32 / min.f32, sm_100 and later); min and max do not round,
+// so the values are the same.
+#if defined(RAD_HOST_EMULATION)
+RD float Max3(float a, float b, float c) { return fmaxf(fmaxf(a, b), c); }
+RD float Min3(float a, float b, float c) { return fminf(fminf(a, b), c); }
+#else
+RD float Max3(float a, float b, float c) {
+  float d;
+  asm("max.f32 %0, %1, %2, %3;" : "=f"(d) : "f"(a), "f"(b), "f"(c));
+  return d;
+}
+RD float Min3(float a, float b, float c) {
+  float d;
+  asm("min.f32 %0, %1, %2, %3;" : "=f"(d) : "f"(a), "f"(b), "f"(c));
+  return d;
+}
+#endif
 RD float clampr(float v, float lo, float hi) { return v < lo ? lo : (hi < v ? hi : v); }
 
 // math_ext.h:48-61

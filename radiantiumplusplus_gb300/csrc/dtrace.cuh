@@ -177,6 +177,13 @@ RD bool TestPrim(const DevScene& S, const RayPre& r, uint32_t lp, bool analytic,
 }
 
 RD uint32_t ByteOf(uint32_t w, uint32_t i) { return (w >> (8u * i)) & 0xffu; }
+// Moves bit s of an 8-bit mask to bit s ^ oct (the octant's near-to-far order).
+RD uint32_t XorPerm8(uint32_t x, uint32_t oct) {
+  if (oct & 1u) x = ((x & 0x55u) << 1) | ((x >> 1) & 0x55u);
+  if (oct & 2u) x = ((x & 0x33u) << 2) | ((x >> 2) & 0x33u);
+  if (oct & 4u) x = ((x & 0x0fu) << 4) | ((x >> 4) & 0x0fu);
+  return x;
+}
 // Byte i of w as a float, exactly: the byte becomes the low mantissa bits of
 // 2^23 (one byte permute), and 2^23 is subtracted (one add) -- no conversion unit.
 #if defined(RAD_HOST_EMULATION)
@@ -238,30 +245,25 @@ RD int TravStep(const DevScene& S, const RayPre& r, TraceHit& h, uint2* stack, T
   uint32_t nz0 = r.inv.z >= 0.f ? q3.x : q4.z, nz1 = r.inv.z >= 0.f ? q3.y : q4.w;
   uint32_t fz0 = r.inv.z >= 0.f ? q4.z : q3.x, fz1 = r.inv.z >= 0.f ? q4.w : q3.y;
   uint32_t childBase = q1.x, primBase = q1.y;
-  uint32_t hitInternal = 0;  // bit (slot ^ oct)
-  uint32_t leafHits = 0;     // bit slot
   float tcur = h.t;
+  // all eight child boxes, one bit each in slot order (an empty slot holds an
+  // inverted box, lo 255 / hi 0 on every axis, which no ray passes)
+  uint32_t hits = 0;
 #pragma unroll
   for (uint32_t s = 0; s < 8; s++) {
     uint32_t w = s < 4 ? 0u : 1u, i = s & 3u;
-    uint32_t meta = ByteOf(s < 4 ? q1.z : q1.w, i);
-    bool internal = (imask >> s) & 1u;
-    if (!internal && meta == 0u) continue;
     float tnx = fmaf(ByteAsFloat(w ? nx1 : nx0, i), ax, bx);
     float tfx = fmaf(ByteAsFloat(w ? fx1 : fx0, i), ax, bx);
     float tny = fmaf(ByteAsFloat(w ? ny1 : ny0, i), ay, by);
     float tfy = fmaf(ByteAsFloat(w ? fy1 : fy0, i), ay, by);
     float tnz = fmaf(ByteAsFloat(w ? nz1 : nz0, i), az, bz);
     float tfz = fmaf(ByteAsFloat(w ? fz1 : fz0, i), az, bz);
-    float tn = fmaxf(fmaxf(tnx, tny), fmaxf(tnz, r.tmin));
-    float tf = fminf(fminf(tfx, tfy), fminf(tfz, tcur)) * 1.00000024f;
-    if (tn <= tf) {
-      if (internal)
-        hitInternal |= 1u << (s ^ r.oct);
-      else
-        leafHits |= 1u << s;
-    }
+    float tn = fmaxf(Max3(tnx, tny, tnz), r.tmin);
+    float tf = fminf(Min3(tfx, tfy, tfz), tcur) * 1.00000024f;
+    if (tn <= tf) hits |= 1u << s;
   }
+  const uint32_t leafHits = hits & ~imask;              // bit slot
+  uint32_t hitInternal = XorPerm8(hits & imask, r.oct);  // bit (slot ^ oct)
   // ---- leaves of this node: tested in the following steps, before the next
   // node visit (so the order of node visits and primitive tests is unchanged;
   // the next node below was chosen from the child boxes alone)

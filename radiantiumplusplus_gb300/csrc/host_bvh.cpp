@@ -332,7 +332,11 @@ void BuildBvh8(HostScene& hs) {
     }
     float p[3] = {nb.lo[0], nb.lo[1], nb.lo[2]};
     uint32_t imask = 0;
-    uint8_t meta[8] = {0}, qlo[3][8] = {{0}}, qhi[3][8] = {{0}};
+    // empty slots: an inverted box (lo 255, hi 0 on every axis) that no ray passes,
+    // so traversal tests all eight slots without checking which are in use
+    uint8_t meta[8] = {0}, qlo[3][8], qhi[3][8];
+    std::memset(qlo, 255, sizeof(qlo));
+    std::memset(qhi, 0, sizeof(qhi));
     uint32_t childBase = (uint32_t)hs.nodes.size();
     uint32_t primBase = (uint32_t)hs.prims.size();
     // internal children first (contiguous, in slot order), then leaf primitives (in slot order)
