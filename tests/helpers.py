@@ -207,3 +207,61 @@ BSDFS = [
 
 def bsdf_json(b):
     return json.dumps(b)
+
+
+def close_to(a, b):
+    """Per-sample agreement used by the integrator parity tests: every channel
+    within 1e-3 relative (absolute floor 1e-4)."""
+    return (np.abs(a - b) <= 1e-3 * np.maximum(np.abs(b), 1e-1)).all(axis=1)
+
+
+def ulp_sensitive(o, pix, smp, lo, seeds=64):
+    """Which of these samples change (beyond close_to) when the harness
+    (tests/hostemu: the device code on the host, bit-identical to the oracle)
+    moves transcendental results by one or two ulps, with `seeds` different
+    nudge streams (a given call gets a given nudge with probability 1/8 per
+    stream, so 64 streams miss it with probability 2e-4). The GPU's math library and the oracle's libm differ only in such
+    last-ulp rounding, so a GPU sample that differs from the oracle's must be
+    one of these."""
+    import hemu_lib
+    h = hemu_lib.HemuScene(o.json_text, o.base_dir)
+    sens = np.zeros(len(pix), bool)
+    try:
+        exact = h.render_samples(pix, smp, o.seed)
+        assert ((exact.view(np.uint32) == lo.view(np.uint32)) | (np.isnan(exact) & np.isnan(lo))).all()
+        for k in range(1, seeds + 1):
+            hemu_lib.set_nudge(k * 7919)
+            sens |= ~close_to(h.render_samples(pix, smp, o.seed), lo)
+    finally:
+        hemu_lib.set_nudge(0)
+        h.close()
+    return sens
+
+
+def sample_parity(g, o, spp, min_frac, explain=True):
+    """Every pixel's first `spp` samples through the GPU kernels and the oracle
+    on identical PCG streams. At least `min_frac` agree (close_to), the sample
+    means agree within 2%, and (explain) every sample that disagrees is one
+    whose result flips under one- or two-ulp nudges of the transcendentals. Returns
+    (fraction agreeing, GPU samples, oracle samples)."""
+    W, H = g.width, g.height
+    pix = np.repeat(np.arange(W * H, dtype=np.uint32), spp)
+    smp = np.tile(np.arange(spp, dtype=np.uint32), W * H)
+    return sample_parity_at(g, o, pix, smp, min_frac, explain)
+
+
+def sample_parity_at(g, o, pix, smp, min_frac, explain=True):
+    """sample_parity over given (pixel, sample) pairs."""
+    lg = g.render_samples(pix, smp)
+    lo = o.render_samples(pix, smp)
+    close = close_to(lg, lo)
+    frac = close.mean()
+    mg, mo = lg.mean(0), lo.mean(0)
+    assert frac >= min_frac, "only %.4f of samples agree" % frac
+    assert np.all(np.abs(mg - mo) <= 0.02 * np.abs(mo) + 1e-6), (mg, mo)
+    if explain and not close.all():
+        bad = np.where(~close)[0]
+        sens = ulp_sensitive(o, pix[bad], smp[bad], lo[bad])
+        assert sens.all(), "%d of %d differing samples do not depend on last-ulp rounding: %s" % (
+            (~sens).sum(), len(bad), [(int(pix[i]), int(smp[i])) for i in bad[~sens][:5]])
+    return frac, lg, lo

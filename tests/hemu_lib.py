@@ -89,8 +89,9 @@ class HemuScene:
 
 
 def set_nudge(seed):
-    """0: exact host libm; else every transcendental result is moved by one ulp
-    up or down (probability 1/4 each) from a stream with this seed."""
+    """0: exact host libm; else every transcendental result is moved by one or
+    two ulps up or down (probability 1/8 each; unchanged otherwise) from a
+    stream with this seed."""
     lib().hemu_set_nudge(seed)
 
 

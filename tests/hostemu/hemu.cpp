@@ -27,10 +27,12 @@
 #include "host_scene.h"
 
 // Ulp nudges: with a nonzero seed, every result of the eleven transcendental
-// functions the device code calls is moved by one ulp up or down, each with
-// probability 1/4, from a seeded stream. A sample whose radiance changes under
-// such nudges depends on last-ulp rounding of some transcendental -- the only
-// place the GPU (CUDA's math library) and the oracle (the host libm) differ.
+// functions the device code calls is moved, from a seeded stream, one ulp up
+// or down (probability 1/8 each), two ulps up or down (1/8 each) or left as
+// it is (1/2). A sample whose radiance changes under such nudges depends on
+// the last-ulp rounding of some transcendental -- the only place the GPU
+// (CUDA's math library, whose single-precision functions are within a few
+// ulp) and the oracle (the host libm) differ.
 namespace hemu {
 inline uint64_t g_nudge = 0;
 inline float Nudge(float y) {
@@ -39,9 +41,11 @@ inline float Nudge(float y) {
   z = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ull;
   z = (z ^ (z >> 27)) * 0x94D049BB133111EBull;
   z ^= z >> 31;
-  switch (z >> 62) {
+  switch (z >> 61) {
     case 0: return std::nextafter(y, INFINITY);
     case 1: return std::nextafter(y, -INFINITY);
+    case 2: return std::nextafter(std::nextafter(y, INFINITY), INFINITY);
+    case 3: return std::nextafter(std::nextafter(y, -INFINITY), -INFINITY);
     default: return y;
   }
 }

@@ -72,6 +72,7 @@ def _p(a):
 class OracleScene:
     def __init__(self, json_text, base_dir=""):
         L = lib()
+        self.json_text, self.base_dir = json_text, base_dir
         self.h = L.orc_scene_load(json_text.encode(), base_dir.encode())
         if not self.h:
             raise RuntimeError(L.orc_last_error().decode())

@@ -2,40 +2,35 @@
 the CPU oracle, sample by sample on identical PCG streams, plus film-level
 checks (job film, z-test of the mean against a high-spp oracle reference).
 
-Per-sample tolerance: the GPU uses CUDA's sinf/cosf/logf/expf/powf while the
-oracle uses glibc's, so a path can diverge when a Russian-roulette or lobe
-decision sits on a 1-ulp boundary. Required: >= 97% of samples within 1e-3
-relative (absolute floor 1e-4), and the mean over all samples within 2%.
+Per-sample tolerance: every channel within 1e-3 relative (absolute floor
+1e-4). The device code compiled for the host equals the oracle bit for bit
+(tests/test_hostemu_parity.py); on the GPU only CUDA's sinf/cosf/logf/expf/
+powf/... round differently from glibc's in the last ulp, and a path can take
+the other branch of a roulette or lobe decision that sits on such a boundary.
+Required: >= 99.5% of `path` samples (>= 99% for `vol_path`, whose free
+flights and transmittance take many logf/expf per path) agree, and every
+sample that does not is shown to flip under one- or two-ulp nudges of the
+transcendentals in the host harness. bdpt (not emulated by the harness) keeps
+a fraction bound only.
 """
 
 import numpy as np
 import pytest
 
-from helpers import box, lights, materials, spheres, volume, write
+from helpers import box, lights, materials, sample_parity, spheres, volume, write
 from radiantiumplusplus_gb300 import scenes
 
 pytestmark = pytest.mark.gpu
 
 
-def _sample_parity(g, o, spp, min_frac=0.97):
-    W, H = g.width, g.height
-    pix = np.repeat(np.arange(W * H, dtype=np.uint32), spp)
-    smp = np.tile(np.arange(spp, dtype=np.uint32), W * H)
-    lg = g.render_samples(pix, smp)
-    lo = o.render_samples(pix, smp)
-    tol = 1e-3 * np.maximum(np.abs(lo), 1e-1)
-    close = (np.abs(lg - lo) <= tol).all(axis=1)
-    frac = close.mean()
-    mg, mo = lg.mean(0), lo.mean(0)
-    assert frac >= min_frac, "only %.4f of samples agree" % frac
-    assert np.all(np.abs(mg - mo) <= 0.02 * np.abs(mo) + 1e-6), (mg, mo)
-    return frac, lg, lo
+def _sample_parity(g, o, spp, min_frac, explain=True):
+    return sample_parity(g, o, spp, min_frac, explain)
 
 
 def test_path_samples_box(rad, oracle, scene_dir):
     path, text, d = box(scene_dir, 48, 48, 4)
     g, o = rad.Scene.from_file(path), oracle.OracleScene(text, d)
-    frac, _, _ = _sample_parity(g, o, 4, 0.98)
+    frac, _, _ = _sample_parity(g, o, 4, 0.995)
     g.close()
 
 
@@ -44,21 +39,21 @@ def test_path_samples_materials(rad, oracle, scene_dir):
     two-sided layered materials in one room."""
     path, text, d = materials(scene_dir, 48, 48, 4)
     g, o = rad.Scene.from_file(path), oracle.OracleScene(text, d)
-    _sample_parity(g, o, 4, 0.97)
+    _sample_parity(g, o, 4, 0.995)
     g.close()
 
 
 def test_path_samples_spheres(rad, oracle, scene_dir):
     path, text, d = spheres(scene_dir, 400, 6, 64, 48)
     g, o = rad.Scene.from_file(path), oracle.OracleScene(text, d)
-    _sample_parity(g, o, 2, 0.95)
+    _sample_parity(g, o, 2, 0.995)
     g.close()
 
 
 def test_volpath_samples(rad, oracle, scene_dir):
     path, text, d = volume(scene_dir, 32, 32, 2, grid=24)
     g, o = rad.Scene.from_file(path), oracle.OracleScene(text, d)
-    _sample_parity(g, o, 2, 0.93)
+    _sample_parity(g, o, 2, 0.99)
     g.close()
 
 
@@ -68,7 +63,7 @@ def test_ao_samples(rad, oracle, scene_dir):
     sc["renderer"] = {"type": "ao"}
     path, text, d = write(scene_dir, "ao_box", sc)
     g, o = rad.Scene.from_file(path), oracle.OracleScene(text, d)
-    _sample_parity(g, o, 4, 0.99)
+    _sample_parity(g, o, 4, 0.995)
     film = g.render()
     ref, _ = o.render()
     assert abs(film.mean() - ref.mean()) < 1e-3 * ref.mean()
@@ -127,7 +122,7 @@ def test_bdpt_samples_and_film(rad, oracle, scene_dir, light):
     sc["renderer"] = {"type": "bdpt", "max_depth": 6, "use_mis": light != "nomis"}
     path, text, d = write(scene_dir, "bdpt_" + light, sc, assets)
     g, o = rad.Scene.from_file(path), oracle.OracleScene(text, d)
-    _sample_parity(g, o, 4, 0.95)
+    _sample_parity(g, o, 4, 0.95, explain=False)
     film = g.render()
     ref = o.render_bdpt()
     lit = ref.sum(axis=2) > 1e-3
@@ -165,7 +160,7 @@ def test_textured_light(rad, oracle, scene_dir, renderer, light):
         assert close[lit].mean() >= 0.9, close[lit].mean()
         assert abs(film.mean() - ref.mean()) < 0.01 * ref.mean()
     else:
-        _sample_parity(g, o, 4, 0.95)
+        _sample_parity(g, o, 4, {"path": 0.995, "vol_path": 0.99}.get(renderer, 0.95), renderer != "bdpt")
     g.close()
 
 
@@ -190,7 +185,7 @@ def test_bdpt_edge_cases(rad, oracle, scene_dir, case):
         sc["scene"].append({"light": {"type": "skybox", "radiance": [0.8, 0.9, 1.0]}})
     path, text, d = write(scene_dir, "bdpt_edge_" + case, sc)
     g, o = rad.Scene.from_file(path), oracle.OracleScene(text, d)
-    frac, lg, lo = _sample_parity(g, o, 8, 0.95)
+    frac, lg, lo = _sample_parity(g, o, 8, 0.95, explain=False)
     film = g.render()
     ref = o.render_bdpt()
     if case == "nolight":
@@ -205,7 +200,7 @@ def test_path_samples_lights(rad, oracle, scene_dir):
     an area emitter."""
     path, text, d = lights(scene_dir, 48, 48, 4)
     g, o = rad.Scene.from_file(path), oracle.OracleScene(text, d)
-    _sample_parity(g, o, 4, 0.97)
+    _sample_parity(g, o, 4, 0.995)
     g.close()
 
 
@@ -218,7 +213,7 @@ def test_volpath_samples_point_light(rad, oracle, scene_dir):
                         "light": {"type": "projection", "fov": 30.0, "irradiance": [4.0, 3.0, 2.0]}})
     path, text, d = write(scene_dir, "vol_point_32", sc, assets)
     g, o = rad.Scene.from_file(path), oracle.OracleScene(text, d)
-    _sample_parity(g, o, 2, 0.93)
+    _sample_parity(g, o, 2, 0.99)
     g.close()
 
 
