@@ -215,14 +215,15 @@ def close_to(a, b):
     return (np.abs(a - b) <= 1e-3 * np.maximum(np.abs(b), 1e-1)).all(axis=1)
 
 
-def ulp_sensitive(o, pix, smp, lo, seeds=64):
+def ulp_sensitive(o, pix, smp, lo, seeds=32, max_calls=50000):
     """Which of these samples change (beyond close_to) when the harness
     (tests/hostemu: the device code on the host, bit-identical to the oracle)
-    moves transcendental results by one or two ulps, with `seeds` different
-    nudge streams (a given call gets a given nudge with probability 1/8 per
-    stream, so 64 streams miss it with probability 2e-4). The GPU's math library and the oracle's libm differ only in such
-    last-ulp rounding, so a GPU sample that differs from the oracle's must be
-    one of these."""
+    moves transcendental results by one or two ulps. The GPU's math library
+    and the oracle's libm differ only in such last-ulp rounding, so a GPU
+    sample that differs from the oracle's must be one of these. First `seeds`
+    random nudge streams over the whole batch; then, for each sample not yet
+    shown to flip, rendered alone, every one of its transcendental calls in
+    turn moved by -2, -1, +1 and +2 ulps."""
     import hemu_lib
     h = hemu_lib.HemuScene(o.json_text, o.base_dir)
     sens = np.zeros(len(pix), bool)
@@ -232,8 +233,23 @@ def ulp_sensitive(o, pix, smp, lo, seeds=64):
         for k in range(1, seeds + 1):
             hemu_lib.set_nudge(k * 7919)
             sens |= ~close_to(h.render_samples(pix, smp, o.seed), lo)
+        hemu_lib.set_nudge(0)
+        for i in np.where(~sens)[0]:
+            p1, s1 = pix[i:i + 1], smp[i:i + 1]
+            h.render_samples(p1, s1, o.seed)
+            calls = min(int(hemu_lib.last_calls()), max_calls)
+            for c in range(calls):
+                for u in (-2, -1, 1, 2):
+                    hemu_lib.set_nudge_target(c, u)
+                    if not close_to(h.render_samples(p1, s1, o.seed), lo[i:i + 1])[0]:
+                        sens[i] = True
+                        break
+                if sens[i]:
+                    break
+            hemu_lib.set_nudge_target(-1, 0)
     finally:
         hemu_lib.set_nudge(0)
+        hemu_lib.set_nudge_target(-1, 0)
         h.close()
     return sens
 

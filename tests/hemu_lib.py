@@ -30,6 +30,9 @@ def lib():
         L.hemu_bsdf_sample.argtypes = [ctypes.c_char_p, P, P, ctypes.c_int64, P, P, P, P, P]
         L.hemu_render_samples.argtypes = [P, P, P, ctypes.c_int64, ctypes.c_uint32, ctypes.c_uint32, P]
         L.hemu_set_nudge.argtypes = [ctypes.c_uint64]
+        L.hemu_set_nudge_config.argtypes = [ctypes.c_uint32, ctypes.c_uint32]
+        L.hemu_set_nudge_target.argtypes = [ctypes.c_int64, ctypes.c_int32]
+        L.hemu_last_calls.restype = ctypes.c_uint64
         _lib = L
     return _lib
 
@@ -89,10 +92,28 @@ class HemuScene:
 
 
 def set_nudge(seed):
-    """0: exact host libm; else every transcendental result is moved by one or
-    two ulps up or down (probability 1/8 each; unchanged otherwise) from a
-    stream with this seed."""
+    """0: exact host libm; else, from a stream with this seed, each nudged
+    transcendental result moves (probability 1/2) by 1 .. max_ulps ulps up or
+    down (set_nudge_config)."""
     lib().hemu_set_nudge(seed)
+
+
+NUDGE_FUNCTIONS = ["sinf", "cosf", "tanf", "expf", "logf", "log2f", "powf", "atan2f", "acosf", "asinf", "erff"]
+
+
+def set_nudge_target(index=-1, ulps=0):
+    """Move only call number `index` of each render by `ulps` (signed); -1 ends it."""
+    lib().hemu_set_nudge_target(index, ulps)
+
+
+def last_calls():
+    """Transcendental calls made by the last render."""
+    return lib().hemu_last_calls()
+
+
+def set_nudge_config(mask=0x7FF, max_ulps=2):
+    """Bit i of mask: NUDGE_FUNCTIONS[i] is nudged; results move by at most max_ulps."""
+    lib().hemu_set_nudge_config(mask, max_ulps)
 
 
 def bsdf_eval(bsdf_json, wi, wo):

@@ -26,41 +26,54 @@
 #include "host_json.h"
 #include "host_scene.h"
 
-// Ulp nudges: with a nonzero seed, every result of the eleven transcendental
-// functions the device code calls is moved, from a seeded stream, one ulp up
-// or down (probability 1/8 each), two ulps up or down (1/8 each) or left as
-// it is (1/2). A sample whose radiance changes under such nudges depends on
-// the last-ulp rounding of some transcendental -- the only place the GPU
-// (CUDA's math library, whose single-precision functions are within a few
-// ulp) and the oracle (the host libm) differ.
+// Ulp nudges: with a nonzero seed, each result of the eleven transcendental
+// functions the device code calls (those whose bit in the mask is set) is
+// moved, from a seeded stream, with probability 1/2 by 1 .. max_ulps ulps
+// (uniform) up or down (1/2 each), else left as it is. A sample whose
+// radiance changes under such nudges depends on the last-ulp rounding of some
+// transcendental -- the only place the GPU (CUDA's math library, whose
+// single-precision functions are within a few ulp) and the oracle (the host
+// libm) differ. Targeted mode instead moves exactly one call (by its index
+// among the calls of a render) by a given number of ulps.
 namespace hemu {
 inline uint64_t g_nudge = 0;
-inline float Nudge(float y) {
-  if (g_nudge == 0 || !std::isfinite(y)) return y;
+inline uint32_t g_mask = 0x7ffu;
+inline uint32_t g_maxUlps = 2;
+inline uint64_t g_calls = 0;      // transcendental calls of the current render
+inline int64_t g_target = -1;     // targeted mode: the call to move
+inline int32_t g_targetUlps = 0;  // and by how many ulps (signed)
+inline float Nudge(float y, uint32_t fn) {
+  const uint64_t call = g_calls++;
+  if (!std::isfinite(y)) return y;
+  if (g_target >= 0) {
+    if ((int64_t)call != g_target) return y;
+    const float dir = g_targetUlps > 0 ? INFINITY : -INFINITY;
+    for (int32_t i = 0; i < std::abs(g_targetUlps); i++) y = std::nextafter(y, dir);
+    return y;
+  }
+  if (g_nudge == 0 || !((g_mask >> fn) & 1u)) return y;
   uint64_t z = (g_nudge += 0x9E3779B97F4A7C15ull);
   z = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ull;
   z = (z ^ (z >> 27)) * 0x94D049BB133111EBull;
   z ^= z >> 31;
-  switch (z >> 61) {
-    case 0: return std::nextafter(y, INFINITY);
-    case 1: return std::nextafter(y, -INFINITY);
-    case 2: return std::nextafter(std::nextafter(y, INFINITY), INFINITY);
-    case 3: return std::nextafter(std::nextafter(y, -INFINITY), -INFINITY);
-    default: return y;
-  }
+  if (z >> 63) return y;
+  const float dir = ((z >> 62) & 1u) ? INFINITY : -INFINITY;
+  uint32_t k = 1u + (uint32_t)((z & 0xffffffffu) % g_maxUlps);
+  for (uint32_t i = 0; i < k; i++) y = std::nextafter(y, dir);
+  return y;
 }
 }  // namespace hemu
-#define sinf(x) hemu::Nudge(::sinf(x))
-#define cosf(x) hemu::Nudge(::cosf(x))
-#define tanf(x) hemu::Nudge(::tanf(x))
-#define expf(x) hemu::Nudge(::expf(x))
-#define logf(x) hemu::Nudge(::logf(x))
-#define log2f(x) hemu::Nudge(::log2f(x))
-#define powf(x, y) hemu::Nudge(::powf(x, y))
-#define atan2f(y, x) hemu::Nudge(::atan2f(y, x))
-#define acosf(x) hemu::Nudge(::acosf(x))
-#define asinf(x) hemu::Nudge(::asinf(x))
-#define erff(x) hemu::Nudge(::erff(x))
+#define sinf(x) hemu::Nudge(::sinf(x), 0)
+#define cosf(x) hemu::Nudge(::cosf(x), 1)
+#define tanf(x) hemu::Nudge(::tanf(x), 2)
+#define expf(x) hemu::Nudge(::expf(x), 3)
+#define logf(x) hemu::Nudge(::logf(x), 4)
+#define log2f(x) hemu::Nudge(::log2f(x), 5)
+#define powf(x, y) hemu::Nudge(::powf(x, y), 6)
+#define atan2f(y, x) hemu::Nudge(::atan2f(y, x), 7)
+#define acosf(x) hemu::Nudge(::acosf(x), 8)
+#define asinf(x) hemu::Nudge(::asinf(x), 9)
+#define erff(x) hemu::Nudge(::erff(x), 10)
 
 #include "k_path.cu"
 #include "k_vol.cu"
@@ -252,6 +265,20 @@ const char* hemu_last_error() { return g_err.c_str(); }
 
 // 0 = exact host libm results (the default); else the seed of the ulp nudges.
 void hemu_set_nudge(uint64_t seed) { hemu::g_nudge = seed; }
+// Which functions are nudged (bit i: sinf, cosf, tanf, expf, logf, log2f,
+// powf, atan2f, acosf, asinf, erff) and by at most how many ulps.
+void hemu_set_nudge_config(uint32_t mask, uint32_t max_ulps) {
+  hemu::g_mask = mask;
+  hemu::g_maxUlps = max_ulps < 1u ? 1u : max_ulps;
+}
+// Targeted mode: only call number `index` of each render moves, by `ulps`
+// (signed); index < 0 leaves targeted mode.
+void hemu_set_nudge_target(int64_t index, int32_t ulps) {
+  hemu::g_target = index;
+  hemu::g_targetUlps = ulps;
+}
+// Transcendental calls made by the last hemu_render_samples.
+uint64_t hemu_last_calls() { return hemu::g_calls; }
 
 void* hemu_scene_load(const char* json, const char* base_dir) {
   auto h = std::make_unique<HemuScene>();
@@ -352,6 +379,7 @@ int hemu_bsdf_sample(const char* json, const float* wi, const float* u, int64_t 
 int hemu_render_samples(void* s, const uint32_t* pix, const uint32_t* smp, int64_t n, uint32_t seed,
                         uint32_t vol_mode, float* out) {
   const DevScene& S = static_cast<HemuScene*>(s)->S;
+  hemu::g_calls = 0;
   return Guarded([&] {
     if (S.isParticle || S.isBdpt) throw std::runtime_error("renderer has no emulated per-sample wave");
     const uint64_t npix = (uint64_t)S.cam.width * S.cam.height;

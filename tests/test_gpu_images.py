@@ -2,16 +2,23 @@
 (tests/golden, made by tests/golden/make_references.py from the oracle's
 Path::Li / VolPath::Li).
 
-* 64 spp: a per-pixel z-test of the GPU mean. Each pixel channel's error is
-  scaled by the standard error of the 64-sample mean (from the GPU samples'
-  own variance, plus the reference's); at most 1% of pixel channels may lie
-  beyond 4 standard errors (Monte Carlo means at 64 spp are heavy tailed, so
-  the fraction allowed is far above a normal tail's 6e-5, but a biased
-  estimator fails it wholesale), and the frame means agree within 3 standard
-  errors.
-* converged: the GPU job film at many samples per pixel reaches
-  relMSE < 1e-3 against the reference, relMSE = mean over pixel channels of
-  (x - ref)^2 / (ref^2 + 1e-2 * mean(ref)^2).
+Each pixel's per-sample variance sigma^2 is estimated from 1,024 (box room)
+or 4,096 further GPU samples, independent of the ones tested.
+
+* 64 spp: a per-pixel z-test of the GPU mean, z = (mean - ref) / se with
+  se^2 = sigma^2 (1/64 + 1/N_ref), plus the half-ulp of the reference's fp16
+  storage. At most 1% of pixel channels may lie beyond 4 standard errors
+  (means of 64 heavy-tailed Monte Carlo samples are not normal, so the
+  allowance is above a normal tail's 6e-5, but a biased estimator fails it
+  wholesale), and the frame means agree within 3 standard errors.
+* converged: the GPU job film at 16,384 (box room) or 65,536 samples per pixel
+  against the reference, relMSE = mean over pixel channels of
+  (x - ref)^2 / (ref^2 + 1e-2 mean(ref)^2). Two independent unbiased renders
+  differ by relMSE ~ E[sigma^2 / (ref^2 + eps)] (1/N_gpu + 1/N_ref); the test
+  requires at most twice that, and below 1e-3 where the reference's own
+  noise allows it (box room, many spheres). The fBm volume is heavy tailed
+  (E[sigma^2 / ref^2] ~ 340 per sample): its 65,536-spp reference alone
+  carries relMSE ~ 5e-3, so there only the noise-consistency bound applies.
 """
 import os
 import sys
@@ -26,6 +33,9 @@ import make_references as refs  # noqa: E402
 
 pytestmark = pytest.mark.gpu
 
+VAR_SAMPLES = {"box_room_256": 1024, "many_spheres_96x54": 4096, "fbm_volume_64": 4096}
+CONVERGED = {"box_room_256": (16384, True), "many_spheres_96x54": (65536, True), "fbm_volume_64": (65536, False)}
+
 
 def _reference(name):
     d = np.load(os.path.join(HERE, "golden", name + ".npz"))
@@ -39,25 +49,41 @@ def _scene(rad, scene_dir, name):
     return rad.Scene.from_file(path)
 
 
+def _moments(s, first, n):
+    """Per-pixel mean and variance of samples [first, first + n) through
+    rad_render_samples (invalid samples count as zero, as the film drops them)."""
+    H, W = s.height, s.width
+    m1 = np.zeros((H * W, 3))
+    m2 = np.zeros((H * W, 3))
+    chunk = max(1, (1 << 20) // n)
+    for p0 in range(0, H * W, chunk):
+        px = np.arange(p0, min(H * W, p0 + chunk), dtype=np.uint32)
+        pix = np.repeat(px, n)
+        smp = np.tile(np.arange(first, first + n, dtype=np.uint32), len(px))
+        L = s.render_samples(pix, smp).reshape(len(px), n, 3).astype(np.float64)
+        bad = np.isnan(L).any(-1) | np.isinf(L[..., 0]) | (L[..., 0] < 0)
+        L[bad] = 0.0
+        m1[px] = L.mean(1)
+        m2[px] = L.var(1, ddof=1)
+    return m1.reshape(H, W, 3), m2.reshape(H, W, 3)
+
+
+def _eps(ref):
+    return 1e-2 * ref.mean() ** 2
+
+
 def rel_mse(x, ref):
-    eps = 1e-2 * ref.mean() ** 2
-    return float(np.mean((x - ref) ** 2 / (ref ** 2 + eps)))
+    return float(np.mean((x - ref) ** 2 / (ref ** 2 + _eps(ref))))
 
 
 @pytest.mark.parametrize("name", refs.NAMES)
 def test_64spp_ztest_against_reference(rad, scene_dir, name):
     ref, ref_spp = _reference(name)
     s = _scene(rad, scene_dir, name)
-    H, W = ref.shape[:2]
     spp = 64
-    pix = np.repeat(np.arange(W * H, dtype=np.uint32), spp)
-    smp = np.tile(np.arange(spp, dtype=np.uint32), W * H)
-    L = s.render_samples(pix, smp).reshape(H, W, spp, 3).astype(np.float64)
-    bad = np.isnan(L).any(-1) | np.isinf(L[..., 0]) | (L[..., 0] < 0)  # dropped as the film drops them
-    L[bad] = 0.0
-    mean = L.mean(2)
-    var = L.var(2, ddof=1)
-    se = np.sqrt(var / spp + var / ref_spp) + 1e-7
+    mean, _ = _moments(s, 0, spp)
+    _, var = _moments(s, 100000, VAR_SAMPLES[name])
+    se = np.sqrt(var / spp + var / ref_spp) + np.abs(ref) * 2.0 ** -11 + 1e-7
     z = np.abs(mean - ref) / se
     frac = float((z > 4).mean())
     assert frac < 0.01, "%s: %.4f of pixel channels beyond 4 standard errors" % (name, frac)
@@ -69,15 +95,19 @@ def test_64spp_ztest_against_reference(rad, scene_dir, name):
     s.close()
 
 
-@pytest.mark.parametrize("name,spp", [("box_room_256", 16384), ("many_spheres_96x54", 65536),
-                                      ("fbm_volume_64", 65536)])
-def test_converged_relmse_below_1e3(rad, scene_dir, name, spp):
+@pytest.mark.parametrize("name", refs.NAMES)
+def test_converged_relmse(rad, scene_dir, name):
     ref, ref_spp = _reference(name)
+    spp, below_1e3 = CONVERGED[name]
     s = _scene(rad, scene_dir, name)
+    _, var = _moments(s, 100000, VAR_SAMPLES[name])
     j = s.submit(spp=spp, seed=424242)
     j.wait()
     film = j.film().astype(np.float64)
     j.close()
     s.close()
     r = rel_mse(film, ref)
-    assert r < 1e-3, "%s: relMSE %.2e at %d spp" % (name, r, spp)
+    expected = float(np.mean(var / (ref ** 2 + _eps(ref)))) * (1.0 / spp + 1.0 / ref_spp)
+    assert r < 2 * expected + 1e-6, "%s: relMSE %.2e at %d spp, noise alone %.2e" % (name, r, spp, expected)
+    if below_1e3:
+        assert r < 1e-3, "%s: relMSE %.2e at %d spp" % (name, r, spp)

@@ -226,3 +226,20 @@ def test_render_samples_fbm_volume_256_bit_exact(oracle, tmp_path):
     _samples_bit_exact(h, o, 4096, seed=13)
     h.close()
     o.close()
+
+
+def test_ulp_explanation_discriminates(oracle, scene_dir):
+    """The GPU parity tests accept a differing sample only if one- or two-ulp
+    moves of its transcendental results flip it in the harness. That must not
+    hold for samples in general, or it would explain away a real device bug:
+    of random vol_path samples (the most ulp-sensitive renderer here) almost
+    none flip."""
+    from helpers import ulp_sensitive
+    path, text, d = volume(scene_dir, 32, 32, 4, grid=24)
+    o = oracle.OracleScene(text, d)
+    rng = np.random.default_rng(17)
+    pix = rng.integers(0, 32 * 32, 48).astype(np.uint32)
+    smp = rng.integers(0, 1 << 16, 48).astype(np.uint32)
+    lo = o.render_samples(pix, smp)
+    sens = ulp_sensitive(o, pix, smp, lo)
+    assert sens.mean() <= 0.1, sens.mean()
