@@ -281,3 +281,39 @@ def sample_parity_at(g, o, pix, smp, min_frac, explain=True):
         assert sens.all(), "%d of %d differing samples do not depend on last-ulp rounding: %s" % (
             (~sens).sum(), len(bad), [(int(pix[i]), int(smp[i])) for i in bad[~sens][:5]])
     return frac, lg, lo
+
+
+def _disney(rng):
+    b = {"type": "disney"}
+    if rng.uniform() < 0.8:
+        b["base_color"] = rng.uniform(0, 1, 3).round(6).tolist()
+    for k in ("metallic", "roughness", "specular", "spec_tint", "spec_trans", "anisotropic", "sheen", "sheen_tint",
+              "clearcoat", "clearcoat_gloss", "flatness"):
+        r = rng.uniform()
+        if r < 0.5:
+            b[k] = float(np.float32(rng.uniform()))
+        elif r < 0.6:
+            b[k] = 0.0  # present but zero: the reference's "present" flags need nonzero
+    return b
+
+
+def bsdf_sweep(n_disney, seed=11):
+    """Seeded parameter sets over the many-spheres materials' ranges."""
+    rng = np.random.default_rng(seed)
+    out = [dict(b) for b in BSDFS]
+    out += [_disney(rng) for _ in range(n_disney)]
+    for a in [0.0, 1e-4, 1e-3] + list(rng.uniform(0, 0.3, 40)):
+        out.append({"type": "rough_glass", "int_ior": 1.5, "ext_ior": 1.0, "alpha": float(np.float32(a))})
+    out.append({"type": "rough_glass", "int_ior": 1.33, "ext_ior": 1.0, "alpha": 0.0})
+    for _ in range(60):
+        b = {"type": "rough_metal", "distribution": "ggx" if rng.uniform() < 0.7 else "beckmann",
+             "sample_visible": bool(rng.uniform() < 0.8)}
+        if rng.uniform() < 0.3:
+            b["alpha_u"] = float(np.float32(rng.uniform(0.05, 0.5)))
+            b["alpha_v"] = float(np.float32(rng.uniform(0.05, 0.5)))
+        else:
+            b["alpha"] = float(np.float32(rng.uniform(0.05, 0.5)))
+        out.append(b)
+    for _ in range(20):
+        out.append({"type": "diffuse", "reflectance": rng.uniform(0.1, 0.9, 3).round(6).tolist()})
+    return out

@@ -18,7 +18,7 @@ import numpy as np
 import pytest
 
 import hemu_lib
-from helpers import BSDFS, box, directions, lights, materials, spheres, textured, volume, write
+from helpers import box, bsdf_sweep, directions, lights, materials, spheres, textured, volume, write
 from radiantiumplusplus_gb300 import scenes
 
 
@@ -103,42 +103,6 @@ def test_trace_box_edge_cases_bit_exact(oracle, scene_dir):
     h.close()
 
 
-def _disney(rng):
-    b = {"type": "disney"}
-    if rng.uniform() < 0.8:
-        b["base_color"] = rng.uniform(0, 1, 3).round(6).tolist()
-    for k in ("metallic", "roughness", "specular", "spec_tint", "spec_trans", "anisotropic", "sheen", "sheen_tint",
-              "clearcoat", "clearcoat_gloss", "flatness"):
-        r = rng.uniform()
-        if r < 0.5:
-            b[k] = float(np.float32(rng.uniform()))
-        elif r < 0.6:
-            b[k] = 0.0  # present but zero: the reference's "present" flags need nonzero
-    return b
-
-
-def _sweep_bsdfs(n_disney, seed=11):
-    """Seeded parameter sets over the many-spheres materials' ranges."""
-    rng = np.random.default_rng(seed)
-    out = [dict(b) for b in BSDFS]
-    out += [_disney(rng) for _ in range(n_disney)]
-    for a in [0.0, 1e-4, 1e-3] + list(rng.uniform(0, 0.3, 40)):
-        out.append({"type": "rough_glass", "int_ior": 1.5, "ext_ior": 1.0, "alpha": float(np.float32(a))})
-    out.append({"type": "rough_glass", "int_ior": 1.33, "ext_ior": 1.0, "alpha": 0.0})
-    for _ in range(60):
-        b = {"type": "rough_metal", "distribution": "ggx" if rng.uniform() < 0.7 else "beckmann",
-             "sample_visible": bool(rng.uniform() < 0.8)}
-        if rng.uniform() < 0.3:
-            b["alpha_u"] = float(np.float32(rng.uniform(0.05, 0.5)))
-            b["alpha_v"] = float(np.float32(rng.uniform(0.05, 0.5)))
-        else:
-            b["alpha"] = float(np.float32(rng.uniform(0.05, 0.5)))
-        out.append(b)
-    for _ in range(20):
-        out.append({"type": "diffuse", "reflectance": rng.uniform(0.1, 0.9, 3).round(6).tolist()})
-    return out
-
-
 def test_bsdf_sweep_bit_exact(oracle):
     """Eval / pdf / sample of 2,000 Disney parameter sets (every parameter
     U[0, 1], each key present, present-and-zero or absent), rough glass at
@@ -147,7 +111,7 @@ def test_bsdf_sweep_bit_exact(oracle):
     and 64 samples each, identical bits."""
     rng = np.random.default_rng(12)
     bad = []
-    for b in _sweep_bsdfs(2000):
+    for b in bsdf_sweep(2000):
         js = json.dumps(b)
         wi, wo = directions(rng, 64), directions(rng, 64)
         wi[:8, 2] = np.abs(wi[:8, 2])  # a few same-hemisphere pairs for the reflection lobes
