@@ -38,9 +38,14 @@ sys.path.insert(0, ROOT)
 
 W, H = 1920, 1080
 MAX_DEPTH = 16
-# DRAM bytes per KExtend launch on this workload, measured by ncu (one wave, mean of 16 launches);
-# algorithmic bytes per launch are ~7x larger, the rest is served from L1/L2.
-EXTEND_DRAM_BYTES_PER_LAUNCH = 125.9e6
+# DRAM bytes (read + written) per closest-hit ray of KExtend on this scene, from one ncu capture of a whole
+# wave (16 launches) with the tuned launch parameters: 593.0 MB for 1,731,983 rays at a 960x540 frame of the
+# same scene (the BVH and primitives are the full scene's; traffic per ray follows the BVH and the ray mix, not
+# the frame size). The algorithmic bytes per ray are ~6x larger: L1/L2 serve the rest.
+EXTEND_DRAM_BYTES_PER_RAY = 342.4
+# Issue-side counters of the same capture (bounce-1 launch): the kernel's limiter.
+EXTEND_ISSUE = {"lanes_active_per_warp_inst": 15.48, "issue_active_pct": 72.4, "alu_pipe_pct": 58.5,
+                "fma_pipe_pct": 27.5}
 BYTES_QUEUE, BYTES_RAY, BYTES_HIT, BYTES_NODE, BYTES_PRIM = 4, 32, 32, 80, 48
 
 
@@ -257,6 +262,8 @@ def run_ours(args, world, rank, local):
                                            + prims_per_ray * BYTES_PRIM)
         ext_launch_ms = pst["ms_extend"] / n_ext
         achieved = (ext_bytes / n_ext) / (ext_launch_ms / 1000.0) / 1e9 if ext_launch_ms > 0 else 0.0
+        traffic = EXTEND_DRAM_BYTES_PER_RAY * pst["rays_closest"] / n_ext
+        dram_gbs = traffic / (ext_launch_ms / 1000.0) / 1e9 if ext_launch_ms > 0 else 0.0
         cpu = None
         if rank == 0 and world == 1 and not args.no_cpu:
             cpu = cpu_baseline(path, row_step=args.cpu_row_step)
@@ -280,9 +287,15 @@ def run_ours(args, world, rank, local):
         "gpu_launches": st["kernel_launches"],
         "kernel_ms_profiled_2spp": {k: round(v, 3) for k, v in kern.items()},
         "roofline": {"bound": "hbm", "kernel": "extend (BVH8 closest hit)", "achieved": achieved, "peak": hbm_peak,
-                     "unit": "GB/s", "frac": achieved / hbm_peak, "traffic": EXTEND_DRAM_BYTES_PER_LAUNCH,
-                     "traffic_source": "ncu dram__bytes_read.sum + dram__bytes_write.sum, mean over the 16 extend "
-                                       "launches of one wave of this workload",
+                     "unit": "GB/s", "frac": achieved / hbm_peak, "traffic": traffic,
+                     "traffic_source": "ncu dram__bytes_read.sum + dram__bytes_write.sum over one wave of the tuned "
+                                       "kernel (342.4 B per closest-hit ray) x closest-hit rays per launch",
+                     "achieved_is": "algorithmic bytes (nodes, primitives, ray, hit) per launch / launch time; "
+                                    "mostly served by L1/L2",
+                     "dram_gbs": dram_gbs, "dram_frac": dram_gbs / hbm_peak,
+                     "limiter": "instruction issue (ALU pipe), not HBM: see issue",
+                     "issue": dict(EXTEND_ISSUE, simt_efficiency=EXTEND_ISSUE["lanes_active_per_warp_inst"] / 32.0,
+                                   source="ncu --set full, bounce-1 launch, 960x540 frame of this scene"),
                      "peak_source": peak_src, "dominant_kernel_by_time": dominant,
                      "nodes_per_ray": nodes_per_ray, "prims_per_ray": prims_per_ray,
                      "bytes_per_ray": BYTES_QUEUE + BYTES_RAY + BYTES_HIT + nodes_per_ray * BYTES_NODE

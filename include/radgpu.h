@@ -109,6 +109,10 @@ typedef struct rad_stats {
    * device time of the guide inference and training stages */
   uint64_t guide_records, guide_train_steps;
   double ms_guide_infer, ms_guide_train;
+  /* waves of this job that held paths of other jobs too (mixed waves: plain
+   * `path` jobs running together share every launch of a wave; the rays of such
+   * a wave are apportioned to its jobs by their shares of its paths) */
+  uint64_t mixed_waves;
 } rad_stats;
 
 /* ---- library ------------------------------------------------------------ */

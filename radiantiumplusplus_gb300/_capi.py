@@ -79,7 +79,7 @@ class Stats(ctypes.Structure):
                 ("trav_prims_closest", ctypes.c_uint64), ("trav_nodes_shadow", ctypes.c_uint64),
                 ("trav_prims_shadow", ctypes.c_uint64), ("guide_records", ctypes.c_uint64),
                 ("guide_train_steps", ctypes.c_uint64), ("ms_guide_infer", ctypes.c_double),
-                ("ms_guide_train", ctypes.c_double)]
+                ("ms_guide_train", ctypes.c_double), ("mixed_waves", ctypes.c_uint64)]
 
 
 class TuneResult(ctypes.Structure):

@@ -54,6 +54,28 @@ __device__ __forceinline__ uint32_t WarpAppend(uint32_t* counter, bool pred) {
   return base + __popc(mask & ((1u << lane) - 1u));
 }
 
+// Camera ray, PCG stream and path state of path slot i (pixel `pix`, sample `smp`).
+__device__ __forceinline__ void GeneratePath(const DevScene& S, const PathBuffers& B, uint32_t i, uint32_t pix,
+                                             uint32_t smp, uint32_t seed) {
+  uint32_t x = pix % (uint32_t)S.cam.width, y = pix / (uint32_t)S.cam.width;
+  Pcg32 rng = PcgForSample(pix, smp, seed);
+  float jx = Next1D(rng);
+  float jy = Next1D(rng);
+  V3 O, D;
+  float tmin, tmax;
+  CameraRay(S.cam, (float)x + jx, (float)y + jy, O, D, tmin, tmax);
+  B.rayO[i] = make_float4(O.x, O.y, O.z, tmin);
+  B.rayD[i] = make_float4(D.x, D.y, D.z, tmax);
+  B.thr[i] = make_float4(1.f, 1.f, 1.f, 1.f);
+  B.L[i] = make_float4(0.f, 0.f, 0.f, 1.f);
+  // the first shading point has no previous vertex: the slot carries the screen
+  // position, from which textured materials rebuild the camera ray differentials
+  B.prev[i] = make_float4((float)x + jx, (float)y + jy, 0.f, __uint_as_float(1u));
+  B.rng[i] = make_uint2((uint32_t)rng.state, (uint32_t)(rng.state >> 32));
+  B.pixel[i] = pix;
+  B.q[0][i] = i;
+}
+
 __global__ void __launch_bounds__(kBlock) KGenerate(DevScene S, PathBuffers B, WaveParams w) {
   uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
   // reset this wave's counters (all but the sticky device-error word)
@@ -73,23 +95,28 @@ __global__ void __launch_bounds__(kBlock) KGenerate(DevScene S, PathBuffers B, W
   }
   uint32_t smp = w.sampleList ? w.sampleList[i] : (w.ctx ? w.ctx->sample : w.sample) + s;
   uint32_t seed = w.ctx ? w.ctx->seed : w.seed;
-  uint32_t x = pix % (uint32_t)S.cam.width, y = pix / (uint32_t)S.cam.width;
-  Pcg32 rng = PcgForSample(pix, smp, seed);
-  float jx = Next1D(rng);
-  float jy = Next1D(rng);
-  V3 O, D;
-  float tmin, tmax;
-  CameraRay(S.cam, (float)x + jx, (float)y + jy, O, D, tmin, tmax);
-  B.rayO[i] = make_float4(O.x, O.y, O.z, tmin);
-  B.rayD[i] = make_float4(D.x, D.y, D.z, tmax);
-  B.thr[i] = make_float4(1.f, 1.f, 1.f, 1.f);
-  B.L[i] = make_float4(0.f, 0.f, 0.f, 1.f);
-  // the first shading point has no previous vertex: the slot carries the screen
-  // position, from which textured materials rebuild the camera ray differentials
-  B.prev[i] = make_float4((float)x + jx, (float)y + jy, 0.f, __uint_as_float(1u));
-  B.rng[i] = make_uint2((uint32_t)rng.state, (uint32_t)(rng.state >> 32));
-  B.pixel[i] = pix;
-  B.q[0][i] = i;
+  GeneratePath(S, B, i, pix, smp, seed);
+}
+
+// Job of path slot i in a mixed wave (jobs hold ascending, contiguous slot ranges).
+__device__ __forceinline__ uint32_t MixJobOf(const MixJob* mix, uint32_t nJobs, uint32_t i) {
+  uint32_t k = 0;
+  while (k + 1u < nJobs && i >= mix[k + 1u].pathBegin) k++;
+  return k;
+}
+
+// Mixed wave: every job's paths, each with its own scene, pixels, samples and seed.
+__global__ void __launch_bounds__(kBlock) KGenerateMix(PathBuffers B, uint32_t total, uint32_t nJobs) {
+  uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+  for (uint32_t k = i; k < (uint32_t)kCounterWords; k += gridDim.x * blockDim.x) {
+    if (k != (uint32_t)(kMiscBase + 1)) B.counters[k] = k == 0 ? total : 0u;
+  }
+  if (i >= total) return;
+  const uint32_t k = MixJobOf(B.mix, nJobs, i);
+  const MixJob& J = B.mix[k];
+  const uint32_t local = i - J.pathBegin;
+  B.job[i] = (uint8_t)k;
+  GeneratePath(J.S, B, i, J.pixelBegin + local % J.npc, J.sample + local / J.npc, J.seed);
 }
 
 // Adds per-warp sums of traversal counters into 64-bit totals (counting variants only).
@@ -110,19 +137,30 @@ __device__ __forceinline__ void FlushTravCounts(unsigned long long* out, uint32_
 // the queue from a per-bounce counter (one atomic per warp). Lanes of a warp thus
 // stay busy although ray traversal lengths vary widely (one ray per thread left
 // ~9 of 32 lanes active per instruction).
-template <bool COUNT>
+// The scene of a path: the wave's one scene, or in a mixed wave that of its job jb.
+template <bool MIX>
+__device__ __forceinline__ const DevScene& SceneOf(const DevScene& S0, const PathBuffers& B, uint32_t jb) {
+  if constexpr (MIX) {
+    return B.mix[jb].S;
+  } else {
+    return S0;
+  }
+}
+
+// MIX: a mixed wave; each lane's ray belongs to the job B.job[p] of B.mix, whose
+// scene it traces (the default instantiation reads the one scene S0).
+template <bool COUNT, bool MIX>
 __global__ void __launch_bounds__(kBlock, 8)
-    KExtend(DevScene S, PathBuffers B, int depth, unsigned long long* trav, int refillBusy, int leafFrac8) {
+    KExtend(DevScene S0, PathBuffers B, int depth, unsigned long long* trav, int refillBusy, int leafFrac8) {
   const uint32_t count = B.counters[depth];
   const uint32_t* qin = B.q[depth & 1];
   uint32_t* fetch = B.counters + kFetchBase + 2 * depth;
   uint32_t* err = B.counters + kMiscBase + 1;
   uint32_t* classCnt = B.counters + kClassBase + depth * kShadeClasses;
-  const bool lastDepth = S.maxDepth >= 0 && depth + 1 >= S.maxDepth;
   const uint32_t lane = threadIdx.x & 31u;
   uint32_t nN = 0, nP = 0;
   bool live = false, done = false, drained = false;
-  uint32_t p = 0;
+  uint32_t p = 0, jb = 0;
   RayPre r;
   TraceHit h;
   TravState st;
@@ -140,11 +178,12 @@ __global__ void __launch_bounds__(kBlock, 8)
         uint32_t i = base + __popc(need & ((1u << lane) - 1u));
         if (i < count) {
           p = qin[i];
+          if (MIX) jb = B.job[p];
           float4 o = B.rayO[p], d = B.rayD[p];
           r = MakeRayPre(V3{o.x, o.y, o.z}, V3{d.x, d.y, d.z}, o.w);
           TraceInit(d.w, h, st);
           live = true;
-          done = S.nNodes == 0;
+          done = SceneOf<MIX>(S0, B, jb).nNodes == 0;
         }
       }
     }
@@ -159,12 +198,14 @@ __global__ void __launch_bounds__(kBlock, 8)
       if (nb < minBusy || nb == 0) break;
       const bool leafPhase = 8 * __popc(__ballot_sync(0xffffffffu, pend)) >= leafFrac8 * nb;
       if (busy && pend == leafPhase)
-        done = TravStep<false, COUNT>(S, r, h, stack, st, err, &nN, &nP) != kTravContinue;
+        done = TravStep<false, COUNT>(SceneOf<MIX>(S0, B, jb), r, h, stack, st, err, &nN, &nP) != kTravContinue;
     }
     // ---- finished lanes: hit record and shade-class append
     const bool fin = live && done;
     uint32_t cls = 0xffu;
     if (fin) {
+      const DevScene& S = SceneOf<MIX>(S0, B, jb);
+      const bool lastDepth = S.maxDepth >= 0 && depth + 1 >= S.maxDepth;
       HitRec hr;
       hr.t = h.t;
       hr.u = h.u;
@@ -264,8 +305,8 @@ __device__ __forceinline__ bool GuidedScatter(const DevScene& S, const PathBuffe
 // SC_EMIT: misses, emitter hits, shapes without a BSDF and the last bounce --
 // emitter MIS only, then the path ends. Other classes: hits on a non-emitter
 // shape with a BSDF of that class -- NEE, BSDF sample, Russian roulette.
-template <int K, bool GUIDED>
-__global__ void __launch_bounds__(kBlock) KShadeClass(DevScene S, PathBuffers B, GuideDev G, int depth) {
+template <int K, bool GUIDED, bool MIX>
+__global__ void __launch_bounds__(kBlock) KShadeClass(DevScene S0, PathBuffers B, GuideDev G, int depth) {
   uint32_t count = B.counters[kClassBase + depth * kShadeClasses + K];
   const uint32_t* qin = B.classQ + (size_t)K * B.capacity;
   uint32_t* qout = B.q[(depth + 1) & 1];
@@ -280,6 +321,7 @@ __global__ void __launch_bounds__(kBlock) KShadeClass(DevScene S, PathBuffers B,
     float4 shO = make_float4(0, 0, 0, 0), shD = shO, shC = shO;
     if (active) {
       p = qin[i];
+      const DevScene& S = SceneOf<MIX>(S0, B, MIX ? B.job[p] : 0u);
       HitRec h = B.hit[p];
       float4 ro = B.rayO[p], rd = B.rayD[p];
       V3 O{ro.x, ro.y, ro.z}, D{rd.x, rd.y, rd.z};
@@ -472,16 +514,16 @@ __global__ void __launch_bounds__(kBlock) KShadeAO(DevScene S, PathBuffers B) {
   }
 }
 
-template <bool COUNT>
+template <bool COUNT, bool MIX>
 __global__ void __launch_bounds__(kBlock, 8)
-    KShadow(DevScene S, PathBuffers B, int depth, unsigned long long* trav, int refillBusy, int leafFrac8) {
+    KShadow(DevScene S0, PathBuffers B, int depth, unsigned long long* trav, int refillBusy, int leafFrac8) {
   const uint32_t count = B.counters[kShadowBase + depth];
   uint32_t* fetch = B.counters + kFetchBase + 2 * depth + 1;
   uint32_t* err = B.counters + kMiscBase + 1;
   const uint32_t lane = threadIdx.x & 31u;
   uint32_t nN = 0, nP = 0;
   bool live = false, done = false, drained = false, occ = false;
-  uint32_t i = 0;
+  uint32_t i = 0, jb = 0;
   RayPre r;
   TraceHit h;
   TravState st;
@@ -499,10 +541,11 @@ __global__ void __launch_bounds__(kBlock, 8)
         if (k < count) {
           i = k;
           float4 o = B.shO[i], d = B.shD[i];
+          if (MIX) jb = B.job[__float_as_uint(d.w)];
           r = MakeRayPre(V3{o.x, o.y, o.z}, V3{d.x, d.y, d.z}, 0.f);
           TraceInit(o.w, h, st);
           live = true;
-          done = S.nNodes == 0;
+          done = SceneOf<MIX>(S0, B, jb).nNodes == 0;
           occ = false;
         }
       }
@@ -515,7 +558,7 @@ __global__ void __launch_bounds__(kBlock, 8)
       if (nb < minBusy || nb == 0) break;
       const bool leafPhase = 8 * __popc(__ballot_sync(0xffffffffu, pend)) >= leafFrac8 * nb;
       if (busy && pend == leafPhase) {
-        int res = TravStep<true, COUNT>(S, r, h, stack, st, err, &nN, &nP);
+        int res = TravStep<true, COUNT>(SceneOf<MIX>(S0, B, jb), r, h, stack, st, err, &nN, &nP);
         if (res != kTravContinue) {
           done = true;
           occ = res == kTravDone && h.prim != kNoPrim;
@@ -588,6 +631,55 @@ __global__ void __launch_bounds__(256)
   if (nbad && (threadIdx.x & 31u) == 0 && film.stats) atomicAdd(film.stats + 2, (unsigned long long)nbad);
 }
 
+// Mixed wave: one thread per (job, pixel) of the wave adds that pixel's spw
+// samples, in sample order, into its job's film, with KAccumulate's
+// invalid-sample rule. Samples and invalid samples are counted per job; the
+// wave's rays are apportioned to its jobs by their shares of its paths.
+__global__ void __launch_bounds__(256)
+    KAccumulateMix(PathBuffers B, uint32_t totalPix, uint32_t total, uint32_t nJobs) {
+  const uint32_t t = blockIdx.x * blockDim.x + threadIdx.x;
+  if (t == 0) {
+    unsigned long long cl = 0, sh = 0;
+    for (int k = 0; k <= kMaxBounce; k++) {
+      cl += B.counters[k];
+      sh += B.counters[kShadowBase + k];
+    }
+    for (uint32_t k = 0; k < nJobs; k++) {
+      unsigned long long* st = B.mix[k].stats;
+      const unsigned long long c = B.mix[k].count;
+      if (!st) continue;
+      st[0] += cl * c / total;
+      st[1] += sh * c / total;
+      st[3] += c;
+    }
+  }
+  if (t >= totalPix) return;
+  uint32_t k = 0, base = 0;
+  while (k + 1u < nJobs && t >= base + B.mix[k].npc) {
+    base += B.mix[k].npc;
+    k++;
+  }
+  const MixJob& J = B.mix[k];
+  const uint32_t j = t - base;
+  float4* px = J.film + (J.pixelBegin + j);
+  float4 a = *px;
+  uint32_t nbad = 0;
+  for (uint32_t s = 0; s < J.spw; s++) {
+    float4 l = B.L[J.pathBegin + s * J.npc + j];
+    bool bad = isnan(l.x) || isnan(l.y) || isnan(l.z) || isinf(l.x) || l.x < 0.f;
+    if (!bad) {
+      a.x += l.x;
+      a.y += l.y;
+      a.z += l.z;
+    } else {
+      nbad++;
+    }
+    a.w += 1.f;
+  }
+  *px = a;
+  if (nbad && J.stats) atomicAdd(J.stats + 2, (unsigned long long)nbad);
+}
+
 __global__ void KGatherRadiance(PathBuffers B, uint32_t count, float* out) {
   uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= count) return;
@@ -614,28 +706,39 @@ cudaError_t LaunchGenerate(const DevScene& S, const PathBuffers& B, const WavePa
   return cudaGetLastError();
 }
 cudaError_t LaunchExtend(const DevScene& S, const PathBuffers& B, int depth, int grid, cudaStream_t st,
-                         unsigned long long* trav, int refillBusy, int leafFrac8) {
-  if (trav)
-    KExtend<true><<<grid, kBlock, 0, st>>>(S, B, depth, trav, refillBusy, leafFrac8);
+                         unsigned long long* trav, int refillBusy, int leafFrac8, bool mix) {
+  if (mix)
+    KExtend<false, true><<<grid, kBlock, 0, st>>>(S, B, depth, nullptr, refillBusy, leafFrac8);
+  else if (trav)
+    KExtend<true, false><<<grid, kBlock, 0, st>>>(S, B, depth, trav, refillBusy, leafFrac8);
   else
-    KExtend<false><<<grid, kBlock, 0, st>>>(S, B, depth, nullptr, refillBusy, leafFrac8);
+    KExtend<false, false><<<grid, kBlock, 0, st>>>(S, B, depth, nullptr, refillBusy, leafFrac8);
   return cudaGetLastError();
 }
 cudaError_t LaunchShade(const DevScene& S, const PathBuffers& B, int depth, int grid, cudaStream_t st,
-                        const GuideDev* G) {
+                        const GuideDev* G, bool mix) {
   GuideDev none{};
-  KShadeClass<SC_EMIT, false><<<grid, kBlock, 0, st>>>(S, B, none, depth);
-  KShadeClass<SC_GLASS, false><<<grid, kBlock, 0, st>>>(S, B, none, depth);
+  if (mix) {  // mixed waves hold plain jobs only
+    KShadeClass<SC_EMIT, false, true><<<grid, kBlock, 0, st>>>(S, B, none, depth);
+    KShadeClass<SC_GLASS, false, true><<<grid, kBlock, 0, st>>>(S, B, none, depth);
+    KShadeClass<SC_DIFFUSE, false, true><<<grid, kBlock, 0, st>>>(S, B, none, depth);
+    KShadeClass<SC_METAL, false, true><<<grid, kBlock, 0, st>>>(S, B, none, depth);
+    KShadeClass<SC_DISNEY, false, true><<<grid, kBlock, 0, st>>>(S, B, none, depth);
+    KShadeClass<SC_GENERIC, false, true><<<grid, kBlock, 0, st>>>(S, B, none, depth);
+    return cudaGetLastError();
+  }
+  KShadeClass<SC_EMIT, false, false><<<grid, kBlock, 0, st>>>(S, B, none, depth);
+  KShadeClass<SC_GLASS, false, false><<<grid, kBlock, 0, st>>>(S, B, none, depth);
   if (G) {
-    KShadeClass<SC_DIFFUSE, true><<<grid, kBlock, 0, st>>>(S, B, *G, depth);
-    KShadeClass<SC_METAL, true><<<grid, kBlock, 0, st>>>(S, B, *G, depth);
-    KShadeClass<SC_DISNEY, true><<<grid, kBlock, 0, st>>>(S, B, *G, depth);
-    KShadeClass<SC_GENERIC, true><<<grid, kBlock, 0, st>>>(S, B, *G, depth);
+    KShadeClass<SC_DIFFUSE, true, false><<<grid, kBlock, 0, st>>>(S, B, *G, depth);
+    KShadeClass<SC_METAL, true, false><<<grid, kBlock, 0, st>>>(S, B, *G, depth);
+    KShadeClass<SC_DISNEY, true, false><<<grid, kBlock, 0, st>>>(S, B, *G, depth);
+    KShadeClass<SC_GENERIC, true, false><<<grid, kBlock, 0, st>>>(S, B, *G, depth);
   } else {
-    KShadeClass<SC_DIFFUSE, false><<<grid, kBlock, 0, st>>>(S, B, none, depth);
-    KShadeClass<SC_METAL, false><<<grid, kBlock, 0, st>>>(S, B, none, depth);
-    KShadeClass<SC_DISNEY, false><<<grid, kBlock, 0, st>>>(S, B, none, depth);
-    KShadeClass<SC_GENERIC, false><<<grid, kBlock, 0, st>>>(S, B, none, depth);
+    KShadeClass<SC_DIFFUSE, false, false><<<grid, kBlock, 0, st>>>(S, B, none, depth);
+    KShadeClass<SC_METAL, false, false><<<grid, kBlock, 0, st>>>(S, B, none, depth);
+    KShadeClass<SC_DISNEY, false, false><<<grid, kBlock, 0, st>>>(S, B, none, depth);
+    KShadeClass<SC_GENERIC, false, false><<<grid, kBlock, 0, st>>>(S, B, none, depth);
   }
   return cudaGetLastError();
 }
@@ -644,11 +747,13 @@ cudaError_t LaunchShadeAO(const DevScene& S, const PathBuffers& B, int grid, cud
   return cudaGetLastError();
 }
 cudaError_t LaunchShadow(const DevScene& S, const PathBuffers& B, int depth, int grid, cudaStream_t st,
-                         unsigned long long* trav, int refillBusy, int leafFrac8) {
-  if (trav)
-    KShadow<true><<<grid, kBlock, 0, st>>>(S, B, depth, trav, refillBusy, leafFrac8);
+                         unsigned long long* trav, int refillBusy, int leafFrac8, bool mix) {
+  if (mix)
+    KShadow<false, true><<<grid, kBlock, 0, st>>>(S, B, depth, nullptr, refillBusy, leafFrac8);
+  else if (trav)
+    KShadow<true, false><<<grid, kBlock, 0, st>>>(S, B, depth, trav, refillBusy, leafFrac8);
   else
-    KShadow<false><<<grid, kBlock, 0, st>>>(S, B, depth, nullptr, refillBusy, leafFrac8);
+    KShadow<false, false><<<grid, kBlock, 0, st>>>(S, B, depth, nullptr, refillBusy, leafFrac8);
   return cudaGetLastError();
 }
 cudaError_t LaunchAccumulate(const PathBuffers& B, const FilmView& film, uint32_t count, cudaStream_t st,
@@ -657,6 +762,17 @@ cudaError_t LaunchAccumulate(const PathBuffers& B, const FilmView& film, uint32_
   if (spw < 1u) spw = 1u;
   uint32_t npc = count / spw;
   KAccumulate<<<(npc + 255) / 256, 256, 0, st>>>(B, film, count, ctx, spw);
+  return cudaGetLastError();
+}
+cudaError_t LaunchGenerateMix(const PathBuffers& B, uint32_t total, uint32_t nJobs, cudaStream_t st) {
+  uint32_t n = total > (uint32_t)kCounterWords ? total : (uint32_t)kCounterWords;
+  KGenerateMix<<<(n + kBlock - 1) / kBlock, kBlock, 0, st>>>(B, total, nJobs);
+  return cudaGetLastError();
+}
+cudaError_t LaunchAccumulateMix(const PathBuffers& B, uint32_t totalPixels, uint32_t total, uint32_t nJobs,
+                                cudaStream_t st) {
+  if (totalPixels == 0) return cudaSuccess;
+  KAccumulateMix<<<(totalPixels + 255) / 256, 256, 0, st>>>(B, totalPixels, total, nJobs);
   return cudaGetLastError();
 }
 cudaError_t LaunchGatherRadiance(const PathBuffers& B, uint32_t count, float* out, cudaStream_t st) {

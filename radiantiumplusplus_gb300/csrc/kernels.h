@@ -9,6 +9,8 @@
 
 namespace rad {
 
+struct MixJob;
+
 // Wavefront path state, structure of arrays, one slot per path in flight.
 struct PathBuffers {
   float4* rayO;    // origin xyz, tmin
@@ -28,6 +30,22 @@ struct PathBuffers {
                        // [kClassBase + depth * kShadeClasses + class]: shade-class counts
   uint32_t capacity;
   float4* guideRec;    // guide training records (shadow stage adds NEE into them), or null
+  // mixed waves: the job (index into `mix`) of each path slot, and the wave's job table
+  uint8_t* job;
+  const MixJob* mix;
+};
+
+// One job's share of a mixed wave (several jobs' paths in one launch of each
+// stage). Its paths occupy slots [pathBegin, pathBegin + count): spw
+// consecutive samples (from `sample`) of the npc pixels [pixelBegin,
+// pixelBegin + npc), path pathBegin + s * npc + j being pixel pixelBegin + j,
+// sample sample + s -- the layout of a one-job wave.
+constexpr int kMaxMix = 16;
+struct MixJob {
+  DevScene S;
+  float4* film;
+  unsigned long long* stats;
+  uint32_t pathBegin, count, pixelBegin, npc, spw, sample, seed, pad;
 };
 
 constexpr int kMaxBounce = 256;
@@ -117,10 +135,15 @@ struct TraceTune {
 };
 // trav (optional, 4 x u64): extend node visits, extend prim tests, shadow node visits, shadow prim tests
 cudaError_t LaunchExtend(const DevScene& S, const PathBuffers& B, int depth, int grid, cudaStream_t st,
-                         unsigned long long* trav = nullptr, int refillBusy = 20, int leafFrac8 = 4);
+                         unsigned long long* trav = nullptr, int refillBusy = 20, int leafFrac8 = 4, bool mix = false);
 // G (optional): guide network; its classes then sample the one-sample MIS mixture.
 cudaError_t LaunchShade(const DevScene& S, const PathBuffers& B, int depth, int grid, cudaStream_t st,
-                        const GuideDev* G = nullptr);
+                        const GuideDev* G = nullptr, bool mix = false);
+// Mixed waves: generate (w.count = paths of all jobs, w.spw = number of jobs in
+// B.mix) and accumulate (into each job's film, in sample order per pixel).
+cudaError_t LaunchGenerateMix(const PathBuffers& B, uint32_t total, uint32_t nJobs, cudaStream_t st);
+cudaError_t LaunchAccumulateMix(const PathBuffers& B, uint32_t totalPixels, uint32_t total, uint32_t nJobs,
+                                cudaStream_t st);
 // renderer "particle_tracer": light paths [first, first + count), splatted into `film`
 struct ParticleParams {
   uint64_t first, count;
@@ -190,7 +213,7 @@ cudaError_t LaunchParticleBounce(const DevScene& S, const PathBuffers& B, int d,
 // renderer "ao": for every path of bounce 0 with a hit, one cosine-sampled visibility ray
 cudaError_t LaunchShadeAO(const DevScene& S, const PathBuffers& B, int grid, cudaStream_t st);
 cudaError_t LaunchShadow(const DevScene& S, const PathBuffers& B, int depth, int grid, cudaStream_t st,
-                         unsigned long long* trav = nullptr, int refillBusy = 20, int leafFrac8 = 4);
+                         unsigned long long* trav = nullptr, int refillBusy = 20, int leafFrac8 = 4, bool mix = false);
 // spw: samples per wave of the generate stage (per pixel, in sample order, as
 // spw one-sample waves would add them).
 cudaError_t LaunchAccumulate(const PathBuffers& B, const FilmView& film, uint32_t count, cudaStream_t st,

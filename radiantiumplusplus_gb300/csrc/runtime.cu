@@ -155,6 +155,7 @@ struct rad_job {
   std::vector<int> profKind;
   uint32_t trainSamples = 0;  // guided jobs train during their first trainSamples samples
   uint32_t spw = 0;           // samples per wave (0 = not chosen yet; see WaveSamples)
+  uint32_t mixCursor = 0;     // mixed waves: next pixel of the current sample (0: at a sample boundary)
   // CUDA graph per pixel chunk: one captured wave replayed once per sample
   WaveCtx* ctx = nullptr;  // device, one per chunk
   bool ctxStale = false;   // graphs taken over from an earlier job: contexts not yet written
@@ -165,6 +166,11 @@ struct rad_job {
 };
 
 namespace {
+
+// Waves the worker may have queued on the stream ahead of the GPU (see WorkerMain),
+// and the mixed-wave job tables kept for them.
+constexpr size_t kMaxWavesInFlight = 3;
+constexpr int kMixRing = (int)kMaxWavesInFlight + 1;
 
 struct Lib {
   bool inited = false;
@@ -182,6 +188,11 @@ struct Lib {
   std::vector<void*> pathAllocs;
   uint64_t pathBytes = 0;
   uint32_t* hCounters = nullptr;  // pinned
+  // mixed waves: a ring of job tables (device, with pinned staging), one per wave in flight
+  bool mixJobs = true;
+  MixJob* mixDev = nullptr;
+  MixJob* mixHost = nullptr;
+  uint32_t mixSlot = 0;
   std::mutex gpuMu;
   // serving loop
   std::thread worker;
@@ -244,9 +255,13 @@ void AllocPaths(Lib& lib) {
   B.shC = DevAlloc<float4>(P, o, b);
   B.classQ = DevAlloc<uint32_t>((size_t)P * kShadeClasses, o, b);
   B.counters = DevAlloc<uint32_t>(kCounterWords, o, b);
+  B.job = DevAlloc<uint8_t>(P, o, b);
+  B.mix = nullptr;
+  lib.mixDev = DevAlloc<MixJob>((size_t)kMixRing * kMaxMix, o, b);
   Check(cudaMemset(B.counters, 0, kCounterWords * sizeof(uint32_t)), "cudaMemset");
   B.capacity = P;
   Check(cudaMallocHost(&lib.hCounters, kCounterWords * sizeof(uint32_t)), "cudaMallocHost");
+  Check(cudaMallocHost(&lib.mixHost, (size_t)kMixRing * kMaxMix * sizeof(MixJob)), "cudaMallocHost");
   lib.used += b;
 }
 
@@ -259,6 +274,7 @@ void InitLocked(const char* cfg) {
     if (cfg && *cfg) {
       JValue c = JsonReader::Parse(cfg);
       if (const JValue* v = c.get("budget_bytes")) lib.budget = (uint64_t)v->n;
+      if (const JValue* v = c.get("mix_jobs")) lib.mixJobs = v->n != 0;
     }
     return;
   }
@@ -267,6 +283,7 @@ void InitLocked(const char* cfg) {
     if (const JValue* v = c.get("device")) lib.device = (int)v->n;
     if (const JValue* v = c.get("budget_bytes")) lib.budget = (uint64_t)v->n;
     if (const JValue* v = c.get("max_paths")) lib.maxPaths = (uint32_t)v->n;
+    if (const JValue* v = c.get("mix_jobs")) lib.mixJobs = v->n != 0;
   }
   if (lib.maxPaths < 1024) lib.maxPaths = 1024;
   int n = 0;
@@ -627,15 +644,18 @@ void RunWaveGraph(rad_job* j) {
       c.sample = j->first + j->nextSample;
       c.seed = j->seed;
     }
-    Check(cudaMemcpy(j->ctx, host.data(), nChunks * sizeof(WaveCtx), cudaMemcpyHostToDevice), "ctx upload");
+    // stream-ordered: an earlier wave of this job may still be reading the context
+    Check(cudaMemcpyAsync(j->ctx, host.data(), nChunks * sizeof(WaveCtx), cudaMemcpyHostToDevice, lib.stream),
+          "ctx upload");
   };
-  if (j->ctxStale) {
+  if (j->ctxStale && !j->graphs.empty()) {
     uploadCtx();
     j->ctxStale = false;
   }
   if (j->graphs.empty()) {
     Check(cudaMalloc(&j->ctx, nChunks * sizeof(WaveCtx)), "cudaMalloc");
     uploadCtx();
+    j->ctxStale = false;
     ProfSink none{nullptr};
     FilmView film{j->accum, (int32_t)W, (int32_t)H, j->dStats};
     for (size_t c = 0; c < nChunks; c++) {
@@ -740,6 +760,110 @@ void RunWaveBdpt(rad_job* j) {
   }
   j->nextSample += k;
   j->launched += npix * k;
+}
+
+// Jobs whose waves can share launches with other jobs' (mixed waves): plain
+// `path` jobs of bounded depth, without guiding, profiling or traversal counts.
+bool Mixable(const rad_job* j) {
+  const DevScene& S = j->scene->dev;
+  return !S.isVol && !S.isAO && !S.isParticle && !S.isBdpt && S.maxDepth >= 0 &&
+         !(j->flags & (RAD_JOB_GUIDE | RAD_JOB_PROFILE_KERNELS | RAD_JOB_COUNT_TRAVERSAL));
+}
+
+// One wave holding paths of several jobs (of any scenes): the path slots are
+// split evenly between the jobs (processor sharing), and a share a job cannot
+// use goes to the others. A job whose share covers its frame takes whole
+// samples (as many consecutive ones as fit); otherwise it takes the next pixel
+// chunk of its current sample, so each pixel still receives its samples in
+// order and the film is the same as when the job runs alone. Every stage is one
+// launch over all jobs' paths; each path finds its scene, film, pixels and
+// stream through the wave's job table.
+void RunMixedWave(const std::vector<rad_job*>& js) {
+  Lib& lib = L();
+  const uint64_t P = lib.maxPaths;
+  const size_t m = js.size();
+  std::vector<uint64_t> need(m), give(m, 0);
+  for (size_t i = 0; i < m; i++) {
+    const DevScene& S = js[i]->scene->dev;
+    const uint64_t npix = (uint64_t)S.cam.width * S.cam.height;
+    need[i] = (uint64_t)(js[i]->spp - js[i]->nextSample) * npix - js[i]->mixCursor;
+  }
+  uint64_t left = P;
+  for (int pass = 0; pass < 3 && left > 0; pass++) {
+    size_t open = 0;
+    for (size_t i = 0; i < m; i++) open += give[i] < need[i] ? 1 : 0;
+    if (open == 0) break;
+    const uint64_t share = std::max<uint64_t>(1, left / open);
+    for (size_t i = 0; i < m && left > 0; i++) {
+      if (give[i] >= need[i]) continue;
+      uint64_t g = std::min(std::min(share, need[i] - give[i]), left);
+      give[i] += g;
+      left -= g;
+    }
+  }
+  MixJob* tab = lib.mixHost + (size_t)lib.mixSlot * kMaxMix;
+  MixJob* dtab = lib.mixDev + (size_t)lib.mixSlot * kMaxMix;
+  lib.mixSlot = (lib.mixSlot + 1) % kMixRing;
+  uint32_t n = 0, pathBegin = 0, totalPix = 0;
+  int maxDepth = 1;
+  for (size_t i = 0; i < m; i++) {
+    if (give[i] == 0) continue;
+    rad_job* j = js[i];
+    const DevScene& S = j->scene->dev;
+    const uint32_t npix = (uint32_t)S.cam.width * (uint32_t)S.cam.height;
+    MixJob& J = tab[n++];
+    J = MixJob{};
+    J.S = S;
+    J.film = j->accum;
+    J.stats = j->dStats;
+    J.seed = j->seed;
+    J.sample = j->first + j->nextSample;
+    if (j->mixCursor == 0 && give[i] >= npix) {
+      J.pixelBegin = 0;
+      J.npc = npix;
+      J.spw = (uint32_t)std::min<uint64_t>(give[i] / npix, j->spp - j->nextSample);
+      j->nextSample += J.spw;
+    } else {
+      J.pixelBegin = j->mixCursor;
+      J.npc = (uint32_t)std::min<uint64_t>(give[i], npix - j->mixCursor);
+      J.spw = 1;
+      j->mixCursor += J.npc;
+      if (j->mixCursor == npix) {
+        j->mixCursor = 0;
+        j->nextSample++;
+      }
+    }
+    J.count = J.npc * J.spw;
+    J.pathBegin = pathBegin;
+    pathBegin += J.count;
+    totalPix += J.npc;
+    j->launched += J.count;
+    j->ctxStale = true;  // its graph waves, if any, must re-read the sample index
+    maxDepth = std::max(maxDepth, S.maxDepth);
+  }
+  if (n == 0) return;
+  Check(cudaMemcpyAsync(dtab, tab, n * sizeof(MixJob), cudaMemcpyHostToDevice, lib.stream), "job table");
+  PathBuffers B = lib.paths;
+  B.mix = dtab;
+  const uint32_t count = pathBegin;
+  const TraceTune& tu = js[0]->scene->tune;
+  const DevScene& S0 = tab[0].S;  // not read by the mixed kernels; launch argument only
+  int grid = std::max(1, std::min(lib.sms * 8, (int)((count + 127) / 128)));
+  int tgrid = std::max(1, std::min(lib.sms * tu.blocksPerSm, (int)((count + 127) / 128)));
+  const int iters = std::min(maxDepth, kMaxBounce);
+  Check(LaunchGenerateMix(B, count, n, lib.stream), "generate");
+  for (int d = 0; d < iters; d++) {
+    Check(LaunchExtend(S0, B, d, tgrid, lib.stream, nullptr, tu.refillBusy, tu.leafFrac8, true), "extend");
+    Check(LaunchShade(S0, B, d, grid, lib.stream, nullptr, true), "shade");
+    Check(LaunchShadow(S0, B, d, tgrid, lib.stream, nullptr, tu.refillBusy, tu.leafFrac8, true), "shadow");
+  }
+  Check(LaunchAccumulateMix(B, totalPix, count, n, lib.stream), "accumulate");
+  const uint64_t launches = 2 + (uint64_t)iters * (2 + kShadeClasses);
+  for (size_t i = 0; i < m; i++)
+    if (give[i] > 0) {
+      js[i]->stats.kernel_launches += launches;
+      if (n > 1) js[i]->stats.mixed_waves++;
+    }
 }
 
 // Runs wave(s) for the job's next sample index over all its pixels.
@@ -960,11 +1084,10 @@ void EndJobLaunch(rad_job* j) {
   j->state = kCompleting;
 }
 
-// Waves the worker may have queued on the stream ahead of the GPU. Bounding
-// the run-ahead keeps scheduling decisions late: a job that arrives (or is
-// cancelled) meanwhile waits at most this many waves, instead of behind every
-// wave already enqueued.
-constexpr size_t kMaxWavesInFlight = 3;
+// The worker keeps at most kMaxWavesInFlight waves queued on the stream ahead
+// of the GPU. Bounding the run-ahead keeps scheduling decisions late: a job
+// that arrives (or is cancelled) meanwhile waits at most this many waves,
+// instead of behind every wave already enqueued.
 
 void WorkerMain() {
   Lib& lib = L();
@@ -986,6 +1109,7 @@ void WorkerMain() {
       inflight.pop_front();
     }
     rad_job* j = nullptr;
+    std::vector<rad_job*> group;  // jobs of the next mixed wave
     bool reclaim = false;  // a pending job waits for memory that parked films hold
     {
       std::unique_lock<std::mutex> lk(lib.qmu);
@@ -1022,18 +1146,67 @@ void WorkerMain() {
         continue;
       }
       if (!lib.running.empty()) {
-        // least attained service: the running job with the fewest samples
-        // launched goes next (processor sharing by samples, so a small job is
-        // not held behind the waves of a large one); ties go to the earlier job
-        j = lib.running[0];
-        for (rad_job* c : lib.running)
-          if (c->launched.load() < j->launched.load()) j = c;
+        // Plain `path` jobs share mixed waves once two of them run (or one has
+        // a sample left half done by one); the other jobs keep waves of their
+        // own. Between those and the mix group (counted by its least-served
+        // member), least attained service decides: the fewest samples
+        // launched goes next, ties to the earlier job.
+        std::vector<rad_job*> mixable;
+        if (lib.mixJobs)
+          for (rad_job* c : lib.running)
+            if (Mixable(c) && !c->cancel && c->nextSample < c->spp) mixable.push_back(c);
+        const bool useGroup = mixable.size() >= 2 || (mixable.size() == 1 && mixable[0]->mixCursor != 0);
+        uint64_t best = UINT64_MAX;
+        for (rad_job* c : lib.running) {
+          if (useGroup && std::find(mixable.begin(), mixable.end(), c) != mixable.end()) continue;
+          if (c->launched.load() < best) {
+            best = c->launched.load();
+            j = c;
+          }
+        }
+        if (useGroup) {
+          std::stable_sort(mixable.begin(), mixable.end(),
+                           [](rad_job* a, rad_job* b) { return a->launched.load() < b->launched.load(); });
+          if (!j || mixable[0]->launched.load() <= best) {
+            if (mixable.size() > (size_t)kMaxMix) mixable.resize(kMaxMix);
+            group = mixable;
+            j = nullptr;
+          }
+        }
       }
     }
     if (reclaim) {
       std::lock_guard<std::mutex> g(lib.gpuMu);
       ReleaseSpares();
       continue;  // admission again, with the parked films' memory free
+    }
+    if (!group.empty()) {
+      std::lock_guard<std::mutex> g(lib.gpuMu);
+      try {
+        for (rad_job* c : group)
+          if (!c->accum) StartJob(c);
+        RunMixedWave(group);
+        cudaEvent_t e = GetEvent();
+        Check(cudaEventRecord(e, lib.stream), "event record");
+        inflight.push_back(e);
+        for (rad_job* c : group) {
+          if (c->nextSample >= c->spp && c->mixCursor == 0) {
+            EndJobLaunch(c);
+            std::lock_guard<std::mutex> lk(lib.qmu);
+            lib.running.erase(std::find(lib.running.begin(), lib.running.end(), c));
+            completing.push_back(c);
+          }
+        }
+      } catch (const Error& e) {
+        std::lock_guard<std::mutex> lk(lib.qmu);
+        for (rad_job* c : group) {
+          auto it = std::find(lib.running.begin(), lib.running.end(), c);
+          if (it != lib.running.end()) {
+            lib.running.erase(it);
+            FinishJob(c, e.code, e.msg);
+          }
+        }
+      }
     }
     if (j) {
       std::lock_guard<std::mutex> g(lib.gpuMu);
@@ -1073,7 +1246,7 @@ void WorkerMain() {
         it = completing.erase(it);
       }
     }
-    if (!j && !completing.empty()) std::this_thread::sleep_for(std::chrono::microseconds(50));
+    if (!j && group.empty() && !completing.empty()) std::this_thread::sleep_for(std::chrono::microseconds(50));
   }
   for (cudaEvent_t e : inflight) {
     cudaEventSynchronize(e);
@@ -1239,6 +1412,9 @@ int rad_shutdown(void) {
     lib.bdpt = BdptBuffers{};
     if (lib.hCounters) cudaFreeHost(lib.hCounters);
     lib.hCounters = nullptr;
+    if (lib.mixHost) cudaFreeHost(lib.mixHost);
+    lib.mixHost = nullptr;
+    lib.mixDev = nullptr;
     for (cudaEvent_t e : lib.evPool) cudaEventDestroy(e);
     lib.evPool.clear();
     cudaStreamDestroy(lib.stream);

@@ -206,21 +206,21 @@ void RenderSamples(const DevScene& S, const uint32_t* pix, const uint32_t* smp, 
       default: throw std::runtime_error("the fp16 grid is not emulated");
     }
   } else if (S.isAO) {
-    Grid(1, 1, [&] { KExtend<false>(S, B, 0, nullptr, 1, 4); });
+    Grid(1, 1, [&] { KExtend<false, false>(S, B, 0, nullptr, 1, 4); });
     Grid(1, 1, [&] { KShadeAO(S, B); });
-    Grid(1, 1, [&] { KShadow<false>(S, B, 0, nullptr, 1, 4); });
+    Grid(1, 1, [&] { KShadow<false, false>(S, B, 0, nullptr, 1, 4); });
   } else {
     int iters = S.maxDepth >= 0 ? std::max(1, S.maxDepth) : kMaxBounce;
     if (iters > kMaxBounce) iters = kMaxBounce;
     for (int d = 0; d < iters && B.counters[d] != 0; d++) {
-      Grid(1, 1, [&] { KExtend<false>(S, B, d, nullptr, 1, 4); });
-      Grid(1, 1, [&] { KShadeClass<SC_EMIT, false>(S, B, none, d); });
-      Grid(1, 1, [&] { KShadeClass<SC_GLASS, false>(S, B, none, d); });
-      Grid(1, 1, [&] { KShadeClass<SC_DIFFUSE, false>(S, B, none, d); });
-      Grid(1, 1, [&] { KShadeClass<SC_METAL, false>(S, B, none, d); });
-      Grid(1, 1, [&] { KShadeClass<SC_DISNEY, false>(S, B, none, d); });
-      Grid(1, 1, [&] { KShadeClass<SC_GENERIC, false>(S, B, none, d); });
-      Grid(1, 1, [&] { KShadow<false>(S, B, d, nullptr, 1, 4); });
+      Grid(1, 1, [&] { KExtend<false, false>(S, B, d, nullptr, 1, 4); });
+      Grid(1, 1, [&] { KShadeClass<SC_EMIT, false, false>(S, B, none, d); });
+      Grid(1, 1, [&] { KShadeClass<SC_GLASS, false, false>(S, B, none, d); });
+      Grid(1, 1, [&] { KShadeClass<SC_DIFFUSE, false, false>(S, B, none, d); });
+      Grid(1, 1, [&] { KShadeClass<SC_METAL, false, false>(S, B, none, d); });
+      Grid(1, 1, [&] { KShadeClass<SC_DISNEY, false, false>(S, B, none, d); });
+      Grid(1, 1, [&] { KShadeClass<SC_GENERIC, false, false>(S, B, none, d); });
+      Grid(1, 1, [&] { KShadow<false, false>(S, B, d, nullptr, 1, 4); });
     }
   }
   if (*err) throw std::runtime_error("device-side check fired, code " + std::to_string(*err));

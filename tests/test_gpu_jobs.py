@@ -194,3 +194,86 @@ def test_wait_times_out(rad, scene_dir):
     assert e.value.code == 9
     j.close()
     s.close()
+
+
+def _films_alone(scenes_):
+    return [s.render() for s in scenes_]
+
+
+def test_mixed_waves_equal_alone(rad, scene_dir):
+    """Jobs of different scenes running together share the launches of each
+    wave (mixed waves); every film is bit-identical to the job rendered alone,
+    including a frame larger than its share of a wave (taken in pixel chunks)
+    and a job whose spp is not a multiple of its samples per wave."""
+    from helpers import materials
+    blocker = rad.Scene.from_file(box(scene_dir, 256, 256, 1, seed=21)[0])
+    big = rad.Scene.from_file(box(scene_dir, 1280, 1000, 3, seed=22)[0])
+    small = [rad.Scene.from_file(box(scene_dir, 40, 40, 6)[0]),
+             rad.Scene.from_file(spheres(scene_dir, 300, 4, 48, 32, 5)[0]),
+             rad.Scene.from_file(materials(scene_dir, 24, 56, 7)[0])]
+    alone = _films_alone([big] + small)
+    jb = blocker.submit(spp=20000)  # keeps waves going while the others are submitted
+    jobs = [s.submit() for s in [big] + small]
+    for j in jobs:
+        j.wait()
+    films = [j.film() for j in jobs]
+    mixed = [j.stats()["mixed_waves"] for j in jobs]
+    jb.cancel()
+    with pytest.raises(rad.RadError):
+        jb.wait()
+    jb.close()
+    for k, (f, a) in enumerate(zip(films, alone)):
+        assert np.array_equal(f, a), k
+    assert min(mixed) > 0, mixed
+    st = jobs[0].stats()
+    assert st["samples"] == 1280 * 1000 * 3
+    for j in jobs:
+        j.close()
+    for s in [blocker, big] + small:
+        s.close()
+
+
+def test_mixed_waves_more_jobs_than_a_wave_holds(rad, scene_dir):
+    """More running jobs than one wave's job table (16): every job still runs
+    to completion and equals its film alone."""
+    blocker = rad.Scene.from_file(box(scene_dir, 256, 256, 1, seed=31)[0])
+    ss = [rad.Scene.from_file(box(scene_dir, 16 + 2 * k, 24, 3 + k % 4, seed=40 + k)[0]) for k in range(20)]
+    alone = _films_alone(ss)
+    jb = blocker.submit(spp=20000)
+    jobs = [s.submit() for s in ss]
+    for j in jobs:
+        j.wait()
+    for j, a in zip(jobs, alone):
+        assert np.array_equal(j.film(), a)
+        j.close()
+    jb.cancel()
+    with pytest.raises(rad.RadError):
+        jb.wait()
+    jb.close()
+    for s in [blocker] + ss:
+        s.close()
+
+
+def test_mixing_can_be_switched_off(rad, scene_dir):
+    """rad_init {"mix_jobs": 0}: jobs take turns wave by wave instead; same films."""
+    a = rad.Scene.from_file(box(scene_dir, 32, 32, 4, seed=51)[0])
+    b = rad.Scene.from_file(box(scene_dir, 48, 16, 4, seed=52)[0])
+    alone = _films_alone([a, b])
+    blocker = rad.Scene.from_file(box(scene_dir, 256, 256, 1, seed=53)[0])
+    try:
+        rad.init({"mix_jobs": 0})
+        jb = blocker.submit(spp=20000)
+        ja, jbb = a.submit(), b.submit()
+        ja.wait()
+        jbb.wait()
+        assert ja.stats()["mixed_waves"] == 0 and jbb.stats()["mixed_waves"] == 0
+        assert np.array_equal(ja.film(), alone[0]) and np.array_equal(jbb.film(), alone[1])
+        jb.cancel()
+        with pytest.raises(rad.RadError):
+            jb.wait()
+        for j in (ja, jbb, jb):
+            j.close()
+    finally:
+        rad.init({"mix_jobs": 1})
+    for s in (a, b, blocker):
+        s.close()
