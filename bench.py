@@ -553,8 +553,25 @@ def run_guided(args, world, rank, local):
     print(json.dumps(line), flush=True)
 
 
+def _serving_pool(rng, n_scenes):
+    """Resident scenes of the serving mix: many-spheres scenes with sphere counts
+    lognormal between 32 and 10,000 (10 k - 3.2 M triangles), frames cycling
+    through 256^2, 512^2, 1280x720 and 1920x1080, depth uniform in 8..16."""
+    import numpy as np
+    res = [(256, 256), (512, 512), (1280, 720), (1920, 1080)]
+    pool = []
+    for k in range(n_scenes):
+        n = int(np.clip(np.exp(rng.normal(np.log(600.0), 1.3)), 32, 10000))
+        w, h = res[k % 4]
+        pool.append((n, w, h, int(rng.integers(8, 17))))
+    return pool
+
+
 def run_serving(args, world, rank, local):
-    """Serving loop: Poisson arrivals of jobs over a pool of resident scenes; throughput and p50/p99 latency."""
+    """Serving loop (continuous batching): Poisson arrivals of jobs over resident
+    scenes, offered at fractions of the measured peak throughput; per load, the
+    throughput and the p50 / p99 of job latency (submit to completion) and of
+    stretch (latency / the job's time alone on the GPU)."""
     import numpy as np
     import torch
     import radiantiumplusplus_gb300 as rad
@@ -562,8 +579,7 @@ def run_serving(args, world, rank, local):
     torch.cuda.set_device(local)
     rad.init({"device": local})
     rng = np.random.default_rng(4)
-    pool = [(30, 256, 256, 8), (100, 512, 512, 10), (300, 1280, 720, 12), (1000, 256, 256, 14),
-            (3000, 512, 512, 16), (10000, 1920, 1080, 16)]
+    pool = _serving_pool(rng, args.serving_scenes)
     with tempfile.TemporaryDirectory(prefix="rad_bench_srv_") as tmp:
         loaded = []
         for k, (n, w, h, depth) in enumerate(pool):
@@ -571,54 +587,100 @@ def run_serving(args, world, rank, local):
                                              seed=40 + k, extent=100.0 * (n / 10000.0) ** (1 / 3))
             path = scenes.write_scene(os.path.join(tmp, "s%d" % k), sc, assets)
             loaded.append(rad.Scene.from_file(path))
-        # service rate of each scene alone (samples/s) from one 2-spp job
-        alone = []
+        # each scene alone: samples/s of a job of ~40 M samples (device-timed), and the
+        # fixed cost of a job through the API (latency of 1-spp jobs minus their GPU time)
+        alone, fixed_ms = [], []
         for sc in loaded:
-            j = sc.submit(spp=2)
+            spp = max(1, int(4e7 / (sc.width * sc.height)))
+            j = sc.submit(spp=spp)
             j.wait()
             st = j.stats()
             j.close()
             alone.append(st["samples"] / max(1e-6, st["gpu_ms"] / 1000.0))
-        results = []
-        for lam in args.rates:
-            n_jobs = max(4, int(lam * args.duration))
-            arrivals = np.cumsum(rng.exponential(1.0 / lam, n_jobs))
-            picks = rng.integers(0, len(loaded), n_jobs)
-            spps = np.exp(rng.uniform(np.log(args.spp_min), np.log(args.spp_max), n_jobs)).astype(int)
-            jobs = []
+            lat1 = []
+            for _ in range(5):
+                j = sc.submit(spp=1)
+                j.wait()
+                st = j.stats()
+                j.close()
+                lat1.append(st["queue_ms"] + st["wall_ms"] - 1000.0 * st["samples"] / alone[-1])
+            fixed_ms.append(max(0.0, float(np.median(lat1))))
+
+        def draw(n, r):
+            picks = r.integers(0, len(loaded), n)
+            spps = np.exp(r.uniform(np.log(args.spp_min), np.log(args.spp_max), n)).astype(int)
+            return picks, spps
+
+        # mean samples per job of the distribution: mean frame x mean of log-uniform spp
+        lo, hi = float(args.spp_min), float(args.spp_max)
+        mean_spp = (hi - lo) / np.log(hi / lo) if hi > lo else lo
+        mean_samples = float(np.mean([sc.width * sc.height for sc in loaded])) * mean_spp
+
+        def run(jobs_spec, arrivals):
+            submitted = []
             t0 = time.perf_counter()
-            for a, k, spp in zip(arrivals, picks, spps):
+            for a, (k, spp) in zip(arrivals, jobs_spec):
                 delay = t0 + a - time.perf_counter()
                 if delay > 0:
                     time.sleep(delay)
-                jobs.append((loaded[k].submit(spp=int(spp)), k, int(spp)))
-            lat, stretch, samples = [], [], 0
-            for j, k, spp in jobs:
+                submitted.append((loaded[k].submit(spp=int(spp)), k))
+            lat, stretch, stretch_e2e, samples, mixed = [], [], [], 0, 0
+            for j, k in submitted:
                 j.wait()
                 st = j.stats()
                 l_ms = st["queue_ms"] + st["wall_ms"]
                 lat.append(l_ms)
                 samples += st["samples"]
-                stretch.append(l_ms / (1000.0 * st["samples"] / alone[k]))
+                mixed += st["mixed_waves"] > 0
+                gpu_alone = 1000.0 * st["samples"] / alone[k]
+                stretch.append(l_ms / gpu_alone)
+                stretch_e2e.append(l_ms / (gpu_alone + fixed_ms[k]))
                 j.close()
-            makespan = time.perf_counter() - t0
-            lat = np.array(lat)
-            results.append({"rate_jobs_per_s": lam, "jobs": n_jobs, "throughput_samples_per_s": samples / makespan,
+            return (time.perf_counter() - t0, np.array(lat), np.array(stretch), np.array(stretch_e2e), samples,
+                    mixed)
+
+        # peak: a burst of jobs submitted at once
+        picks, spps = draw(args.serving_burst, np.random.default_rng(5))
+        span, _, _, _, samples, _ = run(list(zip(picks, spps)), np.zeros(len(picks)))
+        peak = samples / span
+        results = []
+        for load, policy in args.serving_loads:
+            cfg = {"share_exponent": 1.0 if policy == "size" else 0.0,
+                   "deadline_ns_per_sample": float(policy[3:]) if policy.startswith("edf") else 0.0}
+            rad.init(cfg)
+            lam = load * peak / mean_samples
+            r = np.random.default_rng(1000 + int(round(load * 1000)))  # the same jobs for every policy at a load
+            picks, spps = draw(args.serving_jobs, r)
+            arrivals = np.cumsum(r.exponential(1.0 / lam, len(picks)))
+            span, lat, stretch, st_e2e, samples, mixed = run(list(zip(picks, spps)), arrivals)
+            results.append({"offered_load": load, "policy": policy, "rate_jobs_per_s": lam,
+                            "jobs": len(picks), "jobs_in_mixed_waves": int(mixed),
+                            "offered_samples_per_s": samples / arrivals[-1],
+                            "throughput_samples_per_s": samples / span,
                             "p50_ms": float(np.percentile(lat, 50)), "p99_ms": float(np.percentile(lat, 99)),
                             "p99_over_p50": float(np.percentile(lat, 99) / np.percentile(lat, 50)),
                             "stretch_p50": float(np.percentile(stretch, 50)),
-                            "stretch_p99": float(np.percentile(stretch, 99))})
+                            "stretch_p99": float(np.percentile(stretch, 99)),
+                            "stretch_p99_over_p50": float(np.percentile(stretch, 99) / np.percentile(stretch, 50)),
+                            "stretch_e2e_p50": float(np.percentile(st_e2e, 50)),
+                            "stretch_e2e_p99": float(np.percentile(st_e2e, 99)),
+                            "stretch_e2e_p99_over_p50": float(np.percentile(st_e2e, 99) / np.percentile(st_e2e, 50))})
+        rad.init({"share_exponent": 0.0, "deadline_ns_per_sample": 0.0})
         for sc in loaded:
             sc.close()
-    peak = max(r["throughput_samples_per_s"] for r in results)
-    line = {"metric": "serving: throughput and p50/p99 job latency (Poisson arrivals)", "value": peak,
-            "unit": "samples/s", "n_gpus": 1, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
-            "dtype": "f32", "data": "synthetic (seeded many-spheres generator)",
+    line = {"metric": "serving: throughput and p50/p99 job latency (Poisson arrivals, continuous batching)",
+            "value": peak, "unit": "samples/s", "n_gpus": 1, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded many-spheres generator)",
             "config": {"workload": "serving_mix", "scenes": [{"spheres": n, "triangles": 320 * n, "width": w,
                                                               "height": h, "max_depth": d} for n, w, h, d in pool],
                        "spp": "log-uniform [%d, %d]" % (args.spp_min, args.spp_max),
-                       "arrival_window_s": args.duration},
-            "alone_samples_per_s": alone, "sweep": results}
+                       "mean_samples_per_job": mean_samples, "peak_from_burst_of": args.serving_burst,
+                       "budget_bytes": 150e9},
+            "alone_samples_per_s": alone, "fixed_ms_per_job": fixed_ms,
+            "policies": {"fair": "equal path-slot shares in mixed waves (processor sharing)",
+                         "size": "shares in proportion to the work left",
+                         "edfN": "earliest deadline first, deadline = submit + N ns x samples"},
+            "sweep": results}
     print(json.dumps(line), flush=True)
 
 
@@ -643,10 +705,14 @@ def main():
     ap.add_argument("--no-tune", action="store_true", help="skip rad_autotune (keeps launch indices fixed for ncu)")
     ap.add_argument("--vol-res", type=int, default=1024)
     ap.add_argument("--vol-grid", type=int, default=256)
-    ap.add_argument("--rates", type=float, nargs="+", default=[1, 2, 5, 10, 20])
-    ap.add_argument("--duration", type=float, default=10.0, help="serving: arrival window per rate (s)")
-    ap.add_argument("--spp-min", type=int, default=4)
-    ap.add_argument("--spp-max", type=int, default=64)
+    ap.add_argument("--serving-scenes", type=int, default=16, help="serving: resident scenes")
+    ap.add_argument("--serving-jobs", type=int, default=120, help="serving: jobs per load point")
+    ap.add_argument("--serving-burst", type=int, default=40, help="serving: jobs of the peak-throughput burst")
+    ap.add_argument("--serving-loads", type=lambda t: (float(t.split(":")[0]), t.split(":")[1]), nargs="+",
+                    default=[(0.5, "fair"), (0.8, "fair"), (0.8, "edf20"), (1.0, "fair")],
+                    help="serving: offered load (fraction of peak):policy (fair | size | edfN) pairs")
+    ap.add_argument("--spp-min", type=int, default=16)
+    ap.add_argument("--spp-max", type=int, default=1024)
     args = ap.parse_args()
     world, rank, local = dist_setup()
     if args.impl == "reference":

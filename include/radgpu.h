@@ -118,8 +118,15 @@ typedef struct rad_stats {
 /* ---- library ------------------------------------------------------------ */
 /* config_json may be NULL. Keys: "device" (int), "budget_bytes" (admission
  * budget for resident scenes + films, default 150e9), "max_paths" (paths in
- * flight per wave), "block_size". Idempotent: on a library already
- * initialised only "budget_bytes" is applied (a new admission budget). */
+ * flight per wave), "mix_jobs" (default 1: plain `path` jobs running together
+ * share the launches of each wave), "share_exponent" (default 0: a mixed wave
+ * gives its jobs path slots in proportion to (remaining samples)^exponent -- 0
+ * equal shares, 1 in proportion to the work left), "deadline_ns_per_sample"
+ * (default 0 = off; > 0: earliest deadline first, a job's deadline being its
+ * submit time + its samples x this allowance, and mixed waves fill their path
+ * slots in deadline order). Idempotent: on a library already initialised only
+ * "budget_bytes", "mix_jobs", "share_exponent" and "deadline_ns_per_sample"
+ * are applied (deadlines of jobs already submitted are kept). */
 RAD_API int rad_init(const char* config_json);
 RAD_API int rad_shutdown(void);
 /* Copies the calling thread's last error message (NUL-terminated). */

@@ -8,6 +8,7 @@
 #include <algorithm>
 #include <atomic>
 #include <chrono>
+#include <cmath>
 #include <condition_variable>
 #include <cstdio>
 #include <cstring>
@@ -150,6 +151,7 @@ struct rad_job {
   std::atomic<uint64_t> launched{0};
   cudaEvent_t evStart = nullptr, evEnd = nullptr;
   double tSubmit = 0, tStart = 0, tEnd = 0;
+  double deadline = 0;  // earliest-deadline-first mixing: submit time + samples x the per-sample allowance (ms)
   rad_stats stats{};
   std::vector<std::pair<cudaEvent_t, cudaEvent_t>> profEv;
   std::vector<int> profKind;
@@ -169,7 +171,7 @@ namespace {
 
 // Waves the worker may have queued on the stream ahead of the GPU (see WorkerMain),
 // and the mixed-wave job tables kept for them.
-constexpr size_t kMaxWavesInFlight = 3;
+constexpr size_t kMaxWavesInFlight = 2;
 constexpr int kMixRing = (int)kMaxWavesInFlight + 1;
 
 struct Lib {
@@ -190,6 +192,8 @@ struct Lib {
   uint32_t* hCounters = nullptr;  // pinned
   // mixed waves: a ring of job tables (device, with pinned staging), one per wave in flight
   bool mixJobs = true;
+  float shareExp = 0.f;  // mixed-wave shares ~ remaining samples ^ shareExp (0: equal shares)
+  double edfNsPerSample = 0;  // > 0: earliest-deadline-first mixing, deadline = submit + samples x this
   MixJob* mixDev = nullptr;
   MixJob* mixHost = nullptr;
   uint32_t mixSlot = 0;
@@ -275,6 +279,8 @@ void InitLocked(const char* cfg) {
       JValue c = JsonReader::Parse(cfg);
       if (const JValue* v = c.get("budget_bytes")) lib.budget = (uint64_t)v->n;
       if (const JValue* v = c.get("mix_jobs")) lib.mixJobs = v->n != 0;
+      if (const JValue* v = c.get("share_exponent")) lib.shareExp = (float)v->n;
+      if (const JValue* v = c.get("deadline_ns_per_sample")) lib.edfNsPerSample = v->n;
     }
     return;
   }
@@ -284,6 +290,8 @@ void InitLocked(const char* cfg) {
     if (const JValue* v = c.get("budget_bytes")) lib.budget = (uint64_t)v->n;
     if (const JValue* v = c.get("max_paths")) lib.maxPaths = (uint32_t)v->n;
     if (const JValue* v = c.get("mix_jobs")) lib.mixJobs = v->n != 0;
+    if (const JValue* v = c.get("share_exponent")) lib.shareExp = (float)v->n;
+    if (const JValue* v = c.get("deadline_ns_per_sample")) lib.edfNsPerSample = v->n;
   }
   if (lib.maxPaths < 1024) lib.maxPaths = 1024;
   int n = 0;
@@ -770,9 +778,14 @@ bool Mixable(const rad_job* j) {
          !(j->flags & (RAD_JOB_GUIDE | RAD_JOB_PROFILE_KERNELS | RAD_JOB_COUNT_TRAVERSAL));
 }
 
-// One wave holding paths of several jobs (of any scenes): the path slots are
-// split evenly between the jobs (processor sharing), and a share a job cannot
-// use goes to the others. A job whose share covers its frame takes whole
+// One wave holding paths of several jobs (of any scenes). With a deadline
+// allowance set (earliest deadline first; js in deadline order), each job in
+// turn takes as many path slots as it can use. Otherwise the path slots are
+// split between the jobs in proportion to (remaining samples)^shareExp --
+// exponent 0, equal shares (processor sharing: every job's slowdown is about
+// the same); exponent 1, shares in proportion to the work left (jobs running
+// together finish together: latencies even out across job sizes) -- and a
+// share a job cannot use goes to the others. A job whose share covers its frame takes whole
 // samples (as many consecutive ones as fit); otherwise it takes the next pixel
 // chunk of its current sample, so each pixel still receives its samples in
 // order and the film is the same as when the job runs alone. Every stage is one
@@ -789,6 +802,23 @@ void RunMixedWave(const std::vector<rad_job*>& js) {
     need[i] = (uint64_t)(js[i]->spp - js[i]->nextSample) * npix - js[i]->mixCursor;
   }
   uint64_t left = P;
+  if (lib.edfNsPerSample > 0) {
+    // earliest deadline first (js is in deadline order): each job in turn takes what it can use
+    for (size_t i = 0; i < m && left > 0; i++) {
+      give[i] = std::min(need[i], left);
+      left -= give[i];
+    }
+  } else if (lib.shareExp != 0.f && m > 1) {
+    std::vector<double> w(m);
+    double sum = 0;
+    for (size_t i = 0; i < m; i++) sum += (w[i] = std::pow((double)std::max<uint64_t>(need[i], 1), lib.shareExp));
+    for (size_t i = 0; i < m; i++) {
+      uint64_t g = std::min<uint64_t>(need[i], std::max<uint64_t>(1, (uint64_t)((double)P * w[i] / sum)));
+      g = std::min(g, left);
+      give[i] = g;
+      left -= g;
+    }
+  }
   for (int pass = 0; pass < 3 && left > 0; pass++) {
     size_t open = 0;
     for (size_t i = 0; i < m; i++) open += give[i] < need[i] ? 1 : 0;
@@ -1167,7 +1197,11 @@ void WorkerMain() {
         if (useGroup) {
           std::stable_sort(mixable.begin(), mixable.end(),
                            [](rad_job* a, rad_job* b) { return a->launched.load() < b->launched.load(); });
-          if (!j || mixable[0]->launched.load() <= best) {
+          const bool groupFirst = !j || mixable[0]->launched.load() <= best;
+          if (lib.edfNsPerSample > 0)
+            std::stable_sort(mixable.begin(), mixable.end(),
+                             [](rad_job* a, rad_job* b) { return a->deadline < b->deadline; });
+          if (groupFirst) {
             if (mixable.size() > (size_t)kMaxMix) mixable.resize(kMaxMix);
             group = mixable;
             j = nullptr;
@@ -1553,6 +1587,7 @@ int rad_job_submit(rad_scene* scene, const rad_job_desc* desc, rad_job** out) {
     j->total = scene->dev.isParticle ? j->spp : npix * j->spp;  // particle_tracer: spp = light paths
     j->filmBytes = npix * sizeof(float4) + 64;
     j->tSubmit = NowMs();
+    j->deadline = j->tSubmit + (double)j->total * lib.edfNsPerSample * 1e-6;
     scene->jobs++;
     *out = j;
     if (j->flags & RAD_JOB_SYNC) {
