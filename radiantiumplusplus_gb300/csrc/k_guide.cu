@@ -14,6 +14,7 @@
 
 #include "dguide.cuh"
 #include "dscene.cuh"
+#include "dtc.cuh"
 #include "kernels.h"
 
 namespace rad {
@@ -215,6 +216,161 @@ __device__ __forceinline__ void StoreMix(const float* o, const GuideDev& G, floa
   mx[10] = make_float4(m.c, 0.f, 0.f, 0.f);
 }
 
+// ---- the MLP on the fifth-generation tensor cores (tcgen05, accumulator in TMEM)
+// One tile = 128 queries (a CTA of 4 warps, one query per thread): every layer
+// is one M = 128 MMA chain over K in steps of 16, issued by one thread, with
+// the activations and the four weight matrices in shared memory in the K-major
+// core-matrix layout (dtc.cuh) and the fp32 accumulator in 64 TMEM columns. The
+// epilogue (ReLU, fp16) reads each thread's row back with tcgen05.ld and writes
+// the next layer's operand. Every wait is bounded: on a timeout the kernel sets
+// kErrGuideTc, waits (bounded) for its outstanding MMA, frees its TMEM and ends.
+constexpr int kTcRows = 128;
+constexpr uint32_t kTcW0 = 0;                                // 64 x 48
+constexpr uint32_t kTcW1 = kTcW0 + kGHid * kGIn * 2;         // 64 x 64
+constexpr uint32_t kTcW2 = kTcW1 + kGHid * kGHid * 2;        // 64 x 64
+constexpr uint32_t kTcW3 = kTcW2 + kGHid * kGHid * 2;        // 48 x 64
+constexpr uint32_t kTcAct = kTcW3 + kGOut * kGHid * 2;       // 128 x 64 activations
+constexpr uint32_t kTcMisc = kTcAct + kTcRows * kGHid * 2;   // mbarrier, TMEM address
+constexpr int kTcSmem = (int)kTcMisc + 16;
+constexpr uint32_t kTcCols = 64;                             // TMEM columns (fp32 accumulator, N <= 64)
+constexpr uint32_t kTcWaitLimit = 1u << 22;
+static_assert(kTcW1 % 16 == 0 && kTcW2 % 16 == 0 && kTcW3 % 16 == 0 && kTcAct % 16 == 0 && kTcMisc % 16 == 0,
+              "descriptor addresses are 16-byte aligned");
+
+__device__ __forceinline__ void TcLoadWeights(const __half* gw, unsigned char* sm) {
+  for (int i = threadIdx.x; i < kGHid * kGIn; i += blockDim.x) {
+    int n = i / kGIn, k = i % kGIn;
+    *reinterpret_cast<__half*>(sm + kTcW0 + TcOffset(n, k, kGIn)) = gw[kGW0 + i];
+  }
+  for (int i = threadIdx.x; i < kGHid * kGHid; i += blockDim.x) {
+    int n = i / kGHid, k = i % kGHid;
+    *reinterpret_cast<__half*>(sm + kTcW1 + TcOffset(n, k, kGHid)) = gw[kGW1 + i];
+    *reinterpret_cast<__half*>(sm + kTcW2 + TcOffset(n, k, kGHid)) = gw[kGW2 + i];
+  }
+  for (int i = threadIdx.x; i < kGOut * kGHid; i += blockDim.x) {
+    int n = i / kGHid, k = i % kGHid;
+    *reinterpret_cast<__half*>(sm + kTcW3 + TcOffset(n, k, kGHid)) = gw[kGW3 + i];
+  }
+}
+
+// The 48 network inputs of one query (32 grid features, N, wo, 1, zeros) as 24 fp16 pairs.
+__device__ __forceinline__ void TcEncodeRow(const GuideDev& G, V3 P, V3 N, V3 wo, uint32_t (&v)[24]) {
+  __half row[kGIn];
+  float u[3];
+  GuidePosToUnit(G, P, u);
+  GuideEncodeLevels(G, u, 0, kGLevels, row);
+  GuideEncodeTail(N, wo, row);
+#pragma unroll
+  for (int i = 0; i < 24; i++) v[i] = *reinterpret_cast<const uint32_t*>(row + 2 * i);
+}
+
+// Writes this thread's 48-input row into the layer-0 operand (K = 48).
+__device__ __forceinline__ void TcStoreInputs(unsigned char* sm, uint32_t r, const uint32_t (&v)[24]) {
+#pragma unroll
+  for (int c = 0; c < kGIn / 8; c++)
+    *reinterpret_cast<uint4*>(sm + kTcAct + TcOffset(r, 8 * c, kGIn)) =
+        make_uint4(v[4 * c], v[4 * c + 1], v[4 * c + 2], v[4 * c + 3]);
+}
+
+// One layer: D = act x W^T into TMEM (thread 0 issues), then every thread waits.
+// Returns false if the wait gave up (the caller stops).
+__device__ __forceinline__ bool TcLayer(unsigned char* sm, uint32_t tmem, uint64_t* mbar, uint32_t& phase,
+                                        uint32_t wOff, int K, int N, int* fail) {
+  if (threadIdx.x == 0) {
+    TcFenceAfter();
+    const uint32_t a0 = SmemAddr(sm + kTcAct), b0 = SmemAddr(sm + wOff);
+    const uint32_t idesc = TcIdescF16(kTcRows, (uint32_t)N);
+    for (int s = 0; s < K / 16; s++)
+      TcMma(tmem, TcSmemDesc(a0 + 256u * s, 128u, 16u * K), TcSmemDesc(b0 + 256u * s, 128u, 16u * K), idesc, s > 0);
+    TcCommit(mbar);
+  }
+  const bool ok = MbarWait(mbar, phase, kTcWaitLimit);
+  if (!ok) atomicOr(fail, 1);
+  __syncthreads();
+  if (*fail) return false;
+  phase ^= 1u;
+  TcFenceAfter();
+  return true;
+}
+
+// ReLU of this thread's 64 accumulator columns, as the next layer's fp16 operand (K = 64).
+__device__ __forceinline__ void TcReluToAct(unsigned char* sm, uint32_t tmemRow, uint32_t r) {
+#pragma unroll
+  for (int c0 = 0; c0 < kGHid; c0 += 16) {
+    float v[16];
+    TcLoad16(tmemRow + c0, v);
+#pragma unroll
+    for (int q = 0; q < 2; q++) {
+      uint4 w;
+      w.x = PackF2(fmaxf(v[8 * q + 0], 0.f), fmaxf(v[8 * q + 1], 0.f));
+      w.y = PackF2(fmaxf(v[8 * q + 2], 0.f), fmaxf(v[8 * q + 3], 0.f));
+      w.z = PackF2(fmaxf(v[8 * q + 4], 0.f), fmaxf(v[8 * q + 5], 0.f));
+      w.w = PackF2(fmaxf(v[8 * q + 6], 0.f), fmaxf(v[8 * q + 7], 0.f));
+      *reinterpret_cast<uint4*>(sm + kTcAct + TcOffset(r, c0 + 8 * q, kGHid)) = w;
+    }
+  }
+}
+
+// The four layers of the tile; o receives this thread's 48 outputs. Returns false on a wait timeout.
+__device__ __forceinline__ bool TcMlpTile(unsigned char* sm, uint32_t tmem, uint64_t* mbar, uint32_t& phase,
+                                          int* fail, float (&o)[kGOut]) {
+  const uint32_t r = threadIdx.x;
+  const uint32_t tmemRow = tmem + ((32u * (threadIdx.x >> 5)) << 16);
+  FenceProxyAsync();
+  TcFenceBefore();
+  __syncthreads();
+  const uint32_t wOff[3] = {kTcW0, kTcW1, kTcW2};
+  for (int l = 0; l < 3; l++) {
+    if (!TcLayer(sm, tmem, mbar, phase, wOff[l], l == 0 ? kGIn : kGHid, kGHid, fail)) return false;
+    TcReluToAct(sm, tmemRow, r);
+    FenceProxyAsync();
+    TcFenceBefore();
+    __syncthreads();
+  }
+  if (!TcLayer(sm, tmem, mbar, phase, kTcW3, kGHid, kGOut, fail)) return false;
+#pragma unroll
+  for (int c0 = 0; c0 < kGOut; c0 += 16) {
+    float v[16];
+    TcLoad16(tmemRow + c0, v);
+#pragma unroll
+    for (int i = 0; i < 16; i++) o[c0 + i] = v[i];
+  }
+  TcFenceBefore();
+  __syncthreads();  // every TMEM read done before the next tile's MMA
+  return true;
+}
+
+// Set-up shared by the tcgen05 kernels: weights, mbarrier, TMEM columns.
+__device__ __forceinline__ uint32_t TcSetup(const GuideDev& G, unsigned char* sm, uint64_t*& mbar, int*& fail) {
+  mbar = reinterpret_cast<uint64_t*>(sm + kTcMisc);
+  uint32_t* slot = reinterpret_cast<uint32_t*>(sm + kTcMisc + 8);
+  fail = reinterpret_cast<int*>(sm + kTcMisc + 12);
+  if (threadIdx.x == 0) {
+    MbarInit(mbar, 1);
+    *fail = 0;
+  }
+  if (threadIdx.x < 32) TcAlloc(slot, kTcCols);
+  TcLoadWeights(G.weights, sm);
+  FenceProxyAsync();
+  TcFenceBefore();
+  __syncthreads();
+  TcFenceAfter();
+  return *slot;
+}
+
+// After the tile loop: on a timeout, one more bounded wait for the MMA still
+// outstanding; then the TMEM columns are freed.
+__device__ __forceinline__ void TcTeardown(uint32_t tmem, uint64_t* mbar, uint32_t phase, int* fail, uint32_t* err) {
+  if (*fail) {
+    MbarWait(mbar, phase, kTcWaitLimit);
+    if (threadIdx.x == 0) atomicOr(err, kErrGuideTc);
+  }
+  TcFenceBefore();
+  __syncthreads();
+  TcFenceAfter();
+  if (threadIdx.x < 32) TcDealloc(tmem, kTcCols);
+}
+
 }  // namespace
 
 // Guided shade classes: all but emitters and rough_glass (near-delta
@@ -266,6 +422,82 @@ __global__ void __launch_bounds__(kInferWarps * 32, 2)
       StoreMix(reinterpret_cast<const float*>(act) + lane * (kActLd / 2), G, G.mix + (size_t)p * kGMixF4);
     __syncwarp();
   }
+}
+
+// KGuideInfer on tcgen05: 128 queries per tile, one per thread.
+__global__ void __launch_bounds__(kTcRows, 1)
+    KGuideInferTc(DevScene S, PathBuffers B, GuideDev G, int depth) {
+  extern __shared__ __align__(1024) unsigned char smtc[];
+  uint64_t* mbar;
+  int* fail;
+  const uint32_t tmem = TcSetup(G, smtc, mbar, fail);
+  uint32_t phase = 0;
+  const uint32_t* cnt = B.counters + kClassBase + depth * kShadeClasses;
+  const uint32_t n1 = cnt[SC_DIFFUSE], n2 = cnt[SC_METAL], n4 = cnt[SC_DISNEY], n5 = cnt[SC_GENERIC];
+  const uint32_t total = n1 + n2 + n4 + n5;
+  for (uint32_t base = blockIdx.x * kTcRows; base < total; base += gridDim.x * kTcRows) {
+    const uint32_t q = base + threadIdx.x;
+    const bool valid = q < total;
+    uint32_t p = 0;
+    uint32_t v[24];
+#pragma unroll
+    for (int i = 0; i < 24; i++) v[i] = 0u;
+    if (valid) {
+      uint32_t j = q, cls;
+      if (j < n1) {
+        cls = SC_DIFFUSE;
+      } else if ((j -= n1) < n2) {
+        cls = SC_METAL;
+      } else if ((j -= n2) < n4) {
+        cls = SC_DISNEY;
+      } else {
+        j -= n4;
+        cls = SC_GENERIC;
+      }
+      p = B.classQ[(size_t)cls * B.capacity + j];
+      HitRec h = B.hit[p];
+      float4 ro = B.rayO[p], rd = B.rayD[p];
+      V3 O{ro.x, ro.y, ro.z}, D{rd.x, rd.y, rd.z};
+      TraceHit th{h.t, h.u, h.v, h.prim, h.shape, h.front};
+      SurfInt si = ComputeSI(S, O, D, th);
+      TcEncodeRow(G, si.P, si.sh.N, -D, v);
+    }
+    TcStoreInputs(smtc, threadIdx.x, v);
+    float o[kGOut];
+    if (!TcMlpTile(smtc, tmem, mbar, phase, fail, o)) break;
+    if (valid) StoreMix(o, G, G.mix + (size_t)p * kGMixF4);
+  }
+  TcTeardown(tmem, mbar, phase, fail, B.counters + kMiscBase + 1);
+}
+
+// KGuideQuery on tcgen05 (the parity hook runs the same network code as inference).
+__global__ void __launch_bounds__(kTcRows, 1)
+    KGuideQueryTc(GuideDev G, const float* queries, uint32_t n, float* raw, float4* mix, uint32_t* err) {
+  extern __shared__ __align__(1024) unsigned char smtc[];
+  uint64_t* mbar;
+  int* fail;
+  const uint32_t tmem = TcSetup(G, smtc, mbar, fail);
+  uint32_t phase = 0;
+  for (uint32_t base = blockIdx.x * kTcRows; base < n; base += gridDim.x * kTcRows) {
+    const uint32_t q = base + threadIdx.x;
+    const bool valid = q < n;
+    uint32_t v[24];
+#pragma unroll
+    for (int i = 0; i < 24; i++) v[i] = 0u;
+    if (valid) {
+      const float* x = queries + (size_t)q * 9;
+      TcEncodeRow(G, V3{x[0], x[1], x[2]}, V3{x[3], x[4], x[5]}, V3{x[6], x[7], x[8]}, v);
+    }
+    TcStoreInputs(smtc, threadIdx.x, v);
+    float o[kGOut];
+    if (!TcMlpTile(smtc, tmem, mbar, phase, fail, o)) break;
+    if (valid) {
+      if (raw)
+        for (int k = 0; k < kGOut; k++) raw[(size_t)q * kGOut + k] = k < kGOutUsed ? o[k] : 0.f;
+      if (mix) StoreMix(o, G, mix + (size_t)q * kGMixF4);
+    }
+  }
+  TcTeardown(tmem, mbar, phase, fail, err);
 }
 
 // queries: n x 9 (P, N, wo); raw: n x kGOut (optional); mix: n x kGMixF4 float4 (optional)
@@ -587,22 +819,27 @@ cudaError_t GuideKernelsInit() {
   if (e != cudaSuccess) return e;
   e = cudaFuncSetAttribute(KGuideQuery, cudaFuncAttributeMaxDynamicSharedMemorySize, kInferSmem);
   if (e != cudaSuccess) return e;
+  e = cudaFuncSetAttribute(KGuideInferTc, cudaFuncAttributeMaxDynamicSharedMemorySize, kTcSmem);
+  if (e != cudaSuccess) return e;
+  e = cudaFuncSetAttribute(KGuideQueryTc, cudaFuncAttributeMaxDynamicSharedMemorySize, kTcSmem);
+  if (e != cudaSuccess) return e;
   return cudaFuncSetAttribute(KGuideTrain, cudaFuncAttributeMaxDynamicSharedMemorySize, kTrainSmem);
 }
 
 cudaError_t LaunchGuideInfer(const DevScene& S, const PathBuffers& B, const GuideDev& G, int depth, uint32_t maxCount,
                              cudaStream_t st) {
-  int blocks = (int)std::min<uint32_t>((maxCount + 255) / 256, (uint32_t)GuideGrid(2));
+  // tcgen05 tiles of 128 queries; at most 4 CTAs per SM (4 x 64 TMEM columns of 512)
+  int blocks = (int)std::min<uint32_t>((maxCount + kTcRows - 1) / kTcRows, (uint32_t)GuideGrid(4));
   if (blocks < 1) blocks = 1;
-  KGuideInfer<<<blocks, kInferWarps * 32, kInferSmem, st>>>(S, B, G, depth);
+  KGuideInferTc<<<blocks, kTcRows, kTcSmem, st>>>(S, B, G, depth);
   return cudaGetLastError();
 }
 
 cudaError_t LaunchGuideQuery(const GuideDev& G, const float* queries, uint32_t n, float* raw, float4* mix,
-                             cudaStream_t st) {
+                             uint32_t* err, cudaStream_t st) {
   if (n == 0) return cudaSuccess;
-  int blocks = (int)std::min<uint32_t>((n + 255) / 256, (uint32_t)GuideGrid(2));
-  KGuideQuery<<<blocks, kInferWarps * 32, kInferSmem, st>>>(G, queries, n, raw, mix);
+  int blocks = (int)std::min<uint32_t>((n + kTcRows - 1) / kTcRows, (uint32_t)GuideGrid(4));
+  KGuideQueryTc<<<blocks, kTcRows, kTcSmem, st>>>(G, queries, n, raw, mix, err);
   return cudaGetLastError();
 }
 

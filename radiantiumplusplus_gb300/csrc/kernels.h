@@ -56,6 +56,7 @@ constexpr int kMiscBase = 2 * kMaxBounce + 2;  // [0] spare, [1] device error wo
 // bits of the device error word: 1 traversal stack, 2 / 4 vol_path iteration
 // bounds, 8 bdpt visibility buffer, kErrPixelRange a pixel index beyond the film
 constexpr uint32_t kErrPixelRange = 16u;
+constexpr uint32_t kErrGuideTc = 32u;  // a tensor-core wait of the guide network gave up
 constexpr int kClassBase = kMiscBase + 8;
 // per-bounce ray-fetch counters of the persistent extend / shadow kernels
 constexpr int kFetchBase = kClassBase + (kMaxBounce + 1) * kShadeClasses;
@@ -230,7 +231,7 @@ cudaError_t LaunchVolPath(const DevScene& S, const PathBuffers& B, const WavePar
 cudaError_t GuideKernelsInit();
 cudaError_t LaunchGuideInfer(const DevScene& S, const PathBuffers& B, const GuideDev& G, int depth, uint32_t maxCount,
                              cudaStream_t st);
-cudaError_t LaunchGuideQuery(const GuideDev& G, const float* queries, uint32_t n, float* raw, float4* mix,
+cudaError_t LaunchGuideQuery(const GuideDev& G, const float* queries, uint32_t n, float* raw, float4* mix, uint32_t* err,
                              cudaStream_t st);
 cudaError_t LaunchGuideMixEval(const float4* mix, const float* dirs, const float* u, uint32_t n, float* pdf,
                                float* outDirs, cudaStream_t st);

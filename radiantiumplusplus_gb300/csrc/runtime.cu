@@ -780,7 +780,7 @@ bool Mixable(const rad_job* j) {
 
 // One wave holding paths of several jobs (of any scenes). With a deadline
 // allowance set (earliest deadline first; js in deadline order), each job in
-// turn takes as many path slots as it can use. Otherwise the path slots are
+// turn takes what it can use of half the slots still free. Otherwise the path slots are
 // split between the jobs in proportion to (remaining samples)^shareExp --
 // exponent 0, equal shares (processor sharing: every job's slowdown is about
 // the same); exponent 1, shares in proportion to the work left (jobs running
@@ -803,9 +803,12 @@ void RunMixedWave(const std::vector<rad_job*>& js) {
   }
   uint64_t left = P;
   if (lib.edfNsPerSample > 0) {
-    // earliest deadline first (js is in deadline order): each job in turn takes what it can use
+    // earliest deadline first (js is in deadline order): each job in turn takes what it can use of half
+    // the slots still free (the last one all of them), so a job that missed its deadline -- and stays
+    // first until it ends -- cannot hold every slot while later, nearer-deadline jobs wait
     for (size_t i = 0; i < m && left > 0; i++) {
-      give[i] = std::min(need[i], left);
+      const uint64_t cap = i + 1 == m ? left : std::max<uint64_t>(left / 2, std::min<uint64_t>(left, 65536));
+      give[i] = std::min(need[i], cap);
       left -= give[i];
     }
   } else if (lib.shareExp != 0.f && m > 1) {
@@ -1964,11 +1967,16 @@ int rad_guide_forward(rad_scene* scene, const float* queries, int64_t n, float* 
     DevBuf<float4> dmix(mix ? (size_t)kGMixF4 * n : 0);
     Check(cudaMemcpyAsync(dq.p, queries, 36 * n, cudaMemcpyHostToDevice, lib.stream), "copy");
     GuideDev G = GuideView(net);
-    Check(LaunchGuideQuery(G, dq.p, (uint32_t)n, draw.p, dmix.p, lib.stream), "guide query");
+    uint32_t* err = lib.paths.counters + kMiscBase + 1;
+    Check(cudaMemsetAsync(err, 0, sizeof(uint32_t), lib.stream), "memset");
+    Check(LaunchGuideQuery(G, dq.p, (uint32_t)n, draw.p, dmix.p, err, lib.stream), "guide query");
     if (raw) Check(cudaMemcpyAsync(raw, draw.p, sizeof(float) * kGOut * n, cudaMemcpyDeviceToHost, lib.stream), "copy");
     if (mix)
       Check(cudaMemcpyAsync(mix, dmix.p, sizeof(float4) * kGMixF4 * n, cudaMemcpyDeviceToHost, lib.stream), "copy");
+    uint32_t errWord = 0;
+    Check(cudaMemcpyAsync(&errWord, err, sizeof(uint32_t), cudaMemcpyDeviceToHost, lib.stream), "copy");
     Check(cudaStreamSynchronize(lib.stream), "sync");
+    if (errWord) throw Error{RAD_ERR_DEVICE_CHECK, "guide network: a tensor-core wait gave up"};
   });
 }
 

@@ -168,23 +168,26 @@ def test_guided_estimator_is_unbiased(rad, scene_dir):
 
 
 def _errors(x, ref):
-    e = ((x - ref) ** 2 / (ref ** 2 + 1e-2)).mean(-1).ravel()
+    """relMSE per pixel with the epsilon scaled to the image, 1e-2 mean(ref)^2:
+    its mean, its mean without the worst 1% of pixels, and its median."""
+    e = ((x - ref) ** 2 / (ref ** 2 + 1e-2 * ref.mean() ** 2)).mean(-1).ravel()
     s = np.sort(e)
     return e.mean(), s[:int(0.99 * s.size)].mean(), np.median(e)
 
 
 def test_trained_guide_beats_plain_sampling(rad, scene_dir):
     """Equal spp on the room lit through a ceiling opening: the guided job, training
-    during its first quarter of samples, has lower error than plain BSDF sampling.
-    Checked on the relMSE without the worst 1 % of pixels and on the median pixel
-    (the mean relMSE of both is dominated by a few fireflies); all are printed."""
+    during its first quarter of samples, has lower error than plain BSDF sampling,
+    against a plain 8192-spp reference, each render with its own seed. Checked on
+    the relMSE without the worst 1 % of pixels and on the median pixel (the mean
+    relMSE of both is dominated by a few fireflies); all are printed."""
     path = _room(scene_dir, 128, 96)
     s = rad.Scene.from_file(path)
     ref = s.render(spp=8192, seed=2000)
     spp = 256
     plain = s.render(spp=spp, seed=5)
     s.guide_enable({"log2_table": 16, "train_path_shift": 0, "max_res": 256, "seed": 3})
-    j = s.submit(spp=spp, seed=5, guide=True)
+    j = s.submit(spp=spp, seed=6, guide=True)
     j.wait()
     st = j.stats()
     guided = j.film()
