@@ -653,7 +653,8 @@ def run_serving(args, world, rank, local):
         results = []
         for load, policy in args.serving_loads:
             cfg = {"share_exponent": 1.0 if policy == "size" else 0.0,
-                   "deadline_ns_per_sample": float(policy[3:]) if policy.startswith("edf") else 0.0}
+                   "deadline_ns_per_sample": float(policy[3:]) if policy.startswith("edf") else 0.0,
+                   "slowdown_ns_per_sample": float(policy[4:]) if policy.startswith("slow") else 0.0}
             rad.init(cfg)
             lam = load * peak / mean_samples
             r = np.random.default_rng(1000 + int(round(load * 1000)))  # the same jobs for every policy at a load
@@ -672,7 +673,7 @@ def run_serving(args, world, rank, local):
                             "stretch_e2e_p50": float(np.percentile(st_e2e, 50)),
                             "stretch_e2e_p99": float(np.percentile(st_e2e, 99)),
                             "stretch_e2e_p99_over_p50": float(np.percentile(st_e2e, 99) / np.percentile(st_e2e, 50))})
-        rad.init({"share_exponent": 0.0, "deadline_ns_per_sample": 0.0})
+        rad.init({"share_exponent": 0.0, "deadline_ns_per_sample": 0.0, "slowdown_ns_per_sample": 0.0})
         for sc in loaded:
             sc.close()
     line = {"metric": "serving: throughput and p50/p99 job latency (Poisson arrivals, continuous batching)",
@@ -686,7 +687,8 @@ def run_serving(args, world, rank, local):
             "alone_samples_per_s": alone, "fixed_ms_per_job": fixed_ms,
             "policies": {"fair": "equal path-slot shares in mixed waves (processor sharing)",
                          "size": "shares in proportion to the work left",
-                         "edfN": "earliest deadline first, deadline = submit + N ns x samples"},
+                         "edfN": "earliest deadline first, deadline = submit + N ns x samples",
+                         "slowN": "highest slowdown first, slowdown = age / (N ns x samples + 20 ms)"},
             "sweep": results}
     print(json.dumps(line), flush=True)
 
@@ -717,7 +719,7 @@ def main():
     ap.add_argument("--serving-burst", type=int, default=40, help="serving: jobs of the peak-throughput burst")
     ap.add_argument("--serving-loads", type=lambda t: (float(t.split(":")[0]), t.split(":")[1]), nargs="+",
                     default=[(0.5, "fair"), (0.8, "fair"), (0.8, "edf20"), (1.0, "fair")],
-                    help="serving: offered load (fraction of peak):policy (fair | size | edfN) pairs")
+                    help="serving: offered load (fraction of peak):policy (fair | size | edfN | slowN) pairs")
     ap.add_argument("--spp-min", type=int, default=16)
     ap.add_argument("--spp-max", type=int, default=1024)
     args = ap.parse_args()

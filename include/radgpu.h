@@ -124,9 +124,12 @@ typedef struct rad_stats {
  * equal shares, 1 in proportion to the work left), "deadline_ns_per_sample"
  * (default 0 = off; > 0: earliest deadline first, a job's deadline being its
  * submit time + its samples x this allowance, and mixed waves fill their path
- * slots in deadline order). Idempotent: on a library already initialised only
- * "budget_bytes", "mix_jobs", "share_exponent" and "deadline_ns_per_sample"
- * are applied (deadlines of jobs already submitted are kept). */
+ * slots in deadline order), "slowdown_ns_per_sample" (default 0 = off; > 0:
+ * highest slowdown first, a job's slowdown being its age over its samples x
+ * this + 20 ms, re-evaluated every wave). Idempotent: on a library already
+ * initialised only "budget_bytes", "mix_jobs", "share_exponent",
+ * "deadline_ns_per_sample" and "slowdown_ns_per_sample" are applied (deadlines
+ * of jobs already submitted are kept). */
 RAD_API int rad_init(const char* config_json);
 RAD_API int rad_shutdown(void);
 /* Copies the calling thread's last error message (NUL-terminated). */

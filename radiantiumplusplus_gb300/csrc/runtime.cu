@@ -194,6 +194,7 @@ struct Lib {
   bool mixJobs = true;
   float shareExp = 0.f;  // mixed-wave shares ~ remaining samples ^ shareExp (0: equal shares)
   double edfNsPerSample = 0;  // > 0: earliest-deadline-first mixing, deadline = submit + samples x this
+  double slowNsPerSample = 0;  // > 0: highest-slowdown-first mixing, slowdown = age / (samples x this + 20 ms)
   MixJob* mixDev = nullptr;
   MixJob* mixHost = nullptr;
   uint32_t mixSlot = 0;
@@ -281,6 +282,7 @@ void InitLocked(const char* cfg) {
       if (const JValue* v = c.get("mix_jobs")) lib.mixJobs = v->n != 0;
       if (const JValue* v = c.get("share_exponent")) lib.shareExp = (float)v->n;
       if (const JValue* v = c.get("deadline_ns_per_sample")) lib.edfNsPerSample = v->n;
+      if (const JValue* v = c.get("slowdown_ns_per_sample")) lib.slowNsPerSample = v->n;
     }
     return;
   }
@@ -292,6 +294,7 @@ void InitLocked(const char* cfg) {
     if (const JValue* v = c.get("mix_jobs")) lib.mixJobs = v->n != 0;
     if (const JValue* v = c.get("share_exponent")) lib.shareExp = (float)v->n;
     if (const JValue* v = c.get("deadline_ns_per_sample")) lib.edfNsPerSample = v->n;
+    if (const JValue* v = c.get("slowdown_ns_per_sample")) lib.slowNsPerSample = v->n;
   }
   if (lib.maxPaths < 1024) lib.maxPaths = 1024;
   int n = 0;
@@ -779,8 +782,9 @@ bool Mixable(const rad_job* j) {
 }
 
 // One wave holding paths of several jobs (of any scenes). With a deadline
-// allowance set (earliest deadline first; js in deadline order), each job in
-// turn takes what it can use of half the slots still free. Otherwise the path slots are
+// allowance set (earliest deadline first) or a slowdown estimate (highest
+// slowdown first), js comes in that order and each job in turn takes what it
+// can use of half the slots still free. Otherwise the path slots are
 // split between the jobs in proportion to (remaining samples)^shareExp --
 // exponent 0, equal shares (processor sharing: every job's slowdown is about
 // the same); exponent 1, shares in proportion to the work left (jobs running
@@ -802,8 +806,8 @@ void RunMixedWave(const std::vector<rad_job*>& js) {
     need[i] = (uint64_t)(js[i]->spp - js[i]->nextSample) * npix - js[i]->mixCursor;
   }
   uint64_t left = P;
-  if (lib.edfNsPerSample > 0) {
-    // earliest deadline first (js is in deadline order): each job in turn takes what it can use of half
+  if (lib.edfNsPerSample > 0 || lib.slowNsPerSample > 0) {
+    // earliest deadline / highest slowdown first (js is in that order): each job in turn takes what it can use of half
     // the slots still free (the last one all of them), so a job that missed its deadline -- and stays
     // first until it ends -- cannot hold every slot while later, nearer-deadline jobs wait
     for (size_t i = 0; i < m && left > 0; i++) {
@@ -1201,9 +1205,15 @@ void WorkerMain() {
           std::stable_sort(mixable.begin(), mixable.end(),
                            [](rad_job* a, rad_job* b) { return a->launched.load() < b->launched.load(); });
           const bool groupFirst = !j || mixable[0]->launched.load() <= best;
-          if (lib.edfNsPerSample > 0)
+          if (lib.slowNsPerSample > 0) {
+            // highest slowdown so far first: age over the job's expected time alone
+            const double now = NowMs(), k = lib.slowNsPerSample * 1e-6;
+            auto slow = [&](rad_job* x) { return (now - x->tSubmit) / ((double)x->total * k + 20.0); };
+            std::stable_sort(mixable.begin(), mixable.end(), [&](rad_job* a, rad_job* b) { return slow(a) > slow(b); });
+          } else if (lib.edfNsPerSample > 0) {
             std::stable_sort(mixable.begin(), mixable.end(),
                              [](rad_job* a, rad_job* b) { return a->deadline < b->deadline; });
+          }
           if (groupFirst) {
             if (mixable.size() > (size_t)kMaxMix) mixable.resize(kMaxMix);
             group = mixable;
