@@ -1,15 +1,18 @@
 // Guide network kernels (see dguide.cuh for the method):
-//   KGuideInfer    -- per bounce: hash-grid encode + MLP for every hit of a
+//   KGuideInferTc  -- per bounce: hash-grid encode + MLP for every hit of a
 //                     guided shade class, mixture parameters per path slot
-//   KGuideQuery    -- the same network on caller-given queries (parity hook)
+//   KGuideQueryTc  -- the same network on caller-given queries (parity hook)
 //   KGuideFinalize -- training weight of each recorded vertex from the path's
 //                     final radiance
 //   KGuideTrain    -- forward + backward of the loss over a batch of records:
 //                     MLP weight gradients and hash-table gradients
 //   KGuideAdam     -- Adam step, refreshes the fp16 copies
-// Matrix products run on the tensor cores with mma.sync m16n8k16 (fp16
-// operands, fp32 accumulation); one warp owns 16 or 32 rows (queries) and the
-// weights sit in shared memory, padded so fragment loads are conflict-free.
+// Inference runs the MLP on the fifth-generation tensor cores (tcgen05: M = 128
+// tiles, operands in shared memory, fp32 accumulator in TMEM; dtc.cuh).
+// Training's products (forward, dIn = G W and dW = G^T In over 64-record tiles)
+// run on mma.sync m16n8k16 (fp16 operands, fp32 accumulation), one warp per 16
+// or 32 rows, with the weights in shared memory padded for conflict-free
+// fragment loads.
 #include <algorithm>
 
 #include "dguide.cuh"
@@ -30,8 +33,6 @@ constexpr int kSW1 = kSW0 + kGHid * kLd48;
 constexpr int kSW2 = kSW1 + kGHid * kLd64;
 constexpr int kSW3 = kSW2 + kGHid * kLd64;
 constexpr int kSWEnd = kSW3 + kGOut * kLd64;  // 16256 halves
-constexpr int kInferWarps = 8;
-constexpr int kInferSmem = (kSWEnd + kInferWarps * 32 * kActLd) * 2;
 
 enum { kRelu = 0, kMask = 1, kF32 = 2 };
 
@@ -192,19 +193,6 @@ __device__ __forceinline__ void GuideEncodeTail(V3 N, V3 wo, __half* row) {
   *reinterpret_cast<uint32_t*>(row + 36) = PackF2(wo.y, wo.z);
   *reinterpret_cast<uint32_t*>(row + 38) = PackF2(1.f, 0.f);
   for (int k = 40; k < kGIn; k += 2) *reinterpret_cast<uint32_t*>(row + k) = 0u;
-}
-
-__device__ __forceinline__ void ZeroRow48(__half* row) {
-  for (int k = 0; k < kGIn; k += 2) *reinterpret_cast<uint32_t*>(row + k) = 0u;
-}
-
-// The four layers on the warp's 32 rows, in place; afterwards row r holds 44
-// fp32 outputs.
-__device__ __forceinline__ void WarpMlp32(const __half* sw, __half* act) {
-  WarpGemm<kGIn, kGHid, 2, kRelu>(act, kActLd, sw + kSW0, kLd48, act, kActLd, nullptr, 0);
-  WarpGemm<kGHid, kGHid, 2, kRelu>(act, kActLd, sw + kSW1, kLd64, act, kActLd, nullptr, 0);
-  WarpGemm<kGHid, kGHid, 2, kRelu>(act, kActLd, sw + kSW2, kLd64, act, kActLd, nullptr, 0);
-  WarpGemm<kGHid, kGOut, 2, kF32>(act, kActLd, sw + kSW3, kLd64, act, kActLd / 2, nullptr, 0);
 }
 
 __device__ __forceinline__ void StoreMix(const float* o, const GuideDev& G, float4* mx) {
@@ -373,58 +361,10 @@ __device__ __forceinline__ void TcTeardown(uint32_t tmem, uint64_t* mbar, uint32
 
 }  // namespace
 
-// Guided shade classes: all but emitters and rough_glass (near-delta
-// transmission gains little from a smooth directional guide).
-__global__ void __launch_bounds__(kInferWarps * 32, 2)
-    KGuideInfer(DevScene S, PathBuffers B, GuideDev G, int depth) {
-  extern __shared__ __align__(16) unsigned char smraw[];
-  __half* sw = reinterpret_cast<__half*>(smraw);
-  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-  __half* act = sw + kSWEnd + warp * 32 * kActLd;
-  LoadFwdWeights(G.weights, sw);
-  __syncthreads();
-  const uint32_t* cnt = B.counters + kClassBase + depth * kShadeClasses;
-  const uint32_t n1 = cnt[SC_DIFFUSE], n2 = cnt[SC_METAL], n4 = cnt[SC_DISNEY], n5 = cnt[SC_GENERIC];
-  const uint32_t total = n1 + n2 + n4 + n5;
-  for (uint32_t base = blockIdx.x * blockDim.x; base < total; base += gridDim.x * blockDim.x) {
-    uint32_t q = base + threadIdx.x;
-    bool valid = q < total;
-    uint32_t p = 0;
-    __half* row = act + lane * kActLd;
-    if (valid) {
-      uint32_t j = q, cls;
-      if (j < n1) {
-        cls = SC_DIFFUSE;
-      } else if ((j -= n1) < n2) {
-        cls = SC_METAL;
-      } else if ((j -= n2) < n4) {
-        cls = SC_DISNEY;
-      } else {
-        j -= n4;
-        cls = SC_GENERIC;
-      }
-      p = B.classQ[(size_t)cls * B.capacity + j];
-      HitRec h = B.hit[p];
-      float4 ro = B.rayO[p], rd = B.rayD[p];
-      V3 O{ro.x, ro.y, ro.z}, D{rd.x, rd.y, rd.z};
-      TraceHit th{h.t, h.u, h.v, h.prim, h.shape, h.front};
-      SurfInt si = ComputeSI(S, O, D, th);
-      float u[3];
-      GuidePosToUnit(G, si.P, u);
-      GuideEncodeLevels(G, u, 0, kGLevels, row);
-      GuideEncodeTail(si.sh.N, -D, row);
-    } else {
-      ZeroRow48(row);
-    }
-    __syncwarp();
-    WarpMlp32(sw, act);
-    if (valid)
-      StoreMix(reinterpret_cast<const float*>(act) + lane * (kActLd / 2), G, G.mix + (size_t)p * kGMixF4);
-    __syncwarp();
-  }
-}
-
-// KGuideInfer on tcgen05: 128 queries per tile, one per thread.
+// Per bounce, the guide network for every hit of a guided shade class (all
+// but emitters and rough_glass: near-delta transmission gains little from a
+// smooth directional guide): 128 queries per tile, one per thread, the MLP on
+// tcgen05.
 __global__ void __launch_bounds__(kTcRows, 1)
     KGuideInferTc(DevScene S, PathBuffers B, GuideDev G, int depth) {
   extern __shared__ __align__(1024) unsigned char smtc[];
@@ -470,7 +410,8 @@ __global__ void __launch_bounds__(kTcRows, 1)
   TcTeardown(tmem, mbar, phase, fail, B.counters + kMiscBase + 1);
 }
 
-// KGuideQuery on tcgen05 (the parity hook runs the same network code as inference).
+// The same network on caller-given queries (the parity hook runs the inference code):
+// queries n x 9 (P, N, wo); raw n x kGOut (optional); mix n x kGMixF4 float4 (optional).
 __global__ void __launch_bounds__(kTcRows, 1)
     KGuideQueryTc(GuideDev G, const float* queries, uint32_t n, float* raw, float4* mix, uint32_t* err) {
   extern __shared__ __align__(1024) unsigned char smtc[];
@@ -498,40 +439,6 @@ __global__ void __launch_bounds__(kTcRows, 1)
     }
   }
   TcTeardown(tmem, mbar, phase, fail, err);
-}
-
-// queries: n x 9 (P, N, wo); raw: n x kGOut (optional); mix: n x kGMixF4 float4 (optional)
-__global__ void __launch_bounds__(kInferWarps * 32, 2)
-    KGuideQuery(GuideDev G, const float* queries, uint32_t n, float* raw, float4* mix) {
-  extern __shared__ __align__(16) unsigned char smraw[];
-  __half* sw = reinterpret_cast<__half*>(smraw);
-  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-  __half* act = sw + kSWEnd + warp * 32 * kActLd;
-  LoadFwdWeights(G.weights, sw);
-  __syncthreads();
-  for (uint32_t base = blockIdx.x * blockDim.x; base < n; base += gridDim.x * blockDim.x) {
-    uint32_t q = base + threadIdx.x;
-    bool valid = q < n;
-    __half* row = act + lane * kActLd;
-    if (valid) {
-      const float* x = queries + (size_t)q * 9;
-      float u[3];
-      GuidePosToUnit(G, V3{x[0], x[1], x[2]}, u);
-      GuideEncodeLevels(G, u, 0, kGLevels, row);
-      GuideEncodeTail(V3{x[3], x[4], x[5]}, V3{x[6], x[7], x[8]}, row);
-    } else {
-      ZeroRow48(row);
-    }
-    __syncwarp();
-    WarpMlp32(sw, act);
-    if (valid) {
-      const float* o = reinterpret_cast<const float*>(act) + lane * (kActLd / 2);
-      if (raw)
-        for (int k = 0; k < kGOut; k++) raw[(size_t)q * kGOut + k] = k < kGOutUsed ? o[k] : 0.f;
-      if (mix) StoreMix(o, G, mix + (size_t)q * kGMixF4);
-    }
-    __syncwarp();
-  }
 }
 
 // Mixture pdf at given directions, and samples from u (n x 3) of packed mixtures.
@@ -815,11 +722,7 @@ __global__ void KFloatToHalf(const float* src, __half* dst, uint64_t n) {
 static int GuideGrid(int perSm) { return PathGridBlocks() / 8 * perSm; }
 
 cudaError_t GuideKernelsInit() {
-  cudaError_t e = cudaFuncSetAttribute(KGuideInfer, cudaFuncAttributeMaxDynamicSharedMemorySize, kInferSmem);
-  if (e != cudaSuccess) return e;
-  e = cudaFuncSetAttribute(KGuideQuery, cudaFuncAttributeMaxDynamicSharedMemorySize, kInferSmem);
-  if (e != cudaSuccess) return e;
-  e = cudaFuncSetAttribute(KGuideInferTc, cudaFuncAttributeMaxDynamicSharedMemorySize, kTcSmem);
+  cudaError_t e = cudaFuncSetAttribute(KGuideInferTc, cudaFuncAttributeMaxDynamicSharedMemorySize, kTcSmem);
   if (e != cudaSuccess) return e;
   e = cudaFuncSetAttribute(KGuideQueryTc, cudaFuncAttributeMaxDynamicSharedMemorySize, kTcSmem);
   if (e != cudaSuccess) return e;
