@@ -706,9 +706,9 @@ def main():
     ap.add_argument("--bdpt-depth", type=int, default=MAX_DEPTH, help="renderers: bdpt max_depth")
     ap.add_argument("--renderers-res", type=int, nargs=2, default=[W, H], help="renderers: frame size")
     ap.add_argument("--bdpt-cpu-row-step", type=int, default=8, help="renderers: oracle bdpt row sample")
-    ap.add_argument("--guided-res", type=int, nargs=2, default=[480, 270])
+    ap.add_argument("--guided-res", type=int, nargs=2, default=[240, 135])
     ap.add_argument("--guided-spheres", type=int, default=10000)
-    ap.add_argument("--guided-ref-spp", type=int, default=65536)
+    ap.add_argument("--guided-ref-spp", type=int, default=1 << 20)
     ap.add_argument("--guided-spp", type=int, nargs="+", default=[8, 16, 24, 32, 48, 64])
     ap.add_argument("--guided-config", default="{}", help="JSON of rad_guide_enable settings for the guided jobs")
     ap.add_argument("--no-tune", action="store_true", help="skip rad_autotune (keeps launch indices fixed for ncu)")

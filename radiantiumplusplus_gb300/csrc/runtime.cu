@@ -585,6 +585,8 @@ void GuideTrainWave(GuideNet& net, const GuideDev& G, ProfSink& ps, rad_job* j) 
 
 // A guided wave: the bounce loop with the guide inference stage, then (while
 // the job is in its training fraction) the training steps on its records.
+uint32_t WaveSamples(rad_job* j);
+
 void RunWaveGuided(rad_job* j) {
   Lib& lib = L();
   const DevScene& S = j->scene->dev;
@@ -595,10 +597,13 @@ void RunWaveGuided(rad_job* j) {
   ProfSink ps{j};
   FilmView film{j->accum, (int32_t)W, (int32_t)H, j->dStats};
   bool train = j->nextSample < j->trainSamples;
+  // training waves hold one sample (records and Adam steps per sample as configured); the
+  // inference-only waves after them hold several consecutive samples of a small frame, as plain waves do
+  const uint32_t k = train ? 1u : std::min(WaveSamples(j), j->spp - j->nextSample);
   for (uint64_t p0 = 0; p0 < npix; p0 += lib.maxPaths) {
-    uint32_t count = (uint32_t)std::min<uint64_t>(lib.maxPaths, npix - p0);
+    uint32_t count = (uint32_t)std::min<uint64_t>(lib.maxPaths, npix - p0) * k;
     uint32_t smp = j->first + j->nextSample;
-    WaveParams w{(uint32_t)p0, count, smp, j->seed, nullptr, nullptr};
+    WaveParams w{(uint32_t)p0, count, smp, j->seed, nullptr, nullptr, nullptr, k};
     GuideDev G = GuideView(net);
     G.mix = lib.guideMix;
     G.rec = lib.guideRec;
@@ -613,14 +618,14 @@ void RunWaveGuided(rad_job* j) {
     ps.End(0, a);
     uint64_t launches = 1 + LaunchBounces(S, j->scene->tune, count, ps, nullptr, &G);
     ps.Begin(4, a);
-    Check(LaunchAccumulate(lib.paths, film, count, lib.stream), "accumulate");
+    Check(LaunchAccumulate(lib.paths, film, count, lib.stream, nullptr, k), "accumulate");
     ps.End(4, a);
     launches++;
     j->stats.kernel_launches += launches;
     if (train) GuideTrainWave(net, G, ps, j);
   }
-  j->nextSample++;
-  j->launched += npix;
+  j->nextSample += k;
+  j->launched += npix * k;
 }
 
 // Runs the job's next sample over its pixels as replays of one captured graph
