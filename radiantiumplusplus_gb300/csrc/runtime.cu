@@ -562,12 +562,15 @@ void EnsureGuideBuffers(Lib& lib, uint32_t recCap) {
 
 // Training steps after a guided training wave: record weights, then
 // cfg.stepsPerWave Adam steps, each on every stepsPerWave-th record.
-void GuideTrainWave(GuideNet& net, const GuideDev& G, ProfSink& ps, rad_job* j) {
+// Adam steps on the wave's records: stepsPerWave per sample the wave holds, each
+// on a strided batch (every S-th record), so steps and batch sizes per training
+// sample do not depend on how many samples share a wave.
+void GuideTrainWave(GuideNet& net, const GuideDev& G, ProfSink& ps, rad_job* j, uint32_t samples) {
   Lib& lib = L();
   cudaEvent_t a = nullptr;
   ps.Begin(7, a);
   Check(LaunchGuideFinalize(lib.paths, G, lib.stream), "guide finalize");
-  uint32_t S = net.cfg.stepsPerWave;
+  uint32_t S = net.cfg.stepsPerWave * std::max(1u, samples);
   uint32_t maxBatch = (G.recCap + S - 1) / S;
   for (uint32_t s = 0; s < S; s++) {
     Check(LaunchGuideTrain(G, G.rec, G.ctl, 0, G.recCap, S, s, net.cfg.weightClamp, net.g, net.g + net.nTable,
@@ -597,9 +600,10 @@ void RunWaveGuided(rad_job* j) {
   ProfSink ps{j};
   FilmView film{j->accum, (int32_t)W, (int32_t)H, j->dStats};
   bool train = j->nextSample < j->trainSamples;
-  // training waves hold one sample (records and Adam steps per sample as configured); the
-  // inference-only waves after them hold several consecutive samples of a small frame, as plain waves do
-  const uint32_t k = train ? 1u : std::min(WaveSamples(j), j->spp - j->nextSample);
+  // a small frame's wave holds several consecutive samples, as plain waves do; a training wave
+  // stops at the end of the training fraction, and its Adam steps scale with its samples
+  uint32_t k = std::min(WaveSamples(j), j->spp - j->nextSample);
+  if (train) k = std::min(k, j->trainSamples - j->nextSample);
   for (uint64_t p0 = 0; p0 < npix; p0 += lib.maxPaths) {
     uint32_t count = (uint32_t)std::min<uint64_t>(lib.maxPaths, npix - p0) * k;
     uint32_t smp = j->first + j->nextSample;
@@ -622,7 +626,7 @@ void RunWaveGuided(rad_job* j) {
     ps.End(4, a);
     launches++;
     j->stats.kernel_launches += launches;
-    if (train) GuideTrainWave(net, G, ps, j);
+    if (train) GuideTrainWave(net, G, ps, j, k);
   }
   j->nextSample += k;
   j->launched += npix * k;
