@@ -51,7 +51,7 @@ struct GuideDev {
   uint32_t recCap;
   uint32_t train;          // append training records in this wave
   uint32_t trainSalt;      // per-wave salt of the training-path selection hash
-  uint32_t trainShift;     // a path trains when Hash(pixel ^ salt) >> (32 - shift) == 0
+  uint32_t trainShift;     // a path trains when Hash(path slot ^ salt) >> (32 - shift) == 0
   uint32_t trainDepth;     // only vertices with depth < trainDepth train
   unsigned long long* recTotal;  // optional job counter of training records
   float logKMax;           // kappa <= exp(logKMax)

@@ -285,7 +285,7 @@ __device__ __forceinline__ bool GuidedScatter(const DevScene& S, const PathBuffe
   float4 L4 = B.L[p];
   B.L[p] = make_float4(L4.x, L4.y, L4.z, pm);
   if (G.train && !discrete && (uint32_t)depth < G.trainDepth &&
-      (G.trainShift == 0u || (GuideHash32(B.pixel[p] ^ G.trainSalt) >> (32u - G.trainShift)) == 0u)) {
+      (G.trainShift == 0u || (GuideHash32(p ^ G.trainSalt) >> (32u - G.trainShift)) == 0u)) {
     uint32_t slot = atomicAdd(G.ctl, 1u);
     if (slot < G.recCap) {
       float4* r = G.rec + (size_t)slot * kGRecF4;

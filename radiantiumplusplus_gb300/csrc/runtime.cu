@@ -600,10 +600,11 @@ void RunWaveGuided(rad_job* j) {
   ProfSink ps{j};
   FilmView film{j->accum, (int32_t)W, (int32_t)H, j->dStats};
   bool train = j->nextSample < j->trainSamples;
-  // a small frame's wave holds several consecutive samples, as plain waves do; a training wave
-  // stops at the end of the training fraction, and its Adam steps scale with its samples
+  // a small frame's wave holds several consecutive samples, as plain waves do; a training wave holds
+  // at most 4 (the guide learns between waves, so the samples it shades stay close to its current
+  // state), stops at the end of the training fraction, and its Adam steps scale with its samples
   uint32_t k = std::min(WaveSamples(j), j->spp - j->nextSample);
-  if (train) k = std::min(k, j->trainSamples - j->nextSample);
+  if (train) k = std::min(std::min(k, 4u), j->trainSamples - j->nextSample);
   for (uint64_t p0 = 0; p0 < npix; p0 += lib.maxPaths) {
     uint32_t count = (uint32_t)std::min<uint64_t>(lib.maxPaths, npix - p0) * k;
     uint32_t smp = j->first + j->nextSample;
