@@ -205,6 +205,7 @@ def run_ours(args, world, rank, local):
         spp_step = 1
         # launch parameters of the traversal kernels for this scene (rad_autotune, not timed)
         tune = scene.autotune() if not args.no_tune else {"refill_busy": 20, "blocks_per_sm": 8, "leaf_frac8": 4,
+                                                             "shade_block": 128,
                                                              "best_ms": 0.0, "default_ms": 0.0}
         # traversal statistics for the roofline's algorithmic bytes (not timed)
         j = scene.submit(spp=1, first_sample=10_000, count_traversal=True)
@@ -279,6 +280,7 @@ def run_ours(args, world, rank, local):
                    "l2": "inputs larger than L2: resident scene + path state > 129 MB",
                    "scene_load_s": round(load_s, 3),
                    "autotune": {"refill_busy": tune["refill_busy"], "blocks_per_sm": tune["blocks_per_sm"],
+                                "shade_block": tune["shade_block"],
                                 "leaf_frac8": tune["leaf_frac8"],
                                 "wave_ms_tuned": round(tune["best_ms"], 3),
                                 "wave_ms_default": round(tune["default_ms"], 3)}},
@@ -352,6 +354,11 @@ def run_volume(args, world, rank, local):
         jr.wait()
         st_ref = jr.stats()
         jr.close()
+        # the same frame on the persistent single-kernel schedule (warp-voted loop parts)
+        jp = scene.submit(spp=args.steps, profile=True, vol_persistent=True, **fast)
+        jp.wait()
+        st_per = jp.stats()
+        jp.close()
         value = st["samples"] / (st["gpu_ms"] / 1000.0)
         cpu = None
         if rank == 0 and not args.no_cpu:
@@ -380,6 +387,10 @@ def run_volume(args, world, rank, local):
             "gpu_launches": st["kernel_launches"], "kernel_ms": {"vol_path": st["ms_volpath"]}, "clocks": clk,
             "mode": "the reference's delta tracking (global majorant, null collisions counted as depth) on the "
                     "fp16 grid (RAD_JOB_VOL_FP16)",
+            "schedule": "per-event wavefront (a kernel per loop part over queues; state in HBM between parts)",
+            "persistent_kernel": {"samples_per_s": st_per["samples"] / (st_per["gpu_ms"] / 1000.0),
+                                  "gpu_launches": st_per["kernel_launches"],
+                                  "schedule": "one persistent kernel, lanes vote on the loop part each warp step"},
             "unbiased_depth": {"global_majorant_samples_per_s": st_glob["samples"] / (st_glob["gpu_ms"] / 1000.0),
                                "brick_majorants_samples_per_s": st_brk["samples"] / (st_brk["gpu_ms"] / 1000.0),
                                "brick_mrays_per_s": (st_brk["rays_closest"] + st_brk["rays_shadow"])

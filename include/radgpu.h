@@ -86,6 +86,8 @@ typedef struct rad_job_desc {
 #define RAD_JOB_VOL_REAL_DEPTH 64u /* `vol_path`: null collisions count neither toward max_depth nor for
                                       Russian roulette. The reference counts them (vol_path.cpp:40-52
                                       run per loop iteration), so its truncation depends on the majorant */
+#define RAD_JOB_VOL_PERSISTENT 128u /* `vol_path`: one persistent kernel instead of the per-event wavefront
+                                       (same radiance bit for bit; no wavefront state memory) */
 #define RAD_JOB_GUIDE 8u           /* `path` only: sample directions with the scene's learned guide
                                       (one-sample MIS with the BSDF) and train it during the
                                       job's first train_fraction of samples; no reference counterpart */
@@ -275,18 +277,21 @@ RAD_API int rad_guide_grad(rad_scene* scene, const float* records, int64_t n, fl
  * fraction of a warp's busy lanes that must hold pending leaves before it tests
  * leaves (leaf_frac8 / 8), the warp refill threshold of the persistent
  * closest-hit and shadow kernels (lanes still tracing before idle lanes take new
- * rays) and the number of blocks per SM of their grids. The winner is kept in
- * the scene and used by later jobs and rad_render_samples; results do not
- * depend on it. config_json may be NULL; keys: leaf_frac8 (list, default
- * [2,3,4,5,6]), refill_busy (list, default [16,20,24,28,32]), blocks_per_sm
- * (list, default [4,6,8]), reps (timed waves per candidate, 2).
+ * rays), the number of blocks per SM of their grids, and the block size of the
+ * shade-class kernels. The winner is kept in the scene and used by later jobs,
+ * mixed waves and rad_render_samples; results do not depend on it. config_json
+ * may be NULL; keys: leaf_frac8 (list, default [2,3,4,5,6]), refill_busy (list,
+ * default [16,20,24,28,32]), blocks_per_sm (list, default [4,6,8]),
+ * shade_block (list of 64 / 128 / 256, default all three), reps (timed waves
+ * per candidate, 2).
  * RAD_ERR_UNSUPPORTED for `vol_path`, `particle_tracer` and `bdpt` scenes. */
 typedef struct rad_tune_result {
   int32_t refill_busy, blocks_per_sm; /* chosen */
   int32_t candidates;                 /* configurations timed */
   double best_ms;    /* time of one wave with the chosen parameters */
-  double default_ms; /* with the defaults (20, 8, 4), when they were timed */
+  double default_ms; /* with the defaults (20, 8, 4, 128), when they were timed */
   int32_t leaf_frac8; /* chosen */
+  int32_t shade_block; /* chosen */
 } rad_tune_result;
 RAD_API int rad_autotune(rad_scene* scene, const char* config_json, rad_tune_result* out);
 

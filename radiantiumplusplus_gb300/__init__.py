@@ -136,9 +136,9 @@ class Scene:
         return out
 
     def submit(self, spp=0, seed=None, first_sample=0, profile=False, sync=False, count_traversal=False,
-               guide=False, vol_bricks=False, vol_fp16=False, vol_real_depth=False):
+               guide=False, vol_bricks=False, vol_fp16=False, vol_real_depth=False, vol_persistent=False):
         return Job(self, spp, seed, first_sample, profile, sync, count_traversal, guide, vol_bricks, vol_fp16,
-                   vol_real_depth)
+                   vol_real_depth, vol_persistent)
 
     def autotune(self, config=None):
         """Pick the traversal launch parameters for this scene by timing waves (rad_autotune)."""
@@ -203,7 +203,7 @@ class Job:
     """One render job (rad_job_*)."""
 
     def __init__(self, scene, spp=0, seed=None, first_sample=0, profile=False, sync=False, count_traversal=False,
-                 guide=False, vol_bricks=False, vol_fp16=False, vol_real_depth=False):
+                 guide=False, vol_bricks=False, vol_fp16=False, vol_real_depth=False, vol_persistent=False):
         self.scene = scene
         flags = (_capi.RAD_JOB_PROFILE_KERNELS if profile else 0) | (_capi.RAD_JOB_SYNC if sync else 0)
         flags |= _capi.RAD_JOB_COUNT_TRAVERSAL if count_traversal else 0
@@ -211,6 +211,7 @@ class Job:
         flags |= _capi.RAD_JOB_VOL_BRICKS if vol_bricks else 0
         flags |= _capi.RAD_JOB_VOL_FP16 if vol_fp16 else 0
         flags |= _capi.RAD_JOB_VOL_REAL_DEPTH if vol_real_depth else 0
+        flags |= _capi.RAD_JOB_VOL_PERSISTENT if vol_persistent else 0
         d = _capi.JobDesc(spp, 0xFFFFFFFF if seed is None else seed, first_sample, flags)
         h = ctypes.c_void_p()
         check(lib().rad_job_submit(scene.handle, ctypes.byref(d), ctypes.byref(h)))

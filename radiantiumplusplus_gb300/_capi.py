@@ -34,6 +34,7 @@ RAD_JOB_GUIDE = 8
 RAD_JOB_VOL_BRICKS = 16
 RAD_JOB_VOL_FP16 = 32
 RAD_JOB_VOL_REAL_DEPTH = 64
+RAD_JOB_VOL_PERSISTENT = 128
 
 # Every symbol the header declares (the export test checks this list).
 EXPORTS = [
@@ -84,7 +85,8 @@ class Stats(ctypes.Structure):
 
 class TuneResult(ctypes.Structure):
     _fields_ = [("refill_busy", ctypes.c_int32), ("blocks_per_sm", ctypes.c_int32), ("candidates", ctypes.c_int32),
-                ("best_ms", ctypes.c_double), ("default_ms", ctypes.c_double), ("leaf_frac8", ctypes.c_int32)]
+                ("best_ms", ctypes.c_double), ("default_ms", ctypes.c_double), ("leaf_frac8", ctypes.c_int32),
+                ("shade_block", ctypes.c_int32)]
 
 
 class GuideInfo(ctypes.Structure):

@@ -147,7 +147,7 @@ extern "C" RAD_API int rad_render_samples_noalloc(rad_scene* scene, const uint32
     }
     for (int d = 0; d < iters; d++) {
       if (LaunchExtend(S, B, d, tgrid, st, nullptr, tu.refillBusy, tu.leafFrac8) != cudaSuccess ||
-          LaunchShade(S, B, d, grid, st) != cudaSuccess ||
+          LaunchShade(S, B, d, grid, st, nullptr, false, tu.shadeBlock) != cudaSuccess ||
           LaunchShadow(S, B, d, tgrid, st, nullptr, tu.refillBusy, tu.leafFrac8) != cudaSuccess)
         return done(RAD_ERR_CUDA, "bounce launch failed");
       if (S.maxDepth < 0 && (d % 8) == 7) {

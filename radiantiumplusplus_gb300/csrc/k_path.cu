@@ -305,8 +305,10 @@ __device__ __forceinline__ bool GuidedScatter(const DevScene& S, const PathBuffe
 // SC_EMIT: misses, emitter hits, shapes without a BSDF and the last bounce --
 // emitter MIS only, then the path ends. Other classes: hits on a non-emitter
 // shape with a BSDF of that class -- NEE, BSDF sample, Russian roulette.
+constexpr int kShadeMaxBlock = 256;  // the tuner's largest shade block
+
 template <int K, bool GUIDED, bool MIX>
-__global__ void __launch_bounds__(kBlock) KShadeClass(DevScene S0, PathBuffers B, GuideDev G, int depth) {
+__global__ void __launch_bounds__(kShadeMaxBlock) KShadeClass(DevScene S0, PathBuffers B, GuideDev G, int depth) {
   uint32_t count = B.counters[kClassBase + depth * kShadeClasses + K];
   const uint32_t* qin = B.classQ + (size_t)K * B.capacity;
   uint32_t* qout = B.q[(depth + 1) & 1];
@@ -716,29 +718,31 @@ cudaError_t LaunchExtend(const DevScene& S, const PathBuffers& B, int depth, int
   return cudaGetLastError();
 }
 cudaError_t LaunchShade(const DevScene& S, const PathBuffers& B, int depth, int grid, cudaStream_t st,
-                        const GuideDev* G, bool mix) {
+                        const GuideDev* G, bool mix, int block) {
   GuideDev none{};
+  if (block != 64 && block != 256) block = kBlock;
+  grid = std::max(1, grid * kBlock / block);
   if (mix) {  // mixed waves hold plain jobs only
-    KShadeClass<SC_EMIT, false, true><<<grid, kBlock, 0, st>>>(S, B, none, depth);
-    KShadeClass<SC_GLASS, false, true><<<grid, kBlock, 0, st>>>(S, B, none, depth);
-    KShadeClass<SC_DIFFUSE, false, true><<<grid, kBlock, 0, st>>>(S, B, none, depth);
-    KShadeClass<SC_METAL, false, true><<<grid, kBlock, 0, st>>>(S, B, none, depth);
-    KShadeClass<SC_DISNEY, false, true><<<grid, kBlock, 0, st>>>(S, B, none, depth);
-    KShadeClass<SC_GENERIC, false, true><<<grid, kBlock, 0, st>>>(S, B, none, depth);
+    KShadeClass<SC_EMIT, false, true><<<grid, block, 0, st>>>(S, B, none, depth);
+    KShadeClass<SC_GLASS, false, true><<<grid, block, 0, st>>>(S, B, none, depth);
+    KShadeClass<SC_DIFFUSE, false, true><<<grid, block, 0, st>>>(S, B, none, depth);
+    KShadeClass<SC_METAL, false, true><<<grid, block, 0, st>>>(S, B, none, depth);
+    KShadeClass<SC_DISNEY, false, true><<<grid, block, 0, st>>>(S, B, none, depth);
+    KShadeClass<SC_GENERIC, false, true><<<grid, block, 0, st>>>(S, B, none, depth);
     return cudaGetLastError();
   }
-  KShadeClass<SC_EMIT, false, false><<<grid, kBlock, 0, st>>>(S, B, none, depth);
-  KShadeClass<SC_GLASS, false, false><<<grid, kBlock, 0, st>>>(S, B, none, depth);
+  KShadeClass<SC_EMIT, false, false><<<grid, block, 0, st>>>(S, B, none, depth);
+  KShadeClass<SC_GLASS, false, false><<<grid, block, 0, st>>>(S, B, none, depth);
   if (G) {
-    KShadeClass<SC_DIFFUSE, true, false><<<grid, kBlock, 0, st>>>(S, B, *G, depth);
-    KShadeClass<SC_METAL, true, false><<<grid, kBlock, 0, st>>>(S, B, *G, depth);
-    KShadeClass<SC_DISNEY, true, false><<<grid, kBlock, 0, st>>>(S, B, *G, depth);
-    KShadeClass<SC_GENERIC, true, false><<<grid, kBlock, 0, st>>>(S, B, *G, depth);
+    KShadeClass<SC_DIFFUSE, true, false><<<grid, block, 0, st>>>(S, B, *G, depth);
+    KShadeClass<SC_METAL, true, false><<<grid, block, 0, st>>>(S, B, *G, depth);
+    KShadeClass<SC_DISNEY, true, false><<<grid, block, 0, st>>>(S, B, *G, depth);
+    KShadeClass<SC_GENERIC, true, false><<<grid, block, 0, st>>>(S, B, *G, depth);
   } else {
-    KShadeClass<SC_DIFFUSE, false, false><<<grid, kBlock, 0, st>>>(S, B, none, depth);
-    KShadeClass<SC_METAL, false, false><<<grid, kBlock, 0, st>>>(S, B, none, depth);
-    KShadeClass<SC_DISNEY, false, false><<<grid, kBlock, 0, st>>>(S, B, none, depth);
-    KShadeClass<SC_GENERIC, false, false><<<grid, kBlock, 0, st>>>(S, B, none, depth);
+    KShadeClass<SC_DIFFUSE, false, false><<<grid, block, 0, st>>>(S, B, none, depth);
+    KShadeClass<SC_METAL, false, false><<<grid, block, 0, st>>>(S, B, none, depth);
+    KShadeClass<SC_DISNEY, false, false><<<grid, block, 0, st>>>(S, B, none, depth);
+    KShadeClass<SC_GENERIC, false, false><<<grid, block, 0, st>>>(S, B, none, depth);
   }
   return cudaGetLastError();
 }

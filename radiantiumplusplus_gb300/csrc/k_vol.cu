@@ -1,10 +1,13 @@
-// `vol_path` integrator (VolPath::Li, rad.offline/src/renderer/vol_path.cpp:27-349)
-// as one thread per path sample running the whole delta-tracking loop: free
-// flights against the medium majorant (medium.cpp:19-43), null / real
+// `vol_path` integrator (VolPath::Li, rad.offline/src/renderer/vol_path.cpp:27-349):
+// free flights against the medium majorant (medium.cpp:19-43), null / real
 // collisions with hero-channel spectral MIS, phase-function NEE with the
 // ratio-tracking transmittance loop (vol_path.cpp:224-342) and index-matched
-// boundaries. Camera rays and PCG streams come from the wavefront generate
-// stage; the radiance goes to the path's L slot for the accumulate stage.
+// boundaries. The loop is cut into parts that a path runs in order (VolAct);
+// two schedules run them: a per-event wavefront (one kernel per part over a
+// queue of the paths at that part, state in HBM between parts) and a
+// persistent kernel (lanes vote on the part to run each warp step). Camera
+// rays and PCG streams come from the generate stage; the radiance goes to the
+// path's L slot for the accumulate stage.
 #include <algorithm>
 
 #include "dbsdf.cuh"
@@ -234,7 +237,7 @@ RDN bool NeeStep(const DevScene& S, Pcg32& rng, int channel, NeeState& n, uint32
 // Per-path state of the `vol_path` loop (VolPath::Li's locals), so that a lane
 // can run a path one loop iteration at a time and take a new path when its own
 // ends (KVolPath).
-struct VolPathState {
+struct alignas(16) VolPathState {
   VRay ray;
   V3 thr, result, prevP;
   float eta, prevPdf;
@@ -259,6 +262,7 @@ struct VolPathState {
 // per warp step.
 constexpr int kActTop = 0, kActScatter = 1, kActSurface = 2, kActNee = 3, kActScatterEnd = 4, kActSurfaceEnd = 5;
 constexpr int kActs = 6;
+static_assert(kActs == kVolActs, "one wavefront queue per loop part");
 
 RD void VolInit(const DevScene& S, VolPathState& p, VRay ray, Pcg32 rng) {
   p.ray = ray;
@@ -591,6 +595,102 @@ __global__ void __launch_bounds__(kVolBlock, 5)
   if (nShadow) atomicAdd(B.counters + kMiscBase + 3, (uint32_t)nShadow);
 }
 
+// ---- per-event wavefront ------------------------------------------------------
+// Part order within a round: top, scatter, surface, NEE, scatter end, surface
+// end. Every part hands its paths to a later part of the same round, except the
+// loop's increment (scatter end, surface end, an index-matched boundary), which
+// queues the path for the next round's top: queues of the current round have
+// parity `cur`, the next round's top queue parity cur ^ 1.
+size_t VolStateBytes() { return sizeof(VolPathState); }
+
+RD uint32_t VolQueueOf(int act, uint32_t cur) { return (act == kActTop ? (cur ^ 1u) : cur) * kVolActs + (uint32_t)act; }
+
+// Appends idx to queue `dst` for every lane with dst >= 0; all lanes of the warp
+// call it. One atomic per destination and warp.
+RD void VolPush(const VolWave& V, int dst, uint32_t idx) {
+  const uint32_t lane = threadIdx.x & 31u;
+  const uint32_t same = __match_any_sync(0xffffffffu, (uint32_t)dst);
+  const int leader = __ffs(same) - 1;
+  uint32_t base = 0;
+  if ((int)lane == leader && dst >= 0) base = atomicAdd(V.cnt + dst, (uint32_t)__popc(same));
+  base = __shfl_sync(0xffffffffu, base, leader);
+  if (dst >= 0) V.q[(size_t)dst * V.capacity + base + __popc(same & ((1u << lane) - 1u))] = idx;
+}
+
+// One loop part over its queue. A lane runs its path's part (the top repeats
+// through null collisions, the NEE through its transmittance steps) until the
+// path moves to another part, stores the state, queues the path there and
+// takes the next one from this part's queue. FRESH (first round's top): the
+// queue is the wave's paths 0..count-1, started from the generate stage's rays.
+template <int ACT, bool FRESH, bool BRICKS, bool HALF>
+__global__ void __launch_bounds__(kVolBlock, 4)
+    KVolEvent(DevScene S, PathBuffers B, VolWave V, uint32_t count, uint32_t cur, uint32_t* err, uint32_t mode) {
+  const uint32_t lane = threadIdx.x & 31u;
+  const uint32_t in = cur * kVolActs + (uint32_t)ACT;
+  const uint32_t n = FRESH ? count : V.cnt[in];
+  uint32_t* head = V.cnt + 2 * kVolActs + ACT;
+  VolPathState* states = static_cast<VolPathState*>(V.state);
+  VolPathState p;
+  uint32_t idx = 0, ended = 0;
+  bool live = false, drained = n == 0;
+  unsigned long long nRays = 0, nShadow = 0;
+  for (;;) {
+    const uint32_t need = __ballot_sync(0xffffffffu, !live);
+    if (need && !drained) {
+      const int leader = __ffs(need) - 1;
+      uint32_t base = 0;
+      if ((int)lane == leader) base = atomicAdd(head, (uint32_t)__popc(need));
+      base = __shfl_sync(0xffffffffu, base, leader);
+      if (base + (uint32_t)__popc(need) >= n) drained = true;
+      if (!live) {
+        const uint32_t i = base + __popc(need & ((1u << lane) - 1u));
+        if (i < n) {
+          if (FRESH) {
+            idx = i;
+            const float4 ro = B.rayO[idx], rd = B.rayD[idx];
+            const uint2 rs = B.rng[idx];
+            Pcg32 rng;
+            rng.state = ((uint64_t)rs.y << 32) | rs.x;
+            VolInit(S, p, VRay{V3{ro.x, ro.y, ro.z}, V3{rd.x, rd.y, rd.z}, ro.w, rd.w}, rng);
+          } else {
+            idx = V.q[(size_t)in * V.capacity + i];
+            p = states[idx];
+          }
+          live = true;
+        }
+      }
+    }
+    if (__ballot_sync(0xffffffffu, live) == 0u) break;
+    int dst = -1;
+    if (live) {
+      if (!VolAct<BRICKS, HALF>(S, p, ACT, mode, err)) {
+        B.L[idx] = make_float4(p.result.x, p.result.y, p.result.z, 0.f);
+        nRays += p.nRays;
+        nShadow += p.nShadow;
+        ended++;
+        live = false;
+      } else if (p.act != ACT) {
+        states[idx] = p;
+        dst = (int)VolQueueOf(p.act, cur);
+        live = false;
+      }
+    }
+    if (__ballot_sync(0xffffffffu, dst >= 0) != 0u) VolPush(V, dst, idx);
+  }
+  if (nRays) atomicAdd(B.counters + kMiscBase + 2, (uint32_t)nRays);
+  if (nShadow) atomicAdd(B.counters + kMiscBase + 3, (uint32_t)nShadow);
+  if (ended) atomicAdd(V.cnt + kVolEndedWord, ended);
+}
+
+// End of a round: the current parity's queues and every head start empty.
+__global__ void KVolRoundEnd(VolWave V, uint32_t cur) {
+  const uint32_t t = threadIdx.x;
+  if (t < (uint32_t)kVolActs) {
+    V.cnt[cur * kVolActs + t] = 0u;
+    V.cnt[2 * kVolActs + t] = 0u;
+  }
+}
+
 #ifndef RAD_HOST_EMULATION
 cudaError_t LaunchVolPath(const DevScene& S, const PathBuffers& B, const WaveParams& w, uint32_t* err,
                           cudaStream_t st, uint32_t mode) {
@@ -606,6 +706,61 @@ cudaError_t LaunchVolPath(const DevScene& S, const PathBuffers& B, const WavePar
     default: KVolPath<true, true><<<blocks, kVolBlock, 0, st>>>(S, B, w.count, err, mode); break;
   }
   return cudaGetLastError();
+}
+
+template <bool BRICKS, bool HALF>
+static cudaError_t VolRound(const DevScene& S, const PathBuffers& B, const VolWave& V, uint32_t count, uint32_t r,
+                            int blocks, uint32_t* err, cudaStream_t st, uint32_t mode) {
+  const uint32_t cur = r & 1u;
+  if (r == 0)
+    KVolEvent<kActTop, true, BRICKS, HALF><<<blocks, kVolBlock, 0, st>>>(S, B, V, count, cur, err, mode);
+  else
+    KVolEvent<kActTop, false, BRICKS, HALF><<<blocks, kVolBlock, 0, st>>>(S, B, V, count, cur, err, mode);
+  KVolEvent<kActScatter, false, BRICKS, HALF><<<blocks, kVolBlock, 0, st>>>(S, B, V, count, cur, err, mode);
+  KVolEvent<kActSurface, false, BRICKS, HALF><<<blocks, kVolBlock, 0, st>>>(S, B, V, count, cur, err, mode);
+  KVolEvent<kActNee, false, BRICKS, HALF><<<blocks, kVolBlock, 0, st>>>(S, B, V, count, cur, err, mode);
+  KVolEvent<kActScatterEnd, false, BRICKS, HALF><<<blocks, kVolBlock, 0, st>>>(S, B, V, count, cur, err, mode);
+  KVolEvent<kActSurfaceEnd, false, BRICKS, HALF><<<blocks, kVolBlock, 0, st>>>(S, B, V, count, cur, err, mode);
+  KVolRoundEnd<<<1, 32, 0, st>>>(V, cur);
+  return cudaGetLastError();
+}
+
+cudaError_t LaunchVolWavefront(const DevScene& S, const PathBuffers& B, const VolWave& V, const WaveParams& w,
+                               uint32_t* err, cudaStream_t st, uint32_t mode, uint32_t* hostCounts,
+                               uint64_t* launches) {
+  if (w.count == 0) return cudaSuccess;
+  if (w.count > V.capacity) return cudaErrorInvalidValue;
+  cudaError_t e = cudaMemsetAsync(V.cnt, 0, kVolCountWords * sizeof(uint32_t), st);
+  if (e != cudaSuccess) return e;
+  int perSm = 0;
+  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&perSm, KVolEvent<kActTop, false, false, true>, kVolBlock, 0);
+  const int cap = PathGridBlocks() / 8 * (perSm > 0 ? perSm : 4);
+  const int blocks = (int)std::min<uint32_t>((w.count + kVolBlock - 1) / kVolBlock, (uint32_t)cap);
+  // At the end of a round every live path waits in the next round's top queue,
+  // so ended + queued = count, and the wave is done when that queue is empty.
+  // The counters are read back every 4 rounds from round 8 on (a path ends
+  // within max_depth rounds unless null collisions are free or it crosses
+  // index-matched boundaries). Every round advances each live path by at least
+  // one loop iteration, so the per-path iteration bound bounds the rounds.
+  for (uint32_t r = 0; r <= (uint32_t)kMaxVolIter; r++) {
+    switch (mode & (kVolBricks | kVolHalf)) {
+      case 0: e = VolRound<false, false>(S, B, V, w.count, r, blocks, err, st, mode); break;
+      case kVolBricks: e = VolRound<true, false>(S, B, V, w.count, r, blocks, err, st, mode); break;
+      case kVolHalf: e = VolRound<false, true>(S, B, V, w.count, r, blocks, err, st, mode); break;
+      default: e = VolRound<true, true>(S, B, V, w.count, r, blocks, err, st, mode); break;
+    }
+    if (e != cudaSuccess) return e;
+    if (launches) *launches += kVolActs + 1;
+    if (r + 1 >= 8 && (r + 1) % 4 == 0) {
+      e = cudaMemcpyAsync(hostCounts, V.cnt, kVolCountWords * sizeof(uint32_t), cudaMemcpyDeviceToHost, st);
+      if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+      if (e != cudaSuccess) return e;
+      const uint32_t queued = hostCounts[((r & 1u) ^ 1u) * kVolActs + kActTop];
+      if ((uint64_t)hostCounts[kVolEndedWord] + queued != w.count) return cudaErrorIllegalState;
+      if (queued == 0) return cudaSuccess;
+    }
+  }
+  return cudaErrorIllegalState;
 }
 
 #endif  // RAD_HOST_EMULATION

@@ -129,17 +129,20 @@ cudaError_t LaunchGenerate(const DevScene& S, const PathBuffers& B, const WavePa
 // the autotuner (rad_autotune): a warp refills its idle lanes once fewer than
 // refillBusy lanes are still tracing; it tests pending leaves once at least
 // leafFrac8 / 8 of its busy lanes hold some; grids hold blocksPerSm blocks per SM.
+// The shade-class kernels run blocks of shadeBlock threads (64, 128 or 256).
 struct TraceTune {
   int32_t refillBusy = 20;
   int32_t blocksPerSm = 8;
   int32_t leafFrac8 = 4;
+  int32_t shadeBlock = 128;
 };
 // trav (optional, 4 x u64): extend node visits, extend prim tests, shadow node visits, shadow prim tests
 cudaError_t LaunchExtend(const DevScene& S, const PathBuffers& B, int depth, int grid, cudaStream_t st,
                          unsigned long long* trav = nullptr, int refillBusy = 20, int leafFrac8 = 4, bool mix = false);
 // G (optional): guide network; its classes then sample the one-sample MIS mixture.
+// grid counts blocks of 128 threads; with block != 128 the grid keeps the same number of threads.
 cudaError_t LaunchShade(const DevScene& S, const PathBuffers& B, int depth, int grid, cudaStream_t st,
-                        const GuideDev* G = nullptr, bool mix = false);
+                        const GuideDev* G = nullptr, bool mix = false, int block = 128);
 // Mixed waves: generate (w.count = paths of all jobs, w.spw = number of jobs in
 // B.mix) and accumulate (into each job's film, in sample order per pixel).
 cudaError_t LaunchGenerateMix(const PathBuffers& B, uint32_t total, uint32_t nJobs, cudaStream_t st);
@@ -222,10 +225,35 @@ cudaError_t LaunchAccumulate(const PathBuffers& B, const FilmView& film, uint32_
 cudaError_t LaunchGatherRadiance(const PathBuffers& B, uint32_t count, float* out, cudaStream_t st);
 cudaError_t LaunchResolveFilm(const FilmView& film, float scale, float* out, cudaStream_t st);
 
-// ---- volumetric path tracer (k_vol.cu): one thread per path, full Li loop
+// ---- volumetric path tracer (k_vol.cu)
 // mode bits kVolBricks / kVolHalf / kVolRealDepth: see dvol.cuh
+// Persistent kernel: lanes run their paths one part of a loop iteration at a
+// time, every warp step the part most lanes are at; needs no memory beyond B.
 cudaError_t LaunchVolPath(const DevScene& S, const PathBuffers& B, const WaveParams& w, uint32_t* err,
                           cudaStream_t st, uint32_t mode = 0);
+// Per-event wavefront: the loop parts (top / medium scatter / surface / NEE
+// transmittance / scatter end / surface end) as kernels over queues of the
+// paths at each part, path state in HBM between them. The same arithmetic per
+// path as LaunchVolPath, so the same radiance bit for bit.
+constexpr int kVolActs = 6;
+// counter words: [par * kVolActs + act] queue lengths (two parities),
+// [2 kVolActs + act] queue heads, [3 kVolActs] paths ended
+constexpr int kVolEndedWord = 3 * kVolActs;
+constexpr int kVolCountWords = 3 * kVolActs + 1;
+struct VolWave {
+  void* state;        // capacity per-path loop states (VolStateBytes() each, 16-byte aligned)
+  uint32_t* q;        // [2 * kVolActs][capacity] path indices
+  uint32_t* cnt;      // kVolCountWords counters
+  uint32_t capacity;
+};
+size_t VolStateBytes();
+// Runs the wave's rounds; host-side it waits on the stream every few rounds to
+// see whether every path has ended (hostCounts: pinned, kVolCountWords words).
+// launches: kernels run. cudaErrorIllegalState if the path count is not
+// conserved (a path neither ended nor queued).
+cudaError_t LaunchVolWavefront(const DevScene& S, const PathBuffers& B, const VolWave& V, const WaveParams& w,
+                               uint32_t* err, cudaStream_t st, uint32_t mode, uint32_t* hostCounts,
+                               uint64_t* launches);
 
 // ---- guide network (k_guide.cu)
 cudaError_t GuideKernelsInit();

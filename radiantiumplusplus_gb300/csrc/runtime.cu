@@ -217,6 +217,11 @@ struct Lib {
   BdptBuffers bdpt{};
   std::vector<void*> bdptAllocs;
   uint64_t bdptBytes = 0;
+  // vol_path wavefront: per-path loop states and part queues, allocated with the first vol_path wave
+  VolWave vol{};
+  std::vector<void*> volAllocs;
+  uint64_t volBytes = 0;
+  uint32_t* hVolWord = nullptr;  // pinned, kVolCountWords words
 };
 
 // Never destroyed: at process exit the worker thread may still be parked on
@@ -344,6 +349,23 @@ constexpr uint64_t kBdptScratchBytes = 4ull << 30;
 
 int BdptCap(const DevScene& S) {
   return S.maxDepth >= 0 ? std::min(kMaxBdptVertices, S.maxDepth + 2) : kMaxBdptVertices;
+}
+
+const VolWave& EnsureVolWave() {
+  Lib& lib = L();
+  if (lib.vol.state) return lib.vol;
+  const uint32_t P = lib.maxPaths;
+  VolWave V{};
+  auto& o = lib.volAllocs;
+  uint64_t& b = lib.volBytes;
+  V.state = DevAlloc<uint8_t>((size_t)P * VolStateBytes(), o, b);
+  V.q = DevAlloc<uint32_t>((size_t)2 * kVolActs * P, o, b);
+  V.cnt = DevAlloc<uint32_t>(kVolCountWords, o, b);
+  V.capacity = P;
+  if (!lib.hVolWord) Check(cudaMallocHost(&lib.hVolWord, kVolCountWords * sizeof(uint32_t)), "cudaMallocHost");
+  lib.used += b;
+  lib.vol = V;
+  return lib.vol;
 }
 
 const BdptBuffers& EnsureBdpt(int cap) {
@@ -503,7 +525,7 @@ uint64_t LaunchBounces(const DevScene& S, const TraceTune& tu, uint32_t count, P
       launches++;
     }
     ps.Begin(2, a);
-    Check(LaunchShade(S, lib.paths, d, grid, lib.stream, G), "shade");
+    Check(LaunchShade(S, lib.paths, d, grid, lib.stream, G, false, tu.shadeBlock), "shade");
     ps.End(2, a);
     ps.Begin(3, a);
     Check(LaunchShadow(S, lib.paths, d, tgrid, lib.stream, trav, tu.refillBusy, tu.leafFrac8), "shadow");
@@ -901,7 +923,7 @@ void RunMixedWave(const std::vector<rad_job*>& js) {
   Check(LaunchGenerateMix(B, count, n, lib.stream), "generate");
   for (int d = 0; d < iters; d++) {
     Check(LaunchExtend(S0, B, d, tgrid, lib.stream, nullptr, tu.refillBusy, tu.leafFrac8, true), "extend");
-    Check(LaunchShade(S0, B, d, grid, lib.stream, nullptr, true), "shade");
+    Check(LaunchShade(S0, B, d, grid, lib.stream, nullptr, true, tu.shadeBlock), "shade");
     Check(LaunchShadow(S0, B, d, tgrid, lib.stream, nullptr, tu.refillBusy, tu.leafFrac8, true), "shadow");
   }
   Check(LaunchAccumulateMix(B, totalPix, count, n, lib.stream), "accumulate");
@@ -951,9 +973,15 @@ void RunWave(rad_job* j) {
       ps.Begin(5, a);
       uint32_t mode = ((j->flags & RAD_JOB_VOL_BRICKS) ? kVolBricks : 0u) | ((j->flags & RAD_JOB_VOL_FP16) ? kVolHalf : 0u) |
                       ((j->flags & RAD_JOB_VOL_REAL_DEPTH) ? kVolRealDepth : 0u);
-      Check(LaunchVolPath(S, lib.paths, w, lib.paths.counters + kMiscBase + 1, lib.stream, mode), "vol_path");
+      uint32_t* err = lib.paths.counters + kMiscBase + 1;
+      if (j->flags & RAD_JOB_VOL_PERSISTENT) {
+        Check(LaunchVolPath(S, lib.paths, w, err, lib.stream, mode), "vol_path");
+        launches++;
+      } else {
+        Check(LaunchVolWavefront(S, lib.paths, EnsureVolWave(), w, err, lib.stream, mode, lib.hVolWord, &launches),
+              "vol_path wavefront");
+      }
       ps.End(5, a);
-      launches++;
     } else {
       launches += LaunchBounces(S, j->scene->tune, count, ps,
                                 (j->flags & RAD_JOB_COUNT_TRAVERSAL) ? j->dStats + 4 : nullptr);
@@ -1467,6 +1495,12 @@ int rad_shutdown(void) {
     lib.used -= lib.bdptBytes;
     lib.bdptBytes = 0;
     lib.bdpt = BdptBuffers{};
+    FreeAll(lib.volAllocs);
+    lib.used -= lib.volBytes;
+    lib.volBytes = 0;
+    lib.vol = VolWave{};
+    if (lib.hVolWord) cudaFreeHost(lib.hVolWord);
+    lib.hVolWord = nullptr;
     if (lib.hCounters) cudaFreeHost(lib.hCounters);
     lib.hCounters = nullptr;
     if (lib.mixHost) cudaFreeHost(lib.mixHost);
@@ -1892,7 +1926,9 @@ int rad_render_samples(rad_scene* scene, const uint32_t* pixels, const uint32_t*
       }
       Check(LaunchGenerate(scene->dev, lib.paths, w, lib.stream), "generate");
       if (scene->dev.isVol) {
-        Check(LaunchVolPath(scene->dev, lib.paths, w, lib.paths.counters + kMiscBase + 1, lib.stream), "vol_path");
+        Check(LaunchVolWavefront(scene->dev, lib.paths, EnsureVolWave(), w, lib.paths.counters + kMiscBase + 1,
+                                 lib.stream, 0u, lib.hVolWord, nullptr),
+              "vol_path wavefront");
       } else {
         LaunchBounces(scene->dev, scene->tune, count, ps);
       }
@@ -2089,7 +2125,7 @@ int rad_autotune(rad_scene* scene, const char* config_json, rad_tune_result* out
   return Guard([&] {
     EnsureInit();
     int reps = 2;
-    std::vector<int> leaf = {2, 3, 4, 5, 6}, refill = {16, 20, 24, 28, 32}, perSm = {4, 6, 8};
+    std::vector<int> leaf = {2, 3, 4, 5, 6}, refill = {16, 20, 24, 28, 32}, perSm = {4, 6, 8}, shade = {64, 128, 256};
     if (config_json && *config_json) {
       JValue c = JsonReader::Parse(config_json);
       if (const JValue* v = c.get("reps")) reps = std::max(1, (int)v->n);
@@ -2107,6 +2143,9 @@ int rad_autotune(rad_scene* scene, const char* config_json, rad_tune_result* out
       list("leaf_frac8", leaf, 1, 8);
       list("refill_busy", refill, 1, 32);
       list("blocks_per_sm", perSm, 1, 8);
+      list("shade_block", shade, 64, 256);
+      for (int v : shade)
+        if (v != 64 && v != 128 && v != 256) throw Error{RAD_ERR_INVALID_ARG, "shade_block values are 64, 128 or 256"};
     }
     Lib& lib = L();
     std::lock_guard<std::mutex> g(lib.gpuMu);
@@ -2124,7 +2163,7 @@ int rad_autotune(rad_scene* scene, const char* config_json, rad_tune_result* out
     auto time = [&](const TraceTune& tu) -> float {
       for (const auto& t : timed)
         if (t.first.refillBusy == tu.refillBusy && t.first.blocksPerSm == tu.blocksPerSm &&
-            t.first.leafFrac8 == tu.leafFrac8)
+            t.first.leafFrac8 == tu.leafFrac8 && t.first.shadeBlock == tu.shadeBlock)
           return t.second;
       wave(tu);  // warm-up
       Check(cudaEventRecord(a, lib.stream), "event");
@@ -2143,6 +2182,7 @@ int rad_autotune(rad_scene* scene, const char* config_json, rad_tune_result* out
     if (std::find(leaf.begin(), leaf.end(), best.leafFrac8) == leaf.end()) best.leafFrac8 = leaf[0];
     if (std::find(refill.begin(), refill.end(), best.refillBusy) == refill.end()) best.refillBusy = refill[0];
     if (std::find(perSm.begin(), perSm.end(), best.blocksPerSm) == perSm.end()) best.blocksPerSm = perSm[0];
+    if (std::find(shade.begin(), shade.end(), best.shadeBlock) == shade.end()) best.shadeBlock = shade[0];
     float bestMs = time(best);
     auto axis = [&](const std::vector<int>& vals, int32_t TraceTune::*field) {
       for (int v : vals) {
@@ -2158,7 +2198,9 @@ int rad_autotune(rad_scene* scene, const char* config_json, rad_tune_result* out
     axis(leaf, &TraceTune::leafFrac8);
     axis(refill, &TraceTune::refillBusy);
     axis(perSm, &TraceTune::blocksPerSm);
+    axis(shade, &TraceTune::shadeBlock);
     rad_tune_result res{};
+    res.shade_block = best.shadeBlock;
     res.refill_busy = best.refillBusy;
     res.blocks_per_sm = best.blocksPerSm;
     res.leaf_frac8 = best.leafFrac8;
@@ -2167,7 +2209,7 @@ int rad_autotune(rad_scene* scene, const char* config_json, rad_tune_result* out
     const TraceTune def;
     for (const auto& t : timed)
       if (t.first.refillBusy == def.refillBusy && t.first.blocksPerSm == def.blocksPerSm &&
-          t.first.leafFrac8 == def.leafFrac8)
+          t.first.leafFrac8 == def.leafFrac8 && t.first.shadeBlock == def.shadeBlock)
         res.default_ms = t.second;
     lib.evPool.push_back(a);
     lib.evPool.push_back(b);

@@ -186,6 +186,31 @@ struct HostPaths {
   }
 };
 
+// vol_path as the per-event wavefront: the rounds of part kernels of
+// LaunchVolWavefront, each over a grid of two one-lane warps, until every path
+// has ended.
+constexpr uint32_t kHemuVolWavefront = 256u;
+template <bool BRICKS>
+void VolWavefront(const DevScene& S, PathBuffers& B, uint32_t n, uint32_t* err, uint32_t mode) {
+  std::vector<VolPathState> states(n);
+  std::vector<uint32_t> q((size_t)2 * kVolActs * n, 0u), cnt(kVolCountWords, 0u);
+  VolWave V{states.data(), q.data(), cnt.data(), n};
+  for (uint32_t r = 0; cnt[kVolEndedWord] < n; r++) {
+    if (r > 4096) throw std::runtime_error("vol_path wavefront: paths left after 4096 rounds");
+    const uint32_t cur = r & 1u;
+    if (r == 0)
+      Grid(1, 2, [&] { KVolEvent<kActTop, true, BRICKS, false>(S, B, V, n, cur, err, mode); });
+    else
+      Grid(1, 2, [&] { KVolEvent<kActTop, false, BRICKS, false>(S, B, V, n, cur, err, mode); });
+    Grid(1, 2, [&] { KVolEvent<kActScatter, false, BRICKS, false>(S, B, V, n, cur, err, mode); });
+    Grid(1, 2, [&] { KVolEvent<kActSurface, false, BRICKS, false>(S, B, V, n, cur, err, mode); });
+    Grid(1, 2, [&] { KVolEvent<kActNee, false, BRICKS, false>(S, B, V, n, cur, err, mode); });
+    Grid(1, 2, [&] { KVolEvent<kActScatterEnd, false, BRICKS, false>(S, B, V, n, cur, err, mode); });
+    Grid(1, 2, [&] { KVolEvent<kActSurfaceEnd, false, BRICKS, false>(S, B, V, n, cur, err, mode); });
+    Grid(1, 32, [&] { KVolRoundEnd(V, cur); });
+  }
+}
+
 // The wave of rad_render_samples: generate, then the bounce loop (extend, the
 // shade classes, shadow) or the vol_path kernel, with the kernels' own code.
 // Traversal refills a lane as soon as it is idle (a warp of one lane), which
@@ -199,7 +224,13 @@ void RenderSamples(const DevScene& S, const uint32_t* pix, const uint32_t* smp, 
   Grid((gen + kBlock - 1) / kBlock, kBlock, [&] { KGenerate(S, B, w); });
   uint32_t* err = B.counters + kMiscBase + 1;
   GuideDev none{};
-  if (S.isVol) {
+  if (S.isVol && (volMode & kHemuVolWavefront)) {
+    if (volMode & kVolHalf) throw std::runtime_error("the fp16 grid is not emulated");
+    if (volMode & kVolBricks)
+      VolWavefront<true>(S, B, n, err, volMode & ~kHemuVolWavefront);
+    else
+      VolWavefront<false>(S, B, n, err, volMode & ~kHemuVolWavefront);
+  } else if (S.isVol) {
     switch (volMode & (kVolBricks | kVolHalf)) {
       case 0: Grid(1, 1, [&] { KVolPath<false, false>(S, B, n, err, volMode); }); break;
       case kVolBricks: Grid(1, 1, [&] { KVolPath<true, false>(S, B, n, err, volMode); }); break;

@@ -90,15 +90,19 @@ def test_autotune_picks_parameters_and_keeps_results(rad, scene_dir):
     s = rad.Scene.from_file(spheres(scene_dir, 200, 3, 40, 24, 5)[0])
     before = s.render(spp=3, seed=7)
     r = s.autotune({"reps": 1})
-    assert r["candidates"] == 11 and r["refill_busy"] in (16, 20, 24, 28, 32) and r["blocks_per_sm"] in (4, 6, 8)
-    assert r["leaf_frac8"] in (2, 3, 4, 5, 6)
+    assert r["candidates"] == 13 and r["refill_busy"] in (16, 20, 24, 28, 32) and r["blocks_per_sm"] in (4, 6, 8)
+    assert r["leaf_frac8"] in (2, 3, 4, 5, 6) and r["shade_block"] in (64, 128, 256)
     assert r["best_ms"] > 0 and r["best_ms"] <= r["default_ms"]
     assert np.array_equal(before, s.render(spp=3, seed=7))
-    r2 = s.autotune({"refill_busy": [1, 32], "blocks_per_sm": [2], "leaf_frac8": [8], "reps": 1})
-    assert r2["candidates"] == 2 and r2["blocks_per_sm"] == 2 and r2["leaf_frac8"] == 8
+    r2 = s.autotune({"refill_busy": [1, 32], "blocks_per_sm": [2], "leaf_frac8": [8], "shade_block": [256], "reps": 1})
+    assert r2["candidates"] == 2 and r2["blocks_per_sm"] == 2 and r2["leaf_frac8"] == 8 and r2["shade_block"] == 256
     assert np.array_equal(before, s.render(spp=3, seed=7))
-    with pytest.raises(rad.RadError):
-        s.autotune({"refill_busy": [40]})
+    r3 = s.autotune({"refill_busy": [24], "blocks_per_sm": [8], "leaf_frac8": [3], "shade_block": [64], "reps": 1})
+    assert r3["shade_block"] == 64
+    assert np.array_equal(before, s.render(spp=3, seed=7))
+    for bad in ({"refill_busy": [40]}, {"shade_block": [96]}):
+        with pytest.raises(rad.RadError):
+            s.autotune(bad)
     s.close()
 
 

@@ -14,6 +14,8 @@ transcendentals in the host harness. bdpt (not emulated by the harness) keeps
 a fraction bound only.
 """
 
+import os
+
 import numpy as np
 import pytest
 
@@ -298,6 +300,49 @@ def test_volpath_modes_keep_the_expectation(rad, scene_dir, base, flags):
     am, bm = a.mean(axis=(1, 2, 3)), b.mean(axis=(1, 2, 3))
     zt = (bm.mean() - am.mean()) / np.sqrt(am.var(ddof=1) / am.size + bm.var(ddof=1) / bm.size)
     assert abs(zt) < 4.0, zt
+    s.close()
+
+
+@pytest.mark.parametrize("flags", [{}, {"vol_fp16": True}, {"vol_real_depth": True}, {"vol_bricks": True},
+                                   {"vol_bricks": True, "vol_fp16": True}])
+def test_volpath_wavefront_equals_persistent(rad, scene_dir, flags):
+    """The per-event wavefront (default) and the persistent kernel run the same
+    loop parts in the same order per path: job films, ray counts and the 256^3
+    fBm frame's samples are bit-identical."""
+    path, text, d = volume(scene_dir, 48, 40, 4, grid=32)
+    s = rad.Scene.from_file(path)
+    films, rays = [], []
+    for persistent in (False, True):
+        j = s.submit(spp=6, seed=17, vol_persistent=persistent, **flags)
+        j.wait()
+        films.append(j.film())
+        st = j.stats()
+        rays.append((st["rays_closest"], st["rays_shadow"]))
+        j.close()
+    assert np.array_equal(films[0], films[1]) and films[0].mean() > 0
+    assert rays[0] == rays[1]
+    s.close()
+
+
+def test_volpath_wavefront_fbm_256(rad, scene_dir):
+    """The bench's volume (256^3 fBm grid, depth 32) at 128x128, 4 spp: both
+    schedules give the same film, and the wavefront's samples match
+    rad_render_samples."""
+    sc, assets = scenes.volume_box(width=128, height=128, spp=4, grid=256)
+    path = scenes.write_scene(os.path.join(str(scene_dir), "fbm256_wf"), sc, assets)
+    s = rad.Scene.from_file(path)
+    films = []
+    for persistent in (False, True):
+        j = s.submit(spp=4, seed=3, vol_persistent=persistent)
+        j.wait()
+        films.append(j.film())
+        j.close()
+    assert np.array_equal(films[0], films[1]) and films[0].mean() > 0
+    pix = np.repeat(np.arange(128 * 128, dtype=np.uint32), 4)
+    smp = np.tile(np.arange(4, dtype=np.uint32), 128 * 128)
+    L = s.render_samples(pix, smp, seed=3).reshape(128 * 128, 4, 3).astype(np.float64)
+    L[~np.isfinite(L).all(-1) | (L[..., 0] < 0)] = 0.0
+    assert np.allclose(L.mean(1).reshape(128, 128, 3), films[0], rtol=1e-5, atol=1e-6)
     s.close()
 
 

@@ -188,8 +188,31 @@ def test_render_samples_fbm_volume_256_bit_exact(oracle, tmp_path):
         text = fh.read()
     h, o = hemu_lib.HemuScene(text, str(tmp_path)), oracle.OracleScene(text, str(tmp_path))
     _samples_bit_exact(h, o, 4096, seed=13)
+    _samples_bit_exact(h, o, 4096, seed=14, vol_mode=VOL_WAVEFRONT)
     h.close()
     o.close()
+
+
+VOL_WAVEFRONT = 256  # hemu_render_samples: run vol_path as the per-event wavefront
+
+
+def test_volume_wavefront_bit_exact(oracle, scene_dir):
+    """The per-event wavefront schedule of vol_path (a kernel per loop part over
+    queues, state stored between parts) gives every path the radiance of the
+    persistent schedule and of the oracle, bit for bit; with the opt-in
+    estimators (real depth, brick majorants) it equals the persistent kernel."""
+    path, text, d = volume(scene_dir, 32, 32, 4, grid=24)
+    h, o = hemu_lib.HemuScene(text, d), oracle.OracleScene(text, d)
+    _samples_bit_exact(h, o, 4096, seed=21, vol_mode=VOL_WAVEFRONT)
+    rng = np.random.default_rng(5)
+    pix = rng.integers(0, o.width * o.height, 2048).astype(np.uint32)
+    smp = rng.integers(0, 1 << 16, 2048).astype(np.uint32)
+    for mode in (4, 1):  # kVolRealDepth, kVolBricks
+        a = h.render_samples(pix, smp, o.seed, mode)
+        b = h.render_samples(pix, smp, o.seed, mode | VOL_WAVEFRONT)
+        assert _same(a, b).all(), mode
+        assert np.abs(a).sum() > 0
+    h.close()
 
 
 def test_ulp_explanation_discriminates(oracle, scene_dir):
