@@ -324,6 +324,8 @@ def run_volume(args, world, rank, local):
         sc, assets = scenes.volume_box(width=res, height=res, spp=1, max_depth=32, grid=args.vol_grid)
         path = scenes.write_scene(tmp, sc, assets)
         scene = rad.Scene.from_file(path)
+        # lane top-up threshold and blocks per SM of the wavefront's part kernels (rad_autotune, not timed)
+        tune = scene.autotune() if not args.no_tune else None
         j = scene.submit(spp=args.warmup, first_sample=20_000)
         j.wait()
         j.close()
@@ -382,7 +384,11 @@ def run_volume(args, world, rank, local):
             "ms_per_step": st["gpu_ms"] / args.steps, "higher_is_better": True, "scaling": "weak",
             "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded fBm grid)",
             "config": {"workload": "volume_box", "width": res, "height": res, "grid": args.vol_grid,
-                       "max_depth": 32, "rr_depth": 5, "sigma_t_scale": 20, "albedo": 0.9, "hg_g": 0.6},
+                       "max_depth": 32, "rr_depth": 5, "sigma_t_scale": 20, "albedo": 0.9, "hg_g": 0.6,
+                       "autotune": None if tune is None else
+                       {"refill_busy": tune["refill_busy"], "blocks_per_sm": tune["blocks_per_sm"],
+                        "vol_chunk": tune["vol_chunk"], "wave_ms_tuned": round(tune["best_ms"], 3),
+                        "wave_ms_default": round(tune["default_ms"], 3)}},
             "mrays_per_s": (st["rays_closest"] + st["rays_shadow"]) / (st["gpu_ms"] / 1000.0) / 1e6,
             "gpu_launches": st["kernel_launches"], "kernel_ms": {"vol_path": st["ms_volpath"]}, "clocks": clk,
             "mode": "the reference's delta tracking (global majorant, null collisions counted as depth) on the "

@@ -284,14 +284,23 @@ RAD_API int rad_guide_grad(rad_scene* scene, const float* records, int64_t n, fl
  * default [16,20,24,28,32]), blocks_per_sm (list, default [4,6,8]),
  * shade_block (list of 64 / 128 / 256, default all three), reps (timed waves
  * per candidate, 2).
- * RAD_ERR_UNSUPPORTED for `vol_path`, `particle_tracer` and `bdpt` scenes. */
+ * `vol_path` scenes: the axes are those of the per-event wavefront's part
+ * kernels -- refill_busy (a warp tops up its lanes once fewer than this many
+ * still run a path; default [8,12,16,20,24,28,32]), blocks_per_sm (default
+ * [2,3,4]; 4 is the kernels' occupancy, larger values run as 4) and vol_chunk
+ * (steps of a repeating part -- null collisions, NEE transmittance -- a lane runs
+ * per path and launch before the path continues in the next round; default
+ * [4,8,16,32,64]); leaf_frac8 and shade_block do not apply. Waves use the
+ * reference's estimator on the fp32 grid.
+ * RAD_ERR_UNSUPPORTED for `particle_tracer` and `bdpt` scenes. */
 typedef struct rad_tune_result {
   int32_t refill_busy, blocks_per_sm; /* chosen */
   int32_t candidates;                 /* configurations timed */
   double best_ms;    /* time of one wave with the chosen parameters */
-  double default_ms; /* with the defaults (20, 8, 4, 128), when they were timed */
+  double default_ms; /* with the defaults (20, 8, 4, 128, 16), when they were timed */
   int32_t leaf_frac8; /* chosen */
   int32_t shade_block; /* chosen */
+  int32_t vol_chunk;   /* chosen (`vol_path`; 16 elsewhere) */
 } rad_tune_result;
 RAD_API int rad_autotune(rad_scene* scene, const char* config_json, rad_tune_result* out);
 

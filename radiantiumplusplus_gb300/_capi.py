@@ -86,7 +86,8 @@ class Stats(ctypes.Structure):
 class TuneResult(ctypes.Structure):
     _fields_ = [("refill_busy", ctypes.c_int32), ("blocks_per_sm", ctypes.c_int32), ("candidates", ctypes.c_int32),
                 ("best_ms", ctypes.c_double), ("default_ms", ctypes.c_double), ("leaf_frac8", ctypes.c_int32),
-                ("shade_block", ctypes.c_int32)]
+                ("shade_block", ctypes.c_int32),
+                ("vol_chunk", ctypes.c_int32)]
 
 
 class GuideInfo(ctypes.Structure):

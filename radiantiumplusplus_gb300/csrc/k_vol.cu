@@ -597,13 +597,19 @@ __global__ void __launch_bounds__(kVolBlock, 5)
 
 // ---- per-event wavefront ------------------------------------------------------
 // Part order within a round: top, scatter, surface, NEE, scatter end, surface
-// end. Every part hands its paths to a later part of the same round, except the
-// loop's increment (scatter end, surface end, an index-matched boundary), which
-// queues the path for the next round's top: queues of the current round have
-// parity `cur`, the next round's top queue parity cur ^ 1.
+// end. A part hands its paths to a later part of the same round (queues of
+// parity `cur`), except the loop's increment (scatter end, surface end, an
+// index-matched boundary), which queues the path for the next round's top, and
+// a repeating part (top through null collisions, the NEE's transmittance steps)
+// that has run `chunk` steps of a path in this launch, which queues it to
+// continue in the next round (parity cur ^ 1). The chunk bounds how long the
+// last lanes of a launch run on after its queue has drained.
 size_t VolStateBytes() { return sizeof(VolPathState); }
 
-RD uint32_t VolQueueOf(int act, uint32_t cur) { return (act == kActTop ? (cur ^ 1u) : cur) * kVolActs + (uint32_t)act; }
+// Queue of a path moving from part `from` to part `act`.
+RD uint32_t VolQueueOf(int from, int act, uint32_t cur) {
+  return (act <= from ? (cur ^ 1u) : cur) * kVolActs + (uint32_t)act;
+}
 
 // Appends idx to queue `dst` for every lane with dst >= 0; all lanes of the warp
 // call it. One atomic per destination and warp.
@@ -619,12 +625,18 @@ RD void VolPush(const VolWave& V, int dst, uint32_t idx) {
 
 // One loop part over its queue. A lane runs its path's part (the top repeats
 // through null collisions, the NEE through its transmittance steps) until the
-// path moves to another part, stores the state, queues the path there and
-// takes the next one from this part's queue. FRESH (first round's top): the
-// queue is the wave's paths 0..count-1, started from the generate stage's rays.
+// path ends, moves to another part or has run `chunk` steps of this one.
+// Lanes are topped up in batches: once at
+// most `refillBelow` lanes of the warp still run a path (or none do), the lanes
+// whose paths moved store their states and queue them at their next part, and
+// the idle lanes take the next paths of this part's queue -- so the state
+// copies run with many lanes at once instead of one lane at a time. FRESH
+// (first round's top): the queue is the wave's paths 0..count-1, started from
+// the generate stage's rays.
 template <int ACT, bool FRESH, bool BRICKS, bool HALF>
 __global__ void __launch_bounds__(kVolBlock, 4)
-    KVolEvent(DevScene S, PathBuffers B, VolWave V, uint32_t count, uint32_t cur, uint32_t* err, uint32_t mode) {
+    KVolEvent(DevScene S, PathBuffers B, VolWave V, uint32_t count, uint32_t cur, uint32_t* err, uint32_t mode,
+              int refillBelow, int chunk) {
   const uint32_t lane = threadIdx.x & 31u;
   const uint32_t in = cur * kVolActs + (uint32_t)ACT;
   const uint32_t n = FRESH ? count : V.cnt[in];
@@ -632,36 +644,46 @@ __global__ void __launch_bounds__(kVolBlock, 4)
   VolPathState* states = static_cast<VolPathState*>(V.state);
   VolPathState p;
   uint32_t idx = 0, ended = 0;
+  int steps = 0;  // of this part, for the lane's path in this launch
+  int dst = -1;   // a path that moved on, held until the next batch hand-off
   bool live = false, drained = n == 0;
   unsigned long long nRays = 0, nShadow = 0;
   for (;;) {
-    const uint32_t need = __ballot_sync(0xffffffffu, !live);
-    if (need && !drained) {
-      const int leader = __ffs(need) - 1;
-      uint32_t base = 0;
-      if ((int)lane == leader) base = atomicAdd(head, (uint32_t)__popc(need));
-      base = __shfl_sync(0xffffffffu, base, leader);
-      if (base + (uint32_t)__popc(need) >= n) drained = true;
-      if (!live) {
-        const uint32_t i = base + __popc(need & ((1u << lane) - 1u));
-        if (i < n) {
-          if (FRESH) {
-            idx = i;
-            const float4 ro = B.rayO[idx], rd = B.rayD[idx];
-            const uint2 rs = B.rng[idx];
-            Pcg32 rng;
-            rng.state = ((uint64_t)rs.y << 32) | rs.x;
-            VolInit(S, p, VRay{V3{ro.x, ro.y, ro.z}, V3{rd.x, rd.y, rd.z}, ro.w, rd.w}, rng);
-          } else {
-            idx = V.q[(size_t)in * V.capacity + i];
-            p = states[idx];
+    const uint32_t liveMask = __ballot_sync(0xffffffffu, live);
+    if (liveMask == 0u || (!drained && __popc(liveMask) <= refillBelow)) {
+      if (__ballot_sync(0xffffffffu, dst >= 0) != 0u) {
+        if (dst >= 0) states[idx] = p;
+        VolPush(V, dst, idx);
+        dst = -1;
+      }
+      const uint32_t need = __ballot_sync(0xffffffffu, !live);
+      if (!drained && need != 0u) {
+        const int leader = __ffs(need) - 1;
+        uint32_t base = 0;
+        if ((int)lane == leader) base = atomicAdd(head, (uint32_t)__popc(need));
+        base = __shfl_sync(0xffffffffu, base, leader);
+        if (base + (uint32_t)__popc(need) >= n) drained = true;
+        if (!live) {
+          const uint32_t i = base + __popc(need & ((1u << lane) - 1u));
+          if (i < n) {
+            if (FRESH) {
+              idx = i;
+              const float4 ro = B.rayO[idx], rd = B.rayD[idx];
+              const uint2 rs = B.rng[idx];
+              Pcg32 rng;
+              rng.state = ((uint64_t)rs.y << 32) | rs.x;
+              VolInit(S, p, VRay{V3{ro.x, ro.y, ro.z}, V3{rd.x, rd.y, rd.z}, ro.w, rd.w}, rng);
+            } else {
+              idx = V.q[(size_t)in * V.capacity + i];
+              p = states[idx];
+            }
+            steps = 0;
+            live = true;
           }
-          live = true;
         }
       }
+      if (__ballot_sync(0xffffffffu, live) == 0u) break;
     }
-    if (__ballot_sync(0xffffffffu, live) == 0u) break;
-    int dst = -1;
     if (live) {
       if (!VolAct<BRICKS, HALF>(S, p, ACT, mode, err)) {
         B.L[idx] = make_float4(p.result.x, p.result.y, p.result.z, 0.f);
@@ -669,13 +691,11 @@ __global__ void __launch_bounds__(kVolBlock, 4)
         nShadow += p.nShadow;
         ended++;
         live = false;
-      } else if (p.act != ACT) {
-        states[idx] = p;
-        dst = (int)VolQueueOf(p.act, cur);
+      } else if (p.act != ACT || ++steps >= chunk) {
+        dst = (int)VolQueueOf(ACT, p.act, cur);
         live = false;
       }
     }
-    if (__ballot_sync(0xffffffffu, dst >= 0) != 0u) VolPush(V, dst, idx);
   }
   if (nRays) atomicAdd(B.counters + kMiscBase + 2, (uint32_t)nRays);
   if (nShadow) atomicAdd(B.counters + kMiscBase + 3, (uint32_t)nShadow);
@@ -710,44 +730,48 @@ cudaError_t LaunchVolPath(const DevScene& S, const PathBuffers& B, const WavePar
 
 template <bool BRICKS, bool HALF>
 static cudaError_t VolRound(const DevScene& S, const PathBuffers& B, const VolWave& V, uint32_t count, uint32_t r,
-                            int blocks, uint32_t* err, cudaStream_t st, uint32_t mode) {
+                            int blocks, uint32_t* err, cudaStream_t st, uint32_t mode, int refillBelow,
+                            int chunk) {
   const uint32_t cur = r & 1u;
   if (r == 0)
-    KVolEvent<kActTop, true, BRICKS, HALF><<<blocks, kVolBlock, 0, st>>>(S, B, V, count, cur, err, mode);
+    KVolEvent<kActTop, true, BRICKS, HALF><<<blocks, kVolBlock, 0, st>>>(S, B, V, count, cur, err, mode, refillBelow, chunk);
   else
-    KVolEvent<kActTop, false, BRICKS, HALF><<<blocks, kVolBlock, 0, st>>>(S, B, V, count, cur, err, mode);
-  KVolEvent<kActScatter, false, BRICKS, HALF><<<blocks, kVolBlock, 0, st>>>(S, B, V, count, cur, err, mode);
-  KVolEvent<kActSurface, false, BRICKS, HALF><<<blocks, kVolBlock, 0, st>>>(S, B, V, count, cur, err, mode);
-  KVolEvent<kActNee, false, BRICKS, HALF><<<blocks, kVolBlock, 0, st>>>(S, B, V, count, cur, err, mode);
-  KVolEvent<kActScatterEnd, false, BRICKS, HALF><<<blocks, kVolBlock, 0, st>>>(S, B, V, count, cur, err, mode);
-  KVolEvent<kActSurfaceEnd, false, BRICKS, HALF><<<blocks, kVolBlock, 0, st>>>(S, B, V, count, cur, err, mode);
+    KVolEvent<kActTop, false, BRICKS, HALF><<<blocks, kVolBlock, 0, st>>>(S, B, V, count, cur, err, mode, refillBelow, chunk);
+  KVolEvent<kActScatter, false, BRICKS, HALF><<<blocks, kVolBlock, 0, st>>>(S, B, V, count, cur, err, mode, refillBelow, chunk);
+  KVolEvent<kActSurface, false, BRICKS, HALF><<<blocks, kVolBlock, 0, st>>>(S, B, V, count, cur, err, mode, refillBelow, chunk);
+  KVolEvent<kActNee, false, BRICKS, HALF><<<blocks, kVolBlock, 0, st>>>(S, B, V, count, cur, err, mode, refillBelow, chunk);
+  KVolEvent<kActScatterEnd, false, BRICKS, HALF><<<blocks, kVolBlock, 0, st>>>(S, B, V, count, cur, err, mode, refillBelow, chunk);
+  KVolEvent<kActSurfaceEnd, false, BRICKS, HALF><<<blocks, kVolBlock, 0, st>>>(S, B, V, count, cur, err, mode, refillBelow, chunk);
   KVolRoundEnd<<<1, 32, 0, st>>>(V, cur);
   return cudaGetLastError();
 }
 
 cudaError_t LaunchVolWavefront(const DevScene& S, const PathBuffers& B, const VolWave& V, const WaveParams& w,
-                               uint32_t* err, cudaStream_t st, uint32_t mode, uint32_t* hostCounts,
-                               uint64_t* launches) {
+                               uint32_t* err, cudaStream_t st, uint32_t mode, const TraceTune& tu,
+                               uint32_t* hostCounts, uint64_t* launches) {
   if (w.count == 0) return cudaSuccess;
   if (w.count > V.capacity) return cudaErrorInvalidValue;
   cudaError_t e = cudaMemsetAsync(V.cnt, 0, kVolCountWords * sizeof(uint32_t), st);
   if (e != cudaSuccess) return e;
   int perSm = 0;
   cudaOccupancyMaxActiveBlocksPerMultiprocessor(&perSm, KVolEvent<kActTop, false, false, true>, kVolBlock, 0);
-  const int cap = PathGridBlocks() / 8 * (perSm > 0 ? perSm : 4);
+  perSm = std::max(1, std::min(perSm > 0 ? perSm : 4, tu.blocksPerSm));
+  const int cap = PathGridBlocks() / 8 * perSm;
   const int blocks = (int)std::min<uint32_t>((w.count + kVolBlock - 1) / kVolBlock, (uint32_t)cap);
-  // At the end of a round every live path waits in the next round's top queue,
-  // so ended + queued = count, and the wave is done when that queue is empty.
-  // The counters are read back every 4 rounds from round 8 on (a path ends
-  // within max_depth rounds unless null collisions are free or it crosses
-  // index-matched boundaries). Every round advances each live path by at least
-  // one loop iteration, so the per-path iteration bound bounds the rounds.
+  const int refillBelow = std::max(0, std::min(31, tu.refillBusy - 1));
+  const int chunk = std::max(1, tu.volChunk);
+  // At the end of a round every live path waits in a queue of the next round,
+  // so ended + queued = count, and the wave is done when those are empty.
+  // The counters are read back every 4 rounds from round 8 on. Every round
+  // advances each live path by at least one step of its part, and the steps of
+  // a path are bounded (loop iterations, transmittance steps), so the rounds
+  // are too; the host loop's own bound turns a runaway into an error.
   for (uint32_t r = 0; r <= (uint32_t)kMaxVolIter; r++) {
     switch (mode & (kVolBricks | kVolHalf)) {
-      case 0: e = VolRound<false, false>(S, B, V, w.count, r, blocks, err, st, mode); break;
-      case kVolBricks: e = VolRound<true, false>(S, B, V, w.count, r, blocks, err, st, mode); break;
-      case kVolHalf: e = VolRound<false, true>(S, B, V, w.count, r, blocks, err, st, mode); break;
-      default: e = VolRound<true, true>(S, B, V, w.count, r, blocks, err, st, mode); break;
+      case 0: e = VolRound<false, false>(S, B, V, w.count, r, blocks, err, st, mode, refillBelow, chunk); break;
+      case kVolBricks: e = VolRound<true, false>(S, B, V, w.count, r, blocks, err, st, mode, refillBelow, chunk); break;
+      case kVolHalf: e = VolRound<false, true>(S, B, V, w.count, r, blocks, err, st, mode, refillBelow, chunk); break;
+      default: e = VolRound<true, true>(S, B, V, w.count, r, blocks, err, st, mode, refillBelow, chunk); break;
     }
     if (e != cudaSuccess) return e;
     if (launches) *launches += kVolActs + 1;
@@ -755,7 +779,8 @@ cudaError_t LaunchVolWavefront(const DevScene& S, const PathBuffers& B, const Vo
       e = cudaMemcpyAsync(hostCounts, V.cnt, kVolCountWords * sizeof(uint32_t), cudaMemcpyDeviceToHost, st);
       if (e == cudaSuccess) e = cudaStreamSynchronize(st);
       if (e != cudaSuccess) return e;
-      const uint32_t queued = hostCounts[((r & 1u) ^ 1u) * kVolActs + kActTop];
+      uint32_t queued = 0;
+      for (int a = 0; a < kVolActs; a++) queued += hostCounts[((r & 1u) ^ 1u) * kVolActs + a];
       if ((uint64_t)hostCounts[kVolEndedWord] + queued != w.count) return cudaErrorIllegalState;
       if (queued == 0) return cudaSuccess;
     }

@@ -135,6 +135,7 @@ struct TraceTune {
   int32_t blocksPerSm = 8;
   int32_t leafFrac8 = 4;
   int32_t shadeBlock = 128;
+  int32_t volChunk = 16;  // vol_path wavefront: loop steps of one part a lane runs per launch
 };
 // trav (optional, 4 x u64): extend node visits, extend prim tests, shadow node visits, shadow prim tests
 cudaError_t LaunchExtend(const DevScene& S, const PathBuffers& B, int depth, int grid, cudaStream_t st,
@@ -236,7 +237,9 @@ cudaError_t LaunchVolPath(const DevScene& S, const PathBuffers& B, const WavePar
 // paths at each part, path state in HBM between them. The same arithmetic per
 // path as LaunchVolPath, so the same radiance bit for bit.
 constexpr int kVolActs = 6;
-// counter words: [par * kVolActs + act] queue lengths (two parities),
+// counter words: [par * kVolActs + act] queue lengths (two parities: a path
+// moving to a later part of the round goes to the current parity, one moving
+// back or continuing its part to the next round's),
 // [2 kVolActs + act] queue heads, [3 kVolActs] paths ended
 constexpr int kVolEndedWord = 3 * kVolActs;
 constexpr int kVolCountWords = 3 * kVolActs + 1;
@@ -251,9 +254,13 @@ size_t VolStateBytes();
 // see whether every path has ended (hostCounts: pinned, kVolCountWords words).
 // launches: kernels run. cudaErrorIllegalState if the path count is not
 // conserved (a path neither ended nor queued).
+// tu.refillBusy: a warp tops up its lanes once fewer than this many run a path;
+// tu.blocksPerSm: resident blocks per SM of the part kernels (at most their occupancy);
+// tu.volChunk: steps of the repeating parts (null collisions, NEE transmittance)
+// a lane runs per path and launch before the path continues in the next round.
 cudaError_t LaunchVolWavefront(const DevScene& S, const PathBuffers& B, const VolWave& V, const WaveParams& w,
-                               uint32_t* err, cudaStream_t st, uint32_t mode, uint32_t* hostCounts,
-                               uint64_t* launches);
+                               uint32_t* err, cudaStream_t st, uint32_t mode, const TraceTune& tu,
+                               uint32_t* hostCounts, uint64_t* launches);
 
 // ---- guide network (k_guide.cu)
 cudaError_t GuideKernelsInit();

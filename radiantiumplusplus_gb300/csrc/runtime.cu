@@ -978,7 +978,8 @@ void RunWave(rad_job* j) {
         Check(LaunchVolPath(S, lib.paths, w, err, lib.stream, mode), "vol_path");
         launches++;
       } else {
-        Check(LaunchVolWavefront(S, lib.paths, EnsureVolWave(), w, err, lib.stream, mode, lib.hVolWord, &launches),
+        Check(LaunchVolWavefront(S, lib.paths, EnsureVolWave(), w, err, lib.stream, mode, j->scene->tune,
+                                 lib.hVolWord, &launches),
               "vol_path wavefront");
       }
       ps.End(5, a);
@@ -1927,7 +1928,7 @@ int rad_render_samples(rad_scene* scene, const uint32_t* pixels, const uint32_t*
       Check(LaunchGenerate(scene->dev, lib.paths, w, lib.stream), "generate");
       if (scene->dev.isVol) {
         Check(LaunchVolWavefront(scene->dev, lib.paths, EnsureVolWave(), w, lib.paths.counters + kMiscBase + 1,
-                                 lib.stream, 0u, lib.hVolWord, nullptr),
+                                 lib.stream, 0u, scene->tune, lib.hVolWord, nullptr),
               "vol_path wavefront");
       } else {
         LaunchBounces(scene->dev, scene->tune, count, ps);
@@ -2120,12 +2121,24 @@ int rad_guide_info(rad_scene* scene, rad_guide_info_t* info) {
 // configuration and keeps the fastest in the scene.
 int rad_autotune(rad_scene* scene, const char* config_json, rad_tune_result* out) {
   if (!scene) return Fail(RAD_ERR_INVALID_ARG, "null scene");
-  if (scene->dev.isVol || scene->dev.isParticle || scene->dev.isBdpt)
-    return Fail(RAD_ERR_UNSUPPORTED, "the autotuner covers the `path` traversal kernels");
+  if (scene->dev.isParticle || scene->dev.isBdpt)
+    return Fail(RAD_ERR_UNSUPPORTED, "the autotuner covers the `path` and `vol_path` kernels");
   return Guard([&] {
     EnsureInit();
     int reps = 2;
+    const bool vol = scene->dev.isVol != 0;
     std::vector<int> leaf = {2, 3, 4, 5, 6}, refill = {16, 20, 24, 28, 32}, perSm = {4, 6, 8}, shade = {64, 128, 256};
+    std::vector<int> chunk = {TraceTune{}.volChunk};
+    if (vol) {
+      // vol_path's part kernels: the lane top-up threshold and blocks per SM (at
+      // most 4 resident); the leaf vote and shade block do not apply
+      const TraceTune def;
+      leaf = {def.leafFrac8};
+      shade = {def.shadeBlock};
+      refill = {8, 12, 16, 20, 24, 28, 32};
+      perSm = {2, 3, 4};
+      chunk = {4, 8, 16, 32, 64};
+    }
     if (config_json && *config_json) {
       JValue c = JsonReader::Parse(config_json);
       if (const JValue* v = c.get("reps")) reps = std::max(1, (int)v->n);
@@ -2144,6 +2157,7 @@ int rad_autotune(rad_scene* scene, const char* config_json, rad_tune_result* out
       list("refill_busy", refill, 1, 32);
       list("blocks_per_sm", perSm, 1, 8);
       list("shade_block", shade, 64, 256);
+      if (vol) list("vol_chunk", chunk, 1, 1 << 20);
       for (int v : shade)
         if (v != 64 && v != 128 && v != 256) throw Error{RAD_ERR_INVALID_ARG, "shade_block values are 64, 128 or 256"};
     }
@@ -2157,13 +2171,19 @@ int rad_autotune(rad_scene* scene, const char* config_json, rad_tune_result* out
     auto wave = [&](const TraceTune& tu) {
       WaveParams w{0, count, 0, scene->info.seed, nullptr, nullptr};
       Check(LaunchGenerate(S, lib.paths, w, lib.stream), "generate");
-      LaunchBounces(S, tu, count, none);
+      if (vol)
+        Check(LaunchVolWavefront(S, lib.paths, EnsureVolWave(), w, lib.paths.counters + kMiscBase + 1, lib.stream, 0u,
+                                 tu, lib.hVolWord, nullptr),
+              "vol_path wavefront");
+      else
+        LaunchBounces(S, tu, count, none);
     };
     std::vector<std::pair<TraceTune, float>> timed;
     auto time = [&](const TraceTune& tu) -> float {
       for (const auto& t : timed)
         if (t.first.refillBusy == tu.refillBusy && t.first.blocksPerSm == tu.blocksPerSm &&
-            t.first.leafFrac8 == tu.leafFrac8 && t.first.shadeBlock == tu.shadeBlock)
+            t.first.leafFrac8 == tu.leafFrac8 && t.first.shadeBlock == tu.shadeBlock &&
+            t.first.volChunk == tu.volChunk)
           return t.second;
       wave(tu);  // warm-up
       Check(cudaEventRecord(a, lib.stream), "event");
@@ -2178,11 +2198,14 @@ int rad_autotune(rad_scene* scene, const char* config_json, rad_tune_result* out
     };
     // coordinate descent from the defaults: each axis in turn, the others held at
     // the best values found so far
+    // (vol_path: the defaults' 8 blocks per SM run as the part kernels' 4, outside the list)
+    const float volDefaultMs = vol ? time(TraceTune{}) : 0.f;
     TraceTune best;
     if (std::find(leaf.begin(), leaf.end(), best.leafFrac8) == leaf.end()) best.leafFrac8 = leaf[0];
     if (std::find(refill.begin(), refill.end(), best.refillBusy) == refill.end()) best.refillBusy = refill[0];
     if (std::find(perSm.begin(), perSm.end(), best.blocksPerSm) == perSm.end()) best.blocksPerSm = perSm[0];
     if (std::find(shade.begin(), shade.end(), best.shadeBlock) == shade.end()) best.shadeBlock = shade[0];
+    if (std::find(chunk.begin(), chunk.end(), best.volChunk) == chunk.end()) best.volChunk = chunk[0];
     float bestMs = time(best);
     auto axis = [&](const std::vector<int>& vals, int32_t TraceTune::*field) {
       for (int v : vals) {
@@ -2199,7 +2222,9 @@ int rad_autotune(rad_scene* scene, const char* config_json, rad_tune_result* out
     axis(refill, &TraceTune::refillBusy);
     axis(perSm, &TraceTune::blocksPerSm);
     axis(shade, &TraceTune::shadeBlock);
+    axis(chunk, &TraceTune::volChunk);
     rad_tune_result res{};
+    res.vol_chunk = best.volChunk;
     res.shade_block = best.shadeBlock;
     res.refill_busy = best.refillBusy;
     res.blocks_per_sm = best.blocksPerSm;
@@ -2207,9 +2232,11 @@ int rad_autotune(rad_scene* scene, const char* config_json, rad_tune_result* out
     res.best_ms = bestMs;
     res.candidates = (int32_t)timed.size();
     const TraceTune def;
+    res.default_ms = volDefaultMs;
     for (const auto& t : timed)
-      if (t.first.refillBusy == def.refillBusy && t.first.blocksPerSm == def.blocksPerSm &&
-          t.first.leafFrac8 == def.leafFrac8 && t.first.shadeBlock == def.shadeBlock)
+      if (!vol && t.first.refillBusy == def.refillBusy && t.first.blocksPerSm == def.blocksPerSm &&
+          t.first.leafFrac8 == def.leafFrac8 && t.first.shadeBlock == def.shadeBlock &&
+          t.first.volChunk == def.volChunk)
         res.default_ms = t.second;
     lib.evPool.push_back(a);
     lib.evPool.push_back(b);

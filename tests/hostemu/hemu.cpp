@@ -191,22 +191,22 @@ struct HostPaths {
 // has ended.
 constexpr uint32_t kHemuVolWavefront = 256u;
 template <bool BRICKS>
-void VolWavefront(const DevScene& S, PathBuffers& B, uint32_t n, uint32_t* err, uint32_t mode) {
+void VolWavefront(const DevScene& S, PathBuffers& B, uint32_t n, uint32_t* err, uint32_t mode, int chunk) {
   std::vector<VolPathState> states(n);
   std::vector<uint32_t> q((size_t)2 * kVolActs * n, 0u), cnt(kVolCountWords, 0u);
   VolWave V{states.data(), q.data(), cnt.data(), n};
   for (uint32_t r = 0; cnt[kVolEndedWord] < n; r++) {
-    if (r > 4096) throw std::runtime_error("vol_path wavefront: paths left after 4096 rounds");
+    if (r > 65536) throw std::runtime_error("vol_path wavefront: paths left after 65536 rounds");
     const uint32_t cur = r & 1u;
     if (r == 0)
-      Grid(1, 2, [&] { KVolEvent<kActTop, true, BRICKS, false>(S, B, V, n, cur, err, mode); });
+      Grid(1, 2, [&] { KVolEvent<kActTop, true, BRICKS, false>(S, B, V, n, cur, err, mode, 16, chunk); });
     else
-      Grid(1, 2, [&] { KVolEvent<kActTop, false, BRICKS, false>(S, B, V, n, cur, err, mode); });
-    Grid(1, 2, [&] { KVolEvent<kActScatter, false, BRICKS, false>(S, B, V, n, cur, err, mode); });
-    Grid(1, 2, [&] { KVolEvent<kActSurface, false, BRICKS, false>(S, B, V, n, cur, err, mode); });
-    Grid(1, 2, [&] { KVolEvent<kActNee, false, BRICKS, false>(S, B, V, n, cur, err, mode); });
-    Grid(1, 2, [&] { KVolEvent<kActScatterEnd, false, BRICKS, false>(S, B, V, n, cur, err, mode); });
-    Grid(1, 2, [&] { KVolEvent<kActSurfaceEnd, false, BRICKS, false>(S, B, V, n, cur, err, mode); });
+      Grid(1, 2, [&] { KVolEvent<kActTop, false, BRICKS, false>(S, B, V, n, cur, err, mode, 16, chunk); });
+    Grid(1, 2, [&] { KVolEvent<kActScatter, false, BRICKS, false>(S, B, V, n, cur, err, mode, 16, chunk); });
+    Grid(1, 2, [&] { KVolEvent<kActSurface, false, BRICKS, false>(S, B, V, n, cur, err, mode, 16, chunk); });
+    Grid(1, 2, [&] { KVolEvent<kActNee, false, BRICKS, false>(S, B, V, n, cur, err, mode, 16, chunk); });
+    Grid(1, 2, [&] { KVolEvent<kActScatterEnd, false, BRICKS, false>(S, B, V, n, cur, err, mode, 16, chunk); });
+    Grid(1, 2, [&] { KVolEvent<kActSurfaceEnd, false, BRICKS, false>(S, B, V, n, cur, err, mode, 16, chunk); });
     Grid(1, 32, [&] { KVolRoundEnd(V, cur); });
   }
 }
@@ -226,10 +226,11 @@ void RenderSamples(const DevScene& S, const uint32_t* pix, const uint32_t* smp, 
   GuideDev none{};
   if (S.isVol && (volMode & kHemuVolWavefront)) {
     if (volMode & kVolHalf) throw std::runtime_error("the fp16 grid is not emulated");
+    // a short chunk, so that paths often continue their part in a later round
     if (volMode & kVolBricks)
-      VolWavefront<true>(S, B, n, err, volMode & ~kHemuVolWavefront);
+      VolWavefront<true>(S, B, n, err, volMode & ~kHemuVolWavefront, 3);
     else
-      VolWavefront<false>(S, B, n, err, volMode & ~kHemuVolWavefront);
+      VolWavefront<false>(S, B, n, err, volMode & ~kHemuVolWavefront, 3);
   } else if (S.isVol) {
     switch (volMode & (kVolBricks | kVolHalf)) {
       case 0: Grid(1, 1, [&] { KVolPath<false, false>(S, B, n, err, volMode); }); break;

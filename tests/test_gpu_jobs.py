@@ -106,6 +106,24 @@ def test_autotune_picks_parameters_and_keeps_results(rad, scene_dir):
     s.close()
 
 
+def test_autotune_volume_wavefront(rad, scene_dir):
+    """On a vol_path scene the tuner times the wavefront's part kernels (lane
+    top-up threshold, blocks per SM); the film is bit-identical before and after."""
+    from helpers import volume
+    path, _, _ = volume(scene_dir, 40, 32, 3, grid=24)
+    s = rad.Scene.from_file(path)
+    before = s.render(spp=3, seed=5)
+    r = s.autotune({"reps": 1})
+    assert r["refill_busy"] in (8, 12, 16, 20, 24, 28, 32) and r["blocks_per_sm"] in (2, 3, 4)
+    assert r["vol_chunk"] in (4, 8, 16, 32, 64)
+    assert r["candidates"] >= 12 and r["best_ms"] > 0 and r["default_ms"] > 0
+    assert np.array_equal(before, s.render(spp=3, seed=5))
+    r2 = s.autotune({"refill_busy": [1], "blocks_per_sm": [1], "vol_chunk": [1], "reps": 1})
+    assert r2["refill_busy"] == 1 and r2["blocks_per_sm"] == 1 and r2["vol_chunk"] == 1
+    assert np.array_equal(before, s.render(spp=3, seed=5))
+    s.close()
+
+
 def test_cli_renders_and_saves(rad, scene_dir):
     """python -m radiantiumplusplus_gb300 --scene x.json writes <dir>/<stem>.exr equal to the job film."""
     import os
