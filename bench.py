@@ -318,7 +318,8 @@ def run_volume(args, world, rank, local):
     import radiantiumplusplus_gb300 as rad
     from radiantiumplusplus_gb300 import scenes
     torch.cuda.set_device(local)
-    rad.init({"device": local})
+    # waves of max_paths paths (samples of whole pixel rows): 4 samples of the 1024^2 frame per wave
+    rad.init({"device": local, "max_paths": args.vol_max_paths})
     res = args.vol_res
     with tempfile.TemporaryDirectory(prefix="rad_bench_vol_") as tmp:
         sc, assets = scenes.volume_box(width=res, height=res, spp=1, max_depth=32, grid=args.vol_grid)
@@ -384,6 +385,7 @@ def run_volume(args, world, rank, local):
             "ms_per_step": st["gpu_ms"] / args.steps, "higher_is_better": True, "scaling": "weak",
             "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded fBm grid)",
             "config": {"workload": "volume_box", "width": res, "height": res, "grid": args.vol_grid,
+                       "max_paths": args.vol_max_paths,
                        "max_depth": 32, "rr_depth": 5, "sigma_t_scale": 20, "albedo": 0.9, "hg_g": 0.6,
                        "autotune": None if tune is None else
                        {"refill_busy": tune["refill_busy"], "blocks_per_sm": tune["blocks_per_sm"],
@@ -735,6 +737,8 @@ def main():
     ap.add_argument("--guided-config", default="{}", help="JSON of rad_guide_enable settings for the guided jobs")
     ap.add_argument("--no-tune", action="store_true", help="skip rad_autotune (keeps launch indices fixed for ncu)")
     ap.add_argument("--vol-res", type=int, default=1024)
+    ap.add_argument("--vol-max-paths", type=int, default=1 << 22,
+                    help="volume workload: paths per wave (rad_init max_paths)")
     ap.add_argument("--vol-grid", type=int, default=256)
     ap.add_argument("--serving-scenes", type=int, default=16, help="serving: resident scenes")
     ap.add_argument("--serving-jobs", type=int, default=120, help="serving: jobs per load point")

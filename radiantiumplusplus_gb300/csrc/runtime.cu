@@ -2130,8 +2130,9 @@ int rad_autotune(rad_scene* scene, const char* config_json, rad_tune_result* out
     std::vector<int> leaf = {2, 3, 4, 5, 6}, refill = {16, 20, 24, 28, 32}, perSm = {4, 6, 8}, shade = {64, 128, 256};
     std::vector<int> chunk = {TraceTune{}.volChunk};
     if (vol) {
-      // vol_path's part kernels: the lane top-up threshold and blocks per SM (at
-      // most 4 resident); the leaf vote and shade block do not apply
+      // vol_path's part kernels: the lane top-up threshold, blocks per SM (at
+      // most their occupancy, 4) and the chunk of steps; the leaf vote and shade
+      // block do not apply
       const TraceTune def;
       leaf = {def.leafFrac8};
       shade = {def.shadeBlock};
@@ -2198,7 +2199,7 @@ int rad_autotune(rad_scene* scene, const char* config_json, rad_tune_result* out
     };
     // coordinate descent from the defaults: each axis in turn, the others held at
     // the best values found so far
-    // (vol_path: the defaults' 8 blocks per SM run as the part kernels' 4, outside the list)
+    // (vol_path: the defaults' 8 blocks per SM run as each part kernel's occupancy, outside the list)
     const float volDefaultMs = vol ? time(TraceTune{}) : 0.f;
     TraceTune best;
     if (std::find(leaf.begin(), leaf.end(), best.leafFrac8) == leaf.end()) best.leafFrac8 = leaf[0];
