@@ -544,7 +544,7 @@ def run_guided(args, world, rank, local):
             j.close()
             return dt, st, f
 
-        timed(4, False)  # warm-up (graph capture, allocations)
+        timed(64, False)  # warm-up: the timed plain job's wave graphs (64 samples a wave) and allocations
         scene.guide_enable(gcfg)
         timed(4, True)
         clocks = ClockSampler(local)

@@ -691,6 +691,11 @@ struct GuideAdamArgs {
   uint32_t cap, steps, step;
 };
 
+// Hash-table entries ([0, split)) without a gradient in the batch keep their
+// parameters and moments (the lazy update of sparse embedding tables): a batch
+// touches a few percent of the table, so the step reads the gradient of every
+// entry but the moments and parameters of the touched ones only. The MLP's
+// parameters ([split, n)) take every step.
 __global__ void KGuideAdam(GuideAdamArgs a) {
   if (a.ctl) {
     uint32_t count = min(a.ctl[0], a.cap);
@@ -699,7 +704,9 @@ __global__ void KGuideAdam(GuideAdamArgs a) {
     a.gscale = 1.f / (float)batch;
   }
   for (uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; i < a.n; i += (uint64_t)gridDim.x * blockDim.x) {
-    float gi = a.g[i] * a.gscale;
+    const float graw = a.g[i];
+    if (graw == 0.f && i < a.split) continue;
+    float gi = graw * a.gscale;
     if (!isfinite(gi)) gi = 0.f;
     float m = a.b1 * a.m[i] + (1.f - a.b1) * gi;
     float v = a.b2 * a.v[i] + (1.f - a.b2) * gi * gi;
