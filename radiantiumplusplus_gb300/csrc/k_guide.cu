@@ -9,10 +9,10 @@
 //   KGuideAdam     -- Adam step, refreshes the fp16 copies
 // Inference runs the MLP on the fifth-generation tensor cores (tcgen05: M = 128
 // tiles, operands in shared memory, fp32 accumulator in TMEM; dtc.cuh).
-// Training's products (forward, dIn = G W and dW = G^T In over 64-record tiles)
-// run on mma.sync m16n8k16 (fp16 operands, fp32 accumulation), one warp per 16
-// or 32 rows, with the weights in shared memory padded for conflict-free
-// fragment loads.
+// Training runs on them too: 128-record tiles, the forward as in inference,
+// then per layer dIn = G W (M = 128 records) and dW = G^T In (M = the layer's
+// outputs padded to 128, K = records) with dW accumulated in TMEM over the
+// CTA's tiles.
 #include <algorithm>
 
 #include "dguide.cuh"
@@ -24,137 +24,11 @@ namespace rad {
 
 namespace {
 
-constexpr int kLd48 = 56;    // smem row stride (halves) of a 48-wide operand
-constexpr int kLd64 = 72;    // ... of a 64-wide operand
-constexpr int kActLd = 88;   // activation row: 88 halves = 44 floats of output
-// forward weights in shared memory, [out][in] with padded rows
-constexpr int kSW0 = 0;
-constexpr int kSW1 = kSW0 + kGHid * kLd48;
-constexpr int kSW2 = kSW1 + kGHid * kLd64;
-constexpr int kSW3 = kSW2 + kGHid * kLd64;
-constexpr int kSWEnd = kSW3 + kGOut * kLd64;  // 16256 halves
-
-enum { kRelu = 0, kMask = 1, kF32 = 2 };
-
-__device__ __forceinline__ void Mma16816(float (&d)[4], const uint32_t (&a)[4], const uint32_t (&b)[2]) {
-  asm volatile(
-      "mma.sync.aligned.m16n8k16.row.col.f32.f16.f16.f32 {%0,%1,%2,%3}, {%4,%5,%6,%7}, {%8,%9}, "
-      "{%0,%1,%2,%3};\n"
-      : "+f"(d[0]), "+f"(d[1]), "+f"(d[2]), "+f"(d[3])
-      : "r"(a[0]), "r"(a[1]), "r"(a[2]), "r"(a[3]), "r"(b[0]), "r"(b[1]));
-}
-
-__device__ __forceinline__ uint32_t Ld32(const __half* p) { return *reinterpret_cast<const uint32_t*>(p); }
 __device__ __forceinline__ uint32_t Pack2(__half lo, __half hi) {
   return (uint32_t)__half_as_ushort(lo) | ((uint32_t)__half_as_ushort(hi) << 16);
 }
 __device__ __forceinline__ uint32_t PackF2(float lo, float hi) {
   return Pack2(__float2half_rn(lo), __float2half_rn(hi));
-}
-
-// D[r][n] = sum_k A[r][k] Bm[n][k] over the warp's MT x 16 rows. A and the
-// output may alias (each 16-row tile is read completely before it is written).
-// Epilogues: kRelu -> fp16 max(0, x); kMask -> fp16 x where mask[r][n] > 0;
-// kF32 -> fp32, columns below `ldo` only.
-template <int K, int N, int MT, int MODE>
-__device__ __forceinline__ void WarpGemm(const __half* A, int lda, const __half* Bm, int ldb, void* out, int ldo,
-                                         const __half* mask, int ldm) {
-  const int lane = threadIdx.x & 31, g = lane >> 2, t = lane & 3;
-#pragma unroll
-  for (int mt = 0; mt < MT; mt++) {
-    float acc[N / 8][4];
-#pragma unroll
-    for (int i = 0; i < N / 8; i++) acc[i][0] = acc[i][1] = acc[i][2] = acc[i][3] = 0.f;
-#pragma unroll
-    for (int kk = 0; kk < K; kk += 16) {
-      const __half* ap = A + (mt * 16 + g) * lda + kk + 2 * t;
-      uint32_t a[4] = {Ld32(ap), Ld32(ap + 8 * lda), Ld32(ap + 8), Ld32(ap + 8 * lda + 8)};
-#pragma unroll
-      for (int nt = 0; nt < N / 8; nt++) {
-        const __half* bp = Bm + (nt * 8 + g) * ldb + kk + 2 * t;
-        uint32_t b[2] = {Ld32(bp), Ld32(bp + 8)};
-        Mma16816(acc[nt], a, b);
-      }
-    }
-    __syncwarp();
-#pragma unroll
-    for (int nt = 0; nt < N / 8; nt++) {
-      const int r0 = mt * 16 + g, c = nt * 8 + 2 * t;
-      if constexpr (MODE == kF32) {
-        if (c < ldo) {
-          float* o = static_cast<float*>(out);
-          o[r0 * ldo + c] = acc[nt][0];
-          o[r0 * ldo + c + 1] = acc[nt][1];
-          o[(r0 + 8) * ldo + c] = acc[nt][2];
-          o[(r0 + 8) * ldo + c + 1] = acc[nt][3];
-        }
-      } else {
-        float v0 = acc[nt][0], v1 = acc[nt][1], v2 = acc[nt][2], v3 = acc[nt][3];
-        if constexpr (MODE == kRelu) {
-          v0 = fmaxf(v0, 0.f);
-          v1 = fmaxf(v1, 0.f);
-          v2 = fmaxf(v2, 0.f);
-          v3 = fmaxf(v3, 0.f);
-        } else {
-          if (!(__half2float(mask[r0 * ldm + c]) > 0.f)) v0 = 0.f;
-          if (!(__half2float(mask[r0 * ldm + c + 1]) > 0.f)) v1 = 0.f;
-          if (!(__half2float(mask[(r0 + 8) * ldm + c]) > 0.f)) v2 = 0.f;
-          if (!(__half2float(mask[(r0 + 8) * ldm + c + 1]) > 0.f)) v3 = 0.f;
-        }
-        __half* o = static_cast<__half*>(out);
-        *reinterpret_cast<uint32_t*>(o + r0 * ldo + c) = PackF2(v0, v1);
-        *reinterpret_cast<uint32_t*>(o + (r0 + 8) * ldo + c) = PackF2(v2, v3);
-      }
-    }
-    __syncwarp();
-  }
-}
-
-// dW[n][k] += sum_r G[r][n] In[r][k] for n in [n0, n0 + 16), k < KIN, r < 64
-// (a 64-record tile). The warp owns those 16 rows of dW.
-template <int KIN>
-__device__ __forceinline__ void WarpGradW(const __half* G, int ldg, const __half* In, int ldi, float* dW, int n0) {
-  const int lane = threadIdx.x & 31, g = lane >> 2, t = lane & 3;
-  float acc[KIN / 8][4];
-#pragma unroll
-  for (int i = 0; i < KIN / 8; i++) acc[i][0] = acc[i][1] = acc[i][2] = acc[i][3] = 0.f;
-#pragma unroll
-  for (int rr = 0; rr < 64; rr += 16) {
-    const __half* gp = G + (rr + 2 * t) * ldg + n0 + g;
-    uint32_t a[4] = {Pack2(gp[0], gp[ldg]), Pack2(gp[8], gp[ldg + 8]), Pack2(gp[8 * ldg], gp[9 * ldg]),
-                     Pack2(gp[8 * ldg + 8], gp[9 * ldg + 8])};
-#pragma unroll
-    for (int kt = 0; kt < KIN / 8; kt++) {
-      const __half* bp = In + (rr + 2 * t) * ldi + kt * 8 + g;
-      uint32_t b[2] = {Pack2(bp[0], bp[ldi]), Pack2(bp[8 * ldi], bp[9 * ldi])};
-      Mma16816(acc[kt], a, b);
-    }
-  }
-#pragma unroll
-  for (int kt = 0; kt < KIN / 8; kt++) {
-    const int c = kt * 8 + 2 * t;
-    dW[(n0 + g) * KIN + c] += acc[kt][0];
-    dW[(n0 + g) * KIN + c + 1] += acc[kt][1];
-    dW[(n0 + g + 8) * KIN + c] += acc[kt][2];
-    dW[(n0 + g + 8) * KIN + c + 1] += acc[kt][3];
-  }
-}
-
-__device__ void LoadFwdWeights(const __half* gw, __half* s) {
-  const __half z = __float2half_rn(0.f);
-  for (int i = threadIdx.x; i < kGHid * kLd48; i += blockDim.x) {
-    int n = i / kLd48, k = i % kLd48;
-    s[kSW0 + i] = k < kGIn ? gw[kGW0 + n * kGIn + k] : z;
-  }
-  for (int i = threadIdx.x; i < kGHid * kLd64; i += blockDim.x) {
-    int n = i / kLd64, k = i % kLd64;
-    s[kSW1 + i] = k < kGHid ? gw[kGW1 + n * kGHid + k] : z;
-    s[kSW2 + i] = k < kGHid ? gw[kGW2 + n * kGHid + k] : z;
-  }
-  for (int i = threadIdx.x; i < kGOut * kLd64; i += blockDim.x) {
-    int n = i / kLd64, k = i % kLd64;
-    s[kSW3 + i] = k < kGHid ? gw[kGW3 + n * kGHid + k] : z;
-  }
 }
 
 __device__ __forceinline__ void GuidePosToUnit(const GuideDev& G, V3 P, float u[3]) {
@@ -482,22 +356,6 @@ __global__ void KGuideFinalize(PathBuffers B, GuideDev G) {
   if (blockIdx.x == 0 && threadIdx.x == 0 && G.recTotal) *G.recTotal += count;
 }
 
-namespace {
-constexpr int kTRec = 64;  // records per tile (4 warps x 16 rows)
-constexpr int kTB0 = kSWEnd;                 // W0^T [48][72]
-constexpr int kTB1 = kTB0 + kGIn * kLd64;    // W1^T [64][72]
-constexpr int kTB2 = kTB1 + kGHid * kLd64;   // W2^T [64][72]
-constexpr int kTB3 = kTB2 + kGHid * kLd64;   // W3^T [64][56]
-constexpr int kTX = kTB3 + kGHid * kLd48;    // X  [64][56]
-constexpr int kTH1 = kTX + kTRec * kLd48;    // H1 [64][72]
-constexpr int kTH2 = kTH1 + kTRec * kLd64;
-constexpr int kTH3 = kTH2 + kTRec * kLd64;
-constexpr int kTG0 = kTH3 + kTRec * kLd64;   // gradient ping [64][88] (or fp32 [64][44])
-constexpr int kTG1 = kTG0 + kTRec * kActLd;  // gradient pong
-constexpr int kTHalves = kTG1 + kTRec * kActLd;
-constexpr int kTrainSmem = kTHalves * 2 + kGWCount * 4 + kTRec * 5 * 4;
-}  // namespace
-
 struct GuideTrainArgs {
   GuideDev G;
   const float4* rec;     // records (kGRecF4 float4 each; r0..r3 are read)
@@ -508,173 +366,310 @@ struct GuideTrainArgs {
   float* gradTable;      // fp32, [level][entry][feature]
   float* gradW;          // fp32, kGWCount
   float* lossOut;        // fp32 loss sum (optional)
+  uint32_t* err;         // device error word
 };
 
-__global__ void __launch_bounds__(128, 1) KGuideTrain(GuideTrainArgs a) {
-  extern __shared__ __align__(16) unsigned char smraw[];
-  __half* sh = reinterpret_cast<__half*>(smraw);
-  float* dW = reinterpret_cast<float*>(smraw + kTHalves * 2);
-  float* sRec = dW + kGWCount;  // per record: wi xyz, p_bsdf, weight
+// ---- training on the fifth-generation tensor cores
+// One tile = 128 records (one per thread of a 4-warp CTA). Forward: the four
+// layers as in inference; each thread keeps its ReLU masks and also writes its
+// layer inputs transposed (feature-major, K = 128 records) for the weight
+// gradients. Backward, layer l = 3..0, one commit each:
+//   dW_l += G_l^T In_l  (M = out features padded to 128, N = in features,
+//                        K = the tile's 128 records; accumulated in TMEM over
+//                        all of the CTA's tiles)
+//   dIn  = G_l W_l      (M = 128 records, N = in features, K = out features)
+// where G_l is the output gradient of layer l (fp16), kept both record-major
+// (A of dIn) and feature-major (A of dW; rows beyond the layer's outputs hold
+// stale values that only reach accumulator rows that are never read). The
+// masked dIn is the next G; layer 0's dIn (the 32 grid features) is scattered
+// into the hash-table gradients. After the last tile the CTA adds its dW rows
+// to the global gradient. Every wait is bounded (kErrGuideTc, TMEM freed).
+constexpr uint32_t kTrWt0 = kTcW3 + kGOut * kGHid * 2;       // W0^T: N = 48 inputs, K = 64
+constexpr uint32_t kTrWt1 = kTrWt0 + kGIn * kGHid * 2;       // W1^T: 64 x 64
+constexpr uint32_t kTrWt2 = kTrWt1 + kGHid * kGHid * 2;      // W2^T: 64 x 64
+constexpr uint32_t kTrWt3 = kTrWt2 + kGHid * kGHid * 2;      // W3^T: N = 64, K = 48
+constexpr uint32_t kTrAct = kTrWt3 + kGHid * kGOut * 2;      // 128 x 64 activations (A of the forward)
+constexpr uint32_t kTrT0 = kTrAct + kTcRows * kGHid * 2;     // X^T: 48 x 128
+constexpr uint32_t kTrT1 = kTrT0 + kGIn * kTcRows * 2;       // H1^T: 64 x 128
+constexpr uint32_t kTrT2 = kTrT1 + kGHid * kTcRows * 2;
+constexpr uint32_t kTrT3 = kTrT2 + kGHid * kTcRows * 2;
+constexpr uint32_t kTrGf = kTrT3 + kGHid * kTcRows * 2;      // G record-major: 128 x 64
+constexpr uint32_t kTrGt = kTrGf + kTcRows * kGHid * 2;      // G feature-major: 128 (padded) x 128
+constexpr uint32_t kTrMisc = kTrGt + kTcRows * kTcRows * 2;  // mbarrier, TMEM address, fail flag
+constexpr int kTrainSmem = (int)kTrMisc + 16;
+constexpr uint32_t kTrCols = 512;                            // TMEM: scratch 0..63, dW3, dW2, dW1, dW0
+static_assert(kTrWt0 % 16 == 0 && kTrAct % 16 == 0 && kTrT0 % 16 == 0 && kTrGf % 16 == 0 && kTrGt % 16 == 0 &&
+                  kTrMisc % 16 == 0,
+              "descriptor addresses are 16-byte aligned");
+static_assert(kTrainSmem <= 227 * 1024, "training tile fits in shared memory");
+// TMEM column of dW_l: dW0 256..303, dW1 192.., dW2 128.., dW3 64..; 0..63 scratch
+__device__ __forceinline__ uint32_t TrDW(int l) { return 256u - 64u * (uint32_t)l; }
+
+// D[d] (+)= A x B^T over K, both operands K-major with K halves per row (thread 0).
+__device__ __forceinline__ void TcChain(uint32_t d, uint32_t aAddr, uint32_t bAddr, int K, uint32_t idesc, bool acc) {
+  for (int s = 0; s < K / 16; s++)
+    TcMma(d, TcSmemDesc(aAddr + 256u * s, 128u, 16u * K), TcSmemDesc(bAddr + 256u * s, 128u, 16u * K), idesc,
+          acc || s > 0);
+}
+
+// Shared-memory operands written by the threads become visible to the tensor
+// cores; thread 0 issues `issue` and commits; every thread waits (bounded).
+template <class F>
+__device__ __forceinline__ bool TcRun(uint64_t* mbar, uint32_t& phase, int* fail, F issue) {
+  FenceProxyAsync();
+  TcFenceBefore();
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    TcFenceAfter();
+    issue();
+    TcCommit(mbar);
+  }
+  const bool ok = MbarWait(mbar, phase, kTcWaitLimit);
+  if (!ok) atomicOr(fail, 1);
+  __syncthreads();
+  if (*fail) return false;
+  phase ^= 1u;
+  TcFenceAfter();
+  return true;
+}
+
+__device__ __forceinline__ void StoreHalfT(unsigned char* sm, uint32_t base, uint32_t feature, uint32_t r, float v) {
+  *reinterpret_cast<__half*>(sm + base + TcOffset(feature, r, kTcRows)) = __float2half_rn(v);
+}
+
+// This thread's row of the 64-column scratch accumulator after a forward layer:
+// ReLU, fp16, into the next layer's operand (record-major) and into In^T; the
+// ReLU mask is returned (bit k: activation k > 0).
+__device__ __forceinline__ uint64_t TrReluOut(unsigned char* sm, uint32_t tmemRow, uint32_t r, uint32_t tBase) {
+  uint64_t mask = 0;
+#pragma unroll
+  for (int c0 = 0; c0 < kGHid; c0 += 16) {
+    float v[16];
+    TcLoad16(tmemRow + c0, v);
+#pragma unroll
+    for (int i = 0; i < 16; i++) {
+      v[i] = fmaxf(v[i], 0.f);
+      if (v[i] > 0.f) mask |= 1ull << (c0 + i);
+    }
+#pragma unroll
+    for (int q = 0; q < 2; q++) {
+      uint4 w;
+      w.x = PackF2(v[8 * q + 0], v[8 * q + 1]);
+      w.y = PackF2(v[8 * q + 2], v[8 * q + 3]);
+      w.z = PackF2(v[8 * q + 4], v[8 * q + 5]);
+      w.w = PackF2(v[8 * q + 6], v[8 * q + 7]);
+      *reinterpret_cast<uint4*>(sm + kTrAct + TcOffset(r, c0 + 8 * q, kGHid)) = w;
+    }
+#pragma unroll
+    for (int i = 0; i < 16; i++) StoreHalfT(sm, tBase, (uint32_t)(c0 + i), r, v[i]);
+  }
+  return mask;
+}
+
+// This thread's row of dIn (scratch columns, 64 wide) masked by the ReLU mask
+// of the layer input, as the next output gradient (fp16, both layouts).
+__device__ __forceinline__ void TrMaskedGrad(unsigned char* sm, uint32_t tmemRow, uint32_t r, uint64_t mask) {
+#pragma unroll
+  for (int c0 = 0; c0 < kGHid; c0 += 16) {
+    float v[16];
+    TcLoad16(tmemRow + c0, v);
+#pragma unroll
+    for (int i = 0; i < 16; i++) v[i] = ((mask >> (c0 + i)) & 1ull) ? v[i] : 0.f;
+#pragma unroll
+    for (int q = 0; q < 2; q++) {
+      uint4 w;
+      w.x = PackF2(v[8 * q + 0], v[8 * q + 1]);
+      w.y = PackF2(v[8 * q + 2], v[8 * q + 3]);
+      w.z = PackF2(v[8 * q + 4], v[8 * q + 5]);
+      w.w = PackF2(v[8 * q + 6], v[8 * q + 7]);
+      *reinterpret_cast<uint4*>(sm + kTrGf + TcOffset(r, c0 + 8 * q, kGHid)) = w;
+    }
+#pragma unroll
+    for (int i = 0; i < 16; i++) StoreHalfT(sm, kTrGt, (uint32_t)(c0 + i), r, v[i]);
+  }
+}
+
+__global__ void __launch_bounds__(kTcRows, 1) KGuideTrainTc(GuideTrainArgs a) {
+  extern __shared__ __align__(1024) unsigned char sm[];
   const GuideDev& G = a.G;
-  const int tid = threadIdx.x, warp = tid >> 5;
-  // weights: forward [out][in] and transposed [in][out] copies
-  LoadFwdWeights(G.weights, sh);
-  const __half z = __float2half_rn(0.f);
+  const uint32_t r = threadIdx.x;
+  uint64_t* mbar = reinterpret_cast<uint64_t*>(sm + kTrMisc);
+  uint32_t* slot = reinterpret_cast<uint32_t*>(sm + kTrMisc + 8);
+  int* fail = reinterpret_cast<int*>(sm + kTrMisc + 12);
+  if (r == 0) {
+    MbarInit(mbar, 1);
+    *fail = 0;
+  }
+  if (r < 32) TcAlloc(slot, kTrCols);
+  // forward weights [out][in] and transposed [in][out], K-major
+  TcLoadWeights(G.weights, sm);
   const __half* gw = G.weights;
-  for (int i = tid; i < kGIn * kLd64; i += blockDim.x) {
-    int k = i / kLd64, n = i % kLd64;
-    sh[kTB0 + i] = n < kGHid ? gw[kGW0 + n * kGIn + k] : z;
+  for (int i = (int)r; i < kGIn * kGHid; i += blockDim.x) {
+    int n = i / kGHid, k = i % kGHid;  // n: input, k: output
+    *reinterpret_cast<__half*>(sm + kTrWt0 + TcOffset(n, k, kGHid)) = gw[kGW0 + k * kGIn + n];
   }
-  for (int i = tid; i < kGHid * kLd64; i += blockDim.x) {
-    int k = i / kLd64, n = i % kLd64;
-    sh[kTB1 + i] = n < kGHid ? gw[kGW1 + n * kGHid + k] : z;
-    sh[kTB2 + i] = n < kGHid ? gw[kGW2 + n * kGHid + k] : z;
+  for (int i = (int)r; i < kGHid * kGHid; i += blockDim.x) {
+    int n = i / kGHid, k = i % kGHid;
+    *reinterpret_cast<__half*>(sm + kTrWt1 + TcOffset(n, k, kGHid)) = gw[kGW1 + k * kGHid + n];
+    *reinterpret_cast<__half*>(sm + kTrWt2 + TcOffset(n, k, kGHid)) = gw[kGW2 + k * kGHid + n];
   }
-  for (int i = tid; i < kGHid * kLd48; i += blockDim.x) {
-    int k = i / kLd48, n = i % kLd48;
-    sh[kTB3 + i] = n < kGOut ? gw[kGW3 + n * kGHid + k] : z;
+  for (int i = (int)r; i < kGHid * kGOut; i += blockDim.x) {
+    int n = i / kGOut, k = i % kGOut;
+    *reinterpret_cast<__half*>(sm + kTrWt3 + TcOffset(n, k, kGOut)) = gw[kGW3 + k * kGHid + n];
   }
-  for (int i = tid; i < kGWCount; i += blockDim.x) dW[i] = 0.f;
+  FenceProxyAsync();
+  TcFenceBefore();
+  __syncthreads();
+  TcFenceAfter();
+  const uint32_t tmem = *slot;
+  const uint32_t tmemRow = tmem + ((32u * (r >> 5)) << 16);
+  uint32_t phase = 0;
+
   uint32_t count = a.ctl ? min(a.ctl[0], a.cap) : a.count;
   float norm = 1.f;
   if (a.ctl) {
     float s = __uint_as_float(a.ctl[1]);
     norm = (s > 0.f && count > 0) ? (float)count / s : 0.f;
   }
-  uint32_t batch = count > a.step ? (count - a.step + a.steps - 1) / a.steps : 0u;
-  __syncthreads();
-  __half* X = sh + kTX;
-  __half* H1 = sh + kTH1;
-  __half* H2 = sh + kTH2;
-  __half* H3 = sh + kTH3;
-  __half* G0 = sh + kTG0;
-  __half* G1 = sh + kTG1;
+  const uint32_t batch = count > a.step ? (count - a.step + a.steps - 1) / a.steps : 0u;
+  const uint32_t idH = TcIdescF16(kTcRows, kGHid), idO = TcIdescF16(kTcRows, kGOut);
   float lossSum = 0.f;
-  for (uint32_t tb = blockIdx.x * kTRec; tb < batch; tb += gridDim.x * kTRec) {
-    // ---- encode (two threads per record, eight levels each)
+  uint32_t tiles = 0;
+  bool ok = true;
+  for (uint32_t tb = blockIdx.x * kTcRows; tb < batch && ok; tb += gridDim.x * kTcRows, tiles++) {
+    // ---- encode: this thread's record into the layer-0 operand and X^T
+    const uint32_t j = tb + r;
+    const bool valid = j < batch;
+    uint32_t v[24];
+#pragma unroll
+    for (int i = 0; i < 24; i++) v[i] = 0u;
+    V3 wi{0.f, 0.f, 0.f};
+    float pb = 0.f, w = 0.f;
+    float4 r0 = make_float4(0.f, 0.f, 0.f, 0.f);
+    if (valid) {
+      const float4* rc = a.rec + (size_t)(j * a.steps + a.step) * kGRecF4;
+      r0 = rc[0];
+      const float4 r1 = rc[1], r2 = rc[2], r3 = rc[3];
+      TcEncodeRow(G, V3{r0.x, r0.y, r0.z}, V3{r1.x, r1.y, r1.z}, V3{r2.x, r2.y, r2.z}, v);
+      wi = V3{r3.x, r3.y, r3.z};
+      pb = r0.w;
+      w = fminf(r3.w * norm, a.wClamp);
+      if (!(w > 0.f)) w = 0.f;
+    }
+#pragma unroll
+    for (int c = 0; c < kGIn / 8; c++)
+      *reinterpret_cast<uint4*>(sm + kTrAct + TcOffset(r, 8 * c, kGIn)) =
+          make_uint4(v[4 * c], v[4 * c + 1], v[4 * c + 2], v[4 * c + 3]);
+#pragma unroll
+    for (int i = 0; i < 24; i++) {
+      *reinterpret_cast<uint16_t*>(sm + kTrT0 + TcOffset(2 * i, r, kTcRows)) = (uint16_t)(v[i] & 0xffffu);
+      *reinterpret_cast<uint16_t*>(sm + kTrT0 + TcOffset(2 * i + 1, r, kTcRows)) = (uint16_t)(v[i] >> 16);
+    }
+    // ---- forward
+    uint64_t mask[3];
+    const uint32_t fw[3] = {kTcW0, kTcW1, kTcW2}, tOut[3] = {kTrT1, kTrT2, kTrT3};
+    for (int l = 0; l < 3 && ok; l++) {
+      const int K = l == 0 ? kGIn : kGHid;
+      ok = TcRun(mbar, phase, fail, [&] { TcChain(tmem, SmemAddr(sm + kTrAct), SmemAddr(sm + fw[l]), K, idH, false); });
+      if (ok) mask[l] = TrReluOut(sm, tmemRow, r, tOut[l]);
+    }
+    if (!ok) break;
+    ok = TcRun(mbar, phase, fail, [&] { TcChain(tmem, SmemAddr(sm + kTrAct), SmemAddr(sm + kTcW3), kGHid, idO, false); });
+    if (!ok) break;
+    // ---- loss gradient at the outputs: G_3 in both layouts
     {
-      const int r = tid & 63, half = tid >> 6;
-      const uint32_t j = tb + r;
-      const bool valid = j < batch;
-      __half* row = X + r * kLd48;
-      if (valid) {
-        const float4* rc = a.rec + (size_t)(j * a.steps + a.step) * kGRecF4;
-        float4 r0 = rc[0], r1 = rc[1], r2 = rc[2], r3 = rc[3];
-        float u[3];
-        GuidePosToUnit(G, V3{r0.x, r0.y, r0.z}, u);
-        GuideEncodeLevels(G, u, half * 8, half * 8 + 8, row);
-        if (half == 0) {
-          GuideEncodeTail(V3{r1.x, r1.y, r1.z}, V3{r2.x, r2.y, r2.z}, row);
-          float w = fminf(r3.w * norm, a.wClamp);
-          sRec[r * 5 + 0] = r3.x;
-          sRec[r * 5 + 1] = r3.y;
-          sRec[r * 5 + 2] = r3.z;
-          sRec[r * 5 + 3] = r0.w;
-          sRec[r * 5 + 4] = (w > 0.f) ? w : 0.f;
-        }
-      } else {
-        for (int k = half * 24; k < half * 24 + 24; k += 2) *reinterpret_cast<uint32_t*>(row + k) = 0u;
-        if (half == 0)
-          for (int k = 0; k < 5; k++) sRec[r * 5 + k] = 0.f;
+      float o[kGOut], dO[kGOut];
+#pragma unroll
+      for (int c0 = 0; c0 < kGOut; c0 += 16) {
+        float t[16];
+        TcLoad16(tmemRow + c0, t);
+#pragma unroll
+        for (int i = 0; i < 16; i++) o[c0 + i] = c0 + i < kGOutUsed ? t[i] : 0.f;
       }
-    }
-    __syncthreads();
-    // ---- forward, warp w owns rows [16w, 16w + 16)
-    {
-      const int r0 = warp * 16;
-      WarpGemm<kGIn, kGHid, 1, kRelu>(X + r0 * kLd48, kLd48, sh + kSW0, kLd48, H1 + r0 * kLd64, kLd64, nullptr, 0);
-      WarpGemm<kGHid, kGHid, 1, kRelu>(H1 + r0 * kLd64, kLd64, sh + kSW1, kLd64, H2 + r0 * kLd64, kLd64, nullptr, 0);
-      WarpGemm<kGHid, kGHid, 1, kRelu>(H2 + r0 * kLd64, kLd64, sh + kSW2, kLd64, H3 + r0 * kLd64, kLd64, nullptr, 0);
-      WarpGemm<kGHid, kGOut, 1, kF32>(H3 + r0 * kLd64, kLd64, sh + kSW3, kLd64,
-                                      reinterpret_cast<float*>(G0) + r0 * (kActLd / 2), kActLd / 2, nullptr, 0);
-    }
-    __syncthreads();
-    // ---- loss gradient at the outputs (one thread per record)
-    if (tid < kTRec) {
-      const float* o = reinterpret_cast<const float*>(G0) + tid * (kActLd / 2);
-      float dO[kGOut];
-      float w = sRec[tid * 5 + 4];
-      float loss = 0.f;
       if (w > 0.f) {
-        float oo[kGOut];
-        for (int k = 0; k < kGOut; k++) oo[k] = k < kGOutUsed ? o[k] : 0.f;
-        loss = GuideLossGrad(oo, V3{sRec[tid * 5], sRec[tid * 5 + 1], sRec[tid * 5 + 2]}, sRec[tid * 5 + 3], w,
-                             G.logKMax, G.cMax, dO);
+        lossSum += GuideLossGrad(o, wi, pb, w, G.logKMax, G.cMax, dO);
       } else {
         for (int k = 0; k < kGOut; k++) dO[k] = 0.f;
       }
-      lossSum += loss;
-      __half* gr = G1 + tid * kActLd;
-      for (int k = 0; k < kGOut; k += 2) *reinterpret_cast<uint32_t*>(gr + k) = PackF2(dO[k], dO[k + 1]);
+#pragma unroll
+      for (int c = 0; c < kGOut / 8; c++)
+        *reinterpret_cast<uint4*>(sm + kTrGf + TcOffset(r, 8 * c, kGOut)) =
+            make_uint4(PackF2(dO[8 * c], dO[8 * c + 1]), PackF2(dO[8 * c + 2], dO[8 * c + 3]),
+                       PackF2(dO[8 * c + 4], dO[8 * c + 5]), PackF2(dO[8 * c + 6], dO[8 * c + 7]));
+      for (int k = 0; k < kGOut; k++) StoreHalfT(sm, kTrGt, (uint32_t)k, r, dO[k]);
     }
-    __syncthreads();
-    // ---- layer 3: dW3 += dO^T H3, dH3 = (dO W3) * [H3 > 0]
-    {
-      const int r0 = warp * 16;
-      if (warp < 3) WarpGradW<kGHid>(G1, kActLd, H3, kLd64, dW + kGW3, warp * 16);
-      WarpGemm<kGOut, kGHid, 1, kMask>(G1 + r0 * kActLd, kActLd, sh + kTB3, kLd48, G0 + r0 * kActLd, kActLd,
-                                       H3 + r0 * kLd64, kLd64);
+    // ---- backward: dW_l += G^T In_l and dIn = G W_l, layers 3, 2, 1
+    const bool acc = tiles > 0;
+    const uint32_t tIn[4] = {kTrT0, kTrT1, kTrT2, kTrT3}, wt[4] = {kTrWt0, kTrWt1, kTrWt2, kTrWt3};
+    for (int l = 3; l >= 1 && ok; l--) {
+      const int K = l == 3 ? kGOut : kGHid;
+      ok = TcRun(mbar, phase, fail, [&] {
+        TcChain(tmem + TrDW(l), SmemAddr(sm + kTrGt), SmemAddr(sm + tIn[l]), kTcRows, idH, acc);
+        TcChain(tmem, SmemAddr(sm + kTrGf), SmemAddr(sm + wt[l]), K, idH, false);
+      });
+      if (ok) TrMaskedGrad(sm, tmemRow, r, mask[l - 1]);
     }
-    __syncthreads();
-    {
-      const int r0 = warp * 16;
-      WarpGradW<kGHid>(G0, kActLd, H2, kLd64, dW + kGW2, warp * 16);
-      WarpGemm<kGHid, kGHid, 1, kMask>(G0 + r0 * kActLd, kActLd, sh + kTB2, kLd64, G1 + r0 * kActLd, kActLd,
-                                       H2 + r0 * kLd64, kLd64);
-    }
-    __syncthreads();
-    {
-      const int r0 = warp * 16;
-      WarpGradW<kGHid>(G1, kActLd, H1, kLd64, dW + kGW1, warp * 16);
-      WarpGemm<kGHid, kGHid, 1, kMask>(G1 + r0 * kActLd, kActLd, sh + kTB1, kLd64, G0 + r0 * kActLd, kActLd,
-                                       H1 + r0 * kLd64, kLd64);
-    }
-    __syncthreads();
-    {
-      const int r0 = warp * 16;
-      WarpGradW<kGIn>(G0, kActLd, X, kLd48, dW + kGW0, warp * 16);
-      // input gradient of the 32 grid features, fp32
-      WarpGemm<kGHid, 32, 1, kF32>(G0 + r0 * kActLd, kActLd, sh + kTB0, kLd64,
-                                   reinterpret_cast<float*>(G1) + r0 * (kActLd / 2), kActLd / 2, nullptr, 0);
-    }
-    __syncthreads();
+    if (!ok) break;
+    // ---- layer 0: dW0 += G^T X, dX = G W0 (N = 48; the 32 grid features are used)
+    ok = TcRun(mbar, phase, fail, [&] {
+      TcChain(tmem + TrDW(0), SmemAddr(sm + kTrGt), SmemAddr(sm + kTrT0), kTcRows, idO, acc);
+      TcChain(tmem, SmemAddr(sm + kTrGf), SmemAddr(sm + kTrWt0), kGHid, idO, false);
+    });
+    if (!ok) break;
+    float dx[32];
+    TcLoad16(tmemRow, *reinterpret_cast<float(*)[16]>(dx));
+    TcLoad16(tmemRow + 16, *reinterpret_cast<float(*)[16]>(dx + 16));
+    TcFenceBefore();  // the next tile's MMAs are issued after every thread's reads
     // ---- hash-table gradients (scatter)
-    {
-      const int r = tid & 63, half = tid >> 6;
-      const uint32_t j = tb + r;
-      if (j < batch && sRec[r * 5 + 4] > 0.f) {
-        const float4* rc = a.rec + (size_t)(j * a.steps + a.step) * kGRecF4;
-        float4 r0 = rc[0];
-        float u[3];
-        GuidePosToUnit(G, V3{r0.x, r0.y, r0.z}, u);
-        const float* dx = reinterpret_cast<const float*>(G1) + r * (kActLd / 2);
-        for (int l = half * 8; l < half * 8 + 8; l++) {
-          float g0 = dx[2 * l], g1 = dx[2 * l + 1];
-          if (g0 == 0.f && g1 == 0.f) continue;
-          uint32_t res = G.res[l];
-          uint32_t cx, cy, cz;
-          float tx, ty, tz;
-          GuideCell(u[0], res, cx, tx);
-          GuideCell(u[1], res, cy, ty);
-          GuideCell(u[2], res, cz, tz);
-          float2* gt = reinterpret_cast<float2*>(a.gradTable) + ((size_t)l << G.log2T);
-          for (int c = 0; c < 8; c++) {
-            uint32_t bx = c & 1u, by = (c >> 1) & 1u, bz = (c >> 2) & 1u;
-            float w = (bx ? tx : 1.f - tx) * (by ? ty : 1.f - ty) * (bz ? tz : 1.f - tz);
-            uint32_t idx = GuideGridIndex(cx + bx, cy + by, cz + bz, res, G.log2T);
-            atomicAdd(gt + idx, make_float2(w * g0, w * g1));
-          }
+    if (valid && w > 0.f) {
+      float u[3];
+      GuidePosToUnit(G, V3{r0.x, r0.y, r0.z}, u);
+      for (int l = 0; l < kGLevels; l++) {
+        const float g0 = dx[2 * l], g1 = dx[2 * l + 1];
+        if (g0 == 0.f && g1 == 0.f) continue;
+        const uint32_t res = G.res[l];
+        uint32_t cx, cy, cz;
+        float tx, ty, tz;
+        GuideCell(u[0], res, cx, tx);
+        GuideCell(u[1], res, cy, ty);
+        GuideCell(u[2], res, cz, tz);
+        float2* gt = reinterpret_cast<float2*>(a.gradTable) + ((size_t)l << G.log2T);
+        for (int c = 0; c < 8; c++) {
+          const uint32_t bx = c & 1u, by = (c >> 1) & 1u, bz = (c >> 2) & 1u;
+          const float cw = (bx ? tx : 1.f - tx) * (by ? ty : 1.f - ty) * (bz ? tz : 1.f - tz);
+          const uint32_t idx = GuideGridIndex(cx + bx, cy + by, cz + bz, res, G.log2T);
+          atomicAdd(gt + idx, make_float2(cw * g0, cw * g1));
         }
       }
     }
-    __syncthreads();
   }
-  for (int i = tid; i < kGWCount; i += blockDim.x)
-    if (dW[i] != 0.f) atomicAdd(a.gradW + i, dW[i]);
-  if (a.lossOut && tid < kTRec) {  // the loss threads are warps 0 and 1
+  // ---- this CTA's weight gradients: row r of dW_l (out feature r) in TMEM lane r
+  if (ok && tiles > 0 && r < (uint32_t)kGHid) {
+    const int outs[4] = {kGHid, kGHid, kGHid, kGOut}, ins[4] = {kGIn, kGHid, kGHid, kGHid};
+    const int base[4] = {kGW0, kGW1, kGW2, kGW3};
+    for (int l = 0; l < 4; l++) {
+      for (int c0 = 0; c0 < ins[l]; c0 += 16) {
+        float t[16];
+        TcLoad16(tmemRow + TrDW(l) + (uint32_t)c0, t);
+        if ((int)r < outs[l])
+          for (int i = 0; i < 16; i++)
+            if (t[i] != 0.f) atomicAdd(a.gradW + base[l] + (int)r * ins[l] + c0 + i, t[i]);
+      }
+    }
+  }
+  if (a.lossOut) {
     for (int o = 16; o > 0; o >>= 1) lossSum += __shfl_down_sync(0xffffffffu, lossSum, o);
-    if ((tid & 31) == 0 && lossSum != 0.f) atomicAdd(a.lossOut, lossSum);
+    if ((r & 31u) == 0 && lossSum != 0.f) atomicAdd(a.lossOut, lossSum);
   }
+  // teardown: on a timeout, one more bounded wait for the MMA still outstanding
+  if (*fail) {
+    MbarWait(mbar, phase, kTcWaitLimit);
+    if (r == 0) atomicOr(a.err, kErrGuideTc);
+  }
+  TcFenceBefore();
+  __syncthreads();
+  TcFenceAfter();
+  if (r < 32) TcDealloc(tmem, kTrCols);
 }
 
 struct GuideAdamArgs {
@@ -733,7 +728,7 @@ cudaError_t GuideKernelsInit() {
   if (e != cudaSuccess) return e;
   e = cudaFuncSetAttribute(KGuideQueryTc, cudaFuncAttributeMaxDynamicSharedMemorySize, kTcSmem);
   if (e != cudaSuccess) return e;
-  return cudaFuncSetAttribute(KGuideTrain, cudaFuncAttributeMaxDynamicSharedMemorySize, kTrainSmem);
+  return cudaFuncSetAttribute(KGuideTrainTc, cudaFuncAttributeMaxDynamicSharedMemorySize, kTrainSmem);
 }
 
 cudaError_t LaunchGuideInfer(const DevScene& S, const PathBuffers& B, const GuideDev& G, int depth, uint32_t maxCount,
@@ -767,11 +762,12 @@ cudaError_t LaunchGuideFinalize(const PathBuffers& B, const GuideDev& G, cudaStr
 
 cudaError_t LaunchGuideTrain(const GuideDev& G, const float4* rec, const uint32_t* ctl, uint32_t count, uint32_t cap,
                              uint32_t steps, uint32_t step, float wClamp, float* gradTable, float* gradW,
-                             float* lossOut, uint32_t maxBatch, cudaStream_t st) {
-  GuideTrainArgs a{G, rec, ctl, count, cap, steps, step, wClamp, gradTable, gradW, lossOut};
-  int blocks = (int)std::min<uint32_t>((maxBatch + kTRec - 1) / kTRec, (uint32_t)GuideGrid(1));
+                             float* lossOut, uint32_t maxBatch, uint32_t* err, cudaStream_t st) {
+  GuideTrainArgs a{G, rec, ctl, count, cap, steps, step, wClamp, gradTable, gradW, lossOut, err};
+  // one CTA per SM (its shared memory and 512 TMEM columns)
+  int blocks = (int)std::min<uint32_t>((maxBatch + kTcRows - 1) / kTcRows, (uint32_t)GuideGrid(1));
   if (blocks < 1) blocks = 1;
-  KGuideTrain<<<blocks, 128, kTrainSmem, st>>>(a);
+  KGuideTrainTc<<<blocks, kTcRows, kTrainSmem, st>>>(a);
   return cudaGetLastError();
 }
 

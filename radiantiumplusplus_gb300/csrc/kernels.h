@@ -273,9 +273,10 @@ cudaError_t LaunchGuideMixEval(const float4* mix, const float* dirs, const float
 cudaError_t LaunchGuideFinalize(const PathBuffers& B, const GuideDev& G, cudaStream_t st);
 // One training batch: records j * steps + step. With ctl, the count and the
 // mean weight come from the device (ctl[0], ctl[1]); else `count`, weights as given.
+// err: kErrGuideTc is or'ed in if a tensor-core wait gave up.
 cudaError_t LaunchGuideTrain(const GuideDev& G, const float4* rec, const uint32_t* ctl, uint32_t count, uint32_t cap,
                              uint32_t steps, uint32_t step, float wClamp, float* gradTable, float* gradW,
-                             float* lossOut, uint32_t maxBatch, cudaStream_t st);
+                             float* lossOut, uint32_t maxBatch, uint32_t* err, cudaStream_t st);
 // Adam step t (1-based). With ctl, the gradient scale is 1 / (size of batch `step`
 // of `steps`) from the device record count, and an empty batch changes nothing.
 // Parameters [0, split) step with lr, [split, n) with lr2.

@@ -596,7 +596,8 @@ void GuideTrainWave(GuideNet& net, const GuideDev& G, ProfSink& ps, rad_job* j, 
   uint32_t maxBatch = (G.recCap + S - 1) / S;
   for (uint32_t s = 0; s < S; s++) {
     Check(LaunchGuideTrain(G, G.rec, G.ctl, 0, G.recCap, S, s, net.cfg.weightClamp, net.g, net.g + net.nTable,
-                           reinterpret_cast<float*>(net.ctl + 2), maxBatch, lib.stream),
+                           reinterpret_cast<float*>(net.ctl + 2), maxBatch, lib.paths.counters + kMiscBase + 1,
+                           lib.stream),
           "guide train");
     net.step++;
     Check(LaunchGuideAdam(net.p, net.m, net.v, net.g, net.ph, net.nParams, net.cfg.lr, net.nTable, net.cfg.lrMlp,
@@ -2080,15 +2081,20 @@ int rad_guide_grad(rad_scene* scene, const float* records, int64_t n, float* gra
     cudaStreamSynchronize(lib.stream);
     Check(cudaMemsetAsync(net.g, 0, net.nParams * sizeof(float), lib.stream), "memset");
     GuideDev G = GuideView(net);
+    uint32_t* err = lib.paths.counters + kMiscBase + 1;
+    Check(cudaMemsetAsync(err, 0, sizeof(uint32_t), lib.stream), "memset");
     if (n > 0)
       Check(LaunchGuideTrain(G, drec.p, nullptr, (uint32_t)n, (uint32_t)n, 1, 0, INFINITY, net.g, net.g + net.nTable,
-                             dloss.p, (uint32_t)n, lib.stream),
+                             dloss.p, (uint32_t)n, err, lib.stream),
             "guide gradient");
     Check(cudaMemcpyAsync(grad, net.g, net.nParams * sizeof(float), cudaMemcpyDeviceToHost, lib.stream), "copy");
     float l = 0.f;
+    uint32_t errWord = 0;
     Check(cudaMemcpyAsync(&l, dloss.p, 4, cudaMemcpyDeviceToHost, lib.stream), "copy");
+    Check(cudaMemcpyAsync(&errWord, err, sizeof(uint32_t), cudaMemcpyDeviceToHost, lib.stream), "copy");
     Check(cudaMemsetAsync(net.g, 0, net.nParams * sizeof(float), lib.stream), "memset");
     Check(cudaStreamSynchronize(lib.stream), "sync");
+    if (errWord) throw Error{RAD_ERR_DEVICE_CHECK, "guide network: a tensor-core wait gave up"};
     if (loss) *loss = l;
   });
 }
