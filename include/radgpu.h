@@ -245,8 +245,10 @@ typedef struct rad_guide_info_t {
  * lr_mlp (0.001), train_fraction (0.25), train_path_shift (4: 1 in 16 paths
  * records training vertices), train_depth (8), steps_per_wave (8),
  * record_capacity (2^20), weight_clamp (32), log_kappa_max (5), c_max (0.6),
- * seed (5). A checkpoint carries the network, not these settings. Fails while
- * jobs of the scene are live. */
+ * seed (5), lazy_table (1: an Adam step leaves hash-table entries without a
+ * gradient in its batch untouched; 0: every parameter takes every step). A
+ * checkpoint carries the network, not these settings. Fails while jobs of the
+ * scene are live. */
 RAD_API int rad_guide_enable(rad_scene* scene, const char* config_json);
 RAD_API int rad_guide_info(rad_scene* scene, rad_guide_info_t* info);
 /* Serialises parameters and Adam moments into buf (host); *needed gets the

@@ -205,6 +205,7 @@ void GuideParseConfig(const char* json, GuideConfig& c) {
   f("c_max", c.cMax);
   f("lr_mlp", c.lrMlp);
   u("seed", c.seed);
+  u("lazy_table", c.lazyTable);
   if (c.trainShift > 31) throw std::runtime_error("train_path_shift must be <= 31");
   if (!(c.logKappaMax > kGLogKMin) || c.logKappaMax > 12.f) throw std::runtime_error("log_kappa_max must be in (-6, 12]");
   if (!(c.cMax >= 0.f) || c.cMax > 0.95f) throw std::runtime_error("c_max must be in [0, 0.95]");

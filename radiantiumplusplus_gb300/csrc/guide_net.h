@@ -26,6 +26,7 @@ struct GuideConfig {
   float logKappaMax = 5.f;      // vMF concentration cap, log scale (kappa <= ~148: lobes of ~5 degrees)
   float cMax = 0.6f;            // guide selection probability cap (weights grow at most 1 / (1 - cMax))
   uint32_t seed = 5;
+  uint32_t lazyTable = 1;       // Adam leaves table entries without a gradient in the batch untouched
 };
 
 struct GuideNet {

@@ -682,15 +682,16 @@ struct GuideAdamArgs {
   float lr, b1, b2, eps, gscale, bc1, bc2;
   uint64_t split;  // parameters [split, n) use lr2
   float lr2;
+  uint64_t lazySplit;  // parameters below it without a gradient are left untouched (split, or 0)
   const uint32_t* ctl;  // when set: gscale = 1 / (records of batch `step`), no update for an empty batch
   uint32_t cap, steps, step;
 };
 
-// Hash-table entries ([0, split)) without a gradient in the batch keep their
-// parameters and moments (the lazy update of sparse embedding tables): a batch
-// touches a few percent of the table, so the step reads the gradient of every
-// entry but the moments and parameters of the touched ones only. The MLP's
-// parameters ([split, n)) take every step.
+// Hash-table entries ([0, lazySplit), the table when the lazy update is on)
+// without a gradient in the batch keep their parameters and moments (the lazy
+// update of sparse embedding tables): a batch touches a few percent of the
+// table, so the step reads the gradient of every entry but the moments and
+// parameters of the touched ones only. The MLP's parameters take every step.
 __global__ void KGuideAdam(GuideAdamArgs a) {
   if (a.ctl) {
     uint32_t count = min(a.ctl[0], a.cap);
@@ -700,7 +701,7 @@ __global__ void KGuideAdam(GuideAdamArgs a) {
   }
   for (uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; i < a.n; i += (uint64_t)gridDim.x * blockDim.x) {
     const float graw = a.g[i];
-    if (graw == 0.f && i < a.split) continue;
+    if (graw == 0.f && i < a.lazySplit) continue;
     float gi = graw * a.gscale;
     if (!isfinite(gi)) gi = 0.f;
     float m = a.b1 * a.m[i] + (1.f - a.b1) * gi;
@@ -773,9 +774,9 @@ cudaError_t LaunchGuideTrain(const GuideDev& G, const float4* rec, const uint32_
 
 cudaError_t LaunchGuideAdam(float* p, float* m, float* v, float* g, __half* ph, uint64_t n, float lr, uint64_t split,
                             float lr2, float b1, float b2, float eps, float gscale, uint32_t t, const uint32_t* ctl,
-                            uint32_t cap, uint32_t steps, uint32_t step, cudaStream_t st) {
+                            uint32_t cap, uint32_t steps, uint32_t step, bool lazyTable, cudaStream_t st) {
   GuideAdamArgs a{p,     m,   v,   g,   ph,  n,   lr,   b1,   b2,  eps, gscale, 1.f - powf(b1, (float)t),
-                  1.f - powf(b2, (float)t), split, lr2, ctl, cap, steps, step};
+                  1.f - powf(b2, (float)t), split, lr2, lazyTable ? split : 0u, ctl, cap, steps, step};
   KGuideAdam<<<GuideGrid(8), 256, 0, st>>>(a);
   return cudaGetLastError();
 }

@@ -282,7 +282,7 @@ cudaError_t LaunchGuideTrain(const GuideDev& G, const float4* rec, const uint32_
 // Parameters [0, split) step with lr, [split, n) with lr2.
 cudaError_t LaunchGuideAdam(float* p, float* m, float* v, float* g, __half* ph, uint64_t n, float lr, uint64_t split,
                             float lr2, float b1, float b2, float eps, float gscale, uint32_t t, const uint32_t* ctl,
-                            uint32_t cap, uint32_t steps, uint32_t step, cudaStream_t st);
+                            uint32_t cap, uint32_t steps, uint32_t step, bool lazyTable, cudaStream_t st);
 cudaError_t LaunchFloatToHalf(const float* src, __half* dst, uint64_t n, cudaStream_t st);
 
 }  // namespace rad

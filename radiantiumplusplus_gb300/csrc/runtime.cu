@@ -601,7 +601,8 @@ void GuideTrainWave(GuideNet& net, const GuideDev& G, ProfSink& ps, rad_job* j, 
           "guide train");
     net.step++;
     Check(LaunchGuideAdam(net.p, net.m, net.v, net.g, net.ph, net.nParams, net.cfg.lr, net.nTable, net.cfg.lrMlp,
-                          net.cfg.beta1, net.cfg.beta2, net.cfg.eps, 1.f, net.step, G.ctl, G.recCap, S, s, lib.stream),
+                          net.cfg.beta1, net.cfg.beta2, net.cfg.eps, 1.f, net.step, G.ctl, G.recCap, S, s,
+                          net.cfg.lazyTable != 0, lib.stream),
           "guide adam");
   }
   ps.End(7, a);
