@@ -195,14 +195,14 @@ def run_ours(args, world, rank, local):
     import radiantiumplusplus_gb300 as rad
 
     torch.cuda.set_device(local)
-    rad.init({"device": local})
+    rad.init({"device": local, "max_paths": args.max_paths})
     hbm_peak, peak_src = _peaks()
     with tempfile.TemporaryDirectory(prefix="rad_bench_") as tmp:
         path = make_scene(tmp, seed=2)
         t0 = time.perf_counter()
         scene = rad.Scene.from_file(path)
         load_s = time.perf_counter() - t0
-        spp_step = 1
+        spp_step = args.spp_per_step
         # launch parameters of the traversal kernels for this scene (rad_autotune, not timed)
         tune = scene.autotune() if not args.no_tune else {"refill_busy": 20, "blocks_per_sm": 8, "leaf_frac8": 4,
                                                              "shade_block": 128,
@@ -215,7 +215,9 @@ def run_ours(args, world, rank, local):
         nodes_per_ray = cs["trav_nodes_closest"] / max(1, cs["rays_closest"])
         prims_per_ray = cs["trav_prims_closest"] / max(1, cs["rays_closest"])
         # warm-up
-        j = scene.submit(spp=max(1, args.warmup) * spp_step, first_sample=20_000)
+        # warm-up: at least 8 samples, so that its waves hold as many samples as the timed job's
+        # (their CUDA graphs are captured here, outside the timed region)
+        j = scene.submit(spp=max(8, args.warmup) * spp_step, first_sample=20_000)
         j.wait()
         j.close()
         # ---- device-timed value: one job of K samples per pixel, events on the library stream
@@ -229,8 +231,8 @@ def run_ours(args, world, rank, local):
         barrier(world)
         st = job.stats()
         job.close()
-        # per-kernel breakdown (events around every launch, so no graph replay): 2 extra samples, not timed
-        pj = scene.submit(spp=2, first_sample=40_000, profile=True)
+        # per-kernel breakdown (events around every launch, so no graph replay): one more step, not timed
+        pj = scene.submit(spp=max(2, spp_step), first_sample=40_000, profile=True)
         pj.wait()
         pst = pj.stats()
         pj.close()
@@ -238,7 +240,8 @@ def run_ours(args, world, rank, local):
         samples = st["samples"] * world
         value = samples / gpu_s
         mrays = (st["rays_closest"] + st["rays_shadow"]) * world / gpu_s / 1e6
-        # ---- e2e through the C ABI with host buffers: submit 1 spp, wait, film -> pinned host
+        # ---- e2e through the C ABI with host buffers: per step submit a job of the step's samples, wait,
+        # film -> pinned host
         pinned = torch.empty((H, W, 3), dtype=torch.float32, pin_memory=True)
         host_film = pinned.numpy()
         barrier(world)
@@ -252,7 +255,7 @@ def run_ours(args, world, rank, local):
         torch.cuda.synchronize()
         e2e_s = allreduce_max(world, time.perf_counter() - t0)
         barrier(world)
-        clk = clocks.stop()  # sampled through both timed regions (and the 2-spp profile between them)
+        clk = clocks.stop()  # sampled through both timed regions (and the profiled step between them)
         e2e_value = args.steps * W * H * spp_step * world / e2e_s
         # ---- roofline for the dominant kernel
         kern = {"extend": pst["ms_extend"], "shade": pst["ms_shade"], "shadow": pst["ms_shadow"],
@@ -278,6 +281,7 @@ def run_ours(args, world, rank, local):
                    "width": W, "height": H, "spp_per_step": spp_step, "max_depth": MAX_DEPTH, "rr_depth": 3,
                    "parallelism": "replicas" if world > 1 else "single_gpu",
                    "l2": "inputs larger than L2: resident scene + path state > 129 MB",
+                   "max_paths": args.max_paths,
                    "scene_load_s": round(load_s, 3),
                    "autotune": {"refill_busy": tune["refill_busy"], "blocks_per_sm": tune["blocks_per_sm"],
                                 "shade_block": tune["shade_block"],
@@ -287,7 +291,7 @@ def run_ours(args, world, rank, local):
         "mrays_per_s": mrays,
         "rays_per_sample": (st["rays_closest"] + st["rays_shadow"]) / max(1, st["samples"]),
         "gpu_launches": st["kernel_launches"],
-        "kernel_ms_profiled_2spp": {k: round(v, 3) for k, v in kern.items()},
+        "kernel_ms_profiled_step": {k: round(v, 3) for k, v in kern.items()},
         "roofline": {"bound": "hbm", "kernel": "extend (BVH8 closest hit)", "achieved": achieved, "peak": hbm_peak,
                      "unit": "GB/s", "frac": achieved / hbm_peak, "traffic": traffic,
                      "traffic_source": "ncu dram__bytes_read.sum + dram__bytes_write.sum over one wave of the tuned "
@@ -318,7 +322,7 @@ def run_volume(args, world, rank, local):
     import radiantiumplusplus_gb300 as rad
     from radiantiumplusplus_gb300 import scenes
     torch.cuda.set_device(local)
-    # waves of max_paths paths (samples of whole pixel rows): 4 samples of the 1024^2 frame per wave
+    # waves of max_paths paths (samples of whole pixel rows): 8 samples of the 1024^2 frame per wave
     rad.init({"device": local, "max_paths": args.vol_max_paths})
     res = args.vol_res
     with tempfile.TemporaryDirectory(prefix="rad_bench_vol_") as tmp:
@@ -737,7 +741,11 @@ def main():
     ap.add_argument("--guided-config", default="{}", help="JSON of rad_guide_enable settings for the guided jobs")
     ap.add_argument("--no-tune", action="store_true", help="skip rad_autotune (keeps launch indices fixed for ncu)")
     ap.add_argument("--vol-res", type=int, default=1024)
-    ap.add_argument("--vol-max-paths", type=int, default=1 << 22,
+    ap.add_argument("--max-paths", type=int, default=1 << 23,
+                    help="path workload: paths per wave (rad_init max_paths; 2^23 = 4 samples of 1080p)")
+    ap.add_argument("--spp-per-step", type=int, default=4,
+                    help="path workload: samples per pixel of one step (one job of the e2e loop)")
+    ap.add_argument("--vol-max-paths", type=int, default=1 << 23,
                     help="volume workload: paths per wave (rad_init max_paths)")
     ap.add_argument("--vol-grid", type=int, default=256)
     ap.add_argument("--serving-scenes", type=int, default=16, help="serving: resident scenes")
