@@ -38,14 +38,13 @@ sys.path.insert(0, ROOT)
 
 W, H = 1920, 1080
 MAX_DEPTH = 16
-# DRAM bytes (read + written) per closest-hit ray of KExtend on this scene, from one ncu capture of a whole
-# wave (16 launches) with the tuned launch parameters: 593.0 MB for 1,731,983 rays at a 960x540 frame of the
-# same scene (the BVH and primitives are the full scene's; traffic per ray follows the BVH and the ray mix, not
-# the frame size). The algorithmic bytes per ray are ~6x larger: L1/L2 serve the rest.
-EXTEND_DRAM_BYTES_PER_RAY = 342.4
-# Issue-side counters of the same capture (bounce-1 launch): the kernel's limiter.
-EXTEND_ISSUE = {"lanes_active_per_warp_inst": 15.48, "issue_active_pct": 72.4, "alu_pipe_pct": 58.5,
-                "fma_pipe_pct": 27.5}
+# DRAM bytes (read + written) per closest-hit ray of KExtend on this scene, from one ncu capture of the 16
+# launches of one timed wave of this bench (4 samples of the 1080p frame, default launch parameters): 8.009 GB
+# for 27.7 M closest-hit rays. The algorithmic bytes per ray are ~7x larger: L1/L2 serve the rest.
+EXTEND_DRAM_BYTES_PER_RAY = 288.9
+# Issue-side counters of a bounce-1 launch (ncu --set full, 1080p frame, 1-sample waves): the kernel's limiter.
+EXTEND_ISSUE = {"lanes_active_per_warp_inst": 16.51, "issue_active_pct": 76.8, "alu_pipe_pct": 65.6,
+                "fma_pipe_pct": 30.5}
 BYTES_QUEUE, BYTES_RAY, BYTES_HIT, BYTES_NODE, BYTES_PRIM = 4, 32, 32, 80, 48
 
 
@@ -294,14 +293,14 @@ def run_ours(args, world, rank, local):
         "kernel_ms_profiled_step": {k: round(v, 3) for k, v in kern.items()},
         "roofline": {"bound": "hbm", "kernel": "extend (BVH8 closest hit)", "achieved": achieved, "peak": hbm_peak,
                      "unit": "GB/s", "frac": achieved / hbm_peak, "traffic": traffic,
-                     "traffic_source": "ncu dram__bytes_read.sum + dram__bytes_write.sum over one wave of the tuned "
-                                       "kernel (342.4 B per closest-hit ray) x closest-hit rays per launch",
+                     "traffic_source": "ncu dram__bytes_read.sum + dram__bytes_write.sum over the 16 launches of "
+                                       "one timed wave (288.9 B per closest-hit ray) x closest-hit rays per launch",
                      "achieved_is": "algorithmic bytes (nodes, primitives, ray, hit) per launch / launch time; "
                                     "mostly served by L1/L2",
                      "dram_gbs": dram_gbs, "dram_frac": dram_gbs / hbm_peak,
                      "limiter": "instruction issue (ALU pipe), not HBM: see issue",
                      "issue": dict(EXTEND_ISSUE, simt_efficiency=EXTEND_ISSUE["lanes_active_per_warp_inst"] / 32.0,
-                                   source="ncu --set full, bounce-1 launch, 960x540 frame of this scene"),
+                                   source="ncu --set full, bounce-1 launch, 1080p frame of this scene"),
                      "peak_source": peak_src, "dominant_kernel_by_time": dominant,
                      "nodes_per_ray": nodes_per_ray, "prims_per_ray": prims_per_ray,
                      "bytes_per_ray": BYTES_QUEUE + BYTES_RAY + BYTES_HIT + nodes_per_ray * BYTES_NODE
