@@ -352,6 +352,7 @@ __global__ void __launch_bounds__(kBdptBlock) KBdptRound1Head(DevScene S, PathBu
 __global__ void __launch_bounds__(kBdptBlock, 8)
     KBdptShadow(DevScene S, PathBuffers B, BdptBuffers V, int t, float4* film, int refillBusy, int leafFrac8) {
   const uint32_t count = min(B.counters[kShadowBase + (t - 1)], V.shCap);
+  if (blockIdx.x * blockDim.x >= count) return;  // blocks past one thread per ray leave at once
   uint32_t* fetch = B.counters + kFetchBase + 2 * (t - 1) + 1;
   uint32_t* err = B.counters + kMiscBase + 1;
   const uint32_t lane = threadIdx.x & 31u;

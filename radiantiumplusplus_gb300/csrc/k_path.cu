@@ -153,6 +153,9 @@ template <bool COUNT, bool MIX>
 __global__ void __launch_bounds__(kBlock, 8)
     KExtend(DevScene S0, PathBuffers B, int depth, unsigned long long* trav, int refillBusy, int leafFrac8) {
   const uint32_t count = B.counters[depth];
+  // Blocks past one thread per queued ray leave at once: late bounces hold few
+  // rays, and every warp's first fetch is an atomic on the one queue counter.
+  if (blockIdx.x * blockDim.x >= count) return;
   const uint32_t* qin = B.q[depth & 1];
   uint32_t* fetch = B.counters + kFetchBase + 2 * depth;
   uint32_t* err = B.counters + kMiscBase + 1;
@@ -520,6 +523,7 @@ template <bool COUNT, bool MIX>
 __global__ void __launch_bounds__(kBlock, 8)
     KShadow(DevScene S0, PathBuffers B, int depth, unsigned long long* trav, int refillBusy, int leafFrac8) {
   const uint32_t count = B.counters[kShadowBase + depth];
+  if (blockIdx.x * blockDim.x >= count) return;  // as KExtend
   uint32_t* fetch = B.counters + kFetchBase + 2 * depth + 1;
   uint32_t* err = B.counters + kMiscBase + 1;
   const uint32_t lane = threadIdx.x & 31u;

@@ -642,6 +642,9 @@ __global__ void __launch_bounds__(kVolBlock, 4)
   const uint32_t lane = threadIdx.x & 31u;
   const uint32_t in = cur * kVolActs + (uint32_t)ACT;
   const uint32_t n = FRESH ? count : V.cnt[in];
+  // blocks past one thread per queued path leave at once (their first fetch
+  // would be an atomic on the one queue head)
+  if (blockIdx.x * blockDim.x >= n) return;
   uint32_t* head = V.cnt + 2 * kVolActs + ACT;
   VolPathState* states = static_cast<VolPathState*>(V.state);
   VolPathState p;
