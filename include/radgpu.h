@@ -139,7 +139,9 @@ RAD_API int rad_last_error(char* buf, size_t size);
 RAD_API int rad_version(int32_t* major, int32_t* minor);
 /* No counterpart in the reference. Device bytes counted against the admission
  * budget (resident scenes, job films including films parked with a scene for
- * its next job, path-state buffers) and the budget itself. */
+ * its next job, path-state buffers; the `vol_path` wavefront's per-path states
+ * and queues, about 400 B per max_paths slot, from the first `vol_path` wave
+ * on) and the budget itself. */
 RAD_API int rad_device_usage(uint64_t* used_bytes, uint64_t* budget_bytes);
 
 /* ---- scenes (BuildContext::SetFromJson + Build, build_context.cpp:47-321) -- */
