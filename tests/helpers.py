@@ -168,6 +168,24 @@ def volume(dirpath, w=48, h=48, spp=4, grid=32, max_depth=32):
     return write(dirpath, "vol_%dx%d_%d" % (w, h, grid), sc, assets)
 
 
+def volume_variant(dirpath, variant, w=32, h=32):
+    """The fBm volume box (24^3 grid) with its cube made an index-matched boundary
+    (no BSDF), or with a glass sphere of homogeneous medium beside it."""
+    sc, assets = scenes.volume_box(width=w, height=h, spp=1, grid=24)
+    cube = sc["scene"][0]
+    if variant == "index_matched":
+        del cube["bsdf"]
+    elif variant == "homogeneous_sphere":
+        sc["scene"].append({"to_world": {"translate": [1.6, 0.8, 0.6], "scale": [0.6, 0.6, 0.6]},
+                            "shape": {"type": "sphere"},
+                            "bsdf": {"type": "rough_glass", "int_ior": 1.4, "ext_ior": 1.0, "alpha": 0.1},
+                            "in_medium": {"type": "homogeneous", "sigma_t": [1.5, 2.0, 2.5], "albedo": 0.8,
+                                          "scale": 1.0, "phase": {"type": "isotropic_phase"}}})
+    else:
+        raise ValueError(variant)
+    return write(dirpath, "vol_" + variant, sc, assets)
+
+
 def directions(rng, n):
     d = rng.normal(size=(n, 3))
     d /= np.linalg.norm(d, axis=1, keepdims=True)

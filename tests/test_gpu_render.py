@@ -19,7 +19,7 @@ import os
 import numpy as np
 import pytest
 
-from helpers import box, lights, materials, sample_parity, spheres, volume, write
+from helpers import box, lights, materials, sample_parity, spheres, volume, volume_variant, write
 from radiantiumplusplus_gb300 import scenes
 
 pytestmark = pytest.mark.gpu
@@ -56,6 +56,24 @@ def test_volpath_samples(rad, oracle, scene_dir):
     path, text, d = volume(scene_dir, 32, 32, 2, grid=24)
     g, o = rad.Scene.from_file(path), oracle.OracleScene(text, d)
     _sample_parity(g, o, 2, 0.99)
+    g.close()
+
+
+@pytest.mark.parametrize("variant", ["index_matched", "homogeneous_sphere"])
+def test_volpath_media_variants(rad, oracle, scene_dir, variant):
+    """vol_path through an index-matched boundary and through a homogeneous
+    medium in a glass sphere: samples against the oracle, and the wavefront's
+    film equals the persistent kernel's."""
+    path, text, d = volume_variant(scene_dir, variant)
+    g, o = rad.Scene.from_file(path), oracle.OracleScene(text, d)
+    _sample_parity(g, o, 2, 0.99)
+    films = []
+    for persistent in (False, True):
+        j = g.submit(spp=4, seed=9, vol_persistent=persistent)
+        j.wait()
+        films.append(j.film())
+        j.close()
+    assert np.array_equal(films[0], films[1]) and films[0].mean() > 0
     g.close()
 
 

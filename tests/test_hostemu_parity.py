@@ -18,7 +18,8 @@ import numpy as np
 import pytest
 
 import hemu_lib
-from helpers import box, bsdf_sweep, directions, lights, materials, spheres, textured, volume, write
+from helpers import (box, bsdf_sweep, directions, lights, materials, spheres, textured, volume, volume_variant,
+                     write)
 from radiantiumplusplus_gb300 import scenes
 
 
@@ -194,6 +195,19 @@ def test_render_samples_fbm_volume_256_bit_exact(oracle, tmp_path):
 
 
 VOL_WAVEFRONT = 256  # hemu_render_samples: run vol_path as the per-event wavefront
+
+
+@pytest.mark.parametrize("variant", ["index_matched", "homogeneous_sphere"])
+def test_volume_media_variants_bit_exact(oracle, scene_dir, variant):
+    """vol_path through an index-matched boundary (a medium in a shape without a
+    BSDF: the path crosses it and continues in the next loop iteration) and
+    through a homogeneous medium in a glass sphere next to the grid, with both
+    schedules (persistent kernel and per-event wavefront) against the oracle."""
+    path, text, d = volume_variant(scene_dir, variant)
+    h, o = hemu_lib.HemuScene(text, d), oracle.OracleScene(text, d)
+    _samples_bit_exact(h, o, 2048, seed=31)
+    _samples_bit_exact(h, o, 2048, seed=32, vol_mode=VOL_WAVEFRONT)
+    h.close()
 
 
 def test_volume_wavefront_bit_exact(oracle, scene_dir):
