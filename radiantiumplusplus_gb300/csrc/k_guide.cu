@@ -242,13 +242,16 @@ __device__ __forceinline__ void TcTeardown(uint32_t tmem, uint64_t* mbar, uint32
 __global__ void __launch_bounds__(kTcRows, 1)
     KGuideInferTc(DevScene S, PathBuffers B, GuideDev G, int depth) {
   extern __shared__ __align__(1024) unsigned char smtc[];
+  const uint32_t* cnt = B.counters + kClassBase + depth * kShadeClasses;
+  const uint32_t n1 = cnt[SC_DIFFUSE], n2 = cnt[SC_METAL], n4 = cnt[SC_DISNEY], n5 = cnt[SC_GENERIC];
+  const uint32_t total = n1 + n2 + n4 + n5;
+  // CTAs without a tile leave before the weight load and the TMEM allocation
+  // (late bounces hold few queries)
+  if (blockIdx.x * kTcRows >= total) return;
   uint64_t* mbar;
   int* fail;
   const uint32_t tmem = TcSetup(G, smtc, mbar, fail);
   uint32_t phase = 0;
-  const uint32_t* cnt = B.counters + kClassBase + depth * kShadeClasses;
-  const uint32_t n1 = cnt[SC_DIFFUSE], n2 = cnt[SC_METAL], n4 = cnt[SC_DISNEY], n5 = cnt[SC_GENERIC];
-  const uint32_t total = n1 + n2 + n4 + n5;
   for (uint32_t base = blockIdx.x * kTcRows; base < total; base += gridDim.x * kTcRows) {
     const uint32_t q = base + threadIdx.x;
     const bool valid = q < total;
@@ -289,6 +292,7 @@ __global__ void __launch_bounds__(kTcRows, 1)
 __global__ void __launch_bounds__(kTcRows, 1)
     KGuideQueryTc(GuideDev G, const float* queries, uint32_t n, float* raw, float4* mix, uint32_t* err) {
   extern __shared__ __align__(1024) unsigned char smtc[];
+  if (blockIdx.x * kTcRows >= n) return;  // as KGuideInferTc
   uint64_t* mbar;
   int* fail;
   const uint32_t tmem = TcSetup(G, smtc, mbar, fail);
@@ -493,6 +497,10 @@ __global__ void __launch_bounds__(kTcRows, 1) KGuideTrainTc(GuideTrainArgs a) {
   extern __shared__ __align__(1024) unsigned char sm[];
   const GuideDev& G = a.G;
   const uint32_t r = threadIdx.x;
+  const uint32_t count = a.ctl ? min(a.ctl[0], a.cap) : a.count;
+  const uint32_t batch = count > a.step ? (count - a.step + a.steps - 1) / a.steps : 0u;
+  // CTAs without a tile leave before the weight loads and the TMEM allocation
+  if (blockIdx.x * kTcRows >= batch) return;
   uint64_t* mbar = reinterpret_cast<uint64_t*>(sm + kTrMisc);
   uint32_t* slot = reinterpret_cast<uint32_t*>(sm + kTrMisc + 8);
   int* fail = reinterpret_cast<int*>(sm + kTrMisc + 12);
@@ -525,13 +533,11 @@ __global__ void __launch_bounds__(kTcRows, 1) KGuideTrainTc(GuideTrainArgs a) {
   const uint32_t tmemRow = tmem + ((32u * (r >> 5)) << 16);
   uint32_t phase = 0;
 
-  uint32_t count = a.ctl ? min(a.ctl[0], a.cap) : a.count;
   float norm = 1.f;
   if (a.ctl) {
     float s = __uint_as_float(a.ctl[1]);
     norm = (s > 0.f && count > 0) ? (float)count / s : 0.f;
   }
-  const uint32_t batch = count > a.step ? (count - a.step + a.steps - 1) / a.steps : 0u;
   const uint32_t idH = TcIdescF16(kTcRows, kGHid), idO = TcIdescF16(kTcRows, kGOut);
   float lossSum = 0.f;
   uint32_t tiles = 0;
