@@ -514,7 +514,7 @@ def run_guided(args, world, rank, local):
     import radiantiumplusplus_gb300 as rad
     from radiantiumplusplus_gb300 import scenes
     torch.cuda.set_device(local)
-    rad.init({"device": local})
+    rad.init({"device": local, "max_paths": args.guided_max_paths})
     Wg, Hg = args.guided_res
     with tempfile.TemporaryDirectory(prefix="rad_bench_guided_") as tmp:
         sc, assets = scenes.guided_room(n_spheres=args.guided_spheres, width=Wg, height=Hg, spp=64, max_depth=16)
@@ -575,6 +575,7 @@ def run_guided(args, world, rank, local):
             "steps": 1, "warmup": 1, "higher_is_better": False, "scaling": "weak", "vs_baseline": None,
             "dtype": "f32 (guide network fp16 weights, fp32 accumulation)", "data": "synthetic (seeded generator)",
             "config": {"workload": "guided_room", "spheres": args.guided_spheres, "width": Wg, "height": Hg,
+                       "max_paths": args.guided_max_paths,
                        "max_depth": 16, "room": 200, "opening": 5, "irradiance": 1000,
                        "reference": "plain render, %d spp" % args.guided_ref_spp, "ref_mean": float(ref.mean()),
                        "relmse_eps": eps,
@@ -739,6 +740,7 @@ def main():
     ap.add_argument("--guided-ref-spp", type=int, default=1 << 20)
     ap.add_argument("--guided-spp", type=int, nargs="+", default=[8, 16, 24, 32, 48, 64])
     ap.add_argument("--guided-config", default="{}", help="JSON of rad_guide_enable settings for the guided jobs")
+    ap.add_argument("--guided-max-paths", type=int, default=1 << 21, help="guided workload: rad_init max_paths")
     ap.add_argument("--no-tune", action="store_true", help="skip rad_autotune (keeps launch indices fixed for ncu)")
     ap.add_argument("--vol-res", type=int, default=1024)
     ap.add_argument("--max-paths", type=int, default=1 << 23,
