@@ -356,13 +356,20 @@ const VolWave& EnsureVolWave() {
   if (lib.vol.state) return lib.vol;
   const uint32_t P = lib.maxPaths;
   VolWave V{};
-  auto& o = lib.volAllocs;
-  uint64_t& b = lib.volBytes;
-  V.state = DevAlloc<uint8_t>((size_t)P * VolStateBytes(), o, b);
-  V.q = DevAlloc<uint32_t>((size_t)2 * kVolActs * P, o, b);
-  V.cnt = DevAlloc<uint32_t>(kVolCountWords, o, b);
+  std::vector<void*> o;
+  uint64_t b = 0;
+  try {
+    V.state = DevAlloc<uint8_t>((size_t)P * VolStateBytes(), o, b);
+    V.q = DevAlloc<uint32_t>((size_t)2 * kVolActs * P, o, b);
+    V.cnt = DevAlloc<uint32_t>(kVolCountWords, o, b);
+    if (!lib.hVolWord) Check(cudaMallocHost(&lib.hVolWord, kVolCountWords * sizeof(uint32_t)), "cudaMallocHost");
+  } catch (...) {
+    FreeAll(o);  // nothing half-allocated stays behind
+    throw;
+  }
   V.capacity = P;
-  if (!lib.hVolWord) Check(cudaMallocHost(&lib.hVolWord, kVolCountWords * sizeof(uint32_t)), "cudaMallocHost");
+  lib.volAllocs = std::move(o);
+  lib.volBytes = b;
   lib.used += b;
   lib.vol = V;
   return lib.vol;
