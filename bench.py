@@ -425,7 +425,7 @@ def run_renderers(args, world, rank, local):
     import radiantiumplusplus_gb300 as rad
     from radiantiumplusplus_gb300 import scenes
     torch.cuda.set_device(local)
-    rad.init({"device": local})
+    rad.init({"device": local, "max_paths": args.renderers_max_paths, "bdpt_scratch_bytes": args.bdpt_scratch})
     Wr, Hr = args.renderers_res
     npix = Wr * Hr
     out = {}
@@ -491,6 +491,7 @@ def run_renderers(args, world, rank, local):
             "warmup": args.warmup, "ms_per_step": b["gpu_ms"] / args.steps, "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded generator, no dataset)",
             "config": {"workload": "many_spheres_renderers", "spheres": 10000, "triangles": 3200000,
+                       "max_paths": args.renderers_max_paths, "bdpt_scratch_bytes": args.bdpt_scratch,
                        "width": Wr, "height": Hr, "bdpt_max_depth": args.bdpt_depth, "bdpt_rr_depth": 5,
                        "particle_max_depth": MAX_DEPTH, "l2": "inputs larger than L2: resident scene > 129 MB"},
             "gpu_launches": b["gpu_launches"], "clocks": clk, "renderers": out}
@@ -735,6 +736,8 @@ def main():
     ap.add_argument("--bdpt-depth", type=int, default=MAX_DEPTH, help="renderers: bdpt max_depth")
     ap.add_argument("--renderers-res", type=int, nargs=2, default=[W, H], help="renderers: frame size")
     ap.add_argument("--bdpt-cpu-row-step", type=int, default=8, help="renderers: oracle bdpt row sample")
+    ap.add_argument("--renderers-max-paths", type=int, default=1 << 23, help="renderers: rad_init max_paths")
+    ap.add_argument("--bdpt-scratch", type=int, default=16 << 30, help="renderers: rad_init bdpt_scratch_bytes")
     ap.add_argument("--guided-res", type=int, nargs=2, default=[240, 135])
     ap.add_argument("--guided-spheres", type=int, default=10000)
     ap.add_argument("--guided-ref-spp", type=int, default=1 << 20)

@@ -120,7 +120,9 @@ typedef struct rad_stats {
 /* ---- library ------------------------------------------------------------ */
 /* config_json may be NULL. Keys: "device" (int), "budget_bytes" (admission
  * budget for resident scenes + films, default 150e9), "max_paths" (paths in
- * flight per wave), "mix_jobs" (default 1: plain `path` jobs running together
+ * flight per wave, default 2^21; larger waves raise a lone job's throughput),
+ * "bdpt_scratch_bytes" (device bytes a `bdpt` wave's subpath vertices and
+ * visibility rays may take, default 2^32; it sets the bdpt wave size), "mix_jobs" (default 1: plain `path` jobs running together
  * share the launches of each wave), "share_exponent" (default 0: a mixed wave
  * gives its jobs path slots in proportion to (remaining samples)^exponent -- 0
  * equal shares, 1 in proportion to the work left), "deadline_ns_per_sample"

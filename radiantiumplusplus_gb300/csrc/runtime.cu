@@ -174,6 +174,11 @@ namespace {
 constexpr size_t kMaxWavesInFlight = 2;
 constexpr int kMixRing = (int)kMaxWavesInFlight + 1;
 
+// Device bytes the bdpt scratch may take by default (rad_init
+// "bdpt_scratch_bytes"): the wave size follows from the scene's vertex cap
+// (2 subpaths x cap vertices + cap visibility rays a sample).
+constexpr uint64_t kBdptScratchBytes = 4ull << 30;
+
 struct Lib {
   bool inited = false;
   int device = 0;
@@ -217,6 +222,7 @@ struct Lib {
   BdptBuffers bdpt{};
   std::vector<void*> bdptAllocs;
   uint64_t bdptBytes = 0;
+  uint64_t bdptScratch = kBdptScratchBytes;
   // vol_path wavefront: per-path loop states and part queues, allocated with the first vol_path wave
   VolWave vol{};
   std::vector<void*> volAllocs;
@@ -296,6 +302,7 @@ void InitLocked(const char* cfg) {
     if (const JValue* v = c.get("device")) lib.device = (int)v->n;
     if (const JValue* v = c.get("budget_bytes")) lib.budget = (uint64_t)v->n;
     if (const JValue* v = c.get("max_paths")) lib.maxPaths = (uint32_t)v->n;
+    if (const JValue* v = c.get("bdpt_scratch_bytes")) lib.bdptScratch = (uint64_t)v->n;
     if (const JValue* v = c.get("mix_jobs")) lib.mixJobs = v->n != 0;
     if (const JValue* v = c.get("share_exponent")) lib.shareExp = (float)v->n;
     if (const JValue* v = c.get("deadline_ns_per_sample")) lib.edfNsPerSample = v->n;
@@ -343,9 +350,6 @@ struct ProfSink {
 };
 
 // ---- bdpt ---------------------------------------------------------------------
-// Device bytes the bdpt scratch may take: the wave size follows from the
-// scene's vertex cap (2 subpaths x cap vertices + cap visibility rays a sample).
-constexpr uint64_t kBdptScratchBytes = 4ull << 30;
 
 int BdptCap(const DevScene& S) {
   return S.maxDepth >= 0 ? std::min(kMaxBdptVertices, S.maxDepth + 2) : kMaxBdptVertices;
@@ -385,7 +389,7 @@ const BdptBuffers& EnsureBdpt(int cap) {
   uint64_t per = 2ull * cap * kBVertBytes + (uint64_t)cap * (3 * sizeof(float4) + 4) + 3 * sizeof(float4) + 20;
   // at most 2^24 samples a wave: a sorted connection packs its sample slot in 24 bits
   uint32_t nw = (uint32_t)std::min<uint64_t>(std::min<uint64_t>(lib.maxPaths, 1u << 24),
-                                             std::max<uint64_t>(1024, kBdptScratchBytes / per));
+                                             std::max<uint64_t>(1024, lib.bdptScratch / per));
   BdptBuffers V{};
   auto& o = lib.bdptAllocs;
   uint64_t& b = lib.bdptBytes;
