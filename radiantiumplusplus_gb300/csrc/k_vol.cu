@@ -625,14 +625,13 @@ RD void VolPush(const VolWave& V, int dst, uint32_t idx) {
 
 // One loop part over its queue. A lane runs its path's part (the top repeats
 // through null collisions, the NEE through its transmittance steps) until the
-// path ends, moves to another part or has run `chunk` steps of this one.
-// Lanes are topped up in batches: once at
-// most `refillBelow` lanes of the warp still run a path (or none do), the lanes
-// whose paths moved store their states and queue them at their next part, and
-// the idle lanes take the next paths of this part's queue -- so the state
-// copies run with many lanes at once instead of one lane at a time. FRESH
-// (first round's top): the queue is the wave's paths 0..count-1, started from
-// the generate stage's rays.
+// path ends, moves to another part or has run `chunk` steps of this one. Lanes
+// are topped up in batches: once at most `refillBelow` lanes of the warp still
+// run a path (or none do), the lanes whose paths moved store their states and
+// queue them at their next part, and the idle lanes take the next paths of
+// this part's queue -- so the state copies run with many lanes at once instead
+// of one lane at a time. FRESH (first round's top): the queue is the wave's
+// paths 0..count-1, started from the generate stage's rays.
 // 128 registers (4 blocks per SM): capping the top, surface and NEE parts at 80
 // registers (6 blocks) spills little but ran 5% slower on the 1024^2 fBm frame.
 template <int ACT, bool FRESH, bool BRICKS, bool HALF>
