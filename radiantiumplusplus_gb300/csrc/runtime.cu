@@ -253,6 +253,14 @@ cudaEvent_t GetEvent() {
 
 void AllocPaths(Lib& lib) {
   uint32_t P = lib.maxPaths;
+  // refuse path buffers the device cannot hold before allocating any of them
+  const uint64_t perPath = 8 * sizeof(float4) + sizeof(uint2) + sizeof(uint32_t) + sizeof(HitRec) +
+                           (2 + kShadeClasses) * sizeof(uint32_t) + sizeof(uint8_t);
+  size_t freeB = 0, totalB = 0;
+  if (cudaMemGetInfo(&freeB, &totalB) == cudaSuccess && (uint64_t)P * perPath > (uint64_t)freeB)
+    throw Error{RAD_ERR_INVALID_ARG, "max_paths " + std::to_string(P) + " needs " +
+                                         std::to_string((uint64_t)P * perPath) + " bytes of path buffers; " +
+                                         std::to_string((uint64_t)freeB) + " free on the device"};
   PathBuffers& B = lib.paths;
   auto& o = lib.pathAllocs;
   uint64_t& b = lib.pathBytes;
@@ -297,6 +305,8 @@ void InitLocked(const char* cfg) {
     }
     return;
   }
+  const uint32_t maxPaths0 = lib.maxPaths;
+  const uint64_t bdptScratch0 = lib.bdptScratch;
   if (cfg && *cfg) {
     JValue c = JsonReader::Parse(cfg);
     if (const JValue* v = c.get("device")) lib.device = (int)v->n;
@@ -319,8 +329,27 @@ void InitLocked(const char* cfg) {
   Check(cudaSetDevice(lib.device), "cudaSetDevice");
   Check(cudaDeviceGetAttribute(&lib.sms, cudaDevAttrMultiProcessorCount, lib.device), "attribute");
   Check(cudaStreamCreateWithFlags(&lib.stream, cudaStreamNonBlocking), "cudaStreamCreate");
-  Check(GuideKernelsInit(), "guide kernel attributes");
-  AllocPaths(lib);
+  try {
+    Check(GuideKernelsInit(), "guide kernel attributes");
+    AllocPaths(lib);
+  } catch (...) {
+    // a failed first init (e.g. path buffers larger than the device) leaves
+    // nothing behind, and a later rad_init starts from the default sizes
+    FreeAll(lib.pathAllocs);
+    lib.pathBytes = 0;
+    lib.paths = PathBuffers{};
+    lib.mixDev = nullptr;
+    if (lib.hCounters) cudaFreeHost(lib.hCounters);
+    if (lib.mixHost) cudaFreeHost(lib.mixHost);
+    lib.hCounters = nullptr;
+    lib.mixHost = nullptr;
+    cudaStreamDestroy(lib.stream);
+    lib.stream = nullptr;
+    lib.maxPaths = maxPaths0;
+    lib.bdptScratch = bdptScratch0;
+    cudaGetLastError();
+    throw;
+  }
   lib.stop = false;
   lib.worker = std::thread(WorkerMain);
   lib.inited = true;

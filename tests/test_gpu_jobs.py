@@ -1,5 +1,6 @@
 """Serving loop: jobs of different scenes submitted together are admitted,
 interleaved on the device, and each result is identical to rendering it alone."""
+import os
 import time
 
 import numpy as np
@@ -8,6 +9,8 @@ import pytest
 from helpers import box, spheres
 
 pytestmark = pytest.mark.gpu
+
+HERE = os.path.dirname(os.path.abspath(__file__))
 
 
 def test_mix_equals_alone(rad, scene_dir):
@@ -83,6 +86,35 @@ def test_graph_replay_equals_direct_launches(rad, scene_dir):
     g.close()
     d.close()
     s.close()
+
+
+def test_init_refuses_path_buffers_larger_than_the_device(scene_dir):
+    """A first rad_init whose path buffers cannot fit (max_paths 4e9, ~1 TB) fails
+    with an error before allocating, leaves nothing behind, and a second
+    rad_init with the defaults brings the library up; a render then works."""
+    import subprocess
+    import sys
+    import textwrap
+    path = box(scene_dir, 24, 16, 2)[0]
+    script = textwrap.dedent("""
+        import sys
+        sys.path.insert(0, {root!r})
+        import numpy as np
+        import radiantiumplusplus_gb300 as rad
+        try:
+            rad.init({{"device": 0, "max_paths": 4000000000}})
+            print("NO ERROR")
+        except rad.RadError as e:
+            print("REFUSED", e.code)
+        rad.init({{"device": 0}})
+        s = rad.Scene.from_file({path!r})
+        f = s.render(spp=2)
+        print("RENDER", float(f.mean()) > 0)
+        s.close()
+    """).format(root=os.path.dirname(HERE), path=path)
+    r = subprocess.run([sys.executable, "-c", script], capture_output=True, text=True, timeout=300)
+    assert r.returncode == 0, r.stderr[-2000:]
+    assert "REFUSED" in r.stdout and "RENDER True" in r.stdout, r.stdout
 
 
 def test_autotune_picks_parameters_and_keeps_results(rad, scene_dir):
