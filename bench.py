@@ -39,10 +39,10 @@ sys.path.insert(0, ROOT)
 W, H = 1920, 1080
 MAX_DEPTH = 16
 # DRAM bytes (read + written) per closest-hit ray of KExtend on this scene, from one ncu capture of the 16
-# launches of one timed wave of this bench (4 samples of the 1080p frame, tuned launch parameters): 8.038 GB
-# for 27.7 M closest-hit rays (288.9 B with the default parameters). The algorithmic bytes per ray are ~7x
-# larger: L1/L2 serve the rest.
-EXTEND_DRAM_BYTES_PER_RAY = 290.0
+# launches of one timed wave of this bench (16 samples of the 1080p frame, tuned launch parameters): 31.85 GB
+# for 110.9 M closest-hit rays (290.0 B with 4-sample waves). The algorithmic bytes per ray are ~7x larger:
+# L1/L2 serve the rest.
+EXTEND_DRAM_BYTES_PER_RAY = 287.3
 # Issue-side counters of a bounce-1 launch (ncu --set full, 1080p frame, 1-sample waves): the kernel's limiter.
 EXTEND_ISSUE = {"lanes_active_per_warp_inst": 16.51, "issue_active_pct": 76.8, "alu_pipe_pct": 65.6,
                 "fma_pipe_pct": 30.5}
@@ -299,7 +299,7 @@ def run_ours(args, world, rank, local):
         "roofline": {"bound": "hbm", "kernel": "extend (BVH8 closest hit)", "achieved": achieved, "peak": hbm_peak,
                      "unit": "GB/s", "frac": achieved / hbm_peak, "traffic": traffic,
                      "traffic_source": "ncu dram__bytes_read.sum + dram__bytes_write.sum over the 16 launches of "
-                                       "one timed wave (290.0 B per closest-hit ray) x closest-hit rays per launch",
+                                       "one timed wave (287.3 B per closest-hit ray) x closest-hit rays per launch",
                      "achieved_is": "algorithmic bytes (nodes, primitives, ray, hit) per launch / launch time; "
                                     "mostly served by L1/L2",
                      "dram_gbs": dram_gbs, "dram_frac": dram_gbs / hbm_peak,
@@ -750,9 +750,9 @@ def main():
     ap.add_argument("--guided-max-paths", type=int, default=1 << 21, help="guided workload: rad_init max_paths")
     ap.add_argument("--no-tune", action="store_true", help="skip rad_autotune (keeps launch indices fixed for ncu)")
     ap.add_argument("--vol-res", type=int, default=1024)
-    ap.add_argument("--max-paths", type=int, default=1 << 23,
-                    help="path workload: paths per wave (rad_init max_paths; 2^23 = 4 samples of 1080p)")
-    ap.add_argument("--spp-per-step", type=int, default=4,
+    ap.add_argument("--max-paths", type=int, default=1 << 25,
+                    help="path workload: paths per wave (rad_init max_paths; 2^25 = 16 samples of 1080p)")
+    ap.add_argument("--spp-per-step", type=int, default=16,
                     help="path workload: samples per pixel of one step (one job of the e2e loop)")
     ap.add_argument("--vol-max-paths", type=int, default=1 << 23,
                     help="volume workload: paths per wave (rad_init max_paths)")
