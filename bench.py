@@ -326,7 +326,7 @@ def run_volume(args, world, rank, local):
     import radiantiumplusplus_gb300 as rad
     from radiantiumplusplus_gb300 import scenes
     torch.cuda.set_device(local)
-    # waves of max_paths paths (samples of whole pixel rows): 8 samples of the 1024^2 frame per wave
+    # waves of max_paths paths (samples of whole pixel rows): up to 16 samples of the 1024^2 frame per wave
     rad.init({"device": local, "max_paths": args.vol_max_paths})
     res = args.vol_res
     with tempfile.TemporaryDirectory(prefix="rad_bench_vol_") as tmp:
@@ -754,7 +754,7 @@ def main():
                     help="path workload: paths per wave (rad_init max_paths; 2^25 = 16 samples of 1080p)")
     ap.add_argument("--spp-per-step", type=int, default=16,
                     help="path workload: samples per pixel of one step (one job of the e2e loop)")
-    ap.add_argument("--vol-max-paths", type=int, default=1 << 23,
+    ap.add_argument("--vol-max-paths", type=int, default=1 << 24,
                     help="volume workload: paths per wave (rad_init max_paths)")
     ap.add_argument("--vol-grid", type=int, default=256)
     ap.add_argument("--serving-scenes", type=int, default=16, help="serving: resident scenes")
