@@ -740,8 +740,8 @@ def main():
     ap.add_argument("--bdpt-depth", type=int, default=MAX_DEPTH, help="renderers: bdpt max_depth")
     ap.add_argument("--renderers-res", type=int, nargs=2, default=[W, H], help="renderers: frame size")
     ap.add_argument("--bdpt-cpu-row-step", type=int, default=8, help="renderers: oracle bdpt row sample")
-    ap.add_argument("--renderers-max-paths", type=int, default=1 << 23, help="renderers: rad_init max_paths")
-    ap.add_argument("--bdpt-scratch", type=int, default=16 << 30, help="renderers: rad_init bdpt_scratch_bytes")
+    ap.add_argument("--renderers-max-paths", type=int, default=1 << 24, help="renderers: rad_init max_paths")
+    ap.add_argument("--bdpt-scratch", type=int, default=32 << 30, help="renderers: rad_init bdpt_scratch_bytes")
     ap.add_argument("--guided-res", type=int, nargs=2, default=[240, 135])
     ap.add_argument("--guided-spheres", type=int, default=10000)
     ap.add_argument("--guided-ref-spp", type=int, default=1 << 20)
