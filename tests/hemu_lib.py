@@ -29,6 +29,7 @@ def lib():
         L.hemu_bsdf_eval.argtypes = [ctypes.c_char_p, P, P, ctypes.c_int64, P, P]
         L.hemu_bsdf_sample.argtypes = [ctypes.c_char_p, P, P, ctypes.c_int64, P, P, P, P, P]
         L.hemu_render_samples.argtypes = [P, P, P, ctypes.c_int64, ctypes.c_uint32, ctypes.c_uint32, P]
+        L.hemu_render_mixed.argtypes = [P, ctypes.c_int, ctypes.c_uint32, ctypes.c_uint32, P, P]
         L.hemu_set_nudge.argtypes = [ctypes.c_uint64]
         L.hemu_set_nudge_config.argtypes = [ctypes.c_uint32, ctypes.c_uint32]
         L.hemu_set_nudge_target.argtypes = [ctypes.c_int64, ctypes.c_int32]
@@ -89,6 +90,19 @@ class HemuScene:
         out = np.zeros((pixels.shape[0], 3), np.float32)
         _check(lib().hemu_render_samples(self.h, _p(pixels), _p(samples), pixels.shape[0], seed, vol_mode, _p(out)))
         return out
+
+
+def render_mixed(scenes, npix, spw, sample0, seeds):
+    """One mixed wave of the given scenes' jobs (all npix[k] pixels, spw samples
+    from sample0, each with its seed); returns per job its (spw * npix, 3)
+    radiance, path s * npix + j being pixel j, sample sample0 + s."""
+    n = len(scenes)
+    arr = (ctypes.c_void_p * n)(*[sc.h for sc in scenes])
+    outs = [np.zeros((spw * npx, 3), np.float32) for npx in npix]
+    optr = (ctypes.c_void_p * n)(*[o.ctypes.data for o in outs])
+    sd = np.ascontiguousarray(seeds, np.uint32)
+    _check(lib().hemu_render_mixed(arr, n, spw, sample0, _p(sd), optr))
+    return outs
 
 
 def set_nudge(seed):

@@ -406,6 +406,66 @@ int hemu_bsdf_sample(const char* json, const float* wi, const float* u, int64_t 
   });
 }
 
+// A mixed wave of n jobs (the serving loop's RunMixedWave): job k renders every
+// pixel of scene k at samples [sample0, sample0 + spw) with seed seeds[k], all
+// jobs' paths in the same launches of the MIX kernels (generate, extend, shade
+// classes, shadow). out[k]: job k's per-path radiance, path s * npix + j being
+// pixel j, sample sample0 + s.
+int hemu_render_mixed(void** scenes, int n, uint32_t spw, uint32_t sample0, const uint32_t* seeds, float** out) {
+  return Guarded([&] {
+    if (n < 1 || n > kMaxMix) throw std::runtime_error("1 to kMaxMix jobs");
+    std::vector<MixJob> tab((size_t)n);
+    uint32_t total = 0;
+    int iters = 1;
+    for (int k = 0; k < n; k++) {
+      const DevScene& S = static_cast<HemuScene*>(scenes[k])->S;
+      if (S.isVol || S.isAO || S.isParticle || S.isBdpt || S.maxDepth < 0)
+        throw std::runtime_error("mixed waves hold plain path jobs of bounded depth");
+      const uint32_t npix = (uint32_t)S.cam.width * (uint32_t)S.cam.height;
+      MixJob J{};
+      J.S = S;
+      J.pixelBegin = 0;
+      J.npc = npix;
+      J.spw = spw;
+      J.sample = sample0;
+      J.seed = seeds[k];
+      J.count = npix * spw;
+      J.pathBegin = total;
+      total += J.count;
+      tab[(size_t)k] = J;
+      iters = std::max(iters, S.maxDepth);
+    }
+    iters = std::min(iters, kMaxBounce);
+    HostPaths P(total);
+    std::vector<uint8_t> job(total, 0);
+    PathBuffers& B = P.B;
+    B.job = job.data();
+    B.mix = tab.data();
+    const DevScene& S0 = tab[0].S;
+    uint32_t gen = std::max<uint32_t>(total, (uint32_t)kCounterWords);
+    Grid((gen + kBlock - 1) / kBlock, kBlock, [&] { KGenerateMix(B, total, (uint32_t)n); });
+    GuideDev none{};
+    for (int d = 0; d < iters && B.counters[d] != 0; d++) {
+      Grid(1, 1, [&] { KExtend<false, true>(S0, B, d, nullptr, 1, 4); });
+      Grid(1, 1, [&] { KShadeClass<SC_EMIT, false, true>(S0, B, none, d); });
+      Grid(1, 1, [&] { KShadeClass<SC_GLASS, false, true>(S0, B, none, d); });
+      Grid(1, 1, [&] { KShadeClass<SC_DIFFUSE, false, true>(S0, B, none, d); });
+      Grid(1, 1, [&] { KShadeClass<SC_METAL, false, true>(S0, B, none, d); });
+      Grid(1, 1, [&] { KShadeClass<SC_DISNEY, false, true>(S0, B, none, d); });
+      Grid(1, 1, [&] { KShadeClass<SC_GENERIC, false, true>(S0, B, none, d); });
+      Grid(1, 1, [&] { KShadow<false, true>(S0, B, d, nullptr, 1, 4); });
+    }
+    if (B.counters[kMiscBase + 1]) throw std::runtime_error("device-side check fired");
+    for (int k = 0; k < n; k++)
+      for (uint32_t i = 0; i < tab[(size_t)k].count; i++) {
+        const float4 l = B.L[tab[(size_t)k].pathBegin + i];
+        out[k][3 * i] = l.x;
+        out[k][3 * i + 1] = l.y;
+        out[k][3 * i + 2] = l.z;
+      }
+  });
+}
+
 // Li of (pixel, sample) pairs through the emulated kernels (rad_render_samples).
 // vol_mode: the vol_path estimator bits (0 = the reference's algorithm).
 int hemu_render_samples(void* s, const uint32_t* pix, const uint32_t* smp, int64_t n, uint32_t seed,

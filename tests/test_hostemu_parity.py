@@ -167,6 +167,27 @@ def test_render_samples_bit_exact(oracle, scene_dir, which):
     h.close()
 
 
+def test_mixed_wave_bit_exact(oracle, scene_dir):
+    """A mixed wave (the serving loop's several jobs in one launch of each stage,
+    each path with its job's scene, pixels, samples and seed: the MIX kernels)
+    gives every path of every job its scene's oracle Path::Li bit for bit."""
+    made = [box(scene_dir, 24, 16, 4), materials(scene_dir, 20, 20, 4, 2), spheres(scene_dir, 200, 3, 24, 16, 4)]
+    hs = [hemu_lib.HemuScene(text, d) for _, text, d in made]
+    os_ = [oracle.OracleScene(text, d) for _, text, d in made]
+    npix = [o.width * o.height for o in os_]
+    spw, sample0 = 3, 17
+    outs = hemu_lib.render_mixed(hs, npix, spw, sample0, [o.seed for o in os_])
+    for o, n, lh in zip(os_, npix, outs):
+        pix = np.tile(np.arange(n, dtype=np.uint32), spw)
+        smp = np.repeat(np.arange(sample0, sample0 + spw, dtype=np.uint32), n)
+        lo = o.render_samples(pix, smp)
+        same = _same(lh, lo).all(1)
+        assert same.all(), "%d of %d samples differ" % ((~same).sum(), same.size)
+        assert np.abs(lo).sum() > 0
+    for h in hs:
+        h.close()
+
+
 def test_render_samples_box_room_256_bit_exact(oracle, scene_dir):
     """The box room at its stated size: 256x256, depth 8, Russian roulette from 3."""
     path, text, d = box(scene_dir, 256, 256, 64)
