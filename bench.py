@@ -171,13 +171,15 @@ def run_reference(args, world, rank):
         import oracle_lib
         o = oracle_lib.OracleScene.from_file(path)
         threads = os.cpu_count() or 1
-        row_step = 16
+        # the same sample as the GPU arm's cpu_baseline: one-sample passes over every 4th row
+        row_step = args.cpu_row_step
         for _ in range(args.warmup):
             o.render(rows=(0, H, row_step * 4), samples=(0, 1), threads=threads)
         n_tot, t_tot = 0, 0.0
         for k in range(args.steps):
             t0 = time.perf_counter()
-            _, st = o.render(rows=(k % row_step, H, row_step), samples=(0, 1), threads=threads)
+            _, st = o.render(rows=(k % row_step, H, row_step), samples=(k // row_step, k // row_step + 1),
+                             threads=threads)
             t_tot += time.perf_counter() - t0
             n_tot += int(st[2])
         value = n_tot / t_tot
@@ -185,10 +187,12 @@ def run_reference(args, world, rank):
                 "unit": "samples/s", "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
                 "ms_per_step": 1000 * t_tot / args.steps, "higher_is_better": True, "scaling": "weak",
                 "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded generator)",
-                "config": {"workload": "many_spheres_1080p", "spheres": 10000, "triangles": 3200000,
-                           "width": W, "height": H, "max_depth": MAX_DEPTH, "sample_per_step": "1/%d of rows, 1 spp" % row_step},
+                "config": {"workload": "many_spheres_1080p", "spheres": 10000, "triangles": 3200000, "emitters": 20,
+                           "width": W, "height": H, "max_depth": MAX_DEPTH, "rr_depth": 3,
+                           "sample_per_step": "1/%d of the rows, one sample" % row_step},
                 "cpu_baseline": {"value": value, "unit": "samples/s", "cores": threads, "kind": "port",
-                                 "sample": "every %d-th row of the frame at 1 spp per step" % row_step},
+                                 "sample": "per step a one-sample pass over every %d-th row of the frame (%d samples, "
+                                           "%.1f s over %d steps)" % (row_step, n_tot, t_tot, args.steps)},
                 "e2e": {"value": value, "unit": "samples/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
         print(json.dumps(line), flush=True)
 
