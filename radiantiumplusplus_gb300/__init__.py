@@ -141,7 +141,9 @@ class Scene:
                    vol_real_depth, vol_persistent)
 
     def autotune(self, config=None):
-        """Pick the traversal launch parameters for this scene by timing waves (rad_autotune)."""
+        """Pick this scene's launch parameters by timing waves (rad_autotune): for `path` the traversal kernels'
+        refill threshold, blocks per SM and leaf vote and the shade-class block size; for `vol_path` the wavefront
+        part kernels' top-up threshold, blocks per SM and chunk. config: dict of candidate lists and "reps"."""
         r = _capi.TuneResult()
         text = None if config is None else json.dumps(config).encode()
         check(lib().rad_autotune(self._h, text, ctypes.byref(r)))
